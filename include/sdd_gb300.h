@@ -1,0 +1,129 @@
+/*
+ * sdd_gb300.h -- C ABI of the GB300 (sm_103a) pseudospectral time-step / Newton hot path of
+ * mannixp/SpectralDoubleDiffusiveConvection (axisymmetric double-diffusive convection in a spherical
+ * shell, Chebyshev in r x sine/cosine in theta).
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream (as void*), returns an int
+ * status (SDD_OK = 0, negative on error) and is stream-ordered.  No entry point synchronises the
+ * stream except sdd_newton_gmres (it reads its convergence history back to the host).
+ *
+ * State layout (the reference's, Matrix_Operators.py:530-575): one shell's state X has 3*N_fm*nr
+ * doubles; field f (0 psi, 1 T, 2 S) starts at f*N_fm*nr and mode k occupies [k*nr, (k+1)*nr).
+ * psi slot k holds the coefficient of sin((k+1) theta); T/S slot k the coefficient of cos(k theta).
+ * A batch of B shells sharing one plan is B such states back to back.
+ */
+#ifndef SDD_GB300_H
+#define SDD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------------------- */
+#define SDD_OK 0
+#define SDD_ERR_ARG (-1)            /* bad pointer / size / enum                                     */
+#define SDD_ERR_ODD_NFM (-2)        /* N_fm not even: Matrix_Operators.py:758-759 raises ValueError   */
+#define SDD_ERR_UNSUPPORTED (-3)    /* size the kernels do not support (shared memory / FFT radix)   */
+#define SDD_ERR_CUDA (-4)           /* a CUDA runtime call failed; sdd_last_cuda_error() has the code */
+#define SDD_ERR_NOMEM (-5)          /* device allocation failed                                       */
+#define SDD_ERR_NOT_CONVERGED (-6)  /* Newton/GMRES hit its iteration cap (Main.py:541-544)           */
+
+/* precision of the nonlinear term (transforms, products, derivative contractions) */
+#define SDD_PREC_FP64 0             /* plain: FP64 throughout                                         */
+#define SDD_PREC_MIXED 1            /* FP32 nonlinear term; rhs, chains, residuals stay FP64          */
+
+/* transform kinds (Transforms.py) */
+#define SDD_IDCT 0                  /* Transforms.py:116 IDCT(f_hat, n)                               */
+#define SDD_IDST 1                  /* Transforms.py:87  IDST(g_hat, n)                               */
+#define SDD_DCT 2                   /* Transforms.py:102 DCT(f)[..., :n_out]                          */
+#define SDD_DST 3                   /* Transforms.py:73  DST(g)[..., :n_out]                          */
+
+const char* sdd_error_string(int status);
+/* the cudaError_t of the last failing CUDA call made by this library (0 if none) */
+int sdd_last_cuda_error(void);
+/* library version as major*10000 + minor*100 + patch */
+int sdd_version(void);
+
+/* ---- theta transforms ------------------------------------------------------------------------ */
+/* Batched rows.  Replaces Transforms.py:73-129 (DCT, DST, IDCT, IDST).
+ * Inverse kinds (IDCT/IDST): in = rows x n_in sinusoid amplitudes, out = rows x n_out grid values on
+ *   grid(n_out) (Transforms.py:8); n_out >= n_in zero-pads exactly as IDCT(f_hat, n=n_out) does.
+ * Forward kinds (DCT/DST): in = rows x n_in grid values, out = rows x n_out leading sinusoid
+ *   amplitudes (n_out <= n_in), i.e. DCT(f)[..., :n_out].
+ * fp64 arithmetic; in and out may not alias. */
+int sdd_transform(int kind, int rows, int n_in, int n_out, const double* in, double* out,
+                  void* stream);
+
+/* ---- plan: device-resident operators for one (N_fm, N_r, d, dt, Pr, Tau, symmetric) ------------ */
+/* All host arrays are FP64, row-major, built by the caller with the reference's formulas
+ * (Main.py:179-225 Build_Matrix_Operators and the operator builders it calls). */
+typedef struct sdd_plan_desc {
+  int32_t N_fm;            /* theta modes M (even)                                                 */
+  int32_t nr;              /* interior radial points N_r - 1                                       */
+  int32_t symmetric;       /* 1: equatorially symmetric subspace (Main.py:137-176)                  */
+  int32_t precision;       /* SDD_PREC_FP64 or SDD_PREC_MIXED                                      */
+  double dt, Pr, Tau;      /* step of this operator set (dt=1 for Newton, Main.py:430)             */
+  const double* Dr;        /* nr*nr  D[1:-1,1:-1]                         (Matrix_Operators.py:764)*/
+  const double* D2_r2;     /* nr*nr  (diag(1/R^2) D@D)[1:-1,1:-1]         (A2_SINE_R2 :498)        */
+  const double* ir4_r2;    /* nr     1/R^4                                (A2_SINE_R2 :496)        */
+  const double* D2_sine;   /* nr*nr  (D@D)[1:-1,1:-1]                     (A2_SINE :217)           */
+  const double* ir2_sine;  /* nr     1/R^2                                (A2_SINE :216)           */
+  const double* D2_A4;     /* nr*nr  args_A4 D2                           (Main.py:212)            */
+  const double* ir2_A4;    /* nr     diag of args_A4 IR2                  (Main.py:213)            */
+  const double* ir4_A4;    /* nr     diag of args_A4 IR4                  (Main.py:214)            */
+  const double* rsq;       /* nr     R^2 (R2 block diagonal)              (Matrix_Operators.py:85) */
+  const double* dT0;       /* nr     A_T/R^2                              (Main.py:201-202)        */
+  const double* gr;        /* nr     R_1^2/R^2 (kGR_RT diagonal)          (Matrix_Operators.py:113)*/
+  const double* Linv_A4;   /* N_fm*nr*nr  A4_TSTEP_MATS(Pr*dt)            (Matrix_Operators.py:1089)*/
+  const double* Linv_T;    /* N_fm*nr*nr  NAB2_TSTEP_MATS(dt)             (Matrix_Operators.py:1014)*/
+  const double* Linv_S;    /* N_fm*nr*nr  NAB2_TSTEP_MATS(Tau*dt)                                  */
+} sdd_plan_desc;
+
+typedef struct sdd_plan sdd_plan;
+
+/* Uploads the operators to the current device.  Replaces Main.py:179-225 (the returned tuple). */
+int sdd_plan_create(const sdd_plan_desc* desc, sdd_plan** plan);
+int sdd_plan_destroy(sdd_plan* plan);
+/* Pre-allocates the plan's workspace for up to max_batch shells (otherwise grown on first use). */
+int sdd_plan_reserve(sdd_plan* plan, int max_batch);
+/* FP64 elements of one shell's base-state grid cache used by sdd_nlin_dfx (9 * nr * 3N_fm/2). */
+size_t sdd_plan_base_cache_elems(const sdd_plan* plan);
+
+/* ---- Matrix_Operators.py drop-ins (batched over shells sharing the plan) ----------------------- */
+/* F(X,X), Matrix_Operators.py:743-804 NLIN_FX.  X, F: batch x 3*N_fm*nr.
+ * base_cache (nullable, batch x sdd_plan_base_cache_elems): receives X's nine padded grid fields. */
+int sdd_nlin_fx(sdd_plan* plan, int batch, const double* X, double* F, double* base_cache,
+                void* stream);
+/* DF(X) dv = F(X,dv)+F(dv,X), Matrix_Operators.py:807-898 NLIN_DFX.  base_cache (nullable) must hold
+ * X's grid fields from sdd_nlin_fx; when NULL they are recomputed from X. */
+int sdd_nlin_dfx(sdd_plan* plan, int batch, const double* dv, const double* X,
+                 const double* base_cache, double* out, void* stream);
+/* psi solve, Matrix_Operators.py:1115-1194 A4_BSub_TSTEP_V2 with the plan's Linv_A4 and dt*Pr.
+ * g, f: batch x N_fm*nr. */
+int sdd_a4_bsub(sdd_plan* plan, int batch, const double* g, double* f, void* stream);
+/* T (field=1, dt) or S (field=2, Tau*dt) solve, Matrix_Operators.py:1033-1086 NAB2_BSub_TSTEP_V2. */
+int sdd_nab2_bsub(sdd_plan* plan, int field, int batch, const double* g, double* f, void* stream);
+/* theta-coupling recurrences (batch x N_fm*nr in and out):
+ * op 0 J_theta_RT (Matrix_Operators.py:436), 1 A2_SINE_R2 (:475), 2 A2_SINE (:192), 3 DT0_theta (:131) */
+int sdd_theta_op(sdd_plan* plan, int op, int batch, const double* g, double* f, void* stream);
+
+/* ---- Main.py drivers ------------------------------------------------------------------------- */
+/* nsteps IMEX ("CNAB1") steps, Main.py:255-283 Step_Python inside the loop of _Time_Step :286-324
+ * (X <- X_SYM * X_new).  Ra, Ra_s: per-shell device arrays (batch).  X_in and X_out may alias.
+ * linear != 0 drops the nonlinear term (Main.py:261-264). */
+int sdd_step(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, const double* X_in,
+             double* X_out, int nsteps, int linear, void* stream);
+/* Newton residual F(X) = Phi_dt(X) - X, Main.py:473-496 PFX.  base_cache as in sdd_nlin_fx. */
+int sdd_pfx(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, const double* X,
+            double* F, double* base_cache, void* stream);
+/* Jacobian-vector product, Main.py:498-521 PDFX. */
+int sdd_pdfx(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, const double* dv,
+             const double* X, const double* base_cache, double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SDD_GB300_H */

@@ -1,0 +1,103 @@
+"""ctypes binding of ``libsdd_gb300.so`` (the C ABI declared in ``include/sdd_gb300.h``).
+
+There is no CPU fallback: importing a compute entry point without the built library raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsdd_gb300.so")
+
+SDD_OK = 0
+SDD_ERR_ARG = -1
+SDD_ERR_ODD_NFM = -2
+SDD_ERR_UNSUPPORTED = -3
+SDD_ERR_CUDA = -4
+SDD_ERR_NOMEM = -5
+SDD_ERR_NOT_CONVERGED = -6
+
+SDD_PREC_FP64 = 0
+SDD_PREC_MIXED = 1
+
+SDD_IDCT, SDD_IDST, SDD_DCT, SDD_DST = 0, 1, 2, 3
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+class PlanDesc(ctypes.Structure):
+    """Mirror of ``sdd_plan_desc``."""
+    _fields_ = [
+        ("N_fm", ctypes.c_int32), ("nr", ctypes.c_int32), ("symmetric", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("dt", ctypes.c_double), ("Pr", ctypes.c_double), ("Tau", ctypes.c_double),
+        ("Dr", _dp), ("D2_r2", _dp), ("ir4_r2", _dp), ("D2_sine", _dp), ("ir2_sine", _dp),
+        ("D2_A4", _dp), ("ir2_A4", _dp), ("ir4_A4", _dp), ("rsq", _dp), ("dT0", _dp), ("gr", _dp),
+        ("Linv_A4", _dp), ("Linv_T", _dp), ("Linv_S", _dp),
+    ]
+
+
+# (name, restype, argtypes) of every exported symbol; the CPU test checks the header declares these.
+_VP = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+SIGNATURES = [
+    ("sdd_error_string", ctypes.c_char_p, [_I]),
+    ("sdd_last_cuda_error", _I, []),
+    ("sdd_version", _I, []),
+    ("sdd_transform", _I, [_I, _I, _I, _I, _VP, _VP, _VP]),
+    ("sdd_plan_create", _I, [ctypes.POINTER(PlanDesc), ctypes.POINTER(_VP)]),
+    ("sdd_plan_destroy", _I, [_VP]),
+    ("sdd_plan_reserve", _I, [_VP, _I]),
+    ("sdd_plan_base_cache_elems", ctypes.c_size_t, [_VP]),
+    ("sdd_nlin_fx", _I, [_VP, _I, _VP, _VP, _VP, _VP]),
+    ("sdd_nlin_dfx", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP]),
+    ("sdd_a4_bsub", _I, [_VP, _I, _VP, _VP, _VP]),
+    ("sdd_nab2_bsub", _I, [_VP, _I, _I, _VP, _VP, _VP]),
+    ("sdd_theta_op", _I, [_VP, _I, _I, _VP, _VP, _VP]),
+    ("sdd_step", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, _I, _VP]),
+    ("sdd_pfx", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP]),
+    ("sdd_pdfx", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+]
+
+_lib = None
+
+
+class SDDError(RuntimeError):
+    """A non-zero status from libsdd_gb300."""
+
+    def __init__(self, status, where):
+        self.status = status
+        msg = lib().sdd_error_string(status).decode()
+        if status == SDD_ERR_CUDA:
+            msg += f" (cudaError {lib().sdd_last_cuda_error()})"
+        super().__init__(f"{where}: {msg} [status {status}]")
+
+
+def load(path=LIB_PATH):
+    """Load the shared library (no CUDA context is created by loading)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(
+            f"{path} is missing: build it with `python -m spectraldoublediffusiveconvection_gb300.build`"
+            " (there is no CPU fallback)")
+    L = ctypes.CDLL(path)
+    for name, res, args in SIGNATURES:
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def lib():
+    return _lib if _lib is not None else load()
+
+
+def check(status, where):
+    if status != SDD_OK:
+        if status == SDD_ERR_ODD_NFM:
+            raise ValueError(f"The number of Fourier modes is not even ({where})")
+        raise SDDError(status, where)
+    return status

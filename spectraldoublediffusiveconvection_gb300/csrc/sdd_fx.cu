@@ -1,0 +1,680 @@
+// Row kernels of the nonlinear term, the right-hand-side assembly, the theta recurrences and the
+// standalone theta transforms.
+//
+// k_fx_rows: one CTA per (radial row n, shell).  It forms the nine spectral rows of
+// Matrix_Operators.py:631-740 (Derivatives, with J_theta_RT :437 and A2_SINE_R2 :476 evaluated as
+// parity suffix sums along the row), transforms them to the 3/2-padded grid (:776-786), forms the
+// products of :791-793 (NLIN_FX) or :884-887 (NLIN_DFX), and transforms four product rows back
+// (:797-802).  The radial derivative Dr@(JT_psi*omega) of :791 is moved through the (theta-only) DST:
+// the kernel outputs DST(JT_psi*omega) and the rhs kernel applies Dr to it in spectral space, so the
+// row kernel has no cross-row dependency.
+#include <cuda_runtime.h>
+#include "sdd_internal.cuh"
+#include "sdd_fft.cuh"
+
+namespace sdd {
+
+// S[m] = sum_{m' >= m, m' = m mod 2} v[m'] for m < M (warps 0 and 1; caller syncs).
+template <typename T>
+__device__ void parity_suffix(const T* v, T* S, int M) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp < 2) {
+    const int p = warp;
+    const int cnt = (M - p + 1) / 2;
+    T carry = (T)0;
+    for (int t0 = ((cnt - 1) / 32) * 32; t0 >= 0; t0 -= 32) {
+      const int t = t0 + lane;
+      T x = (t < cnt) ? v[p + 2 * t] : (T)0;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        T y = __shfl_down_sync(0xffffffffu, x, off);
+        if (lane + off < 32) x += y;
+      }
+      x += carry;
+      if (t < cnt) S[p + 2 * t] = x;
+      carry = __shfl_sync(0xffffffffu, x, 0);
+    }
+  }
+}
+
+// Exact power-of-two balancing of the rows that share one complex FFT.  The two rows of a pair ride in
+// the real and imaginary parts, and the FFT's rounding error scales with the larger of the two: an
+// unbalanced pair (|komega| ~ 1e3 next to |JT_psi| ~ 1e-2) would leave the small row with an error of
+// eps*1e3.  Each row is therefore scaled by 2^-e, e = exponent of its max |value| (exact), before the
+// transform and scaled back after it.
+template <typename T>
+__device__ __forceinline__ void pow2_scale(T mx, T* s, T* inv) {
+  if (!(mx > (T)0) || !isfinite(mx)) {
+    *s = (T)1;
+    *inv = (T)1;
+    return;
+  }
+  int e;
+  frexp(mx, &e);
+  *s = ldexp((T)1, -e);
+  *inv = ldexp((T)1, e);
+}
+
+// Block-wide max of K per-thread values; writes scale and inverse scale of each into sc[0..K), sc[K..2K).
+// red must hold K*32 values.  Ends with __syncthreads().
+template <typename T, int K>
+__device__ __forceinline__ void block_max_scales(T (&v)[K], T* red, T* sc) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int t = 0; t < K; ++t) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v[t] = fmax(v[t], __shfl_xor_sync(0xffffffffu, v[t], off));
+    if (lane == 0) red[t * 32 + warp] = v[t];
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    T m = (T)0;
+    for (int w = 0; w < nw; ++w) m = fmax(m, red[threadIdx.x * 32 + w]);
+    pow2_scale(m, sc + threadIdx.x, sc + K + threadIdx.x);
+  }
+  __syncthreads();
+}
+
+size_t fx_smem_bytes(int M, int P, int prec) {
+  (void)M;
+  const size_t es = prec == SDD_PREC_MIXED ? sizeof(float) : sizeof(double);
+  return (33 * (size_t)P + 2 * kMaxNr + 9 * 32 + 32) * es;
+}
+
+// DCT3 input x_k of transform t of the nine fields (see the header comment of sdd_fft.cuh).
+// Fields: 0 JT_psi, 1 komega, 2 kDpsi, 3 DT, 4 DC (cosine type); 5 omega, 6 Dpsi, 7 kT, 8 kC (sine type).
+template <typename T>
+__device__ __forceinline__ T fx_x(int t, int k, int M, int P, const T* JP, const T* OM, const T* DP,
+                                  const T* DTv, const T* DCv, const T* Tv, const T* Sv) {
+  if (t < 5) {
+    if (k >= M) return (T)0;
+    switch (t) {
+      case 0: return JP[k];
+      case 1: return k >= 1 ? (T)k * OM[k - 1] : (T)0;
+      case 2: return k >= 1 ? (T)k * DP[k - 1] : (T)0;
+      case 3: return DTv[k];
+      default: return DCv[k];
+    }
+  }
+  if (t > 8) return (T)0;
+  const int w = P - k;  // wavenumber
+  if (k == 0 || w > M - 1) return (T)0;
+  switch (t) {
+    case 5: return OM[w - 1];
+    case 6: return DP[w - 1];
+    case 7: return -(T)w * Tv[w];
+    default: return -(T)w * Sv[w];
+  }
+}
+
+// MODE 0: NLIN_FX (optionally storing the grid fields); 1: NLIN_DFX with base fields from the cache;
+// 2: grid fields only (fills the cache).
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kFxThreads) k_fx_rows(FxArgs a) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int M = a.M, nr = a.nr, P = a.P;
+  const int n = blockIdx.x, b = blockIdx.y;
+  const int tid = threadIdx.x, bd = blockDim.x;
+
+  C* RA = reinterpret_cast<C*>(smem_raw);
+  C* RB = RA + 5 * P;
+  C* Wt = RB + 5 * P;
+  C* Et = Wt + P;
+  T* RG = reinterpret_cast<T*>(Et + P);
+  T* opr = RG + 9 * P;
+  T* red = opr + 2 * kMaxNr;   // 9*32 reduction slots
+  T* scl = red + 9 * 32;       // 9 scales + 9 inverse scales (inverse transforms), reused for 4+4
+  T* pv = RG;
+  T* Tv = pv + M;
+  T* Sv = Tv + M;
+  T* DP = Sv + M;
+  T* OM = DP + M;
+  T* DTv = OM + M;
+  T* DCv = DTv + M;
+  T* JP = DCv + M;
+  T* Sc = JP + M;
+
+  const C* wg = reinterpret_cast<const C*>(a.ops.w);
+  const C* eg = reinterpret_cast<const C*>(a.ops.e);
+  for (int i = tid; i < P; i += bd) {
+    Wt[i] = wg[i];
+    Et[i] = eg[i];
+  }
+  const T* Drg = reinterpret_cast<const T*>(a.ops.Dr);
+  const T* D2g = reinterpret_cast<const T*>(a.ops.D2r2);
+  for (int m = tid; m < nr; m += bd) {
+    opr[m] = Drg[n * nr + m];
+    opr[nr + m] = D2g[n * nr + m];
+  }
+  const T ir4n = reinterpret_cast<const T*>(a.ops.ir4r2)[n];
+  __syncthreads();
+
+  // ---- 1. radial contractions of row n (Derivatives, :698-729) and the row values ----
+  const int N = M * nr;
+  const double* Xs = a.X + (size_t)b * a.x_stride;
+  for (int k = tid; k < M; k += bd) {
+    const double* ps = Xs + (size_t)k * nr;
+    const double* ts = Xs + N + (size_t)k * nr;
+    const double* ss = Xs + 2 * N + (size_t)k * nr;
+    const bool psi_on = !(a.sym && (k % 2 == 0));
+    const bool ts_on = !(a.sym && (k % 2 == 1));
+    T dp = 0, d2 = 0, dtv = 0, dcv = 0, pn = 0, tn = 0, sn = 0;
+    if (psi_on) {
+      for (int m = 0; m < nr; ++m) {
+        const T x = (T)__ldg(ps + m);
+        dp += opr[m] * x;
+        d2 += opr[nr + m] * x;
+      }
+      pn = (T)__ldg(ps + n);
+    }
+    if (ts_on) {
+      for (int m = 0; m < nr; ++m) {
+        dtv += opr[m] * (T)__ldg(ts + m);
+        dcv += opr[m] * (T)__ldg(ss + m);
+      }
+      tn = (T)__ldg(ts + n);
+      sn = (T)__ldg(ss + n);
+    }
+    pv[k] = pn;
+    Tv[k] = tn;
+    Sv[k] = sn;
+    DP[k] = dp;
+    OM[k] = d2;
+    DTv[k] = dtv;
+    DCv[k] = dcv;
+  }
+  __syncthreads();
+  parity_suffix<T>(pv, Sc, M);
+  __syncthreads();
+  // J_theta_RT (:437-472) and A2_SINE_R2 (:476-526) along the row
+  for (int k = tid; k < M; k += bd) {
+    const T s1 = (k + 1 < M) ? Sc[k + 1] : (T)0;
+    JP[k] = (k == 0) ? s1 : (T)(k + 1) * pv[k - 1] + (T)2 * s1;
+    const T s2 = (k + 2 < M) ? Sc[k + 2] : (T)0;
+    OM[k] = OM[k] - (T)(k + 1) * (ir4n * ((T)(k + 2) * pv[k] + (T)2 * s2));
+  }
+  __syncthreads();
+  {
+    T mloc[9];
+#pragma unroll
+    for (int t = 0; t < 9; ++t) mloc[t] = (T)0;
+    for (int k = tid; k < P; k += bd) {
+#pragma unroll
+      for (int t = 0; t < 9; ++t) mloc[t] = fmax(mloc[t], fabs(fx_x<T>(t, k, M, P, JP, OM, DP, DTv, DCv, Tv, Sv)));
+    }
+    block_max_scales<T, 9>(mloc, red, scl);
+  }
+
+  // ---- 2. nine inverse transforms as five paired DCT3s (:776-786) ----
+  for (int idx = tid; idx < 5 * P; idx += bd) {
+    const int p = idx / P;
+    const int k = idx - p * P;
+    C V[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int t = 2 * p + h;
+      const T sc = (t < 9) ? scl[t] : (T)1;
+      const T x = sc * fx_x<T>(t, k, M, P, JP, OM, DP, DTv, DCv, Tv, Sv);
+      if (k == 0) {
+        V[h] = cmk<C>(x, (T)0);
+      } else {
+        const T xr = sc * fx_x<T>(t, P - k, M, P, JP, OM, DP, DTv, DCv, Tv, Sv);
+        const C e = Et[k];
+        V[h] = cmk<C>((T)0.5 * (e.x * x + e.y * xr), (T)0.5 * (e.y * x - e.x * xr));
+      }
+    }
+    RA[idx] = cmk<C>(V[0].x - V[1].y, V[0].y + V[1].x);
+  }
+  __syncthreads();
+  C* res = fft_rows<T, true>(RA, RB, 5, a.st, Wt);
+  for (int idx = tid; idx < 9 * P; idx += bd) {
+    const int t = idx / P;
+    const int i = idx - t * P;
+    const int src = (i & 1) ? (P - 1 - (i >> 1)) : (i >> 1);
+    const C v = res[(t >> 1) * P + src];
+    T val = ((t & 1) ? v.y : v.x) * scl[9 + t];
+    if (t >= 5 && (i & 1)) val = -val;
+    RG[idx] = val;
+  }
+  __syncthreads();
+
+  if (MODE != 1 && a.base != nullptr) {
+    T* bc = reinterpret_cast<T*>(a.base) + (size_t)b * a.base_stride + (size_t)n * 9 * P;
+    for (int idx = tid; idx < 9 * P; idx += bd) bc[idx] = RG[idx];
+  }
+  if (MODE == 2) return;
+
+  // ---- 3. grid products (:791-793 or :884-887); sine outputs pre-multiplied by (-1)^i ----
+  T* PR = reinterpret_cast<T*>(RA);
+  const T* bs = (MODE == 1) ? reinterpret_cast<const T*>(a.base) + (size_t)b * a.base_stride +
+                                  (size_t)n * 9 * P
+                            : nullptr;
+  T m4[4] = {(T)0, (T)0, (T)0, (T)0};
+  for (int i = tid; i < P; i += bd) {
+    const T JT = RG[i], kO = RG[P + i], kDP = RG[2 * P + i], DTg = RG[3 * P + i], DCg = RG[4 * P + i];
+    const T O = RG[5 * P + i], DPg = RG[6 * P + i], kT = RG[7 * P + i], kC = RG[8 * P + i];
+    T Q, Rr, NT, NS;
+    if (MODE == 0) {
+      Q = JT * O;
+      Rr = kDP * O + DPg * kO;
+      NT = JT * DTg - DPg * kT;
+      NS = JT * DCg - DPg * kC;
+    } else {
+      const T aJT = bs[i], akO = bs[P + i], akDP = bs[2 * P + i], aDT = bs[3 * P + i], aDC = bs[4 * P + i];
+      const T aO = bs[5 * P + i], aDP = bs[6 * P + i], akT = bs[7 * P + i], akC = bs[8 * P + i];
+      Q = aJT * O + JT * aO;
+      Rr = (akDP * O + aDP * kO) + (kDP * aO + DPg * akO);
+      NT = (JT * aDT - DPg * akT) + (aJT * DTg - aDP * kT);
+      NS = (JT * aDC - DPg * akC) + (aJT * DCg - aDP * kC);
+    }
+    const T sg = (i & 1) ? (T)-1 : (T)1;
+    PR[i] = sg * Q;
+    PR[P + i] = sg * Rr;
+    PR[2 * P + i] = NT;
+    PR[3 * P + i] = NS;
+    m4[0] = fmax(m4[0], fabs(Q));
+    m4[1] = fmax(m4[1], fabs(Rr));
+    m4[2] = fmax(m4[2], fabs(NT));
+    m4[3] = fmax(m4[3], fabs(NS));
+  }
+  block_max_scales<T, 4>(m4, red, scl);   // scl[0..4) scales, scl[4..8) inverses
+
+  // ---- 4. four forward transforms as two paired DCT2s (:797-802) ----
+  for (int idx = tid; idx < 2 * P; idx += bd) {
+    const int p = idx / P;
+    const int nn = idx - p * P;
+    const int src = makhoul_src(nn, P);
+    RB[idx] = cmk<C>(scl[2 * p] * PR[(2 * p) * P + src], scl[2 * p + 1] * PR[(2 * p + 1) * P + src]);
+  }
+  __syncthreads();
+  C* Z = fft_rows<T, false>(RB, RA, 2, a.st, Wt);
+  double* o = a.out4 + (size_t)b * a.out_stride;
+  const T two_P = (T)2 / (T)P, one_P = (T)1 / (T)P;
+  for (int idx = tid; idx < 2 * M; idx += bd) {
+    const int p = idx / M;
+    const int s = idx - p * M;
+    T ya = 0, yb = 0;
+    bool zero = false;
+    int k;
+    if (p == 0) {            // sine pair: slot s <-> wavenumber s+1, read at k = P-1-s
+      zero = (s == M - 1) || (a.sym && (s % 2 == 0));
+      k = P - 1 - s;
+    } else {
+      zero = a.sym && (s % 2 == 1);
+      k = s;
+    }
+    if (!zero) {
+      const C Zk = Z[p * P + k];
+      const C Zm = Z[p * P + ((P - k) % P)];
+      const C e = Et[k];
+      ya = e.x * (Zk.x + Zm.x) * (T)0.5 + e.y * (Zk.y - Zm.y) * (T)0.5;
+      yb = e.x * (Zk.y + Zm.y) * (T)0.5 - e.y * (Zk.x - Zm.x) * (T)0.5;
+      const T sc = (p == 1 && k == 0) ? one_P : two_P;
+      ya *= sc * scl[4 + 2 * p];
+      yb *= sc * scl[4 + 2 * p + 1];
+    }
+    const size_t q0 = (size_t)(2 * p) * N + (size_t)s * nr + n;
+    o[q0] = (double)ya;
+    o[q0 + N] = (double)yb;
+  }
+}
+
+// ---- right-hand sides of the three implicit solves (Main.py:262-280) ---------------------------
+__global__ void __launch_bounds__(kFxThreads) k_rhs(RhsArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int M = a.M, nr = a.nr;
+  const int n = blockIdx.x, b = blockIdx.y;
+  const int tid = threadIdx.x, bd = blockDim.x;
+  double* sm = reinterpret_cast<double*>(smem_raw);
+  double* pv = sm;
+  double* Sc = pv + M;
+  double* D2p = Sc + M;
+  double* DrQ = D2p + M;
+  double* Tv = DrQ + M;
+  double* Sv = Tv + M;
+  double* opr = Sv + M;  // Dr row n, D2s row n
+  for (int m = tid; m < nr; m += bd) {
+    opr[m] = a.Dr[n * nr + m];
+    opr[nr + m] = a.D2s[n * nr + m];
+  }
+  __syncthreads();
+  const int N = M * nr;
+  const double* Xs = a.X + (size_t)b * a.x_stride;
+  const double* O4 = a.linear ? nullptr : a.out4 + (size_t)b * a.out_stride;
+  for (int k = tid; k < M; k += bd) {
+    const bool psi_on = !(a.sym && (k % 2 == 0));
+    const bool ts_on = !(a.sym && (k % 2 == 1));
+    const double* ps = Xs + (size_t)k * nr;
+    double d2 = 0, pn = 0, q = 0;
+    if (psi_on) {
+      for (int m = 0; m < nr; ++m) d2 += opr[nr + m] * __ldg(ps + m);
+      pn = __ldg(ps + n);
+    }
+    if (O4) {
+      const double* qs = O4 + (size_t)k * nr;
+      for (int m = 0; m < nr; ++m) q += opr[m] * __ldg(qs + m);
+    }
+    pv[k] = pn;
+    D2p[k] = d2;
+    DrQ[k] = q;
+    Tv[k] = ts_on ? __ldg(Xs + N + (size_t)k * nr + n) : 0.0;
+    Sv[k] = ts_on ? __ldg(Xs + 2 * N + (size_t)k * nr + n) : 0.0;
+  }
+  __syncthreads();
+  parity_suffix<double>(pv, Sc, M);
+  __syncthreads();
+  const double dt = a.dt, dtPr = a.dt * a.Pr;
+  const double Ra = a.Ra[b], Ras = a.Ra_s[b];
+  const double ir2 = a.ir2s[n], rsq = a.rsq[n], dT0 = a.dT0[n], gr = a.gr[n];
+  double* R = a.rhs + (size_t)b * a.rhs_stride;
+  for (int k = tid; k < M; k += bd) {
+    const double s1 = (k + 1 < M) ? Sc[k + 1] : 0.0;
+    const double JP = (k == 0) ? 1.0 * s1 : (k + 1.0) * pv[k - 1] + 2.0 * s1;    // J_theta_RT
+    const double s2 = (k + 2 < M) ? Sc[k + 2] : 0.0;
+    const double Om = D2p[k] - (double)(k + 1) * ir2 * ((k + 2.0) * pv[k] + 2.0 * s2);  // A2_SINE
+    const double grv = (k < M - 1) ? (-(double)(k + 1) * gr) * (Ra * Tv[k + 1] - Ras * Sv[k + 1]) : 0.0;
+    double nxp = 0, nxt = 0, nxs = 0;
+    if (O4) {
+      const size_t o = (size_t)k * nr + n;
+      nxp = -dt * (DrQ[k] - O4[N + o]);
+      nxt = -dt * O4[2 * N + o];
+      nxs = -dt * O4[3 * N + o];
+    }
+    const double psiT0 = dT0 * JP;                                              // DT0_theta
+    const size_t o = (size_t)k * nr + n;
+    R[o] = nxp + (Om + dtPr * grv);
+    R[N + o] = nxt + (rsq * Tv[k] - dt * psiT0);
+    R[2 * N + o] = nxs + (rsq * Sv[k] - dt * psiT0);
+  }
+}
+
+// ---- standalone theta recurrences (J_theta_RT, A2_SINE_R2, A2_SINE, DT0_theta) ------------------
+struct ThetaArgs {
+  int op, M, nr, sym;
+  const double* D2;
+  const double* ir;
+  const double* dT0;
+  const double* g;
+  double* f;
+};
+
+__global__ void __launch_bounds__(kFxThreads) k_theta_op(ThetaArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int M = a.M, nr = a.nr;
+  const int n = blockIdx.x, b = blockIdx.y;
+  const int tid = threadIdx.x, bd = blockDim.x;
+  double* sm = reinterpret_cast<double*>(smem_raw);
+  double* pv = sm;
+  double* Sc = pv + M;
+  double* D2p = Sc + M;
+  double* opr = D2p + M;
+  const bool a2 = (a.op == 1 || a.op == 2);
+  if (a2)
+    for (int m = tid; m < nr; m += bd) opr[m] = a.D2[n * nr + m];
+  __syncthreads();
+  const double* g = a.g + (size_t)b * M * nr;
+  for (int k = tid; k < M; k += bd) {
+    const bool on = !(a.sym && (k % 2 == 0));
+    double d2 = 0, pn = 0;
+    if (on) {
+      const double* ps = g + (size_t)k * nr;
+      if (a2)
+        for (int m = 0; m < nr; ++m) d2 += opr[m] * __ldg(ps + m);
+      pn = __ldg(ps + n);
+    }
+    pv[k] = pn;
+    D2p[k] = d2;
+  }
+  __syncthreads();
+  parity_suffix<double>(pv, Sc, M);
+  __syncthreads();
+  double* f = a.f + (size_t)b * M * nr;
+  for (int k = tid; k < M; k += bd) {
+    const double s1 = (k + 1 < M) ? Sc[k + 1] : 0.0;
+    const double s2 = (k + 2 < M) ? Sc[k + 2] : 0.0;
+    double v;
+    if (a2) {
+      v = D2p[k] - (double)(k + 1) * (a.ir[n] * ((k + 2.0) * pv[k] + 2.0 * s2));
+      if (a.sym && (k % 2 == 0)) v = 0.0;
+    } else {
+      const double jp = (k == 0) ? 1.0 * s1 : (k + 1.0) * pv[k - 1] + 2.0 * s1;
+      v = (a.op == 3) ? a.dT0[n] * jp : jp;
+      if (a.sym && (k % 2 == 1)) v = 0.0;
+    }
+    f[(size_t)k * nr + n] = v;
+  }
+}
+
+// ---- standalone batched transforms (Transforms.py) -------------------------------------------
+struct TrArgs {
+  int kind, rows, n_in, n_out, L;
+  StageArgs st;
+  const double2* w;
+  const double2* e;
+  const double* in;
+  double* out;
+};
+
+constexpr int kTrPairs = 2;
+
+__global__ void __launch_bounds__(kFxThreads) k_transform(TrArgs a) {
+  using C = double2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int L = a.L;
+  C* RA = reinterpret_cast<C*>(smem_raw);
+  C* RB = RA + kTrPairs * L;
+  C* Wt = RB + kTrPairs * L;
+  C* Et = Wt + L;
+  double* red = reinterpret_cast<double*>(Et + L);   // 4*32
+  double* scl = red + 4 * 32;                         // 4 scales + 4 inverses
+  const int tid = threadIdx.x, bd = blockDim.x;
+  for (int i = tid; i < L; i += bd) {
+    Wt[i] = a.w[i];
+    Et[i] = a.e[i];
+  }
+  const int r0 = blockIdx.x * 2 * kTrPairs;
+  const bool inverse = (a.kind == SDD_IDCT || a.kind == SDD_IDST);
+  const bool sine = (a.kind == SDD_IDST || a.kind == SDD_DST);
+  const int n_in = a.n_in, n_out = a.n_out;
+  {  // per-row power-of-two balance of the pairs (see pow2_scale)
+    double m[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      const int r = r0 + h;
+      if (r < a.rows)
+        for (int i = tid; i < n_in; i += bd) m[h] = fmax(m[h], fabs(a.in[(size_t)r * n_in + i]));
+    }
+    block_max_scales<double, 4>(m, red, scl);
+  }
+  if (inverse) {
+    for (int idx = tid; idx < kTrPairs * L; idx += bd) {
+      const int p = idx / L;
+      const int k = idx - p * L;
+      C V[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r = r0 + 2 * p + h;
+        double x = 0, xr = 0;
+        if (r < a.rows) {
+          const double* src = a.in + (size_t)r * n_in;
+          for (int pass = 0; pass < 2; ++pass) {
+            const int kk = pass == 0 ? k : L - k;
+            double v = 0;
+            if (pass == 1 && k == 0) break;
+            if (!sine) {
+              v = (kk < n_in) ? src[kk] : 0.0;
+            } else if (kk == 0) {
+              v = (L < n_in) ? 0.5 * src[L] : 0.0;
+            } else {
+              const int w = L - kk;
+              v = (w <= n_in - 1) ? src[w] : 0.0;
+            }
+            if (pass == 0) x = v; else xr = v;
+          }
+          x *= scl[2 * p + h];
+          xr *= scl[2 * p + h];
+        }
+        if (k == 0) {
+          V[h] = make_double2(x, 0.0);
+        } else {
+          const C e = Et[k];
+          V[h] = make_double2(0.5 * (e.x * x + e.y * xr), 0.5 * (e.y * x - e.x * xr));
+        }
+      }
+      RA[idx] = make_double2(V[0].x - V[1].y, V[0].y + V[1].x);
+    }
+    __syncthreads();
+    C* res = fft_rows<double, true>(RA, RB, kTrPairs, a.st, Wt);
+    for (int idx = tid; idx < 2 * kTrPairs * L; idx += bd) {
+      const int t = idx / L;
+      const int i = idx - t * L;
+      const int r = r0 + t;
+      if (r >= a.rows) continue;
+      const int src = (i & 1) ? (L - 1 - (i >> 1)) : (i >> 1);
+      const C v = res[(t >> 1) * L + src];
+      double val = ((t & 1) ? v.y : v.x) * scl[4 + t];
+      if (sine && (i & 1)) val = -val;
+      a.out[(size_t)r * n_out + i] = val;
+    }
+  } else {
+    for (int idx = tid; idx < kTrPairs * L; idx += bd) {
+      const int p = idx / L;
+      const int nn = idx - p * L;
+      const int src = makhoul_src(nn, L);
+      double v[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r = r0 + 2 * p + h;
+        double x = (r < a.rows) ? a.in[(size_t)r * n_in + src] * scl[2 * p + h] : 0.0;
+        if (sine && (src & 1)) x = -x;
+        v[h] = x;
+      }
+      RA[idx] = make_double2(v[0], v[1]);
+    }
+    __syncthreads();
+    C* Z = fft_rows<double, false>(RA, RB, kTrPairs, a.st, Wt);
+    for (int idx = tid; idx < 2 * kTrPairs * n_out; idx += bd) {
+      const int t = idx / n_out;
+      const int s = idx - t * n_out;
+      const int r = r0 + t;
+      if (r >= a.rows) continue;
+      double y = 0;
+      if (!(sine && s == 0)) {
+        const int k = sine ? L - s : s;
+        const int p = t >> 1;
+        const C Zk = Z[p * L + k];
+        const C Zm = Z[p * L + ((L - k) % L)];
+        const C e = Et[k];
+        if ((t & 1) == 0)
+          y = e.x * (Zk.x + Zm.x) * 0.5 + e.y * (Zk.y - Zm.y) * 0.5;
+        else
+          y = e.x * (Zk.y + Zm.y) * 0.5 - e.y * (Zk.x - Zm.x) * 0.5;
+        y *= ((!sine && k == 0) ? 1.0 / L : 2.0 / L) * scl[4 + t];
+      }
+      a.out[(size_t)r * n_out + s] = y;
+    }
+  }
+}
+
+// ---- F in state layout from the four spectral outputs (NLIN_FX/NLIN_DFX drop-ins) --------------
+struct FinishArgs {
+  int M, nr;
+  const double* Dr;
+  const double* out4;
+  size_t out_stride;
+  double* F;
+  size_t f_stride;
+};
+
+__global__ void __launch_bounds__(kFxThreads) k_fx_finish(FinishArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* opr = reinterpret_cast<double*>(smem_raw);
+  const int M = a.M, nr = a.nr, n = blockIdx.x, b = blockIdx.y;
+  for (int m = threadIdx.x; m < nr; m += blockDim.x) opr[m] = a.Dr[n * nr + m];
+  __syncthreads();
+  const int N = M * nr;
+  const double* O4 = a.out4 + (size_t)b * a.out_stride;
+  double* F = a.F + (size_t)b * a.f_stride;
+  for (int k = threadIdx.x; k < M; k += blockDim.x) {
+    const double* qs = O4 + (size_t)k * nr;
+    double q = 0;
+    for (int m = 0; m < nr; ++m) q += opr[m] * qs[m];
+    const size_t o = (size_t)k * nr + n;
+    F[o] = q - O4[N + o];
+    F[N + o] = O4[2 * N + o];
+    F[2 * N + o] = O4[3 * N + o];
+  }
+}
+
+// ---- launchers ---------------------------------------------------------------------------------
+template <typename T, int MODE>
+static cudaError_t launch_fx_t(const FxArgs& a, int batch, cudaStream_t s) {
+  const size_t smem = fx_smem_bytes(a.M, a.P, sizeof(T) == 4 ? SDD_PREC_MIXED : SDD_PREC_FP64);
+  cudaError_t e = cudaFuncSetAttribute(k_fx_rows<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  k_fx_rows<T, MODE><<<dim3(a.nr, batch), kFxThreads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fx(const FxArgs& a, int batch, int mode, int prec, cudaStream_t s) {
+  if (prec == SDD_PREC_MIXED) {
+    if (mode == 0) return launch_fx_t<float, 0>(a, batch, s);
+    if (mode == 1) return launch_fx_t<float, 1>(a, batch, s);
+    return launch_fx_t<float, 2>(a, batch, s);
+  }
+  if (mode == 0) return launch_fx_t<double, 0>(a, batch, s);
+  if (mode == 1) return launch_fx_t<double, 1>(a, batch, s);
+  return launch_fx_t<double, 2>(a, batch, s);
+}
+
+cudaError_t launch_rhs(const RhsArgs& a, int batch, cudaStream_t s) {
+  const size_t smem = (6 * (size_t)a.M + 2 * (size_t)a.nr) * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(k_rhs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_rhs<<<dim3(a.nr, batch), kFxThreads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_theta_op(int op, int M, int nr, int sym, const double* D2, const double* ir,
+                            const double* dT0, const double* g, double* f, int batch, cudaStream_t s) {
+  ThetaArgs a{op, M, nr, sym, D2, ir, dT0, g, f};
+  const size_t smem = (3 * (size_t)M + (size_t)nr) * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(k_theta_op, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_theta_op<<<dim3(nr, batch), kFxThreads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fx_finish(int M, int nr, const double* Dr, const double* out4, size_t out_stride,
+                             double* F, size_t f_stride, int batch, cudaStream_t s) {
+  FinishArgs a{M, nr, Dr, out4, out_stride, F, f_stride};
+  k_fx_finish<<<dim3(nr, batch), kFxThreads, nr * sizeof(double), s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_transform(int kind, int rows, int n_in, int n_out, const FftPlan* fp,
+                             const double* in, double* out, cudaStream_t s) {
+  TrArgs a;
+  a.kind = kind;
+  a.rows = rows;
+  a.n_in = n_in;
+  a.n_out = n_out;
+  a.L = fp->L;
+  a.st.L = fp->L;
+  a.st.nst = fp->nst;
+  for (int i = 0; i < kMaxStages; ++i) a.st.rad[i] = fp->rad[i];
+  a.w = fp->w64;
+  a.e = fp->e64;
+  a.in = in;
+  a.out = out;
+  const size_t smem = (2 * kTrPairs + 2) * (size_t)fp->L * sizeof(double2) + (4 * 32 + 8) * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(k_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int grid = (rows + 2 * kTrPairs - 1) / (2 * kTrPairs);
+  k_transform<<<grid, kFxThreads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace sdd

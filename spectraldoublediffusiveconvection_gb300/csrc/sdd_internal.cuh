@@ -1,0 +1,104 @@
+// Internal declarations shared by the CUDA translation units of libsdd_gb300.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "../../include/sdd_gb300.h"
+
+namespace sdd {
+
+constexpr int kMaxStages = 16;   // FFT stages (radices) per length
+constexpr int kMaxRadix = 7;     // largest radix handled by the butterflies (2,3,4,5,7)
+constexpr int kMaxNr = 64;       // interior radial points supported by the chain kernel
+constexpr int kMaxM = 1024;      // theta modes supported
+constexpr int kFxThreads = 256;  // threads of the row kernels
+
+void set_cuda_error(cudaError_t e);
+
+// Twiddle tables and radix plan of one complex FFT length L (used for DCT-II/III of length L).
+struct FftPlan {
+  int L = 0;
+  int nst = 0;
+  int rad[kMaxStages] = {0};
+  double2* w64 = nullptr;   // exp(-2 pi i k / L), k < L
+  double2* e64 = nullptr;   // exp(+i pi k / (2L)), k < L
+  float2* w32 = nullptr;
+  float2* e32 = nullptr;
+};
+
+// Returns a cached device FFT plan for length L (nullptr if L has a prime factor > kMaxRadix).
+const FftPlan* get_fft_plan(int L);
+
+// Kernel argument blocks -----------------------------------------------------------------------
+
+struct StageArgs {           // radices passed by value
+  int L, nst;
+  int rad[kMaxStages];
+};
+
+struct FxOps {               // FP64 or FP32 copies of the operators the nonlinear term needs
+  const void* Dr;            // nr*nr
+  const void* D2r2;          // nr*nr
+  const void* ir4r2;         // nr
+  const void* w;             // FFT twiddles (complex, P)
+  const void* e;             // DCT twiddles (complex, P)
+};
+
+struct FxArgs {
+  int M, nr, P, sym;
+  StageArgs st;
+  FxOps ops;
+  const double* X;           // state whose nonlinear term (FX) or perturbation (DFX) is formed
+  size_t x_stride;           // doubles between shells in X
+  void* base;                // base-state grid cache [shell][nr][9][P] (T precision), nullable
+  size_t base_stride;        // elements between shells in base
+  double* out4;              // [shell][4][M][nr] : Qhat, Rhat, NJ_T hat, NJ_S hat
+  size_t out_stride;         // doubles between shells in out4
+  double* fx_out;            // optional: write F directly in state layout [shell][3][M][nr]
+  size_t fx_stride;
+};
+
+struct RhsArgs {
+  int M, nr, sym, linear;
+  double dt, Pr;
+  const double* Dr;          // nr*nr
+  const double* D2s;         // nr*nr (A2_SINE)
+  const double* ir2s, *rsq, *dT0, *gr;
+  const double* X;           // state (or perturbation) the linear terms act on
+  size_t x_stride;
+  const double* out4;        // FX spectral outputs (ignored when linear)
+  size_t out_stride;
+  const double* Ra, *Ra_s;   // per shell
+  double* rhs;               // [shell][3][M][nr]
+  size_t rhs_stride;
+};
+
+struct ChainArgs {
+  int M, nr, ldl, sym;
+  int field0;                // first field handled (blockIdx.x/2 + field0)
+  size_t field_off;          // doubles between field blocks (N_fm*nr, or 0 when g/f point at one block)
+  const double* g;           // rhs [shell][3][M][nr]
+  size_t g_stride;
+  double* f;                 // solution [shell][3][M][nr]
+  size_t f_stride;
+  const double* sub;         // nullable: f -= sub (Newton residual), same layout
+  size_t sub_stride;
+  const double* LinvA4, *LinvT, *LinvS;  // [M][nr][ldl]
+  const double* D2A4;        // [nr][nr]
+  const double* ir2A4, *ir4A4;
+  double dtA4, dtT, dtS;     // Pr*dt, dt, Tau*dt
+};
+
+// launchers (return cudaError_t of the launch)
+cudaError_t launch_fx(const FxArgs& a, int batch, int mode, int prec, cudaStream_t s);
+cudaError_t launch_rhs(const RhsArgs& a, int batch, cudaStream_t s);
+cudaError_t launch_chain(const ChainArgs& a, int batch, int nfields, cudaStream_t s);
+cudaError_t launch_theta_op(int op, int M, int nr, int sym, const double* D2, const double* ir,
+                            const double* dT0, const double* g, double* f, int batch,
+                            cudaStream_t s);
+cudaError_t launch_transform(int kind, int rows, int n_in, int n_out, const FftPlan* fp,
+                             const double* in, double* out, cudaStream_t s);
+size_t fx_smem_bytes(int M, int P, int prec);
+
+}  // namespace sdd

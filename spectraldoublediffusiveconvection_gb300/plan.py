@@ -1,0 +1,200 @@
+"""Plans: device-resident operators for one (N_fm, N_r, d, dt, Pr, Tau, symmetric, precision).
+
+A plan replaces the operator tuple of ``Build_Matrix_Operators`` (Main.py:179-225) on the GPU.  The
+operators do not depend on Ra_T (it enters only through the buoyancy coupling, Main.py:271), so shells
+that share (N_fm, N_r, d, dt, Pr, Tau) share one plan and are advanced as a batch.
+
+All compute goes through libsdd_gb300 (C ABI, ``include/sdd_gb300.h``); torch provides device memory
+and the current stream.
+"""
+import ctypes
+import threading
+
+import numpy as np
+
+from . import _lib
+from .operators import plan_arrays
+
+_PREC = {"fp64": _lib.SDD_PREC_FP64, "mixed": _lib.SDD_PREC_MIXED}
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _stream(device):
+    torch = _torch()
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def _dptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+class Plan:
+    """Device operators + workspace for shells of one shape and step.
+
+    Parameters mirror ``Build_Matrix_Operators(N_fm, N_r, d, dt, Pr, Tau)`` plus ``symmetric`` and the
+    nonlinear-term precision ("fp64" plain, "mixed" = FP32 nonlinear term / FP64 solves).
+    """
+
+    def __init__(self, N_fm, N_r, d, dt, Pr, Tau, symmetric=False, precision="fp64", device=None,
+                 arrays=None):
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise RuntimeError("a CUDA device is required (libsdd_gb300 has no CPU path)")
+        if N_fm % 2 != 0:
+            raise ValueError('The number of Fourier modes is not even %d' % N_fm)
+        self.N_fm, self.N_r, self.d, self.dt, self.Pr, self.Tau = int(N_fm), int(N_r), float(d), float(dt), \
+            float(Pr), float(Tau)
+        self.nr = self.N_r - 1
+        self.symmetric = bool(symmetric)
+        self.precision = precision
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.arrays = arrays if arrays is not None else plan_arrays(N_fm, N_r, d, dt, Pr, Tau)
+        A = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in self.arrays.items()
+             if isinstance(v, np.ndarray)}
+        self._host = A
+        desc = _lib.PlanDesc()
+        desc.N_fm, desc.nr, desc.symmetric = self.N_fm, self.nr, int(self.symmetric)
+        desc.precision = _PREC[precision]
+        desc.dt, desc.Pr, desc.Tau = self.dt, self.Pr, self.Tau
+        for name in ("Dr", "D2_r2", "ir4_r2", "D2_sine", "ir2_sine", "D2_A4", "ir2_A4", "ir4_A4", "rsq",
+                     "dT0", "gr", "Linv_A4", "Linv_T", "Linv_S"):
+            setattr(desc, name, _ptr(A[name]))
+        h = ctypes.c_void_p()
+        L = _lib.lib()
+        with torch.cuda.device(self.device):
+            _lib.check(L.sdd_plan_create(ctypes.byref(desc), ctypes.byref(h)), "sdd_plan_create")
+        self._h = h
+        self._L = L
+        self.n_state = 3 * self.N_fm * self.nr
+        self.base_elems = int(L.sdd_plan_base_cache_elems(h))
+
+    # ------------------------------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            torch = _torch()
+            with torch.cuda.device(self.device):
+                self._L.sdd_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------------------------------------
+    def _chk(self, t, n, name):
+        torch = _torch()
+        if not isinstance(t, torch.Tensor) or t.dtype != torch.float64 or t.device != self.device:
+            raise TypeError(f"{name}: expected a float64 tensor on {self.device}")
+        if not t.is_contiguous() or t.numel() % n != 0:
+            raise ValueError(f"{name}: expected a contiguous tensor of batch x {n} elements")
+        return t.numel() // n
+
+    def _vec(self, v, batch):
+        torch = _torch()
+        if isinstance(v, torch.Tensor):
+            v = v.to(device=self.device, dtype=torch.float64).reshape(-1)
+            if v.numel() == 1:
+                v = v.expand(batch).contiguous()
+            return v.contiguous()
+        return torch.full((batch,), float(v), dtype=torch.float64, device=self.device)
+
+    def new_state(self, batch=1):
+        torch = _torch()
+        return torch.zeros((batch, self.n_state), dtype=torch.float64, device=self.device)
+
+    def new_base(self, batch=1):
+        torch = _torch()
+        return torch.empty((batch, self.base_elems), dtype=torch.float64, device=self.device)
+
+    # ---- entry points -------------------------------------------------------------------------
+    def nlin_fx(self, X, out=None, base=None):
+        B = self._chk(X, self.n_state, "X")
+        out = out if out is not None else _torch().empty_like(X)
+        _lib.check(self._L.sdd_nlin_fx(self._h, B, _dptr(X), _dptr(out), _dptr(base), _stream(self.device)),
+                   "sdd_nlin_fx")
+        return out
+
+    def nlin_dfx(self, dv, X=None, base=None, out=None):
+        B = self._chk(dv, self.n_state, "dv")
+        out = out if out is not None else _torch().empty_like(dv)
+        _lib.check(self._L.sdd_nlin_dfx(self._h, B, _dptr(dv), _dptr(X), _dptr(base), _dptr(out),
+                                        _stream(self.device)), "sdd_nlin_dfx")
+        return out
+
+    def a4_bsub(self, g, out=None):
+        B = self._chk(g, self.N_fm * self.nr, "g")
+        out = out if out is not None else _torch().empty_like(g)
+        _lib.check(self._L.sdd_a4_bsub(self._h, B, _dptr(g), _dptr(out), _stream(self.device)), "sdd_a4_bsub")
+        return out
+
+    def nab2_bsub(self, field, g, out=None):
+        B = self._chk(g, self.N_fm * self.nr, "g")
+        out = out if out is not None else _torch().empty_like(g)
+        _lib.check(self._L.sdd_nab2_bsub(self._h, int(field), B, _dptr(g), _dptr(out), _stream(self.device)),
+                   "sdd_nab2_bsub")
+        return out
+
+    def theta_op(self, op, g, out=None):
+        B = self._chk(g, self.N_fm * self.nr, "g")
+        out = out if out is not None else _torch().empty_like(g)
+        _lib.check(self._L.sdd_theta_op(self._h, int(op), B, _dptr(g), _dptr(out), _stream(self.device)),
+                   "sdd_theta_op")
+        return out
+
+    def step(self, X, Ra, Ra_s, nsteps=1, linear=False, out=None):
+        B = self._chk(X, self.n_state, "X")
+        out = out if out is not None else _torch().empty_like(X)
+        ra, ras = self._vec(Ra, B), self._vec(Ra_s, B)
+        _lib.check(self._L.sdd_step(self._h, B, _dptr(ra), _dptr(ras), _dptr(X), _dptr(out), int(nsteps),
+                                    int(bool(linear)), _stream(self.device)), "sdd_step")
+        return out
+
+    def pfx(self, X, Ra, Ra_s, out=None, base=None):
+        B = self._chk(X, self.n_state, "X")
+        out = out if out is not None else _torch().empty_like(X)
+        ra, ras = self._vec(Ra, B), self._vec(Ra_s, B)
+        _lib.check(self._L.sdd_pfx(self._h, B, _dptr(ra), _dptr(ras), _dptr(X), _dptr(out), _dptr(base),
+                                   _stream(self.device)), "sdd_pfx")
+        return out
+
+    def pdfx(self, dv, X, Ra, Ra_s, base=None, out=None):
+        B = self._chk(dv, self.n_state, "dv")
+        out = out if out is not None else _torch().empty_like(dv)
+        ra, ras = self._vec(Ra, B), self._vec(Ra_s, B)
+        _lib.check(self._L.sdd_pdfx(self._h, B, _dptr(ra), _dptr(ras), _dptr(dv), _dptr(X), _dptr(base),
+                                    _dptr(out), _stream(self.device)), "sdd_pdfx")
+        return out
+
+
+_cache = {}
+_cache_lock = threading.Lock()
+
+
+def get_plan(N_fm, N_r, d, dt, Pr, Tau, symmetric=False, precision="fp64", device=None):
+    """Cached plan for the key (N_fm, N_r, d, dt, Pr, Tau, symmetric, precision, device)."""
+    torch = _torch()
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    key = (int(N_fm), int(N_r), float(d), float(dt), float(Pr), float(Tau), bool(symmetric), precision, str(dev))
+    with _cache_lock:
+        p = _cache.get(key)
+        if p is None:
+            p = Plan(N_fm, N_r, d, dt, Pr, Tau, symmetric, precision, dev)
+            _cache[key] = p
+        return p
+
+
+def clear_plans():
+    with _cache_lock:
+        for p in _cache.values():
+            p.close()
+        _cache.clear()

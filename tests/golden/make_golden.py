@@ -1,0 +1,237 @@
+"""Generate the golden vectors in ``tests/golden/*.npz`` by running the reference itself.
+
+The reference (mannixp/SpectralDoubleDiffusiveConvection, Python + numpy + scipy + numba) is imported
+read-only from REF_DIR.  Its pinned third-party packages that are not installed here are replaced by
+shims, so that the reference's own source runs unmodified:
+
+* ``numba.njit``           -> identity decorator (the reference then runs un-JIT'd, same arithmetic
+                               up to fastmath reassociation, i.e. ~1e-16 relative);
+* ``numba.typed.List``     -> ``list``;
+* ``matplotlib``/``pyplot``-> empty stub modules (plotting only);
+* ``h5py``                 -> an in-memory fake whose ``File`` objects keep what ``_Time_Step`` writes
+                               (``Checkpoints/X_DATA``, ``Scalar_Data/*``), so trajectories and per-step
+                               diagnostics can be read back;
+* ``np.RankWarning`` / ``np.trapz`` -> numpy-2 aliases (``Matrix_Operators.py:6``, ``Main.py:9,129``).
+
+Run:  python tests/golden/make_golden.py [REF_DIR]
+It writes small ``.npz`` fixtures beside this script.  They are inputs/outputs of the reference's own
+functions on seeded synthetic states (amplitude 1e-3*exp(-k/8)*exp(-n/4), default_rng seeds below).
+"""
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+
+
+# ----------------------------------------------------------------------------------------------
+# shims
+# ----------------------------------------------------------------------------------------------
+def _install_shims():
+    if not hasattr(np, "RankWarning"):
+        np.RankWarning = np.exceptions.RankWarning
+    if not hasattr(np, "trapz"):
+        np.trapz = np.trapezoid
+
+    numba = types.ModuleType("numba")
+
+    def njit(*a, **k):
+        if len(a) == 1 and callable(a[0]) and not k:
+            return a[0]
+        return lambda f: f
+
+    numba.njit = njit
+    typed = types.ModuleType("numba.typed")
+    typed.List = list
+    numba.typed = typed
+    sys.modules["numba"] = numba
+    sys.modules["numba.typed"] = typed
+
+    mpl = types.ModuleType("matplotlib")
+    plt = types.ModuleType("matplotlib.pyplot")
+    mpl.pyplot = plt
+    sys.modules["matplotlib"] = mpl
+    sys.modules["matplotlib.pyplot"] = plt
+
+    h5py = types.ModuleType("h5py")
+
+    class _Group(dict):
+        def create_group(self, name):
+            g = _Group()
+            self[name] = g
+            return g
+
+        def create_dataset(self, name, data=None):
+            self[name] = np.asarray(data)
+
+        def __setitem__(self, key, value):
+            if not isinstance(value, _Group):
+                value = np.array(value, copy=True)
+            dict.__setitem__(self, key, value)
+
+    class File(_Group):
+        files = {}
+
+        def __init__(self, name, mode="r"):
+            super().__init__()
+            File.files[name] = self
+
+        def close(self):
+            pass
+
+    h5py.File = File
+    sys.modules["h5py"] = h5py
+    return h5py
+
+
+H5 = _install_shims()
+sys.path.insert(0, REF_DIR)
+import Transforms as Tr  # noqa: E402
+import Matrix_Operators as MO  # noqa: E402
+import Main  # noqa: E402
+
+PARAMS = dict(d=2.0, Pr=1.0, Tau=0.01, Ra=8000.0, Ra_s=500.0)
+
+
+def seeded_state(N_fm, nr, seed, symmetric=False):
+    """Seeded Gaussian coefficients of amplitude 1e-3*exp(-k/8)*exp(-n/4) per field (psi, T, S)."""
+    rng = np.random.default_rng(seed)
+    k = np.arange(N_fm)[None, :]
+    n = np.arange(nr)[:, None]
+    amp = 1e-3 * np.exp(-k / 8.0) * np.exp(-n / 4.0)
+    P, T, S = [rng.standard_normal((nr, N_fm)) * amp for _ in range(3)]
+    return MO.Vecs_to_X(P, T, S, N_fm, nr, symmetric)
+
+
+def linear_parts(Xn, NX, ops, N, N_fm, nr, dt, Pr, Tau, Ra, Ra_s, symmetric, subtract):
+    """Main.py:255-283 / 473-496: the linear half of one step after NX = -dt*F has been formed."""
+    D, R, Rsq, DT0, gr_k, LA4, LT, LS, args_A4, args_FX = ops
+    psi, T, S = Xn[0:N], Xn[N:2 * N], Xn[2 * N:3 * N]
+    psi_T0 = MO.DT0_theta(psi, DT0, N_fm, nr, symmetric)
+    Om = MO.A2_SINE(psi, D, R, N_fm, nr, symmetric)
+    NX[0:N] += Om + dt * Pr * gr_k.dot(Ra * T - Ra_s * S)
+    a = MO.A4_BSub_TSTEP_V2(NX[0:N], LA4, *args_A4, Pr * dt, symmetric)
+    NX[N:2 * N] += Rsq.dot(T) - dt * psi_T0
+    b = MO.NAB2_BSub_TSTEP_V2(NX[N:2 * N], LT, N_fm, nr, dt, symmetric)
+    NX[2 * N:3 * N] += Rsq.dot(S) - dt * psi_T0
+    c = MO.NAB2_BSub_TSTEP_V2(NX[2 * N:3 * N], LS, N_fm, nr, Tau * dt, symmetric)
+    if subtract:
+        a, b, c = a - psi, b - T, c - S
+    return np.hstack((a, b, c))
+
+
+def operator_case(tag, N_r, N_fm, dt, symmetric, seed, store_linv=False):
+    d, Pr, Tau, Ra, Ra_s = (PARAMS[k] for k in ("d", "Pr", "Tau", "Ra", "Ra_s"))
+    nr = N_r - 1
+    N = nr * N_fm
+    out = {}
+    ops = Main.Build_Matrix_Operators(N_fm, N_r, d, dt, Pr, Tau)
+    D, R, Rsq, DT0, gr_k, LA4, LT, LS, args_A4, args_FX = ops
+    X = seeded_state(N_fm, nr, seed, symmetric)
+    dv = seeded_state(N_fm, nr, seed + 1, symmetric)
+    if symmetric:
+        X_SYM = Main.Eq_SYM(X, R)
+        X = X_SYM * X
+        dv = X_SYM * dv
+    psi = X[0:N]
+    out.update(D=D, R=R, X=X, dv=dv, DT0=DT0,
+               params=np.array([N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, float(symmetric)]))
+    out["J_theta_RT"] = MO.J_theta_RT(psi, nr, N_fm, symmetric)
+    out["A2_SINE_R2"] = MO.A2_SINE_R2(psi, N_fm, nr, D, R, symmetric)
+    out["A2_SINE"] = MO.A2_SINE(psi, D, R, N_fm, nr, symmetric)
+    out["DT0_theta"] = MO.DT0_theta(psi, DT0, N_fm, nr, symmetric)
+    out["NLIN_FX"] = MO.NLIN_FX(X, *args_FX, symmetric)
+    out["NLIN_DFX"] = MO.NLIN_DFX(dv, X, *args_FX, symmetric)
+    g = dv[0:N] * 1e3
+    out["A4_g"] = g
+    out["A4_BSub"] = MO.A4_BSub_TSTEP_V2(g, LA4, *args_A4, Pr * dt, symmetric)
+    out["NAB2_T"] = MO.NAB2_BSub_TSTEP_V2(g, LT, N_fm, nr, dt, symmetric)
+    out["NAB2_S"] = MO.NAB2_BSub_TSTEP_V2(g, LS, N_fm, nr, Tau * dt, symmetric)
+    # one IMEX ("CNAB1") step, Main.py:255-283
+    NX = -1 * dt * MO.NLIN_FX(X, *args_FX, symmetric)
+    out["step1"] = linear_parts(X, NX, ops, N, N_fm, nr, dt, Pr, Tau, Ra, Ra_s, symmetric, False)
+    NX = np.zeros(3 * N)
+    out["step1_linear"] = linear_parts(X, NX, ops, N, N_fm, nr, dt, Pr, Tau, Ra, Ra_s, symmetric, False)
+    # Newton residual and Jacobian with the dt=1 operator set, Main.py:473-521
+    ops1 = Main.Build_Matrix_Operators(N_fm, N_r, d, 1.0, Pr, Tau)
+    NX = -1.0 * MO.NLIN_FX(X, *ops1[9], symmetric)
+    out["PFX"] = linear_parts(X, NX, ops1, N, N_fm, nr, 1.0, Pr, Tau, Ra, Ra_s, symmetric, True)
+    NX = -1.0 * MO.NLIN_DFX(dv, X, *ops1[9], symmetric)
+    out["PDFX"] = linear_parts(dv, NX, ops1, N, N_fm, nr, 1.0, Pr, Tau, Ra, Ra_s, symmetric, True)
+    # diagnostics, Main.py:41-134
+    out["KE"] = np.array(Main.Kinetic_Energy(X, R, D, N_fm, nr, symmetric))
+    out["NuT"] = np.array(Main.Nusselt(X[N:2 * N], d, R, D, N_fm, nr, check=False))
+    out["NuS"] = np.array(Main.Nusselt(X[2 * N:3 * N], d, R, D, N_fm, nr, check=False))
+    if store_linv:
+        out["Linv_A4"] = np.array(LA4)
+        out["Linv_T"] = np.array(LT)
+        out["Linv_S"] = np.array(LS)
+        out["D2_A4"], out["IR4_A4"], out["IR2_A4"] = args_A4[0], args_A4[1], args_A4[2]
+    np.savez(os.path.join(HERE, f"ops_{tag}.npz"), **out)
+    print("wrote", tag, {k: np.shape(v) for k, v in out.items() if np.ndim(v) > 0 and np.size(v) > 40})
+
+
+def trajectory_case(tag, N_r, N_fm, dt, n_steps, symmetric, seed, linear=False):
+    """Main._Time_Step run as written; X_DATA every n_steps/10 steps and the scalar series come back
+    through the fake h5py File."""
+    d, Pr, Tau, Ra, Ra_s = (PARAMS[k] for k in ("d", "Pr", "Tau", "Ra", "Ra_s"))
+    nr = N_r - 1
+    X0 = seeded_state(N_fm, nr, seed, symmetric)
+    fname = f"golden_{tag}.h5"
+    total = n_steps * dt
+    assert int(total / dt) == n_steps, (total, dt)
+    XN = Main._Time_Step(X0.copy(), Ra, Ra_s, Tau, Pr, d, N_fm, N_r, symmetric, save_filename=fname,
+                         start_time=0, Total_time=total, dt=dt, linear=linear, Verbose=False)
+    f = H5.File.files[fname]
+    out = dict(X0=X0, X_final=XN, X_DATA=np.asarray(f["Checkpoints"]["X_DATA"]),
+               Norm=np.asarray(f["Scalar_Data"]["Norm"]), KE=np.asarray(f["Scalar_Data"]["KE"]),
+               NuT=np.asarray(f["Scalar_Data"]["Nu_T"]), NuS=np.asarray(f["Scalar_Data"]["Nu_S"]),
+               params=np.array([N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, float(symmetric), n_steps]))
+    np.savez(os.path.join(HERE, f"traj_{tag}.npz"), **out)
+    print("wrote", tag, out["X_DATA"].shape)
+
+
+def transform_case():
+    """Transforms.py:73-129 on seeded rows, with and without the 3/2 zero-padding length n."""
+    rng = np.random.default_rng(7)
+    out = {}
+    for M in (8, 10, 16, 64):
+        P = (3 * M) // 2
+        a = rng.standard_normal((3, M))
+        g = rng.standard_normal((3, P))
+        out[f"IDCT_in_{M}"] = a
+        out[f"IDCT_{M}"] = Tr.IDCT(a, n=P)
+        out[f"IDST_{M}"] = Tr.IDST(a, n=P)
+        out[f"IDCT_nonpad_{M}"] = Tr.IDCT(a)
+        out[f"IDST_nonpad_{M}"] = Tr.IDST(a)
+        out[f"DCT_in_{M}"] = g
+        out[f"DCT_{M}"] = Tr.DCT(g)
+        out[f"DST_{M}"] = Tr.DST(g)
+        out[f"DCT_trunc_{M}"] = Tr.DCT(g, n=M)
+        out[f"DST_trunc_{M}"] = Tr.DST(g, n=M)
+        out[f"grid_{M}"] = Tr.grid(P)
+    np.savez(os.path.join(HERE, "transforms.npz"), **out)
+    print("wrote transforms")
+
+
+if __name__ == "__main__":
+    # the reference's own known-answer tests must pass before anything is recorded (Transforms.py:132-374)
+    for k in range(4):
+        Tr.test_Cosine_Transform(k, 64)
+        Tr.test_Sine_Transform(k + 1, 64)
+        Tr.test_Cosine_Transform_deal(k, 64)
+        Tr.test_Sine_Transform_deal(k + 1, 64)
+    Tr.test_Cosine_Transform_NL(64)
+    Tr.test_Sine_Transform_NL(64)
+    transform_case()
+    operator_case("tiny", N_r=6, N_fm=8, dt=1e-3, symmetric=False, seed=11, store_linv=True)
+    operator_case("tiny_sym", N_r=6, N_fm=8, dt=1e-3, symmetric=True, seed=12, store_linv=True)
+    operator_case("m10_sym", N_r=8, N_fm=10, dt=5e-3, symmetric=True, seed=13)
+    operator_case("c1", N_r=20, N_fm=64, dt=1e-3, symmetric=False, seed=1234)
+    operator_case("c1_sym", N_r=20, N_fm=64, dt=1e-3, symmetric=True, seed=1234)
+    trajectory_case("c1", N_r=20, N_fm=64, dt=1e-3, n_steps=2000, symmetric=False, seed=1234)
+    trajectory_case("tiny", N_r=6, N_fm=8, dt=1e-3, n_steps=200, symmetric=False, seed=21)
+    trajectory_case("sym_lin", N_r=8, N_fm=10, dt=5e-3, n_steps=100, symmetric=True, seed=22, linear=True)

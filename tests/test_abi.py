@@ -1,0 +1,41 @@
+"""C ABI: the library builds for sm_103a, loads without a GPU, and exports every declared symbol."""
+import ctypes
+import os
+import re
+
+from conftest import ROOT
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "sdd_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(sdd_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_bound_symbols():
+    from spectraldoublediffusiveconvection_gb300 import _lib
+    bound = sorted(n for n, _, _ in _lib.SIGNATURES)
+    assert bound == _declared()
+
+
+def test_library_loads_and_exports(built_lib):
+    L = ctypes.CDLL(built_lib)
+    for name in _declared():
+        assert hasattr(L, name), name
+    from spectraldoublediffusiveconvection_gb300 import _lib
+    lib = _lib.load(built_lib)
+    assert lib.sdd_version() >= 100
+    assert lib.sdd_error_string(-2).decode().startswith("The number of Fourier modes")
+
+
+def test_argument_errors_need_no_gpu(built_lib):
+    """Argument checks run before any CUDA call, so they are testable on a CPU-only host."""
+    from spectraldoublediffusiveconvection_gb300 import _lib
+    lib = _lib.load(built_lib)
+    assert lib.sdd_transform(9, 1, 4, 6, None, None, None) == _lib.SDD_ERR_ARG
+    assert lib.sdd_plan_create(None, None) == _lib.SDD_ERR_ARG
+    d = _lib.PlanDesc()
+    d.N_fm, d.nr = 7, 4
+    h = ctypes.c_void_p()
+    assert lib.sdd_plan_create(ctypes.byref(d), ctypes.byref(h)) == _lib.SDD_ERR_ODD_NFM
+    assert lib.sdd_step(None, 1, None, None, None, None, 1, 0, None) == _lib.SDD_ERR_ARG

@@ -1,0 +1,191 @@
+"""GPU parity: libsdd_gb300 (through the C ABI) against the reference's golden vectors and the oracle.
+
+Tolerances: FP64 plain path, relative L2 error <= 1e-11 per call (the target is 1e-11 for whole
+trajectories; single operator applications are checked tighter, at 1e-12 or 1e-13).
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel
+from oracle import sdd_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+OPS_CASES = ["tiny", "tiny_sym", "m10_sym", "c1", "c1_sym"]
+
+
+def _case(tag):
+    Z = load_golden(f"ops_{tag}.npz")
+    N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, sym = Z["params"]
+    return Z, int(N_r), int(N_fm), dt, d, Pr, Tau, Ra, Ra_s, bool(sym)
+
+
+def test_transforms_golden(cuda):
+    from spectraldoublediffusiveconvection_gb300 import Transforms as T
+    G = load_golden("transforms.npz")
+    for M in (8, 10, 16, 64):
+        P = 3 * M // 2
+        a, g = G[f"IDCT_in_{M}"], G[f"DCT_in_{M}"]
+        assert np.abs(T.IDCT(a, n=P) - G[f"IDCT_{M}"]).max() < 1e-13
+        assert np.abs(T.IDST(a, n=P) - G[f"IDST_{M}"]).max() < 1e-13
+        assert np.abs(T.IDCT(a) - G[f"IDCT_nonpad_{M}"]).max() < 1e-13
+        assert np.abs(T.IDST(a) - G[f"IDST_nonpad_{M}"]).max() < 1e-13
+        assert np.abs(T.DCT(g) - G[f"DCT_{M}"]).max() < 1e-13
+        assert np.abs(T.DST(g) - G[f"DST_{M}"]).max() < 1e-13
+        assert np.abs(T.DCT(g, n=M) - G[f"DCT_trunc_{M}"]).max() < 1e-13
+        assert np.abs(T.DST(g, n=M) - G[f"DST_trunc_{M}"]).max() < 1e-13
+
+
+@pytest.mark.parametrize("M", [4, 12, 64, 96, 128, 256, 384, 512])
+def test_transforms_random_rows(cuda, M):
+    """Padded inverse and truncated forward transforms at the production lengths (P = 3M/2)."""
+    from spectraldoublediffusiveconvection_gb300 import Transforms as T
+    rng = np.random.default_rng(M)
+    P = 3 * M // 2
+    a = rng.standard_normal((7, M))
+    g = rng.standard_normal((5, P))
+    for fn_dev, fn_or, x, n in ((T.IDCT, O.IDCT, a, P), (T.IDST, O.IDST, a, P)):
+        assert rel(fn_dev(x, n=n), fn_or(x, n=n)) < 1e-13
+    assert rel(T.DCT(g, n=M), O.DCT(g, n=M)) < 1e-13
+    assert rel(T.DST(g, n=M), O.DST(g, n=M)) < 1e-13
+    # a transform along axis 0
+    assert rel(T.IDCT(a.T, n=P, axis=0), O.IDCT(a.T, n=P, axis=0)) < 1e-13
+
+
+def test_transform_known_answers(cuda):
+    """The reference's own KATs (Transforms.py:132-374): a single mode survives a round trip exactly
+    (12 decimals), and the padded transforms of a product of modes give the product's modes."""
+    from spectraldoublediffusiveconvection_gb300 import Transforms as T
+    N = 64
+    x = T.grid(N)
+    for k in range(4):
+        f_hat = np.zeros(N)
+        f_hat[k] = 1
+        assert np.array_equal(np.round(T.DCT(T.IDCT(f_hat)), 12), f_hat)
+        assert np.allclose(T.IDCT(T.DCT(np.cos(k * x))), np.cos(k * x), atol=1e-12)
+        g_hat = np.zeros(N)
+        g_hat[k + 1] = 1
+        assert np.array_equal(np.round(T.DST(T.IDST(g_hat)), 12), g_hat)
+        assert np.allclose(T.IDST(T.DST(np.sin((k + 1) * x))), np.sin((k + 1) * x), atol=1e-12)
+        # dealiased: transform to 3N/2 and back
+        f_hat = np.zeros(N)
+        f_hat[k] = 1
+        f = T.IDCT(f_hat, n=3 * N // 2)
+        assert np.allclose(T.DCT(f, n=N), f_hat, atol=1e-12)
+
+
+@pytest.mark.parametrize("tag", OPS_CASES)
+def test_matrix_operators_golden(cuda, tag):
+    from spectraldoublediffusiveconvection_gb300 import Matrix_Operators as MO
+    Z, N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, sym = _case(tag)
+    nr = N_r - 1
+    N = nr * N_fm
+    D, R = Z["D"], Z["R"]
+    X, dv = Z["X"], Z["dv"]
+    psi = X[:N]
+    assert rel(MO.J_theta_RT(psi, nr, N_fm, sym), Z["J_theta_RT"]) < 1e-13
+    assert rel(MO.A2_SINE_R2(psi, N_fm, nr, D, R, sym), Z["A2_SINE_R2"]) < 1e-13
+    assert rel(MO.A2_SINE(psi, D, R, N_fm, nr, sym), Z["A2_SINE"]) < 1e-13
+    assert rel(MO.DT0_theta(psi, Z["DT0"], N_fm, nr, sym), Z["DT0_theta"]) < 1e-13
+    assert rel(MO.NLIN_FX(X, D, R, N_fm, nr, sym), Z["NLIN_FX"]) < 1e-12
+    assert rel(MO.NLIN_DFX(dv, X, D, R, N_fm, nr, sym), Z["NLIN_DFX"]) < 1e-12
+    ops = O.Operators(N_fm, N_r, d, dt, Pr, Tau)
+    g = Z["A4_g"]
+    assert rel(MO.A4_BSub_TSTEP_V2(g, ops.Linv_A4, ops.D2_A4, np.diag(ops.IR4_A4), np.diag(ops.IR2_A4),
+                                   N_fm, nr, Pr * dt, sym), Z["A4_BSub"]) < 1e-12
+    assert rel(MO.NAB2_BSub_TSTEP_V2(g, list(ops.Linv_T), N_fm, nr, dt, sym), Z["NAB2_T"]) < 1e-12
+    assert rel(MO.NAB2_BSub_TSTEP_V2(g, ops.Linv_S, N_fm, nr, Tau * dt, sym), Z["NAB2_S"]) < 1e-12
+
+
+@pytest.mark.parametrize("tag", OPS_CASES)
+def test_step_and_newton_operators_golden(cuda, tag):
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    Z, N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, sym = _case(tag)
+    p = Plan(N_fm, N_r, d, dt, Pr, Tau, symmetric=sym)
+    X = torch.from_numpy(Z["X"]).cuda().reshape(1, -1)
+    dv = torch.from_numpy(Z["dv"]).cuda().reshape(1, -1)
+    assert rel(p.step(X, Ra, Ra_s).cpu().numpy().ravel(), Z["step1"]) < 1e-12
+    assert rel(p.step(X, Ra, Ra_s, linear=True).cpu().numpy().ravel(), Z["step1_linear"]) < 1e-12
+    p1 = Plan(N_fm, N_r, d, 1.0, Pr, Tau, symmetric=sym)
+    base = p1.new_base(1)
+    F = p1.pfx(X, Ra, Ra_s, base=base)
+    assert rel(F.cpu().numpy().ravel(), Z["PFX"]) < 1e-12
+    J = p1.pdfx(dv, X, Ra, Ra_s, base=base)
+    assert rel(J.cpu().numpy().ravel(), Z["PDFX"]) < 1e-12
+    J2 = p1.pdfx(dv, X, Ra, Ra_s)        # base recomputed from X
+    assert rel(J2.cpu().numpy().ravel(), Z["PDFX"]) < 1e-12
+
+
+def test_trajectory_c1_2000_steps(cuda):
+    """Plain FP64, N_r=20, N_theta=64, dt=1e-3: the states the reference's _Time_Step saved (after steps
+    1, 201, ..., 1801) and the final state after 2000 steps agree to 1e-11 relative."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    Z = load_golden("traj_c1.npz")
+    N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, sym, ns = Z["params"]
+    p = Plan(int(N_fm), int(N_r), d, dt, Pr, Tau, symmetric=bool(sym))
+    X = torch.from_numpy(Z["X0"]).cuda().reshape(1, -1)
+    X = p.step(X, Ra, Ra_s, nsteps=1)
+    done = 1
+    for s, ref in enumerate(Z["X_DATA"]):
+        target = 200 * s + 1
+        if target > done:
+            X = p.step(X, Ra, Ra_s, nsteps=target - done)
+            done = target
+        assert rel(X.cpu().numpy().ravel(), ref) < 1e-11, s
+    X = p.step(X, Ra, Ra_s, nsteps=int(ns) - done)
+    assert rel(X.cpu().numpy().ravel(), Z["X_final"]) < 1e-11
+
+
+@pytest.mark.parametrize("tag", ["tiny", "sym_lin"])
+def test_trajectory_small(cuda, tag):
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    Z = load_golden(f"traj_{tag}.npz")
+    N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, sym, ns = Z["params"]
+    p = Plan(int(N_fm), int(N_r), d, dt, Pr, Tau, symmetric=bool(sym))
+    X = torch.from_numpy(Z["X0"]).cuda().reshape(1, -1)
+    X = p.step(X, Ra, Ra_s, nsteps=int(ns), linear=(tag == "sym_lin"))
+    assert rel(X.cpu().numpy().ravel(), Z["X_final"]) < 1e-11
+
+
+@pytest.mark.parametrize("N_r,N_fm", [(30, 256), (24, 128), (36, 384), (48, 512), (21, 96)])
+def test_production_sizes_against_oracle(cuda, N_r, N_fm):
+    """Sizes of the batched/served workloads, checked against the oracle."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    d, dt, Pr, Tau, Ra, Ra_s = 2.0, 5e-4, 1.0, 0.01, 8000.0, 500.0
+    nr = N_r - 1
+    ops = O.Operators(N_fm, N_r, d, dt, Pr, Tau)
+    X = O.seeded_state(N_fm, nr, 1234)
+    dv = O.seeded_state(N_fm, nr, 99)
+    p = Plan(N_fm, N_r, d, dt, Pr, Tau)
+    Xt = torch.from_numpy(X).cuda().reshape(1, -1)
+    dvt = torch.from_numpy(dv).cuda().reshape(1, -1)
+    assert rel(p.nlin_fx(Xt).cpu().numpy().ravel(), O.NLIN_FX(X, ops.D, ops.R, N_fm, nr, False)) < 1e-12
+    assert rel(p.nlin_dfx(dvt, Xt).cpu().numpy().ravel(),
+               O.NLIN_DFX(dv, X, ops.D, ops.R, N_fm, nr, False)) < 1e-12
+    assert rel(p.step(Xt, Ra, Ra_s).cpu().numpy().ravel(), O.step(ops, X, Ra, Ra_s, False)) < 1e-12
+
+
+def test_batch_matches_single(cuda):
+    """Shells of one plan advance as a batch; each result equals the same shell advanced alone (bitwise:
+    no reduction crosses shells)."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    N_fm, N_r = 64, 20
+    p = Plan(N_fm, N_r, 2.0, 1e-3, 1.0, 0.01)
+    Xs = np.stack([O.seeded_state(N_fm, N_r - 1, s) for s in range(3)])
+    Ra = torch.tensor([6000.0, 8000.0, 12000.0], dtype=torch.float64, device="cuda")
+    Xb = p.step(torch.from_numpy(Xs).cuda(), Ra, 500.0, nsteps=5)
+    for i in range(3):
+        Xi = p.step(torch.from_numpy(Xs[i:i + 1]).cuda(), float(Ra[i]), 500.0, nsteps=5)
+        assert torch.equal(Xb[i:i + 1], Xi)
+
+
+def test_odd_modes_raise(cuda):
+    from spectraldoublediffusiveconvection_gb300 import Matrix_Operators as MO
+    D, R = MO.cheb_radial(8, 2.0)
+    with pytest.raises(ValueError):
+        MO.NLIN_FX(np.zeros(3 * 7 * 7), D, R, 7, 7, False)

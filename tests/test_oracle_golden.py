@@ -1,0 +1,72 @@
+"""The oracle (numpy restatement) against the golden vectors produced by the reference itself."""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel
+from oracle import sdd_oracle as O
+
+OPS_CASES = ["tiny", "tiny_sym", "m10_sym", "c1", "c1_sym"]
+
+
+def test_transforms_match_reference():
+    G = load_golden("transforms.npz")
+    for M in (8, 10, 16, 64):
+        P = 3 * M // 2
+        a, g = G[f"IDCT_in_{M}"], G[f"DCT_in_{M}"]
+        assert np.allclose(O.IDCT(a, n=P), G[f"IDCT_{M}"], rtol=0, atol=1e-13)
+        assert np.allclose(O.IDST(a, n=P), G[f"IDST_{M}"], rtol=0, atol=1e-13)
+        assert np.allclose(O.IDCT(a), G[f"IDCT_nonpad_{M}"], rtol=0, atol=1e-13)
+        assert np.allclose(O.IDST(a), G[f"IDST_nonpad_{M}"], rtol=0, atol=1e-13)
+        assert np.allclose(O.DCT(g), G[f"DCT_{M}"], rtol=0, atol=1e-13)
+        assert np.allclose(O.DST(g), G[f"DST_{M}"], rtol=0, atol=1e-13)
+        assert np.allclose(O.DCT(g, n=M), G[f"DCT_trunc_{M}"], rtol=0, atol=1e-13)
+        assert np.allclose(O.DST(g, n=M), G[f"DST_trunc_{M}"], rtol=0, atol=1e-13)
+        assert np.allclose(O.grid(P), G[f"grid_{M}"], rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("tag", OPS_CASES)
+def test_operators_match_reference(tag):
+    Z = load_golden(f"ops_{tag}.npz")
+    N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, sym = Z["params"]
+    N_r, N_fm, sym = int(N_r), int(N_fm), bool(sym)
+    nr = N_r - 1
+    N = nr * N_fm
+    ops = O.Operators(N_fm, N_r, d, dt, Pr, Tau)
+    X, dv = Z["X"], Z["dv"]
+    psi = X[:N]
+    tol = 1e-13
+    assert rel(ops.D, Z["D"]) < tol
+    assert rel(O.J_theta_RT(psi, nr, N_fm, sym), Z["J_theta_RT"]) < tol
+    assert rel(O.A2_SINE_R2(psi, N_fm, nr, ops.D, ops.R, sym), Z["A2_SINE_R2"]) < tol
+    assert rel(O.A2_SINE(psi, ops.D, ops.R, N_fm, nr, sym), Z["A2_SINE"]) < tol
+    assert rel(O.DT0_theta(psi, ops.DT0, N_fm, nr, sym), Z["DT0_theta"]) < tol
+    assert rel(O.NLIN_FX(X, ops.D, ops.R, N_fm, nr, sym), Z["NLIN_FX"]) < tol
+    assert rel(O.NLIN_DFX(dv, X, ops.D, ops.R, N_fm, nr, sym), Z["NLIN_DFX"]) < tol
+    g = Z["A4_g"]
+    assert rel(O.A4_BSub_TSTEP_V2(g, ops.Linv_A4, ops.D2_A4, ops.IR4_A4, ops.IR2_A4, N_fm, nr, Pr * dt, sym),
+               Z["A4_BSub"]) < tol
+    assert rel(O.NAB2_BSub_TSTEP_V2(g, ops.Linv_T, N_fm, nr, dt, sym), Z["NAB2_T"]) < tol
+    assert rel(O.NAB2_BSub_TSTEP_V2(g, ops.Linv_S, N_fm, nr, Tau * dt, sym), Z["NAB2_S"]) < tol
+    assert rel(O.step(ops, X, Ra, Ra_s, sym), Z["step1"]) < 1e-12
+    assert rel(O.step(ops, X, Ra, Ra_s, sym, linear=True), Z["step1_linear"]) < 1e-12
+    ops1 = O.Operators(N_fm, N_r, d, 1.0, Pr, Tau)
+    assert rel(O.PFX(ops1, X, Ra, Ra_s, sym), Z["PFX"]) < 1e-12
+    assert rel(O.PDFX(ops1, dv, X, Ra, Ra_s, sym), Z["PDFX"]) < 1e-12
+    assert abs(O.Kinetic_Energy(X, ops.R, ops.D, N_fm, nr, sym) - Z["KE"]) <= 1e-12 * abs(Z["KE"])
+    assert abs(O.Nusselt(X[N:2 * N], d, ops.R, ops.D, N_fm, nr) - Z["NuT"]) <= 1e-12 * abs(Z["NuT"])
+    if "Linv_A4" in Z:
+        assert rel(ops.Linv_A4, Z["Linv_A4"]) < tol
+        assert rel(ops.Linv_T, Z["Linv_T"]) < tol
+        assert rel(ops.Linv_S, Z["Linv_S"]) < tol
+
+
+@pytest.mark.parametrize("tag", ["tiny", "sym_lin", "c1"])
+def test_trajectory_matches_reference(tag):
+    Z = load_golden(f"traj_{tag}.npz")
+    N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, sym, ns = Z["params"]
+    N_r, N_fm, sym, ns = int(N_r), int(N_fm), bool(sym), int(ns)
+    ops = O.Operators(N_fm, N_r, d, dt, Pr, Tau)
+    XN, snaps = O.time_step(ops, Z["X0"], Ra, Ra_s, sym, ns, linear=(tag == "sym_lin"), every=ns // 10)
+    assert rel(XN, Z["X_final"]) < 1e-12
+    for s, r in zip(snaps, Z["X_DATA"]):
+        assert rel(s, r) < 1e-12
