@@ -1,0 +1,397 @@
+#!/usr/bin/env python
+"""Benchmark: IMEX time-steps/s of one production-size shell on the GB300, plus the Newton-GMRES
+steady-state solve that follows it.
+
+Workload ("shell N_r=30 N_theta=256, plain FP64"): one axisymmetric shell, N_r=30 Chebyshev points
+(nr=29 interior), N_theta=256 modes, d=2, Pr=1, Tau=0.01, Ra_T=8000, Ra_S=500, dt=5e-4, seeded Gaussian
+coefficients of amplitude 1e-3*exp(-k/8)*exp(-n/4) (synthetic: the reference ships no data).
+One bench step = 100 IMEX time steps (Main.py:255-283) of the shell; the metric counts time steps.
+After the timed time-stepping the state is handed to Newton-GMRES(restart 50) with the dt=1 operators
+until |F|_2 <= 1e-10, reported as "newton".
+
+Arms:
+  default            libsdd_gb300 (hand-written sm_103a kernels through the C ABI)
+  --impl reference   the reference's algorithm on the host cores (the numpy oracle restating it; the
+                     reference itself is Python that needs numba/h5py/matplotlib and cannot run on the
+                     GPU machine), a bounded sample of the same workload.
+
+Run:  python bench.py [--gpus N --steps K --warmup W]   (N>1: launched by torch.distributed.run, one
+independent replica shell per rank, weak scaling, no collective on the data path).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(workload="shell N_r=30 N_theta=256 plain FP64 IMEX time-stepping + Newton-GMRES(50)",
+                N_r=30, N_theta=256, d=2.0, Pr=1.0, Tau=0.01, Ra_T=8000.0, Ra_S=500.0, dt=5e-4,
+                steps_per_bench_step=100, seed=1234)
+METRIC = "time-steps/s"
+UNIT = "time-steps/s"
+L2_FLUSH_BYTES = 512 << 20
+
+
+def algorithmic(M, nr):
+    """Per IMEX step of one shell: FP64 flops and bytes of the reference's algorithm:
+    flops = 21 M nr^2 + 12 nr 2.5 P log2 P + 11 nr P + 40 nr M, bytes = 48 M nr + 24 M nr^2.
+    Chain kernel alone: flops 8 M nr^2, bytes 24 M nr^2 + 48 M nr."""
+    import math
+    P = 3 * M // 2
+    step_flops = 21 * M * nr ** 2 + 12 * nr * 2.5 * P * math.log2(P) + 11 * nr * P + 40 * nr * M
+    step_bytes = 48 * M * nr + 24 * M * nr ** 2
+    chain_flops = 8 * M * nr ** 2
+    chain_bytes = 24 * M * nr ** 2 + 48 * M * nr
+    return step_flops, step_bytes, chain_flops, chain_bytes
+
+
+# ------------------------------------------------------------------------------------------------
+# clocks
+# ------------------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples every 200 ms while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------------
+# CPU baseline (the oracle), run in a child process so its BLAS/OpenMP threads are pinned at start-up
+# ------------------------------------------------------------------------------------------------
+def cpu_worker(seconds, threads, steps_per_sample):
+    """Times IMEX steps of the workload with the oracle; prints one JSON line."""
+    import numpy as np
+    from oracle import sdd_oracle as O
+    w = WORKLOAD
+    M, N_r = w["N_theta"], w["N_r"]
+    ops = O.Operators(M, N_r, w["d"], w["dt"], w["Pr"], w["Tau"])
+    X = O.seeded_state(M, N_r - 1, w["seed"])
+    X = O.step(ops, X, w["Ra_T"], w["Ra_S"], False)    # warm-up
+    n = 0
+    samples = []
+    t_start = time.perf_counter()
+    while True:
+        t0 = time.perf_counter()
+        for _ in range(steps_per_sample):
+            X = O.step(ops, X, w["Ra_T"], w["Ra_S"], False)
+        samples.append(time.perf_counter() - t0)
+        n += steps_per_sample
+        if time.perf_counter() - t_start >= seconds:
+            break
+    total = sum(samples)
+    print(json.dumps({"steps": n, "seconds": total, "samples": samples, "threads": threads,
+                      "finite": bool(np.isfinite(X).all())}))
+
+
+def run_cpu_baseline(seconds=12.0, threads=1, steps_per_sample=5):
+    env = dict(os.environ)
+    for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS", "NUMEXPR_NUM_THREADS"):
+        env[v] = str(threads)
+    env["CUDA_VISIBLE_DEVICES"] = ""
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--cpu-worker", str(seconds), str(threads),
+           str(steps_per_sample)]
+    out = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=600)
+    if out.returncode != 0:
+        raise RuntimeError("cpu baseline failed: " + out.stderr[-2000:])
+    return json.loads(out.stdout.strip().splitlines()[-1])
+
+
+# ------------------------------------------------------------------------------------------------
+# distributed helpers
+# ------------------------------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, ws, device):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------------------------------------
+# reference arm
+# ------------------------------------------------------------------------------------------------
+def bench_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    # a bounded sample per bench step: 5 IMEX steps with all host threads available to BLAS
+    per = 5
+    seconds = max(5.0, min(120.0, 0.02 * per * (args.steps + args.warmup)))
+    r = run_cpu_baseline(seconds=seconds, threads=threads, steps_per_sample=per)
+    samples = r["samples"]
+    timed = samples[min(len(samples) - 1, args.warmup):] if len(samples) > args.warmup else samples
+    tsec = sum(timed)
+    nsteps = per * len(timed)
+    value = nsteps / tsec
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": len(timed), "warmup": min(args.warmup, len(samples) - len(timed)),
+            "ms_per_step": 1e3 * tsec / len(timed), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian coefficients)",
+            "config": dict(WORKLOAD, steps_per_bench_step=per, l2="n/a (host)"),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{nsteps} IMEX steps of the workload ({per} per bench step) with the "
+                                       "numpy oracle restating the reference (reference un-JIT'd: numba "
+                                       "unavailable)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------------------------
+# GB300 arm
+# ------------------------------------------------------------------------------------------------
+def bench_gb300(args):
+    import numpy as np
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    device = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(device)
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from oracle import sdd_oracle as O          # seeded input generator only
+    from spectraldoublediffusiveconvection_gb300 import _lib
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+
+    w = WORKLOAD
+    M, N_r, nr = w["N_theta"], w["N_r"], w["N_r"] - 1
+    chunk = w["steps_per_bench_step"]
+    plan = Plan(M, N_r, w["d"], w["dt"], w["Pr"], w["Tau"], device=device)
+    X0 = O.seeded_state(M, nr, w["seed"] + rank)
+    Ra = torch.full((1,), w["Ra_T"], dtype=torch.float64, device=device)
+    Ras = torch.full((1,), w["Ra_S"], dtype=torch.float64, device=device)
+    Xa = torch.from_numpy(X0).to(device).reshape(1, -1)
+    Xb = torch.empty_like(Xa)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+    stream = torch.cuda.current_stream(device)
+
+    # warm-up
+    for _ in range(args.warmup):
+        plan.step(Xa, Ra, Ras, nsteps=chunk, out=Xb)
+        Xa, Xb = Xb, Xa
+    torch.cuda.synchronize()
+
+    # ---- timed region (device-resident): K bench steps, L2 flushed between them (outside the events) --
+    clocks = ClockSampler(device.index or 0)
+    clocks.start()
+    barrier(ws)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.zero_()
+        evs[i][0].record(stream)
+        plan.step(Xa, Ra, Ras, nsteps=chunk, out=Xb)
+        evs[i][1].record(stream)
+        Xa, Xb = Xb, Xa
+    torch.cuda.synchronize()
+    barrier(ws)
+    ms_total = sum(a.elapsed_time(b) for a, b in evs)
+    ck = clocks.stop()
+    ms_total = max_over_ranks(ms_total, ws, device)
+    X_after = Xa.clone()
+    time_steps = args.steps * chunk * ws
+    value = time_steps / (ms_total * 1e-3)
+
+    # ---- e2e through the public API with host buffers (pinned), copies inside the timed region ----
+    h_in = torch.from_numpy(X0.copy()).reshape(1, -1).pin_memory()
+    h_out = torch.empty_like(h_in).pin_memory()
+    d_in = torch.empty_like(Xa)
+    d_out = torch.empty_like(Xa)
+    for _ in range(max(1, args.warmup)):
+        d_in.copy_(h_in, non_blocking=True)
+        plan.step(d_in, Ra, Ras, nsteps=chunk, out=d_out)
+        h_out.copy_(d_out, non_blocking=True)
+        torch.cuda.synchronize()
+    barrier(ws)
+    e2e_s = 0.0
+    for i in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d_in.copy_(h_in, non_blocking=True)
+        plan.step(d_in, Ra, Ras, nsteps=chunk, out=d_out)
+        h_out.copy_(d_out, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_s += time.perf_counter() - t0
+        h_in, h_out = h_out, h_in
+    barrier(ws)
+    e2e_s = max_over_ranks(e2e_s, ws, device)
+    e2e_value = time_steps / e2e_s
+    nbytes = X0.size * 8
+
+    # ---- per-kernel durations (CUDA events between the three kernels of each step) -------------------
+    nprof = min(200, args.steps * chunk)
+    ms3, _ = plan.step_profile(X_after, Ra, Ras, nprof)
+    ms3 = [m / nprof for m in ms3]
+    names = ["k_fx_rows", "k_rhs", "k_chain"]
+    dom = int(np.argmax(ms3))
+    step_flops, step_bytes, chain_flops, chain_bytes = algorithmic(M, nr)
+    fp64 = __import__("ctypes").c_double(0.0)
+    _lib.check(_lib.lib().sdd_measure_fp64_peak(__import__("ctypes").byref(fp64),
+                                                 __import__("ctypes").c_void_p(stream.cuda_stream)),
+               "sdd_measure_fp64_peak")
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    hbm_src = "of measured" if "hbm_gbs" in peaks else "of fallback"
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        traffic = tr.get(names[dom])
+    except (OSError, ValueError):
+        pass
+    # dominant-kernel algorithmic work per launch (one launch of each kernel per IMEX step of the shell)
+    import math
+    P = 3 * M // 2
+    kflops = {"k_fx_rows": 8 * M * nr ** 2 + 12 * nr * 2.5 * P * math.log2(P) + 11 * nr * P,
+              "k_rhs": 4 * M * nr ** 2 + 40 * nr * M, "k_chain": chain_flops}[names[dom]]
+    kbytes = {"k_fx_rows": 56 * M * nr, "k_rhs": 80 * M * nr, "k_chain": chain_bytes}[names[dom]]
+    dom_s = ms3[dom] * 1e-3
+    achieved_gbs = kbytes / dom_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved_gbs / hbm_peak, "traffic": traffic, "kernel": names[dom],
+                "peak_source": hbm_src, "algorithmic_bytes_per_launch": kbytes,
+                "fp64": {"achieved_gflops": kflops / dom_s / 1e9, "peak_gflops": fp64.value,
+                         "frac": kflops / dom_s / 1e9 / fp64.value,
+                         "peak_source": "measured live (sdd_measure_fp64_peak FMA loop)",
+                         "algorithmic_flops_per_launch": kflops},
+                "kernel_ms_per_step": dict(zip(names, ms3)),
+                "step_fp64_gflops": step_flops / (ms_total * 1e-3 / (args.steps * chunk)) / 1e9}
+
+    # ---- Newton-GMRES(50) from the state after the time stepping --------------------------------------
+    newton = None
+    if not args.no_newton:
+        plan1 = Plan(M, N_r, w["d"], 1.0, w["Pr"], w["Tau"], device=device)
+        Xn = X_after.clone()
+        plan1.newton(Xn.clone(), Ra, Ras, tol=1e-10, restart=50, max_newton=2)   # warm-up (allocations)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = plan1.newton(Xn, Ra, Ras, tol=1e-10, restart=50, gmres_rtol=1e-4, max_newton=20)[0]
+        torch.cuda.synchronize()
+        tn = time.perf_counter() - t0
+        newton = {"solves_per_s": 1.0 / tn, "seconds": tn, "newton_iters": res["newton_iters"],
+                  "matvecs": res["matvecs"], "residual0": res["residual0"], "residual": res["residual"],
+                  "converged": res["converged"], "tol": 1e-10, "restart": 50}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        r = run_cpu_baseline(seconds=args.cpu_seconds, threads=1, steps_per_sample=5)
+        cpu = {"value": r["steps"] / r["seconds"], "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{r['steps']} IMEX steps of the same shell with the numpy oracle restating the "
+                         "reference, 1 thread (reference un-JIT'd: numba unavailable)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded Gaussian coefficients, amplitude 1e-3 exp(-k/8) exp(-n/4))",
+                "config": dict(WORKLOAD, parallelism=f"replicas x{ws}" if ws > 1 else "single shell",
+                               l2="flushed between timed bench steps (512 MiB write)"),
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+                        "d2h_bytes_per_step": nbytes,
+                        "api": "Plan.step on a pinned host state copied in/out every bench step"},
+                "gpu_launches": args.steps * chunk * 3,
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": ck, "newton": newton}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "--cpu-worker":
+        cpu_worker(float(sys.argv[2]), int(sys.argv[3]), int(sys.argv[4]))
+        return 0
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-newton", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return bench_reference(args)
+    return bench_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

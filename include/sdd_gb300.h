@@ -123,6 +123,45 @@ int sdd_pfx(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, con
 int sdd_pdfx(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, const double* dv,
              const double* X, const double* base_cache, double* out, void* stream);
 
+/* ---- matrix-free Newton-GMRES steady states (Main.py:430-554 _Newton) -------------------------- */
+/* The reference solves DF(X) dv = F(X) with scipy lgmres and stops on the relative step
+ * |dv|/|X| < tol (Main.py:523-536), which cannot be met when the solution is X = 0.  Here the stop is
+ * the absolute FP64 residual |F(X)|_2 <= tol; the inner solve is restarted GMRES(restart) with CGS2
+ * orthogonalisation and inner tolerance gmres_rtol*|F| (the reference's atol = tol_gmres*|F|). */
+typedef struct sdd_newton_opts {
+  double tol;              /* absolute |F(X)|_2 target                                              */
+  double gmres_rtol;       /* inner tolerance relative to |F(X)|                                     */
+  int32_t restart;         /* GMRES restart length (<= 64)                                          */
+  int32_t max_restarts;    /* GMRES cycles per Newton iteration                                     */
+  int32_t max_newton;      /* Newton iteration cap                                                  */
+  int32_t mixed_matvec;    /* 1: FP32 nonlinear term inside the Jacobian products (plan must be mixed) */
+} sdd_newton_opts;
+
+typedef struct sdd_newton_result {
+  double residual0;        /* |F(X0)|_2                                                             */
+  double residual;         /* |F(X)|_2 at exit (FP64)                                               */
+  int32_t newton_iters;    /* Newton updates applied                                                */
+  int32_t matvecs;         /* Jacobian-vector products (batch-wide)                                 */
+  int32_t converged;       /* residual <= tol                                                       */
+  int32_t pad;
+} sdd_newton_result;
+
+/* In place: X (batch x 3*N_fm*nr, device) is replaced by the Newton iterate.  results: host array of
+ * batch entries.  Uses the plan's dt (1 for Newton, Main.py:430).  Synchronises the stream (it reads
+ * residuals back to decide convergence).  Returns SDD_ERR_NOT_CONVERGED if a shell misses tol. */
+int sdd_newton_gmres(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, double* X,
+                     const sdd_newton_opts* opts, sdd_newton_result* results, void* stream);
+
+/* ---- instrumentation (no counterpart in the reference) ---------------------------------------- */
+/* Runs nsteps steps like sdd_step with CUDA events between the three kernels of each step and adds the
+ * elapsed milliseconds to ms[0] (nonlinear-term row kernel), ms[1] (rhs kernel), ms[2] (chain kernel).
+ * Synchronises the stream. */
+int sdd_step_profile(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, const double* X_in,
+                     double* X_out, int nsteps, double* ms, void* stream);
+/* Measured FP64 FMA throughput of the current device in GFLOP/s (a register-resident FMA loop over
+ * all SMs, a few milliseconds).  The roofline denominator of the FP64-bound kernels. */
+int sdd_measure_fp64_peak(double* gflops, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

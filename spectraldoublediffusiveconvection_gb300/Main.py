@@ -1,0 +1,187 @@
+"""Drop-in for the drivers of the reference's ``Main.py``.
+
+``Build_Matrix_Operators``, ``_Time_Step`` and ``_Newton`` keep the reference's signatures
+(Main.py:179, 228, 430).  Time integration and Newton-GMRES run on the GPU through a cached device
+plan: the state stays resident for the whole call and comes back to the host once at the end (and at
+the save points).
+
+Differences from the reference, by design:
+* ``_Newton`` stops on the absolute FP64 residual |F(X)|_2 <= tol_newton.  The reference's relative
+  step test |dv|/|X| < tol (Main.py:536) cannot be met when the steady state is X = 0, where the seeded
+  states of the benchmark converge.  GMRES restarts every min(Krylov_Space_Size, 50) vectors.
+* ``_Time_Step`` evaluates Norm/KE/Nu at the save points (every N_iters/10 steps) rather than after every
+  step, and writes the HDF5 file only when h5py is importable.
+"""
+import os
+import time
+import warnings
+
+import numpy as np
+
+from . import Matrix_Operators as MO
+from . import operators as _ops
+from .Transforms import IDCT, IDST, grid
+from .plan import get_plan
+
+
+def uniquify(path):
+    """Main.py:12-20: next free file name of the form name_<n>.ext."""
+    filename, extension = os.path.splitext(path)
+    counter = int(filename.split('_')[1])
+    while os.path.exists(path):
+        path = filename.split('_')[0] + "_" + str(counter) + extension
+        counter += 1
+    return path
+
+
+def Base_State_Coeffs(d):
+    """Main.py:23-38."""
+    return _ops.base_state_coeffs(d)
+
+
+def Nusselt(T_hat, d, R, D, N_fm, nr, check=True):
+    """Main.py:41-68: convective Nusselt number from the even cosine modes of T (or S)."""
+    T_hat = np.asarray(T_hat.cpu() if hasattr(T_hat, "cpu") else T_hat, dtype=np.float64)
+    A_T = _ops.base_state_coeffs(d)[0]
+    TT = np.zeros((N_fm // 2 + N_fm % 2, len(R)))
+    ks = np.arange(0, N_fm, 2)
+    TT[:, 1:-1] = T_hat.reshape(N_fm, nr)[ks]
+    NuM1 = ((TT @ D.T) / (1.0 - ks[:, None] ** 2)).sum(axis=0)
+    NuM1 = ((R ** 2) / A_T) * NuM1
+    error = abs(NuM1[-1] - NuM1[0]) / abs(NuM1[-1])
+    if check and error > 1e-03:
+        raise ValueError("|Nu(R_1) - Nu(R_2)|/|Nu(R_1)| = ", error, " > .1%, Increase Nr \n")
+    return NuM1[0]
+
+
+def Kinetic_Energy(X_hat, R, D, N_fm, nr, symmetric):
+    """Main.py:71-134: volume-averaged kinetic energy; the transforms run on the GPU."""
+    X_hat = np.asarray(X_hat.cpu() if hasattr(X_hat, "cpu") else X_hat, dtype=np.float64)
+    N = N_fm * nr
+    Dr = D[1:-1, 1:-1]
+    JPSI = np.asarray(MO.J_theta_RT(X_hat[0:N], nr, N_fm, symmetric)).reshape(N_fm, nr)
+    PSI = X_hat[0:N].reshape(N_fm, nr)
+    Dpsi_h = (PSI @ Dr.T).T
+    Jpsi_h = (JPSI / R[1:-1][None, :]).T
+    Dpsi_s = np.zeros_like(Dpsi_h)
+    Dpsi_s[:, 1:] = Dpsi_h[:, :-1]
+    th = grid(3 * N_fm)
+    Jpsi = IDCT(Jpsi_h, n=3 * N_fm)
+    Dpsi = IDST(Dpsi_s, n=3 * N_fm)
+    KE_rt = Jpsi ** 2 + Dpsi ** 2
+    KE_t = np.trapezoid(KE_rt, x=R[1:-1], axis=0)
+    KE = np.trapezoid(KE_t * np.sin(th), x=th, axis=-1)
+    V = (2.0 / 3.0) * (R[-1] ** 3 - R[0] ** 3)
+    return (0.5 / V) * KE
+
+
+def Eq_SYM(X1, R):
+    """Main.py:137-176: mask keeping psi odd slots and T/S even slots."""
+    nr = len(R[1:-1])
+    N_fm = int(X1.shape[0] / (3 * nr))
+    m = np.ones((3, N_fm, nr))
+    m[0, 0::2] = 0.0
+    m[1:, 1::2] = 0.0
+    return m.reshape(-1)
+
+
+def Build_Matrix_Operators(N_fm, N_r, d, dt, Pr, Tau):
+    """Main.py:179-225: the reference's operator tuple (host FP64; the device copies live in the plan)."""
+    D, R = _ops.cheb_radial(N_r, d)
+    Rsq = MO.R2(R, N_fm)
+    gr_K = MO.kGR_RT(R, N_fm, d)
+    A_T = _ops.base_state_coeffs(d)[0]
+    DT0 = A_T / (R[1:-1] ** 2)
+    nr = len(R[1:-1])
+    L_inv_A4 = MO.A4_TSTEP_MATS(Pr * dt, N_fm, nr, D, R)
+    L_inv_NAB2_T = MO.NAB2_TSTEP_MATS(dt, N_fm, nr, D, R)
+    L_inv_NAB2_S = MO.NAB2_TSTEP_MATS(Tau * dt, N_fm, nr, D, R)
+    D2, _, IR2, IR4 = _ops.a4_pieces(D, R)
+    args_A4 = (np.ascontiguousarray(D2), np.ascontiguousarray(IR4), np.ascontiguousarray(IR2), N_fm, nr)
+    args_FXS = (np.ascontiguousarray(D), R, N_fm, nr)
+    return D, R, Rsq, DT0, gr_K, L_inv_A4, L_inv_NAB2_T, L_inv_NAB2_S, args_A4, args_FXS
+
+
+def _to_state(X, plan):
+    import torch
+    if isinstance(X, torch.Tensor):
+        return X.to(device=plan.device, dtype=torch.float64).reshape(1, -1).contiguous(), False
+    return torch.from_numpy(np.ascontiguousarray(X, dtype=np.float64)).to(plan.device).reshape(1, -1), True
+
+
+def _diagnostics(Xh, R, D, N_fm, nr, d, symmetric):
+    N = N_fm * nr
+    return (np.linalg.norm(Xh, 2), Kinetic_Energy(Xh, R, D, N_fm, nr, symmetric),
+            Nusselt(Xh[N:2 * N], d, R, D, N_fm, nr, check=False),
+            Nusselt(Xh[2 * N:3 * N], d, R, D, N_fm, nr, check=False))
+
+
+def _Time_Step(X, Ra, Ra_s, Tau, Pr, d, N_fm, N_r, symmetric, save_filename='TimeStep_0.h5', start_time=0,
+               Total_time=1, dt=1e-04, linear=False, Verbose=False):
+    """Main.py:228-329: int(Total_time/dt) IMEX ("CNAB1") steps on the GPU; returns X_new."""
+    plan = get_plan(N_fm, N_r, d, dt, Pr, Tau, symmetric)
+    Xd, was_np = _to_state(X, plan)
+    N_iters = int(Total_time / dt)
+    N_save = max(1, int(N_iters / 10))
+    D, R = plan.arrays["D"], plan.arrays["R"]
+    nr = N_r - 1
+    rec = dict(X_DATA=[], Norm=[], KE=[], Nu_T=[], Nu_S=[], Time=[])
+    t0 = time.time()
+    done = 0
+    while done < N_iters:
+        # the reference saves after iterations 0, N_save, 2 N_save, ...  (Main.py:301)
+        nxt = 1 if done == 0 else min(N_iters, done + N_save)
+        Xd = plan.step(Xd, Ra, Ra_s, nsteps=nxt - done, linear=linear)
+        done = nxt
+        if (done - 1) % N_save == 0:
+            Xh = Xd.cpu().numpy().ravel()
+            nrm, ke, nut, nus = _diagnostics(Xh, R, D, N_fm, nr, d, symmetric)
+            rec["X_DATA"].append(Xh)
+            rec["Norm"].append(nrm)
+            rec["KE"].append(ke)
+            rec["Nu_T"].append(nut)
+            rec["Nu_S"].append(nus)
+            rec["Time"].append(start_time + dt * (done - 1))
+            if Verbose:
+                print("Iteration =%i, Time = %e, Energy = %e, NuT = %e \n " % (done - 1, rec["Time"][-1], ke, nut))
+    if save_filename:
+        _write_h5(save_filename, rec, dict(Ra=Ra, Ra_s=Ra_s, Tau=Tau, Pr=Pr, d=d, N_r=N_r, N_fm=N_fm, dt=dt,
+                                           start_time=start_time, symmetric=symmetric))
+    if Verbose:
+        print("Avg time = %e \n" % ((time.time() - t0) / max(1, N_iters)))
+    return Xd.cpu().numpy().ravel() if was_np else Xd.reshape(-1)
+
+
+def _write_h5(filename, rec, params):
+    try:
+        import h5py
+    except ImportError:
+        warnings.warn("h5py is not installed: %s was not written" % filename)
+        return
+    with h5py.File(filename, 'w') as f:
+        f.create_group("Checkpoints")['X_DATA'] = rec["X_DATA"]
+        g = f.create_group("Scalar_Data")
+        for k in ("Norm", "KE", "Nu_T", "Nu_S", "Time"):
+            g[k] = rec[k]
+        p = f.create_group("Parameters")
+        for k, v in params.items():
+            p[k] = v
+
+
+def _Newton(X, Ra, Ra_s, Tau, Pr, d, N_fm, N_r, symmetric, dt=1, tol_newton=1e-08, tol_gmres=1e-04,
+            Krylov_Space_Size=300, max_newton=20):
+    """Main.py:430-554: steady state of Phi_dt(X) - X by Newton-GMRES on the GPU.
+
+    Returns (X, Norm, KE, NuT, NuS, True) on convergence (|F(X)|_2 <= tol_newton) and
+    (None, None, None, None, None, False) otherwise, as the reference does (Main.py:541-544)."""
+    plan = get_plan(N_fm, N_r, d, dt, Pr, Tau, symmetric)
+    Xd, was_np = _to_state(X, plan)
+    Xd = Xd.clone()
+    res = plan.newton(Xd, Ra, Ra_s, tol=tol_newton, restart=min(int(Krylov_Space_Size), 50),
+                      gmres_rtol=tol_gmres, max_newton=max_newton)[0]
+    if not res["converged"]:
+        print('Newton iteration could not converge')
+        return None, None, None, None, None, False
+    Xh = Xd.cpu().numpy().ravel()
+    Norm, KE, NuT, NuS = _diagnostics(Xh, plan.arrays["R"], plan.arrays["D"], N_fm, N_r - 1, d, symmetric)
+    return (Xh if was_np else Xd.reshape(-1)), Norm, KE, NuT, NuS, True

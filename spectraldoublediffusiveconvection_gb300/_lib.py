@@ -36,6 +36,20 @@ class PlanDesc(ctypes.Structure):
     ]
 
 
+class NewtonOpts(ctypes.Structure):
+    """Mirror of ``sdd_newton_opts``."""
+    _fields_ = [("tol", ctypes.c_double), ("gmres_rtol", ctypes.c_double), ("restart", ctypes.c_int32),
+                ("max_restarts", ctypes.c_int32), ("max_newton", ctypes.c_int32),
+                ("mixed_matvec", ctypes.c_int32)]
+
+
+class NewtonResult(ctypes.Structure):
+    """Mirror of ``sdd_newton_result``."""
+    _fields_ = [("residual0", ctypes.c_double), ("residual", ctypes.c_double),
+                ("newton_iters", ctypes.c_int32), ("matvecs", ctypes.c_int32),
+                ("converged", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
 # (name, restype, argtypes) of every exported symbol; the CPU test checks the header declares these.
 _VP = ctypes.c_void_p
 _I = ctypes.c_int
@@ -57,6 +71,10 @@ SIGNATURES = [
     ("sdd_step", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, _I, _VP]),
     ("sdd_pfx", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP]),
     ("sdd_pdfx", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    ("sdd_newton_gmres", _I, [_VP, _I, _VP, _VP, _VP, ctypes.POINTER(NewtonOpts), ctypes.POINTER(NewtonResult),
+                              _VP]),
+    ("sdd_step_profile", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, ctypes.POINTER(ctypes.c_double), _VP]),
+    ("sdd_measure_fp64_peak", _I, [ctypes.POINTER(ctypes.c_double), _VP]),
 ]
 
 _lib = None

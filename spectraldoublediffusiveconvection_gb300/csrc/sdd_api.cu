@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "sdd_internal.cuh"
+#include "sdd_krylov.cuh"
 
 namespace sdd {
 cudaError_t launch_fx_finish(int M, int nr, const double* Dr, const double* out4, size_t out_stride,
@@ -100,6 +101,14 @@ struct sdd_plan {
   double* rhs;      // [B][3][M][nr]
   double* xtmp;     // [B][3][M][nr]
   void* base_tmp;   // [B][nr][9][P] (T precision), for DFX without a caller cache
+  // Newton-GMRES workspace
+  int nw_B, nw_m;
+  double *nw_V, *nw_F, *nw_x, *nw_w, *nw_r, *nw_part, *nw_nrm2, *nw_base64;
+  float* nw_base32;
+  double *nw_small;   // H, hcol, h2, cs, sn, g, y, beta, inv, resid, target
+  int* nw_ismall;     // active, solve, kb, newton mask
+  double* h_dbl;      // pinned host: nrm2 / resid
+  int* h_int;         // pinned host: active flags
 };
 
 extern "C" {
@@ -167,6 +176,12 @@ static void free_plan(sdd_plan* p) {
   for (double* x : d) cudaFree(x);
   cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232);
   cudaFree(p->base_tmp);
+  double* nw[] = {p->nw_V, p->nw_F, p->nw_x, p->nw_w, p->nw_r, p->nw_part, p->nw_nrm2, p->nw_base64, p->nw_small};
+  for (double* x : nw) cudaFree(x);
+  cudaFree(p->nw_base32);
+  cudaFree(p->nw_ismall);
+  cudaFreeHost(p->h_dbl);
+  cudaFreeHost(p->h_int);
   delete p;
 }
 
@@ -425,3 +440,247 @@ int sdd_pdfx(sdd_plan* p, int batch, const double* Ra, const double* Ras, const 
 }
 
 }  // extern "C"
+
+// ---- Newton-GMRES --------------------------------------------------------------------------------
+static int newton_reserve(sdd_plan* p, int B, int m) {
+  if (p->nw_B >= B && p->nw_m >= m) return SDD_OK;
+  double* nw[] = {p->nw_V, p->nw_F, p->nw_x, p->nw_w, p->nw_r, p->nw_part, p->nw_nrm2, p->nw_base64, p->nw_small};
+  for (double* x : nw) cudaFree(x);
+  cudaFree(p->nw_base32); cudaFree(p->nw_ismall); cudaFreeHost(p->h_dbl); cudaFreeHost(p->h_int);
+  p->nw_V = p->nw_F = p->nw_x = p->nw_w = p->nw_r = p->nw_part = p->nw_nrm2 = p->nw_base64 = p->nw_small = nullptr;
+  p->nw_base32 = nullptr; p->nw_ismall = nullptr; p->h_dbl = nullptr; p->h_int = nullptr;
+  p->nw_B = p->nw_m = 0;
+  const size_t n = shell_elems(p), be = sdd_plan_base_cache_elems(p);
+  const int nchunk = (int)((n + kDotChunk - 1) / kDotChunk);
+  SDD_CUDA(cudaMalloc(&p->nw_V, (size_t)(m + 1) * B * n * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->nw_F, (size_t)B * n * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->nw_x, (size_t)B * n * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->nw_w, (size_t)B * n * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->nw_r, (size_t)B * n * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->nw_part, (size_t)B * (m + 1) * nchunk * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->nw_nrm2, (size_t)B * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->nw_base64, (size_t)B * be * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->nw_base32, (size_t)B * be * sizeof(float)));
+  const size_t small = (size_t)B * ((size_t)(m + 1) * m + 3 * (m + 1) + 3 * m + 4);
+  SDD_CUDA(cudaMalloc(&p->nw_small, small * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->nw_ismall, (size_t)4 * B * sizeof(int)));
+  SDD_CUDA(cudaMallocHost(&p->h_dbl, (size_t)B * sizeof(double)));
+  SDD_CUDA(cudaMallocHost(&p->h_int, (size_t)B * sizeof(int)));
+  p->nw_B = B;
+  p->nw_m = m;
+  return SDD_OK;
+}
+
+static GmresState gmres_state(sdd_plan* p, int B, int m) {
+  GmresState s;
+  s.m = m;
+  double* q = p->nw_small;
+  s.H = q; q += (size_t)B * (m + 1) * m;
+  s.hcol = q; q += (size_t)B * (m + 1);
+  s.h2 = q; q += (size_t)B * (m + 1);
+  s.g = q; q += (size_t)B * (m + 1);
+  s.cs = q; q += (size_t)B * m;
+  s.sn = q; q += (size_t)B * m;
+  s.y = q; q += (size_t)B * m;
+  s.beta = q; q += B;
+  s.inv = q; q += B;
+  s.resid = q; q += B;
+  s.target = q; q += B;
+  int* iq = p->nw_ismall;
+  s.active = iq; iq += B;
+  s.solve = iq; iq += B;
+  s.kb = iq; iq += B;
+  return s;
+}
+
+extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const double* Ras, double* X,
+                                const sdd_newton_opts* o, sdd_newton_result* res, void* stream) {
+  int st = check_plan(p, B);
+  if (st) return st;
+  if (!Ra || !Ras || !X || !o || !res) return SDD_ERR_ARG;
+  const int m = o->restart;
+  if (m < 1 || m > 64 || o->max_newton < 0 || o->max_restarts < 1 || !(o->tol >= 0.0)) return SDD_ERR_ARG;
+  if (o->mixed_matvec && p->prec != SDD_PREC_MIXED) return SDD_ERR_ARG;
+  st = newton_reserve(p, B, m);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = (int)shell_elems(p);
+  const size_t vs = (size_t)B * n;            // stride between Krylov vectors
+  GmresState G = gmres_state(p, B, m);
+  int* newton_mask = p->nw_ismall + 3 * B;
+  const int mv_prec = o->mixed_matvec ? SDD_PREC_MIXED : SDD_PREC_FP64;
+  void* base_mv = o->mixed_matvec ? (void*)p->nw_base32 : (void*)p->nw_base64;
+  std::vector<double> resF(B, 0.0), target(B, 0.0);
+  std::vector<int> nmask(B, 0), iters(B, 0);
+  int matvecs = 0;
+
+  auto norms = [&](const double* v) -> int {   // ||v_b||^2 -> p->h_dbl
+    SDD_CUDA(krylov_dots(v, 0, v, n, 1, B, p->nw_part, p->nw_nrm2, 1, 0, s));
+    SDD_CUDA(cudaMemcpyAsync(p->h_dbl, p->nw_nrm2, B * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SDD_CUDA(cudaStreamSynchronize(s));
+    return SDD_OK;
+  };
+  auto jac = [&](const double* v, double* out) -> int {   // out = PDFX(v) about the cached base
+    ++matvecs;
+    return apply_step(p, B, Ra, Ras, v, out, v, 1, base_mv, mv_prec, s);
+  };
+
+  for (int it = 0;; ++it) {
+    st = apply_step(p, B, Ra, Ras, X, p->nw_F, X, 0, p->nw_base64, SDD_PREC_FP64, s);   // F = PFX(X)
+    if (st) return st;
+    if ((st = norms(p->nw_F))) return st;
+    bool any = false;
+    for (int b = 0; b < B; ++b) {
+      resF[b] = std::sqrt(p->h_dbl[b]);
+      if (it == 0) res[b].residual0 = resF[b];
+      nmask[b] = (resF[b] > o->tol) ? 1 : 0;
+      any = any || nmask[b];
+    }
+    if (!any || it >= o->max_newton) break;
+    if (o->mixed_matvec) {
+      FxArgs ga = fx_args(p, SDD_PREC_MIXED, X, p->nw_base32, p->out4);
+      SDD_CUDA(launch_fx(ga, B, 2, SDD_PREC_MIXED, s));
+    }
+    for (int b = 0; b < B; ++b) target[b] = o->gmres_rtol * resF[b];
+    SDD_CUDA(cudaMemcpyAsync(G.target, target.data(), B * sizeof(double), cudaMemcpyHostToDevice, s));
+    SDD_CUDA(cudaMemcpyAsync(G.solve, nmask.data(), B * sizeof(int), cudaMemcpyHostToDevice, s));
+    SDD_CUDA(cudaMemcpyAsync(newton_mask, nmask.data(), B * sizeof(int), cudaMemcpyHostToDevice, s));
+    SDD_CUDA(cudaMemsetAsync(p->nw_x, 0, (size_t)B * n * sizeof(double), s));
+    for (int cyc = 0; cyc < o->max_restarts; ++cyc) {
+      const double* r = p->nw_F;
+      if (cyc > 0) {                                  // r = F - J x
+        if ((st = jac(p->nw_x, p->nw_w))) return st;
+        SDD_CUDA(krylov_sub(p->nw_F, p->nw_w, p->nw_r, (size_t)B * n, s));
+        r = p->nw_r;
+      }
+      SDD_CUDA(krylov_dots(r, 0, r, n, 1, B, p->nw_part, p->nw_nrm2, 1, 0, s));
+      SDD_CUDA(krylov_cycle_start(G, p->nw_nrm2, B, s));
+      SDD_CUDA(krylov_scale(r, G.inv, p->nw_V, n, B, s));
+      for (int j = 0; j < m; ++j) {
+        double* Vj = p->nw_V + (size_t)j * vs;
+        if ((st = jac(Vj, p->nw_w))) return st;
+        SDD_CUDA(krylov_dots(p->nw_V, vs, p->nw_w, n, j + 1, B, p->nw_part, G.hcol, m + 1, 0, s));
+        SDD_CUDA(krylov_sub_combination(p->nw_V, vs, p->nw_w, G.hcol, m + 1, n, j + 1, B, s));
+        SDD_CUDA(krylov_dots(p->nw_V, vs, p->nw_w, n, j + 1, B, p->nw_part, G.h2, m + 1, 0, s));
+        SDD_CUDA(krylov_sub_combination(p->nw_V, vs, p->nw_w, G.h2, m + 1, n, j + 1, B, s));
+        SDD_CUDA(krylov_dots(p->nw_w, 0, p->nw_w, n, 1, B, p->nw_part, p->nw_nrm2, 1, 0, s));
+        SDD_CUDA(krylov_arnoldi_finish(G, p->nw_nrm2, j, B, s));
+        if (j + 1 < m) SDD_CUDA(krylov_scale(p->nw_w, G.inv, p->nw_V + (size_t)(j + 1) * vs, n, B, s));
+        SDD_CUDA(cudaMemcpyAsync(p->h_int, G.active, B * sizeof(int), cudaMemcpyDeviceToHost, s));
+        SDD_CUDA(cudaStreamSynchronize(s));
+        bool act = false;
+        for (int b = 0; b < B; ++b) act = act || p->h_int[b];
+        if (!act) break;
+      }
+      SDD_CUDA(krylov_solve_y(G, B, s));
+      SDD_CUDA(krylov_add_combination(p->nw_V, vs, p->nw_x, G.y, m, G.kb, n, B, s));
+      SDD_CUDA(cudaMemcpyAsync(p->h_dbl, G.resid, B * sizeof(double), cudaMemcpyDeviceToHost, s));
+      SDD_CUDA(cudaStreamSynchronize(s));
+      std::vector<int> again(B, 0);
+      bool more = false;
+      for (int b = 0; b < B; ++b) {
+        again[b] = nmask[b] && p->h_dbl[b] > target[b];
+        more = more || again[b];
+      }
+      if (!more) break;
+      SDD_CUDA(cudaMemcpyAsync(G.solve, again.data(), B * sizeof(int), cudaMemcpyHostToDevice, s));
+    }
+    SDD_CUDA(krylov_masked_sub(X, p->nw_x, newton_mask, n, B, s));
+    for (int b = 0; b < B; ++b) iters[b] += nmask[b];
+  }
+  bool all = true;
+  for (int b = 0; b < B; ++b) {
+    res[b].residual = resF[b];
+    res[b].newton_iters = iters[b];
+    res[b].matvecs = matvecs;
+    res[b].converged = resF[b] <= o->tol ? 1 : 0;
+    res[b].pad = 0;
+    all = all && res[b].converged;
+  }
+  return all ? SDD_OK : SDD_ERR_NOT_CONVERGED;
+}
+
+// ---- instrumentation ------------------------------------------------------------------------------
+extern "C" int sdd_step_profile(sdd_plan* p, int B, const double* Ra, const double* Ras, const double* X_in,
+                                double* X_out, int nsteps, double* ms, void* stream) {
+  int st = check_plan(p, B);
+  if (st) return st;
+  if (!Ra || !Ras || !X_in || !X_out || !ms || nsteps < 1 || X_in == X_out) return SDD_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaEvent_t ev[4];
+  for (auto& e : ev) SDD_CUDA(cudaEventCreate(&e));
+  const double* cur = X_in;
+  int rc = SDD_OK;
+  for (int it = 0; it < nsteps && rc == SDD_OK; ++it) {
+    const int left = nsteps - it;
+    double* dst = (left % 2 == 1) ? X_out : p->xtmp;
+    cudaError_t e = cudaEventRecord(ev[0], s);
+    FxArgs fa = fx_args(p, p->prec, cur, nullptr, p->out4);
+    if (e == cudaSuccess) e = launch_fx(fa, B, 0, p->prec, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], s);
+    RhsArgs ra = rhs_args(p, cur, p->out4, Ra, Ras, p->rhs, 0);
+    if (e == cudaSuccess) e = launch_rhs(ra, B, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[2], s);
+    ChainArgs ca = chain_args(p, p->rhs, dst, nullptr);
+    if (e == cudaSuccess) e = launch_chain(ca, B, 3, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[3], s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[3]);
+    float t = 0.f;
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+      e = cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+      ms[k] += t;
+    }
+    if (e != cudaSuccess) {
+      set_cuda_error(e);
+      rc = SDD_ERR_CUDA;
+    }
+    cur = dst;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return rc;
+}
+
+namespace sdd {
+__global__ void k_fp64_fma_loop(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+}  // namespace sdd
+
+extern "C" int sdd_measure_fp64_peak(double* gflops, void* stream) {
+  if (!gflops) return SDD_ERR_ARG;
+  int dev = 0, sms = 0;
+  SDD_CUDA(cudaGetDevice(&dev));
+  SDD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = sms * 8, threads = 256, iters = 2000;
+  cudaStream_t s = (cudaStream_t)stream;
+  double* out = nullptr;
+  SDD_CUDA(cudaMalloc(&out, (size_t)blocks * threads * sizeof(double)));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  cudaError_t e = cudaSuccess;
+  for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+    cudaEventRecord(e0, s);
+    k_fp64_fma_loop<<<blocks, threads, 0, s>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(e1, s);
+    e = cudaEventSynchronize(e1);
+    float t = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    if (t > 0.f && t < best) best = t;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) {
+    set_cuda_error(e);
+    return SDD_ERR_CUDA;
+  }
+  *gflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e9;
+  return SDD_OK;
+}

@@ -156,7 +156,8 @@ __global__ void k_chain(ChainArgs a) {
 cudaError_t launch_chain(const ChainArgs& a, int batch, int nfields, cudaStream_t s) {
   const int blk = a.nr * a.ldl;
   const size_t smem = (3 * (size_t)blk + (size_t)a.nr * a.nr + 4 * (size_t)a.nr) * sizeof(double);
-  cudaError_t e = cudaFuncSetAttribute(k_chain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  static unsigned long long done = 0;
+  cudaError_t e = ensure_smem_attr(k_chain, &done);
   if (e != cudaSuccess) return e;
   const int threads = ((4 * a.nr + 31) / 32) * 32;
   k_chain<<<dim3(2 * nfields, batch), threads, smem, s>>>(a);

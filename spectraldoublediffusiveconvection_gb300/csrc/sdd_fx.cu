@@ -611,8 +611,8 @@ __global__ void __launch_bounds__(kFxThreads) k_fx_finish(FinishArgs a) {
 template <typename T, int MODE>
 static cudaError_t launch_fx_t(const FxArgs& a, int batch, cudaStream_t s) {
   const size_t smem = fx_smem_bytes(a.M, a.P, sizeof(T) == 4 ? SDD_PREC_MIXED : SDD_PREC_FP64);
-  cudaError_t e = cudaFuncSetAttribute(k_fx_rows<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
+  static unsigned long long done = 0;
+  cudaError_t e = ensure_smem_attr(k_fx_rows<T, MODE>, &done);
   if (e != cudaSuccess) return e;
   k_fx_rows<T, MODE><<<dim3(a.nr, batch), kFxThreads, smem, s>>>(a);
   return cudaGetLastError();
@@ -631,7 +631,8 @@ cudaError_t launch_fx(const FxArgs& a, int batch, int mode, int prec, cudaStream
 
 cudaError_t launch_rhs(const RhsArgs& a, int batch, cudaStream_t s) {
   const size_t smem = (6 * (size_t)a.M + 2 * (size_t)a.nr) * sizeof(double);
-  cudaError_t e = cudaFuncSetAttribute(k_rhs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  static unsigned long long done = 0;
+  cudaError_t e = ensure_smem_attr(k_rhs, &done);
   if (e != cudaSuccess) return e;
   k_rhs<<<dim3(a.nr, batch), kFxThreads, smem, s>>>(a);
   return cudaGetLastError();
@@ -641,7 +642,8 @@ cudaError_t launch_theta_op(int op, int M, int nr, int sym, const double* D2, co
                             const double* dT0, const double* g, double* f, int batch, cudaStream_t s) {
   ThetaArgs a{op, M, nr, sym, D2, ir, dT0, g, f};
   const size_t smem = (3 * (size_t)M + (size_t)nr) * sizeof(double);
-  cudaError_t e = cudaFuncSetAttribute(k_theta_op, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  static unsigned long long done = 0;
+  cudaError_t e = ensure_smem_attr(k_theta_op, &done);
   if (e != cudaSuccess) return e;
   k_theta_op<<<dim3(nr, batch), kFxThreads, smem, s>>>(a);
   return cudaGetLastError();
@@ -670,7 +672,8 @@ cudaError_t launch_transform(int kind, int rows, int n_in, int n_out, const FftP
   a.in = in;
   a.out = out;
   const size_t smem = (2 * kTrPairs + 2) * (size_t)fp->L * sizeof(double2) + (4 * 32 + 8) * sizeof(double);
-  cudaError_t e = cudaFuncSetAttribute(k_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  static unsigned long long done = 0;
+  cudaError_t e = ensure_smem_attr(k_transform, &done);
   if (e != cudaSuccess) return e;
   const int grid = (rows + 2 * kTrPairs - 1) / (2 * kTrPairs);
   k_transform<<<grid, kFxThreads, smem, s>>>(a);

@@ -16,6 +16,23 @@ constexpr int kFxThreads = 256;  // threads of the row kernels
 
 void set_cuda_error(cudaError_t e);
 
+// Raises a kernel's dynamic shared-memory limit to the device's opt-in maximum once per device, so
+// launches do not pay a cudaFuncSetAttribute call each.
+template <typename F>
+inline cudaError_t ensure_smem_attr(F* fn, unsigned long long* done_mask) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (__atomic_load_n(done_mask, __ATOMIC_ACQUIRE) & bit) return cudaSuccess;
+  int optin = 0;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(reinterpret_cast<const void*>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  if (e == cudaSuccess) __atomic_fetch_or(done_mask, bit, __ATOMIC_ACQ_REL);
+  return e;
+}
+
 // Twiddle tables and radix plan of one complex FFT length L (used for DCT-II/III of length L).
 struct FftPlan {
   int L = 0;

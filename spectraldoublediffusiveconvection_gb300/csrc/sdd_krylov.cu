@@ -1,0 +1,241 @@
+// Device Krylov kernels for the matrix-free Newton-GMRES of Main.py:523-536 (the reference calls
+// scipy.sparse.linalg.lgmres on a LinearOperator wrapping PDFX).  Here: restarted GMRES(m) with
+// classical Gram-Schmidt applied twice (CGS2), FP64 throughout, one Krylov space per shell of a batch.
+//
+// Reductions are deterministic: every dot product is a fixed-order two-level sum (per-CTA partials over
+// fixed element chunks, then a fixed-order sum of the partials), so a shell's result does not depend
+// on the other shells in the batch.
+//
+// Vector layout: V[i][b][n] (Krylov vector i of shell b has n = 3*N_fm*nr contiguous doubles).
+#include <cuda_runtime.h>
+
+#include "sdd_krylov.cuh"
+
+namespace sdd {
+
+constexpr int kDotThreads = 256;
+
+// part[(b*(nv) + i)*nchunk + c] = sum over chunk c of V_i[b] . w[b],  i < nv
+__global__ void __launch_bounds__(kDotThreads) k_dot_partials(const double* __restrict__ V, size_t vstride_i,
+                                                             const double* __restrict__ w, int n, int nv,
+                                                             int chunk, double* __restrict__ part) {
+  __shared__ double red[kDotThreads / 32];
+  const int c = blockIdx.x, b = blockIdx.y, nchunk = gridDim.x;
+  const int e0 = c * chunk, e1 = min(n, e0 + chunk);
+  const double* wb = w + (size_t)b * n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = 0; i < nv; ++i) {
+    const double* vb = V + (size_t)i * vstride_i + (size_t)b * n;
+    double s = 0.0;
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) s += vb[e] * wb[e];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (lane == 0) red[warp] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int q = 0; q < (int)(blockDim.x / 32); ++q) t += red[q];
+      part[((size_t)b * nv + i) * nchunk + c] = t;
+    }
+    __syncthreads();
+  }
+}
+
+// h[b*ldh + i] (+)= sum_c part[(b*nv+i)*nchunk + c]
+__global__ void k_dot_reduce(const double* __restrict__ part, int nv, int nchunk, double* __restrict__ h,
+                             int ldh, int accumulate) {
+  const int b = blockIdx.x;
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    double t = 0.0;
+    const double* p = part + ((size_t)b * nv + i) * nchunk;
+    for (int c = 0; c < nchunk; ++c) t += p[c];
+    if (accumulate) h[(size_t)b * ldh + i] += t;
+    else h[(size_t)b * ldh + i] = t;
+  }
+}
+
+// w[b] -= sum_{i<nv} V_i[b] * coef[b*ldc + i]
+__global__ void k_sub_combination(const double* __restrict__ V, size_t vstride_i, double* __restrict__ w,
+                                  const double* __restrict__ coef, int ldc, int n, int nv) {
+  const int b = blockIdx.y;
+  const double* cb = coef + (size_t)b * ldc;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int i = 0; i < nv; ++i) s += V[(size_t)i * vstride_i + (size_t)b * n + e] * cb[i];
+    w[(size_t)b * n + e] -= s;
+  }
+}
+
+// x[b] += sum_{i<k_b} V_i[b] * y[b*ldy + i]
+__global__ void k_add_combination(const double* __restrict__ V, size_t vstride_i, double* __restrict__ x,
+                                  const double* __restrict__ y, int ldy, const int* __restrict__ kb, int n) {
+  const int b = blockIdx.y;
+  const int k = kb[b];
+  const double* yb = y + (size_t)b * ldy;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int i = 0; i < k; ++i) s += V[(size_t)i * vstride_i + (size_t)b * n + e] * yb[i];
+    x[(size_t)b * n + e] += s;
+  }
+}
+
+// out[b] = a[b] * scale[b]  (scale may be per shell)
+__global__ void k_scale(const double* __restrict__ a, const double* __restrict__ scale, double* __restrict__ out,
+                        int n) {
+  const int b = blockIdx.y;
+  const double s = scale[b];
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
+    out[(size_t)b * n + e] = a[(size_t)b * n + e] * s;
+}
+
+// out = a - b
+__global__ void k_sub(const double* __restrict__ a, const double* __restrict__ bb, double* __restrict__ out,
+                      size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    out[e] = a[e] - bb[e];
+}
+
+// X[b] -= dx[b] where mask[b] != 0
+__global__ void k_masked_sub(double* __restrict__ X, const double* __restrict__ dx, const int* __restrict__ mask,
+                             int n) {
+  const int b = blockIdx.y;
+  if (!mask[b]) return;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
+    X[(size_t)b * n + e] -= dx[(size_t)b * n + e];
+}
+
+// Start of a GMRES cycle.  nrm2[b] = ||r_b||^2.  Sets beta, g = [beta,0..], inv = 1/beta, and the
+// per-shell activity flag (active while the shell is being solved and beta is above its target).
+__global__ void k_cycle_start(GmresState s, const double* __restrict__ nrm2, int B) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const double beta = sqrt(nrm2[b]);
+  s.beta[b] = beta;
+  double* g = s.g + (size_t)b * (s.m + 1);
+  for (int i = 0; i <= s.m; ++i) g[i] = 0.0;
+  g[0] = beta;
+  const int act = s.solve[b] && beta > s.target[b] && beta > 0.0;
+  s.active[b] = act;
+  s.kb[b] = 0;
+  s.inv[b] = (act && beta > 0.0) ? 1.0 / beta : 0.0;
+  s.resid[b] = beta;
+}
+
+// After CGS2 for column j: hcol[b][0..j] holds the projections, nrm2[b] = ||w||^2.  Stores the column in H,
+// applies the previous Givens rotations, makes the new one, updates g and the residual estimate.
+__global__ void k_arnoldi_finish(GmresState s, const double* __restrict__ nrm2, int j, int B) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const int m = s.m;
+  double* H = s.H + (size_t)b * (m + 1) * m;   // H[row*m + col]
+  const double* hc = s.hcol + (size_t)b * (m + 1);
+  const double* hd = s.h2 + (size_t)b * (m + 1);
+  double* cs = s.cs + (size_t)b * m;
+  double* sn = s.sn + (size_t)b * m;
+  double* g = s.g + (size_t)b * (m + 1);
+  const double hnext = sqrt(nrm2[b]);
+  if (!s.active[b]) {
+    s.inv[b] = 0.0;
+    return;
+  }
+  for (int i = 0; i <= j; ++i) H[i * m + j] = hc[i] + hd[i];
+  H[(j + 1) * m + j] = hnext;
+  for (int i = 0; i < j; ++i) {
+    const double a = H[i * m + j], c = H[(i + 1) * m + j];
+    H[i * m + j] = cs[i] * a + sn[i] * c;
+    H[(i + 1) * m + j] = -sn[i] * a + cs[i] * c;
+  }
+  const double a = H[j * m + j], c = H[(j + 1) * m + j];
+  const double r = hypot(a, c);
+  double cj = 1.0, sj = 0.0;
+  if (r > 0.0) {
+    cj = a / r;
+    sj = c / r;
+  }
+  cs[j] = cj;
+  sn[j] = sj;
+  H[j * m + j] = r;
+  H[(j + 1) * m + j] = 0.0;
+  g[j + 1] = -sj * g[j];
+  g[j] = cj * g[j];
+  const double res = fabs(g[j + 1]);
+  s.resid[b] = res;
+  s.kb[b] = j + 1;
+  const bool breakdown = !(hnext > 1e-300 * s.beta[b]);
+  if (res <= s.target[b] || breakdown || j + 1 == m) s.active[b] = 0;
+  s.inv[b] = (s.active[b] && hnext > 0.0) ? 1.0 / hnext : 0.0;
+}
+
+// Back substitution R y = g over the first kb[b] columns.
+__global__ void k_solve_y(GmresState s, int B) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const int m = s.m, k = s.kb[b];
+  const double* H = s.H + (size_t)b * (m + 1) * m;
+  const double* g = s.g + (size_t)b * (m + 1);
+  double* y = s.y + (size_t)b * m;
+  for (int i = k - 1; i >= 0; --i) {
+    double t = g[i];
+    for (int c = i + 1; c < k; ++c) t -= H[i * m + c] * y[c];
+    const double d = H[i * m + i];
+    y[i] = d != 0.0 ? t / d : 0.0;
+  }
+}
+
+// ---- host wrappers ------------------------------------------------------------------------------
+static int grid_x(int n) {
+  int g = (n + 255) / 256;
+  return g < 1 ? 1 : (g > 1024 ? 1024 : g);
+}
+
+cudaError_t krylov_dots(const double* V, size_t vstride_i, const double* w, int n, int nv, int B, double* part,
+                        double* h, int ldh, int accumulate, cudaStream_t st) {
+  const int nchunk = (n + kDotChunk - 1) / kDotChunk;
+  k_dot_partials<<<dim3(nchunk, B), kDotThreads, 0, st>>>(V, vstride_i, w, n, nv, kDotChunk, part);
+  k_dot_reduce<<<B, 64, 0, st>>>(part, nv, nchunk, h, ldh, accumulate);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_sub_combination(const double* V, size_t vstride_i, double* w, const double* coef, int ldc,
+                                   int n, int nv, int B, cudaStream_t st) {
+  k_sub_combination<<<dim3(grid_x(n), B), 256, 0, st>>>(V, vstride_i, w, coef, ldc, n, nv);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_add_combination(const double* V, size_t vstride_i, double* x, const double* y, int ldy,
+                                   const int* kb, int n, int B, cudaStream_t st) {
+  k_add_combination<<<dim3(grid_x(n), B), 256, 0, st>>>(V, vstride_i, x, y, ldy, kb, n);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_scale(const double* a, const double* scale, double* out, int n, int B, cudaStream_t st) {
+  k_scale<<<dim3(grid_x(n), B), 256, 0, st>>>(a, scale, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_sub(const double* a, const double* b, double* out, size_t n, cudaStream_t st) {
+  k_sub<<<grid_x((int)(n > (1u << 30) ? (1u << 30) : n)), 256, 0, st>>>(a, b, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_masked_sub(double* X, const double* dx, const int* mask, int n, int B, cudaStream_t st) {
+  k_masked_sub<<<dim3(grid_x(n), B), 256, 0, st>>>(X, dx, mask, n);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_cycle_start(const GmresState& s, const double* nrm2, int B, cudaStream_t st) {
+  k_cycle_start<<<(B + 63) / 64, 64, 0, st>>>(s, nrm2, B);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_arnoldi_finish(const GmresState& s, const double* nrm2, int j, int B, cudaStream_t st) {
+  k_arnoldi_finish<<<(B + 63) / 64, 64, 0, st>>>(s, nrm2, j, B);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_solve_y(const GmresState& s, int B, cudaStream_t st) {
+  k_solve_y<<<(B + 63) / 64, 64, 0, st>>>(s, B);
+  return cudaGetLastError();
+}
+
+}  // namespace sdd

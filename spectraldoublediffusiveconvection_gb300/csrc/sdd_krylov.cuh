@@ -1,0 +1,41 @@
+// Krylov (GMRES) device state and kernel wrappers, see sdd_krylov.cu.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace sdd {
+
+constexpr int kDotChunk = 4096;   // elements per CTA in the two-level dot products
+
+struct GmresState {
+  int m;            // restart length
+  double* H;        // [B][m+1][m] Hessenberg, rotated in place to R
+  double* hcol;     // [B][m+1] first Gram-Schmidt pass projections of the current column
+  double* h2;       // [B][m+1] second pass projections
+  double* cs;       // [B][m]
+  double* sn;       // [B][m]
+  double* g;        // [B][m+1] rotated right-hand side beta e1
+  double* y;        // [B][m]
+  double* beta;     // [B]
+  double* inv;      // [B] 1/beta or 1/h_{j+1,j} (0 when the shell is inactive)
+  double* resid;    // [B] current GMRES residual estimate |g_{j+1}|
+  double* target;   // [B] inner tolerance (absolute)
+  int* active;      // [B] still iterating in the current cycle
+  int* solve;       // [B] shell takes part in this solve
+  int* kb;          // [B] columns used
+};
+
+cudaError_t krylov_dots(const double* V, size_t vstride_i, const double* w, int n, int nv, int B, double* part,
+                        double* h, int ldh, int accumulate, cudaStream_t st);
+cudaError_t krylov_sub_combination(const double* V, size_t vstride_i, double* w, const double* coef, int ldc,
+                                   int n, int nv, int B, cudaStream_t st);
+cudaError_t krylov_add_combination(const double* V, size_t vstride_i, double* x, const double* y, int ldy,
+                                   const int* kb, int n, int B, cudaStream_t st);
+cudaError_t krylov_scale(const double* a, const double* scale, double* out, int n, int B, cudaStream_t st);
+cudaError_t krylov_sub(const double* a, const double* b, double* out, size_t n, cudaStream_t st);
+cudaError_t krylov_masked_sub(double* X, const double* dx, const int* mask, int n, int B, cudaStream_t st);
+cudaError_t krylov_cycle_start(const GmresState& s, const double* nrm2, int B, cudaStream_t st);
+cudaError_t krylov_arnoldi_finish(const GmresState& s, const double* nrm2, int j, int B, cudaStream_t st);
+cudaError_t krylov_solve_y(const GmresState& s, int B, cudaStream_t st);
+
+}  // namespace sdd

@@ -176,6 +176,33 @@ class Plan:
         return out
 
 
+    def step_profile(self, X, Ra, Ra_s, nsteps):
+        """Per-kernel milliseconds (fx, rhs, chain) summed over nsteps steps from X (CUDA events)."""
+        B = self._chk(X, self.n_state, "X")
+        ra, ras = self._vec(Ra, B), self._vec(Ra_s, B)
+        out = _torch().empty_like(X)
+        ms = (ctypes.c_double * 3)(0.0, 0.0, 0.0)
+        _lib.check(self._L.sdd_step_profile(self._h, B, _dptr(ra), _dptr(ras), _dptr(X), _dptr(out), int(nsteps),
+                                            ms, _stream(self.device)), "sdd_step_profile")
+        return list(ms), out
+
+    def newton(self, X, Ra, Ra_s, tol=1e-10, restart=50, gmres_rtol=1e-4, max_newton=20, max_restarts=20,
+               mixed_matvec=False, raise_on_fail=False):
+        """Newton-GMRES on F(X) = Phi_dt(X) - X in place on X (batch x n_state); returns per-shell dicts
+        (residual0, residual, newton_iters, matvecs, converged).  The plan's dt should be 1 (Main.py:430)."""
+        B = self._chk(X, self.n_state, "X")
+        ra, ras = self._vec(Ra, B), self._vec(Ra_s, B)
+        o = _lib.NewtonOpts(float(tol), float(gmres_rtol), int(restart), int(max_restarts), int(max_newton),
+                            int(bool(mixed_matvec)))
+        res = (_lib.NewtonResult * B)()
+        st = self._L.sdd_newton_gmres(self._h, B, _dptr(ra), _dptr(ras), _dptr(X), ctypes.byref(o), res,
+                                      _stream(self.device))
+        if st not in (_lib.SDD_OK, _lib.SDD_ERR_NOT_CONVERGED) or (raise_on_fail and st != _lib.SDD_OK):
+            _lib.check(st, "sdd_newton_gmres")
+        return [dict(residual0=r.residual0, residual=r.residual, newton_iters=r.newton_iters,
+                     matvecs=r.matvecs, converged=bool(r.converged)) for r in res]
+
+
 _cache = {}
 _cache_lock = threading.Lock()
 
