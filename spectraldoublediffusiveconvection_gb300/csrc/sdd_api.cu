@@ -60,7 +60,7 @@ const FftPlan* get_fft_plan(int L) {
     const double a = 2.0 * pi * (double)k / (double)L;
     w[k] = make_double2(std::cos(a), -std::sin(a));
     const double b = pi * (double)k / (2.0 * (double)L);
-    e[k] = make_double2(std::cos(b), std::sin(b));
+    e[k] = make_double2(0.5 * std::cos(b), 0.5 * std::sin(b));
     wf[k] = make_float2((float)w[k].x, (float)w[k].y);
     ef[k] = make_float2((float)e[k].x, (float)e[k].y);
   }
@@ -93,6 +93,7 @@ struct sdd_plan {
   // FP64 operators
   double *Dr, *D2r2, *ir4r2, *D2s, *ir2s, *D2A4, *ir2A4, *ir4A4, *rsq, *dT0, *gr;
   double *LinvA4, *LinvT, *LinvS;
+  double *coefA4, *coefT, *coefS;   // per-step scalars of the chains
   // FP32 copies used by the mixed-precision nonlinear term
   float *Dr32, *D2r232, *ir4r232;
   // workspace
@@ -158,12 +159,14 @@ static int upload32(float** dst, const double* src, size_t n) {
   SDD_CUDA(cudaMemcpy(*dst, h.data(), n * sizeof(float), cudaMemcpyHostToDevice));
   return SDD_OK;
 }
+// Linv blocks (and D2_A4 with M = 1) go to the device transposed, column c of a block contiguous with
+// leading dimension ldl (even, so every block starts on a 16-byte boundary for cp.async).
 static int upload_linv(double** dst, const double* src, int M, int nr, int ldl) {
   if (!src) return SDD_ERR_ARG;
   std::vector<double> h((size_t)M * nr * ldl, 0.0);
   for (int m = 0; m < M; ++m)
     for (int i = 0; i < nr; ++i)
-      for (int c = 0; c < nr; ++c) h[((size_t)m * nr + i) * ldl + c] = src[((size_t)m * nr + i) * nr + c];
+      for (int c = 0; c < nr; ++c) h[((size_t)m * nr + c) * ldl + i] = src[((size_t)m * nr + i) * nr + c];
   SDD_CUDA(cudaMalloc(dst, h.size() * sizeof(double)));
   SDD_CUDA(cudaMemcpy(*dst, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
   return SDD_OK;
@@ -172,7 +175,7 @@ static int upload_linv(double** dst, const double* src, int M, int nr, int ldl) 
 static void free_plan(sdd_plan* p) {
   if (!p) return;
   double* d[] = {p->Dr, p->D2r2, p->ir4r2, p->D2s, p->ir2s, p->D2A4, p->ir2A4, p->ir4A4, p->rsq, p->dT0,
-                 p->gr, p->LinvA4, p->LinvT, p->LinvS, p->out4, p->rhs, p->xtmp};
+                 p->gr, p->LinvA4, p->LinvT, p->LinvS, p->out4, p->rhs, p->xtmp, p->coefA4, p->coefT, p->coefS};
   for (double* x : d) cudaFree(x);
   cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232);
   cudaFree(p->base_tmp);
@@ -212,7 +215,7 @@ int sdd_plan_create(const sdd_plan_desc* d, sdd_plan** out) {
   int st = SDD_OK;
   if ((st = upload(&p->Dr, d->Dr, nn)) || (st = upload(&p->D2r2, d->D2_r2, nn)) ||
       (st = upload(&p->ir4r2, d->ir4_r2, nr)) || (st = upload(&p->D2s, d->D2_sine, nn)) ||
-      (st = upload(&p->ir2s, d->ir2_sine, nr)) || (st = upload(&p->D2A4, d->D2_A4, nn)) ||
+      (st = upload(&p->ir2s, d->ir2_sine, nr)) || (st = upload_linv(&p->D2A4, d->D2_A4, 1, nr, p->ldl)) ||
       (st = upload(&p->ir2A4, d->ir2_A4, nr)) || (st = upload(&p->ir4A4, d->ir4_A4, nr)) ||
       (st = upload(&p->rsq, d->rsq, nr)) || (st = upload(&p->dT0, d->dT0, nr)) ||
       (st = upload(&p->gr, d->gr, nr)) || (st = upload_linv(&p->LinvA4, d->Linv_A4, M, nr, p->ldl)) ||
@@ -224,6 +227,28 @@ int sdd_plan_create(const sdd_plan_desc* d, sdd_plan** out) {
     return st;
   }
   (void)nm;
+  {  // per-step scalars of the chains (Matrix_Operators.py:1143-1159 and 1056-1083)
+    std::vector<double> cA((size_t)M * 4), cT((size_t)M * 4), cS((size_t)M * 4);
+    const double dA = d->Pr * d->dt, dT = d->dt, dS = d->Tau * d->dt;
+    for (int jj = 0; jj < M; ++jj) {
+      const double j = (double)(M - jj);
+      const double bj = -j * (j + 1.0), bjt = -2.0 * j;
+      cA[4 * jj] = dA * bjt;
+      cA[4 * jj + 1] = dA * bjt * bj;
+      cA[4 * jj + 2] = bj;
+      cA[4 * jj + 3] = bjt;
+      const double jc = (double)(M - 1 - jj);
+      cT[4 * jj] = -dT * (-2.0 * (jc + 2.0));
+      cS[4 * jj] = -dS * (-2.0 * (jc + 2.0));
+      cT[4 * jj + 1] = cS[4 * jj + 1] = (M - 1 - jj == 0) ? 0.5 : 1.0;
+      cT[4 * jj + 2] = cT[4 * jj + 3] = cS[4 * jj + 2] = cS[4 * jj + 3] = 0.0;
+    }
+    if ((st = upload(&p->coefA4, cA.data(), cA.size())) || (st = upload(&p->coefT, cT.data(), cT.size())) ||
+        (st = upload(&p->coefS, cS.data(), cS.size()))) {
+      free_plan(p);
+      return st;
+    }
+  }
   *out = p;
   return SDD_OK;
 }
@@ -299,6 +324,7 @@ static ChainArgs chain_args(const sdd_plan* p, const double* g, double* f, const
   a.sub = sub; a.sub_stride = shell_elems(p);
   a.LinvA4 = p->LinvA4; a.LinvT = p->LinvT; a.LinvS = p->LinvS;
   a.D2A4 = p->D2A4; a.ir2A4 = p->ir2A4; a.ir4A4 = p->ir4A4;
+  a.coefA4 = p->coefA4; a.coefT = p->coefT; a.coefS = p->coefS;
   a.dtA4 = p->Pr * p->dt; a.dtT = p->dt; a.dtS = p->Tau * p->dt;
   return a;
 }

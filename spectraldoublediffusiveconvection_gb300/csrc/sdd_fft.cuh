@@ -11,6 +11,7 @@
 //   DCT2: z_n = f_A[src(n)] + i f_B[src(n)],  Z = DFT(z),
 //         y_A[k] = c (Z_k + Z_{-k})_re/2 + s (Z_k - Z_{-k})_im/2,
 //         y_B[k] = c (Z_k + Z_{-k})_im/2 - s (Z_k - Z_{-k})_re/2,   (c, s) = (cos, sin)(pi k/2P).
+// The DCT twiddle table holds 0.5 (cos, sin)(pi k/2P), the factor 1/2 of both formulas folded in.
 // Sine transforms use sin(w theta_i) = (-1)^i cos((P-w) theta_i).
 // The complex FFT is a Stockham autosort FFT (natural order in and out) with radix-2/3/4/5/7 passes,
 // ping-ponging between two shared-memory buffers; twiddles come from a table exp(-2 pi i k/L) built on
@@ -45,23 +46,22 @@ __device__ __forceinline__ typename Cplx<T>::type tw_at(const typename Cplx<T>::
   return t;
 }
 
-// In-register radix-R DFT of v[0..R-1]; w is the length-L twiddle table.
-template <typename T, bool INV>
-__device__ __forceinline__ void butterfly(typename Cplx<T>::type* v, int R, const typename Cplx<T>::type* w,
-                                          int L) {
+// In-register radix-R DFT of v[0..R-1] (R a compile-time constant); w is the length-L twiddle table.
+template <typename T, bool INV, int R>
+__device__ __forceinline__ void butterfly(typename Cplx<T>::type (&v)[R], const typename Cplx<T>::type* w, int L) {
   using C = typename Cplx<T>::type;
-  if (R == 2) {
+  if constexpr (R == 2) {
     C a = v[0], b = v[1];
     v[0] = cadd(a, b);
     v[1] = csub(a, b);
-  } else if (R == 4) {
+  } else if constexpr (R == 4) {
     C t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
     C t2 = cadd(v[1], v[3]), t3 = cmul_mi<C, INV>(csub(v[1], v[3]));
     v[0] = cadd(t0, t2);
     v[2] = csub(t0, t2);
     v[1] = cadd(t1, t3);
     v[3] = csub(t1, t3);
-  } else if (R == 3) {
+  } else if constexpr (R == 3) {
     const T h = (T)0.86602540378443864676;  // sqrt(3)/2
     C s = cadd(v[1], v[2]);
     C d = csub(v[1], v[2]);
@@ -70,28 +70,26 @@ __device__ __forceinline__ void butterfly(typename Cplx<T>::type* v, int R, cons
     v[0] = cadd(v[0], s);
     v[1] = cmk<C>(t.x + h * u.x, t.y + h * u.y);
     v[2] = cmk<C>(t.x - h * u.x, t.y - h * u.y);
-  } else {  // generic small prime radix (5, 7) from the table
-    C o[kMaxRadix];
+  } else {  // small prime radix (5, 7): direct DFT with roots of unity from the table
+    C o[R];
     const int step = L / R;
 #pragma unroll
-    for (int q = 0; q < kMaxRadix; ++q) {
-      if (q < R) {
-        C acc = v[0];
-        for (int r = 1; r < R; ++r) acc = cadd(acc, cmul(v[r], tw_at<T, INV>(w, ((q * r) % R) * step)));
-        o[q] = acc;
-      }
+    for (int q = 0; q < R; ++q) {
+      C acc = v[0];
+#pragma unroll
+      for (int r = 1; r < R; ++r) acc = cadd(acc, cmul(v[r], tw_at<T, INV>(w, ((q * r) % R) * step)));
+      o[q] = acc;
     }
 #pragma unroll
-    for (int q = 0; q < kMaxRadix; ++q)
-      if (q < R) v[q] = o[q];
+    for (int q = 0; q < R; ++q) v[q] = o[q];
   }
 }
 
-// One Stockham pass over nf FFTs of length L stored back to back (stride L).
-template <typename T, bool INV>
-__device__ __forceinline__ void fft_pass(const typename Cplx<T>::type* __restrict__ in,
-                                         typename Cplx<T>::type* __restrict__ out, int L, int nf, int R,
-                                         int Ns, const typename Cplx<T>::type* w) {
+// One Stockham pass of radix R over nf FFTs of length L stored back to back (stride L).
+template <typename T, bool INV, int R>
+__device__ __forceinline__ void fft_pass_r(const typename Cplx<T>::type* __restrict__ in,
+                                           typename Cplx<T>::type* __restrict__ out, int L, int nf, int Ns,
+                                           const typename Cplx<T>::type* w) {
   using C = typename Cplx<T>::type;
   const int nb = L / R;
   const int total = nf * nb;
@@ -102,20 +100,30 @@ __device__ __forceinline__ void fft_pass(const typename Cplx<T>::type* __restric
     const C* src = in + f * L;
     C* dst = out + f * L;
     const int k = j % Ns;
-    C v[kMaxRadix];
+    C v[R];
 #pragma unroll
-    for (int r = 0; r < kMaxRadix; ++r)
-      if (r < R) v[r] = src[j + r * nb];
+    for (int r = 0; r < R; ++r) v[r] = src[j + r * nb];
     if (Ns > 1) {
 #pragma unroll
-      for (int r = 1; r < kMaxRadix; ++r)
-        if (r < R) v[r] = cmul(v[r], tw_at<T, INV>(w, k * r * tws));
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw_at<T, INV>(w, k * r * tws));
     }
-    butterfly<T, INV>(v, R, w, L);
+    butterfly<T, INV, R>(v, w, L);
     const int idxD = (j / Ns) * Ns * R + k;
 #pragma unroll
-    for (int r = 0; r < kMaxRadix; ++r)
-      if (r < R) dst[idxD + r * Ns] = v[r];
+    for (int r = 0; r < R; ++r) dst[idxD + r * Ns] = v[r];
+  }
+}
+
+template <typename T, bool INV>
+__device__ __forceinline__ void fft_pass(const typename Cplx<T>::type* __restrict__ in,
+                                         typename Cplx<T>::type* __restrict__ out, int L, int nf, int R, int Ns,
+                                         const typename Cplx<T>::type* w) {
+  switch (R) {
+    case 4: fft_pass_r<T, INV, 4>(in, out, L, nf, Ns, w); break;
+    case 2: fft_pass_r<T, INV, 2>(in, out, L, nf, Ns, w); break;
+    case 3: fft_pass_r<T, INV, 3>(in, out, L, nf, Ns, w); break;
+    case 5: fft_pass_r<T, INV, 5>(in, out, L, nf, Ns, w); break;
+    default: fft_pass_r<T, INV, 7>(in, out, L, nf, Ns, w); break;
   }
 }
 

@@ -41,7 +41,21 @@ __device__ void parity_suffix(const T* v, T* S, int M) {
 // the real and imaginary parts, and the FFT's rounding error scales with the larger of the two: an
 // unbalanced pair (|komega| ~ 1e3 next to |JT_psi| ~ 1e-2) would leave the small row with an error of
 // eps*1e3.  Each row is therefore scaled by 2^-e, e = exponent of its max |value| (exact), before the
-// transform and scaled back after it.
+// transform and scaled back after it.  The maxima are taken on the IEEE bit patterns (for non-negative
+// values the unsigned order is the numeric order), i.e. with integer instructions: on GB300 the FP64
+// pipe is the scarce resource of these kernels.
+template <typename T> struct Bits;
+template <> struct Bits<double> {
+  using U = unsigned long long;
+  static __device__ __forceinline__ U absbits(double x) { return (U)__double_as_longlong(x) & 0x7fffffffffffffffull; }
+  static __device__ __forceinline__ double val(U u) { return __longlong_as_double((long long)u); }
+};
+template <> struct Bits<float> {
+  using U = unsigned int;
+  static __device__ __forceinline__ U absbits(float x) { return __float_as_uint(x) & 0x7fffffffu; }
+  static __device__ __forceinline__ float val(U u) { return __uint_as_float(u); }
+};
+
 template <typename T>
 __device__ __forceinline__ void pow2_scale(T mx, T* s, T* inv) {
   if (!(mx > (T)0) || !isfinite(mx)) {
@@ -55,62 +69,66 @@ __device__ __forceinline__ void pow2_scale(T mx, T* s, T* inv) {
   *inv = ldexp((T)1, e);
 }
 
-// Block-wide max of K per-thread values; writes scale and inverse scale of each into sc[0..K), sc[K..2K).
-// red must hold K*32 values.  Ends with __syncthreads().
+// Block-wide max of K per-thread |value| bit patterns; writes the scale and inverse scale of each into
+// sc[0..K), sc[K..2K).  red must hold K*32 words of U.  Ends with __syncthreads().
 template <typename T, int K>
-__device__ __forceinline__ void block_max_scales(T (&v)[K], T* red, T* sc) {
+__device__ __forceinline__ void block_max_scales(typename Bits<T>::U (&v)[K], typename Bits<T>::U* red, T* sc) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
   for (int t = 0; t < K; ++t) {
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v[t] = fmax(v[t], __shfl_xor_sync(0xffffffffu, v[t], off));
+    for (int off = 16; off > 0; off >>= 1) {
+      const typename Bits<T>::U o = __shfl_xor_sync(0xffffffffu, v[t], off);
+      v[t] = o > v[t] ? o : v[t];
+    }
     if (lane == 0) red[t * 32 + warp] = v[t];
   }
   __syncthreads();
   if (threadIdx.x < K) {
-    T m = (T)0;
-    for (int w = 0; w < nw; ++w) m = fmax(m, red[threadIdx.x * 32 + w]);
-    pow2_scale(m, sc + threadIdx.x, sc + K + threadIdx.x);
+    typename Bits<T>::U m = 0;
+    for (int w = 0; w < nw; ++w) m = red[threadIdx.x * 32 + w] > m ? red[threadIdx.x * 32 + w] : m;
+    pow2_scale(Bits<T>::val(m), sc + threadIdx.x, sc + K + threadIdx.x);
   }
   __syncthreads();
 }
 
+// shared memory of k_fx_rows in units of T: RA, RB (5P complex each), W, E (P complex each), RG (9P),
+// kf (P), operator rows (2 kMaxNr), reduction words (9*32 of 8 bytes), scales (32)
 size_t fx_smem_bytes(int M, int P, int prec) {
   (void)M;
   const size_t es = prec == SDD_PREC_MIXED ? sizeof(float) : sizeof(double);
-  return (33 * (size_t)P + 2 * kMaxNr + 9 * 32 + 32) * es;
+  return (34 * (size_t)P + 2 * kMaxNr + 32) * es + 9 * 32 * 8;
 }
 
-// DCT3 input x_k of transform t of the nine fields (see the header comment of sdd_fft.cuh).
+// DCT3 input x_k of transform t of the nine fields (see the header comment of sdd_fft.cuh); kf[k] = k.
 // Fields: 0 JT_psi, 1 komega, 2 kDpsi, 3 DT, 4 DC (cosine type); 5 omega, 6 Dpsi, 7 kT, 8 kC (sine type).
 template <typename T>
-__device__ __forceinline__ T fx_x(int t, int k, int M, int P, const T* JP, const T* OM, const T* DP,
-                                  const T* DTv, const T* DCv, const T* Tv, const T* Sv) {
+__device__ __forceinline__ T fx_x(int t, int k, int M, int P, const T* kf, const T* JP, const T* OM,
+                                  const T* DP, const T* DTv, const T* DCv, const T* Tv, const T* Sv) {
   if (t < 5) {
     if (k >= M) return (T)0;
     switch (t) {
       case 0: return JP[k];
-      case 1: return k >= 1 ? (T)k * OM[k - 1] : (T)0;
-      case 2: return k >= 1 ? (T)k * DP[k - 1] : (T)0;
+      case 1: return k >= 1 ? kf[k] * OM[k - 1] : (T)0;
+      case 2: return k >= 1 ? kf[k] * DP[k - 1] : (T)0;
       case 3: return DTv[k];
       default: return DCv[k];
     }
   }
-  if (t > 8) return (T)0;
   const int w = P - k;  // wavenumber
   if (k == 0 || w > M - 1) return (T)0;
   switch (t) {
     case 5: return OM[w - 1];
     case 6: return DP[w - 1];
-    case 7: return -(T)w * Tv[w];
-    default: return -(T)w * Sv[w];
+    case 7: return -(kf[w] * Tv[w]);
+    default: return -(kf[w] * Sv[w]);
   }
 }
 
 // MODE 0: NLIN_FX (optionally storing the grid fields); 1: NLIN_DFX with base fields from the cache;
 // 2: grid fields only (fills the cache).
 template <typename T, int MODE>
-__global__ void __launch_bounds__(kFxThreads) k_fx_rows(FxArgs a) {
+__global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
   using C = typename Cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int M = a.M, nr = a.nr, P = a.P;
@@ -122,9 +140,11 @@ __global__ void __launch_bounds__(kFxThreads) k_fx_rows(FxArgs a) {
   C* Wt = RB + 5 * P;
   C* Et = Wt + P;
   T* RG = reinterpret_cast<T*>(Et + P);
-  T* opr = RG + 9 * P;
-  T* red = opr + 2 * kMaxNr;   // 9*32 reduction slots
-  T* scl = red + 9 * 32;       // 9 scales + 9 inverse scales (inverse transforms), reused for 4+4
+  T* kf = RG + 9 * P;          // kf[k] = k, k < P
+  T* opr = kf + P;
+  T* scl = opr + 2 * kMaxNr;   // 9 scales + 9 inverse scales (inverse transforms), reused for 4+4
+  using U = typename Bits<T>::U;
+  U* red = reinterpret_cast<U*>(scl + 32);   // 9*32 reduction words
   T* pv = RG;
   T* Tv = pv + M;
   T* Sv = Tv + M;
@@ -140,6 +160,7 @@ __global__ void __launch_bounds__(kFxThreads) k_fx_rows(FxArgs a) {
   for (int i = tid; i < P; i += bd) {
     Wt[i] = wg[i];
     Et[i] = eg[i];
+    kf[i] = (T)i;
   }
   const T* Drg = reinterpret_cast<const T*>(a.ops.Dr);
   const T* D2g = reinterpret_cast<const T*>(a.ops.D2r2);
@@ -190,41 +211,45 @@ __global__ void __launch_bounds__(kFxThreads) k_fx_rows(FxArgs a) {
   // J_theta_RT (:437-472) and A2_SINE_R2 (:476-526) along the row
   for (int k = tid; k < M; k += bd) {
     const T s1 = (k + 1 < M) ? Sc[k + 1] : (T)0;
-    JP[k] = (k == 0) ? s1 : (T)(k + 1) * pv[k - 1] + (T)2 * s1;
+    JP[k] = (k == 0) ? s1 : kf[k + 1] * pv[k - 1] + (T)2 * s1;
     const T s2 = (k + 2 < M) ? Sc[k + 2] : (T)0;
-    OM[k] = OM[k] - (T)(k + 1) * (ir4n * ((T)(k + 2) * pv[k] + (T)2 * s2));
+    OM[k] = OM[k] - kf[k + 1] * (ir4n * (kf[k + 2] * pv[k] + (T)2 * s2));
   }
   __syncthreads();
-  {
-    T mloc[9];
-#pragma unroll
-    for (int t = 0; t < 9; ++t) mloc[t] = (T)0;
-    for (int k = tid; k < P; k += bd) {
-#pragma unroll
-      for (int t = 0; t < 9; ++t) mloc[t] = fmax(mloc[t], fabs(fx_x<T>(t, k, M, P, JP, OM, DP, DTv, DCv, Tv, Sv)));
-    }
-    block_max_scales<T, 9>(mloc, red, scl);
-  }
-
   // ---- 2. nine inverse transforms as five paired DCT3s (:776-786) ----
+  // the nine DCT3 input rows, materialised once (in RB, free until the FFT), with their maxima
+  T* XV = reinterpret_cast<T*>(RB);
+  {
+    U mb[9];
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+      mb[t] = 0;
+      for (int k = tid; k < P; k += bd) {
+        const T v = fx_x<T>(t, k, M, P, kf, JP, OM, DP, DTv, DCv, Tv, Sv);
+        XV[t * P + k] = v;
+        const U u = Bits<T>::absbits(v);
+        mb[t] = u > mb[t] ? u : mb[t];
+      }
+    }
+    block_max_scales<T, 9>(mb, red, scl);
+  }
+  // W_k = s_A V_A(k) + i s_B V_B(k),  V(k) = 0.5 e^{i pi k/2P} (x_k - i x_{P-k}),  V(0) = x_0;
+  // Et holds 0.5 e^{i pi k/2P}.
   for (int idx = tid; idx < 5 * P; idx += bd) {
     const int p = idx / P;
     const int k = idx - p * P;
-    C V[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int t = 2 * p + h;
-      const T sc = (t < 9) ? scl[t] : (T)1;
-      const T x = sc * fx_x<T>(t, k, M, P, JP, OM, DP, DTv, DCv, Tv, Sv);
-      if (k == 0) {
-        V[h] = cmk<C>(x, (T)0);
-      } else {
-        const T xr = sc * fx_x<T>(t, P - k, M, P, JP, OM, DP, DTv, DCv, Tv, Sv);
-        const C e = Et[k];
-        V[h] = cmk<C>((T)0.5 * (e.x * x + e.y * xr), (T)0.5 * (e.y * x - e.x * xr));
-      }
+    const int ta = 2 * p, tb = 2 * p + 1;
+    const T sa = scl[ta], sb = (tb < 9) ? scl[tb] : (T)0;
+    const T xa = XV[ta * P + k], xb = (tb < 9) ? XV[tb * P + k] : (T)0;
+    if (k == 0) {
+      RA[idx] = cmk<C>(sa * xa, sb * xb);
+    } else {
+      const T xar = XV[ta * P + P - k], xbr = (tb < 9) ? XV[tb * P + P - k] : (T)0;
+      const C e = Et[k];
+      const T a1 = e.x * xa + e.y * xar, a2 = e.y * xa - e.x * xar;
+      const T b1 = e.x * xb + e.y * xbr, b2 = e.y * xb - e.x * xbr;
+      RA[idx] = cmk<C>(sa * a1 - sb * b2, sa * a2 + sb * b1);
     }
-    RA[idx] = cmk<C>(V[0].x - V[1].y, V[0].y + V[1].x);
   }
   __syncthreads();
   C* res = fft_rows<T, true>(RA, RB, 5, a.st, Wt);
@@ -250,7 +275,7 @@ __global__ void __launch_bounds__(kFxThreads) k_fx_rows(FxArgs a) {
   const T* bs = (MODE == 1) ? reinterpret_cast<const T*>(a.base) + (size_t)b * a.base_stride +
                                   (size_t)n * 9 * P
                             : nullptr;
-  T m4[4] = {(T)0, (T)0, (T)0, (T)0};
+  U m4[4] = {0, 0, 0, 0};
   for (int i = tid; i < P; i += bd) {
     const T JT = RG[i], kO = RG[P + i], kDP = RG[2 * P + i], DTg = RG[3 * P + i], DCg = RG[4 * P + i];
     const T O = RG[5 * P + i], DPg = RG[6 * P + i], kT = RG[7 * P + i], kC = RG[8 * P + i];
@@ -273,10 +298,12 @@ __global__ void __launch_bounds__(kFxThreads) k_fx_rows(FxArgs a) {
     PR[P + i] = sg * Rr;
     PR[2 * P + i] = NT;
     PR[3 * P + i] = NS;
-    m4[0] = fmax(m4[0], fabs(Q));
-    m4[1] = fmax(m4[1], fabs(Rr));
-    m4[2] = fmax(m4[2], fabs(NT));
-    m4[3] = fmax(m4[3], fabs(NS));
+    const U u0 = Bits<T>::absbits(Q), u1 = Bits<T>::absbits(Rr), u2 = Bits<T>::absbits(NT),
+            u3 = Bits<T>::absbits(NS);
+    m4[0] = u0 > m4[0] ? u0 : m4[0];
+    m4[1] = u1 > m4[1] ? u1 : m4[1];
+    m4[2] = u2 > m4[2] ? u2 : m4[2];
+    m4[3] = u3 > m4[3] ? u3 : m4[3];
   }
   block_max_scales<T, 4>(m4, red, scl);   // scl[0..4) scales, scl[4..8) inverses
 
@@ -308,8 +335,8 @@ __global__ void __launch_bounds__(kFxThreads) k_fx_rows(FxArgs a) {
       const C Zk = Z[p * P + k];
       const C Zm = Z[p * P + ((P - k) % P)];
       const C e = Et[k];
-      ya = e.x * (Zk.x + Zm.x) * (T)0.5 + e.y * (Zk.y - Zm.y) * (T)0.5;
-      yb = e.x * (Zk.y + Zm.y) * (T)0.5 - e.y * (Zk.x - Zm.x) * (T)0.5;
+      ya = e.x * (Zk.x + Zm.x) + e.y * (Zk.y - Zm.y);
+      yb = e.x * (Zk.y + Zm.y) - e.y * (Zk.x - Zm.x);
       const T sc = (p == 1 && k == 0) ? one_P : two_P;
       ya *= sc * scl[4 + 2 * p];
       yb *= sc * scl[4 + 2 * p + 1];
@@ -466,8 +493,8 @@ __global__ void __launch_bounds__(kFxThreads) k_transform(TrArgs a) {
   C* RB = RA + kTrPairs * L;
   C* Wt = RB + kTrPairs * L;
   C* Et = Wt + L;
-  double* red = reinterpret_cast<double*>(Et + L);   // 4*32
-  double* scl = red + 4 * 32;                         // 4 scales + 4 inverses
+  double* scl = reinterpret_cast<double*>(Et + L);   // 4 scales + 4 inverses
+  unsigned long long* red = reinterpret_cast<unsigned long long*>(scl + 8);   // 4*32
   const int tid = threadIdx.x, bd = blockDim.x;
   for (int i = tid; i < L; i += bd) {
     Wt[i] = a.w[i];
@@ -478,12 +505,15 @@ __global__ void __launch_bounds__(kFxThreads) k_transform(TrArgs a) {
   const bool sine = (a.kind == SDD_IDST || a.kind == SDD_DST);
   const int n_in = a.n_in, n_out = a.n_out;
   {  // per-row power-of-two balance of the pairs (see pow2_scale)
-    double m[4] = {0.0, 0.0, 0.0, 0.0};
+    unsigned long long m[4] = {0, 0, 0, 0};
 #pragma unroll
     for (int h = 0; h < 4; ++h) {
       const int r = r0 + h;
       if (r < a.rows)
-        for (int i = tid; i < n_in; i += bd) m[h] = fmax(m[h], fabs(a.in[(size_t)r * n_in + i]));
+        for (int i = tid; i < n_in; i += bd) {
+          const unsigned long long u = Bits<double>::absbits(a.in[(size_t)r * n_in + i]);
+          m[h] = u > m[h] ? u : m[h];
+        }
     }
     block_max_scales<double, 4>(m, red, scl);
   }
@@ -519,7 +549,7 @@ __global__ void __launch_bounds__(kFxThreads) k_transform(TrArgs a) {
           V[h] = make_double2(x, 0.0);
         } else {
           const C e = Et[k];
-          V[h] = make_double2(0.5 * (e.x * x + e.y * xr), 0.5 * (e.y * x - e.x * xr));
+          V[h] = make_double2(e.x * x + e.y * xr, e.y * x - e.x * xr);
         }
       }
       RA[idx] = make_double2(V[0].x - V[1].y, V[0].y + V[1].x);
@@ -567,9 +597,9 @@ __global__ void __launch_bounds__(kFxThreads) k_transform(TrArgs a) {
         const C Zm = Z[p * L + ((L - k) % L)];
         const C e = Et[k];
         if ((t & 1) == 0)
-          y = e.x * (Zk.x + Zm.x) * 0.5 + e.y * (Zk.y - Zm.y) * 0.5;
+          y = e.x * (Zk.x + Zm.x) + e.y * (Zk.y - Zm.y);
         else
-          y = e.x * (Zk.y + Zm.y) * 0.5 - e.y * (Zk.x - Zm.x) * 0.5;
+          y = e.x * (Zk.y + Zm.y) - e.y * (Zk.x - Zm.x);
         y *= ((!sine && k == 0) ? 1.0 / L : 2.0 / L) * scl[4 + t];
       }
       a.out[(size_t)r * n_out + s] = y;
@@ -614,7 +644,7 @@ static cudaError_t launch_fx_t(const FxArgs& a, int batch, cudaStream_t s) {
   static unsigned long long done = 0;
   cudaError_t e = ensure_smem_attr(k_fx_rows<T, MODE>, &done);
   if (e != cudaSuccess) return e;
-  k_fx_rows<T, MODE><<<dim3(a.nr, batch), kFxThreads, smem, s>>>(a);
+  k_fx_rows<T, MODE><<<dim3(a.nr, batch), kFxRowThreads, smem, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -671,7 +701,7 @@ cudaError_t launch_transform(int kind, int rows, int n_in, int n_out, const FftP
   a.e = fp->e64;
   a.in = in;
   a.out = out;
-  const size_t smem = (2 * kTrPairs + 2) * (size_t)fp->L * sizeof(double2) + (4 * 32 + 8) * sizeof(double);
+  const size_t smem = (2 * kTrPairs + 2) * (size_t)fp->L * sizeof(double2) + (4 * 32 + 8) * 8;
   static unsigned long long done = 0;
   cudaError_t e = ensure_smem_attr(k_transform, &done);
   if (e != cudaSuccess) return e;

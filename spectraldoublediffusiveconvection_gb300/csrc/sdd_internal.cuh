@@ -12,7 +12,8 @@ constexpr int kMaxStages = 16;   // FFT stages (radices) per length
 constexpr int kMaxRadix = 7;     // largest radix handled by the butterflies (2,3,4,5,7)
 constexpr int kMaxNr = 64;       // interior radial points supported by the chain kernel
 constexpr int kMaxM = 1024;      // theta modes supported
-constexpr int kFxThreads = 256;  // threads of the row kernels
+constexpr int kFxThreads = 256;  // threads of the rhs / theta / transform row kernels
+constexpr int kFxRowThreads = 512;  // threads of the nonlinear-term row kernel
 
 void set_cuda_error(cudaError_t e);
 
@@ -39,7 +40,7 @@ struct FftPlan {
   int nst = 0;
   int rad[kMaxStages] = {0};
   double2* w64 = nullptr;   // exp(-2 pi i k / L), k < L
-  double2* e64 = nullptr;   // exp(+i pi k / (2L)), k < L
+  double2* e64 = nullptr;   // 0.5 exp(+i pi k / (2L)), k < L
   float2* w32 = nullptr;
   float2* e32 = nullptr;
 };
@@ -101,9 +102,11 @@ struct ChainArgs {
   size_t f_stride;
   const double* sub;         // nullable: f -= sub (Newton residual), same layout
   size_t sub_stride;
-  const double* LinvA4, *LinvT, *LinvS;  // [M][nr][ldl]
-  const double* D2A4;        // [nr][nr]
+  const double* LinvA4, *LinvT, *LinvS;  // [M][nr cols][ldl] transposed blocks
+  const double* D2A4;        // [nr cols][ldl] transposed
   const double* ir2A4, *ir4A4;
+  const double* coefA4;      // [M][4] per jj: (dt bjt, dt bjt bj, bj, bjt), dt = Pr*dt, j = M - jj
+  const double* coefT, *coefS;  // [M][4] per jj: (2 dt (j+2), 0.5 if j == 0 else 1, 0, 0), j = M-1-jj
   double dtA4, dtT, dtS;     // Pr*dt, dt, Tau*dt
 };
 
