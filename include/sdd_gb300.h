@@ -152,6 +152,20 @@ typedef struct sdd_newton_result {
 int sdd_newton_gmres(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, double* X,
                      const sdd_newton_opts* opts, sdd_newton_result* results, void* stream);
 
+/* ---- nonlinear term without any allocation (no counterpart in the reference) --------------------- */
+/* NLIN_FX like sdd_nlin_fx, for callers that must not allocate device memory when they call it: hosts
+ * whose device memory is owned by another allocator (a framework's caching allocator, a serving runtime
+ * that reserves the whole budget up front) and latency-critical paths where cudaMalloc/cudaFree, which can
+ * synchronise the device, are not allowed.  The plan (created earlier) supplies the operators; X and F are
+ * the caller's.  The intermediate spectral outputs (4*N_fm*nr doubles per shell) go to a fixed scratch
+ * array of SDD_NOALLOC_SCRATCH_DOUBLES doubles (8 MiB) that the library keeps in device memory on every
+ * GPU it is loaded on until the process exits; batch*4*N_fm*nr above that limit returns
+ * SDD_ERR_UNSUPPORTED.  The first call on a device looks up the array's device address, so make that first
+ * call before any stream capture.  Every call on a device shares the one array (each call overwrites all
+ * of it that it reads, so stale contents never leak into a result): calls that overlap on the GPU race. */
+#define SDD_NOALLOC_SCRATCH_DOUBLES (1 << 20)
+int sdd_nlin_fx_noalloc(sdd_plan* plan, int batch, const double* X, double* F, void* stream);
+
 /* ---- instrumentation (no counterpart in the reference) ---------------------------------------- */
 /* Runs nsteps steps like sdd_step with CUDA events between the three kernels of each step and adds the
  * elapsed milliseconds to ms[0] (nonlinear-term row kernel), ms[1] (rhs kernel), ms[2] (chain kernel).

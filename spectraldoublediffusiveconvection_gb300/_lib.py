@@ -21,6 +21,8 @@ SDD_PREC_MIXED = 1
 
 SDD_IDCT, SDD_IDST, SDD_DCT, SDD_DST = 0, 1, 2, 3
 
+SDD_NOALLOC_SCRATCH_DOUBLES = 1 << 20
+
 _dp = ctypes.POINTER(ctypes.c_double)
 
 
@@ -73,6 +75,7 @@ SIGNATURES = [
     ("sdd_pdfx", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     ("sdd_newton_gmres", _I, [_VP, _I, _VP, _VP, _VP, ctypes.POINTER(NewtonOpts), ctypes.POINTER(NewtonResult),
                               _VP]),
+    ("sdd_nlin_fx_noalloc", _I, [_VP, _I, _VP, _VP, _VP]),
     ("sdd_step_profile", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, ctypes.POINTER(ctypes.c_double), _VP]),
     ("sdd_measure_fp64_peak", _I, [ctypes.POINTER(ctypes.c_double), _VP]),
 ]

@@ -710,3 +710,45 @@ extern "C" int sdd_measure_fp64_peak(double* gflops, void* stream) {
   *gflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e9;
   return SDD_OK;
 }
+
+// ---- NLIN_FX with a fixed, library-owned scratch (no allocation on the call) ------------------------
+// The scratch lives in a file-scope __device__ array.  In host code its name is only a host-side
+// stand-in, so its device address is looked up with cudaGetSymbolAddress once per device (with that
+// device current) and that address is what the kernels receive.
+static __device__ __align__(256) double g_noalloc_scratch[SDD_NOALLOC_SCRATCH_DOUBLES];
+static std::mutex g_noalloc_mu;
+static double* g_noalloc_ptr[64] = {nullptr};
+
+static int noalloc_scratch(int dev, double** out) {
+  if (dev < 0 || dev >= 64) return SDD_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || ptr == nullptr) {
+      set_cuda_error(e);
+      return SDD_ERR_CUDA;
+    }
+    g_noalloc_ptr[dev] = static_cast<double*>(ptr);
+  }
+  *out = g_noalloc_ptr[dev];
+  return SDD_OK;
+}
+
+extern "C" int sdd_nlin_fx_noalloc(sdd_plan* p, int batch, const double* X, double* F, void* stream) {
+  if (!p || batch < 1 || !X || !F) return SDD_ERR_ARG;
+  int dev = 0;
+  SDD_CUDA(cudaGetDevice(&dev));
+  if (dev != p->device) return SDD_ERR_ARG;
+  const size_t need = (size_t)batch * 4 * p->M * p->nr;
+  if (need > (size_t)SDD_NOALLOC_SCRATCH_DOUBLES) return SDD_ERR_UNSUPPORTED;
+  double* scratch = nullptr;
+  const int st = noalloc_scratch(dev, &scratch);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  // the row kernel writes every element of the batch's 4*N_fm*nr outputs before k_fx_finish reads them
+  FxArgs fa = fx_args(p, SDD_PREC_FP64, X, nullptr, scratch);
+  SDD_CUDA(launch_fx(fa, batch, 0, SDD_PREC_FP64, s));
+  SDD_CUDA(launch_fx_finish(p->M, p->nr, p->Dr, scratch, (size_t)4 * p->M * p->nr, F, shell_elems(p), batch, s));
+  return SDD_OK;
+}
