@@ -93,6 +93,7 @@ struct sdd_plan {
   // FP64 operators
   double *Dr, *D2r2, *ir4r2, *D2s, *ir2s, *D2A4, *ir2A4, *ir4A4, *rsq, *dT0, *gr;
   double *LinvA4, *LinvT, *LinvS;
+  double *ABA4;                     // transposed [A_j B_j] of the psi chain
   double *coefA4, *coefT, *coefS;   // per-step scalars of the chains
   // FP32 copies used by the mixed-precision nonlinear term
   float *Dr32, *D2r232, *ir4r232;
@@ -101,6 +102,7 @@ struct sdd_plan {
   double* out4;     // [B][4][M][nr]
   double* rhs;      // [B][3][M][nr]
   double* xtmp;     // [B][3][M][nr]
+  double* hbuf;     // [B][3][M][nr] h = Linv g of the chains
   void* base_tmp;   // [B][nr][9][P] (T precision), for DFX without a caller cache
   // Newton-GMRES workspace
   int nw_B, nw_m;
@@ -175,7 +177,7 @@ static int upload_linv(double** dst, const double* src, int M, int nr, int ldl) 
 static void free_plan(sdd_plan* p) {
   if (!p) return;
   double* d[] = {p->Dr, p->D2r2, p->ir4r2, p->D2s, p->ir2s, p->D2A4, p->ir2A4, p->ir4A4, p->rsq, p->dT0,
-                 p->gr, p->LinvA4, p->LinvT, p->LinvS, p->out4, p->rhs, p->xtmp, p->coefA4, p->coefT, p->coefS};
+                 p->gr, p->LinvA4, p->LinvT, p->LinvS, p->out4, p->rhs, p->xtmp, p->coefA4, p->coefT, p->coefS, p->ABA4, p->hbuf};
   for (double* x : d) cudaFree(x);
   cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232);
   cudaFree(p->base_tmp);
@@ -248,6 +250,35 @@ int sdd_plan_create(const sdd_plan_desc* d, sdd_plan** out) {
       free_plan(p);
       return st;
     }
+    // psi chain step matrices (exact algebra of b_test, Matrix_Operators.py:1149-1157):
+    //   A_j = Linv_j (c1 D2 + diag(alpha)), B_j = Linv_j diag(beta),
+    //   c1 = dt bjt, alpha = c1 bj IR4 - bjt IR2, beta = c1 IR4;  stored transposed, [A B] per mode.
+    const int ldl = p->ldl;
+    std::vector<double> AB((size_t)M * 2 * nr * ldl, 0.0);
+    std::vector<double> LD((size_t)nr * nr);
+    for (int jj = 0; jj < M; ++jj) {
+      const double c1 = cA[4 * jj], bj = cA[4 * jj + 2], bjt = cA[4 * jj + 3];
+      const double* L = d->Linv_A4 + (size_t)jj * nr * nr;
+      for (int i = 0; i < nr; ++i)
+        for (int c = 0; c < nr; ++c) {
+          double acc = 0.0;
+          for (int k = 0; k < nr; ++k) acc += L[i * nr + k] * d->D2_A4[k * nr + c];
+          LD[(size_t)i * nr + c] = acc;
+        }
+      double* blk = AB.data() + (size_t)jj * 2 * nr * ldl;
+      for (int c = 0; c < nr; ++c) {
+        const double alpha = c1 * bj * d->ir4_A4[c] - bjt * d->ir2_A4[c];
+        const double beta = c1 * d->ir4_A4[c];
+        for (int i = 0; i < nr; ++i) {
+          blk[(size_t)c * ldl + i] = c1 * LD[(size_t)i * nr + c] + L[i * nr + c] * alpha;
+          blk[(size_t)(nr + c) * ldl + i] = L[i * nr + c] * beta;
+        }
+      }
+    }
+    if ((st = upload(&p->ABA4, AB.data(), AB.size()))) {
+      free_plan(p);
+      return st;
+    }
   }
   *out = p;
   return SDD_OK;
@@ -266,8 +297,8 @@ static size_t shell_elems(const sdd_plan* p) { return (size_t)3 * p->M * p->nr; 
 int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   if (!p || max_batch < 1) return SDD_ERR_ARG;
   if (max_batch <= p->ws_batch) return SDD_OK;
-  cudaFree(p->out4); cudaFree(p->rhs); cudaFree(p->xtmp); cudaFree(p->base_tmp);
-  p->out4 = p->rhs = p->xtmp = nullptr;
+  cudaFree(p->out4); cudaFree(p->rhs); cudaFree(p->xtmp); cudaFree(p->base_tmp); cudaFree(p->hbuf);
+  p->out4 = p->rhs = p->xtmp = p->hbuf = nullptr;
   p->base_tmp = nullptr;
   p->ws_batch = 0;
   const size_t se = shell_elems(p);
@@ -275,6 +306,7 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   SDD_CUDA(cudaMalloc(&p->out4, (size_t)max_batch * 4 * p->M * p->nr * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->rhs, (size_t)max_batch * se * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->xtmp, (size_t)max_batch * se * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->hbuf, (size_t)max_batch * se * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->base_tmp, (size_t)max_batch * be * sizeof(double)));
   p->ws_batch = max_batch;
   return SDD_OK;
@@ -323,7 +355,8 @@ static ChainArgs chain_args(const sdd_plan* p, const double* g, double* f, const
   a.f = f; a.f_stride = shell_elems(p);
   a.sub = sub; a.sub_stride = shell_elems(p);
   a.LinvA4 = p->LinvA4; a.LinvT = p->LinvT; a.LinvS = p->LinvS;
-  a.D2A4 = p->D2A4; a.ir2A4 = p->ir2A4; a.ir4A4 = p->ir4A4;
+  a.ABA4 = p->ABA4; a.ir2A4 = p->ir2A4; a.ir4A4 = p->ir4A4;
+  a.h = p->hbuf;
   a.coefA4 = p->coefA4; a.coefT = p->coefT; a.coefS = p->coefS;
   a.dtA4 = p->Pr * p->dt; a.dtT = p->dt; a.dtS = p->Tau * p->dt;
   return a;
@@ -388,7 +421,9 @@ int sdd_nlin_dfx(sdd_plan* p, int batch, const double* dv, const double* X, cons
 }
 
 int sdd_a4_bsub(sdd_plan* p, int batch, const double* g, double* f, void* stream) {
-  if (!p || batch < 1 || !g || !f) return SDD_ERR_ARG;
+  if (!g || !f) return SDD_ERR_ARG;
+  int st = check_plan(p, batch);
+  if (st) return st;
   ChainArgs a = chain_args(p, g, f, nullptr);
   a.g_stride = a.f_stride = (size_t)p->M * p->nr;
   a.field0 = 0;
@@ -398,7 +433,9 @@ int sdd_a4_bsub(sdd_plan* p, int batch, const double* g, double* f, void* stream
 }
 
 int sdd_nab2_bsub(sdd_plan* p, int field, int batch, const double* g, double* f, void* stream) {
-  if (!p || batch < 1 || !g || !f || (field != 1 && field != 2)) return SDD_ERR_ARG;
+  if (!g || !f || (field != 1 && field != 2)) return SDD_ERR_ARG;
+  int st = check_plan(p, batch);
+  if (st) return st;
   const size_t N = (size_t)p->M * p->nr;
   ChainArgs a = chain_args(p, g, f, nullptr);
   a.g_stride = a.f_stride = N;

@@ -103,7 +103,8 @@ struct ChainArgs {
   const double* sub;         // nullable: f -= sub (Newton residual), same layout
   size_t sub_stride;
   const double* LinvA4, *LinvT, *LinvS;  // [M][nr cols][ldl] transposed blocks
-  const double* D2A4;        // [nr cols][ldl] transposed
+  const double* ABA4;        // [M][2 nr cols][ldl]: transposed [A_j B_j] of the psi chain
+  double* h;                 // [shell][3][M][nr] h = Linv g (same strides as f)
   const double* ir2A4, *ir4A4;
   const double* coefA4;      // [M][4] per jj: (dt bjt, dt bjt bj, bj, bjt), dt = Pr*dt, j = M - jj
   const double* coefT, *coefS;  // [M][4] per jj: (2 dt (j+2), 0.5 if j == 0 else 1, 0, 0), j = M-1-jj
