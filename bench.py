@@ -205,6 +205,35 @@ def bench_reference(args):
 
 
 # ------------------------------------------------------------------------------------------------
+# batched workload: 64 shells of uneven (N_r, N_theta) and Ra_T, one captured graph per launch
+# ------------------------------------------------------------------------------------------------
+def bench_batched(device, precision, steps=1000, steps_per_launch=10, n_shells=64):
+    import numpy as np
+    import torch
+    from spectraldoublediffusiveconvection_gb300.batch import ShellBatch, config4_shells
+    shells = config4_shells(n_shells, seed=1234)
+    b = ShellBatch(shells, d=2.0, dt=1e-3, Pr=1.0, Tau=0.01, Ra_s=500.0, precision=precision, device=device)
+    tuning = b.autotune(steps_per_launch=steps_per_launch, reps=2)
+    launches = max(1, steps // steps_per_launch)
+    b.replay(1)
+    torch.cuda.synchronize(device)
+    stream = torch.cuda.current_stream(device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.replay(launches)
+    e1.record(stream)
+    torch.cuda.synchronize(device)
+    sec = e0.elapsed_time(e1) * 1e-3
+    finite = all(np.isfinite(x).all() for x in b.states())
+    shell_steps = n_shells * launches * steps_per_launch
+    groups = sorted(((g.plan.N_r, g.plan.N_fm, len(g.idx)) for g in b.groups), reverse=True)
+    return {"shell_steps_per_s": shell_steps / sec, "seconds": sec, "shells": n_shells,
+            "steps_per_shell": launches * steps_per_launch, "precision": precision,
+            "graph": f"{launches} launches of one CUDA graph, {steps_per_launch} steps of all groups each",
+            "groups": [f"N_r={a} N_theta={c} x{n}" for a, c, n in groups], "tuning": tuning, "finite": finite}
+
+
+# ------------------------------------------------------------------------------------------------
 # GB300 arm
 # ------------------------------------------------------------------------------------------------
 def bench_gb300(args):
@@ -347,6 +376,18 @@ def bench_gb300(args):
                   "matvecs": res["matvecs"], "residual0": res["residual0"], "residual": res["residual"],
                   "converged": res["converged"], "tol": 1e-10, "restart": 50}
 
+    batched = None
+    if not args.no_batched:
+        import numpy as np  # noqa: F401
+        bm = bench_batched(device, "mixed")
+        bd = bench_batched(device, "fp64")
+        plain = value / ws
+        batched = {"mixed": bm, "fp64": bd,
+                   "mixed_vs_plain_single_shell": bm["shell_steps_per_s"] / plain,
+                   "fp64_vs_plain_single_shell": bd["shell_steps_per_s"] / plain,
+                   "workload": "64 shells, N_r in {20,24,30,36}, N_theta in {64,128,256,384}, Ra_T ~ U[6000,12000],"
+                               " Ra_S=500, Pr=1, Tau=0.01, dt=1e-3, 1000 steps each (seed 1234)"}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         r = run_cpu_baseline(seconds=args.cpu_seconds, threads=1, steps_per_sample=5)
@@ -365,7 +406,7 @@ def bench_gb300(args):
                         "d2h_bytes_per_step": nbytes,
                         "api": "Plan.step on a pinned host state copied in/out every bench step"},
                 "gpu_launches": args.steps * chunk * 3,
-                "roofline": roofline, "cpu_baseline": cpu, "clocks": ck, "newton": newton}
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": ck, "newton": newton, "batched": batched}
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
@@ -384,6 +425,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-newton", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -1,0 +1,168 @@
+"""Many independent shells of uneven (N_r, N_theta) and Ra_T advanced together on one GPU.
+
+The reference advances one shell per process (Main.py:228-329).  Here a batch of shells is grouped by
+shape; every group shares one device plan (the operators depend on (N_fm, N_r, d, dt, Pr, Tau) only, not
+on Ra_T, Main.py:179-225) and holds its shells' states contiguously on the device.  A batched step
+launches the plan's kernels once per group; ``capture`` records ``steps_per_launch`` steps of every group
+into ONE CUDA graph, each group on its own stream branch so the groups run concurrently, and ``replay``
+then advances every shell with a single graph launch.  ``autotune`` picks each group's chain layout
+(one lane per matrix row, or rows split over four warps) by timing the captured graph, and records the
+choice.
+"""
+import time
+
+import numpy as np
+
+from .plan import get_plan
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class _Group:
+    def __init__(self, plan, idx, X, Ra, Ra_s, device):
+        torch = _torch()
+        self.plan = plan
+        self.idx = list(idx)                 # positions of the shells in the caller's list
+        self.X = torch.from_numpy(np.ascontiguousarray(np.stack(X))).to(device)
+        self.Ra = torch.tensor(Ra, dtype=torch.float64, device=device)
+        self.Ras = torch.tensor(Ra_s, dtype=torch.float64, device=device)
+        self.stream = torch.cuda.Stream(device=device)
+
+    @property
+    def shape(self):
+        return (self.plan.N_r, self.plan.N_fm)
+
+
+class ShellBatch:
+    """shells: list of dicts with keys N_r, N_theta, Ra (Ra_T) and optionally Ra_s, X (initial state,
+    flat numpy array in the reference layout; seeded if absent) and symmetric."""
+
+    def __init__(self, shells, d=2.0, dt=1e-3, Pr=1.0, Tau=0.01, Ra_s=500.0, precision="mixed",
+                 device=None, seed=1234):
+        torch = _torch()
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.d, self.dt, self.Pr, self.Tau, self.precision = d, dt, Pr, Tau, precision
+        self.n_shells = len(shells)
+        groups = {}
+        rng = np.random.default_rng(seed)
+        for i, s in enumerate(shells):
+            key = (int(s["N_r"]), int(s["N_theta"]), bool(s.get("symmetric", False)))
+            groups.setdefault(key, []).append(i)
+        self.groups = []
+        for (N_r, M, sym), idx in sorted(groups.items(), key=lambda kv: -kv[0][1] * kv[0][0]):
+            plan = get_plan(M, N_r, d, dt, Pr, Tau, symmetric=sym, precision=precision, device=self.device)
+            X = []
+            for i in idx:
+                x0 = shells[i].get("X")
+                X.append(np.asarray(x0, dtype=np.float64) if x0 is not None else
+                         _seeded(M, N_r - 1, rng))
+            g = _Group(plan, idx, X, [float(shells[i]["Ra"]) for i in idx],
+                       [float(shells[i].get("Ra_s", Ra_s)) for i in idx], self.device)
+            plan.reserve(len(idx))
+            self.groups.append(g)
+        self.graph = None
+        self.steps_per_launch = 0
+        self.tuning = {}
+
+    # ---- eager ---------------------------------------------------------------------------------
+    def step(self, nsteps=1):
+        """Advance every shell by nsteps (one launch sequence per group, groups on their own streams)."""
+        torch = _torch()
+        main = torch.cuda.current_stream(self.device)
+        for g in self.groups:
+            g.stream.wait_stream(main)
+            with torch.cuda.stream(g.stream):
+                g.plan.step(g.X, g.Ra, g.Ras, nsteps=nsteps, out=g.X)
+        for g in self.groups:
+            main.wait_stream(g.stream)
+
+    # ---- graph ---------------------------------------------------------------------------------
+    def capture(self, steps_per_launch=10):
+        """Record steps_per_launch steps of every group into one CUDA graph (groups as parallel branches)."""
+        torch = _torch()
+        saved = [g.X.clone() for g in self.groups]
+        self.step(1)                      # kernel attributes and workspaces are set up outside capture
+        for g, x in zip(self.groups, saved):
+            g.X.copy_(x)
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        cap = torch.cuda.Stream(device=self.device)
+        with torch.cuda.stream(cap):
+            with torch.cuda.graph(g, stream=cap, capture_error_mode="thread_local"):
+                for grp in self.groups:
+                    grp.stream.wait_stream(cap)
+                    with torch.cuda.stream(grp.stream):
+                        grp.plan.step(grp.X, grp.Ra, grp.Ras, nsteps=steps_per_launch, out=grp.X)
+                for grp in self.groups:
+                    cap.wait_stream(grp.stream)
+        self.graph = g
+        self.steps_per_launch = steps_per_launch
+        return g
+
+    def replay(self, launches=1):
+        for _ in range(launches):
+            self.graph.replay()
+
+    # ---- tuning --------------------------------------------------------------------------------
+    def _time_graph(self, reps):
+        torch = _torch()
+        self.capture(self.steps_per_launch or 5)
+        self.graph.replay()
+        torch.cuda.synchronize(self.device)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            self.graph.replay()
+        torch.cuda.synchronize(self.device)
+        return (time.perf_counter() - t0) / reps
+
+    def autotune(self, steps_per_launch=5, reps=3, layouts=(1, 4)):
+        """Greedy per-group choice of the chain layout minimising the time of one graph launch.  The
+        shells' states are restored afterwards: tuning does not advance them."""
+        saved = [g.X.clone() for g in self.groups]
+        self.steps_per_launch = steps_per_launch
+        best = self._time_graph(reps)
+        for g in self.groups:
+            choice = getattr(g.plan, "chain_layout", 0)
+            for lay in layouts:
+                g.plan.set_chain_layout(lay)
+                t = self._time_graph(reps)
+                if t < best:
+                    best, choice = t, lay
+            g.plan.set_chain_layout(choice)
+            self.tuning["N_r=%d,N_theta=%d" % g.shape] = {"chain_layout": choice}
+        for g, x in zip(self.groups, saved):
+            g.X.copy_(x)
+        self.capture(steps_per_launch)
+        return dict(self.tuning, seconds_per_launch=best)
+
+    # ---- results -------------------------------------------------------------------------------
+    def states(self):
+        """Per-shell states (numpy), in the caller's order."""
+        out = [None] * self.n_shells
+        for g in self.groups:
+            Xh = g.X.cpu().numpy()
+            for k, i in enumerate(g.idx):
+                out[i] = Xh[k].copy()
+        return out
+
+
+def _seeded(M, nr, rng):
+    k = np.arange(M)[None, :]
+    n = np.arange(nr)[:, None]
+    amp = 1e-3 * np.exp(-k / 8.0) * np.exp(-n / 4.0)
+    P, T, S = [rng.standard_normal((nr, M)) * amp for _ in range(3)]
+    X = np.zeros((3, M, nr))
+    X[0], X[1], X[2] = P.T, T.T, S.T
+    return X.reshape(-1)
+
+
+def config4_shells(n=64, seed=1234):
+    """The batched workload: N_r in {20,24,30,36}, N_theta in {64,128,256,384}, Ra_T ~ U[6000,12000]."""
+    rng = np.random.default_rng(seed)
+    Nr = rng.choice([20, 24, 30, 36], size=n)
+    Nt = rng.choice([64, 128, 256, 384], size=n)
+    Ra = rng.uniform(6000.0, 12000.0, size=n)
+    return [dict(N_r=int(a), N_theta=int(b), Ra=float(c)) for a, b, c in zip(Nr, Nt, Ra)]

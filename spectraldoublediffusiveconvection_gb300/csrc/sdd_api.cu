@@ -88,6 +88,7 @@ using namespace sdd;
 // ---- plan ---------------------------------------------------------------------------------------
 struct sdd_plan {
   int M, nr, P, ldl, sym, prec, device;
+  int chain_layout;
   double dt, Pr, Tau;
   const FftPlan* fft;
   // FP64 operators
@@ -290,6 +291,12 @@ int sdd_plan_destroy(sdd_plan* p) {
   return SDD_OK;
 }
 
+int sdd_plan_set_chain_layout(sdd_plan* p, int layout) {
+  if (!p || (layout != 0 && layout != 1 && layout != 4)) return SDD_ERR_ARG;
+  p->chain_layout = layout;
+  return SDD_OK;
+}
+
 size_t sdd_plan_base_cache_elems(const sdd_plan* p) { return p ? (size_t)9 * p->nr * p->P : 0; }
 
 static size_t shell_elems(const sdd_plan* p) { return (size_t)3 * p->M * p->nr; }
@@ -349,7 +356,7 @@ static RhsArgs rhs_args(const sdd_plan* p, const double* X, const double* out4, 
 
 static ChainArgs chain_args(const sdd_plan* p, const double* g, double* f, const double* sub) {
   ChainArgs a;
-  a.M = p->M; a.nr = p->nr; a.ldl = p->ldl; a.sym = p->sym; a.field0 = 0;
+  a.M = p->M; a.nr = p->nr; a.ldl = p->ldl; a.sym = p->sym; a.field0 = 0; a.layout = p->chain_layout;
   a.field_off = (size_t)p->M * p->nr;
   a.g = g; a.g_stride = shell_elems(p);
   a.f = f; a.f_stride = shell_elems(p);

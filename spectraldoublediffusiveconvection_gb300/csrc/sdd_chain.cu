@@ -213,11 +213,12 @@ cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStre
     if (sms <= 0) sms = 1;
   }
   const dim3 grid(2 * nfields, batch);
-  if (2 * nfields * batch <= sms && a.nr <= 32) {
+  const bool split = a.layout == 4 || (a.layout == 0 && 2 * nfields * batch <= sms);
+  if (split && a.nr <= 32) {
     static unsigned long long done = 0;
     if ((e = ensure_smem_attr(k_chain<4>, &done)) != cudaSuccess) return e;
     k_chain<4><<<grid, 128, smem, s>>>(a);
-  } else if (2 * nfields * batch <= sms) {
+  } else if (split) {
     static unsigned long long done = 0;
     if ((e = ensure_smem_attr(k_chain<2>, &done)) != cudaSuccess) return e;
     k_chain<2><<<grid, 128, smem, s>>>(a);

@@ -95,6 +95,7 @@ struct RhsArgs {
 struct ChainArgs {
   int M, nr, ldl, sym;
   int field0;                // first field handled (blockIdx.x/2 + field0)
+  int layout;                // 0 auto, 1 one lane per row, 4 rows split over 4 warps
   size_t field_off;          // doubles between field blocks (N_fm*nr, or 0 when g/f point at one block)
   const double* g;           // rhs [shell][3][M][nr]
   size_t g_stride;

@@ -108,6 +108,17 @@ class Plan:
             return v.contiguous()
         return torch.full((batch,), float(v), dtype=torch.float64, device=self.device)
 
+    def reserve(self, batch):
+        """Allocate the plan's workspace for up to ``batch`` shells now (required before graph capture)."""
+        torch = _torch()
+        with torch.cuda.device(self.device):
+            _lib.check(self._L.sdd_plan_reserve(self._h, int(batch)), "sdd_plan_reserve")
+
+    def set_chain_layout(self, layout):
+        """0 automatic, 1 one lane per row, 4 rows split over 4 warps (see sdd_plan_set_chain_layout)."""
+        _lib.check(self._L.sdd_plan_set_chain_layout(self._h, int(layout)), "sdd_plan_set_chain_layout")
+        self.chain_layout = int(layout)
+
     def new_state(self, batch=1):
         torch = _torch()
         return torch.zeros((batch, self.n_state), dtype=torch.float64, device=self.device)
