@@ -21,7 +21,8 @@ import os
 import sys
 import types
 
-import numpy as np
+sys.dont_write_bytecode = True      # never write __pycache__ into the (read-only) reference tree
+import numpy as np  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
