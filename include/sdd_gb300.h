@@ -156,6 +156,38 @@ typedef struct sdd_newton_result {
 int sdd_newton_gmres(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, double* X,
                      const sdd_newton_opts* opts, sdd_newton_result* results, void* stream);
 
+/* ---- pseudo-arclength continuation step (Main.py:742-955 _ContinC) ------------------------------ */
+/* One step along the branch of steady states in Ra_T.  Predictor: with dt = 1 the reference always
+ * recomputes the tangent from DF_X xi = -DF_mu (Main.py:845-862): mu_dot = sign/sqrt(1 + delta(|xi|-1)),
+ * X_dot = mu_dot xi, delta = 1/(3 N_fm nr); prediction Y = Y0 + ds Y_dot.  Corrector: Newton on the
+ * bordered system [[DF_X, DF_mu], [delta X_dot^T, (1-delta) mu_dot]] (Main.py:914-920) solved by GMRES; ds is
+ * halved after max_corrector iterations (Main.py:888-899).  The stop is absolute: |F(X,Ra)|_2 <= tol and
+ * |arclength residual| <= tol.  New tangent: DG y = e_last, normalised (Main.py:944-953).
+ * X (batch x 3 N_fm nr) and Ra (batch) are device arrays updated in place; X_dot (device, batch x n)
+ * receives the new tangent's state part; sign and ds are host arrays (batch). */
+typedef struct sdd_contin_opts {
+  double tol;              /* absolute corrector tolerance                                          */
+  double gmres_rtol;       /* corrector inner tolerance relative to the bordered residual (:919)    */
+  double tangent_rtol;     /* predictor/tangent inner tolerance (the reference uses tol_newton)    */
+  int32_t restart, max_restarts;
+  int32_t max_corrector;   /* corrector iterations before ds is halved (5)                         */
+  int32_t max_halvings;
+  int32_t mixed_matvec;
+  int32_t pad;
+} sdd_contin_opts;
+
+typedef struct sdd_contin_result {
+  double residual;         /* |F(X,Ra)|_2 at exit                                                  */
+  double arclength;        /* |arclength residual| at exit                                          */
+  double ds;               /* step for the next call (doubled after <= 4 corrector iterations)     */
+  double Ra_dot;           /* parameter component of the new normalised tangent                    */
+  int32_t corrector_iters, halvings, matvecs, converged;
+} sdd_contin_result;
+
+int sdd_contin_step(sdd_plan* plan, int batch, double* X, double* Ra, const double* Ra_s, double* X_dot,
+                    const double* sign, const double* ds, const sdd_contin_opts* opts,
+                    sdd_contin_result* results, void* stream);
+
 /* ---- nonlinear term without any allocation (no counterpart in the reference) --------------------- */
 /* NLIN_FX like sdd_nlin_fx, for callers that must not allocate device memory when they call it: hosts
  * whose device memory is owned by another allocator (a framework's caching allocator, a serving runtime

@@ -185,3 +185,127 @@ def _Newton(X, Ra, Ra_s, Tau, Pr, d, N_fm, N_r, symmetric, dt=1, tol_newton=1e-0
     Xh = Xd.cpu().numpy().ravel()
     Norm, KE, NuT, NuS = _diagnostics(Xh, plan.arrays["R"], plan.arrays["D"], N_fm, N_r - 1, d, symmetric)
     return (Xh if was_np else Xd.reshape(-1)), Norm, KE, NuT, NuS, True
+
+
+class result():
+    """Main.py:677-714: record of a continuation run."""
+
+    def __init__(self):
+        self.NuT = []
+        self.NuS = []
+        self.KE = []
+        self.Norm = []
+        self.Ra = []
+        self.Ra_dot = []
+        self.Y_FOLD = []
+        self.X_DATA = []
+        self.Ra_DATA = []
+        self.Iterations = 0
+
+    def __str__(self):
+        i = self.Iterations
+        return ('Continuation succeed \n' + 'Total iterations  = ' + str(i) + '\n' + 'Ra                = '
+                + str(self.Ra[i]) + '\n' + 'Ra_dot            = ' + str(self.Ra_dot[i]) + '\n'
+                + 'NuT               = ' + str(self.NuT[i]) + '\n' + 'NuS               = ' + str(self.NuS[i])
+                + '\n' + 'KE                = ' + str(self.KE[i]) + '\n')
+
+
+def _NewtonC(Y, sign, ds, **kwargs_f):
+    """Main.py:717-739: natural-parameter step Ra -> Ra + sign*ds solved by Newton; ds doubles on success
+    and halves on failure."""
+    Y = np.asarray(Y.cpu() if hasattr(Y, "cpu") else Y, dtype=np.float64)
+    X = Y[0:-1].copy()
+    Ra = Y[-1] + sign * ds
+    kwargs_f = dict(kwargs_f)
+    kwargs_f["Ra"] = Ra
+    kwargs_f.setdefault("tol_newton", 1e-08)
+    X_new, Norm, KE, NuT, NuS, exitcode = _Newton(X, **kwargs_f)
+    if exitcode:
+        return np.hstack((X_new, Ra)), sign, ds * 2, Norm, KE, NuT, NuS, exitcode
+    return Y, sign, ds * 0.5, Norm, KE, NuT, NuS, exitcode
+
+
+def _ContinC(Y_0_dot, Y_0, sign, ds, Ra, Ra_s, Tau, Pr, d, N_fm, N_r, symmetric, dt=1, tol_newton=1e-08,
+             tol_gmres=1e-04, Krylov_Space_Size=300):
+    """Main.py:742-955: one pseudo-arclength step on the GPU (sdd_contin_step).
+
+    Returns (Y_dot, Y, sign, ds, Norm, KE, NuT, NuS, True) like the reference.  The corrector stops on the
+    absolute residuals |F(X,Ra)|_2 <= tol_newton and |arclength residual| <= tol_newton; a step that cannot be
+    corrected after ds has been halved raises ValueError as the reference does (Main.py:895)."""
+    import torch
+    plan = get_plan(N_fm, N_r, d, dt, Pr, Tau, symmetric)
+    Y_0 = np.asarray(Y_0.cpu() if hasattr(Y_0, "cpu") else Y_0, dtype=np.float64)
+    X = torch.from_numpy(Y_0[0:-1].copy()).to(plan.device).reshape(1, -1)
+    if symmetric:
+        X = X * torch.from_numpy(Eq_SYM(Y_0[0:-1], plan.arrays["R"])).to(plan.device).reshape(1, -1)
+    Ra_d = torch.tensor([float(Y_0[-1])], dtype=torch.float64, device=plan.device)
+    Xd, res = plan.contin_step(X, Ra_d, Ra_s, sign, ds, tol=tol_newton, restart=min(int(Krylov_Space_Size), 50),
+                               gmres_rtol=tol_gmres, tangent_rtol=tol_newton)
+    r = res[0]
+    if not r["converged"]:
+        raise ValueError("\n Step-size ds has become too small terminating \n")
+    Xh = X.cpu().numpy().ravel()
+    Y = np.hstack((Xh, float(Ra_d.item())))
+    Y_dot = np.hstack((Xd.cpu().numpy().ravel(), r["Ra_dot"]))
+    Norm, KE, NuT, NuS = _diagnostics(Xh, plan.arrays["R"], plan.arrays["D"], N_fm, N_r - 1, d, symmetric)
+    return Y_dot, Y, sign, r["ds"], Norm, KE, NuT, NuS, True
+
+
+def _Continuation(filename, N_steps, sign, Y, **kwargs):
+    """Main.py:958-1045: branch following; natural-parameter Newton steps while ds > 1, pseudo-arclength
+    steps otherwise, fold detection by a sign change of Ra_dot.  Returns the ``result`` record (the reference
+    returns None and writes it to ``filename``; the file is written here only if h5py is importable)."""
+    Y = np.array(Y, dtype=np.float64, copy=True)
+    Y_dot = 0.0 * Y
+    ds, ds_min, ds_max = 0.01, 1.0, 10.0
+    Result = result()
+    while Result.Iterations < N_steps:
+        Y_dot_new = None
+        if ds > ds_min:
+            OUT = _NewtonC(Y, sign, ds, **kwargs)
+            if OUT[-1] is False:
+                print('Switching to arc-length \n')
+                Y_dot_new, Y_new, sign, ds, Norm, KE, NuT, NuS, _ = _ContinC(Y_dot, Y, sign, ds, **kwargs)
+            else:
+                Y_new, sign, ds, Norm, KE, NuT, NuS = OUT[0], OUT[1], OUT[2], OUT[3], OUT[4], OUT[5], OUT[6]
+            if ds > ds_max:
+                ds = ds_max
+        else:
+            Y_dot_new, Y_new, sign, ds, Norm, KE, NuT, NuS, _ = _ContinC(Y_dot, Y, sign, ds, **kwargs)
+            if (Y_dot_new[-1] * Y_dot[-1]) < 0:
+                Result.Y_FOLD.append(Y_new)
+            sign = 1.0 if Y_new[-1] > Y[-1] else -1.0
+        Y = Y_new.copy()
+        Y_dot = Y_dot_new.copy() if Y_dot_new is not None else 0.0 * Y
+        Result.Ra.append(Y[-1])
+        Result.Ra_dot.append(Y_dot[-1])
+        Result.Norm.append(Norm)
+        Result.KE.append(KE)
+        Result.NuT.append(NuT)
+        Result.NuS.append(NuS)
+        if Result.Iterations % 5 == 0:
+            Result.X_DATA.append(Y[0:-1])
+            Result.Ra_DATA.append(Y[-1])
+            if filename:
+                _write_continuation_h5(filename, Result, kwargs)
+        print(Result, flush=True)
+        Result.Iterations += 1
+    return Result
+
+
+def _write_continuation_h5(filename, Result, kwargs):
+    try:
+        import h5py
+    except ImportError:
+        warnings.warn("h5py is not installed: %s was not written" % filename)
+        return
+    with h5py.File(filename, 'w') as f:
+        c = f.create_group("Checkpoints")
+        c['X_DATA'] = Result.X_DATA
+        c['Ra_DATA'] = Result.Ra_DATA
+        p = f.create_group("Parameters")
+        for k, v in kwargs.items():
+            p[k] = v
+        b = f.create_group("Bifurcation")
+        for k, v in vars(Result).items():
+            b.create_dataset(k, data=v)

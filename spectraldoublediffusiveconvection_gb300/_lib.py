@@ -52,6 +52,20 @@ class NewtonResult(ctypes.Structure):
                 ("converged", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
+class ContinOpts(ctypes.Structure):
+    """Mirror of ``sdd_contin_opts``."""
+    _fields_ = [("tol", ctypes.c_double), ("gmres_rtol", ctypes.c_double), ("tangent_rtol", ctypes.c_double),
+                ("restart", ctypes.c_int32), ("max_restarts", ctypes.c_int32), ("max_corrector", ctypes.c_int32),
+                ("max_halvings", ctypes.c_int32), ("mixed_matvec", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+class ContinResult(ctypes.Structure):
+    """Mirror of ``sdd_contin_result``."""
+    _fields_ = [("residual", ctypes.c_double), ("arclength", ctypes.c_double), ("ds", ctypes.c_double),
+                ("Ra_dot", ctypes.c_double), ("corrector_iters", ctypes.c_int32), ("halvings", ctypes.c_int32),
+                ("matvecs", ctypes.c_int32), ("converged", ctypes.c_int32)]
+
+
 # (name, restype, argtypes) of every exported symbol; the CPU test checks the header declares these.
 _VP = ctypes.c_void_p
 _I = ctypes.c_int
@@ -76,6 +90,9 @@ SIGNATURES = [
     ("sdd_pdfx", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     ("sdd_newton_gmres", _I, [_VP, _I, _VP, _VP, _VP, ctypes.POINTER(NewtonOpts), ctypes.POINTER(NewtonResult),
                               _VP]),
+    ("sdd_contin_step", _I, [_VP, _I, _VP, _VP, _VP, _VP, ctypes.POINTER(ctypes.c_double),
+                             ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ContinOpts),
+                             ctypes.POINTER(ContinResult), _VP]),
     ("sdd_nlin_fx_noalloc", _I, [_VP, _I, _VP, _VP, _VP]),
     ("sdd_step_profile", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, ctypes.POINTER(ctypes.c_double), _VP]),
     ("sdd_measure_fp64_peak", _I, [ctypes.POINTER(ctypes.c_double), _VP]),

@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -105,14 +106,14 @@ struct sdd_plan {
   double* xtmp;     // [B][3][M][nr]
   double* hbuf;     // [B][3][M][nr] h = Linv g of the chains
   void* base_tmp;   // [B][nr][9][P] (T precision), for DFX without a caller cache
-  // Newton-GMRES workspace
-  int nw_B, nw_m;
-  double *nw_V, *nw_F, *nw_x, *nw_w, *nw_r, *nw_part, *nw_nrm2, *nw_base64;
-  float* nw_base32;
-  double *nw_small;   // H, hcol, h2, cs, sn, g, y, beta, inv, resid, target
-  int* nw_ismall;     // active, solve, kb, newton mask
-  double* h_dbl;      // pinned host: nrm2 / resid
-  int* h_int;         // pinned host: active flags
+  // Krylov / Newton / continuation workspace (grown on demand)
+  int sv_B, sv_m;
+  double *kv_V, *kv_w, *kv_r, *kv_part, *kv_nrm2, *kv_small, *kv_dot;
+  int* kv_ismall;
+  double* h_dbl;      // pinned host scalars
+  int* h_int;         // pinned host flags
+  double *sv_F, *sv_x, *sv_X0, *sv_Xd, *sv_t, *sv_G, *sv_Jmu, *sv_g, *sv_base64, *sv_dev;
+  float* sv_base32;
 };
 
 extern "C" {
@@ -175,6 +176,24 @@ static int upload_linv(double** dst, const double* src, int M, int nr, int ldl) 
   return SDD_OK;
 }
 
+static void solver_free(sdd_plan* p) {
+  double* d[] = {p->kv_V, p->kv_w, p->kv_r, p->kv_part, p->kv_nrm2, p->kv_small, p->kv_dot, p->sv_F, p->sv_x,
+                 p->sv_X0, p->sv_Xd, p->sv_t, p->sv_G, p->sv_Jmu, p->sv_g, p->sv_base64, p->sv_dev};
+  for (double* x : d) cudaFree(x);
+  cudaFree(p->sv_base32);
+  cudaFree(p->kv_ismall);
+  cudaFreeHost(p->h_dbl);
+  cudaFreeHost(p->h_int);
+  p->kv_V = p->kv_w = p->kv_r = p->kv_part = p->kv_nrm2 = p->kv_small = p->kv_dot = nullptr;
+  p->sv_F = p->sv_x = p->sv_X0 = p->sv_Xd = p->sv_t = p->sv_G = p->sv_Jmu = p->sv_g = p->sv_base64 = nullptr;
+  p->sv_dev = nullptr;
+  p->sv_base32 = nullptr;
+  p->kv_ismall = nullptr;
+  p->h_dbl = nullptr;
+  p->h_int = nullptr;
+  p->sv_B = p->sv_m = 0;
+}
+
 static void free_plan(sdd_plan* p) {
   if (!p) return;
   double* d[] = {p->Dr, p->D2r2, p->ir4r2, p->D2s, p->ir2s, p->D2A4, p->ir2A4, p->ir4A4, p->rsq, p->dT0,
@@ -182,12 +201,7 @@ static void free_plan(sdd_plan* p) {
   for (double* x : d) cudaFree(x);
   cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232);
   cudaFree(p->base_tmp);
-  double* nw[] = {p->nw_V, p->nw_F, p->nw_x, p->nw_w, p->nw_r, p->nw_part, p->nw_nrm2, p->nw_base64, p->nw_small};
-  for (double* x : nw) cudaFree(x);
-  cudaFree(p->nw_base32);
-  cudaFree(p->nw_ismall);
-  cudaFreeHost(p->h_dbl);
-  cudaFreeHost(p->h_int);
+  solver_free(p);
   delete p;
 }
 
@@ -364,6 +378,7 @@ static ChainArgs chain_args(const sdd_plan* p, const double* g, double* f, const
   a.LinvA4 = p->LinvA4; a.LinvT = p->LinvT; a.LinvS = p->LinvS;
   a.ABA4 = p->ABA4; a.ir2A4 = p->ir2A4; a.ir4A4 = p->ir4A4;
   a.h = p->hbuf;
+  a.h_stride = shell_elems(p);
   a.coefA4 = p->coefA4; a.coefT = p->coefT; a.coefS = p->coefS;
   a.dtA4 = p->Pr * p->dt; a.dtT = p->dt; a.dtS = p->Tau * p->dt;
   return a;
@@ -379,19 +394,31 @@ static int check_plan(sdd_plan* p, int batch) {
 
 // One application of Phi (the step map) or its Jacobian to X (or dv), into out.
 // mode 0: FX (nonlinear term of X); 1: DFX about the base in `base`; 2: linear only.
-static int apply_step(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X,
-                      double* out, const double* sub, int mode, void* base, int prec, cudaStream_t s) {
+// Same as apply_step with explicit strides (doubles between shells) of the input X, the output and sub.
+static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X, size_t ldx,
+                         double* out, size_t ldo, const double* sub, size_t lds, int mode, void* base, int prec,
+                         cudaStream_t s) {
   cudaError_t e;
   if (mode != 2) {
     FxArgs fa = fx_args(p, prec, X, base, p->out4);
+    fa.x_stride = ldx;
     e = launch_fx(fa, batch, mode == 1 ? 1 : 0, prec, s);
     SDD_CUDA(e);
   }
   RhsArgs ra = rhs_args(p, X, p->out4, Ra, Ras, p->rhs, mode == 2);
+  ra.x_stride = ldx;
   SDD_CUDA(launch_rhs(ra, batch, s));
   ChainArgs ca = chain_args(p, p->rhs, out, sub);
+  ca.f_stride = ldo;
+  ca.sub_stride = lds;
   SDD_CUDA(launch_chain(ca, batch, 3, s));
   return SDD_OK;
+}
+
+static int apply_step(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X,
+                      double* out, const double* sub, int mode, void* base, int prec, cudaStream_t s) {
+  const size_t n = shell_elems(p);
+  return apply_step_ld(p, batch, Ra, Ras, X, n, out, n, sub, n, mode, base, prec, s);
 }
 
 extern "C" {
@@ -511,40 +538,43 @@ int sdd_pdfx(sdd_plan* p, int batch, const double* Ra, const double* Ras, const 
 
 }  // extern "C"
 
-// ---- Newton-GMRES --------------------------------------------------------------------------------
-static int newton_reserve(sdd_plan* p, int B, int m) {
-  if (p->nw_B >= B && p->nw_m >= m) return SDD_OK;
-  double* nw[] = {p->nw_V, p->nw_F, p->nw_x, p->nw_w, p->nw_r, p->nw_part, p->nw_nrm2, p->nw_base64, p->nw_small};
-  for (double* x : nw) cudaFree(x);
-  cudaFree(p->nw_base32); cudaFree(p->nw_ismall); cudaFreeHost(p->h_dbl); cudaFreeHost(p->h_int);
-  p->nw_V = p->nw_F = p->nw_x = p->nw_w = p->nw_r = p->nw_part = p->nw_nrm2 = p->nw_base64 = p->nw_small = nullptr;
-  p->nw_base32 = nullptr; p->nw_ismall = nullptr; p->h_dbl = nullptr; p->h_int = nullptr;
-  p->nw_B = p->nw_m = 0;
-  const size_t n = shell_elems(p), be = sdd_plan_base_cache_elems(p);
-  const int nchunk = (int)((n + kDotChunk - 1) / kDotChunk);
-  SDD_CUDA(cudaMalloc(&p->nw_V, (size_t)(m + 1) * B * n * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->nw_F, (size_t)B * n * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->nw_x, (size_t)B * n * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->nw_w, (size_t)B * n * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->nw_r, (size_t)B * n * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->nw_part, (size_t)B * (m + 1) * nchunk * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->nw_nrm2, (size_t)B * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->nw_base64, (size_t)B * be * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->nw_base32, (size_t)B * be * sizeof(float)));
+// ---- Krylov workspace, generic GMRES, Newton and pseudo-arclength continuation ----------------------
+// Vectors of the solvers have stride ld = n + 1 per shell (n = 3*N_fm*nr): the Newton solves use the first
+// n doubles, the bordered continuation system all n + 1 (the last is the continuation parameter).
+static int solver_reserve(sdd_plan* p, int B, int m) {
+  if (p->sv_B >= B && p->sv_m >= m) return SDD_OK;
+  solver_free(p);
+  const size_t n = shell_elems(p), ld = n + 1, be = sdd_plan_base_cache_elems(p);
+  const int nchunk = (int)((ld + kDotChunk - 1) / kDotChunk);
+  const size_t vb = (size_t)B * ld * sizeof(double);
+  SDD_CUDA(cudaMalloc(&p->kv_V, (size_t)(m + 1) * vb));
+  SDD_CUDA(cudaMalloc(&p->kv_w, vb));
+  SDD_CUDA(cudaMalloc(&p->kv_r, vb));
+  SDD_CUDA(cudaMalloc(&p->kv_part, (size_t)B * (m + 1) * nchunk * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->kv_nrm2, (size_t)B * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->kv_dot, (size_t)B * sizeof(double)));
   const size_t small = (size_t)B * ((size_t)(m + 1) * m + 3 * (m + 1) + 3 * m + 4);
-  SDD_CUDA(cudaMalloc(&p->nw_small, small * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->nw_ismall, (size_t)4 * B * sizeof(int)));
-  SDD_CUDA(cudaMallocHost(&p->h_dbl, (size_t)B * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->kv_small, small * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->kv_ismall, (size_t)4 * B * sizeof(int)));
+  SDD_CUDA(cudaMallocHost(&p->h_dbl, (size_t)2 * B * sizeof(double)));
   SDD_CUDA(cudaMallocHost(&p->h_int, (size_t)B * sizeof(int)));
-  p->nw_B = B;
-  p->nw_m = m;
+  double** v[] = {&p->sv_F, &p->sv_x, &p->sv_Xd, &p->sv_t, &p->sv_G};
+  for (double** q : v) SDD_CUDA(cudaMalloc(q, vb));
+  SDD_CUDA(cudaMalloc(&p->sv_X0, (size_t)B * n * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->sv_Jmu, (size_t)B * n * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->sv_g, (size_t)B * n * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->sv_base64, (size_t)B * be * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->sv_base32, (size_t)B * be * sizeof(float)));
+  SDD_CUDA(cudaMalloc(&p->sv_dev, (size_t)8 * B * sizeof(double)));
+  p->sv_B = B;
+  p->sv_m = m;
   return SDD_OK;
 }
 
 static GmresState gmres_state(sdd_plan* p, int B, int m) {
   GmresState s;
   s.m = m;
-  double* q = p->nw_small;
+  double* q = p->kv_small;
   s.H = q; q += (size_t)B * (m + 1) * m;
   s.hcol = q; q += (size_t)B * (m + 1);
   s.h2 = q; q += (size_t)B * (m + 1);
@@ -556,11 +586,80 @@ static GmresState gmres_state(sdd_plan* p, int B, int m) {
   s.inv = q; q += B;
   s.resid = q; q += B;
   s.target = q; q += B;
-  int* iq = p->nw_ismall;
+  int* iq = p->kv_ismall;
   s.active = iq; iq += B;
   s.solve = iq; iq += B;
   s.kb = iq; iq += B;
   return s;
+}
+
+// Device matvec on B shells: out = A v (vectors of stride ld).
+using MatVec = std::function<int(const double* v, double* out)>;
+
+// Restarted GMRES(m), CGS2, for the shells with solve[b] != 0: A x = rhs, x starts at 0, inner stop
+// |r_b| <= target[b] (absolute).  x, rhs have stride ld with nu used doubles.  resid (host) receives the
+// final residual estimates.
+static int gmres_solve(sdd_plan* p, const MatVec& A, const double* rhs, double* x, int B, int nu, int ld, int m,
+                       int max_restarts, const std::vector<double>& target, const std::vector<int>& solve,
+                       cudaStream_t s, int* matvecs, std::vector<double>& resid) {
+  GmresState G = gmres_state(p, B, m);
+  const size_t vs = (size_t)B * ld;
+  int st;
+  resid.assign(B, 0.0);
+  SDD_CUDA(cudaMemcpyAsync(G.target, target.data(), B * sizeof(double), cudaMemcpyHostToDevice, s));
+  SDD_CUDA(cudaMemcpyAsync(G.solve, solve.data(), B * sizeof(int), cudaMemcpyHostToDevice, s));
+  SDD_CUDA(cudaMemsetAsync(x, 0, vs * sizeof(double), s));
+  std::vector<int> again(solve);
+  for (int cyc = 0; cyc < max_restarts; ++cyc) {
+    const double* r = rhs;
+    if (cyc > 0) {                                   // r = rhs - A x
+      if ((st = A(x, p->kv_w))) return st;
+      ++*matvecs;
+      SDD_CUDA(krylov_sub(rhs, p->kv_w, p->kv_r, vs, s));
+      r = p->kv_r;
+    }
+    SDD_CUDA(krylov_dots(r, 0, r, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s));
+    SDD_CUDA(krylov_cycle_start(G, p->kv_nrm2, B, s));
+    SDD_CUDA(krylov_scale(r, G.inv, p->kv_V, nu, ld, B, s));
+    for (int j = 0; j < m; ++j) {
+      double* Vj = p->kv_V + (size_t)j * vs;
+      if ((st = A(Vj, p->kv_w))) return st;
+      ++*matvecs;
+      SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.hcol, m + 1, 0, s));
+      SDD_CUDA(krylov_sub_combination(p->kv_V, vs, p->kv_w, G.hcol, m + 1, nu, ld, j + 1, B, s));
+      SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.h2, m + 1, 0, s));
+      SDD_CUDA(krylov_sub_combination(p->kv_V, vs, p->kv_w, G.h2, m + 1, nu, ld, j + 1, B, s));
+      SDD_CUDA(krylov_dots(p->kv_w, 0, p->kv_w, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s));
+      SDD_CUDA(krylov_arnoldi_finish(G, p->kv_nrm2, j, B, s));
+      if (j + 1 < m) SDD_CUDA(krylov_scale(p->kv_w, G.inv, p->kv_V + (size_t)(j + 1) * vs, nu, ld, B, s));
+      SDD_CUDA(cudaMemcpyAsync(p->h_int, G.active, B * sizeof(int), cudaMemcpyDeviceToHost, s));
+      SDD_CUDA(cudaStreamSynchronize(s));
+      bool act = false;
+      for (int b = 0; b < B; ++b) act = act || p->h_int[b];
+      if (!act) break;
+    }
+    SDD_CUDA(krylov_solve_y(G, B, s));
+    SDD_CUDA(krylov_add_combination(p->kv_V, vs, x, G.y, m, G.kb, nu, ld, B, s));
+    SDD_CUDA(cudaMemcpyAsync(p->h_dbl, G.resid, B * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SDD_CUDA(cudaStreamSynchronize(s));
+    bool more = false;
+    for (int b = 0; b < B; ++b) {
+      if (again[b]) resid[b] = p->h_dbl[b];
+      again[b] = again[b] && p->h_dbl[b] > target[b];
+      more = more || again[b];
+    }
+    if (!more) break;
+    SDD_CUDA(cudaMemcpyAsync(G.solve, again.data(), B * sizeof(int), cudaMemcpyHostToDevice, s));
+  }
+  return SDD_OK;
+}
+
+// |v_b|^2 over nu doubles at stride ld -> host h_dbl[0..B)
+static int host_norms2(sdd_plan* p, const double* v, int nu, int ld, int B, cudaStream_t s) {
+  SDD_CUDA(krylov_dots(v, 0, v, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s));
+  SDD_CUDA(cudaMemcpyAsync(p->h_dbl, p->kv_nrm2, B * sizeof(double), cudaMemcpyDeviceToHost, s));
+  SDD_CUDA(cudaStreamSynchronize(s));
+  return SDD_OK;
 }
 
 extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const double* Ras, double* X,
@@ -571,34 +670,22 @@ extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const doub
   const int m = o->restart;
   if (m < 1 || m > 64 || o->max_newton < 0 || o->max_restarts < 1 || !(o->tol >= 0.0)) return SDD_ERR_ARG;
   if (o->mixed_matvec && p->prec != SDD_PREC_MIXED) return SDD_ERR_ARG;
-  st = newton_reserve(p, B, m);
-  if (st) return st;
+  if ((st = solver_reserve(p, B, m))) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  const int n = (int)shell_elems(p);
-  const size_t vs = (size_t)B * n;            // stride between Krylov vectors
-  GmresState G = gmres_state(p, B, m);
-  int* newton_mask = p->nw_ismall + 3 * B;
+  const int n = (int)shell_elems(p), ld = n + 1;
   const int mv_prec = o->mixed_matvec ? SDD_PREC_MIXED : SDD_PREC_FP64;
-  void* base_mv = o->mixed_matvec ? (void*)p->nw_base32 : (void*)p->nw_base64;
-  std::vector<double> resF(B, 0.0), target(B, 0.0);
+  void* base_mv = o->mixed_matvec ? (void*)p->sv_base32 : (void*)p->sv_base64;
+  std::vector<double> resF(B, 0.0), target(B, 0.0), resid;
   std::vector<int> nmask(B, 0), iters(B, 0);
   int matvecs = 0;
-
-  auto norms = [&](const double* v) -> int {   // ||v_b||^2 -> p->h_dbl
-    SDD_CUDA(krylov_dots(v, 0, v, n, 1, B, p->nw_part, p->nw_nrm2, 1, 0, s));
-    SDD_CUDA(cudaMemcpyAsync(p->h_dbl, p->nw_nrm2, B * sizeof(double), cudaMemcpyDeviceToHost, s));
-    SDD_CUDA(cudaStreamSynchronize(s));
-    return SDD_OK;
+  // the Jacobian of PFX about the cached base state, on vectors of stride ld
+  MatVec J = [&](const double* v, double* out) {
+    return apply_step_ld(p, B, Ra, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s);
   };
-  auto jac = [&](const double* v, double* out) -> int {   // out = PDFX(v) about the cached base
-    ++matvecs;
-    return apply_step(p, B, Ra, Ras, v, out, v, 1, base_mv, mv_prec, s);
-  };
-
   for (int it = 0;; ++it) {
-    st = apply_step(p, B, Ra, Ras, X, p->nw_F, X, 0, p->nw_base64, SDD_PREC_FP64, s);   // F = PFX(X)
-    if (st) return st;
-    if ((st = norms(p->nw_F))) return st;
+    if ((st = apply_step_ld(p, B, Ra, Ras, X, n, p->sv_F, ld, X, n, 0, p->sv_base64, SDD_PREC_FP64, s)))
+      return st;                                                         // F = PFX(X), base cached
+    if ((st = host_norms2(p, p->sv_F, n, ld, B, s))) return st;
     bool any = false;
     for (int b = 0; b < B; ++b) {
       resF[b] = std::sqrt(p->h_dbl[b]);
@@ -608,54 +695,15 @@ extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const doub
     }
     if (!any || it >= o->max_newton) break;
     if (o->mixed_matvec) {
-      FxArgs ga = fx_args(p, SDD_PREC_MIXED, X, p->nw_base32, p->out4);
+      FxArgs ga = fx_args(p, SDD_PREC_MIXED, X, p->sv_base32, p->out4);
       SDD_CUDA(launch_fx(ga, B, 2, SDD_PREC_MIXED, s));
     }
     for (int b = 0; b < B; ++b) target[b] = o->gmres_rtol * resF[b];
-    SDD_CUDA(cudaMemcpyAsync(G.target, target.data(), B * sizeof(double), cudaMemcpyHostToDevice, s));
-    SDD_CUDA(cudaMemcpyAsync(G.solve, nmask.data(), B * sizeof(int), cudaMemcpyHostToDevice, s));
-    SDD_CUDA(cudaMemcpyAsync(newton_mask, nmask.data(), B * sizeof(int), cudaMemcpyHostToDevice, s));
-    SDD_CUDA(cudaMemsetAsync(p->nw_x, 0, (size_t)B * n * sizeof(double), s));
-    for (int cyc = 0; cyc < o->max_restarts; ++cyc) {
-      const double* r = p->nw_F;
-      if (cyc > 0) {                                  // r = F - J x
-        if ((st = jac(p->nw_x, p->nw_w))) return st;
-        SDD_CUDA(krylov_sub(p->nw_F, p->nw_w, p->nw_r, (size_t)B * n, s));
-        r = p->nw_r;
-      }
-      SDD_CUDA(krylov_dots(r, 0, r, n, 1, B, p->nw_part, p->nw_nrm2, 1, 0, s));
-      SDD_CUDA(krylov_cycle_start(G, p->nw_nrm2, B, s));
-      SDD_CUDA(krylov_scale(r, G.inv, p->nw_V, n, B, s));
-      for (int j = 0; j < m; ++j) {
-        double* Vj = p->nw_V + (size_t)j * vs;
-        if ((st = jac(Vj, p->nw_w))) return st;
-        SDD_CUDA(krylov_dots(p->nw_V, vs, p->nw_w, n, j + 1, B, p->nw_part, G.hcol, m + 1, 0, s));
-        SDD_CUDA(krylov_sub_combination(p->nw_V, vs, p->nw_w, G.hcol, m + 1, n, j + 1, B, s));
-        SDD_CUDA(krylov_dots(p->nw_V, vs, p->nw_w, n, j + 1, B, p->nw_part, G.h2, m + 1, 0, s));
-        SDD_CUDA(krylov_sub_combination(p->nw_V, vs, p->nw_w, G.h2, m + 1, n, j + 1, B, s));
-        SDD_CUDA(krylov_dots(p->nw_w, 0, p->nw_w, n, 1, B, p->nw_part, p->nw_nrm2, 1, 0, s));
-        SDD_CUDA(krylov_arnoldi_finish(G, p->nw_nrm2, j, B, s));
-        if (j + 1 < m) SDD_CUDA(krylov_scale(p->nw_w, G.inv, p->nw_V + (size_t)(j + 1) * vs, n, B, s));
-        SDD_CUDA(cudaMemcpyAsync(p->h_int, G.active, B * sizeof(int), cudaMemcpyDeviceToHost, s));
-        SDD_CUDA(cudaStreamSynchronize(s));
-        bool act = false;
-        for (int b = 0; b < B; ++b) act = act || p->h_int[b];
-        if (!act) break;
-      }
-      SDD_CUDA(krylov_solve_y(G, B, s));
-      SDD_CUDA(krylov_add_combination(p->nw_V, vs, p->nw_x, G.y, m, G.kb, n, B, s));
-      SDD_CUDA(cudaMemcpyAsync(p->h_dbl, G.resid, B * sizeof(double), cudaMemcpyDeviceToHost, s));
-      SDD_CUDA(cudaStreamSynchronize(s));
-      std::vector<int> again(B, 0);
-      bool more = false;
-      for (int b = 0; b < B; ++b) {
-        again[b] = nmask[b] && p->h_dbl[b] > target[b];
-        more = more || again[b];
-      }
-      if (!more) break;
-      SDD_CUDA(cudaMemcpyAsync(G.solve, again.data(), B * sizeof(int), cudaMemcpyHostToDevice, s));
-    }
-    SDD_CUDA(krylov_masked_sub(X, p->nw_x, newton_mask, n, B, s));
+    if ((st = gmres_solve(p, J, p->sv_F, p->sv_x, B, n, ld, m, o->max_restarts, target, nmask, s, &matvecs, resid)))
+      return st;
+    int* mask_dev = p->kv_ismall + 3 * B;
+    SDD_CUDA(cudaMemcpyAsync(mask_dev, nmask.data(), B * sizeof(int), cudaMemcpyHostToDevice, s));
+    SDD_CUDA(krylov_masked_sub(X, p->sv_x, mask_dev, n, n, ld, B, s));
     for (int b = 0; b < B; ++b) iters[b] += nmask[b];
   }
   bool all = true;
@@ -666,6 +714,202 @@ extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const doub
     res[b].converged = resF[b] <= o->tol ? 1 : 0;
     res[b].pad = 0;
     all = all && res[b].converged;
+  }
+  return all ? SDD_OK : SDD_ERR_NOT_CONVERGED;
+}
+
+// PDFmu(X) = [A4 solve of dt Pr gr_k T; 0; 0] (Main.py:829-837) into p->sv_Jmu (stride n)
+static int pdfmu(sdd_plan* p, int B, const double* X, int ldx, cudaStream_t s) {
+  const int n = (int)shell_elems(p);
+  SDD_CUDA(contin_grk_T(X, ldx, p->sv_g, p->M, p->nr, p->gr, p->dt * p->Pr, p->sym, B, s));
+  SDD_CUDA(cudaMemsetAsync(p->sv_Jmu, 0, (size_t)B * n * sizeof(double), s));
+  ChainArgs ca = chain_args(p, p->sv_g, p->sv_Jmu, nullptr);
+  SDD_CUDA(launch_chain(ca, B, 1, s));
+  return SDD_OK;
+}
+
+extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const double* Ras, double* X_dot,
+                               const double* sign, const double* ds_in, const sdd_contin_opts* o,
+                               sdd_contin_result* res, void* stream) {
+  int st = check_plan(p, B);
+  if (st) return st;
+  if (!X || !Ra || !Ras || !X_dot || !sign || !ds_in || !o || !res) return SDD_ERR_ARG;
+  const int m = o->restart;
+  if (m < 1 || m > 64 || o->max_restarts < 1 || o->max_corrector < 1 || o->max_halvings < 0 || !(o->tol > 0.0))
+    return SDD_ERR_ARG;
+  if (o->mixed_matvec && p->prec != SDD_PREC_MIXED) return SDD_ERR_ARG;
+  if ((st = solver_reserve(p, B, m))) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = (int)shell_elems(p), ld = n + 1, Npsi = p->M * p->nr;
+  const double delta = 1.0 / n;                         // 1/(3N), Main.py:771
+  const int mv_prec = o->mixed_matvec ? SDD_PREC_MIXED : SDD_PREC_FP64;
+  void* base_mv = o->mixed_matvec ? (void*)p->sv_base32 : (void*)p->sv_base64;
+  double* mu_dev = p->sv_dev;            // current parameter Ra (per shell)
+  double* mudot_dev = p->sv_dev + B;
+  double* c_dev = p->sv_dev + 2 * B;     // per-shell scalars
+  double* last_dev = p->sv_dev + 3 * B;
+  std::vector<double> mu0(B), mu(B), mudot(B), ds(ds_in, ds_in + B), resF(B, 0.0), gl(B, 0.0), c(B), tgt(B), resid;
+  std::vector<int> it(B, 0), halv(B, 0), conv(B, 0), fail(B, 0), solve(B, 0);
+  int matvecs = 0;
+  SDD_CUDA(cudaMemcpyAsync(mu0.data(), Ra, B * sizeof(double), cudaMemcpyDeviceToHost, s));
+  SDD_CUDA(cudaStreamSynchronize(s));
+  mu = mu0;
+  auto upload = [&](double* dst, const std::vector<double>& v) {
+    return cudaMemcpyAsync(dst, v.data(), B * sizeof(double), cudaMemcpyHostToDevice, s);
+  };
+  auto base_at = [&](const double* Xs) -> int {        // F = PFX(Xs, mu) into sv_F (stride ld), base cached
+    int r = apply_step_ld(p, B, mu_dev, Ras, Xs, n, p->sv_F, ld, Xs, n, 0, p->sv_base64, SDD_PREC_FP64, s);
+    if (r) return r;
+    if (o->mixed_matvec) {
+      FxArgs ga = fx_args(p, SDD_PREC_MIXED, Xs, p->sv_base32, p->out4);
+      SDD_CUDA(launch_fx(ga, B, 2, SDD_PREC_MIXED, s));
+    }
+    return pdfmu(p, B, Xs, n, s);
+  };
+  MatVec J = [&](const double* v, double* out) {
+    return apply_step_ld(p, B, mu_dev, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s);
+  };
+  // bordered operator DG = [[DF_X, DF_mu], [delta X_dot^T, (1-delta) mu_dot]]  (Main.py:914-915)
+  MatVec DG = [&](const double* v, double* out) -> int {
+    int r = apply_step_ld(p, B, mu_dev, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s);
+    if (r) return r;
+    SDD_CUDA(krylov_dots(p->sv_Xd, 0, v, n, ld, 1, B, p->kv_part, p->kv_dot, 1, 0, s));
+    SDD_CUDA(contin_border(v, out, n, ld, p->sv_Jmu, n, Npsi, p->kv_dot, mudot_dev, delta, B, s));
+    return SDD_OK;
+  };
+
+  // ---- predictor (Main.py:839-876; with dt < 10 the tangent is always recomputed) ----
+  SDD_CUDA(upload(mu_dev, mu));
+  if ((st = base_at(X))) return st;
+  SDD_CUDA(krylov_copy_scaled(p->sv_Jmu, n, p->sv_G, ld, n, -1.0, nullptr, B, s));   // rhs = -DF_mu
+  if ((st = host_norms2(p, p->sv_G, n, ld, B, s))) return st;
+  for (int b = 0; b < B; ++b) {
+    const double nj = std::sqrt(p->h_dbl[b]);
+    tgt[b] = o->tangent_rtol * nj;
+    solve[b] = nj > 0.0;
+  }
+  if ((st = gmres_solve(p, J, p->sv_G, p->sv_x, B, n, ld, m, o->max_restarts, tgt, solve, s, &matvecs, resid)))
+    return st;
+  if ((st = host_norms2(p, p->sv_x, n, ld, B, s))) return st;
+  for (int b = 0; b < B; ++b) {
+    const double nxi = std::sqrt(p->h_dbl[b]);
+    mudot[b] = sign[b] / std::sqrt(1.0 + delta * (nxi - 1.0));    // Main.py:861
+    c[b] = mudot[b];
+  }
+  SDD_CUDA(upload(mudot_dev, mudot));
+  SDD_CUDA(upload(c_dev, c));
+  SDD_CUDA(krylov_scale(p->sv_x, c_dev, p->sv_Xd, n, ld, B, s));                     // X_dot = mu_dot xi
+  SDD_CUDA(cudaMemcpyAsync(p->sv_X0, X, (size_t)B * n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  auto predict = [&](int b) -> int {                     // X_b = X0_b + ds_b X_dot_b, mu_b = mu0_b + ds_b mu_dot_b
+    c[b] = ds[b];
+    SDD_CUDA(cudaMemcpyAsync(c_dev + b, &c[b], sizeof(double), cudaMemcpyHostToDevice, s));
+    SDD_CUDA(krylov_axpy_shell(p->sv_X0 + (size_t)b * n, n, p->sv_Xd + (size_t)b * ld, ld, c_dev + b,
+                               X + (size_t)b * n, n, n, 1, s));
+    mu[b] = mu0[b] + ds[b] * mudot[b];
+    return SDD_OK;
+  };
+  for (int b = 0; b < B; ++b)
+    if ((st = predict(b))) return st;
+
+  // ---- corrector (Main.py:885-930), stopping on absolute residuals ----
+  const int max_rounds = (o->max_halvings + 1) * (o->max_corrector + 1) + 1;
+  for (int round = 0; round < max_rounds; ++round) {
+    SDD_CUDA(upload(mu_dev, mu));
+    if ((st = base_at(X))) return st;
+    // arclength residual p = delta X_dot.(X - X0) + (1 - delta) mu_dot (mu - mu0) - ds   (Main.py:910)
+    SDD_CUDA(krylov_copy_scaled(X, n, p->sv_t, ld, n, 1.0, nullptr, B, s));
+    for (int b = 0; b < B; ++b) c[b] = -1.0;
+    SDD_CUDA(upload(c_dev, c));
+    SDD_CUDA(krylov_axpy_shell(p->sv_t, ld, p->sv_X0, n, c_dev, p->sv_t, ld, n, B, s));
+    SDD_CUDA(krylov_dots(p->sv_Xd, 0, p->sv_t, n, ld, 1, B, p->kv_part, p->kv_dot, 1, 0, s));
+    SDD_CUDA(cudaMemcpyAsync(p->h_dbl + B, p->kv_dot, B * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if ((st = host_norms2(p, p->sv_F, n, ld, B, s))) return st;
+    bool pending = false;
+    for (int b = 0; b < B; ++b) {
+      resF[b] = std::sqrt(p->h_dbl[b]);
+      gl[b] = delta * p->h_dbl[B + b] + (1.0 - delta) * mudot[b] * (mu[b] - mu0[b]) - ds[b];
+      solve[b] = 0;
+      if (conv[b] || fail[b]) continue;
+      if (resF[b] <= o->tol && std::fabs(gl[b]) <= o->tol) {
+        conv[b] = 1;
+        continue;
+      }
+      if (it[b] >= o->max_corrector) {                    // halve ds and predict again (Main.py:888-899)
+        ds[b] *= 0.5;
+        ++halv[b];
+        it[b] = 0;
+        if (halv[b] > o->max_halvings || ds[b] < o->tol) {
+          fail[b] = 1;
+          continue;
+        }
+        if ((st = predict(b))) return st;
+        pending = true;
+        continue;
+      }
+      solve[b] = 1;
+      pending = true;
+    }
+    if (!pending) break;
+    bool any = false;
+    for (int b = 0; b < B; ++b) any = any || solve[b];
+    if (!any) continue;                                   // only re-predicted shells this round
+    SDD_CUDA(upload(last_dev, gl));
+    SDD_CUDA(krylov_copy_scaled(p->sv_F, ld, p->sv_G, ld, n, 1.0, last_dev, B, s));     // G = [F; p]
+    for (int b = 0; b < B; ++b)
+      tgt[b] = o->gmres_rtol * std::sqrt(delta * resF[b] * resF[b] + (1.0 - delta) * gl[b] * gl[b]);  // :919
+    if ((st = gmres_solve(p, DG, p->sv_G, p->sv_x, B, n + 1, ld, m, o->max_restarts, tgt, solve, s, &matvecs,
+                          resid)))
+      return st;
+    int* mask_dev = p->kv_ismall + 3 * B;
+    SDD_CUDA(cudaMemcpyAsync(mask_dev, solve.data(), B * sizeof(int), cudaMemcpyHostToDevice, s));
+    SDD_CUDA(krylov_masked_sub(X, p->sv_x, mask_dev, n, n, ld, B, s));                   // Y -= dY
+    SDD_CUDA(cudaMemcpy2DAsync(p->h_dbl, sizeof(double), p->sv_x + n, ld * sizeof(double), sizeof(double), B,
+                               cudaMemcpyDeviceToHost, s));
+    SDD_CUDA(cudaStreamSynchronize(s));
+    for (int b = 0; b < B; ++b)
+      if (solve[b]) {
+        mu[b] -= p->h_dbl[b];
+        ++it[b];
+      }
+  }
+
+  // ---- new tangent: DG y = e_last at the converged point, normalised (Main.py:944-953) ----
+  SDD_CUDA(cudaMemsetAsync(p->sv_G, 0, (size_t)B * ld * sizeof(double), s));
+  for (int b = 0; b < B; ++b) c[b] = 1.0;
+  SDD_CUDA(upload(last_dev, c));
+  SDD_CUDA(krylov_copy_scaled(p->sv_G, ld, p->sv_G, ld, n, 1.0, last_dev, B, s));   // G = e_last (G[n] = 1)
+  for (int b = 0; b < B; ++b) {
+    tgt[b] = o->tangent_rtol;
+    solve[b] = conv[b];
+  }
+  if ((st = gmres_solve(p, DG, p->sv_G, p->sv_x, B, n + 1, ld, m, o->max_restarts, tgt, solve, s, &matvecs, resid)))
+    return st;
+  if ((st = host_norms2(p, p->sv_x, n, ld, B, s))) return st;
+  std::vector<double> yx2(p->h_dbl, p->h_dbl + B);
+  SDD_CUDA(cudaMemcpy2DAsync(p->h_dbl, sizeof(double), p->sv_x + n, ld * sizeof(double), sizeof(double), B,
+                             cudaMemcpyDeviceToHost, s));
+  SDD_CUDA(cudaStreamSynchronize(s));
+  for (int b = 0; b < B; ++b) {
+    const double yl = p->h_dbl[b];
+    const double nrm = std::sqrt(delta * yx2[b] + (1.0 - delta) * yl * yl);
+    c[b] = (conv[b] && nrm > 0.0) ? 1.0 / nrm : 0.0;
+    res[b].Ra_dot = c[b] * yl;
+  }
+  SDD_CUDA(upload(c_dev, c));
+  SDD_CUDA(krylov_scale(p->sv_x, c_dev, p->sv_t, n, ld, B, s));
+  SDD_CUDA(krylov_copy_scaled(p->sv_t, ld, X_dot, n, n, 1.0, nullptr, B, s));
+  SDD_CUDA(upload(Ra, mu));
+  SDD_CUDA(cudaStreamSynchronize(s));
+  bool all = true;
+  for (int b = 0; b < B; ++b) {
+    res[b].residual = resF[b];
+    res[b].arclength = std::fabs(gl[b]);
+    res[b].ds = (conv[b] && it[b] <= 4) ? 2.0 * ds[b] : ds[b];        // Main.py:933-935
+    res[b].corrector_iters = it[b];
+    res[b].halvings = halv[b];
+    res[b].matvecs = matvecs;
+    res[b].converged = conv[b];
+    all = all && conv[b];
   }
   return all ? SDD_OK : SDD_ERR_NOT_CONVERGED;
 }

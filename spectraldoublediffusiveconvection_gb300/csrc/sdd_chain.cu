@@ -183,7 +183,7 @@ __global__ void k_hpre(ChainArgs a, int nfields) {
   const int row = M - 1 - jj;
   const size_t foff = (size_t)field * a.field_off;
   const double* g = a.g + (size_t)b * a.g_stride + foff + (size_t)row * nr;
-  double* hout = a.h + (size_t)b * a.f_stride + foff + (size_t)row * nr;
+  double* hout = a.h + (size_t)b * a.h_stride + foff + (size_t)row * nr;
   const double* L = (field == 0 ? a.LinvA4 : (field == 1 ? a.LinvT : a.LinvS)) + (size_t)jj * nr * ldl;
   for (int i = lane; i < nr; i += 32) {
     double acc = 0.0;
@@ -203,7 +203,7 @@ cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStre
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   a.g = a.h;
-  a.g_stride = a.f_stride;
+  a.g_stride = a.h_stride;
   const size_t smem = chain_smem_bytes(a.M, a.nr, a.ldl);
   static int sms = 0;
   if (sms == 0) {

@@ -105,7 +105,8 @@ struct ChainArgs {
   size_t sub_stride;
   const double* LinvA4, *LinvT, *LinvS;  // [M][nr cols][ldl] transposed blocks
   const double* ABA4;        // [M][2 nr cols][ldl]: transposed [A_j B_j] of the psi chain
-  double* h;                 // [shell][3][M][nr] h = Linv g (same strides as f)
+  double* h;                 // [shell][3][M][nr] h = Linv g
+  size_t h_stride;           // doubles between shells in h
   const double* ir2A4, *ir4A4;
   const double* coefA4;      // [M][4] per jj: (dt bjt, dt bjt bj, bj, bjt), dt = Pr*dt, j = M - jj
   const double* coefT, *coefS;  // [M][4] per jj: (2 dt (j+2), 0.5 if j == 0 else 1, 0, 0), j = M-1-jj

@@ -6,7 +6,8 @@
 // fixed element chunks, then a fixed-order sum of the partials), so a shell's result does not depend
 // on the other shells in the batch.
 //
-// Vector layout: V[i][b][n] (Krylov vector i of shell b has n = 3*N_fm*nr contiguous doubles).
+// Vector layout: V[i][b][ld]: Krylov vector i of shell b has n used doubles at stride ld (n = 3*N_fm*nr
+// for Newton, n+1 with the continuation parameter appended for the bordered arclength system).
 #include <cuda_runtime.h>
 
 #include "sdd_krylov.cuh"
@@ -17,15 +18,15 @@ constexpr int kDotThreads = 256;
 
 // part[(b*(nv) + i)*nchunk + c] = sum over chunk c of V_i[b] . w[b],  i < nv
 __global__ void __launch_bounds__(kDotThreads) k_dot_partials(const double* __restrict__ V, size_t vstride_i,
-                                                             const double* __restrict__ w, int n, int nv,
+                                                             const double* __restrict__ w, int n, int ld, int nv,
                                                              int chunk, double* __restrict__ part) {
   __shared__ double red[kDotThreads / 32];
   const int c = blockIdx.x, b = blockIdx.y, nchunk = gridDim.x;
   const int e0 = c * chunk, e1 = min(n, e0 + chunk);
-  const double* wb = w + (size_t)b * n;
+  const double* wb = w + (size_t)b * ld;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int i = 0; i < nv; ++i) {
-    const double* vb = V + (size_t)i * vstride_i + (size_t)b * n;
+    const double* vb = V + (size_t)i * vstride_i + (size_t)b * ld;
     double s = 0.0;
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) s += vb[e] * wb[e];
 #pragma unroll
@@ -56,36 +57,37 @@ __global__ void k_dot_reduce(const double* __restrict__ part, int nv, int nchunk
 
 // w[b] -= sum_{i<nv} V_i[b] * coef[b*ldc + i]
 __global__ void k_sub_combination(const double* __restrict__ V, size_t vstride_i, double* __restrict__ w,
-                                  const double* __restrict__ coef, int ldc, int n, int nv) {
+                                  const double* __restrict__ coef, int ldc, int n, int ld, int nv) {
   const int b = blockIdx.y;
   const double* cb = coef + (size_t)b * ldc;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
     double s = 0.0;
-    for (int i = 0; i < nv; ++i) s += V[(size_t)i * vstride_i + (size_t)b * n + e] * cb[i];
-    w[(size_t)b * n + e] -= s;
+    for (int i = 0; i < nv; ++i) s += V[(size_t)i * vstride_i + (size_t)b * ld + e] * cb[i];
+    w[(size_t)b * ld + e] -= s;
   }
 }
 
 // x[b] += sum_{i<k_b} V_i[b] * y[b*ldy + i]
 __global__ void k_add_combination(const double* __restrict__ V, size_t vstride_i, double* __restrict__ x,
-                                  const double* __restrict__ y, int ldy, const int* __restrict__ kb, int n) {
+                                  const double* __restrict__ y, int ldy, const int* __restrict__ kb, int n,
+                                  int ld) {
   const int b = blockIdx.y;
   const int k = kb[b];
   const double* yb = y + (size_t)b * ldy;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
     double s = 0.0;
-    for (int i = 0; i < k; ++i) s += V[(size_t)i * vstride_i + (size_t)b * n + e] * yb[i];
-    x[(size_t)b * n + e] += s;
+    for (int i = 0; i < k; ++i) s += V[(size_t)i * vstride_i + (size_t)b * ld + e] * yb[i];
+    x[(size_t)b * ld + e] += s;
   }
 }
 
 // out[b] = a[b] * scale[b]  (scale may be per shell)
 __global__ void k_scale(const double* __restrict__ a, const double* __restrict__ scale, double* __restrict__ out,
-                        int n) {
+                        int n, int ld) {
   const int b = blockIdx.y;
   const double s = scale[b];
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
-    out[(size_t)b * n + e] = a[(size_t)b * n + e] * s;
+    out[(size_t)b * ld + e] = a[(size_t)b * ld + e] * s;
 }
 
 // out = a - b
@@ -95,13 +97,13 @@ __global__ void k_sub(const double* __restrict__ a, const double* __restrict__ b
     out[e] = a[e] - bb[e];
 }
 
-// X[b] -= dx[b] where mask[b] != 0
+// X[b] (stride ldx) -= dx[b] (stride ld) where mask[b] != 0
 __global__ void k_masked_sub(double* __restrict__ X, const double* __restrict__ dx, const int* __restrict__ mask,
-                             int n) {
+                             int n, int ldx, int ld) {
   const int b = blockIdx.y;
   if (!mask[b]) return;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
-    X[(size_t)b * n + e] -= dx[(size_t)b * n + e];
+    X[(size_t)b * ldx + e] -= dx[(size_t)b * ld + e];
 }
 
 // Start of a GMRES cycle.  nrm2[b] = ||r_b||^2.  Sets beta, g = [beta,0..], inv = 1/beta, and the
@@ -182,34 +184,82 @@ __global__ void k_solve_y(GmresState s, int B) {
   }
 }
 
+// ---- pseudo-arclength continuation helpers (Main.py:829-837, 910-917) ------------------------------
+// g[b][k][n] = dtPr * (-(k+1)) gr[n] T[b][k+1][n] for k < M-1, 0 for k = M-1: the psi right-hand side of
+// PDFmu (kGR_RT applied to T, Matrix_Operators.py:97-128); symmetric plans drop the odd T slots.
+__global__ void k_grk_T(const double* __restrict__ X, int ldx, double* __restrict__ g, int M, int nr,
+                        const double* __restrict__ gr, double dtPr, int sym) {
+  const int b = blockIdx.y;
+  const int N = M * nr;
+  const double* T = X + (size_t)b * ldx + N;
+  double* gb = g + (size_t)b * 3 * N;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 3 * N; e += gridDim.x * blockDim.x) {
+    double v = 0.0;
+    if (e < N) {
+      const int k = e / nr, n = e - k * nr;
+      if (k < M - 1 && !(sym && ((k + 1) & 1))) v = dtPr * ((-(double)(k + 1) * gr[n]) * T[(size_t)(k + 1) * nr + n]);
+    }
+    gb[e] = v;
+  }
+}
+
+// out[b][0..N) += v[b][n] * Jmu[b][0..N)  (psi block; Jmu stride ldj);  out[b][n] = delta*dot[b] + (1-delta)*mudot[b]*v[b][n]
+__global__ void k_border(const double* __restrict__ v, double* __restrict__ out, int n, int ld,
+                         const double* __restrict__ Jmu, int ldj, int Npsi, const double* __restrict__ dot,
+                         const double* __restrict__ mudot, double delta) {
+  const int b = blockIdx.y;
+  const double vl = v[(size_t)b * ld + n];
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < Npsi; e += gridDim.x * blockDim.x)
+    out[(size_t)b * ld + e] += vl * Jmu[(size_t)b * ldj + e];
+  if (blockIdx.x == 0 && threadIdx.x == 0) out[(size_t)b * ld + n] = delta * dot[b] + (1.0 - delta) * mudot[b] * vl;
+}
+
+// dst[b][e] (stride ldd) = a * src[b][e] (stride lds), e < n; optionally dst[b][n] = last[b]
+__global__ void k_copy_scaled(const double* __restrict__ src, int lds, double* __restrict__ dst, int ldd, int n,
+                              double a, const double* __restrict__ last) {
+  const int b = blockIdx.y;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
+    dst[(size_t)b * ldd + e] = a * src[(size_t)b * lds + e];
+  if (last && blockIdx.x == 0 && threadIdx.x == 0) dst[(size_t)b * ldd + n] = last[b];
+}
+
+// y[b] (stride ldy) = x0[b] (stride ldx0) + c[b] * d[b] (stride ldd), e < n
+__global__ void k_axpy_shell(const double* __restrict__ x0, int ldx0, const double* __restrict__ d, int ldd,
+                             const double* __restrict__ c, double* __restrict__ y, int ldy, int n) {
+  const int b = blockIdx.y;
+  const double cb = c[b];
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
+    y[(size_t)b * ldy + e] = x0[(size_t)b * ldx0 + e] + cb * d[(size_t)b * ldd + e];
+}
+
 // ---- host wrappers ------------------------------------------------------------------------------
 static int grid_x(int n) {
   int g = (n + 255) / 256;
   return g < 1 ? 1 : (g > 1024 ? 1024 : g);
 }
 
-cudaError_t krylov_dots(const double* V, size_t vstride_i, const double* w, int n, int nv, int B, double* part,
-                        double* h, int ldh, int accumulate, cudaStream_t st) {
+cudaError_t krylov_dots(const double* V, size_t vstride_i, const double* w, int n, int ld, int nv, int B,
+                        double* part, double* h, int ldh, int accumulate, cudaStream_t st) {
   const int nchunk = (n + kDotChunk - 1) / kDotChunk;
-  k_dot_partials<<<dim3(nchunk, B), kDotThreads, 0, st>>>(V, vstride_i, w, n, nv, kDotChunk, part);
+  k_dot_partials<<<dim3(nchunk, B), kDotThreads, 0, st>>>(V, vstride_i, w, n, ld, nv, kDotChunk, part);
   k_dot_reduce<<<B, 64, 0, st>>>(part, nv, nchunk, h, ldh, accumulate);
   return cudaGetLastError();
 }
 
 cudaError_t krylov_sub_combination(const double* V, size_t vstride_i, double* w, const double* coef, int ldc,
-                                   int n, int nv, int B, cudaStream_t st) {
-  k_sub_combination<<<dim3(grid_x(n), B), 256, 0, st>>>(V, vstride_i, w, coef, ldc, n, nv);
+                                   int n, int ld, int nv, int B, cudaStream_t st) {
+  k_sub_combination<<<dim3(grid_x(n), B), 256, 0, st>>>(V, vstride_i, w, coef, ldc, n, ld, nv);
   return cudaGetLastError();
 }
 
 cudaError_t krylov_add_combination(const double* V, size_t vstride_i, double* x, const double* y, int ldy,
-                                   const int* kb, int n, int B, cudaStream_t st) {
-  k_add_combination<<<dim3(grid_x(n), B), 256, 0, st>>>(V, vstride_i, x, y, ldy, kb, n);
+                                   const int* kb, int n, int ld, int B, cudaStream_t st) {
+  k_add_combination<<<dim3(grid_x(n), B), 256, 0, st>>>(V, vstride_i, x, y, ldy, kb, n, ld);
   return cudaGetLastError();
 }
 
-cudaError_t krylov_scale(const double* a, const double* scale, double* out, int n, int B, cudaStream_t st) {
-  k_scale<<<dim3(grid_x(n), B), 256, 0, st>>>(a, scale, out, n);
+cudaError_t krylov_scale(const double* a, const double* scale, double* out, int n, int ld, int B, cudaStream_t st) {
+  k_scale<<<dim3(grid_x(n), B), 256, 0, st>>>(a, scale, out, n, ld);
   return cudaGetLastError();
 }
 
@@ -218,8 +268,9 @@ cudaError_t krylov_sub(const double* a, const double* b, double* out, size_t n, 
   return cudaGetLastError();
 }
 
-cudaError_t krylov_masked_sub(double* X, const double* dx, const int* mask, int n, int B, cudaStream_t st) {
-  k_masked_sub<<<dim3(grid_x(n), B), 256, 0, st>>>(X, dx, mask, n);
+cudaError_t krylov_masked_sub(double* X, const double* dx, const int* mask, int n, int ldx, int ld, int B,
+                              cudaStream_t st) {
+  k_masked_sub<<<dim3(grid_x(n), B), 256, 0, st>>>(X, dx, mask, n, ldx, ld);
   return cudaGetLastError();
 }
 
@@ -230,6 +281,30 @@ cudaError_t krylov_cycle_start(const GmresState& s, const double* nrm2, int B, c
 
 cudaError_t krylov_arnoldi_finish(const GmresState& s, const double* nrm2, int j, int B, cudaStream_t st) {
   k_arnoldi_finish<<<(B + 63) / 64, 64, 0, st>>>(s, nrm2, j, B);
+  return cudaGetLastError();
+}
+
+cudaError_t contin_grk_T(const double* X, int ldx, double* g, int M, int nr, const double* gr, double dtPr, int sym,
+                         int B, cudaStream_t st) {
+  k_grk_T<<<dim3(grid_x(3 * M * nr), B), 256, 0, st>>>(X, ldx, g, M, nr, gr, dtPr, sym);
+  return cudaGetLastError();
+}
+
+cudaError_t contin_border(const double* v, double* out, int n, int ld, const double* Jmu, int ldj, int Npsi,
+                          const double* dot, const double* mudot, double delta, int B, cudaStream_t st) {
+  k_border<<<dim3(grid_x(Npsi), B), 256, 0, st>>>(v, out, n, ld, Jmu, ldj, Npsi, dot, mudot, delta);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_copy_scaled(const double* src, int lds, double* dst, int ldd, int n, double a, const double* last,
+                               int B, cudaStream_t st) {
+  k_copy_scaled<<<dim3(grid_x(n), B), 256, 0, st>>>(src, lds, dst, ldd, n, a, last);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_axpy_shell(const double* x0, int ldx0, const double* d, int ldd, const double* c, double* y,
+                              int ldy, int n, int B, cudaStream_t st) {
+  k_axpy_shell<<<dim3(grid_x(n), B), 256, 0, st>>>(x0, ldx0, d, ldd, c, y, ldy, n);
   return cudaGetLastError();
 }
 

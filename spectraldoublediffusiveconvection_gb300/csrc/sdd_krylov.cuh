@@ -25,17 +25,27 @@ struct GmresState {
   int* kb;          // [B] columns used
 };
 
-cudaError_t krylov_dots(const double* V, size_t vstride_i, const double* w, int n, int nv, int B, double* part,
-                        double* h, int ldh, int accumulate, cudaStream_t st);
+// n: used doubles per shell, ld: stride between shells (n <= ld)
+cudaError_t krylov_dots(const double* V, size_t vstride_i, const double* w, int n, int ld, int nv, int B,
+                        double* part, double* h, int ldh, int accumulate, cudaStream_t st);
 cudaError_t krylov_sub_combination(const double* V, size_t vstride_i, double* w, const double* coef, int ldc,
-                                   int n, int nv, int B, cudaStream_t st);
+                                   int n, int ld, int nv, int B, cudaStream_t st);
 cudaError_t krylov_add_combination(const double* V, size_t vstride_i, double* x, const double* y, int ldy,
-                                   const int* kb, int n, int B, cudaStream_t st);
-cudaError_t krylov_scale(const double* a, const double* scale, double* out, int n, int B, cudaStream_t st);
+                                   const int* kb, int n, int ld, int B, cudaStream_t st);
+cudaError_t krylov_scale(const double* a, const double* scale, double* out, int n, int ld, int B, cudaStream_t st);
 cudaError_t krylov_sub(const double* a, const double* b, double* out, size_t n, cudaStream_t st);
-cudaError_t krylov_masked_sub(double* X, const double* dx, const int* mask, int n, int B, cudaStream_t st);
+cudaError_t krylov_masked_sub(double* X, const double* dx, const int* mask, int n, int ldx, int ld, int B,
+                              cudaStream_t st);
 cudaError_t krylov_cycle_start(const GmresState& s, const double* nrm2, int B, cudaStream_t st);
 cudaError_t krylov_arnoldi_finish(const GmresState& s, const double* nrm2, int j, int B, cudaStream_t st);
 cudaError_t krylov_solve_y(const GmresState& s, int B, cudaStream_t st);
+cudaError_t krylov_copy_scaled(const double* src, int lds, double* dst, int ldd, int n, double a, const double* last,
+                               int B, cudaStream_t st);
+cudaError_t krylov_axpy_shell(const double* x0, int ldx0, const double* d, int ldd, const double* c, double* y,
+                              int ldy, int n, int B, cudaStream_t st);
+cudaError_t contin_grk_T(const double* X, int ldx, double* g, int M, int nr, const double* gr, double dtPr, int sym,
+                         int B, cudaStream_t st);
+cudaError_t contin_border(const double* v, double* out, int n, int ld, const double* Jmu, int ldj, int Npsi,
+                          const double* dot, const double* mudot, double delta, int B, cudaStream_t st);
 
 }  // namespace sdd

@@ -214,6 +214,31 @@ class Plan:
                      matvecs=r.matvecs, converged=bool(r.converged)) for r in res]
 
 
+    def contin_step(self, X, Ra, Ra_s, sign, ds, tol=1e-10, restart=50, gmres_rtol=1e-4, tangent_rtol=1e-8,
+                    max_restarts=20, max_corrector=5, max_halvings=8, mixed_matvec=False):
+        """One pseudo-arclength step (sdd_contin_step) in place on X (batch x n_state) and Ra (device,
+        batch).  Returns (X_dot tensor, per-shell result dicts)."""
+        torch = _torch()
+        B = self._chk(X, self.n_state, "X")
+        if not (isinstance(Ra, torch.Tensor) and Ra.dtype == torch.float64 and Ra.device == self.device
+                and Ra.numel() == B and Ra.is_contiguous()):
+            raise TypeError("Ra: expected a contiguous float64 device tensor with one entry per shell")
+        ras = self._vec(Ra_s, B)
+        Xd = torch.empty_like(X)
+        sg = (ctypes.c_double * B)(*[float(v) for v in np.broadcast_to(np.asarray(sign, dtype=float), (B,))])
+        dd = (ctypes.c_double * B)(*[float(v) for v in np.broadcast_to(np.asarray(ds, dtype=float), (B,))])
+        o = _lib.ContinOpts(float(tol), float(gmres_rtol), float(tangent_rtol), int(restart), int(max_restarts),
+                            int(max_corrector), int(max_halvings), int(bool(mixed_matvec)), 0)
+        res = (_lib.ContinResult * B)()
+        st = self._L.sdd_contin_step(self._h, B, _dptr(X), _dptr(Ra), _dptr(ras), _dptr(Xd), sg, dd,
+                                     ctypes.byref(o), res, _stream(self.device))
+        if st not in (_lib.SDD_OK, _lib.SDD_ERR_NOT_CONVERGED):
+            _lib.check(st, "sdd_contin_step")
+        return Xd, [dict(residual=r.residual, arclength=r.arclength, ds=r.ds, Ra_dot=r.Ra_dot,
+                         corrector_iters=r.corrector_iters, halvings=r.halvings, matvecs=r.matvecs,
+                         converged=bool(r.converged)) for r in res]
+
+
 _cache = {}
 _cache_lock = threading.Lock()
 

@@ -195,6 +195,31 @@ def trajectory_case(tag, N_r, N_fm, dt, n_steps, symmetric, seed, linear=False):
     print("wrote", tag, out["X_DATA"].shape)
 
 
+def continuation_case(tag, N_r, N_fm, Ra0, Tau, ds, n_steps, dt_ts, seed):
+    """A nontrivial steady convective state (Tau = 1, the reference's validation regime: critical Ra_T
+    near 7270 at d = 2, Tests/Run_Tests.py:55-65) and one pseudo-arclength step from it, both by the
+    reference: _Time_Step to saturation, _Newton to polish, then _ContinC (Main.py:742-955)."""
+    d, Pr, Ra_s = PARAMS["d"], PARAMS["Pr"], PARAMS["Ra_s"]
+    nr = N_r - 1
+    X0 = seeded_state(N_fm, nr, seed)
+    fname = f"golden_cont_{tag}.h5"
+    Xt = Main._Time_Step(X0.copy(), Ra0, Ra_s, Tau, Pr, d, N_fm, N_r, False, save_filename=fname,
+                         start_time=0, Total_time=n_steps * dt_ts, dt=dt_ts, linear=False, Verbose=False)
+    Xs, Norm, KE, NuT, NuS, ok = Main._Newton(Xt, Ra0, Ra_s, Tau, Pr, d, N_fm, N_r, False, dt=1,
+                                              tol_newton=1e-10, tol_gmres=1e-6, Krylov_Space_Size=300)
+    assert ok, "reference _Newton did not converge"
+    Y0 = np.hstack((Xs, Ra0))
+    out = Main._ContinC(0.0 * Y0, Y0, 1.0, ds, Ra0, Ra_s, Tau, Pr, d, N_fm, N_r, False, dt=1,
+                        tol_newton=1e-8, tol_gmres=1e-4, Krylov_Space_Size=300)
+    Y_dot, Y, sign, ds_new, Norm1, KE1, NuT1, NuS1, flag = out
+    res = dict(X_steady=Xs, Ra0=np.array(Ra0), Y=Y, Y_dot=Y_dot, ds_new=np.array(ds_new), ds=np.array(ds),
+               Norm=np.array(Norm1), KE=np.array(KE1), NuT=np.array(NuT1), NuS=np.array(NuS1),
+               steady_diag=np.array([Norm, KE, NuT, NuS]),
+               params=np.array([N_r, N_fm, 1.0, d, Pr, Tau, Ra0, Ra_s, 0.0]))
+    np.savez(os.path.join(HERE, f"cont_{tag}.npz"), **res)
+    print("wrote cont", tag, "|X_s| %.4e" % np.linalg.norm(Xs), "Ra %.6f -> %.6f" % (Ra0, Y[-1]))
+
+
 def transform_case():
     """Transforms.py:73-129 on seeded rows, with and without the 3/2 zero-padding length n."""
     rng = np.random.default_rng(7)
@@ -219,6 +244,9 @@ def transform_case():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) > 2 and sys.argv[2] == "--only-continuation":
+        continuation_case("tau1", N_r=16, N_fm=16, Ra0=9000.0, Tau=1.0, ds=50.0, n_steps=40000, dt_ts=5e-3, seed=31)
+        sys.exit(0)
     # the reference's own known-answer tests must pass before anything is recorded (Transforms.py:132-374)
     for k in range(4):
         Tr.test_Cosine_Transform(k, 64)
@@ -236,3 +264,4 @@ if __name__ == "__main__":
     trajectory_case("c1", N_r=20, N_fm=64, dt=1e-3, n_steps=2000, symmetric=False, seed=1234)
     trajectory_case("tiny", N_r=6, N_fm=8, dt=1e-3, n_steps=200, symmetric=False, seed=21)
     trajectory_case("sym_lin", N_r=8, N_fm=10, dt=5e-3, n_steps=100, symmetric=True, seed=22, linear=True)
+    continuation_case("tau1", N_r=16, N_fm=16, Ra0=9000.0, Tau=1.0, ds=50.0, n_steps=40000, dt_ts=5e-3, seed=31)
