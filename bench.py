@@ -234,6 +234,56 @@ def bench_batched(device, precision, steps=1000, steps_per_launch=10, n_shells=6
 
 
 # ------------------------------------------------------------------------------------------------
+# served workload: Poisson arrivals of continuation steps and 500-step integrations
+# ------------------------------------------------------------------------------------------------
+SERVED_SHAPES = [(nr, m) for nr in (20, 28, 36, 48) for m in (64, 128, 256, 512)]
+
+
+def bench_served(device, n_requests=1000, rate=200.0, seed=2024, frac_continue=0.7, con_workers=4, branch=None):
+    import numpy as np
+    import torch
+    from spectraldoublediffusiveconvection_gb300 import serve
+    t0 = time.perf_counter()
+    if branch is None:
+        branch = serve.branch_states(SERVED_SHAPES, Ra=9000.0, d=2.0, Pr=1.0, Tau=1.0, Ra_s=500.0, device=device)
+    t_branch = time.perf_counter() - t0
+    shapes = [s for s in SERVED_SHAPES if s in branch]
+    srv = serve.Server(d=2.0, Pr=1.0, Tau=1.0, Ra_s=500.0, dt=1e-3, device=device, chain_layout=1,
+                       con_workers=con_workers).start()
+    # warm-up: one request of each kind and shape builds the plans and workspaces
+    warm = []
+    for sh in shapes:
+        warm.append(srv.submit(serve.Request("continue", sh[0], sh[1], 9000.0, X=branch[sh][0], sign=1.0, ds=50.0)))
+        warm.append(srv.submit(serve.Request("integrate", sh[0], sh[1], 9000.0, n_steps=50, seed=1)))
+    srv.drain()
+    torch.cuda.synchronize(device)
+    wl = serve.poisson_workload(n_requests, rate, shapes, branch, frac_continue=frac_continue, n_steps=500,
+                                ds=50.0, seed=seed)
+    st0 = dict(srv.stats)
+    wall = serve.run_workload(srv, wl)
+    srv.stop()
+    reqs = [r for _, r in wl]
+    con = [r for r in reqs if r.kind == "continue"]
+    ok_con = [r for r in con if r.error is None and r.result["converged"] and r.result["residual"] <= 1e-10]
+    ok_int = [r for r in reqs if r.kind == "integrate" and r.error is None and np.isfinite(r.result["X"]).all()]
+    lat = serve.latency_report(reqs)
+    return {"solves_per_s": (len(ok_con) + len(ok_int)) / wall, "requests": len(reqs), "wall_s": wall,
+            "offered_rate_per_s": rate, "p50_ms": lat.get("p50_ms"), "p99_ms": lat.get("p99_ms"),
+            "continuation": dict(serve.latency_report(con), n=len(con), converged_le_1e10=len(ok_con),
+                                 max_residual=max((r.result["residual"] for r in con if r.result), default=None),
+                                 mean_corrector_iters=float(np.mean([r.result["corrector_iters"] for r in con
+                                                                     if r.result])) if con else None),
+            "integration": dict(serve.latency_report([r for r in reqs if r.kind == "integrate"]),
+                                n=len(reqs) - len(con), finite=len(ok_int)),
+            "errors": sum(r.error is not None for r in reqs),
+            "batching": {k: srv.stats[k] - st0[k] for k in srv.stats},
+            "shapes": [f"{a}x{b}" for a, b in shapes], "branch_seconds": t_branch,
+            "workload": "Poisson arrivals; 70% pseudo-arclength steps (ds=50, sign +-1) from steady states at "
+                        "Ra_T=9000 on the Tau=1 branch, 30% 500-step integrations (dt=1e-3, Ra_T~U[8500,9500]) from "
+                        "seeded states; N_r in {20,28,36,48}, N_theta in {64,128,256,512}; Ra_S=500, Pr=1, d=2"}
+
+
+# ------------------------------------------------------------------------------------------------
 # GB300 arm
 # ------------------------------------------------------------------------------------------------
 def bench_gb300(args):
@@ -388,6 +438,10 @@ def bench_gb300(args):
                    "workload": "64 shells, N_r in {20,24,30,36}, N_theta in {64,128,256,384}, Ra_T ~ U[6000,12000],"
                                " Ra_S=500, Pr=1, Tau=0.01, dt=1e-3, 1000 steps each (seed 1234)"}
 
+    served = None
+    if rank == 0 and not args.no_served:
+        served = bench_served(device, n_requests=args.served_requests)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         r = run_cpu_baseline(seconds=args.cpu_seconds, threads=1, steps_per_sample=5)
@@ -406,7 +460,8 @@ def bench_gb300(args):
                         "d2h_bytes_per_step": nbytes,
                         "api": "Plan.step on a pinned host state copied in/out every bench step"},
                 "gpu_launches": args.steps * chunk * 3,
-                "roofline": roofline, "cpu_baseline": cpu, "clocks": ck, "newton": newton, "batched": batched}
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": ck, "newton": newton, "batched": batched,
+                "served": served}
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
@@ -427,6 +482,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--served-requests", type=int, default=1000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

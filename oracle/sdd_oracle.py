@@ -601,6 +601,47 @@ def Kinetic_Energy(X_hat, R, D, N_fm, nr, symmetric):
 
 
 # ---------------------------------------------------------------------------------------------------
+# resolution changes  (Matrix_Operators.py:901-1011)
+# ---------------------------------------------------------------------------------------------------
+
+
+def INTERP_RADIAL(N_n, N_o, X_o, d):
+    """Matrix_Operators.py:901-941: polyfit of degree len(R_o) through (R_o, [0, X, 0]), polyval on R_n."""
+    import warnings
+    if N_n == N_o:
+        return X_o
+    _, R_n = cheb_radial(N_n, d)
+    _, R_o = cheb_radial(N_o, d)
+    nr_n, nr_o = len(R_n[1:-1]), len(R_o[1:-1])
+    N_fm = len(X_o) // (3 * nr_o)
+    X_n = np.zeros(3 * nr_n * N_fm)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        for k in range(N_fm):
+            for f in range(3):
+                io = f * N_fm * nr_o + nr_o * k
+                poly = np.polyfit(R_o, np.hstack(([0.0], X_o[io:io + nr_o], [0.0])), len(R_o))
+                i_n = f * N_fm * nr_n + nr_n * k
+                X_n[i_n:i_n + nr_n] = np.polyval(poly, R_n[1:-1])
+    return X_n
+
+
+def INTERP_THETAS(N_fm_n, N_fm_o, X_o):
+    """Matrix_Operators.py:944-1011: IDST/IDCT of the (zero-padded) modes, DST/DCT back with n = N_fm_n
+    (psi rows in storage order, as the reference)."""
+    if N_fm_n == N_fm_o:
+        return X_o
+    nr = len(X_o) // (3 * N_fm_o)
+    Mx = max(N_fm_n, N_fm_o)
+    V = np.asarray(X_o, dtype=float).reshape(3, N_fm_o, nr)
+    F = np.zeros((3, nr, Mx))
+    for f in range(3):
+        F[f, :, :N_fm_o] = V[f].T
+    out = np.stack([DST(IDST(F[0]), n=N_fm_n), DCT(IDCT(F[1]), n=N_fm_n), DCT(IDCT(F[2]), n=N_fm_n)])
+    return np.ascontiguousarray(out.transpose(0, 2, 1)).reshape(-1)
+
+
+# ---------------------------------------------------------------------------------------------------
 # seeded synthetic states
 # ---------------------------------------------------------------------------------------------------
 

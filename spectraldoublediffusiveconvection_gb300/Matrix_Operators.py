@@ -10,6 +10,7 @@ the layout helpers ``Vecs_to_X``/``X_to_Vecs`` for numpy input.
 Operators handed in as arrays are uploaded once per distinct content and cached in a device plan.
 """
 import hashlib
+import warnings
 
 import numpy as np
 
@@ -208,3 +209,45 @@ def X_to_Vecs(X, N_fm, nr, symmetric):
         out[1][:, 1::2] = 0.0
         out[2][:, 1::2] = 0.0
     return tuple(out)
+
+
+# ---- resolution changes (load-time) ----------------------------------------------------------------
+def INTERP_RADIAL(N_n, N_o, X_o, d):
+    """Matrix_Operators.py:901-941: per mode and field, a polynomial through the old collocation values
+    (with the zero boundary values), evaluated on the new interior points.  Load-time host code (numpy
+    polyfit/polyval, as the reference)."""
+    if N_n == N_o:
+        return X_o
+    X_o = np.asarray(X_o.cpu() if hasattr(X_o, "cpu") else X_o, dtype=np.float64)
+    _, R_n = cheb_radial(N_n, d)
+    _, R_o = cheb_radial(N_o, d)
+    nr_n, nr_o = len(R_n[1:-1]), len(R_o[1:-1])
+    N_fm = len(X_o) // (3 * nr_o)
+    X_n = np.zeros(3 * nr_n * N_fm)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        for k in range(N_fm):
+            for f in range(3):
+                io = f * N_fm * nr_o + nr_o * k
+                poly = np.polyfit(R_o, np.hstack(([0.0], X_o[io:io + nr_o], [0.0])), len(R_o))
+                i_n = f * N_fm * nr_n + nr_n * k
+                X_n[i_n:i_n + nr_n] = np.polyval(poly, R_n[1:-1])
+    return X_n
+
+
+def INTERP_THETAS(N_fm_n, N_fm_o, X_o):
+    """Matrix_Operators.py:944-1011: theta resolution change by a transform to the grid and back (the
+    transforms run on the GPU).  Like the reference, the psi rows go through IDST/DST in storage order."""
+    from .Transforms import DCT, DST, IDCT, IDST
+    if N_fm_n == N_fm_o:
+        return X_o
+    X_o = np.asarray(X_o.cpu() if hasattr(X_o, "cpu") else X_o, dtype=np.float64)
+    nr = len(X_o) // (3 * N_fm_o)
+    Mx = max(N_fm_n, N_fm_o)
+    V = X_o.reshape(3, N_fm_o, nr)
+    F = np.zeros((3, nr, Mx))
+    for f in range(3):
+        F[f, :, :N_fm_o] = V[f].T
+    PSI_X, T_X, S_X = IDST(F[0]), IDCT(F[1]), IDCT(F[2])
+    out = np.stack([DST(PSI_X, n=N_fm_n), DCT(T_X, n=N_fm_n), DCT(S_X, n=N_fm_n)])   # (3, nr, N_fm_n)
+    return np.ascontiguousarray(out.transpose(0, 2, 1)).reshape(-1)

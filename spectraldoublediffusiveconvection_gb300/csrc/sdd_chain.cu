@@ -205,13 +205,12 @@ cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStre
   a.g = a.h;
   a.g_stride = a.h_stride;
   const size_t smem = chain_smem_bytes(a.M, a.nr, a.ldl);
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
+  static const int sms = [] {  // thread-safe one-time initialisation (host threads may launch concurrently)
+    int dev = 0, n = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+  }();
   const dim3 grid(2 * nfields, batch);
   const bool split = a.layout == 4 || (a.layout == 0 && 2 * nfields * batch <= sms);
   if (split && a.nr <= 32) {

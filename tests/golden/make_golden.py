@@ -220,6 +220,18 @@ def continuation_case(tag, N_r, N_fm, Ra0, Tau, ds, n_steps, dt_ts, seed):
     print("wrote cont", tag, "|X_s| %.4e" % np.linalg.norm(Xs), "Ra %.6f -> %.6f" % (Ra0, Y[-1]))
 
 
+def interp_case():
+    """Matrix_Operators.py:901-1011 INTERP_RADIAL / INTERP_THETAS on a seeded state (up and down)."""
+    X = seeded_state(16, 11, 41)                         # N_r = 12, N_fm = 16
+    out = dict(X=X,
+               rad_up=MO.INTERP_RADIAL(20, 12, X, 2.0),
+               rad_down=MO.INTERP_RADIAL(8, 12, X, 2.0),
+               th_up=MO.INTERP_THETAS(32, 16, X),
+               th_down=MO.INTERP_THETAS(8, 16, X))
+    np.savez(os.path.join(HERE, "interp.npz"), **out)
+    print("wrote interp")
+
+
 def transform_case():
     """Transforms.py:73-129 on seeded rows, with and without the 3/2 zero-padding length n."""
     rng = np.random.default_rng(7)
@@ -244,6 +256,9 @@ def transform_case():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) > 2 and sys.argv[2] == "--only-interp":
+        interp_case()
+        sys.exit(0)
     if len(sys.argv) > 2 and sys.argv[2] == "--only-continuation":
         continuation_case("tau1", N_r=16, N_fm=16, Ra0=9000.0, Tau=1.0, ds=50.0, n_steps=40000, dt_ts=5e-3, seed=31)
         sys.exit(0)
@@ -265,3 +280,4 @@ if __name__ == "__main__":
     trajectory_case("tiny", N_r=6, N_fm=8, dt=1e-3, n_steps=200, symmetric=False, seed=21)
     trajectory_case("sym_lin", N_r=8, N_fm=10, dt=5e-3, n_steps=100, symmetric=True, seed=22, linear=True)
     continuation_case("tau1", N_r=16, N_fm=16, Ra0=9000.0, Tau=1.0, ds=50.0, n_steps=40000, dt_ts=5e-3, seed=31)
+    interp_case()

@@ -189,3 +189,17 @@ def test_odd_modes_raise(cuda):
     D, R = MO.cheb_radial(8, 2.0)
     with pytest.raises(ValueError):
         MO.NLIN_FX(np.zeros(3 * 7 * 7), D, R, 7, 7, False)
+
+
+def test_interpolation_dropins_match_reference(cuda):
+    from spectraldoublediffusiveconvection_gb300 import Matrix_Operators as MO
+    Z = load_golden("interp.npz")
+    X = Z["X"]
+    # The reference's radial interpolation is np.polyfit of degree N_o+1 through N_o+1 points: an
+    # underdetermined, ill-conditioned Vandermonde least-squares problem whose minimum-norm answer
+    # depends on the platform's LAPACK at ~1e-6 relative (x86-64 vs aarch64 OpenBLAS differ by 2e-6),
+    # so the radial check carries that tolerance; the theta transforms are well conditioned.
+    assert rel(MO.INTERP_RADIAL(20, 12, X, 2.0), Z["rad_up"]) < 2e-5
+    assert rel(MO.INTERP_RADIAL(8, 12, X, 2.0), Z["rad_down"]) < 2e-5
+    assert rel(MO.INTERP_THETAS(32, 16, X), Z["th_up"]) < 1e-13
+    assert rel(MO.INTERP_THETAS(8, 16, X), Z["th_down"]) < 1e-13

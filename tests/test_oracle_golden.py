@@ -70,3 +70,16 @@ def test_trajectory_matches_reference(tag):
     assert rel(XN, Z["X_final"]) < 1e-12
     for s, r in zip(snaps, Z["X_DATA"]):
         assert rel(s, r) < 1e-12
+
+
+def test_interpolation_matches_reference():
+    Z = load_golden("interp.npz")
+    X = Z["X"]
+    # The reference's radial interpolation is np.polyfit of degree N_o+1 through N_o+1 points: an
+    # underdetermined, ill-conditioned Vandermonde least-squares problem whose minimum-norm answer
+    # depends on the platform's LAPACK at ~1e-6 relative (x86-64 vs aarch64 OpenBLAS differ by 2e-6),
+    # so the radial check carries that tolerance; the theta transforms are well conditioned.
+    assert rel(O.INTERP_RADIAL(20, 12, X, 2.0), Z["rad_up"]) < 2e-5
+    assert rel(O.INTERP_RADIAL(8, 12, X, 2.0), Z["rad_down"]) < 2e-5
+    assert rel(O.INTERP_THETAS(32, 16, X), Z["th_up"]) < 1e-13
+    assert rel(O.INTERP_THETAS(8, 16, X), Z["th_down"]) < 1e-13
