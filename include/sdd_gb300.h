@@ -89,9 +89,10 @@ int sdd_plan_create(const sdd_plan_desc* desc, sdd_plan** plan);
 int sdd_plan_destroy(sdd_plan* plan);
 /* Pre-allocates the plan's workspace for up to max_batch shells (otherwise grown on first use). */
 int sdd_plan_reserve(sdd_plan* plan, int max_batch);
-/* Chain-kernel layout of the implicit solves: 0 automatic (split rows over 4 warps when the launch
- * leaves SMs idle, else one lane per row), 1 one lane per row, 4 split rows over 4 warps.  Set by the
- * batch autotuner; no counterpart in the reference. */
+/* Chain-kernel layout of the implicit solves: 0 automatic (chunked while its CTAs fit the GPU at two per
+ * SM, else split rows over 4 warps when the launch leaves SMs idle, else one lane per row), 1 one lane
+ * per row, 2 chunked (each chain cut into chunks that run concurrently, joined by a short carried-state
+ * recurrence), 4 split rows over 4 warps.  Set by the batch autotuner; no counterpart in the reference. */
 int sdd_plan_set_chain_layout(sdd_plan* plan, int layout);
 /* FP64 elements of one shell's base-state grid cache used by sdd_nlin_dfx (9 * nr * 3N_fm/2). */
 size_t sdd_plan_base_cache_elems(const sdd_plan* plan);

@@ -118,7 +118,7 @@ class ShellBatch:
         torch.cuda.synchronize(self.device)
         return (time.perf_counter() - t0) / reps
 
-    def autotune(self, steps_per_launch=5, reps=3, layouts=(1, 4)):
+    def autotune(self, steps_per_launch=5, reps=3, layouts=(1, 2, 4)):
         """Greedy per-group choice of the chain layout minimising the time of one graph launch.  The
         shells' states are restored afterwards: tuning does not advance them."""
         saved = [g.X.clone() for g in self.groups]

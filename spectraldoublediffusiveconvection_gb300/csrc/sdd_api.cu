@@ -1,6 +1,7 @@
 // C ABI of libsdd_gb300: plans (device-resident operators), FFT tables, workspaces, entry points.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -97,6 +98,10 @@ struct sdd_plan {
   double *LinvA4, *LinvT, *LinvS;
   double *ABA4;                     // transposed [A_j B_j] of the psi chain
   double *coefA4, *coefT, *coefS;   // per-step scalars of the chains
+  // chunked chains (layout 2): chunk length, chunk count, leading dimensions and tables
+  int kc, nch, ldmA, ldmT, ldd;
+  double *GA4, *GT, *GS, *PhiA4, *PhiT, *PhiS;
+  double *dbuf, *cbuf;              // [B][3][2][nch][ldd] chunk end states / carried states
   // FP32 copies used by the mixed-precision nonlinear term
   float *Dr32, *D2r232, *ir4r232;
   // workspace
@@ -197,12 +202,109 @@ static void solver_free(sdd_plan* p) {
 static void free_plan(sdd_plan* p) {
   if (!p) return;
   double* d[] = {p->Dr, p->D2r2, p->ir4r2, p->D2s, p->ir2s, p->D2A4, p->ir2A4, p->ir4A4, p->rsq, p->dT0,
-                 p->gr, p->LinvA4, p->LinvT, p->LinvS, p->out4, p->rhs, p->xtmp, p->coefA4, p->coefT, p->coefS, p->ABA4, p->hbuf};
+                 p->gr, p->LinvA4, p->LinvT, p->LinvS, p->out4, p->rhs, p->xtmp, p->coefA4, p->coefT, p->coefS, p->ABA4, p->hbuf,
+                 p->GA4, p->GT, p->GS, p->PhiA4, p->PhiT, p->PhiS, p->dbuf, p->cbuf};
   for (double* x : d) cudaFree(x);
   cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232);
   cudaFree(p->base_tmp);
   solver_free(p);
   delete p;
+}
+
+// Tables of the chunked chains.  Within a chunk that starts with carried state s, the state before step
+// k is Psi_k s + (its value from a zero start) and f_k = (zero-start f_k) + G_k s, with
+//   psi (s = [f_e; bf_e], m = 2 nr):  G_k = C_k Psi_k, C_k = [A_k B_k];
+//     Psi_{k+1} = [[I, 0], [bjt I, I]] Psi_k + [I; bj I] G_k   (f_e += f, bf_e += bj f + bjt f_e)
+//   T/S (s = b, m = nr):  G_k = -w_k Linv_k Psi_k,  Psi_{k+1} = Psi_k + k_{k+1} G_k   (b += k f before
+//     the next step, k = 2 dt (j+2) of that step, w = 0.5 for j = 0 else 1)
+// with Psi = I at the chunk start, and Phi_c = Psi after the chunk's last step.  G is stored transposed
+// per mode ([jj][m cols][ldl]) and Phi per (parity, chunk) ([m cols][ldm]).
+static void matmul_rows(const double* A, const double* B, double* C, int n, int k, int m) {  // C = A B
+  for (int i = 0; i < n; ++i) {
+    double* c = C + (size_t)i * m;
+    for (int j = 0; j < m; ++j) c[j] = 0.0;
+    for (int l = 0; l < k; ++l) {
+      const double a = A[(size_t)i * k + l];
+      const double* b = B + (size_t)l * m;
+      for (int j = 0; j < m; ++j) c[j] += a * b[j];
+    }
+  }
+}
+
+static int build_chunk_tables(sdd_plan* p, const double* AB, const double* LinvT, const double* LinvS,
+                              const double* cA, const double* cT, const double* cS) {
+  const int M = p->M, nr = p->nr, ldl = p->ldl, S = M / 2;
+  int kc = (int)std::lround(std::sqrt(2.0 * S));
+  kc = std::max(4, std::min(32, kc));
+  const int nch = (S + kc - 1) / kc;
+  p->kc = kc;
+  p->nch = nch;
+  p->ldmA = 2 * nr;
+  p->ldmT = nr + (nr & 1);
+  p->ldd = 2 * nr;
+  {  // psi
+    const int m = 2 * nr, ldm = p->ldmA;
+    std::vector<double> G((size_t)M * m * ldl, 0.0), Phi((size_t)2 * nch * m * ldm, 0.0);
+    std::vector<double> Psi((size_t)m * m), Gs((size_t)nr * m), C((size_t)nr * m);
+    for (int par = 0; par < 2; ++par)
+      for (int c = 0; c < nch; ++c) {
+        std::fill(Psi.begin(), Psi.end(), 0.0);
+        for (int i = 0; i < m; ++i) Psi[(size_t)i * m + i] = 1.0;
+        for (int s = c * kc; s < std::min(S, (c + 1) * kc); ++s) {
+          const int jj = par + 2 * s;
+          const double* blk = AB + (size_t)jj * 2 * nr * ldl;
+          for (int i = 0; i < nr; ++i)
+            for (int col = 0; col < m; ++col) C[(size_t)i * m + col] = blk[(size_t)col * ldl + i];
+          matmul_rows(C.data(), Psi.data(), Gs.data(), nr, m, m);
+          for (int i = 0; i < nr; ++i)
+            for (int col = 0; col < m; ++col) G[((size_t)jj * m + col) * ldl + i] = Gs[(size_t)i * m + col];
+          const double bj = cA[4 * jj + 2], bjt = cA[4 * jj + 3];
+          for (int i = 0; i < nr; ++i)
+            for (int col = 0; col < m; ++col) {
+              const double top = Psi[(size_t)i * m + col], g = Gs[(size_t)i * m + col];
+              Psi[(size_t)(nr + i) * m + col] += bjt * top + bj * g;
+              Psi[(size_t)i * m + col] = top + g;
+            }
+        }
+        if (c + 1 < nch)
+          for (int i = 0; i < m; ++i)
+            for (int col = 0; col < m; ++col)
+              Phi[(((size_t)par * nch + c) * m + col) * ldm + i] = Psi[(size_t)i * m + col];
+      }
+    int st;
+    if ((st = upload(&p->GA4, G.data(), G.size())) || (st = upload(&p->PhiA4, Phi.data(), Phi.size()))) return st;
+  }
+  for (int fld = 1; fld <= 2; ++fld) {  // T, S
+    const int m = nr, ldm = p->ldmT;
+    const double* Linv = fld == 1 ? LinvT : LinvS;
+    const double* cf = fld == 1 ? cT : cS;
+    std::vector<double> G((size_t)M * m * ldl, 0.0), Phi((size_t)2 * nch * m * ldm, 0.0);
+    std::vector<double> Psi((size_t)m * m), Gs((size_t)nr * m);
+    for (int par = 0; par < 2; ++par)
+      for (int c = 0; c < nch; ++c) {
+        std::fill(Psi.begin(), Psi.end(), 0.0);
+        for (int i = 0; i < m; ++i) Psi[(size_t)i * m + i] = 1.0;
+        for (int s = c * kc; s < std::min(S, (c + 1) * kc); ++s) {
+          const int jj = par + 2 * s;
+          matmul_rows(Linv + (size_t)jj * nr * nr, Psi.data(), Gs.data(), nr, nr, m);
+          const double w = cf[4 * jj + 1];
+          for (double& x : Gs) x *= -w;
+          for (int i = 0; i < nr; ++i)
+            for (int col = 0; col < m; ++col) G[((size_t)jj * m + col) * ldl + i] = Gs[(size_t)i * m + col];
+          const double knext = (s + 1 < S) ? cf[4 * (jj + 2)] : 0.0;
+          for (size_t e = 0; e < Psi.size(); ++e) Psi[e] += knext * Gs[e];
+        }
+        if (c + 1 < nch)
+          for (int i = 0; i < m; ++i)
+            for (int col = 0; col < m; ++col)
+              Phi[(((size_t)par * nch + c) * m + col) * ldm + i] = Psi[(size_t)i * m + col];
+      }
+    int st;
+    double** gd = fld == 1 ? &p->GT : &p->GS;
+    double** pd = fld == 1 ? &p->PhiT : &p->PhiS;
+    if ((st = upload(gd, G.data(), G.size())) || (st = upload(pd, Phi.data(), Phi.size()))) return st;
+  }
+  return SDD_OK;
 }
 
 int sdd_plan_create(const sdd_plan_desc* d, sdd_plan** out) {
@@ -290,7 +392,8 @@ int sdd_plan_create(const sdd_plan_desc* d, sdd_plan** out) {
         }
       }
     }
-    if ((st = upload(&p->ABA4, AB.data(), AB.size()))) {
+    if ((st = upload(&p->ABA4, AB.data(), AB.size())) ||
+        (st = build_chunk_tables(p, AB.data(), d->Linv_T, d->Linv_S, cA.data(), cT.data(), cS.data()))) {
       free_plan(p);
       return st;
     }
@@ -306,7 +409,7 @@ int sdd_plan_destroy(sdd_plan* p) {
 }
 
 int sdd_plan_set_chain_layout(sdd_plan* p, int layout) {
-  if (!p || (layout != 0 && layout != 1 && layout != 4)) return SDD_ERR_ARG;
+  if (!p || (layout != 0 && layout != 1 && layout != 2 && layout != 4)) return SDD_ERR_ARG;
   p->chain_layout = layout;
   return SDD_OK;
 }
@@ -319,7 +422,8 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   if (!p || max_batch < 1) return SDD_ERR_ARG;
   if (max_batch <= p->ws_batch) return SDD_OK;
   cudaFree(p->out4); cudaFree(p->rhs); cudaFree(p->xtmp); cudaFree(p->base_tmp); cudaFree(p->hbuf);
-  p->out4 = p->rhs = p->xtmp = p->hbuf = nullptr;
+  cudaFree(p->dbuf); cudaFree(p->cbuf);
+  p->out4 = p->rhs = p->xtmp = p->hbuf = p->dbuf = p->cbuf = nullptr;
   p->base_tmp = nullptr;
   p->ws_batch = 0;
   const size_t se = shell_elems(p);
@@ -329,6 +433,9 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   SDD_CUDA(cudaMalloc(&p->xtmp, (size_t)max_batch * se * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->hbuf, (size_t)max_batch * se * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->base_tmp, (size_t)max_batch * be * sizeof(double)));
+  const size_t de = (size_t)6 * p->nch * p->ldd;
+  SDD_CUDA(cudaMalloc(&p->dbuf, (size_t)max_batch * de * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->cbuf, (size_t)max_batch * de * sizeof(double)));
   p->ws_batch = max_batch;
   return SDD_OK;
 }
@@ -381,6 +488,10 @@ static ChainArgs chain_args(const sdd_plan* p, const double* g, double* f, const
   a.h_stride = shell_elems(p);
   a.coefA4 = p->coefA4; a.coefT = p->coefT; a.coefS = p->coefS;
   a.dtA4 = p->Pr * p->dt; a.dtT = p->dt; a.dtS = p->Tau * p->dt;
+  a.kc = p->kc; a.nch = p->nch; a.ldmA = p->ldmA; a.ldmT = p->ldmT; a.ldd = p->ldd;
+  a.GA4 = p->GA4; a.GT = p->GT; a.GS = p->GS; a.PhiA4 = p->PhiA4; a.PhiT = p->PhiT; a.PhiS = p->PhiS;
+  a.dbuf = p->dbuf; a.cbuf = p->cbuf;
+  a.d_stride = (size_t)6 * p->nch * p->ldd;
   return a;
 }
 

@@ -17,11 +17,18 @@
 // Cost model (measured on GB300): an FP64 warp instruction occupies its SM sub-partition (SMSP) for 64
 // cycles whatever the number of active lanes, and a dependent FP64 chain also advances one instruction
 // per 64 cycles.  A chain is therefore bound by the FP64 warp-instructions each SMSP issues per step.
-// Two layouts, picked by the launcher:
+// Layouts, picked by the launcher:
 //   TPR = 4 (nr <= 32) or 2 (nr <= 64), 4 warps: every matrix row is split over TPR lanes and the rows
 //     over 4 warps, one per SMSP.  Lowest latency for one chain on an otherwise idle SM.
 //   TPR = 1, ceil(nr/32) warps: one lane per row, no reduction adds.  Fewest FP64 instructions per
 //     chain, used when a batch puts several chains on every SM.
+//   chunked (layout 2): the S = N_fm/2 steps of a chain are cut into nch chunks of kc steps that run
+//     concurrently, each from a zero carried state (its own CTA, h = Linv g computed in its prologue).
+//     The chain's carried state s (psi: [f_e; bf_e], 2 nr; T/S: b, nr) enters every later step linearly,
+//     so with the plan's precomputed Phi_c (state over a whole chunk) and G_jj (state -> f_jj):
+//       s_1 = d_0,  s_{c+1} = Phi_c s_c + d_c   (k_chain_carry, one CTA per chain, nch - 2 matvecs)
+//       f_jj += G_jj s_c(jj)                    (k_chain_fix, all modes in parallel)
+//     The critical path drops from S dependent steps to kc + (nch - 2) carried matvecs + one matvec.
 // Matrices are stored transposed (column c contiguous, leading dimension ldl); the block of step s+2
 // streams global->shared with cp.async while step s runs (3-slot ring).  FP64 throughout.
 #include <cuda_runtime.h>
@@ -65,7 +72,12 @@ __device__ __forceinline__ void chain_sync() {
   else __syncthreads();
 }
 
-template <int TPR>
+// One chain (field, parity) of one shell: steps [s0, s1) of the S = (M - par + 1)/2 chain steps.
+// CHUNK = false: the whole chain (s0 = 0, s1 = S) with h = Linv g precomputed by k_hpre.
+// CHUNK = true: chunk blockIdx.z of a.kc steps, started from a zero carried state, computing its own
+// h = Linv g rows first; the end state goes to dbuf (psi: [f_e; bf_e]; T/S: b + k_next f_last, the b the
+// next chunk's first step uses).
+template <int TPR, bool CHUNK>
 __global__ void k_chain(ChainArgs a) {
   extern __shared__ __align__(16) double csm[];
   const int field = a.field0 + (blockIdx.x >> 1);
@@ -74,7 +86,6 @@ __global__ void k_chain(ChainArgs a) {
   const int M = a.M, nr = a.nr, ldl = a.ldl;
   const bool a4 = (field == 0);
   const size_t foff = (size_t)field * a.field_off;
-  const double* h = a.g + (size_t)b * a.g_stride + foff;       // h_j = Linv_j g_j (k_hpre)
   double* f = a.f + (size_t)b * a.f_stride + foff;
   const double* sub = a.sub ? a.sub + (size_t)b * a.sub_stride + foff : nullptr;
   const int tid = threadIdx.x;
@@ -82,46 +93,73 @@ __global__ void k_chain(ChainArgs a) {
   const bool row_ok = i < nr;
   const bool lead = row_ok && q == 0;     // the lane that owns row i's elementwise state
   const int ir = row_ok ? i : 0;
-  const int nsteps = (M - par + 1) / 2;
+  const int S = (M - par + 1) / 2;
+  const int chunk = CHUNK ? (int)blockIdx.z : 0;
+  const int s0 = CHUNK ? chunk * a.kc : 0;
+  const int s1 = CHUNK ? min(S, s0 + a.kc) : S;
+  if (s0 >= S) return;
+  const int nsteps = s1 - s0;
+  double* dout = CHUNK ? a.dbuf + (size_t)b * a.d_stride + ((size_t)(field * 2 + par) * a.nch + chunk) * a.ldd
+                       : nullptr;
 
   // symmetric: only the "evens" loops run (A4 jj = 0,2,..; NAB2 jj = 1,3,..); other rows stay 0.
   const bool active = !a.sym || (a4 ? par == 0 : par == 1);
   if (!active) {
     for (int e = tid; e < nsteps * nr; e += blockDim.x) {
       const int s = e / nr, c = e - s * nr;
-      f[(size_t)(M - 1 - (par + 2 * s)) * nr + c] = 0.0;
+      f[(size_t)(M - 1 - (par + 2 * (s0 + s))) * nr + c] = 0.0;
     }
+    if (CHUNK)
+      for (int e = tid; e < a.ldd; e += blockDim.x) dout[e] = 0.0;
     return;
   }
 
   const int ncol = a4 ? 2 * nr : nr;           // columns of the step matrix ([A B] or Linv)
   const int blk = ncol * ldl;
   double* Lb0 = csm;                           // 3-slot ring of step matrices
-  double* hs = csm + 3 * blk;                  // the chain's h rows, step-ordered
+  double* hs = csm + 3 * blk;                  // the chunk's h rows, step-ordered
   double* cf = hs + (size_t)nsteps * nr;       // per-step scalars (4 per step)
   double* x2 = cf + 4 * (size_t)nsteps;        // matvec operand: A4 [f_e; bf_e], NAB2 b
   const double* Mat = a4 ? a.ABA4 : (field == 1 ? a.LinvT : a.LinvS);
   const double* coef = a4 ? a.coefA4 : (field == 1 ? a.coefT : a.coefS);   // [M][4] indexed by jj
+  const int jj0 = par + 2 * s0;
 
-  copy_block(Lb0, Mat + (size_t)par * blk, blk);
+  copy_block(Lb0, Mat + (size_t)jj0 * blk, blk);
   cp_async_commit();
-  if (nsteps > 1) copy_block(Lb0 + blk, Mat + (size_t)(par + 2) * blk, blk);
+  if (nsteps > 1) copy_block(Lb0 + blk, Mat + (size_t)(jj0 + 2) * blk, blk);
   cp_async_commit();
-  for (int e = tid; e < nsteps * nr; e += blockDim.x) {
-    const int s = e / nr, c = e - s * nr;
-    hs[e] = h[(size_t)(M - 1 - (par + 2 * s)) * nr + c];
+  if (CHUNK) {
+    // h_s = Linv_jj g_row for the chunk's steps (independent dot products, all threads)
+    const double* g = a.g + (size_t)b * a.g_stride + foff;
+    const double* Linv = a4 ? a.LinvA4 : Mat;
+    for (int e = tid; e < nsteps * nr; e += blockDim.x) {
+      const int s = e / nr, r = e - s * nr;
+      const int jj = jj0 + 2 * s;
+      const double* L = Linv + (size_t)jj * nr * ldl + r;
+      const double* gr = g + (size_t)(M - 1 - jj) * nr;
+      double acc = 0.0;
+#pragma unroll 4
+      for (int c = 0; c < nr; ++c) acc = fma(__ldg(L + (size_t)c * ldl), __ldg(gr + c), acc);
+      hs[e] = acc;
+    }
+  } else {
+    const double* h = a.g + (size_t)b * a.g_stride + foff;       // h_j = Linv_j g_j (k_hpre)
+    for (int e = tid; e < nsteps * nr; e += blockDim.x) {
+      const int s = e / nr, c = e - s * nr;
+      hs[e] = h[(size_t)(M - 1 - (par + 2 * s)) * nr + c];
+    }
   }
-  for (int e = tid; e < 4 * nsteps; e += blockDim.x) cf[e] = coef[(size_t)(par + 2 * (e >> 2)) * 4 + (e & 3)];
+  for (int e = tid; e < 4 * nsteps; e += blockDim.x) cf[e] = coef[(size_t)(jj0 + 2 * (e >> 2)) * 4 + (e & 3)];
   for (int c = tid; c < 2 * nr; c += blockDim.x) x2[c] = 0.0;
   __syncthreads();
 
   double fprev = 0.0;
   for (int s = 0; s < nsteps; ++s) {
-    const int jj = par + 2 * s;
+    const int jj = jj0 + 2 * s;
     const int row = M - 1 - jj;
     const double* cur = Lb0 + (s % 3) * blk;
     const double hi = hs[s * nr + ir];
-    if (!a4) {   // b += 2 dt (j+2) f_{j+2}   (cf = (2 dt (j+2), 0.5 or 1, -, -))
+    if (!a4) {   // b += 2 dt (j+2) f_{j+2}   (cf = (2 dt (j+2), 0.5 or 1, -, -)); fprev = 0 at a chunk start
       if (row < M - 2 && lead) x2[i] = fma(cf[4 * s], fprev, x2[i]);
     }
     if (s + 2 < nsteps) copy_block(Lb0 + ((s + 2) % 3) * blk, Mat + (size_t)(jj + 4) * blk, blk);
@@ -153,11 +191,20 @@ __global__ void k_chain(ChainArgs a) {
     fprev = fi;
   }
   cp_async_wait<0>();
-  if (sub) {  // Newton residual: f -= sub over the chain's rows (the block's own writes are visible)
+  if (CHUNK && chunk + 1 < a.nch && lead) {    // end state of the chunk from a zero start
+    if (a4) {
+      dout[i] = x2[i];
+      dout[nr + i] = x2[nr + i];
+    } else {
+      const double knext = coef[(size_t)(jj0 + 2 * nsteps) * 4];
+      dout[i] = fma(knext, fprev, x2[i]);
+    }
+  }
+  if (sub) {  // Newton residual: f -= sub over the chunk's rows (the block's own writes are visible)
     __syncthreads();
     for (int e = tid; e < nsteps * nr; e += blockDim.x) {
       const int s = e / nr, c = e - s * nr;
-      const size_t o = (size_t)(M - 1 - (par + 2 * s)) * nr + c;
+      const size_t o = (size_t)(M - 1 - (par + 2 * (s0 + s))) * nr + c;
       f[o] -= sub[o];
     }
   }
@@ -167,6 +214,99 @@ size_t chain_smem_bytes(int M, int nr, int ldl) {
   const size_t blk = (size_t)2 * nr * ldl;
   const size_t ns = (size_t)((M + 1) / 2);
   return (3 * blk + ns * nr + 4 * ns + 2 * (size_t)nr) * sizeof(double);
+}
+
+static size_t chunk_smem_bytes(int kc, int nr, int ldl) {
+  const size_t blk = (size_t)2 * nr * ldl;
+  return (3 * blk + (size_t)kc * nr + 4 * (size_t)kc + 2 * (size_t)nr) * sizeof(double);
+}
+
+// Carried states of the chunked chains: s_1 = d_0, s_{c+1} = Phi_c s_c + d_c (c = 1 .. nch-2), one CTA per
+// chain.  Rows of Phi split over TPR lanes; Phi_c streams into a 2-slot shared-memory ring when it fits
+// (STAGE), else it is read through L2.
+template <int TPR, bool STAGE>
+__global__ void k_chain_carry(ChainArgs a) {
+  extern __shared__ __align__(16) double csm[];
+  const int field = a.field0 + (blockIdx.x >> 1);
+  const int par = blockIdx.x & 1;
+  const int b = blockIdx.y;
+  const bool a4 = (field == 0);
+  if (a.sym && !(a4 ? par == 0 : par == 1)) return;
+  const int m = a4 ? 2 * a.nr : a.nr;
+  const int ldm = a4 ? a.ldmA : a.ldmT;
+  const int nch = a.nch;
+  const size_t blk = (size_t)m * ldm;
+  const double* Phi = (a4 ? a.PhiA4 : (field == 1 ? a.PhiT : a.PhiS)) + (size_t)par * nch * blk;
+  const size_t slot = (size_t)(field * 2 + par) * nch;
+  const double* d = a.dbuf + (size_t)b * a.d_stride + slot * a.ldd;
+  double* cb = a.cbuf + (size_t)b * a.d_stride + slot * a.ldd;
+  double* ring = csm;                                  // STAGE: 2 * blk
+  double* st = csm + (STAGE ? 2 * blk : 0);            // 2 x ldd state buffers
+  const int tid = threadIdx.x;
+  const int q = tid % TPR;
+  const int rows_per_pass = blockDim.x / TPR;
+
+  if (STAGE && nch > 2) {
+    copy_block(ring, Phi + 1 * blk, (int)blk);
+  }
+  cp_async_commit();
+  for (int e = tid; e < m; e += blockDim.x) {
+    const double v = d[e];                             // s_1 = d_0
+    st[e] = v;
+    cb[a.ldd + e] = v;
+  }
+  for (int c = 1; c + 1 < nch; ++c) {
+    const double* cur_in = st + ((c - 1) & 1) * a.ldd;
+    double* nxt = st + (c & 1) * a.ldd;
+    const double* P = STAGE ? ring + ((c - 1) & 1) * blk : Phi + (size_t)c * blk;
+    if (STAGE && c + 2 < nch) copy_block(ring + (c & 1) * blk, Phi + (size_t)(c + 1) * blk, (int)blk);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();                                   // Phi_c landed, s_c visible
+    const double* dc = d + (size_t)c * a.ldd;
+    double* cout = cb + (size_t)(c + 1) * a.ldd;
+    for (int r0 = 0; r0 < m; r0 += rows_per_pass) {
+      const int r = r0 + tid / TPR;
+      const int rr = r < m ? r : 0;
+      double acc = 0.0;
+      for (int col = q; col < m; col += TPR) acc = fma(P[(size_t)col * ldm + rr], cur_in[col], acc);
+      acc = group_sum<TPR>(acc);
+      if (r < m && q == 0) {
+        const double v = acc + dc[r];
+        nxt[r] = v;
+        cout[r] = v;
+      }
+    }
+    __syncthreads();                                   // Phi_c and s_c are free for the next copy / step
+  }
+  cp_async_wait<0>();
+}
+
+// f_jj += G_jj s_c(jj) for the modes of chunks c >= 1: one warp per (field, mode), lanes = rows.
+__global__ void k_chain_fix(ChainArgs a, int nfields) {
+  const int warps = blockDim.x >> 5;
+  const int wid = blockIdx.x * warps + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  const int M = a.M, nr = a.nr, ldl = a.ldl;
+  if (wid >= nfields * M) return;
+  const int fl = wid / M, jj = wid - fl * M;
+  const int field = a.field0 + fl;
+  const int par = jj & 1, s = jj >> 1;
+  const int c = s / a.kc;
+  if (c == 0) return;
+  const bool a4 = (field == 0);
+  if (a.sym && !(a4 ? par == 0 : par == 1)) return;
+  const int b = blockIdx.y;
+  const int m = a4 ? 2 * nr : nr;
+  const double* G = (a4 ? a.GA4 : (field == 1 ? a.GT : a.GS)) + (size_t)jj * m * ldl;
+  const double* sc = a.cbuf + (size_t)b * a.d_stride + ((size_t)(field * 2 + par) * a.nch + c) * a.ldd;
+  double* f = a.f + (size_t)b * a.f_stride + (size_t)field * a.field_off + (size_t)(M - 1 - jj) * nr;
+  for (int i = lane; i < nr; i += 32) {
+    double acc = 0.0;
+#pragma unroll 4
+    for (int col = 0; col < m; ++col) acc = fma(__ldg(G + (size_t)col * ldl + i), sc[col], acc);
+    f[i] += acc;
+  }
 }
 
 // h[field][row] = Linv_field[jj] g[field][row], row = M-1-jj, for all modes and the fields [field0,
@@ -192,12 +332,82 @@ __global__ void k_hpre(ChainArgs a, int nfields) {
   }
 }
 
+static int sm_count() {
+  static const int sms = [] {  // thread-safe one-time initialisation (host threads may launch concurrently)
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+  }();
+  return sms;
+}
+
+static cudaError_t launch_chunked(const ChainArgs& a, int batch, int nfields, cudaStream_t s) {
+  cudaError_t e;
+  const size_t smem = chunk_smem_bytes(a.kc, a.nr, a.ldl);
+  const dim3 grid(2 * nfields, batch, a.nch);
+  if (a.nr <= 32) {
+    static unsigned long long done = 0;
+    if ((e = ensure_smem_attr(k_chain<4, true>, &done)) != cudaSuccess) return e;
+    k_chain<4, true><<<grid, 128, smem, s>>>(a);
+  } else {
+    static unsigned long long done = 0;
+    if ((e = ensure_smem_attr(k_chain<2, true>, &done)) != cudaSuccess) return e;
+    k_chain<2, true><<<grid, 128, smem, s>>>(a);
+  }
+  if ((e = cudaGetLastError()) != cudaSuccess || a.nch < 2) return e;
+  // carried states: Phi of the psi chain (m = 2 nr) decides staging for all fields of the launch
+  const int mmax = a.field0 == 0 ? 2 * a.nr : a.nr;
+  const int ldmax = a.field0 == 0 ? a.ldmA : a.ldmT;
+  const size_t ring = 2 * (size_t)mmax * ldmax * sizeof(double);
+  const size_t st = 2 * (size_t)a.ldd * sizeof(double);
+  const bool stage = ring + st <= 160 * 1024;
+  const dim3 cg(2 * nfields, batch);
+  if (mmax <= 64) {
+    if (stage) {
+      static unsigned long long done = 0;
+      if ((e = ensure_smem_attr(k_chain_carry<2, true>, &done)) != cudaSuccess) return e;
+      k_chain_carry<2, true><<<cg, 128, ring + st, s>>>(a);
+    } else {
+      k_chain_carry<2, false><<<cg, 128, st, s>>>(a);
+    }
+  } else {
+    if (stage) {
+      static unsigned long long done = 0;
+      if ((e = ensure_smem_attr(k_chain_carry<1, true>, &done)) != cudaSuccess) return e;
+      k_chain_carry<1, true><<<cg, 128, ring + st, s>>>(a);
+    } else {
+      k_chain_carry<1, false><<<cg, 128, st, s>>>(a);
+    }
+  }
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  const int hw = 4;
+  k_chain_fix<<<dim3((nfields * a.M + hw - 1) / hw, batch), 32 * hw, 0, s>>>(a, nfields);
+  return cudaGetLastError();
+}
+
 // One CTA per chain.  When the batch leaves SMs idle (2*nfields*batch <= #SMs) the 4-warp split-row
 // layout gives the shortest chain; otherwise the one-lane-per-row layout issues the fewest FP64
-// instructions and several chains share every SM.  a.g holds the right-hand sides; a.h receives
-// h = Linv g (k_hpre) and is what the chains read.
+// instructions and several chains share every SM.  Layout 2 (chunked: nch CTAs per chain, a short
+// carried-state recurrence and a parallel correction) is chosen automatically while all its CTAs fit
+// on the GPU at two per SM.  a.g holds the right-hand sides; a.h receives h = Linv g (k_hpre) for the
+// one-CTA-per-chain layouts and is what those chains read.
 cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStream_t s) {
   ChainArgs a = a_in;
+  const int sms = sm_count();
+  static const int optin = [] {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return n;
+  }();
+  int layout = a.layout;
+  if (layout == 0 && a.nch > 1 && a.GA4 && 2 * nfields * batch * a.nch <= 2 * sms) layout = 2;
+  if (layout != 2 && chain_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin) layout = 2;  // whole chain too long
+  if (layout == 2) {
+    if (!a.GA4 || a.kc < 1 || a.nch < 1) return cudaErrorInvalidValue;
+    return launch_chunked(a, batch, nfields, s);
+  }
   const int hw = 4;
   k_hpre<<<dim3((nfields * a.M + hw - 1) / hw, batch), 32 * hw, 0, s>>>(a, nfields);
   cudaError_t e = cudaGetLastError();
@@ -205,26 +415,20 @@ cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStre
   a.g = a.h;
   a.g_stride = a.h_stride;
   const size_t smem = chain_smem_bytes(a.M, a.nr, a.ldl);
-  static const int sms = [] {  // thread-safe one-time initialisation (host threads may launch concurrently)
-    int dev = 0, n = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    return n > 0 ? n : 1;
-  }();
   const dim3 grid(2 * nfields, batch);
-  const bool split = a.layout == 4 || (a.layout == 0 && 2 * nfields * batch <= sms);
+  const bool split = layout == 4 || (layout == 0 && 2 * nfields * batch <= sms);
   if (split && a.nr <= 32) {
     static unsigned long long done = 0;
-    if ((e = ensure_smem_attr(k_chain<4>, &done)) != cudaSuccess) return e;
-    k_chain<4><<<grid, 128, smem, s>>>(a);
+    if ((e = ensure_smem_attr(k_chain<4, false>, &done)) != cudaSuccess) return e;
+    k_chain<4, false><<<grid, 128, smem, s>>>(a);
   } else if (split) {
     static unsigned long long done = 0;
-    if ((e = ensure_smem_attr(k_chain<2>, &done)) != cudaSuccess) return e;
-    k_chain<2><<<grid, 128, smem, s>>>(a);
+    if ((e = ensure_smem_attr(k_chain<2, false>, &done)) != cudaSuccess) return e;
+    k_chain<2, false><<<grid, 128, smem, s>>>(a);
   } else {
     static unsigned long long done = 0;
-    if ((e = ensure_smem_attr(k_chain<1>, &done)) != cudaSuccess) return e;
-    k_chain<1><<<grid, ((a.nr + 31) / 32) * 32, smem, s>>>(a);
+    if ((e = ensure_smem_attr(k_chain<1, false>, &done)) != cudaSuccess) return e;
+    k_chain<1, false><<<grid, ((a.nr + 31) / 32) * 32, smem, s>>>(a);
   }
   return cudaGetLastError();
 }

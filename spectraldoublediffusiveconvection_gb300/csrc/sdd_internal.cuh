@@ -95,7 +95,7 @@ struct RhsArgs {
 struct ChainArgs {
   int M, nr, ldl, sym;
   int field0;                // first field handled (blockIdx.x/2 + field0)
-  int layout;                // 0 auto, 1 one lane per row, 4 rows split over 4 warps
+  int layout;                // 1 one lane per row, 4 rows split over 4 warps, 2 chunked (resolved by the host)
   size_t field_off;          // doubles between field blocks (N_fm*nr, or 0 when g/f point at one block)
   const double* g;           // rhs [shell][3][M][nr]
   size_t g_stride;
@@ -111,6 +111,17 @@ struct ChainArgs {
   const double* coefA4;      // [M][4] per jj: (dt bjt, dt bjt bj, bj, bjt), dt = Pr*dt, j = M - jj
   const double* coefT, *coefS;  // [M][4] per jj: (2 dt (j+2), 0.5 if j == 0 else 1, 0, 0), j = M-1-jj
   double dtA4, dtT, dtS;     // Pr*dt, dt, Tau*dt
+  // chunked (parallel-in-modes) chains, layout 2: every chain of S = N_fm/2 steps is cut into nch chunks
+  // of kc steps.  Chunk c runs from a zero carried state (f_local, end state d_c); the carried states
+  // s_c at the chunk starts follow s_{c+1} = Phi_c s_c + d_c; then f += G_jj s_c for the chunk's modes.
+  int kc, nch;               // chunk length (steps) and chunks per chain
+  int ldmA, ldmT;            // leading dimensions of Phi for the psi (m = 2 nr) and T/S (m = nr) states
+  int ldd;                   // doubles per (field, parity, chunk) slot of dbuf / cbuf (>= 2 nr, even)
+  const double* GA4, *GT, *GS;        // [M][m cols][ldl] transposed G_jj (m = 2 nr for psi, nr for T/S)
+  const double* PhiA4, *PhiT, *PhiS;  // [2 parity][nch][m cols][ldm] transposed Phi_c
+  double* dbuf;              // [shell][3][2][nch][ldd] chunk end states from a zero start
+  double* cbuf;              // [shell][3][2][nch][ldd] carried states at the chunk starts (c >= 1)
+  size_t d_stride;           // doubles per shell in dbuf / cbuf
 };
 
 // launchers (return cudaError_t of the launch)

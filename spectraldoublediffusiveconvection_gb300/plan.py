@@ -115,7 +115,7 @@ class Plan:
             _lib.check(self._L.sdd_plan_reserve(self._h, int(batch)), "sdd_plan_reserve")
 
     def set_chain_layout(self, layout):
-        """0 automatic, 1 one lane per row, 4 rows split over 4 warps (see sdd_plan_set_chain_layout)."""
+        """0 automatic, 1 one lane per row, 2 chunked, 4 rows split over 4 warps (sdd_plan_set_chain_layout)."""
         _lib.check(self._L.sdd_plan_set_chain_layout(self._h, int(layout)), "sdd_plan_set_chain_layout")
         self.chain_layout = int(layout)
 

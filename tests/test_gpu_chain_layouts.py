@@ -1,0 +1,81 @@
+"""Every chain layout of the implicit solves (1 one lane per row, 2 chunked, 4 split rows) against the
+oracle's A4_BSub_TSTEP_V2 / NAB2_BSub_TSTEP_V2 chains (Matrix_Operators.py:1033-1194), alone and inside
+the step, the Newton residual and its Jacobian.  The chunked layout reorders the arithmetic (carried
+states through precomputed chunk maps), so it agrees with the sequential chain to rounding, not bitwise."""
+import numpy as np
+import pytest
+
+from conftest import rel
+from oracle import sdd_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(16, 16, False), (20, 64, False), (30, 256, False), (48, 512, False), (36, 384, True), (12, 10, True)]
+
+
+@pytest.mark.parametrize("N_r,N_fm,sym", SHAPES)
+@pytest.mark.parametrize("layout", [1, 2, 4])
+def test_chain_solves_against_oracle(cuda, N_r, N_fm, sym, layout):
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    nr = N_r - 1
+    dt = 5e-4
+    ops = O.Operators(N_fm, N_r, 2.0, dt, 1.0, 0.01)
+    p = Plan(N_fm, N_r, 2.0, dt, 1.0, 0.01, symmetric=sym)
+    p.set_chain_layout(layout)
+    rng = np.random.default_rng(N_fm + nr)
+    G = rng.standard_normal((2, N_fm * nr)) * np.repeat(np.exp(-np.arange(N_fm) / 40.0), nr)
+    Gt = torch.from_numpy(G).cuda()
+    fa = p.a4_bsub(Gt).cpu().numpy()
+    ft = p.nab2_bsub(1, Gt).cpu().numpy()
+    fs = p.nab2_bsub(2, Gt).cpu().numpy()
+    for k in range(2):
+        ra = O.A4_BSub_TSTEP_V2(G[k], ops.Linv_A4, ops.D2_A4, ops.IR4_A4, ops.IR2_A4, N_fm, nr, dt, sym)
+        rt = O.NAB2_BSub_TSTEP_V2(G[k], ops.Linv_T, N_fm, nr, dt, sym)
+        rs = O.NAB2_BSub_TSTEP_V2(G[k], ops.Linv_S, N_fm, nr, 0.01 * dt, sym)
+        assert rel(fa[k], ra) < 1e-13
+        assert rel(ft[k], rt) < 1e-13
+        assert rel(fs[k], rs) < 1e-13
+
+
+@pytest.mark.parametrize("N_r,N_fm", [(20, 64), (30, 256), (48, 512)])
+def test_chunked_step_newton_operators_against_oracle(cuda, N_r, N_fm):
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    nr = N_r - 1
+    X = O.seeded_state(N_fm, nr, 1234)
+    dv = O.seeded_state(N_fm, nr, 77)
+    Xt = torch.from_numpy(np.stack([X, 2 * X])).cuda()
+    dvt = torch.from_numpy(np.stack([dv, dv])).cuda()
+    ops = O.Operators(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01)
+    p = Plan(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01)
+    p.set_chain_layout(2)
+    Y = p.step(Xt, 8000.0, 500.0, nsteps=3).cpu().numpy()
+    for k, x in enumerate([X, 2 * X]):
+        r = x
+        for _ in range(3):
+            r = O.step(ops, r, 8000.0, 500.0, False)
+        assert rel(Y[k], r) < 1e-12
+    ops1 = O.Operators(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
+    p1 = Plan(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
+    p1.set_chain_layout(2)
+    F = p1.pfx(Xt, 8000.0, 500.0).cpu().numpy()
+    J = p1.pdfx(dvt, Xt, 8000.0, 500.0).cpu().numpy()
+    for k, x in enumerate([X, 2 * X]):
+        assert rel(F[k], O.PFX(ops1, x, 8000.0, 500.0, False)) < 1e-12
+        assert rel(J[k], O.PDFX(ops1, dv, x, 8000.0, 500.0, False)) < 1e-12
+
+
+def test_chunked_batch_equals_alone(cuda):
+    """No arithmetic crosses shells in the chunked layout either: a batch equals its shells alone."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    N_fm, N_r = 128, 24
+    p = Plan(N_fm, N_r, 2.0, 1e-3, 1.0, 0.01)
+    p.set_chain_layout(2)
+    Xs = np.stack([O.seeded_state(N_fm, N_r - 1, s) for s in range(4)])
+    Ra = torch.tensor([6000.0, 8000.0, 10000.0, 12000.0], dtype=torch.float64, device="cuda")
+    Xb = p.step(torch.from_numpy(Xs).cuda(), Ra, 500.0, nsteps=4)
+    for i in range(4):
+        Xi = p.step(torch.from_numpy(Xs[i:i + 1]).cuda(), float(Ra[i]), 500.0, nsteps=4)
+        assert torch.equal(Xb[i:i + 1], Xi)
