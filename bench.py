@@ -299,15 +299,15 @@ def bench_gb300(args):
 
     import __graft_entry__
     __graft_entry__.build()
-    from oracle import sdd_oracle as O          # seeded input generator only
     from spectraldoublediffusiveconvection_gb300 import _lib
+    from spectraldoublediffusiveconvection_gb300.seeds import seeded_state
     from spectraldoublediffusiveconvection_gb300.plan import Plan
 
     w = WORKLOAD
     M, N_r, nr = w["N_theta"], w["N_r"], w["N_r"] - 1
     chunk = w["steps_per_bench_step"]
     plan = Plan(M, N_r, w["d"], w["dt"], w["Pr"], w["Tau"], device=device)
-    X0 = O.seeded_state(M, nr, w["seed"] + rank)
+    X0 = seeded_state(M, nr, w["seed"] + rank)
     Ra = torch.full((1,), w["Ra_T"], dtype=torch.float64, device=device)
     Ras = torch.full((1,), w["Ra_S"], dtype=torch.float64, device=device)
     Xa = torch.from_numpy(X0).to(device).reshape(1, -1)
@@ -425,6 +425,26 @@ def bench_gb300(args):
         newton = {"solves_per_s": 1.0 / tn, "seconds": tn, "newton_iters": res["newton_iters"],
                   "matvecs": res["matvecs"], "residual0": res["residual0"], "residual": res["residual"],
                   "converged": res["converged"], "tol": 1e-10, "restart": 50}
+        # batched: 64 shells of the same shape in one sdd_newton_gmres call (each shell its own Krylov
+        # space), FP32 nonlinear term inside the Jacobian products, FP64 residual <= 1e-10
+        nb = 64
+        planm = Plan(M, N_r, w["d"], 1.0, w["Pr"], w["Tau"], precision="mixed", device=device)
+        pert = torch.from_numpy(np.stack([seeded_state(M, N_r - 1, 500 + i) for i in range(nb)])).to(device)
+        Xb0 = X_after.reshape(1, -1) + pert
+        Rab = torch.linspace(7000.0, 9000.0, nb, dtype=torch.float64, device=device)
+        planm.newton(Xb0.clone(), Rab, Ras, tol=1e-10, restart=50, max_newton=1, mixed_matvec=True)  # warm-up
+        Xb = Xb0.clone()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rb = planm.newton(Xb, Rab, Ras, tol=1e-10, restart=50, gmres_rtol=1e-4, max_newton=20, mixed_matvec=True)
+        torch.cuda.synchronize()
+        tb = time.perf_counter() - t0
+        newton["batched"] = {"solves_per_s": nb / tb, "seconds": tb, "shells": nb, "mixed_matvec": True,
+                             "converged": sum(r["converged"] for r in rb),
+                             "max_residual": max(r["residual"] for r in rb), "matvecs": rb[0]["matvecs"],
+                             "vs_plain_single_shell": (nb / tb) / (1.0 / tn),
+                             "workload": "64 shells N_r=30 N_theta=256, Ra_T 7000..9000, Tau=0.01, from the "
+                                         "time-stepped state plus seeded perturbations"}
 
     batched = None
     if not args.no_batched:

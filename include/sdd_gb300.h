@@ -94,6 +94,11 @@ int sdd_plan_reserve(sdd_plan* plan, int max_batch);
  * per row, 2 chunked (each chain cut into chunks that run concurrently, joined by a short carried-state
  * recurrence), 4 split rows over 4 warps.  Set by the batch autotuner; no counterpart in the reference. */
 int sdd_plan_set_chain_layout(sdd_plan* plan, int layout);
+/* Nonlinear-term kernel choice: 0 automatic (split while the fused kernel's nr*batch CTAs would fill
+ * under half the SMs), 1 the fused row kernel (one CTA per radial row), 2 split (7 CTAs per radial row:
+ * five paired inverse transforms, then two paired forward transforms).  Results are identical bit for
+ * bit.  Set by the batch autotuner; no counterpart in the reference. */
+int sdd_plan_set_fx_split(sdd_plan* plan, int mode);
 /* FP64 elements of one shell's base-state grid cache used by sdd_nlin_dfx (9 * nr * 3N_fm/2). */
 size_t sdd_plan_base_cache_elems(const sdd_plan* plan);
 

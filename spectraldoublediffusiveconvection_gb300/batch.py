@@ -13,6 +13,8 @@ import time
 
 import numpy as np
 
+from .seeds import seeded_state
+
 from .plan import get_plan
 
 
@@ -63,6 +65,17 @@ class ShellBatch:
                        [float(shells[i].get("Ra_s", Ra_s)) for i in idx], self.device)
             plan.reserve(len(idx))
             self.groups.append(g)
+        # Starting point of the tuning (measured on the 64-shell mixed batch of N_r in {20..36}, N_theta in
+        # {64..384}): the groups' launches share the GPU inside one graph, so the nonlinear term runs as the
+        # fused row kernel once the batch fills the SMs; the chains use the split-row layout, and chunked
+        # chains for N_theta >= 256 with the FP32 nonlinear term, where the long chains of the largest
+        # shells set the critical path (84k vs 77k shell-steps/s); in FP64 the nonlinear term dominates
+        # and chunking does not pay.
+        sms = _torch().cuda.get_device_properties(self.device).multi_processor_count
+        total_rows = sum(g.plan.nr * len(g.idx) for g in self.groups)
+        for g in self.groups:
+            g.plan.set_chain_layout(2 if (precision == "mixed" and g.plan.N_fm >= 256) else 4)
+            g.plan.set_fx_split(1 if 2 * total_rows > sms else 0)
         self.graph = None
         self.steps_per_launch = 0
         self.tuning = {}
@@ -118,9 +131,10 @@ class ShellBatch:
         torch.cuda.synchronize(self.device)
         return (time.perf_counter() - t0) / reps
 
-    def autotune(self, steps_per_launch=5, reps=3, layouts=(1, 2, 4)):
-        """Greedy per-group choice of the chain layout minimising the time of one graph launch.  The
-        shells' states are restored afterwards: tuning does not advance them."""
+    def autotune(self, steps_per_launch=5, reps=3, layouts=(1, 2, 4), fx_modes=(1, 2)):
+        """Greedy per-group choice of the chain layout, then of the nonlinear-term kernel (fused or split),
+        minimising the time of one graph launch.  The shells' states are restored afterwards: tuning does
+        not advance them."""
         saved = [g.X.clone() for g in self.groups]
         self.steps_per_launch = steps_per_launch
         best = self._time_graph(reps)
@@ -132,7 +146,14 @@ class ShellBatch:
                 if t < best:
                     best, choice = t, lay
             g.plan.set_chain_layout(choice)
-            self.tuning["N_r=%d,N_theta=%d" % g.shape] = {"chain_layout": choice}
+            fx_choice = getattr(g.plan, "fx_split", 0)
+            for fx in fx_modes:
+                g.plan.set_fx_split(fx)
+                t = self._time_graph(reps)
+                if t < best:
+                    best, fx_choice = t, fx
+            g.plan.set_fx_split(fx_choice)
+            self.tuning["N_r=%d,N_theta=%d" % g.shape] = {"chain_layout": choice, "fx_split": fx_choice}
         for g, x in zip(self.groups, saved):
             g.X.copy_(x)
         self.capture(steps_per_launch)
@@ -150,13 +171,7 @@ class ShellBatch:
 
 
 def _seeded(M, nr, rng):
-    k = np.arange(M)[None, :]
-    n = np.arange(nr)[:, None]
-    amp = 1e-3 * np.exp(-k / 8.0) * np.exp(-n / 4.0)
-    P, T, S = [rng.standard_normal((nr, M)) * amp for _ in range(3)]
-    X = np.zeros((3, M, nr))
-    X[0], X[1], X[2] = P.T, T.T, S.T
-    return X.reshape(-1)
+    return seeded_state(M, nr, rng)
 
 
 def config4_shells(n=64, seed=1234):

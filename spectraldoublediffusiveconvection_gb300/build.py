@@ -15,6 +15,9 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsdd_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# The nonlinear-term kernels write every multiply-add as an explicit fma and are compiled without
+# automatic contraction, so the fused and the split kernels (and every batch size) round identically.
+FILE_FLAGS = {"sdd_fx.cu": ["-fmad=false"]}
 
 
 def _nvcc():
@@ -44,6 +47,7 @@ def build(verbose=False, force=False, extra_flags=()):
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(HERE, "..", "include", "sdd_gb300.h"))
+    headers.append(os.path.abspath(__file__))     # flag changes rebuild
     srcs = sources()
     objs = [os.path.join(BUILD, os.path.basename(s)[:-3] + ".o") for s in srcs]
 
@@ -51,7 +55,7 @@ def build(verbose=False, force=False, extra_flags=()):
         src, obj = pair
         if not force and not _stale(obj, [src] + headers):
             return None
-        cmd = [nvcc, *ARCH, *FLAGS, *extra_flags, "-c", src, "-o", obj]
+        cmd = [nvcc, *ARCH, *FLAGS, *FILE_FLAGS.get(os.path.basename(src), []), *extra_flags, "-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

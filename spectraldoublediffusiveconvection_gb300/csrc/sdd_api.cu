@@ -88,9 +88,23 @@ const FftPlan* get_fft_plan(int L) {
 using namespace sdd;
 
 // ---- plan ---------------------------------------------------------------------------------------
+// One instantiated graph of `pairs` step pairs A -> B -> A (B the plan's xtmp), keyed by everything the
+// captured launches bake in.
+struct StepGraph {
+  cudaGraphExec_t exec;
+  const double* A;
+  const double* Ra;
+  const double* Ras;
+  int batch, linear, pairs, layout, fx_split;
+  unsigned long long last_use;
+};
+constexpr int kStepGraphs = 8;
+constexpr int kGraphMinSteps = 8;   // sdd_step replays captured graphs from this many steps on
+
 struct sdd_plan {
   int M, nr, P, ldl, sym, prec, device;
   int chain_layout;
+  int fx_split;                     // 0 auto, 1 fused row kernel, 2 split over 7 CTAs per row
   double dt, Pr, Tau;
   const FftPlan* fft;
   // FP64 operators
@@ -111,6 +125,7 @@ struct sdd_plan {
   double* xtmp;     // [B][3][M][nr]
   double* hbuf;     // [B][3][M][nr] h = Linv g of the chains
   void* base_tmp;   // [B][nr][9][P] (T precision), for DFX without a caller cache
+  void* gridbuf;    // [B][nr][9][P] (T precision), grid fields of the split nonlinear-term path
   // Krylov / Newton / continuation workspace (grown on demand)
   int sv_B, sv_m;
   double *kv_V, *kv_w, *kv_r, *kv_part, *kv_nrm2, *kv_small, *kv_dot;
@@ -119,6 +134,10 @@ struct sdd_plan {
   int* h_int;         // pinned host flags
   double *sv_F, *sv_x, *sv_X0, *sv_Xd, *sv_t, *sv_G, *sv_Jmu, *sv_g, *sv_base64, *sv_dev;
   float* sv_base32;
+  // CUDA graphs of repeated time steps (sdd_step): A -> xtmp -> A pairs, A = the caller's output
+  StepGraph graphs[kStepGraphs];
+  unsigned long long graph_clock;
+  cudaStream_t cap_stream;          // private capture stream (created on first use)
 };
 
 extern "C" {
@@ -199,14 +218,24 @@ static void solver_free(sdd_plan* p) {
   p->sv_B = p->sv_m = 0;
 }
 
+static void clear_step_graphs(sdd_plan* p) {
+  for (int i = 0; i < kStepGraphs; ++i) {
+    if (p->graphs[i].exec) cudaGraphExecDestroy(p->graphs[i].exec);
+    p->graphs[i].exec = nullptr;
+  }
+}
+
 static void free_plan(sdd_plan* p) {
   if (!p) return;
+  clear_step_graphs(p);
+  if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   double* d[] = {p->Dr, p->D2r2, p->ir4r2, p->D2s, p->ir2s, p->D2A4, p->ir2A4, p->ir4A4, p->rsq, p->dT0,
                  p->gr, p->LinvA4, p->LinvT, p->LinvS, p->out4, p->rhs, p->xtmp, p->coefA4, p->coefT, p->coefS, p->ABA4, p->hbuf,
                  p->GA4, p->GT, p->GS, p->PhiA4, p->PhiT, p->PhiS, p->dbuf, p->cbuf};
   for (double* x : d) cudaFree(x);
   cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232);
   cudaFree(p->base_tmp);
+  cudaFree(p->gridbuf);
   solver_free(p);
   delete p;
 }
@@ -408,8 +437,16 @@ int sdd_plan_destroy(sdd_plan* p) {
   return SDD_OK;
 }
 
+int sdd_plan_set_fx_split(sdd_plan* p, int mode) {
+  if (!p || mode < 0 || mode > 2) return SDD_ERR_ARG;
+  if (p->fx_split != mode) clear_step_graphs(p);
+  p->fx_split = mode;
+  return SDD_OK;
+}
+
 int sdd_plan_set_chain_layout(sdd_plan* p, int layout) {
   if (!p || (layout != 0 && layout != 1 && layout != 2 && layout != 4)) return SDD_ERR_ARG;
+  if (p->chain_layout != layout) clear_step_graphs(p);
   p->chain_layout = layout;
   return SDD_OK;
 }
@@ -421,10 +458,11 @@ static size_t shell_elems(const sdd_plan* p) { return (size_t)3 * p->M * p->nr; 
 int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   if (!p || max_batch < 1) return SDD_ERR_ARG;
   if (max_batch <= p->ws_batch) return SDD_OK;
+  clear_step_graphs(p);   // the graphs bake in the workspace pointers
   cudaFree(p->out4); cudaFree(p->rhs); cudaFree(p->xtmp); cudaFree(p->base_tmp); cudaFree(p->hbuf);
-  cudaFree(p->dbuf); cudaFree(p->cbuf);
+  cudaFree(p->dbuf); cudaFree(p->cbuf); cudaFree(p->gridbuf);
   p->out4 = p->rhs = p->xtmp = p->hbuf = p->dbuf = p->cbuf = nullptr;
-  p->base_tmp = nullptr;
+  p->base_tmp = p->gridbuf = nullptr;
   p->ws_batch = 0;
   const size_t se = shell_elems(p);
   const size_t be = sdd_plan_base_cache_elems(p);
@@ -433,6 +471,7 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   SDD_CUDA(cudaMalloc(&p->xtmp, (size_t)max_batch * se * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->hbuf, (size_t)max_batch * se * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->base_tmp, (size_t)max_batch * be * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->gridbuf, (size_t)max_batch * be * sizeof(double)));
   const size_t de = (size_t)6 * p->nch * p->ldd;
   SDD_CUDA(cudaMalloc(&p->dbuf, (size_t)max_batch * de * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->cbuf, (size_t)max_batch * de * sizeof(double)));
@@ -459,6 +498,8 @@ static FxArgs fx_args(const sdd_plan* p, int prec, const double* X, void* base, 
   a.X = X; a.x_stride = shell_elems(p);
   a.base = base; a.base_stride = sdd_plan_base_cache_elems(p);
   a.out4 = out4; a.out_stride = (size_t)4 * p->M * p->nr;
+  a.grid = p->gridbuf; a.grid_stride = sdd_plan_base_cache_elems(p);
+  a.split = p->fx_split;
   return a;
 }
 
@@ -598,6 +639,48 @@ int sdd_theta_op(sdd_plan* p, int op, int batch, const double* g, double* f, voi
   return SDD_OK;
 }
 
+// The instantiated graph of `pairs` step pairs A -> xtmp -> A, captured on first use on the plan's private
+// stream (thread-local capture mode, so other host threads are unaffected).  Returns nullptr when it
+// cannot be built; the caller then launches the steps one by one.
+static cudaGraphExec_t step_graph(sdd_plan* p, int batch, const double* Ra, const double* Ras, double* A, int pairs,
+                                  int linear) {
+  StepGraph* slot = nullptr;
+  for (int i = 0; i < kStepGraphs; ++i) {
+    StepGraph& g = p->graphs[i];
+    if (g.exec && g.A == A && g.Ra == Ra && g.Ras == Ras && g.batch == batch && g.linear == linear &&
+        g.pairs == pairs && g.layout == p->chain_layout && g.fx_split == p->fx_split) {
+      g.last_use = ++p->graph_clock;
+      return g.exec;
+    }
+    if (!slot || !g.exec || (slot->exec && g.last_use < slot->last_use)) slot = &g;
+  }
+  if (!p->cap_stream && cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    p->cap_stream = nullptr;
+    cudaGetLastError();
+    return nullptr;
+  }
+  cudaStream_t cs = p->cap_stream;
+  if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  int st = SDD_OK;
+  for (int i = 0; i < pairs && st == SDD_OK; ++i) {
+    st = apply_step(p, batch, Ra, Ras, A, p->xtmp, nullptr, linear ? 2 : 0, nullptr, p->prec, cs);
+    if (st == SDD_OK) st = apply_step(p, batch, Ra, Ras, p->xtmp, A, nullptr, linear ? 2 : 0, nullptr, p->prec, cs);
+  }
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(cs, &graph);
+  cudaGraphExec_t exec = nullptr;
+  if (st != SDD_OK || ec != cudaSuccess || !graph || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) exec = nullptr;
+  if (graph) cudaGraphDestroy(graph);
+  cudaGetLastError();
+  if (!exec) return nullptr;
+  if (slot->exec) cudaGraphExecDestroy(slot->exec);
+  *slot = StepGraph{exec, A, Ra, Ras, batch, linear, pairs, p->chain_layout, p->fx_split, ++p->graph_clock};
+  return exec;
+}
+
 int sdd_step(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X_in, double* X_out,
              int nsteps, int linear, void* stream) {
   int st = check_plan(p, batch);
@@ -611,8 +694,23 @@ int sdd_step(sdd_plan* p, int batch, const double* Ra, const double* Ras, const 
   }
   // ping-pong so that the last step lands in X_out
   const double* cur = X_in;
+  cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+  SDD_CUDA(cudaStreamIsCapturing(s, &cst));
+  const bool graphs = cst == cudaStreamCaptureStatusNone && nsteps >= kGraphMinSteps && X_out != p->xtmp;
   for (int it = 0; it < nsteps; ++it) {
     const int left = nsteps - it;  // steps remaining including this one
+    if (graphs && it > 0 && cur == X_out && left % 2 == 0) {
+      // the remaining steps are A -> xtmp -> A pairs: replay captured graphs of 8 pairs, then of 1 pair
+      const int npairs = left / 2;
+      cudaGraphExec_t g8 = npairs >= 8 ? step_graph(p, batch, Ra, Ras, X_out, 8, linear) : nullptr;
+      cudaGraphExec_t g1 = step_graph(p, batch, Ra, Ras, X_out, 1, linear);
+      if (g1 && (g8 || npairs < 8)) {
+        int done = 0;
+        for (; g8 && done + 8 <= npairs; done += 8) SDD_CUDA(cudaGraphLaunch(g8, s));
+        for (; done < npairs; ++done) SDD_CUDA(cudaGraphLaunch(g1, s));
+        return SDD_OK;
+      }
+    }
     double* dst = (left % 2 == 1) ? X_out : p->xtmp;
     if (dst == cur) dst = (dst == X_out) ? p->xtmp : X_out;  // never write the input in place
     st = apply_step(p, batch, Ra, Ras, cur, dst, nullptr, linear ? 2 : 0, nullptr, p->prec, s);
@@ -1147,6 +1245,7 @@ extern "C" int sdd_nlin_fx_noalloc(sdd_plan* p, int batch, const double* X, doub
   cudaStream_t s = (cudaStream_t)stream;
   // the row kernel writes every element of the batch's 4*N_fm*nr outputs before k_fx_finish reads them
   FxArgs fa = fx_args(p, SDD_PREC_FP64, X, nullptr, scratch);
+  fa.grid = nullptr;   // the fused row kernel: no grid scratch (the plan's may be smaller than the batch)
   SDD_CUDA(launch_fx(fa, batch, 0, SDD_PREC_FP64, s));
   SDD_CUDA(launch_fx_finish(p->M, p->nr, p->Dr, scratch, (size_t)4 * p->M * p->nr, F, shell_elems(p), batch, s));
   return SDD_OK;

@@ -6,7 +6,7 @@
 //
 // Restructured for a short critical path (exact algebra; checked against the reference formulation to
 // ~3e-16):
-//   h_j = Linv_j g_j for every mode first (k_hpre, all SMs in parallel, off the chains), then
+//   h_j = Linv_j g_j for every mode first (k_mode_mv, all SMs in parallel, off the chains), then
 //   psi:  f_j = h_j + A_j f_e + B_j bf_e,  A_j = Linv_j (dt bjt D2 + diag(alpha_j)),  B_j = Linv_j diag(beta_j),
 //         alpha_j = dt bjt bj IR4 - bjt IR2,  beta_j = dt bjt IR4   (b_test of :1155, expanded)
 //         f_e += f_j,  bf_e += bj f_j + bjt f_e   (:1153, :1159)
@@ -27,7 +27,7 @@
 //     The chain's carried state s (psi: [f_e; bf_e], 2 nr; T/S: b, nr) enters every later step linearly,
 //     so with the plan's precomputed Phi_c (state over a whole chunk) and G_jj (state -> f_jj):
 //       s_1 = d_0,  s_{c+1} = Phi_c s_c + d_c   (k_chain_carry, one CTA per chain, nch - 2 matvecs)
-//       f_jj += G_jj s_c(jj)                    (k_chain_fix, all modes in parallel)
+//       f_jj += G_jj s_c(jj)                    (k_mode_mv, all modes in parallel)
 //     The critical path drops from S dependent steps to kc + (nch - 2) carried matvecs + one matvec.
 // Matrices are stored transposed (column c contiguous, leading dimension ldl); the block of step s+2
 // streams global->shared with cp.async while step s runs (3-slot ring).  FP64 throughout.
@@ -73,10 +73,9 @@ __device__ __forceinline__ void chain_sync() {
 }
 
 // One chain (field, parity) of one shell: steps [s0, s1) of the S = (M - par + 1)/2 chain steps.
-// CHUNK = false: the whole chain (s0 = 0, s1 = S) with h = Linv g precomputed by k_hpre.
-// CHUNK = true: chunk blockIdx.z of a.kc steps, started from a zero carried state, computing its own
-// h = Linv g rows first; the end state goes to dbuf (psi: [f_e; bf_e]; T/S: b + k_next f_last, the b the
-// next chunk's first step uses).
+// CHUNK = false: the whole chain (s0 = 0, s1 = S).  CHUNK = true: chunk blockIdx.z of a.kc steps,
+// started from a zero carried state; its end state goes to dbuf (psi: [f_e; bf_e]; T/S: b + k_next f_last,
+// the b the next chunk's first step uses).  Both read h = Linv g (k_mode_mv) through a.g.
 template <int TPR, bool CHUNK>
 __global__ void k_chain(ChainArgs a) {
   extern __shared__ __align__(16) double csm[];
@@ -128,25 +127,11 @@ __global__ void k_chain(ChainArgs a) {
   cp_async_commit();
   if (nsteps > 1) copy_block(Lb0 + blk, Mat + (size_t)(jj0 + 2) * blk, blk);
   cp_async_commit();
-  if (CHUNK) {
-    // h_s = Linv_jj g_row for the chunk's steps (independent dot products, all threads)
-    const double* g = a.g + (size_t)b * a.g_stride + foff;
-    const double* Linv = a4 ? a.LinvA4 : Mat;
-    for (int e = tid; e < nsteps * nr; e += blockDim.x) {
-      const int s = e / nr, r = e - s * nr;
-      const int jj = jj0 + 2 * s;
-      const double* L = Linv + (size_t)jj * nr * ldl + r;
-      const double* gr = g + (size_t)(M - 1 - jj) * nr;
-      double acc = 0.0;
-#pragma unroll 4
-      for (int c = 0; c < nr; ++c) acc = fma(__ldg(L + (size_t)c * ldl), __ldg(gr + c), acc);
-      hs[e] = acc;
-    }
-  } else {
-    const double* h = a.g + (size_t)b * a.g_stride + foff;       // h_j = Linv_j g_j (k_hpre)
+  {
+    const double* h = a.g + (size_t)b * a.g_stride + foff;       // h_j = Linv_j g_j (k_mode_mv)
     for (int e = tid; e < nsteps * nr; e += blockDim.x) {
       const int s = e / nr, c = e - s * nr;
-      hs[e] = h[(size_t)(M - 1 - (par + 2 * s)) * nr + c];
+      hs[e] = h[(size_t)(M - 1 - (par + 2 * (s0 + s))) * nr + c];
     }
   }
   for (int e = tid; e < 4 * nsteps; e += blockDim.x) cf[e] = coef[(size_t)(jj0 + 2 * (e >> 2)) * 4 + (e & 3)];
@@ -282,54 +267,101 @@ __global__ void k_chain_carry(ChainArgs a) {
   cp_async_wait<0>();
 }
 
-// f_jj += G_jj s_c(jj) for the modes of chunks c >= 1: one warp per (field, mode), lanes = rows.
-__global__ void k_chain_fix(ChainArgs a, int nfields) {
-  const int warps = blockDim.x >> 5;
-  const int wid = blockIdx.x * warps + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
+// Independent per-mode matvecs, one CTA of 128 threads per (field, mode, shell); matrix rows split over
+// TPR lanes (TPR = 4 for nr <= 32, 2 for nr <= 64), every lane's column loads independent of each other:
+//   FIX = false:  h_jj = Linv_jj g_jj                          (the chains' right-hand sides)
+//   FIX = true:   f_jj += G_jj s_c(jj) for the modes of chunks c >= 1   (chunked chains' correction)
+template <int TPR, bool FIX>
+__global__ void __launch_bounds__(128) k_mode_mv(ChainArgs a) {
   const int M = a.M, nr = a.nr, ldl = a.ldl;
-  if (wid >= nfields * M) return;
-  const int fl = wid / M, jj = wid - fl * M;
+  const int fl = blockIdx.x / M, jj = blockIdx.x - fl * M;
   const int field = a.field0 + fl;
-  const int par = jj & 1, s = jj >> 1;
-  const int c = s / a.kc;
-  if (c == 0) return;
-  const bool a4 = (field == 0);
-  if (a.sym && !(a4 ? par == 0 : par == 1)) return;
   const int b = blockIdx.y;
-  const int m = a4 ? 2 * nr : nr;
-  const double* G = (a4 ? a.GA4 : (field == 1 ? a.GT : a.GS)) + (size_t)jj * m * ldl;
-  const double* sc = a.cbuf + (size_t)b * a.d_stride + ((size_t)(field * 2 + par) * a.nch + c) * a.ldd;
-  double* f = a.f + (size_t)b * a.f_stride + (size_t)field * a.field_off + (size_t)(M - 1 - jj) * nr;
-  for (int i = lane; i < nr; i += 32) {
+  const int row = M - 1 - jj;
+  const size_t foff = (size_t)field * a.field_off;
+  const bool a4 = field == 0;
+  const double* A;
+  const double* x;
+  double* y;
+  int m;
+  if (FIX) {
+    const int par = jj & 1, c = (jj >> 1) / a.kc;
+    if (c == 0 || (a.sym && !(a4 ? par == 0 : par == 1))) return;
+    m = a4 ? 2 * nr : nr;
+    A = (a4 ? a.GA4 : (field == 1 ? a.GT : a.GS)) + (size_t)jj * m * ldl;
+    x = a.cbuf + (size_t)b * a.d_stride + ((size_t)(field * 2 + par) * a.nch + c) * a.ldd;
+    y = a.f + (size_t)b * a.f_stride + foff + (size_t)row * nr;
+  } else {
+    m = nr;
+    A = (a4 ? a.LinvA4 : (field == 1 ? a.LinvT : a.LinvS)) + (size_t)jj * nr * ldl;
+    x = a.g + (size_t)b * a.g_stride + foff + (size_t)row * nr;
+    y = a.h + (size_t)b * a.h_stride + foff + (size_t)row * nr;
+  }
+  const int i = threadIdx.x / TPR, q = threadIdx.x % TPR;
+  for (int r0 = 0; r0 < nr; r0 += 128 / TPR) {
+    const int r = r0 + i;
+    const int rr = r < nr ? r : 0;
     double acc = 0.0;
-#pragma unroll 4
-    for (int col = 0; col < m; ++col) acc = fma(__ldg(G + (size_t)col * ldl + i), sc[col], acc);
-    f[i] += acc;
+#pragma unroll 8
+    for (int col = q; col < m; col += TPR) acc = fma(__ldg(A + (size_t)col * ldl + rr), __ldg(x + col), acc);
+    acc = group_sum<TPR>(acc);
+    if (r < nr && q == 0) {
+      if (FIX) y[r] += acc;
+      else y[r] = acc;
+    }
   }
 }
 
-// h[field][row] = Linv_field[jj] g[field][row], row = M-1-jj, for all modes and the fields [field0,
-// field0+nfields): one warp per (field, mode), lanes = rows, fully parallel over the GPU.
-__global__ void k_hpre(ChainArgs a, int nfields) {
-  const int warps = blockDim.x >> 5;
-  const int wid = blockIdx.x * warps + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
+// The same matvecs with one warp per (field, mode, shell) and one lane per row: the fewest FP64
+// instructions, for launches that share the GPU with many others (lane-per-row chain layout).
+template <bool FIX>
+__global__ void __launch_bounds__(128) k_mode_mv_warp(ChainArgs a, int nfields) {
   const int M = a.M, nr = a.nr, ldl = a.ldl;
+  const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
   if (wid >= nfields * M) return;
   const int fl = wid / M, jj = wid - fl * M;
   const int field = a.field0 + fl;
   const int b = blockIdx.y;
   const int row = M - 1 - jj;
   const size_t foff = (size_t)field * a.field_off;
-  const double* g = a.g + (size_t)b * a.g_stride + foff + (size_t)row * nr;
-  double* hout = a.h + (size_t)b * a.h_stride + foff + (size_t)row * nr;
-  const double* L = (field == 0 ? a.LinvA4 : (field == 1 ? a.LinvT : a.LinvS)) + (size_t)jj * nr * ldl;
-  for (int i = lane; i < nr; i += 32) {
-    double acc = 0.0;
-    for (int c = 0; c < nr; ++c) acc = fma(__ldg(L + (size_t)c * ldl + i), __ldg(g + c), acc);
-    hout[i] = acc;
+  const bool a4 = field == 0;
+  const double* A;
+  const double* x;
+  double* y;
+  int m;
+  if (FIX) {
+    const int par = jj & 1, c = (jj >> 1) / a.kc;
+    if (c == 0 || (a.sym && !(a4 ? par == 0 : par == 1))) return;
+    m = a4 ? 2 * nr : nr;
+    A = (a4 ? a.GA4 : (field == 1 ? a.GT : a.GS)) + (size_t)jj * m * ldl;
+    x = a.cbuf + (size_t)b * a.d_stride + ((size_t)(field * 2 + par) * a.nch + c) * a.ldd;
+    y = a.f + (size_t)b * a.f_stride + foff + (size_t)row * nr;
+  } else {
+    m = nr;
+    A = (a4 ? a.LinvA4 : (field == 1 ? a.LinvT : a.LinvS)) + (size_t)jj * nr * ldl;
+    x = a.g + (size_t)b * a.g_stride + foff + (size_t)row * nr;
+    y = a.h + (size_t)b * a.h_stride + foff + (size_t)row * nr;
   }
+  for (int r = lane; r < nr; r += 32) {
+    double acc = 0.0;
+#pragma unroll 8
+    for (int col = 0; col < m; ++col) acc = fma(__ldg(A + (size_t)col * ldl + r), __ldg(x + col), acc);
+    if (FIX) y[r] += acc;
+    else y[r] = acc;
+  }
+}
+
+template <bool FIX>
+static cudaError_t launch_mode_mv(const ChainArgs& a, int batch, int nfields, cudaStream_t s, bool per_warp) {
+  if (per_warp) {
+    k_mode_mv_warp<FIX><<<dim3((nfields * a.M + 3) / 4, batch), 128, 0, s>>>(a, nfields);
+    return cudaGetLastError();
+  }
+  const dim3 grid(nfields * a.M, batch);
+  if (a.nr <= 32) k_mode_mv<4, FIX><<<grid, 128, 0, s>>>(a);
+  else k_mode_mv<2, FIX><<<grid, 128, 0, s>>>(a);
+  return cudaGetLastError();
 }
 
 static int sm_count() {
@@ -342,8 +374,12 @@ static int sm_count() {
   return sms;
 }
 
-static cudaError_t launch_chunked(const ChainArgs& a, int batch, int nfields, cudaStream_t s) {
+static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields, cudaStream_t s) {
   cudaError_t e;
+  if ((e = launch_mode_mv<false>(a_in, batch, nfields, s, false)) != cudaSuccess) return e;   // h = Linv g
+  ChainArgs a = a_in;
+  a.g = a.h;
+  a.g_stride = a.h_stride;
   const size_t smem = chunk_smem_bytes(a.kc, a.nr, a.ldl);
   const dim3 grid(2 * nfields, batch, a.nch);
   if (a.nr <= 32) {
@@ -381,17 +417,15 @@ static cudaError_t launch_chunked(const ChainArgs& a, int batch, int nfields, cu
     }
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  const int hw = 4;
-  k_chain_fix<<<dim3((nfields * a.M + hw - 1) / hw, batch), 32 * hw, 0, s>>>(a, nfields);
-  return cudaGetLastError();
+  return launch_mode_mv<true>(a, batch, nfields, s, false);
 }
 
 // One CTA per chain.  When the batch leaves SMs idle (2*nfields*batch <= #SMs) the 4-warp split-row
 // layout gives the shortest chain; otherwise the one-lane-per-row layout issues the fewest FP64
 // instructions and several chains share every SM.  Layout 2 (chunked: nch CTAs per chain, a short
 // carried-state recurrence and a parallel correction) is chosen automatically while all its CTAs fit
-// on the GPU at two per SM.  a.g holds the right-hand sides; a.h receives h = Linv g (k_hpre) for the
-// one-CTA-per-chain layouts and is what those chains read.
+// on the GPU at two per SM.  a.g holds the right-hand sides; a.h receives h = Linv g (k_mode_mv), which
+// is what the chains read.
 cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStream_t s) {
   ChainArgs a = a_in;
   const int sms = sm_count();
@@ -408,15 +442,13 @@ cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStre
     if (!a.GA4 || a.kc < 1 || a.nch < 1) return cudaErrorInvalidValue;
     return launch_chunked(a, batch, nfields, s);
   }
-  const int hw = 4;
-  k_hpre<<<dim3((nfields * a.M + hw - 1) / hw, batch), 32 * hw, 0, s>>>(a, nfields);
-  cudaError_t e = cudaGetLastError();
+  const bool split = layout == 4 || (layout == 0 && 2 * nfields * batch <= sms);
+  cudaError_t e = launch_mode_mv<false>(a, batch, nfields, s, !split);   // h = Linv g
   if (e != cudaSuccess) return e;
   a.g = a.h;
   a.g_stride = a.h_stride;
   const size_t smem = chain_smem_bytes(a.M, a.nr, a.ldl);
   const dim3 grid(2 * nfields, batch);
-  const bool split = layout == 4 || (layout == 0 && 2 * nfields * batch <= sms);
   if (split && a.nr <= 32) {
     static unsigned long long done = 0;
     if ((e = ensure_smem_attr(k_chain<4, false>, &done)) != cudaSuccess) return e;

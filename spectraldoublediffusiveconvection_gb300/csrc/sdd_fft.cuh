@@ -31,8 +31,11 @@ template <typename C> __device__ __forceinline__ C cmk(decltype(C::x) a, decltyp
 }
 template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return cmk<C>(a.x + b.x, a.y + b.y); }
 template <typename C> __device__ __forceinline__ C csub(C a, C b) { return cmk<C>(a.x - b.x, a.y - b.y); }
+// Every multiply-add is an explicit fma (the translation units that include this file are compiled
+// without automatic contraction), so the rounding of a transform does not depend on the kernel it is
+// inlined into.
 template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
-  return cmk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  return cmk<C>(fma(a.x, b.x, -(a.y * b.y)), fma(a.x, b.y, a.y * b.x));
 }
 // multiply by -i (forward) or +i (inverse)
 template <typename C, bool INV> __device__ __forceinline__ C cmul_mi(C a) {
@@ -65,11 +68,11 @@ __device__ __forceinline__ void butterfly(typename Cplx<T>::type (&v)[R], const 
     const T h = (T)0.86602540378443864676;  // sqrt(3)/2
     C s = cadd(v[1], v[2]);
     C d = csub(v[1], v[2]);
-    C t = cmk<C>(v[0].x - (T)0.5 * s.x, v[0].y - (T)0.5 * s.y);
+    C t = cmk<C>(fma((T)-0.5, s.x, v[0].x), fma((T)-0.5, s.y, v[0].y));
     C u = cmul_mi<C, INV>(d);  // -i d forward
     v[0] = cadd(v[0], s);
-    v[1] = cmk<C>(t.x + h * u.x, t.y + h * u.y);
-    v[2] = cmk<C>(t.x - h * u.x, t.y - h * u.y);
+    v[1] = cmk<C>(fma(h, u.x, t.x), fma(h, u.y, t.y));
+    v[2] = cmk<C>(fma(-h, u.x, t.x), fma(-h, u.y, t.y));
   } else {  // small prime radix (5, 7): direct DFT with roots of unity from the table
     C o[R];
     const int step = L / R;

@@ -97,7 +97,7 @@ __device__ __forceinline__ void block_max_scales(typename Bits<T>::U (&v)[K], ty
 size_t fx_smem_bytes(int M, int P, int prec) {
   (void)M;
   const size_t es = prec == SDD_PREC_MIXED ? sizeof(float) : sizeof(double);
-  return (34 * (size_t)P + 2 * kMaxNr + 32) * es + 9 * 32 * 8;
+  return (34 * (size_t)P + 2 + 2 * kMaxNr + 32) * es + 9 * 32 * 8;
 }
 
 // DCT3 input x_k of transform t of the nine fields (see the header comment of sdd_fft.cuh); kf[k] = k.
@@ -125,6 +125,59 @@ __device__ __forceinline__ T fx_x(int t, int k, int M, int P, const T* kf, const
   }
 }
 
+// Arithmetic shared by the fused and the split nonlinear-term kernels.  This file is compiled without
+// automatic fma contraction and every multiply-add below is an explicit fma, so both kernels round
+// identically.
+// J_theta_RT (:437-472) and A2_SINE_R2 (:476-526) at mode k along a row: jp, and om updated from D2 psi.
+template <typename T>
+__device__ __forceinline__ void jp_om(int k, int M, const T* kf, const T* pv, const T* Sc, T ir4n, T& jp, T& om) {
+  const T s1 = (k + 1 < M) ? Sc[k + 1] : (T)0;
+  jp = (k == 0) ? s1 : fma(kf[k + 1], pv[k - 1], (T)2 * s1);
+  const T s2 = (k + 2 < M) ? Sc[k + 2] : (T)0;
+  om = fma(-kf[k + 1], ir4n * fma(kf[k + 2], pv[k], (T)2 * s2), om);
+}
+// W_k of a DCT3 pair (rows A, B with scales sa, sb): s_A V_A(k) + i s_B V_B(k), V(k) = e_k (x_k - i x_{P-k}).
+template <typename T, typename C>
+__device__ __forceinline__ C dct3_pack(C e, T xa, T xar, T xb, T xbr, T sa, T sb) {
+  const T a1 = fma(e.x, xa, e.y * xar), a2 = fma(e.y, xa, -(e.x * xar));
+  const T b1 = fma(e.x, xb, e.y * xbr), b2 = fma(e.y, xb, -(e.x * xbr));
+  return cmk<C>(fma(sa, a1, -(sb * b2)), fma(sa, a2, sb * b1));
+}
+// y_A, y_B of a DCT2 pair from Z_k, Z_{-k} and e_k = 0.5 (cos, sin)(pi k/2P).
+template <typename T, typename C>
+__device__ __forceinline__ void dct2_unpack(C Zk, C Zm, C e, T& ya, T& yb) {
+  ya = fma(e.x, Zk.x + Zm.x, e.y * (Zk.y - Zm.y));
+  yb = fma(e.x, Zk.y + Zm.y, -(e.y * (Zk.x - Zm.x)));
+}
+// Grid products at point i (:791-793 for MODE 0, :884-887 for MODE 1 with base fields bs):
+// pair 0 = (Q, R) (sine type), pair 1 = (NT, NS) (cosine type).
+template <typename T, int MODE>
+__device__ __forceinline__ void grid_products(int pair, const T* RG, const T* bs, int i, int P, T& v0, T& v1) {
+  const T JT = RG[i], DPg = RG[6 * P + i];
+  if (pair == 0) {
+    const T kO = RG[P + i], kDP = RG[2 * P + i], O = RG[5 * P + i];
+    if (MODE != 1) {
+      v0 = JT * O;
+      v1 = fma(kDP, O, DPg * kO);
+    } else {
+      const T aJT = bs[i], akO = bs[P + i], akDP = bs[2 * P + i], aO = bs[5 * P + i], aDP = bs[6 * P + i];
+      v0 = fma(aJT, O, JT * aO);
+      v1 = fma(akDP, O, aDP * kO) + fma(kDP, aO, DPg * akO);
+    }
+  } else {
+    const T DTg = RG[3 * P + i], DCg = RG[4 * P + i], kT = RG[7 * P + i], kC = RG[8 * P + i];
+    if (MODE != 1) {
+      v0 = fma(JT, DTg, -(DPg * kT));
+      v1 = fma(JT, DCg, -(DPg * kC));
+    } else {
+      const T aJT = bs[i], aDT = bs[3 * P + i], aDC = bs[4 * P + i], aDP = bs[6 * P + i];
+      const T akT = bs[7 * P + i], akC = bs[8 * P + i];
+      v0 = fma(JT, aDT, -(DPg * akT)) + fma(aJT, DTg, -(aDP * kT));
+      v1 = fma(JT, aDC, -(DPg * akC)) + fma(aJT, DCg, -(aDP * kC));
+    }
+  }
+}
+
 // MODE 0: NLIN_FX (optionally storing the grid fields); 1: NLIN_DFX with base fields from the cache;
 // 2: grid fields only (fills the cache).
 template <typename T, int MODE>
@@ -140,8 +193,8 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
   C* Wt = RB + 5 * P;
   C* Et = Wt + P;
   T* RG = reinterpret_cast<T*>(Et + P);
-  T* kf = RG + 9 * P;          // kf[k] = k, k < P
-  T* opr = kf + P;
+  T* kf = RG + 9 * P;          // kf[k] = k, k < P + 2
+  T* opr = kf + P + 2;
   T* scl = opr + 2 * kMaxNr;   // 9 scales + 9 inverse scales (inverse transforms), reused for 4+4
   using U = typename Bits<T>::U;
   U* red = reinterpret_cast<U*>(scl + 32);   // 9*32 reduction words
@@ -160,8 +213,8 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
   for (int i = tid; i < P; i += bd) {
     Wt[i] = wg[i];
     Et[i] = eg[i];
-    kf[i] = (T)i;
   }
+  for (int i = tid; i < P + 2; i += bd) kf[i] = (T)i;
   const T* Drg = reinterpret_cast<const T*>(a.ops.Dr);
   const T* D2g = reinterpret_cast<const T*>(a.ops.D2r2);
   for (int m = tid; m < nr; m += bd) {
@@ -184,15 +237,15 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
     if (psi_on) {
       for (int m = 0; m < nr; ++m) {
         const T x = (T)__ldg(ps + m);
-        dp += opr[m] * x;
-        d2 += opr[nr + m] * x;
+        dp = fma(opr[m], x, dp);
+        d2 = fma(opr[nr + m], x, d2);
       }
       pn = (T)__ldg(ps + n);
     }
     if (ts_on) {
       for (int m = 0; m < nr; ++m) {
-        dtv += opr[m] * (T)__ldg(ts + m);
-        dcv += opr[m] * (T)__ldg(ss + m);
+        dtv = fma(opr[m], (T)__ldg(ts + m), dtv);
+        dcv = fma(opr[m], (T)__ldg(ss + m), dcv);
       }
       tn = (T)__ldg(ts + n);
       sn = (T)__ldg(ss + n);
@@ -209,12 +262,7 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
   parity_suffix<T>(pv, Sc, M);
   __syncthreads();
   // J_theta_RT (:437-472) and A2_SINE_R2 (:476-526) along the row
-  for (int k = tid; k < M; k += bd) {
-    const T s1 = (k + 1 < M) ? Sc[k + 1] : (T)0;
-    JP[k] = (k == 0) ? s1 : kf[k + 1] * pv[k - 1] + (T)2 * s1;
-    const T s2 = (k + 2 < M) ? Sc[k + 2] : (T)0;
-    OM[k] = OM[k] - kf[k + 1] * (ir4n * (kf[k + 2] * pv[k] + (T)2 * s2));
-  }
+  for (int k = tid; k < M; k += bd) jp_om<T>(k, M, kf, pv, Sc, ir4n, JP[k], OM[k]);
   __syncthreads();
   // ---- 2. nine inverse transforms as five paired DCT3s (:776-786) ----
   // the nine DCT3 input rows, materialised once (in RB, free until the FFT), with their maxima
@@ -245,10 +293,7 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
       RA[idx] = cmk<C>(sa * xa, sb * xb);
     } else {
       const T xar = XV[ta * P + P - k], xbr = (tb < 9) ? XV[tb * P + P - k] : (T)0;
-      const C e = Et[k];
-      const T a1 = e.x * xa + e.y * xar, a2 = e.y * xa - e.x * xar;
-      const T b1 = e.x * xb + e.y * xbr, b2 = e.y * xb - e.x * xbr;
-      RA[idx] = cmk<C>(sa * a1 - sb * b2, sa * a2 + sb * b1);
+      RA[idx] = dct3_pack<T, C>(Et[k], xa, xar, xb, xbr, sa, sb);
     }
   }
   __syncthreads();
@@ -277,22 +322,9 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
                             : nullptr;
   U m4[4] = {0, 0, 0, 0};
   for (int i = tid; i < P; i += bd) {
-    const T JT = RG[i], kO = RG[P + i], kDP = RG[2 * P + i], DTg = RG[3 * P + i], DCg = RG[4 * P + i];
-    const T O = RG[5 * P + i], DPg = RG[6 * P + i], kT = RG[7 * P + i], kC = RG[8 * P + i];
     T Q, Rr, NT, NS;
-    if (MODE == 0) {
-      Q = JT * O;
-      Rr = kDP * O + DPg * kO;
-      NT = JT * DTg - DPg * kT;
-      NS = JT * DCg - DPg * kC;
-    } else {
-      const T aJT = bs[i], akO = bs[P + i], akDP = bs[2 * P + i], aDT = bs[3 * P + i], aDC = bs[4 * P + i];
-      const T aO = bs[5 * P + i], aDP = bs[6 * P + i], akT = bs[7 * P + i], akC = bs[8 * P + i];
-      Q = aJT * O + JT * aO;
-      Rr = (akDP * O + aDP * kO) + (kDP * aO + DPg * akO);
-      NT = (JT * aDT - DPg * akT) + (aJT * DTg - aDP * kT);
-      NS = (JT * aDC - DPg * akC) + (aJT * DCg - aDP * kC);
-    }
+    grid_products<T, MODE>(0, RG, bs, i, P, Q, Rr);
+    grid_products<T, MODE>(1, RG, bs, i, P, NT, NS);
     const T sg = (i & 1) ? (T)-1 : (T)1;
     PR[i] = sg * Q;
     PR[P + i] = sg * Rr;
@@ -332,14 +364,235 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
       k = s;
     }
     if (!zero) {
-      const C Zk = Z[p * P + k];
-      const C Zm = Z[p * P + ((P - k) % P)];
-      const C e = Et[k];
-      ya = e.x * (Zk.x + Zm.x) + e.y * (Zk.y - Zm.y);
-      yb = e.x * (Zk.y + Zm.y) - e.y * (Zk.x - Zm.x);
+      dct2_unpack<T, C>(Z[p * P + k], Z[p * P + ((P - k) % P)], Et[k], ya, yb);
       const T sc = (p == 1 && k == 0) ? one_P : two_P;
       ya *= sc * scl[4 + 2 * p];
       yb *= sc * scl[4 + 2 * p + 1];
+    }
+    const size_t q0 = (size_t)(2 * p) * N + (size_t)s * nr + n;
+    o[q0] = (double)ya;
+    o[q0 + N] = (double)yb;
+  }
+}
+
+// ---- split nonlinear term: the same arithmetic over 7 CTAs per radial row ------------------------
+// k_fx_rows runs a row's five paired inverse and two paired forward transforms one after the other on
+// one SM, so a single shell occupies only nr SMs.  For small batches the work is split:
+//   k_fx_grid (nr x 5 CTAs per shell): CTA (n, p) forms the DCT3 input rows t = 2p, 2p+1 of row n (with
+//     the radial contractions those two fields need), runs their paired inverse transform and writes the
+//     two grid rows to grid[shell][n][t][P] (the layout of the base-state cache);
+//   k_fx_prod (nr x 2 CTAs per shell): CTA (n, p) forms product pair p on the grid of row n (p = 0: the
+//     sine-type Q, R; p = 1: the cosine-type NT, NS) and runs their paired forward transform into out4.
+// Per element the operations and their order are those of k_fx_rows, so the results are identical.
+constexpr int kFxSplitThreads = 256;
+
+size_t fx_grid_smem_bytes(int M, int P, int prec) {
+  const size_t es = prec == SDD_PREC_MIXED ? sizeof(float) : sizeof(double);
+  return (8 * (size_t)P + P + 2 + 9 * (size_t)M + 2 * kMaxNr + 32) * es + 2 * 32 * 8;
+}
+size_t fx_prod_smem_bytes(int P, int prec) {
+  const size_t es = prec == SDD_PREC_MIXED ? sizeof(float) : sizeof(double);
+  return (8 * (size_t)P + 2 * (size_t)P + 32) * es + 2 * 32 * 8;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, size_t grid_stride) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int M = a.M, nr = a.nr, P = a.P;
+  const int n = blockIdx.x, pr = blockIdx.y, b = blockIdx.z;
+  const int tid = threadIdx.x, bd = blockDim.x;
+  const int ta = 2 * pr, tb = 2 * pr + 1;      // tb = 9 (absent) for the last pair
+
+  C* RA = reinterpret_cast<C*>(smem_raw);
+  C* RB = RA + P;
+  C* Wt = RB + P;
+  C* Et = Wt + P;
+  T* kf = reinterpret_cast<T*>(Et + P);   // kf[k] = k, k < P + 2
+  T* pv = kf + P + 2;
+  T* Tv = pv + M;
+  T* Sv = Tv + M;
+  T* DP = Sv + M;
+  T* OM = DP + M;
+  T* DTv = OM + M;
+  T* DCv = DTv + M;
+  T* JP = DCv + M;
+  T* Sc = JP + M;
+  T* opr = Sc + M;
+  T* scl = opr + 2 * kMaxNr;
+  using U = typename Bits<T>::U;
+  U* red = reinterpret_cast<U*>(scl + 32);
+
+  const C* wg = reinterpret_cast<const C*>(a.ops.w);
+  const C* eg = reinterpret_cast<const C*>(a.ops.e);
+  for (int i = tid; i < P; i += bd) {
+    Wt[i] = wg[i];
+    Et[i] = eg[i];
+  }
+  for (int i = tid; i < P + 2; i += bd) kf[i] = (T)i;
+  const T* Drg = reinterpret_cast<const T*>(a.ops.Dr);
+  const T* D2g = reinterpret_cast<const T*>(a.ops.D2r2);
+  for (int m = tid; m < nr; m += bd) {
+    opr[m] = Drg[n * nr + m];
+    opr[nr + m] = D2g[n * nr + m];
+  }
+  const T ir4n = reinterpret_cast<const T*>(a.ops.ir4r2)[n];
+  __syncthreads();
+
+  // which row quantities the pair's two fields need (fields: 0 JT_psi, 1 komega, 2 kDpsi, 3 DT, 4 DC,
+  // 5 omega, 6 Dpsi, 7 kT, 8 kC)
+  const bool need_psi = pr == 0 || pr == 2;            // pv (JT_psi, omega's A2 term) and D2 psi (omega)
+  const bool need_dp = pr == 1 || pr == 3;             // Dr psi
+  const bool need_dt = pr == 1, need_dc = pr == 2;   // pairs 3 and 4 also use the T / S row values
+  const int N = M * nr;
+  const double* Xs = a.X + (size_t)b * a.x_stride;
+  for (int k = tid; k < M; k += bd) {
+    const double* ps = Xs + (size_t)k * nr;
+    const double* ts = Xs + N + (size_t)k * nr;
+    const double* ss = Xs + 2 * N + (size_t)k * nr;
+    const bool psi_on = !(a.sym && (k % 2 == 0));
+    const bool ts_on = !(a.sym && (k % 2 == 1));
+    T dp = 0, d2 = 0, dtv = 0, dcv = 0, pn = 0, tn = 0, sn = 0;
+    if (psi_on && (need_psi || need_dp)) {
+      for (int m = 0; m < nr; ++m) {
+        const T x = (T)__ldg(ps + m);
+        if (need_dp) dp = fma(opr[m], x, dp);
+        if (need_psi) d2 = fma(opr[nr + m], x, d2);
+      }
+      pn = (T)__ldg(ps + n);
+    }
+    if (ts_on) {
+      if (need_dt)
+        for (int m = 0; m < nr; ++m) dtv = fma(opr[m], (T)__ldg(ts + m), dtv);
+      if (need_dc)
+        for (int m = 0; m < nr; ++m) dcv = fma(opr[m], (T)__ldg(ss + m), dcv);
+      tn = (T)__ldg(ts + n);
+      sn = (T)__ldg(ss + n);
+    }
+    pv[k] = pn;
+    Tv[k] = tn;
+    Sv[k] = sn;
+    DP[k] = dp;
+    OM[k] = d2;
+    DTv[k] = dtv;
+    DCv[k] = dcv;
+  }
+  __syncthreads();
+  if (need_psi) {
+    parity_suffix<T>(pv, Sc, M);
+    __syncthreads();
+    for (int k = tid; k < M; k += bd) jp_om<T>(k, M, kf, pv, Sc, ir4n, JP[k], OM[k]);
+    __syncthreads();
+  }
+  // the pair's two DCT3 input rows (in RB, free until the FFT) and their maxima
+  T* XV = reinterpret_cast<T*>(RB);
+  {
+    U mb[2] = {0, 0};
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int t = ta + u;
+      if (t < 9)
+        for (int k = tid; k < P; k += bd) {
+          const T v = fx_x<T>(t, k, M, P, kf, JP, OM, DP, DTv, DCv, Tv, Sv);
+          XV[u * P + k] = v;
+          const U w = Bits<T>::absbits(v);
+          mb[u] = w > mb[u] ? w : mb[u];
+        }
+    }
+    block_max_scales<T, 2>(mb, red, scl);
+  }
+  const T sa = scl[0], sb = (tb < 9) ? scl[1] : (T)0;
+  for (int k = tid; k < P; k += bd) {
+    const T xa = XV[k], xb = (tb < 9) ? XV[P + k] : (T)0;
+    if (k == 0) {
+      RA[k] = cmk<C>(sa * xa, sb * xb);
+    } else {
+      const T xar = XV[P - k], xbr = (tb < 9) ? XV[P + P - k] : (T)0;
+      RA[k] = dct3_pack<T, C>(Et[k], xa, xar, xb, xbr, sa, sb);
+    }
+  }
+  __syncthreads();
+  C* res = fft_rows<T, true>(RA, RB, 1, a.st, Wt);
+  T* g = grid + (size_t)b * grid_stride + (size_t)n * 9 * P;
+  const int nt = (tb < 9) ? 2 : 1;
+  for (int idx = tid; idx < nt * P; idx += bd) {
+    const int u = idx / P;
+    const int i = idx - u * P;
+    const int t = ta + u;
+    const int src = (i & 1) ? (P - 1 - (i >> 1)) : (i >> 1);
+    const C v = res[src];
+    T val = (u ? v.y : v.x) * scl[2 + u];
+    if (t >= 5 && (i & 1)) val = -val;
+    g[(size_t)t * P + i] = val;
+  }
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kFxSplitThreads) k_fx_prod(FxArgs a, const T* grid, size_t grid_stride) {
+  using C = typename Cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int M = a.M, nr = a.nr, P = a.P;
+  const int n = blockIdx.x, p = blockIdx.y, b = blockIdx.z;
+  const int tid = threadIdx.x, bd = blockDim.x;
+  C* RA = reinterpret_cast<C*>(smem_raw);
+  C* RB = RA + P;
+  C* Wt = RB + P;
+  C* Et = Wt + P;
+  T* PR = reinterpret_cast<T*>(Et + P);
+  T* scl = PR + 2 * P;
+  using U = typename Bits<T>::U;
+  U* red = reinterpret_cast<U*>(scl + 32);
+  const C* wg = reinterpret_cast<const C*>(a.ops.w);
+  const C* eg = reinterpret_cast<const C*>(a.ops.e);
+  for (int i = tid; i < P; i += bd) {
+    Wt[i] = wg[i];
+    Et[i] = eg[i];
+  }
+  const T* RG = grid + (size_t)b * grid_stride + (size_t)n * 9 * P;
+  const T* bs = (MODE == 1) ? reinterpret_cast<const T*>(a.base) + (size_t)b * a.base_stride + (size_t)n * 9 * P
+                            : nullptr;
+  U m2[2] = {0, 0};
+  for (int i = tid; i < P; i += bd) {
+    T v0, v1;
+    grid_products<T, MODE>(p, RG, bs, i, P, v0, v1);
+    if (p == 0) {
+      const T sg = (i & 1) ? (T)-1 : (T)1;
+      PR[i] = sg * v0;
+      PR[P + i] = sg * v1;
+    } else {
+      PR[i] = v0;
+      PR[P + i] = v1;
+    }
+    const U u0 = Bits<T>::absbits(v0), u1 = Bits<T>::absbits(v1);
+    m2[0] = u0 > m2[0] ? u0 : m2[0];
+    m2[1] = u1 > m2[1] ? u1 : m2[1];
+  }
+  block_max_scales<T, 2>(m2, red, scl);   // scl[0..2) scales, scl[2..4) inverses
+  for (int nn = tid; nn < P; nn += bd) {
+    const int src = makhoul_src(nn, P);
+    RB[nn] = cmk<C>(scl[0] * PR[src], scl[1] * PR[P + src]);
+  }
+  __syncthreads();
+  C* Z = fft_rows<T, false>(RB, RA, 1, a.st, Wt);
+  const int N = M * nr;
+  double* o = a.out4 + (size_t)b * a.out_stride;
+  const T two_P = (T)2 / (T)P, one_P = (T)1 / (T)P;
+  for (int s = tid; s < M; s += bd) {
+    T ya = 0, yb = 0;
+    bool zero;
+    int k;
+    if (p == 0) {            // sine pair: slot s <-> wavenumber s+1, read at k = P-1-s
+      zero = (s == M - 1) || (a.sym && (s % 2 == 0));
+      k = P - 1 - s;
+    } else {
+      zero = a.sym && (s % 2 == 1);
+      k = s;
+    }
+    if (!zero) {
+      dct2_unpack<T, C>(Z[k], Z[(P - k) % P], Et[k], ya, yb);
+      const T sc = (p == 1 && k == 0) ? one_P : two_P;
+      ya *= sc * scl[2];
+      yb *= sc * scl[3];
     }
     const size_t q0 = (size_t)(2 * p) * N + (size_t)s * nr + n;
     o[q0] = (double)ya;
@@ -375,12 +628,12 @@ __global__ void __launch_bounds__(kFxThreads) k_rhs(RhsArgs a) {
     const double* ps = Xs + (size_t)k * nr;
     double d2 = 0, pn = 0, q = 0;
     if (psi_on) {
-      for (int m = 0; m < nr; ++m) d2 += opr[nr + m] * __ldg(ps + m);
+      for (int m = 0; m < nr; ++m) d2 = fma(opr[nr + m], __ldg(ps + m), d2);
       pn = __ldg(ps + n);
     }
     if (O4) {
       const double* qs = O4 + (size_t)k * nr;
-      for (int m = 0; m < nr; ++m) q += opr[m] * __ldg(qs + m);
+      for (int m = 0; m < nr; ++m) q = fma(opr[m], __ldg(qs + m), q);
     }
     pv[k] = pn;
     D2p[k] = d2;
@@ -447,7 +700,7 @@ __global__ void __launch_bounds__(kFxThreads) k_theta_op(ThetaArgs a) {
     if (on) {
       const double* ps = g + (size_t)k * nr;
       if (a2)
-        for (int m = 0; m < nr; ++m) d2 += opr[m] * __ldg(ps + m);
+        for (int m = 0; m < nr; ++m) d2 = fma(opr[m], __ldg(ps + m), d2);
       pn = __ldg(ps + n);
     }
     pv[k] = pn;
@@ -549,7 +802,7 @@ __global__ void __launch_bounds__(kFxThreads) k_transform(TrArgs a) {
           V[h] = make_double2(x, 0.0);
         } else {
           const C e = Et[k];
-          V[h] = make_double2(e.x * x + e.y * xr, e.y * x - e.x * xr);
+          V[h] = make_double2(fma(e.x, x, e.y * xr), fma(e.y, x, -(e.x * xr)));
         }
       }
       RA[idx] = make_double2(V[0].x - V[1].y, V[0].y + V[1].x);
@@ -597,9 +850,9 @@ __global__ void __launch_bounds__(kFxThreads) k_transform(TrArgs a) {
         const C Zm = Z[p * L + ((L - k) % L)];
         const C e = Et[k];
         if ((t & 1) == 0)
-          y = e.x * (Zk.x + Zm.x) + e.y * (Zk.y - Zm.y);
+          y = fma(e.x, Zk.x + Zm.x, e.y * (Zk.y - Zm.y));
         else
-          y = e.x * (Zk.y + Zm.y) - e.y * (Zk.x - Zm.x);
+          y = fma(e.x, Zk.y + Zm.y, -(e.y * (Zk.x - Zm.x)));
         y *= ((!sine && k == 0) ? 1.0 / L : 2.0 / L) * scl[4 + t];
       }
       a.out[(size_t)r * n_out + s] = y;
@@ -629,7 +882,7 @@ __global__ void __launch_bounds__(kFxThreads) k_fx_finish(FinishArgs a) {
   for (int k = threadIdx.x; k < M; k += blockDim.x) {
     const double* qs = O4 + (size_t)k * nr;
     double q = 0;
-    for (int m = 0; m < nr; ++m) q += opr[m] * qs[m];
+    for (int m = 0; m < nr; ++m) q = fma(opr[m], qs[m], q);
     const size_t o = (size_t)k * nr + n;
     F[o] = q - O4[N + o];
     F[N + o] = O4[2 * N + o];
@@ -648,7 +901,57 @@ static cudaError_t launch_fx_t(const FxArgs& a, int batch, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+template <typename T, int MODE>
+static cudaError_t launch_fx_split_t(const FxArgs& a, int batch, cudaStream_t s) {
+  const int prec = sizeof(T) == 4 ? SDD_PREC_MIXED : SDD_PREC_FP64;
+  // grid rows go to the caller's cache when one is given (modes 0 and 2), else to the scratch
+  T* grid = reinterpret_cast<T*>((MODE != 1 && a.base) ? a.base : a.grid);
+  const size_t gs = (MODE != 1 && a.base) ? a.base_stride : a.grid_stride;
+  cudaError_t e;
+  {
+    static unsigned long long done = 0;
+    if ((e = ensure_smem_attr(k_fx_grid<T>, &done)) != cudaSuccess) return e;
+    k_fx_grid<T><<<dim3(a.nr, 5, batch), kFxSplitThreads, fx_grid_smem_bytes(a.M, a.P, prec), s>>>(a, grid, gs);
+    if ((e = cudaGetLastError()) != cudaSuccess || MODE == 2) return e;
+  }
+  constexpr int PM = MODE == 1 ? 1 : 0;
+  static unsigned long long done = 0;
+  if ((e = ensure_smem_attr(k_fx_prod<T, PM>, &done)) != cudaSuccess) return e;
+  k_fx_prod<T, PM><<<dim3(a.nr, 2, batch), kFxSplitThreads, fx_prod_smem_bytes(a.P, prec), s>>>(a, grid, gs);
+  return cudaGetLastError();
+}
+
+static int fx_sm_count() {
+  static const int sms = [] {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+  }();
+  return sms;
+}
+
+// The split path is taken when forced (split = 2) or, automatically, while the fused kernel would leave
+// most SMs idle (nr * batch CTAs below half the SMs); it needs a grid scratch (or none: mode 2 and
+// cached mode 0 write the cache).  A batch that shares the GPU with other launches (the captured
+// multi-group graphs) is better served by the fused kernel; its autotuner sets the choice per plan.
+static bool use_split(const FxArgs& a, int batch, int mode) {
+  const bool has_grid = (mode != 1 && a.base) || a.grid;
+  if (!has_grid || a.split == 1) return false;
+  return a.split == 2 || 2 * a.nr * batch <= fx_sm_count();
+}
+
 cudaError_t launch_fx(const FxArgs& a, int batch, int mode, int prec, cudaStream_t s) {
+  if (use_split(a, batch, mode)) {
+    if (prec == SDD_PREC_MIXED) {
+      if (mode == 0) return launch_fx_split_t<float, 0>(a, batch, s);
+      if (mode == 1) return launch_fx_split_t<float, 1>(a, batch, s);
+      return launch_fx_split_t<float, 2>(a, batch, s);
+    }
+    if (mode == 0) return launch_fx_split_t<double, 0>(a, batch, s);
+    if (mode == 1) return launch_fx_split_t<double, 1>(a, batch, s);
+    return launch_fx_split_t<double, 2>(a, batch, s);
+  }
   if (prec == SDD_PREC_MIXED) {
     if (mode == 0) return launch_fx_t<float, 0>(a, batch, s);
     if (mode == 1) return launch_fx_t<float, 1>(a, batch, s);

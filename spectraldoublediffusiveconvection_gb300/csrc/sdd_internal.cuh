@@ -75,6 +75,9 @@ struct FxArgs {
   size_t out_stride;         // doubles between shells in out4
   double* fx_out;            // optional: write F directly in state layout [shell][3][M][nr]
   size_t fx_stride;
+  void* grid;                // nullable: grid-field scratch [shell][nr][9][P] (T precision) of the split path
+  size_t grid_stride;        // elements between shells in grid
+  int split;                 // 0 auto, 1 fused row kernel, 2 split (needs grid or a cache)
 };
 
 struct RhsArgs {

@@ -74,6 +74,7 @@ class Plan:
         self._h = h
         self._L = L
         self.n_state = 3 * self.N_fm * self.nr
+        self._scalars = {}
         self.base_elems = int(L.sdd_plan_base_cache_elems(h))
 
     # ------------------------------------------------------------------------------------------
@@ -106,7 +107,16 @@ class Plan:
             if v.numel() == 1:
                 v = v.expand(batch).contiguous()
             return v.contiguous()
-        return torch.full((batch,), float(v), dtype=torch.float64, device=self.device)
+        # scalar parameters: one cached device vector per (value, batch), so repeated calls pass the same
+        # pointers (sdd_step replays its captured graphs only for the pointers they were captured with)
+        key = (float(v), int(batch))
+        t = self._scalars.get(key)
+        if t is None:
+            if len(self._scalars) >= 64:
+                self._scalars.clear()
+            t = torch.full((batch,), float(v), dtype=torch.float64, device=self.device)
+            self._scalars[key] = t
+        return t
 
     def reserve(self, batch):
         """Allocate the plan's workspace for up to ``batch`` shells now (required before graph capture)."""
@@ -118,6 +128,11 @@ class Plan:
         """0 automatic, 1 one lane per row, 2 chunked, 4 rows split over 4 warps (sdd_plan_set_chain_layout)."""
         _lib.check(self._L.sdd_plan_set_chain_layout(self._h, int(layout)), "sdd_plan_set_chain_layout")
         self.chain_layout = int(layout)
+
+    def set_fx_split(self, mode):
+        """0 automatic, 1 fused row kernel, 2 split row work (sdd_plan_set_fx_split); identical results."""
+        _lib.check(self._L.sdd_plan_set_fx_split(self._h, int(mode)), "sdd_plan_set_fx_split")
+        self.fx_split = int(mode)
 
     def new_state(self, batch=1):
         torch = _torch()

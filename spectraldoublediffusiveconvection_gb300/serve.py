@@ -28,6 +28,7 @@ import time
 import numpy as np
 
 from .plan import Plan
+from .seeds import seeded_state
 
 
 def _torch():
@@ -62,14 +63,7 @@ class Request:
 
 
 def _seeded(M, nr, seed):
-    rng = np.random.default_rng(seed)
-    k = np.arange(M)[None, :]
-    n = np.arange(nr)[:, None]
-    amp = 1e-3 * np.exp(-k / 8.0) * np.exp(-n / 4.0)
-    P, T, S = [rng.standard_normal((nr, M)) * amp for _ in range(3)]
-    X = np.zeros((3, M, nr))
-    X[0], X[1], X[2] = P.T, T.T, S.T
-    return X.reshape(-1)
+    return seeded_state(M, nr, seed)
 
 
 class _IntGroup:

@@ -79,3 +79,41 @@ def test_chunked_batch_equals_alone(cuda):
     for i in range(4):
         Xi = p.step(torch.from_numpy(Xs[i:i + 1]).cuda(), float(Ra[i]), 500.0, nsteps=4)
         assert torch.equal(Xb[i:i + 1], Xi)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_split_nonlinear_term_equals_fused(cuda, precision):
+    """Small batches run the nonlinear term split over 7 CTAs per radial row, large ones the fused row
+    kernel; per element the arithmetic is the same, so a shell gives identical bits either way."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    N_fm, N_r = 256, 30        # split while 2 * 29 * batch <= #SMs: batch 1 split, batch 4 fused
+    p = Plan(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01, precision=precision)
+    p.set_chain_layout(1)
+    Xs = torch.from_numpy(np.stack([O.seeded_state(N_fm, N_r - 1, s) for s in range(4)])).cuda()
+    dvs = torch.from_numpy(np.stack([O.seeded_state(N_fm, N_r - 1, 50 + s) for s in range(4)])).cuda()
+    Fb = p.nlin_fx(Xs)
+    Db = p.nlin_dfx(dvs, Xs)
+    Sb = p.step(Xs, 8000.0, 500.0, nsteps=2)
+    for i in range(4):
+        assert torch.equal(p.nlin_fx(Xs[i:i + 1]), Fb[i:i + 1])
+        assert torch.equal(p.nlin_dfx(dvs[i:i + 1], Xs[i:i + 1]), Db[i:i + 1])
+        assert torch.equal(p.step(Xs[i:i + 1], 8000.0, 500.0, nsteps=2), Sb[i:i + 1])
+
+
+def test_forced_nonlinear_term_paths_agree(cuda):
+    """sdd_plan_set_fx_split: the forced fused and forced split kernels give the same bits on one batch."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    N_fm, N_r = 128, 24
+    p = Plan(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
+    Xs = torch.from_numpy(np.stack([O.seeded_state(N_fm, N_r - 1, s) for s in range(5)])).cuda()
+    dvs = torch.from_numpy(np.stack([O.seeded_state(N_fm, N_r - 1, 20 + s) for s in range(5)])).cuda()
+    out = []
+    for mode in (1, 2):
+        p.set_fx_split(mode)
+        out.append((p.nlin_fx(Xs), p.nlin_dfx(dvs, Xs), p.pfx(Xs, 9000.0, 500.0), p.pdfx(dvs, Xs, 9000.0, 500.0)))
+    for a, b in zip(*out):
+        assert torch.equal(a, b)
+    with pytest.raises(Exception):
+        p.set_fx_split(3)
