@@ -126,6 +126,7 @@ struct sdd_plan {
   double* hbuf;     // [B][3][M][nr] h = Linv g of the chains
   void* base_tmp;   // [B][nr][9][P] (T precision), for DFX without a caller cache
   void* gridbuf;    // [B][nr][9][P] (T precision), grid fields of the split nonlinear-term path
+  void* derivbuf;   // [B][4][M][nr] (T precision), radial derivatives of the split path
   // Krylov / Newton / continuation workspace (grown on demand)
   int sv_B, sv_m;
   double *kv_V, *kv_w, *kv_r, *kv_part, *kv_nrm2, *kv_small, *kv_dot;
@@ -236,6 +237,7 @@ static void free_plan(sdd_plan* p) {
   cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232);
   cudaFree(p->base_tmp);
   cudaFree(p->gridbuf);
+  cudaFree(p->derivbuf);
   solver_free(p);
   delete p;
 }
@@ -460,9 +462,9 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   if (max_batch <= p->ws_batch) return SDD_OK;
   clear_step_graphs(p);   // the graphs bake in the workspace pointers
   cudaFree(p->out4); cudaFree(p->rhs); cudaFree(p->xtmp); cudaFree(p->base_tmp); cudaFree(p->hbuf);
-  cudaFree(p->dbuf); cudaFree(p->cbuf); cudaFree(p->gridbuf);
+  cudaFree(p->dbuf); cudaFree(p->cbuf); cudaFree(p->gridbuf); cudaFree(p->derivbuf);
   p->out4 = p->rhs = p->xtmp = p->hbuf = p->dbuf = p->cbuf = nullptr;
-  p->base_tmp = p->gridbuf = nullptr;
+  p->base_tmp = p->gridbuf = p->derivbuf = nullptr;
   p->ws_batch = 0;
   const size_t se = shell_elems(p);
   const size_t be = sdd_plan_base_cache_elems(p);
@@ -472,6 +474,7 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   SDD_CUDA(cudaMalloc(&p->hbuf, (size_t)max_batch * se * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->base_tmp, (size_t)max_batch * be * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->gridbuf, (size_t)max_batch * be * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->derivbuf, (size_t)max_batch * 5 * p->M * p->nr * sizeof(double)));
   const size_t de = (size_t)6 * p->nch * p->ldd;
   SDD_CUDA(cudaMalloc(&p->dbuf, (size_t)max_batch * de * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->cbuf, (size_t)max_batch * de * sizeof(double)));
@@ -500,12 +503,14 @@ static FxArgs fx_args(const sdd_plan* p, int prec, const double* X, void* base, 
   a.out4 = out4; a.out_stride = (size_t)4 * p->M * p->nr;
   a.grid = p->gridbuf; a.grid_stride = sdd_plan_base_cache_elems(p);
   a.split = p->fx_split;
+  a.deriv = p->derivbuf; a.deriv_stride = (size_t)5 * p->M * p->nr;
   return a;
 }
 
 static RhsArgs rhs_args(const sdd_plan* p, const double* X, const double* out4, const double* Ra,
                         const double* Ras, double* rhs, int linear) {
   RhsArgs a;
+  std::memset(&a, 0, sizeof(a));
   a.M = p->M; a.nr = p->nr; a.sym = p->sym; a.linear = linear;
   a.dt = p->dt; a.Pr = p->Pr;
   a.Dr = p->Dr; a.D2s = p->D2s; a.ir2s = p->ir2s; a.rsq = p->rsq; a.dT0 = p->dT0; a.gr = p->gr;
@@ -518,6 +523,7 @@ static RhsArgs rhs_args(const sdd_plan* p, const double* X, const double* out4, 
 
 static ChainArgs chain_args(const sdd_plan* p, const double* g, double* f, const double* sub) {
   ChainArgs a;
+  std::memset(&a, 0, sizeof(a));
   a.M = p->M; a.nr = p->nr; a.ldl = p->ldl; a.sym = p->sym; a.field0 = 0; a.layout = p->chain_layout;
   a.field_off = (size_t)p->M * p->nr;
   a.g = g; a.g_stride = shell_elems(p);
@@ -547,23 +553,43 @@ static int check_plan(sdd_plan* p, int batch) {
 // One application of Phi (the step map) or its Jacobian to X (or dv), into out.
 // mode 0: FX (nonlinear term of X); 1: DFX about the base in `base`; 2: linear only.
 // Same as apply_step with explicit strides (doubles between shells) of the input X, the output and sub.
+// With the FP64 split nonlinear term, the right-hand sides are not assembled by k_rhs: the grid kernel
+// writes their linear parts and the chains' h kernel adds the nonlinear parts (same roundings).
+// ev (nullable): four events recorded around the nonlinear term, the rhs and the chains.
 static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X, size_t ldx,
                          double* out, size_t ldo, const double* sub, size_t lds, int mode, void* base, int prec,
-                         cudaStream_t s) {
-  cudaError_t e;
+                         cudaStream_t s, cudaEvent_t* ev = nullptr) {
+  RhsArgs ra = rhs_args(p, X, p->out4, Ra, Ras, p->rhs, mode == 2);
+  ra.x_stride = ldx;
+  bool fuse = false;
+  if (ev) SDD_CUDA(cudaEventRecord(ev[0], s));
   if (mode != 2) {
     FxArgs fa = fx_args(p, prec, X, base, p->out4);
     fa.x_stride = ldx;
-    e = launch_fx(fa, batch, mode == 1 ? 1 : 0, prec, s);
-    SDD_CUDA(e);
+    const int fm = mode == 1 ? 1 : 0;
+    fuse = prec == SDD_PREC_FP64 && fx_uses_split(fa, batch, fm);
+    if (fuse) {
+      fa.fuse_rhs = 1;
+      fa.rl = ra;
+    }
+    SDD_CUDA(launch_fx(fa, batch, fm, prec, s));
   }
-  RhsArgs ra = rhs_args(p, X, p->out4, Ra, Ras, p->rhs, mode == 2);
-  ra.x_stride = ldx;
-  SDD_CUDA(launch_rhs(ra, batch, s));
+  if (ev) SDD_CUDA(cudaEventRecord(ev[1], s));
+  if (!fuse) SDD_CUDA(launch_rhs(ra, batch, s));
+  if (ev) SDD_CUDA(cudaEventRecord(ev[2], s));
   ChainArgs ca = chain_args(p, p->rhs, out, sub);
   ca.f_stride = ldo;
   ca.sub_stride = lds;
+  if (fuse) {
+    ca.fuse_rhs = 1;
+    ca.lin = p->rhs;
+    ca.out4 = p->out4;
+    ca.out_stride = (size_t)4 * p->M * p->nr;
+    ca.Dr = p->Dr;
+    ca.dt = p->dt;
+  }
   SDD_CUDA(launch_chain(ca, batch, 3, s));
+  if (ev) SDD_CUDA(cudaEventRecord(ev[3], s));
   return SDD_OK;
 }
 
@@ -1137,17 +1163,10 @@ extern "C" int sdd_step_profile(sdd_plan* p, int B, const double* Ra, const doub
   for (int it = 0; it < nsteps && rc == SDD_OK; ++it) {
     const int left = nsteps - it;
     double* dst = (left % 2 == 1) ? X_out : p->xtmp;
-    cudaError_t e = cudaEventRecord(ev[0], s);
-    FxArgs fa = fx_args(p, p->prec, cur, nullptr, p->out4);
-    if (e == cudaSuccess) e = launch_fx(fa, B, 0, p->prec, s);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[1], s);
-    RhsArgs ra = rhs_args(p, cur, p->out4, Ra, Ras, p->rhs, 0);
-    if (e == cudaSuccess) e = launch_rhs(ra, B, s);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[2], s);
-    ChainArgs ca = chain_args(p, p->rhs, dst, nullptr);
-    if (e == cudaSuccess) e = launch_chain(ca, B, 3, s);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[3], s);
-    if (e == cudaSuccess) e = cudaEventSynchronize(ev[3]);
+    const size_t n = shell_elems(p);
+    rc = apply_step_ld(p, B, Ra, Ras, cur, n, dst, n, nullptr, n, 0, nullptr, p->prec, s, ev);
+    if (rc != SDD_OK) break;
+    cudaError_t e = cudaEventSynchronize(ev[3]);
     float t = 0.f;
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
       e = cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
@@ -1246,6 +1265,7 @@ extern "C" int sdd_nlin_fx_noalloc(sdd_plan* p, int batch, const double* X, doub
   // the row kernel writes every element of the batch's 4*N_fm*nr outputs before k_fx_finish reads them
   FxArgs fa = fx_args(p, SDD_PREC_FP64, X, nullptr, scratch);
   fa.grid = nullptr;   // the fused row kernel: no grid scratch (the plan's may be smaller than the batch)
+  fa.deriv = nullptr;
   SDD_CUDA(launch_fx(fa, batch, 0, SDD_PREC_FP64, s));
   SDD_CUDA(launch_fx_finish(p->M, p->nr, p->Dr, scratch, (size_t)4 * p->M * p->nr, F, shell_elems(p), batch, s));
   return SDD_OK;

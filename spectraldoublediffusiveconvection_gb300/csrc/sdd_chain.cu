@@ -117,8 +117,8 @@ __global__ void k_chain(ChainArgs a) {
   const int blk = ncol * ldl;
   double* Lb0 = csm;                           // 3-slot ring of step matrices
   double* hs = csm + 3 * blk;                  // the chunk's h rows, step-ordered
-  double* cf = hs + (size_t)nsteps * nr;       // per-step scalars (4 per step)
-  double* x2 = cf + 4 * (size_t)nsteps;        // matvec operand: A4 [f_e; bf_e], NAB2 b
+  double* cf = hs + (size_t)nsteps * nr;       // per-step scalars (4 per step, one step past the chunk)
+  double* x2 = cf + 4 * (size_t)(nsteps + 1);  // 2 buffers of the matvec operand: A4 [f_e; bf_e], NAB2 b
   const double* Mat = a4 ? a.ABA4 : (field == 1 ? a.LinvT : a.LinvS);
   const double* coef = a4 ? a.coefA4 : (field == 1 ? a.coefT : a.coefS);   // [M][4] indexed by jj
   const int jj0 = par + 2 * s0;
@@ -134,56 +134,56 @@ __global__ void k_chain(ChainArgs a) {
       hs[e] = h[(size_t)(M - 1 - (par + 2 * (s0 + s))) * nr + c];
     }
   }
-  for (int e = tid; e < 4 * nsteps; e += blockDim.x) cf[e] = coef[(size_t)(jj0 + 2 * (e >> 2)) * 4 + (e & 3)];
-  for (int c = tid; c < 2 * nr; c += blockDim.x) x2[c] = 0.0;
-  __syncthreads();
+  for (int e = tid; e < 4 * (nsteps + 1); e += blockDim.x) {
+    const int jj = jj0 + 2 * (e >> 2);
+    cf[e] = jj < M ? coef[(size_t)jj * 4 + (e & 3)] : 0.0;
+  }
+  for (int c = tid; c < 4 * nr; c += blockDim.x) x2[c] = 0.0;
 
-  double fprev = 0.0;
+  // The lead lane of row i keeps the row's carried state in registers and publishes it to the other
+  // buffer of x2 for the next step's matvec: one barrier per step.
+  //   psi:  f = h + [A B] [f_e; bf_e];  f_e += f,  bf_e += bj f + bjt f_e   (cf = (dt bjt, dt bjt bj, bj, bjt))
+  //   T/S:  f = h - w Linv b;  then b += k' f with k' = 2 dt (j'+2) of the next step   (cf = (k, w, -, -))
+  double fe = 0.0, bfe = 0.0;                  // psi: f_e_i, bf_e_i;  T/S: b_i in fe
   for (int s = 0; s < nsteps; ++s) {
     const int jj = jj0 + 2 * s;
     const int row = M - 1 - jj;
     const double* cur = Lb0 + (s % 3) * blk;
-    const double hi = hs[s * nr + ir];
-    if (!a4) {   // b += 2 dt (j+2) f_{j+2}   (cf = (2 dt (j+2), 0.5 or 1, -, -)); fprev = 0 at a chunk start
-      if (row < M - 2 && lead) x2[i] = fma(cf[4 * s], fprev, x2[i]);
-    }
+    const double* xs = x2 + (s & 1) * 2 * nr;
+    double* xn = x2 + ((s + 1) & 1) * 2 * nr;
+    cp_async_wait<1>();
+    chain_sync();                              // block s landed; this step's x2 visible; step s-1 done
     if (s + 2 < nsteps) copy_block(Lb0 + ((s + 2) % 3) * blk, Mat + (size_t)(jj + 4) * blk, blk);
     cp_async_commit();
-    cp_async_wait<2>();
-    chain_sync();                              // block s landed; x2 of this step visible
+    const double hi = hs[s * nr + ir];
     double fi;
     if (a4) {
-      // f = h + [A B] [f_e; bf_e]   (cf = (dt bjt, dt bjt bj, bj, bjt)); the first step has f_e = bf_e = 0
-      double acc = 0.0;
+      const double pre = fma(cf[4 * s + 3], fe, bfe);   // bf_e + bjt f_e, off the matvec's path
+      double acc = (q == 0) ? hi : 0.0;
       if (s > 0)
-        for (int c = q; c < ncol; c += TPR) acc = fma(cur[c * ldl + ir], x2[c], acc);
-      fi = hi + group_sum<TPR>(acc);
+#pragma unroll 8
+        for (int c = q; c < ncol; c += TPR) acc = fma(cur[c * ldl + ir], xs[c], acc);
+      fi = group_sum<TPR>(acc);
+      fe += fi;
+      bfe = fma(cf[4 * s + 2], fi, pre);
+      if (lead) {
+        xn[i] = fe;
+        xn[nr + i] = bfe;
+      }
     } else {
       double acc = 0.0;
-      for (int c = q; c < nr; c += TPR) acc = fma(cur[c * ldl + ir], x2[c], acc);
+#pragma unroll 8
+      for (int c = q; c < nr; c += TPR) acc = fma(cur[c * ldl + ir], xs[c], acc);
       fi = fma(-cf[4 * s + 1], group_sum<TPR>(acc), hi);
+      fe = fma(cf[4 * (s + 1)], fi, fe);       // the b of the next step (of the next chunk after the last)
+      if (lead) xn[i] = fe;
     }
-    chain_sync();                              // all lanes done reading x2 before it is updated
-    if (lead) {
-      f[(size_t)row * nr + i] = fi;
-      if (a4) {
-        const double bj = cf[4 * s + 2], bjt = cf[4 * s + 3];
-        const double fe = x2[i];
-        x2[nr + i] = fma(bj, fi, fma(bjt, fe, x2[nr + i]));   // bf_e += bj f + bjt f_e
-        x2[i] = fe + fi;                                       // f_e += f (used from the next step on)
-      }
-    }
-    fprev = fi;
+    if (lead) f[(size_t)row * nr + i] = fi;
   }
   cp_async_wait<0>();
   if (CHUNK && chunk + 1 < a.nch && lead) {    // end state of the chunk from a zero start
-    if (a4) {
-      dout[i] = x2[i];
-      dout[nr + i] = x2[nr + i];
-    } else {
-      const double knext = coef[(size_t)(jj0 + 2 * nsteps) * 4];
-      dout[i] = fma(knext, fprev, x2[i]);
-    }
+    dout[i] = fe;
+    if (a4) dout[nr + i] = bfe;
   }
   if (sub) {  // Newton residual: f -= sub over the chunk's rows (the block's own writes are visible)
     __syncthreads();
@@ -198,12 +198,12 @@ __global__ void k_chain(ChainArgs a) {
 size_t chain_smem_bytes(int M, int nr, int ldl) {
   const size_t blk = (size_t)2 * nr * ldl;
   const size_t ns = (size_t)((M + 1) / 2);
-  return (3 * blk + ns * nr + 4 * ns + 2 * (size_t)nr) * sizeof(double);
+  return (3 * blk + ns * nr + 4 * (ns + 1) + 4 * (size_t)nr) * sizeof(double);
 }
 
 static size_t chunk_smem_bytes(int kc, int nr, int ldl) {
   const size_t blk = (size_t)2 * nr * ldl;
-  return (3 * blk + (size_t)kc * nr + 4 * (size_t)kc + 2 * (size_t)nr) * sizeof(double);
+  return (3 * blk + (size_t)kc * nr + 4 * ((size_t)kc + 1) + 4 * (size_t)nr) * sizeof(double);
 }
 
 // Carried states of the chunked chains: s_1 = d_0, s_{c+1} = Phi_c s_c + d_c (c = 1 .. nch-2), one CTA per
@@ -244,16 +244,17 @@ __global__ void k_chain_carry(ChainArgs a) {
     const double* cur_in = st + ((c - 1) & 1) * a.ldd;
     double* nxt = st + (c & 1) * a.ldd;
     const double* P = STAGE ? ring + ((c - 1) & 1) * blk : Phi + (size_t)c * blk;
+    cp_async_wait<0>();
+    __syncthreads();                                   // Phi_c landed, s_c visible, step c-1 done
     if (STAGE && c + 2 < nch) copy_block(ring + (c & 1) * blk, Phi + (size_t)(c + 1) * blk, (int)blk);
     cp_async_commit();
-    cp_async_wait<1>();
-    __syncthreads();                                   // Phi_c landed, s_c visible
     const double* dc = d + (size_t)c * a.ldd;
     double* cout = cb + (size_t)(c + 1) * a.ldd;
     for (int r0 = 0; r0 < m; r0 += rows_per_pass) {
       const int r = r0 + tid / TPR;
       const int rr = r < m ? r : 0;
       double acc = 0.0;
+#pragma unroll 8
       for (int col = q; col < m; col += TPR) acc = fma(P[(size_t)col * ldm + rr], cur_in[col], acc);
       acc = group_sum<TPR>(acc);
       if (r < m && q == 0) {
@@ -262,9 +263,27 @@ __global__ void k_chain_carry(ChainArgs a) {
         cout[r] = v;
       }
     }
-    __syncthreads();                                   // Phi_c and s_c are free for the next copy / step
   }
   cp_async_wait<0>();
+}
+
+// g of mode `row` for the fused right-hand side, element n (see ChainArgs::fuse_rhs): the roundings of
+// k_rhs, psi: (-dt (Dr Q - R)) + lin, T: (-dt NT) + lin, S: (-dt NS) + lin.
+__device__ __forceinline__ double fused_g(const ChainArgs& a, int b, int field, int row, int n) {
+  const int M = a.M, nr = a.nr;
+  const size_t N = (size_t)M * nr;
+  const double* o4 = a.out4 + (size_t)b * a.out_stride;
+  double nl;
+  if (field == 0) {
+    const double* qs = o4 + (size_t)row * nr;
+    const double* drn = a.Dr + (size_t)n * nr;
+    double dq = 0.0;
+    for (int c = 0; c < nr; ++c) dq = fma(drn[c], qs[c], dq);
+    nl = __dmul_rn(-a.dt, __dsub_rn(dq, o4[N + (size_t)row * nr + n]));
+  } else {
+    nl = __dmul_rn(-a.dt, o4[(size_t)(field + 1) * N + (size_t)row * nr + n]);
+  }
+  return __dadd_rn(nl, a.lin[(size_t)b * a.g_stride + (size_t)field * a.field_off + (size_t)row * nr + n]);
 }
 
 // Independent per-mode matvecs, one CTA of 128 threads per (field, mode, shell); matrix rows split over
@@ -296,6 +315,12 @@ __global__ void __launch_bounds__(128) k_mode_mv(ChainArgs a) {
     A = (a4 ? a.LinvA4 : (field == 1 ? a.LinvT : a.LinvS)) + (size_t)jj * nr * ldl;
     x = a.g + (size_t)b * a.g_stride + foff + (size_t)row * nr;
     y = a.h + (size_t)b * a.h_stride + foff + (size_t)row * nr;
+    if (a.fuse_rhs) {
+      __shared__ double gsm[kMaxNr];
+      for (int n = threadIdx.x; n < nr; n += blockDim.x) gsm[n] = fused_g(a, b, field, row, n);
+      __syncthreads();
+      x = gsm;
+    }
   }
   const int i = threadIdx.x / TPR, q = threadIdx.x % TPR;
   for (int r0 = 0; r0 < nr; r0 += 128 / TPR) {
@@ -303,7 +328,7 @@ __global__ void __launch_bounds__(128) k_mode_mv(ChainArgs a) {
     const int rr = r < nr ? r : 0;
     double acc = 0.0;
 #pragma unroll 8
-    for (int col = q; col < m; col += TPR) acc = fma(__ldg(A + (size_t)col * ldl + rr), __ldg(x + col), acc);
+    for (int col = q; col < m; col += TPR) acc = fma(__ldg(A + (size_t)col * ldl + rr), x[col], acc);
     acc = group_sum<TPR>(acc);
     if (r < nr && q == 0) {
       if (FIX) y[r] += acc;
@@ -342,11 +367,18 @@ __global__ void __launch_bounds__(128) k_mode_mv_warp(ChainArgs a, int nfields) 
     A = (a4 ? a.LinvA4 : (field == 1 ? a.LinvT : a.LinvS)) + (size_t)jj * nr * ldl;
     x = a.g + (size_t)b * a.g_stride + foff + (size_t)row * nr;
     y = a.h + (size_t)b * a.h_stride + foff + (size_t)row * nr;
+    if (a.fuse_rhs) {
+      __shared__ double gsm[4][kMaxNr];
+      double* gw = gsm[threadIdx.x >> 5];
+      for (int n = lane; n < nr; n += 32) gw[n] = fused_g(a, b, field, row, n);
+      __syncwarp();
+      x = gw;
+    }
   }
   for (int r = lane; r < nr; r += 32) {
     double acc = 0.0;
 #pragma unroll 8
-    for (int col = 0; col < m; ++col) acc = fma(__ldg(A + (size_t)col * ldl + r), __ldg(x + col), acc);
+    for (int col = 0; col < m; ++col) acc = fma(__ldg(A + (size_t)col * ldl + r), x[col], acc);
     if (FIX) y[r] += acc;
     else y[r] = acc;
   }

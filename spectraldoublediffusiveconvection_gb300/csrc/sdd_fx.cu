@@ -388,11 +388,55 @@ constexpr int kFxSplitThreads = 256;
 
 size_t fx_grid_smem_bytes(int M, int P, int prec) {
   const size_t es = prec == SDD_PREC_MIXED ? sizeof(float) : sizeof(double);
-  return (8 * (size_t)P + P + 2 + 9 * (size_t)M + 2 * kMaxNr + 32) * es + 2 * 32 * 8;
+  return (8 * (size_t)P + P + 2 + 9 * (size_t)M + 32) * es + 2 * 32 * 8;
 }
 size_t fx_prod_smem_bytes(int P, int prec) {
   const size_t es = prec == SDD_PREC_MIXED ? sizeof(float) : sizeof(double);
   return (8 * (size_t)P + 2 * (size_t)P + 32) * es + 2 * 32 * 8;
+}
+
+// Radial contractions of the split path (Derivatives, Matrix_Operators.py:698-729), one CTA per (mode,
+// shell): Dr psi_k, D2r2 psi_k, Dr T_k, Dr S_k for every radial row n, each a sequential fma chain over the
+// columns in the order of the fused kernel's (so both paths round identically).
+template <typename T>
+__global__ void __launch_bounds__(256) k_fx_deriv(FxArgs a, T* deriv, size_t deriv_stride) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int M = a.M, nr = a.nr;
+  const int k = blockIdx.x, b = blockIdx.y;
+  T* ops = reinterpret_cast<T*>(smem_raw);     // Dr, D2r2 (nr x nr each, row-major)
+  T* xv = ops + 2 * nr * nr;                  // psi_k, T_k, S_k
+  const T* Drg = reinterpret_cast<const T*>(a.ops.Dr);
+  const T* D2g = reinterpret_cast<const T*>(a.ops.D2r2);
+  for (int e = threadIdx.x; e < nr * nr; e += blockDim.x) {
+    ops[e] = Drg[e];
+    ops[nr * nr + e] = D2g[e];
+  }
+  const int N = M * nr;
+  const double* Xs = a.X + (size_t)b * a.x_stride + (size_t)k * nr;
+  for (int e = threadIdx.x; e < 3 * nr; e += blockDim.x) {
+    const int f = e / nr, m = e - f * nr;
+    xv[e] = (T)__ldg(Xs + (size_t)f * N + m);
+  }
+  __syncthreads();
+  T* D = deriv + (size_t)b * deriv_stride;
+  for (int e = threadIdx.x; e < 4 * nr; e += blockDim.x) {
+    const int op = e / nr, n = e - op * nr;
+    const T* row = ops + (op == 1 ? nr * nr : 0) + (size_t)n * nr;
+    const T* x = xv + (op < 2 ? 0 : (op - 1) * nr);
+    T acc = 0;
+    for (int m = 0; m < nr; ++m) acc = fma(row[m], x[m], acc);
+    D[((size_t)op * M + k) * nr + n] = acc;
+  }
+  if (a.fuse_rhs) {   // A2_SINE's D2 psi for the right-hand side (FP64; the order of k_rhs's dot)
+    const double* ps = a.X + (size_t)b * a.x_stride + (size_t)k * nr;
+    double* D5 = reinterpret_cast<double*>(D) + (size_t)4 * M * nr;
+    for (int n = threadIdx.x; n < nr; n += blockDim.x) {
+      const double* row = a.rl.D2s + (size_t)n * nr;
+      double acc = 0;
+      for (int m = 0; m < nr; ++m) acc = fma(row[m], __ldg(ps + m), acc);
+      D5[(size_t)k * nr + n] = acc;
+    }
+  }
 }
 
 template <typename T>
@@ -418,8 +462,7 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
   T* DCv = DTv + M;
   T* JP = DCv + M;
   T* Sc = JP + M;
-  T* opr = Sc + M;
-  T* scl = opr + 2 * kMaxNr;
+  T* scl = Sc + M;
   using U = typename Bits<T>::U;
   U* red = reinterpret_cast<U*>(scl + 32);
 
@@ -430,44 +473,29 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
     Et[i] = eg[i];
   }
   for (int i = tid; i < P + 2; i += bd) kf[i] = (T)i;
-  const T* Drg = reinterpret_cast<const T*>(a.ops.Dr);
-  const T* D2g = reinterpret_cast<const T*>(a.ops.D2r2);
-  for (int m = tid; m < nr; m += bd) {
-    opr[m] = Drg[n * nr + m];
-    opr[nr + m] = D2g[n * nr + m];
-  }
   const T ir4n = reinterpret_cast<const T*>(a.ops.ir4r2)[n];
   __syncthreads();
 
   // which row quantities the pair's two fields need (fields: 0 JT_psi, 1 komega, 2 kDpsi, 3 DT, 4 DC,
   // 5 omega, 6 Dpsi, 7 kT, 8 kC)
   const bool need_psi = pr == 0 || pr == 2;            // pv (JT_psi, omega's A2 term) and D2 psi (omega)
-  const bool need_dp = pr == 1 || pr == 3;             // Dr psi
-  const bool need_dt = pr == 1, need_dc = pr == 2;   // pairs 3 and 4 also use the T / S row values
   const int N = M * nr;
   const double* Xs = a.X + (size_t)b * a.x_stride;
+  const T* Dv = reinterpret_cast<const T*>(a.deriv) + (size_t)b * a.deriv_stride;   // k_fx_deriv
   for (int k = tid; k < M; k += bd) {
-    const double* ps = Xs + (size_t)k * nr;
-    const double* ts = Xs + N + (size_t)k * nr;
-    const double* ss = Xs + 2 * N + (size_t)k * nr;
     const bool psi_on = !(a.sym && (k % 2 == 0));
     const bool ts_on = !(a.sym && (k % 2 == 1));
     T dp = 0, d2 = 0, dtv = 0, dcv = 0, pn = 0, tn = 0, sn = 0;
-    if (psi_on && (need_psi || need_dp)) {
-      for (int m = 0; m < nr; ++m) {
-        const T x = (T)__ldg(ps + m);
-        if (need_dp) dp = fma(opr[m], x, dp);
-        if (need_psi) d2 = fma(opr[nr + m], x, d2);
-      }
-      pn = (T)__ldg(ps + n);
+    if (psi_on) {
+      dp = Dv[(size_t)k * nr + n];
+      d2 = Dv[((size_t)M + k) * nr + n];
+      pn = (T)__ldg(Xs + (size_t)k * nr + n);
     }
     if (ts_on) {
-      if (need_dt)
-        for (int m = 0; m < nr; ++m) dtv = fma(opr[m], (T)__ldg(ts + m), dtv);
-      if (need_dc)
-        for (int m = 0; m < nr; ++m) dcv = fma(opr[m], (T)__ldg(ss + m), dcv);
-      tn = (T)__ldg(ts + n);
-      sn = (T)__ldg(ss + n);
+      dtv = Dv[((size_t)2 * M + k) * nr + n];
+      dcv = Dv[((size_t)3 * M + k) * nr + n];
+      tn = (T)__ldg(Xs + N + (size_t)k * nr + n);
+      sn = (T)__ldg(Xs + 2 * N + (size_t)k * nr + n);
     }
     pv[k] = pn;
     Tv[k] = tn;
@@ -481,6 +509,31 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
   if (need_psi) {
     parity_suffix<T>(pv, Sc, M);
     __syncthreads();
+    if (sizeof(T) == 8 && pr == 0 && a.fuse_rhs) {
+      // the linear parts of the right-hand sides at row n (k_rhs's expressions, Main.py:262-280)
+      const RhsArgs& r = a.rl;
+      const double* D2p = reinterpret_cast<const double*>(Dv) + (size_t)4 * M * nr;
+      const double dt = r.dt, dtPr = r.dt * r.Pr;
+      const double Ra = r.Ra[b], Ras = r.Ra_s[b];
+      const double ir2 = r.ir2s[n], rsq = r.rsq[n], dT0 = r.dT0[n], gr = r.gr[n];
+      double* R = r.rhs + (size_t)b * r.rhs_stride;
+      for (int k = tid; k < M; k += bd) {
+        const double pk = (double)pv[k], pkm = k > 0 ? (double)pv[k - 1] : 0.0;
+        const double s1 = (k + 1 < M) ? (double)Sc[k + 1] : 0.0;
+        const double JPk = (k == 0) ? 1.0 * s1 : (k + 1.0) * pkm + 2.0 * s1;
+        const double s2 = (k + 2 < M) ? (double)Sc[k + 2] : 0.0;
+        const bool psi_on = !(a.sym && (k % 2 == 0));
+        const double d2s = psi_on ? D2p[(size_t)k * nr + n] : 0.0;
+        const double Om = d2s - (double)(k + 1) * ir2 * ((k + 2.0) * pk + 2.0 * s2);
+        const double grv = (k < M - 1) ? (-(double)(k + 1) * gr) * (Ra * (double)Tv[k + 1] - Ras * (double)Sv[k + 1])
+                                       : 0.0;
+        const double psiT0 = dT0 * JPk;
+        const size_t o = (size_t)k * nr + n;
+        R[o] = Om + dtPr * grv;
+        R[N + o] = rsq * (double)Tv[k] - dt * psiT0;
+        R[2 * N + o] = rsq * (double)Sv[k] - dt * psiT0;
+      }
+    }
     for (int k = tid; k < M; k += bd) jp_om<T>(k, M, kf, pv, Sc, ir4n, JP[k], OM[k]);
     __syncthreads();
   }
@@ -908,6 +961,10 @@ static cudaError_t launch_fx_split_t(const FxArgs& a, int batch, cudaStream_t s)
   T* grid = reinterpret_cast<T*>((MODE != 1 && a.base) ? a.base : a.grid);
   const size_t gs = (MODE != 1 && a.base) ? a.base_stride : a.grid_stride;
   cudaError_t e;
+  if (sizeof(T) != 8 && a.fuse_rhs) return cudaErrorInvalidValue;   // the fused rhs is FP64-only
+  k_fx_deriv<T><<<dim3(a.M, batch), 256, (2 * a.nr * a.nr + 3 * a.nr) * sizeof(T), s>>>(
+      a, reinterpret_cast<T*>(a.deriv), a.deriv_stride);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
   {
     static unsigned long long done = 0;
     if ((e = ensure_smem_attr(k_fx_grid<T>, &done)) != cudaSuccess) return e;
@@ -935,14 +992,14 @@ static int fx_sm_count() {
 // most SMs idle (nr * batch CTAs below half the SMs); it needs a grid scratch (or none: mode 2 and
 // cached mode 0 write the cache).  A batch that shares the GPU with other launches (the captured
 // multi-group graphs) is better served by the fused kernel; its autotuner sets the choice per plan.
-static bool use_split(const FxArgs& a, int batch, int mode) {
+bool fx_uses_split(const FxArgs& a, int batch, int mode) {
   const bool has_grid = (mode != 1 && a.base) || a.grid;
-  if (!has_grid || a.split == 1) return false;
+  if (!has_grid || !a.deriv || a.split == 1) return false;
   return a.split == 2 || 2 * a.nr * batch <= fx_sm_count();
 }
 
 cudaError_t launch_fx(const FxArgs& a, int batch, int mode, int prec, cudaStream_t s) {
-  if (use_split(a, batch, mode)) {
+  if (fx_uses_split(a, batch, mode)) {
     if (prec == SDD_PREC_MIXED) {
       if (mode == 0) return launch_fx_split_t<float, 0>(a, batch, s);
       if (mode == 1) return launch_fx_split_t<float, 1>(a, batch, s);

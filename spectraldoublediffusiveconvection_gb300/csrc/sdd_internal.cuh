@@ -63,6 +63,21 @@ struct FxOps {               // FP64 or FP32 copies of the operators the nonline
   const void* e;             // DCT twiddles (complex, P)
 };
 
+struct RhsArgs {
+  int M, nr, sym, linear;
+  double dt, Pr;
+  const double* Dr;          // nr*nr
+  const double* D2s;         // nr*nr (A2_SINE)
+  const double* ir2s, *rsq, *dT0, *gr;
+  const double* X;           // state (or perturbation) the linear terms act on
+  size_t x_stride;
+  const double* out4;        // FX spectral outputs (ignored when linear)
+  size_t out_stride;
+  const double* Ra, *Ra_s;   // per shell
+  double* rhs;               // [shell][3][M][nr]
+  size_t rhs_stride;
+};
+
 struct FxArgs {
   int M, nr, P, sym;
   StageArgs st;
@@ -78,22 +93,17 @@ struct FxArgs {
   void* grid;                // nullable: grid-field scratch [shell][nr][9][P] (T precision) of the split path
   size_t grid_stride;        // elements between shells in grid
   int split;                 // 0 auto, 1 fused row kernel, 2 split (needs grid or a cache)
+  void* deriv;               // split path: radial derivatives [shell][5][M][nr] (T): Dr psi, D2r2 psi, Dr T, Dr S
+                             // (and, with fuse_rhs, D2s psi in FP64 as the fifth block)
+  size_t deriv_stride;       // elements between shells in deriv
+  // fuse_rhs (FP64 split path): k_fx_grid writes the linear parts of the three right-hand sides into
+  // rl.rhs (the terms of k_rhs that do not involve the nonlinear term); the chains' h kernel adds the
+  // nonlinear parts from out4.  rl carries the operators, parameters and the rhs buffer.
+  int fuse_rhs;
+  RhsArgs rl;
 };
 
-struct RhsArgs {
-  int M, nr, sym, linear;
-  double dt, Pr;
-  const double* Dr;          // nr*nr
-  const double* D2s;         // nr*nr (A2_SINE)
-  const double* ir2s, *rsq, *dT0, *gr;
-  const double* X;           // state (or perturbation) the linear terms act on
-  size_t x_stride;
-  const double* out4;        // FX spectral outputs (ignored when linear)
-  size_t out_stride;
-  const double* Ra, *Ra_s;   // per shell
-  double* rhs;               // [shell][3][M][nr]
-  size_t rhs_stride;
-};
+
 
 struct ChainArgs {
   int M, nr, ldl, sym;
@@ -114,6 +124,14 @@ struct ChainArgs {
   const double* coefA4;      // [M][4] per jj: (dt bjt, dt bjt bj, bj, bjt), dt = Pr*dt, j = M - jj
   const double* coefT, *coefS;  // [M][4] per jj: (2 dt (j+2), 0.5 if j == 0 else 1, 0, 0), j = M-1-jj
   double dtA4, dtT, dtS;     // Pr*dt, dt, Tau*dt
+  // fuse_rhs: g is not read; the h kernel forms g from the linear parts in `lin` and the nonlinear-term
+  // outputs in out4 (psi: -dt (Dr Q - R) + lin; T, S: -dt N + lin), exactly as k_rhs would
+  int fuse_rhs;
+  const double* lin;         // [shell][3][M][nr] linear parts (k_fx_grid), stride g_stride
+  const double* out4;        // [shell][4][M][nr]
+  size_t out_stride;
+  const double* Dr;          // nr*nr (FP64)
+  double dt;                 // the step's dt
   // chunked (parallel-in-modes) chains, layout 2: every chain of S = N_fm/2 steps is cut into nch chunks
   // of kc steps.  Chunk c runs from a zero carried state (f_local, end state d_c); the carried states
   // s_c at the chunk starts follow s_{c+1} = Phi_c s_c + d_c; then f += G_jj s_c for the chunk's modes.
@@ -129,6 +147,8 @@ struct ChainArgs {
 
 // launchers (return cudaError_t of the launch)
 cudaError_t launch_fx(const FxArgs& a, int batch, int mode, int prec, cudaStream_t s);
+// whether launch_fx takes the split path for these arguments
+bool fx_uses_split(const FxArgs& a, int batch, int mode);
 cudaError_t launch_rhs(const RhsArgs& a, int batch, cudaStream_t s);
 cudaError_t launch_chain(const ChainArgs& a, int batch, int nfields, cudaStream_t s);
 cudaError_t launch_theta_op(int op, int M, int nr, int sym, const double* D2, const double* ir,
