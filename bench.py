@@ -239,7 +239,8 @@ def bench_batched(device, precision, steps=1000, steps_per_launch=10, n_shells=6
 SERVED_SHAPES = [(nr, m) for nr in (20, 28, 36, 48) for m in (64, 128, 256, 512)]
 
 
-def bench_served(device, n_requests=1000, rate=200.0, seed=2024, frac_continue=0.7, con_workers=4, branch=None):
+def bench_served(device, n_requests=1000, rate=200.0, seed=2024, frac_continue=0.7, con_workers=4, branch=None,
+                 **server_kw):
     import numpy as np
     import torch
     from spectraldoublediffusiveconvection_gb300 import serve
@@ -248,8 +249,8 @@ def bench_served(device, n_requests=1000, rate=200.0, seed=2024, frac_continue=0
         branch = serve.branch_states(SERVED_SHAPES, Ra=9000.0, d=2.0, Pr=1.0, Tau=1.0, Ra_s=500.0, device=device)
     t_branch = time.perf_counter() - t0
     shapes = [s for s in SERVED_SHAPES if s in branch]
-    srv = serve.Server(d=2.0, Pr=1.0, Tau=1.0, Ra_s=500.0, dt=1e-3, device=device, chain_layout=1,
-                       con_workers=con_workers).start()
+    srv = serve.Server(d=2.0, Pr=1.0, Tau=1.0, Ra_s=500.0, dt=1e-3, device=device, con_workers=con_workers,
+                       **server_kw).start()
     # warm-up: one request of each kind and shape builds the plans and workspaces
     warm = []
     for sh in shapes:
@@ -278,6 +279,9 @@ def bench_served(device, n_requests=1000, rate=200.0, seed=2024, frac_continue=0
             "errors": sum(r.error is not None for r in reqs),
             "batching": {k: srv.stats[k] - st0[k] for k in srv.stats},
             "shapes": [f"{a}x{b}" for a, b in shapes], "branch_seconds": t_branch,
+            "precision": {"integration": srv.int_precision + " (FP32 nonlinear term, FP64 implicit solves)",
+                          "continuation": "FP32 nonlinear term inside the Jacobian products, FP64 residual <= 1e-10"},
+            "chain_layout": srv.chain_layout, "tangent_rtol": srv.tangent_rtol, "con_workers": con_workers,
             "workload": "Poisson arrivals; 70% pseudo-arclength steps (ds=50, sign +-1) from steady states at "
                         "Ra_T=9000 on the Tau=1 branch, 30% 500-step integrations (dt=1e-3, Ra_T~U[8500,9500]) from "
                         "seeded states; N_r in {20,28,36,48}, N_theta in {64,128,256,512}; Ra_S=500, Pr=1, d=2"}

@@ -46,7 +46,7 @@ def test_served_results_equal_alone(cuda, branch):
     from spectraldoublediffusiveconvection_gb300 import serve
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     torch = cuda
-    srv = serve.Server(d=D, Pr=PR, Tau=TAU, Ra_s=RAS, dt=1e-3, quantum=50, chain_layout=1).start()
+    srv = serve.Server(d=D, Pr=PR, Tau=TAU, Ra_s=RAS, dt=1e-3, quantum=50).start()
     reqs = _requests(serve, branch)
     for r in reqs:
         srv.submit(r)
@@ -56,17 +56,18 @@ def test_served_results_equal_alone(cuda, branch):
     assert srv.used == 0
     for r in reqs:
         if r.kind == "integrate":
-            p = Plan(r.N_theta, r.N_r, D, 1e-3, PR, TAU)
-            p.set_chain_layout(1)
+            p = Plan(r.N_theta, r.N_r, D, 1e-3, PR, TAU, precision=srv.int_precision)
+            p.set_chain_layout(srv.chain_layout)
             X = torch.from_numpy(serve._seeded(r.N_theta, r.N_r - 1, r.seed)).cuda().reshape(1, -1)
             Y = p.step(X, r.Ra, RAS, nsteps=r.n_steps)
             assert np.array_equal(Y.cpu().numpy().ravel(), r.result["X"]), r.id
         else:
             p = Plan(r.N_theta, r.N_r, D, 1.0, PR, TAU, precision="mixed")
-            p.set_chain_layout(1)
+            p.set_chain_layout(srv.chain_layout)
             X = torch.from_numpy(np.asarray(r.X).copy()).cuda().reshape(1, -1)
             Ra = torch.tensor([r.Ra], dtype=torch.float64, device="cuda")
-            Xd, res = p.contin_step(X, Ra, RAS, r.sign, r.ds, tol=1e-10, restart=50, mixed_matvec=True)
+            Xd, res = p.contin_step(X, Ra, RAS, r.sign, r.ds, tol=1e-10, restart=50, mixed_matvec=True,
+                                    tangent_rtol=srv.tangent_rtol)
             assert res[0]["converged"] and r.result["converged"]
             assert np.array_equal(X.cpu().numpy().ravel(), r.result["X"]), r.id
             assert float(Ra.item()) == r.result["Ra"]
@@ -75,7 +76,7 @@ def test_served_results_equal_alone(cuda, branch):
 
 def test_served_continuation_steps_reach_fp64_residual(cuda, branch):
     from spectraldoublediffusiveconvection_gb300 import serve
-    srv = serve.Server(d=D, Pr=PR, Tau=TAU, Ra_s=RAS, chain_layout=1).start()
+    srv = serve.Server(d=D, Pr=PR, Tau=TAU, Ra_s=RAS).start()
     reqs = [srv.submit(serve.Request("continue", 16, 16, 9000.0, X=branch[(16, 16)][0], sign=s, ds=50.0))
             for s in (1.0, -1.0)]
     assert srv.drain(timeout=300)
@@ -94,7 +95,7 @@ def test_served_continuation_steps_reach_fp64_residual(cuda, branch):
 
 def test_poisson_workload_runs_to_completion(cuda, branch):
     from spectraldoublediffusiveconvection_gb300 import serve
-    srv = serve.Server(d=D, Pr=PR, Tau=TAU, Ra_s=RAS, chain_layout=1).start()
+    srv = serve.Server(d=D, Pr=PR, Tau=TAU, Ra_s=RAS).start()
     wl = serve.poisson_workload(24, 400.0, [(16, 16), (20, 32)], branch, n_steps=100, seed=5)
     wall = serve.run_workload(srv, wl)
     srv.stop()
