@@ -50,6 +50,37 @@ def algorithmic(M, nr):
     return step_flops, step_bytes, chain_flops, chain_bytes
 
 
+def kernel_algorithmic(name, M, nr, nch):
+    """Algorithmic FP64 flops and bytes of ONE launch of a step kernel for one shell (one IMEX step),
+    P = 3M/2 grid points, nch chunks per chain (chunked layout):
+      k_chain         the chain steps: flops 8 M nr^2 (psi [A B] 2nr x nr, T and S Linv nr x nr per mode),
+                      bytes 32 M nr^2 (those matrices) + 48 M nr (h in, f out)
+      k_chain_carry   (nch-2) carried matvecs per chain: flops 24 (nch-2) nr^2, bytes 96 (nch-2) nr^2
+      k_mode_mv(h)    h = Linv g: flops 6 M nr^2, bytes 24 M nr^2 + 48 M nr
+      k_mode_mv(fix)  f += G s: flops 8 M nr^2 (nch-1)/nch, bytes 32 M nr^2 (nch-1)/nch + 48 M nr
+      k_fx_deriv      4 radial contractions: flops 8 M nr^2, bytes 56 M nr
+      k_fx_grid       9 inverse transforms (2.5 P log2 P each): flops 22.5 nr P log2 P, bytes 56 M nr + 72 nr P
+      k_fx_prod       products + 3 forward transforms: flops 7.5 nr P log2 P + 11 nr P, bytes 72 nr P + 32 M nr
+      k_fx_rows       fused nonlinear term: flops 8 M nr^2 + 30 nr P log2 P + 11 nr P, bytes 56 M nr
+      k_rhs           flops 4 M nr^2 + 40 nr M, bytes 80 M nr"""
+    import math
+    P = 3 * M // 2
+    lg = math.log2(P)
+    f = (nch - 1) / nch if nch > 0 else 0.0
+    table = {
+        "k_chain": (8 * M * nr ** 2, 32 * M * nr ** 2 + 48 * M * nr),
+        "k_chain_carry": (24 * max(nch - 2, 0) * nr ** 2, 96 * max(nch - 2, 0) * nr ** 2),
+        "k_mode_mv(h)": (6 * M * nr ** 2, 24 * M * nr ** 2 + 48 * M * nr),
+        "k_mode_mv(fix)": (8 * M * nr ** 2 * f, 32 * M * nr ** 2 * f + 48 * M * nr),
+        "k_fx_deriv": (8 * M * nr ** 2, 56 * M * nr),
+        "k_fx_grid": (22.5 * nr * P * lg, 56 * M * nr + 72 * nr * P),
+        "k_fx_prod": (7.5 * nr * P * lg + 11 * nr * P, 72 * nr * P + 32 * M * nr),
+        "k_fx_rows": (8 * M * nr ** 2 + 30 * nr * P * lg + 11 * nr * P, 56 * M * nr),
+        "k_rhs": (4 * M * nr ** 2 + 40 * nr * M, 80 * M * nr),
+    }
+    return table[name]
+
+
 # ------------------------------------------------------------------------------------------------
 # clocks
 # ------------------------------------------------------------------------------------------------
@@ -373,12 +404,14 @@ def bench_gb300(args):
     e2e_value = time_steps / e2e_s
     nbytes = X0.size * 8
 
-    # ---- per-kernel durations (CUDA events between the three kernels of each step) -------------------
+    # ---- per-kernel durations: a CUDA event after every kernel launch of each step (launched one by one) --
     nprof = min(200, args.steps * chunk)
+    kp = plan.kernel_profile(X_after, Ra, Ras, nprof)
     ms3, _ = plan.step_profile(X_after, Ra, Ras, nprof)
     ms3 = [m / nprof for m in ms3]
-    names = ["k_fx_rows", "k_rhs", "k_chain"]
-    dom = int(np.argmax(ms3))
+    kavg = {k: v[0] / v[1] for k, v in kp.items()}                 # ms per launch
+    kstep = {k: v[0] / nprof for k, v in kp.items()}               # ms per step
+    dom = max(kstep, key=kstep.get)
     step_flops, step_bytes, chain_flops, chain_bytes = algorithmic(M, nr)
     fp64 = __import__("ctypes").c_double(0.0)
     _lib.check(_lib.lib().sdd_measure_fp64_peak(__import__("ctypes").byref(fp64),
@@ -394,25 +427,22 @@ def bench_gb300(args):
     traffic = None
     try:
         tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
-        traffic = tr.get(names[dom])
+        traffic = tr.get(dom)
     except (OSError, ValueError):
         pass
-    # dominant-kernel algorithmic work per launch (one launch of each kernel per IMEX step of the shell)
-    import math
-    P = 3 * M // 2
-    kflops = {"k_fx_rows": 8 * M * nr ** 2 + 12 * nr * 2.5 * P * math.log2(P) + 11 * nr * P,
-              "k_rhs": 4 * M * nr ** 2 + 40 * nr * M, "k_chain": chain_flops}[names[dom]]
-    kbytes = {"k_fx_rows": 56 * M * nr, "k_rhs": 80 * M * nr, "k_chain": chain_bytes}[names[dom]]
-    dom_s = ms3[dom] * 1e-3
+    kflops, kbytes = kernel_algorithmic(dom, M, nr, plan.chunks())
+    dom_s = kavg[dom] * 1e-3
     achieved_gbs = kbytes / dom_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved_gbs / hbm_peak, "traffic": traffic, "kernel": names[dom],
+                "frac": achieved_gbs / hbm_peak, "traffic": traffic, "kernel": dom,
                 "peak_source": hbm_src, "algorithmic_bytes_per_launch": kbytes,
+                "launch_ms": kavg[dom],
                 "fp64": {"achieved_gflops": kflops / dom_s / 1e9, "peak_gflops": fp64.value,
                          "frac": kflops / dom_s / 1e9 / fp64.value,
                          "peak_source": "measured live (sdd_measure_fp64_peak FMA loop)",
                          "algorithmic_flops_per_launch": kflops},
-                "kernel_ms_per_step": dict(zip(names, ms3)),
+                "kernel_ms_per_step": kstep,
+                "stage_ms_per_step": dict(zip(["nonlinear_term", "rhs", "implicit_solves"], ms3)),
                 "step_fp64_gflops": step_flops / (ms_total * 1e-3 / (args.steps * chunk)) / 1e9}
 
     # ---- Newton-GMRES(50) from the state after the time stepping --------------------------------------
@@ -483,7 +513,7 @@ def bench_gb300(args):
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                         "d2h_bytes_per_step": nbytes,
                         "api": "Plan.step on a pinned host state copied in/out every bench step"},
-                "gpu_launches": args.steps * chunk * 3,
+                "gpu_launches": args.steps * chunk * sum(v[1] for v in kp.values()) // nprof,
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": ck, "newton": newton, "batched": batched,
                 "served": served}
         print(json.dumps(line), flush=True)

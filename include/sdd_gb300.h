@@ -209,11 +209,29 @@ int sdd_contin_step(sdd_plan* plan, int batch, double* X, double* Ra, const doub
 int sdd_nlin_fx_noalloc(sdd_plan* plan, int batch, const double* X, double* F, void* stream);
 
 /* ---- instrumentation (no counterpart in the reference) ---------------------------------------- */
-/* Runs nsteps steps like sdd_step with CUDA events between the three kernels of each step and adds the
- * elapsed milliseconds to ms[0] (nonlinear-term row kernel), ms[1] (rhs kernel), ms[2] (chain kernel).
- * Synchronises the stream. */
+/* Runs nsteps steps like sdd_step (launched one by one, not from graphs) with CUDA events between the
+ * three stages of each step and adds the elapsed milliseconds to ms[0] (nonlinear term), ms[1]
+ * (right-hand sides; ~0 when fused into the other two) and ms[2] (implicit solves).  Synchronises the
+ * stream. */
 int sdd_step_profile(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, const double* X_in,
                      double* X_out, int nsteps, double* ms, void* stream);
+/* Kernel ids of sdd_step_kernel_profile and their names (sdd_kernel_name). */
+#define SDD_K_FX_ROWS 0      /* fused nonlinear-term row kernel */
+#define SDD_K_FX_DERIV 1     /* split path: radial derivatives per mode */
+#define SDD_K_FX_GRID 2      /* split path: paired inverse transforms to the grid */
+#define SDD_K_FX_PROD 3      /* split path: grid products and paired forward transforms */
+#define SDD_K_RHS 4          /* right-hand sides */
+#define SDD_K_MODE_H 5       /* h = Linv g per mode */
+#define SDD_K_CHAIN 6        /* the chains (whole, or the concurrent chunks) */
+#define SDD_K_CHAIN_CARRY 7  /* chunked chains: carried states */
+#define SDD_K_MODE_FIX 8     /* chunked chains: correction per mode */
+#define SDD_NUM_KERNELS 9
+const char* sdd_kernel_name(int id);
+/* Like sdd_step_profile, but with an event after every kernel launch: adds the elapsed milliseconds of
+ * each kernel to ms[id] and counts its launches in launches[id] (arrays of SDD_NUM_KERNELS). */
+int sdd_step_kernel_profile(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s,
+                            const double* X_in, double* X_out, int nsteps, double* ms, int* launches,
+                            void* stream);
 /* Measured FP64 FMA throughput of the current device in GFLOP/s (a register-resident FMA loop over
  * all SMs, a few milliseconds).  The roofline denominator of the FP64-bound kernels. */
 int sdd_measure_fp64_peak(double* gflops, void* stream);

@@ -96,6 +96,9 @@ SIGNATURES = [
                              ctypes.POINTER(ContinResult), _VP]),
     ("sdd_nlin_fx_noalloc", _I, [_VP, _I, _VP, _VP, _VP]),
     ("sdd_step_profile", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, ctypes.POINTER(ctypes.c_double), _VP]),
+    ("sdd_kernel_name", ctypes.c_char_p, [_I]),
+    ("sdd_step_kernel_profile", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(ctypes.c_int), _VP]),
     ("sdd_measure_fp64_peak", _I, [ctypes.POINTER(ctypes.c_double), _VP]),
 ]
 

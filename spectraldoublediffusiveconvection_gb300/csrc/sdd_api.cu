@@ -18,6 +18,7 @@ cudaError_t launch_fx_finish(int M, int nr, const double* Dr, const double* out4
                              double* F, size_t f_stride, int batch, cudaStream_t s);
 
 static thread_local int g_last_cuda = 0;
+thread_local KernelTimer* g_ktimer = nullptr;
 void set_cuda_error(cudaError_t e) { g_last_cuda = (int)e; }
 
 #define SDD_CUDA(call)                         \
@@ -1179,6 +1180,64 @@ extern "C" int sdd_step_profile(sdd_plan* p, int B, const double* Ra, const doub
     cur = dst;
   }
   for (auto& e : ev) cudaEventDestroy(e);
+  return rc;
+}
+
+extern "C" const char* sdd_kernel_name(int id) {
+  static const char* names[SDD_NUM_KERNELS] = {"k_fx_rows", "k_fx_deriv", "k_fx_grid", "k_fx_prod", "k_rhs",
+                                               "k_mode_mv(h)", "k_chain", "k_chain_carry", "k_mode_mv(fix)"};
+  return (id >= 0 && id < SDD_NUM_KERNELS) ? names[id] : "unknown";
+}
+
+extern "C" int sdd_step_kernel_profile(sdd_plan* p, int B, const double* Ra, const double* Ras, const double* X_in,
+                                       double* X_out, int nsteps, double* ms, int* launches, void* stream) {
+  int st = check_plan(p, B);
+  if (st) return st;
+  if (!Ra || !Ras || !X_in || !X_out || !ms || !launches || nsteps < 1 || X_in == X_out) return SDD_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  KernelTimer t;
+  t.n = 0;
+  cudaEvent_t start;
+  SDD_CUDA(cudaEventCreate(&start));
+  int made = 0;
+  cudaError_t e = cudaSuccess;
+  for (; made < KernelTimer::kMax && e == cudaSuccess; ++made) e = cudaEventCreate(&t.ev[made]);
+  if (e != cudaSuccess) --made;
+  const double* cur = X_in;
+  int rc = e == cudaSuccess ? SDD_OK : SDD_ERR_CUDA;
+  if (rc) set_cuda_error(e);
+  for (int it = 0; it < nsteps && rc == SDD_OK; ++it) {
+    double* dst = ((nsteps - it) % 2 == 1) ? X_out : p->xtmp;
+    t.n = 0;
+    if ((e = cudaEventRecord(start, s)) != cudaSuccess) {
+      set_cuda_error(e);
+      rc = SDD_ERR_CUDA;
+      break;
+    }
+    g_ktimer = &t;
+    const size_t n = shell_elems(p);
+    rc = apply_step_ld(p, B, Ra, Ras, cur, n, dst, n, nullptr, n, 0, nullptr, p->prec, s);
+    g_ktimer = nullptr;
+    if (rc != SDD_OK) break;
+    if (t.n > 0 && (e = cudaEventSynchronize(t.ev[t.n - 1])) != cudaSuccess) {
+      set_cuda_error(e);
+      rc = SDD_ERR_CUDA;
+      break;
+    }
+    cudaEvent_t prev = start;
+    for (int k = 0; k < t.n; ++k) {
+      float ms_k = 0.f;
+      if (cudaEventElapsedTime(&ms_k, prev, t.ev[k]) == cudaSuccess && t.id[k] >= 0 && t.id[k] < SDD_NUM_KERNELS) {
+        ms[t.id[k]] += ms_k;
+        launches[t.id[k]] += 1;
+      }
+      prev = t.ev[k];
+    }
+    cur = dst;
+  }
+  g_ktimer = nullptr;
+  for (int k = 0; k < made; ++k) cudaEventDestroy(t.ev[k]);
+  cudaEventDestroy(start);
   return rc;
 }
 

@@ -388,11 +388,13 @@ template <bool FIX>
 static cudaError_t launch_mode_mv(const ChainArgs& a, int batch, int nfields, cudaStream_t s, bool per_warp) {
   if (per_warp) {
     k_mode_mv_warp<FIX><<<dim3((nfields * a.M + 3) / 4, batch), 128, 0, s>>>(a, nfields);
+    ktimer_mark(FIX ? SDD_K_MODE_FIX : SDD_K_MODE_H, s);
     return cudaGetLastError();
   }
   const dim3 grid(nfields * a.M, batch);
   if (a.nr <= 32) k_mode_mv<4, FIX><<<grid, 128, 0, s>>>(a);
   else k_mode_mv<2, FIX><<<grid, 128, 0, s>>>(a);
+  ktimer_mark(FIX ? SDD_K_MODE_FIX : SDD_K_MODE_H, s);
   return cudaGetLastError();
 }
 
@@ -423,6 +425,7 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
     if ((e = ensure_smem_attr(k_chain<2, true>, &done)) != cudaSuccess) return e;
     k_chain<2, true><<<grid, 128, smem, s>>>(a);
   }
+  ktimer_mark(SDD_K_CHAIN, s);
   if ((e = cudaGetLastError()) != cudaSuccess || a.nch < 2) return e;
   // carried states: Phi of the psi chain (m = 2 nr) decides staging for all fields of the launch
   const int mmax = a.field0 == 0 ? 2 * a.nr : a.nr;
@@ -448,6 +451,7 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
       k_chain_carry<1, false><<<cg, 128, st, s>>>(a);
     }
   }
+  ktimer_mark(SDD_K_CHAIN_CARRY, s);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   return launch_mode_mv<true>(a, batch, nfields, s, false);
 }
@@ -494,6 +498,7 @@ cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStre
     if ((e = ensure_smem_attr(k_chain<1, false>, &done)) != cudaSuccess) return e;
     k_chain<1, false><<<grid, ((a.nr + 31) / 32) * 32, smem, s>>>(a);
   }
+  ktimer_mark(SDD_K_CHAIN, s);
   return cudaGetLastError();
 }
 

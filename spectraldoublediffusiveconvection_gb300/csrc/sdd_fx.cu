@@ -951,6 +951,7 @@ static cudaError_t launch_fx_t(const FxArgs& a, int batch, cudaStream_t s) {
   cudaError_t e = ensure_smem_attr(k_fx_rows<T, MODE>, &done);
   if (e != cudaSuccess) return e;
   k_fx_rows<T, MODE><<<dim3(a.nr, batch), kFxRowThreads, smem, s>>>(a);
+  ktimer_mark(SDD_K_FX_ROWS, s);
   return cudaGetLastError();
 }
 
@@ -964,17 +965,20 @@ static cudaError_t launch_fx_split_t(const FxArgs& a, int batch, cudaStream_t s)
   if (sizeof(T) != 8 && a.fuse_rhs) return cudaErrorInvalidValue;   // the fused rhs is FP64-only
   k_fx_deriv<T><<<dim3(a.M, batch), 256, (2 * a.nr * a.nr + 3 * a.nr) * sizeof(T), s>>>(
       a, reinterpret_cast<T*>(a.deriv), a.deriv_stride);
+  ktimer_mark(SDD_K_FX_DERIV, s);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   {
     static unsigned long long done = 0;
     if ((e = ensure_smem_attr(k_fx_grid<T>, &done)) != cudaSuccess) return e;
     k_fx_grid<T><<<dim3(a.nr, 5, batch), kFxSplitThreads, fx_grid_smem_bytes(a.M, a.P, prec), s>>>(a, grid, gs);
+    ktimer_mark(SDD_K_FX_GRID, s);
     if ((e = cudaGetLastError()) != cudaSuccess || MODE == 2) return e;
   }
   constexpr int PM = MODE == 1 ? 1 : 0;
   static unsigned long long done = 0;
   if ((e = ensure_smem_attr(k_fx_prod<T, PM>, &done)) != cudaSuccess) return e;
   k_fx_prod<T, PM><<<dim3(a.nr, 2, batch), kFxSplitThreads, fx_prod_smem_bytes(a.P, prec), s>>>(a, grid, gs);
+  ktimer_mark(SDD_K_FX_PROD, s);
   return cudaGetLastError();
 }
 
@@ -1025,6 +1029,7 @@ cudaError_t launch_rhs(const RhsArgs& a, int batch, cudaStream_t s) {
   cudaError_t e = ensure_smem_attr(k_rhs, &done);
   if (e != cudaSuccess) return e;
   k_rhs<<<dim3(a.nr, batch), kFxThreads, smem, s>>>(a);
+  ktimer_mark(SDD_K_RHS, s);
   return cudaGetLastError();
 }
 

@@ -17,6 +17,21 @@ constexpr int kFxRowThreads = 512;  // threads of the nonlinear-term row kernel
 
 void set_cuda_error(cudaError_t e);
 
+// Per-kernel timing for sdd_step_kernel_profile: while a KernelTimer is installed on the calling thread,
+// every launcher records an event after each launch, tagged with the kernel's id (SDD_K_* in the public
+// header).  Off (one thread-local load per launch) otherwise, and always off during graph capture.
+struct KernelTimer {
+  static constexpr int kMax = 64;
+  cudaEvent_t ev[kMax];
+  int id[kMax];
+  int n;
+};
+extern thread_local KernelTimer* g_ktimer;
+inline void ktimer_mark(int id, cudaStream_t s) {
+  KernelTimer* t = g_ktimer;
+  if (t && t->n < KernelTimer::kMax && cudaEventRecord(t->ev[t->n], s) == cudaSuccess) t->id[t->n++] = id;
+}
+
 // Raises a kernel's dynamic shared-memory limit to the device's opt-in maximum once per device, so
 // launches do not pay a cudaFuncSetAttribute call each.
 template <typename F>

@@ -212,6 +212,27 @@ class Plan:
                                             ms, _stream(self.device)), "sdd_step_profile")
         return list(ms), out
 
+    def chunks(self):
+        """Chunks per chain of the chunked layout: kc = clamp(round(sqrt(N_fm)), 4, 32) steps each."""
+        import math
+        S = self.N_fm // 2
+        kc = max(4, min(32, int(math.floor(math.sqrt(2.0 * S) + 0.5))))
+        return (S + kc - 1) // kc
+
+    def kernel_profile(self, X, Ra, Ra_s, nsteps):
+        """{kernel name: (total milliseconds, launches)} over nsteps steps from X, with a CUDA event after
+        every kernel launch (sdd_step_kernel_profile); kernels that did not run are left out."""
+        B = self._chk(X, self.n_state, "X")
+        ra, ras = self._vec(Ra, B), self._vec(Ra_s, B)
+        out = _torch().empty_like(X)
+        n = 9
+        ms = (ctypes.c_double * n)(*([0.0] * n))
+        cnt = (ctypes.c_int * n)(*([0] * n))
+        _lib.check(self._L.sdd_step_kernel_profile(self._h, B, _dptr(ra), _dptr(ras), _dptr(X), _dptr(out),
+                                                   int(nsteps), ms, cnt, _stream(self.device)),
+                   "sdd_step_kernel_profile")
+        return {self._L.sdd_kernel_name(k).decode(): (ms[k], cnt[k]) for k in range(n) if cnt[k] > 0}
+
     def newton(self, X, Ra, Ra_s, tol=1e-10, restart=50, gmres_rtol=1e-4, max_newton=20, max_restarts=20,
                mixed_matvec=False, raise_on_fail=False):
         """Newton-GMRES on F(X) = Phi_dt(X) - X in place on X (batch x n_state); returns per-shell dicts
