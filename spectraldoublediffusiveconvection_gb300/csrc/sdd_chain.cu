@@ -127,6 +127,11 @@ __global__ void k_chain(ChainArgs a) {
   cp_async_commit();
   if (nsteps > 1) copy_block(Lb0 + blk, Mat + (size_t)(jj0 + 2) * blk, blk);
   cp_async_commit();
+  for (int e = tid; e < 4 * (nsteps + 1); e += blockDim.x) {
+    const int jj = jj0 + 2 * (e >> 2);
+    cf[e] = jj < M ? coef[(size_t)jj * 4 + (e & 3)] : 0.0;
+  }
+  for (int c = tid; c < 4 * nr; c += blockDim.x) x2[c] = 0.0;
   {
     const double* h = a.g + (size_t)b * a.g_stride + foff;       // h_j = Linv_j g_j (k_mode_mv)
     for (int e = tid; e < nsteps * nr; e += blockDim.x) {
@@ -134,11 +139,6 @@ __global__ void k_chain(ChainArgs a) {
       hs[e] = h[(size_t)(M - 1 - (par + 2 * (s0 + s))) * nr + c];
     }
   }
-  for (int e = tid; e < 4 * (nsteps + 1); e += blockDim.x) {
-    const int jj = jj0 + 2 * (e >> 2);
-    cf[e] = jj < M ? coef[(size_t)jj * 4 + (e & 3)] : 0.0;
-  }
-  for (int c = tid; c < 4 * nr; c += blockDim.x) x2[c] = 0.0;
 
   // The lead lane of row i keeps the row's carried state in registers and publishes it to the other
   // buffer of x2 for the next step's matvec: one barrier per step.
@@ -207,9 +207,10 @@ static size_t chunk_smem_bytes(int kc, int nr, int ldl) {
 }
 
 // Carried states of the chunked chains: s_1 = d_0, s_{c+1} = Phi_c s_c + d_c (c = 1 .. nch-2), one CTA per
-// chain.  Rows of Phi split over TPR lanes; Phi_c streams into a 2-slot shared-memory ring when it fits
-// (STAGE), else it is read through L2.
-template <int TPR, bool STAGE>
+// chain.  Rows of Phi split over TPR lanes.  Phi_c streams into an R-slot shared-memory ring, R - 1 matrices
+// ahead of the one in use (R = 0: read through L2).  One barrier per step: the copy into the slot of
+// Phi_{c-1} is issued after the step-c barrier, when every thread is done with it.
+template <int TPR, int R>
 __global__ void k_chain_carry(ChainArgs a) {
   extern __shared__ __align__(16) double csm[];
   const int field = a.field0 + (blockIdx.x >> 1);
@@ -225,29 +226,37 @@ __global__ void k_chain_carry(ChainArgs a) {
   const size_t slot = (size_t)(field * 2 + par) * nch;
   const double* d = a.dbuf + (size_t)b * a.d_stride + slot * a.ldd;
   double* cb = a.cbuf + (size_t)b * a.d_stride + slot * a.ldd;
-  double* ring = csm;                                  // STAGE: 2 * blk
-  double* st = csm + (STAGE ? 2 * blk : 0);            // 2 x ldd state buffers
+  double* ring = csm;                                  // R * blk
+  double* st = csm + (size_t)R * blk;                  // 2 x ldd state buffers
   const int tid = threadIdx.x;
   const int q = tid % TPR;
   const int rows_per_pass = blockDim.x / TPR;
+  const int last = nch - 2;                            // Phi_1 .. Phi_last are used
+  constexpr int RR = R > 0 ? R : 1;
 
-  if (STAGE && nch > 2) {
-    copy_block(ring, Phi + 1 * blk, (int)blk);
+  if (R > 0) {
+#pragma unroll
+    for (int k = 1; k < RR; ++k) {                     // Phi_1 .. Phi_{R-1}
+      if (k <= last) copy_block(ring + (size_t)((k - 1) % RR) * blk, Phi + (size_t)k * blk, (int)blk);
+      cp_async_commit();
+    }
   }
-  cp_async_commit();
   for (int e = tid; e < m; e += blockDim.x) {
     const double v = d[e];                             // s_1 = d_0
     st[e] = v;
     cb[a.ldd + e] = v;
   }
-  for (int c = 1; c + 1 < nch; ++c) {
+  for (int c = 1; c <= last; ++c) {
     const double* cur_in = st + ((c - 1) & 1) * a.ldd;
     double* nxt = st + (c & 1) * a.ldd;
-    const double* P = STAGE ? ring + ((c - 1) & 1) * blk : Phi + (size_t)c * blk;
-    cp_async_wait<0>();
+    const double* P = R > 0 ? ring + (size_t)((c - 1) % RR) * blk : Phi + (size_t)c * blk;
+    if (R > 0) cp_async_wait<(R > 1 ? R - 2 : 0)>();
     __syncthreads();                                   // Phi_c landed, s_c visible, step c-1 done
-    if (STAGE && c + 2 < nch) copy_block(ring + (c & 1) * blk, Phi + (size_t)(c + 1) * blk, (int)blk);
-    cp_async_commit();
+    if (R > 0) {
+      const int k = c + R - 1;                         // into the slot of Phi_{c-1}
+      if (k <= last) copy_block(ring + (size_t)((k - 1) % RR) * blk, Phi + (size_t)k * blk, (int)blk);
+      cp_async_commit();
+    }
     const double* dc = d + (size_t)c * a.ldd;
     double* cout = cb + (size_t)(c + 1) * a.ldd;
     for (int r0 = 0; r0 < m; r0 += rows_per_pass) {
@@ -387,15 +396,16 @@ __global__ void __launch_bounds__(128) k_mode_mv_warp(ChainArgs a, int nfields) 
 template <bool FIX>
 static cudaError_t launch_mode_mv(const ChainArgs& a, int batch, int nfields, cudaStream_t s, bool per_warp) {
   if (per_warp) {
-    k_mode_mv_warp<FIX><<<dim3((nfields * a.M + 3) / 4, batch), 128, 0, s>>>(a, nfields);
+    const cudaError_t e = launch_kernel(k_mode_mv_warp<FIX>, dim3((nfields * a.M + 3) / 4, batch), dim3(128), 0, s, a,
+                                     nfields);
     ktimer_mark(FIX ? SDD_K_MODE_FIX : SDD_K_MODE_H, s);
-    return cudaGetLastError();
+    return e;
   }
   const dim3 grid(nfields * a.M, batch);
-  if (a.nr <= 32) k_mode_mv<4, FIX><<<grid, 128, 0, s>>>(a);
-  else k_mode_mv<2, FIX><<<grid, 128, 0, s>>>(a);
+  const cudaError_t e = a.nr <= 32 ? launch_kernel(k_mode_mv<4, FIX>, grid, dim3(128), 0, s, a)
+                                   : launch_kernel(k_mode_mv<2, FIX>, grid, dim3(128), 0, s, a);
   ktimer_mark(FIX ? SDD_K_MODE_FIX : SDD_K_MODE_H, s);
-  return cudaGetLastError();
+  return e;
 }
 
 static int sm_count() {
@@ -419,38 +429,38 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
   if (a.nr <= 32) {
     static unsigned long long done = 0;
     if ((e = ensure_smem_attr(k_chain<4, true>, &done)) != cudaSuccess) return e;
-    k_chain<4, true><<<grid, 128, smem, s>>>(a);
+    if ((e = launch_kernel(k_chain<4, true>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e;
   } else {
     static unsigned long long done = 0;
     if ((e = ensure_smem_attr(k_chain<2, true>, &done)) != cudaSuccess) return e;
-    k_chain<2, true><<<grid, 128, smem, s>>>(a);
+    if ((e = launch_kernel(k_chain<2, true>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e;
   }
   ktimer_mark(SDD_K_CHAIN, s);
   if ((e = cudaGetLastError()) != cudaSuccess || a.nch < 2) return e;
-  // carried states: Phi of the psi chain (m = 2 nr) decides staging for all fields of the launch
+  // carried states: Phi of the psi chain (m = 2 nr) decides the ring depth for all fields of the launch
   const int mmax = a.field0 == 0 ? 2 * a.nr : a.nr;
   const int ldmax = a.field0 == 0 ? a.ldmA : a.ldmT;
-  const size_t ring = 2 * (size_t)mmax * ldmax * sizeof(double);
+  const size_t blkb = (size_t)mmax * ldmax * sizeof(double);
   const size_t st = 2 * (size_t)a.ldd * sizeof(double);
-  const bool stage = ring + st <= 160 * 1024;
+  const int depth = (4 * blkb + st <= 200 * 1024) ? 4 : (2 * blkb + st <= 200 * 1024) ? 2 : 0;
+  const size_t smc = depth * blkb + st;
   const dim3 cg(2 * nfields, batch);
+#define SDD_CARRY(TPR_, R_)                                                         \
+  do {                                                                              \
+    static unsigned long long done = 0;                                             \
+    if ((e = ensure_smem_attr(k_chain_carry<TPR_, R_>, &done)) != cudaSuccess) return e; \
+    if ((e = launch_kernel(k_chain_carry<TPR_, R_>, cg, dim3(128), smc, s, a)) != cudaSuccess) return e; \
+  } while (0)
   if (mmax <= 64) {
-    if (stage) {
-      static unsigned long long done = 0;
-      if ((e = ensure_smem_attr(k_chain_carry<2, true>, &done)) != cudaSuccess) return e;
-      k_chain_carry<2, true><<<cg, 128, ring + st, s>>>(a);
-    } else {
-      k_chain_carry<2, false><<<cg, 128, st, s>>>(a);
-    }
+    if (depth == 4) SDD_CARRY(2, 4);
+    else if (depth == 2) SDD_CARRY(2, 2);
+    else SDD_CARRY(2, 0);
   } else {
-    if (stage) {
-      static unsigned long long done = 0;
-      if ((e = ensure_smem_attr(k_chain_carry<1, true>, &done)) != cudaSuccess) return e;
-      k_chain_carry<1, true><<<cg, 128, ring + st, s>>>(a);
-    } else {
-      k_chain_carry<1, false><<<cg, 128, st, s>>>(a);
-    }
+    if (depth == 4) SDD_CARRY(1, 4);
+    else if (depth == 2) SDD_CARRY(1, 2);
+    else SDD_CARRY(1, 0);
   }
+#undef SDD_CARRY
   ktimer_mark(SDD_K_CHAIN_CARRY, s);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   return launch_mode_mv<true>(a, batch, nfields, s, false);
@@ -488,15 +498,15 @@ cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStre
   if (split && a.nr <= 32) {
     static unsigned long long done = 0;
     if ((e = ensure_smem_attr(k_chain<4, false>, &done)) != cudaSuccess) return e;
-    k_chain<4, false><<<grid, 128, smem, s>>>(a);
+    if ((e = launch_kernel(k_chain<4, false>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e;
   } else if (split) {
     static unsigned long long done = 0;
     if ((e = ensure_smem_attr(k_chain<2, false>, &done)) != cudaSuccess) return e;
-    k_chain<2, false><<<grid, 128, smem, s>>>(a);
+    if ((e = launch_kernel(k_chain<2, false>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e;
   } else {
     static unsigned long long done = 0;
     if ((e = ensure_smem_attr(k_chain<1, false>, &done)) != cudaSuccess) return e;
-    k_chain<1, false><<<grid, ((a.nr + 31) / 32) * 32, smem, s>>>(a);
+    if ((e = launch_kernel(k_chain<1, false>, grid, dim3(((a.nr + 31) / 32) * 32), smem, s, a)) != cudaSuccess) return e;
   }
   ktimer_mark(SDD_K_CHAIN, s);
   return cudaGetLastError();

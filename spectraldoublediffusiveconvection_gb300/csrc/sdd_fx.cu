@@ -207,7 +207,6 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
   T* DCv = DTv + M;
   T* JP = DCv + M;
   T* Sc = JP + M;
-
   const C* wg = reinterpret_cast<const C*>(a.ops.w);
   const C* eg = reinterpret_cast<const C*>(a.ops.e);
   for (int i = tid; i < P; i += bd) {
@@ -419,22 +418,21 @@ __global__ void __launch_bounds__(256) k_fx_deriv(FxArgs a, T* deriv, size_t der
   }
   __syncthreads();
   T* D = deriv + (size_t)b * deriv_stride;
-  for (int e = threadIdx.x; e < 4 * nr; e += blockDim.x) {
+  const int nops = a.fuse_rhs ? 5 : 4;
+  for (int e = threadIdx.x; e < nops * nr; e += blockDim.x) {
     const int op = e / nr, n = e - op * nr;
-    const T* row = ops + (op == 1 ? nr * nr : 0) + (size_t)n * nr;
-    const T* x = xv + (op < 2 ? 0 : (op - 1) * nr);
-    T acc = 0;
-    for (int m = 0; m < nr; ++m) acc = fma(row[m], x[m], acc);
-    D[((size_t)op * M + k) * nr + n] = acc;
-  }
-  if (a.fuse_rhs) {   // A2_SINE's D2 psi for the right-hand side (FP64; the order of k_rhs's dot)
-    const double* ps = a.X + (size_t)b * a.x_stride + (size_t)k * nr;
-    double* D5 = reinterpret_cast<double*>(D) + (size_t)4 * M * nr;
-    for (int n = threadIdx.x; n < nr; n += blockDim.x) {
+    if (op < 4) {
+      const T* row = ops + (op == 1 ? nr * nr : 0) + (size_t)n * nr;
+      const T* x = xv + (op < 2 ? 0 : (op - 1) * nr);
+      T acc = 0;
+      for (int m = 0; m < nr; ++m) acc = fma(row[m], x[m], acc);
+      D[((size_t)op * M + k) * nr + n] = acc;
+    } else {   // A2_SINE's D2 psi for the fused right-hand side (FP64; the order of k_rhs's dot)
+      const double* ps = a.X + (size_t)b * a.x_stride + (size_t)k * nr;
       const double* row = a.rl.D2s + (size_t)n * nr;
       double acc = 0;
-      for (int m = 0; m < nr; ++m) acc = fma(row[m], __ldg(ps + m), acc);
-      D5[(size_t)k * nr + n] = acc;
+      for (int m = 0; m < nr; ++m) acc = fma(__ldg(row + m), __ldg(ps + m), acc);
+      reinterpret_cast<double*>(D)[(size_t)4 * M * nr + (size_t)k * nr + n] = acc;
     }
   }
 }
@@ -465,7 +463,6 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
   T* scl = Sc + M;
   using U = typename Bits<T>::U;
   U* red = reinterpret_cast<U*>(scl + 32);
-
   const C* wg = reinterpret_cast<const C*>(a.ops.w);
   const C* eg = reinterpret_cast<const C*>(a.ops.e);
   for (int i = tid; i < P; i += bd) {
@@ -950,9 +947,9 @@ static cudaError_t launch_fx_t(const FxArgs& a, int batch, cudaStream_t s) {
   static unsigned long long done = 0;
   cudaError_t e = ensure_smem_attr(k_fx_rows<T, MODE>, &done);
   if (e != cudaSuccess) return e;
-  k_fx_rows<T, MODE><<<dim3(a.nr, batch), kFxRowThreads, smem, s>>>(a);
+  e = launch_kernel(k_fx_rows<T, MODE>, dim3(a.nr, batch), dim3(kFxRowThreads), smem, s, a);
   ktimer_mark(SDD_K_FX_ROWS, s);
-  return cudaGetLastError();
+  return e;
 }
 
 template <typename T, int MODE>
@@ -963,23 +960,25 @@ static cudaError_t launch_fx_split_t(const FxArgs& a, int batch, cudaStream_t s)
   const size_t gs = (MODE != 1 && a.base) ? a.base_stride : a.grid_stride;
   cudaError_t e;
   if (sizeof(T) != 8 && a.fuse_rhs) return cudaErrorInvalidValue;   // the fused rhs is FP64-only
-  k_fx_deriv<T><<<dim3(a.M, batch), 256, (2 * a.nr * a.nr + 3 * a.nr) * sizeof(T), s>>>(
-      a, reinterpret_cast<T*>(a.deriv), a.deriv_stride);
+  e = launch_kernel(k_fx_deriv<T>, dim3(a.M, batch), dim3(256), (2 * a.nr * a.nr + 3 * a.nr) * sizeof(T), s, a,
+                 reinterpret_cast<T*>(a.deriv), a.deriv_stride);
   ktimer_mark(SDD_K_FX_DERIV, s);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (e != cudaSuccess) return e;
   {
     static unsigned long long done = 0;
     if ((e = ensure_smem_attr(k_fx_grid<T>, &done)) != cudaSuccess) return e;
-    k_fx_grid<T><<<dim3(a.nr, 5, batch), kFxSplitThreads, fx_grid_smem_bytes(a.M, a.P, prec), s>>>(a, grid, gs);
+    e = launch_kernel(k_fx_grid<T>, dim3(a.nr, 5, batch), dim3(kFxSplitThreads), fx_grid_smem_bytes(a.M, a.P, prec),
+                   s, a, grid, gs);
     ktimer_mark(SDD_K_FX_GRID, s);
-    if ((e = cudaGetLastError()) != cudaSuccess || MODE == 2) return e;
+    if (e != cudaSuccess || MODE == 2) return e;
   }
   constexpr int PM = MODE == 1 ? 1 : 0;
   static unsigned long long done = 0;
   if ((e = ensure_smem_attr(k_fx_prod<T, PM>, &done)) != cudaSuccess) return e;
-  k_fx_prod<T, PM><<<dim3(a.nr, 2, batch), kFxSplitThreads, fx_prod_smem_bytes(a.P, prec), s>>>(a, grid, gs);
+  e = launch_kernel(k_fx_prod<T, PM>, dim3(a.nr, 2, batch), dim3(kFxSplitThreads), fx_prod_smem_bytes(a.P, prec), s,
+                 a, (const T*)grid, gs);
   ktimer_mark(SDD_K_FX_PROD, s);
-  return cudaGetLastError();
+  return e;
 }
 
 static int fx_sm_count() {
@@ -1028,8 +1027,9 @@ cudaError_t launch_rhs(const RhsArgs& a, int batch, cudaStream_t s) {
   static unsigned long long done = 0;
   cudaError_t e = ensure_smem_attr(k_rhs, &done);
   if (e != cudaSuccess) return e;
-  k_rhs<<<dim3(a.nr, batch), kFxThreads, smem, s>>>(a);
+  const cudaError_t er = launch_kernel(k_rhs, dim3(a.nr, batch), dim3(kFxThreads), smem, s, a);
   ktimer_mark(SDD_K_RHS, s);
+  if (er != cudaSuccess) return er;
   return cudaGetLastError();
 }
 
