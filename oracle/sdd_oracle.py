@@ -655,3 +655,18 @@ def seeded_state(N_fm, nr, seed, symmetric=False):
     amp = 1e-3 * np.exp(-k / 8.0) * np.exp(-n / 4.0)
     P, T, S = [rng.standard_normal((nr, N_fm)) * amp for _ in range(3)]
     return Vecs_to_X(P, T, S, N_fm, nr, symmetric)
+
+
+def Full_Eig_Vec(f, l, N_fm, nr, symmetric=False):
+    """Linear_Problem.py:295-317: radial profiles f = [psi; T; S] times -sin(theta) C^{3/2}_{l-1}(cos theta)
+    (psi) and P_l(cos theta) (T, S), transformed (DST/DCT with n = N_fm; psi shifted to the code's sine
+    convention) and laid out by Vecs_to_X."""
+    from scipy.special import eval_gegenbauer, eval_legendre
+    th = grid(N_fm)
+    Gl_hat = np.array(DST(-np.sin(th) * eval_gegenbauer(l - 1, 1.5, np.cos(th)), n=N_fm), dtype=float)
+    Pl_hat = np.array(DCT(eval_legendre(l, np.cos(th)), n=N_fm), dtype=float)
+    Gl_hat[:-1] = Gl_hat[1:].copy()
+    Gl_hat[-1] = 0.0
+    f = np.asarray(f, dtype=float).reshape(-1)
+    return Vecs_to_X(np.outer(f[:nr], Gl_hat), np.outer(f[nr:2 * nr], Pl_hat), np.outer(f[2 * nr:3 * nr], Pl_hat),
+                     N_fm, nr, symmetric)

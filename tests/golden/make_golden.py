@@ -53,6 +53,7 @@ def _install_shims():
 
     mpl = types.ModuleType("matplotlib")
     plt = types.ModuleType("matplotlib.pyplot")
+    plt.rcParams = {}                  # Linear_Problem.py:5 updates it at import
     mpl.pyplot = plt
     sys.modules["matplotlib"] = mpl
     sys.modules["matplotlib.pyplot"] = plt
@@ -232,6 +233,39 @@ def interp_case():
     print("wrote interp")
 
 
+def eigen_case():
+    """Linear_Problem.py:16-85 and 295-317: eigenvalues and eigenvectors of the single-mode linear
+    problem (Linear_Matrix_Operators.py ML_0 / Ll_0), and the full-state vector built from one."""
+    import Linear_Matrix_Operators as LMO
+    # Linear_Problem.py does not parse as Python: an IPython "%matplotlib inline" line sits inside a
+    # function (Linear_Problem.py:594).  Compile it in memory with that line replaced by "pass" (the file
+    # itself is not touched); nothing on the path of the functions recorded here changes.
+    src_path = os.path.join(REF_DIR, "Linear_Problem.py")
+    lines = open(src_path).read().split("\n")
+    lines = [ln[:len(ln) - len(ln.lstrip())] + "pass" if ln.lstrip().startswith("%") else ln for ln in lines]
+    LP = types.ModuleType("Linear_Problem")
+    LP.__file__ = src_path
+    exec(compile("\n".join(lines), src_path, "exec"), LP.__dict__)
+    out = {}
+    for tag, (Ra, l, d, Ra_s, Pr, Tau, Nr) in {"a": (9000.0, 2.0, 2.0, 500.0, 1.0, 1.0, 20),
+                                               "b": (4525.9, 13.0, 0.31325, 150.0, 1.0, 1.0 / 15.0, 16)}.items():
+        D, R = LMO.cheb_radial(Nr, d)
+        out[f"D_{tag}"], out[f"R_{tag}"] = D, R
+        out[f"ML0_{tag}"] = np.asarray(LMO.ML_0(D, R, l))
+        out[f"Ll0_{tag}"] = np.asarray(LMO.Ll_0(D, R, d, l, Ra, Ra_s, Pr, Tau))
+        out[f"vals_{tag}"] = LP.Eig_Vals(Ra, l, d, 5, Ra_s=Ra_s, Pr=Pr, Tau=Tau, Nr=Nr)
+        out[f"val1_{tag}"] = LP.Eig_Vals(Ra, l, d, 1, Ra_s=Ra_s, Pr=Pr, Tau=Tau, Nr=Nr)
+        for k in (0, 1):
+            out[f"vec{k}_{tag}"] = LP.Eig_Vec(Ra, l, d, k, Ra_s=Ra_s, Pr=Pr, Tau=Tau, Nr=Nr)
+        out[f"params_{tag}"] = np.array([Ra, l, d, Ra_s, Pr, Tau, Nr])
+    f = out["vec0_a"]
+    for N_fm in (16, 32):
+        out[f"full_{N_fm}"] = LP.Full_Eig_Vec(f, 2.0, N_fm, 19, symmetric=False)
+    out["full_sym_16"] = LP.Full_Eig_Vec(f, 2.0, 16, 19, symmetric=True)
+    np.savez(os.path.join(HERE, "eigen.npz"), **out)
+    print("wrote eigen")
+
+
 def transform_case():
     """Transforms.py:73-129 on seeded rows, with and without the 3/2 zero-padding length n."""
     rng = np.random.default_rng(7)
@@ -256,6 +290,9 @@ def transform_case():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) > 2 and sys.argv[2] == "--only-eigen":
+        eigen_case()
+        sys.exit(0)
     if len(sys.argv) > 2 and sys.argv[2] == "--only-interp":
         interp_case()
         sys.exit(0)

@@ -203,3 +203,13 @@ def test_interpolation_dropins_match_reference(cuda):
     assert rel(MO.INTERP_RADIAL(8, 12, X, 2.0), Z["rad_down"]) < 2e-5
     assert rel(MO.INTERP_THETAS(32, 16, X), Z["th_up"]) < 1e-13
     assert rel(MO.INTERP_THETAS(8, 16, X), Z["th_down"]) < 1e-13
+
+
+def test_full_eig_vec_dropin_matches_reference(cuda):
+    """Linear_Problem.py:295-317 through the GPU transforms."""
+    from spectraldoublediffusiveconvection_gb300 import Linear_Problem as LP
+    Z = load_golden("eigen.npz")
+    f = Z["vec0_a"]
+    for N_fm in (16, 32):
+        assert rel(LP.Full_Eig_Vec(f, 2.0, N_fm, 19), Z[f"full_{N_fm}"]) < 1e-13
+    assert rel(LP.Full_Eig_Vec(f, 2.0, 16, 19, symmetric=True), Z["full_sym_16"]) < 1e-13

@@ -91,3 +91,30 @@ def test_package_seeded_state_matches_oracle():
     from spectraldoublediffusiveconvection_gb300.seeds import seeded_state
     for (M, nr, seed, sym) in [(64, 19, 1234, False), (16, 11, 7, True), (256, 29, 1, False)]:
         assert np.array_equal(seeded_state(M, nr, seed, sym), O.seeded_state(M, nr, seed, sym))
+
+
+def test_linear_problem_matches_reference():
+    """Linear_Matrix_Operators.py ML_0/Ll_0 and Linear_Problem.py Eig_Vals/Eig_Vec (host dense eigenproblem,
+    the library's own host code) and the oracle's Full_Eig_Vec against the reference's outputs.  The
+    eigenvectors are LAPACK's up to sign; M^-1 L is formed by a solve instead of an inverse (1e-13)."""
+    import numpy as np
+    from spectraldoublediffusiveconvection_gb300 import Linear_Matrix_Operators as LMO
+    from spectraldoublediffusiveconvection_gb300 import Linear_Problem as LP
+    Z = load_golden("eigen.npz")
+    for tag in ("a", "b"):
+        Ra, l, d, Ras, Pr, Tau, Nr = Z[f"params_{tag}"]
+        Nr = int(Nr)
+        D, R = LMO.cheb_radial(Nr, d)
+        assert rel(D, Z[f"D_{tag}"]) < 1e-14 and rel(R, Z[f"R_{tag}"]) < 1e-15
+        assert rel(LMO.ML_0(D, R, l), Z[f"ML0_{tag}"]) < 1e-14
+        assert rel(LMO.Ll_0(D, R, d, l, Ra, Ras, Pr, Tau), Z[f"Ll0_{tag}"]) < 1e-14
+        vals, ref = LP.Eig_Vals(Ra, l, d, 5, Ras, Pr, Tau, Nr), Z[f"vals_{tag}"]     # complex
+        assert np.abs(vals - ref).max() < 1e-11 * np.abs(ref).max()
+        assert abs(LP.Eig_Vals(Ra, l, d, 1, Ras, Pr, Tau, Nr) - Z[f"val1_{tag}"]) < 1e-10 * (1 + abs(Z[f"val1_{tag}"]))
+        for k in (0, 1):
+            e, g = LP.Eig_Vec(Ra, l, d, k, Ras, Pr, Tau, Nr).ravel(), Z[f"vec{k}_{tag}"].ravel()
+            assert rel(np.sign(e @ g) * e, g) < 1e-10
+    f = Z["vec0_a"]
+    for N_fm in (16, 32):
+        assert rel(O.Full_Eig_Vec(f, 2.0, N_fm, 19), Z[f"full_{N_fm}"]) < 1e-13
+    assert rel(O.Full_Eig_Vec(f, 2.0, 16, 19, symmetric=True), Z["full_sym_16"]) < 1e-13
