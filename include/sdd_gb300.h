@@ -80,6 +80,11 @@ typedef struct sdd_plan_desc {
   const double* Linv_A4;   /* N_fm*nr*nr  A4_TSTEP_MATS(Pr*dt)            (Matrix_Operators.py:1089)*/
   const double* Linv_T;    /* N_fm*nr*nr  NAB2_TSTEP_MATS(dt)             (Matrix_Operators.py:1014)*/
   const double* Linv_S;    /* N_fm*nr*nr  NAB2_TSTEP_MATS(Tau*dt)                                  */
+  /* diagnostics (sdd_diagnostics / sdd_step_diag); nullable: without them those entry points return
+   * SDD_ERR_UNSUPPORTED                                                                             */
+  const double* nu_w;      /* nr     (R[0]^2/A_T) D[0][1..nr]: Nusselt weights (Main.py:41-68)         */
+  const double* r_int;     /* nr     interior radii R[1:-1] (Kinetic_Energy trapezoid, Main.py:124-131) */
+  double r_i, r_o;         /* R[0], R[-1] (Kinetic_Energy volume, Main.py:132)                      */
 } sdd_plan_desc;
 
 typedef struct sdd_plan sdd_plan;
@@ -215,6 +220,14 @@ int sdd_nlin_fx_noalloc(sdd_plan* plan, int batch, const double* X, double* F, v
  * stream. */
 int sdd_step_profile(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, const double* X_in,
                      double* X_out, int nsteps, double* ms, void* stream);
+/* Per-shell diagnostics of the state X (device, batch x 3*N_fm*nr) into out (device, batch x 4):
+ * |X|_2, Kinetic_Energy (Main.py:71-134), Nusselt of T and of S (Main.py:41-68, without the check).
+ * Replaces the per-step scalar records of _Time_Step (Main.py:285-296). */
+int sdd_diagnostics(sdd_plan* plan, int batch, const double* X, double* out, void* stream);
+/* nsteps steps like sdd_step (launched one by one), with the diagnostics of the state after every step
+ * written to diag (device, nsteps x batch x 4). */
+int sdd_step_diag(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, const double* X_in,
+                  double* X_out, int nsteps, int linear, double* diag, void* stream);
 /* Kernel ids of sdd_step_kernel_profile and their names (sdd_kernel_name). */
 #define SDD_K_FX_ROWS 0      /* fused nonlinear-term row kernel */
 #define SDD_K_FX_DERIV 1     /* split path: radial derivatives per mode */

@@ -109,41 +109,45 @@ def _to_state(X, plan):
     return torch.from_numpy(np.ascontiguousarray(X, dtype=np.float64)).to(plan.device).reshape(1, -1), True
 
 
-def _diagnostics(Xh, R, D, N_fm, nr, d, symmetric):
-    N = N_fm * nr
-    return (np.linalg.norm(Xh, 2), Kinetic_Energy(Xh, R, D, N_fm, nr, symmetric),
-            Nusselt(Xh[N:2 * N], d, R, D, N_fm, nr, check=False),
-            Nusselt(Xh[2 * N:3 * N], d, R, D, N_fm, nr, check=False))
+def _diagnostics(plan, Xd):
+    """|X|_2, Kinetic_Energy, Nusselt(T), Nusselt(S) of a device state (Main.py:41-134, on the device)."""
+    return tuple(float(v) for v in plan.diagnostics(Xd.reshape(1, -1))[0].tolist())
 
 
 def _Time_Step(X, Ra, Ra_s, Tau, Pr, d, N_fm, N_r, symmetric, save_filename='TimeStep_0.h5', start_time=0,
                Total_time=1, dt=1e-04, linear=False, Verbose=False):
-    """Main.py:228-329: int(Total_time/dt) IMEX ("CNAB1") steps on the GPU; returns X_new."""
+    """Main.py:228-329: int(Total_time/dt) IMEX ("CNAB1") steps on the GPU; returns X_new.  As the
+    reference, it records |X|_2, KE, Nu_T and Nu_S after every step (computed on the device,
+    sdd_step_diag) and the state at every N_iters/10-th step, and writes them to save_filename when h5py
+    is available (the file holds the series up to the last save point, as the reference's last write)."""
     plan = get_plan(N_fm, N_r, d, dt, Pr, Tau, symmetric)
     Xd, was_np = _to_state(X, plan)
     N_iters = int(Total_time / dt)
     N_save = max(1, int(N_iters / 10))
-    D, R = plan.arrays["D"], plan.arrays["R"]
-    nr = N_r - 1
     rec = dict(X_DATA=[], Norm=[], KE=[], Nu_T=[], Nu_S=[], Time=[])
+    diags = []
     t0 = time.time()
     done = 0
+    last_save = -1
     while done < N_iters:
         # the reference saves after iterations 0, N_save, 2 N_save, ...  (Main.py:301)
         nxt = 1 if done == 0 else min(N_iters, done + N_save)
-        Xd = plan.step(Xd, Ra, Ra_s, nsteps=nxt - done, linear=linear)
+        Xd, dg = plan.step_diag(Xd, Ra, Ra_s, nsteps=nxt - done, linear=linear)
+        diags.append(dg[:, 0, :])
         done = nxt
         if (done - 1) % N_save == 0:
-            Xh = Xd.cpu().numpy().ravel()
-            nrm, ke, nut, nus = _diagnostics(Xh, R, D, N_fm, nr, d, symmetric)
-            rec["X_DATA"].append(Xh)
-            rec["Norm"].append(nrm)
-            rec["KE"].append(ke)
-            rec["Nu_T"].append(nut)
-            rec["Nu_S"].append(nus)
-            rec["Time"].append(start_time + dt * (done - 1))
+            rec["X_DATA"].append(Xd.cpu().numpy().ravel())
+            last_save = done - 1
             if Verbose:
-                print("Iteration =%i, Time = %e, Energy = %e, NuT = %e \n " % (done - 1, rec["Time"][-1], ke, nut))
+                ke, nut = dg[-1, 0, 1].item(), dg[-1, 0, 2].item()
+                print("Iteration =%i, Time = %e, Energy = %e, NuT = %e \n " % (done - 1, start_time + dt * (done - 1),
+                                                                              ke, nut))
+    import torch
+    series = torch.cat(diags).cpu().numpy() if diags else np.zeros((0, 4))
+    n_rec = last_save + 1
+    rec["Norm"], rec["KE"], rec["Nu_T"], rec["Nu_S"] = (series[:n_rec, q].copy() for q in range(4))
+    rec["Time"] = start_time + dt * np.arange(n_rec)
+    _Time_Step.last_record = dict(rec, series=series)
     if save_filename:
         _write_h5(save_filename, rec, dict(Ra=Ra, Ra_s=Ra_s, Tau=Tau, Pr=Pr, d=d, N_r=N_r, N_fm=N_fm, dt=dt,
                                            start_time=start_time, symmetric=symmetric))
@@ -183,7 +187,7 @@ def _Newton(X, Ra, Ra_s, Tau, Pr, d, N_fm, N_r, symmetric, dt=1, tol_newton=1e-0
         print('Newton iteration could not converge')
         return None, None, None, None, None, False
     Xh = Xd.cpu().numpy().ravel()
-    Norm, KE, NuT, NuS = _diagnostics(Xh, plan.arrays["R"], plan.arrays["D"], N_fm, N_r - 1, d, symmetric)
+    Norm, KE, NuT, NuS = _diagnostics(plan, Xd)
     return (Xh if was_np else Xd.reshape(-1)), Norm, KE, NuT, NuS, True
 
 
@@ -247,7 +251,7 @@ def _ContinC(Y_0_dot, Y_0, sign, ds, Ra, Ra_s, Tau, Pr, d, N_fm, N_r, symmetric,
     Xh = X.cpu().numpy().ravel()
     Y = np.hstack((Xh, float(Ra_d.item())))
     Y_dot = np.hstack((Xd.cpu().numpy().ravel(), r["Ra_dot"]))
-    Norm, KE, NuT, NuS = _diagnostics(Xh, plan.arrays["R"], plan.arrays["D"], N_fm, N_r - 1, d, symmetric)
+    Norm, KE, NuT, NuS = _diagnostics(plan, X)
     return Y_dot, Y, sign, r["ds"], Norm, KE, NuT, NuS, True
 
 

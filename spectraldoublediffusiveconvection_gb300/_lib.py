@@ -35,6 +35,7 @@ class PlanDesc(ctypes.Structure):
         ("Dr", _dp), ("D2_r2", _dp), ("ir4_r2", _dp), ("D2_sine", _dp), ("ir2_sine", _dp),
         ("D2_A4", _dp), ("ir2_A4", _dp), ("ir4_A4", _dp), ("rsq", _dp), ("dT0", _dp), ("gr", _dp),
         ("Linv_A4", _dp), ("Linv_T", _dp), ("Linv_S", _dp),
+        ("nu_w", _dp), ("r_int", _dp), ("r_i", ctypes.c_double), ("r_o", ctypes.c_double),
     ]
 
 
@@ -96,6 +97,8 @@ SIGNATURES = [
                              ctypes.POINTER(ContinResult), _VP]),
     ("sdd_nlin_fx_noalloc", _I, [_VP, _I, _VP, _VP, _VP]),
     ("sdd_step_profile", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, ctypes.POINTER(ctypes.c_double), _VP]),
+    ("sdd_diagnostics", _I, [_VP, _I, _VP, _VP, _VP]),
+    ("sdd_step_diag", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, _I, _VP, _VP]),
     ("sdd_kernel_name", ctypes.c_char_p, [_I]),
     ("sdd_step_kernel_profile", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, ctypes.POINTER(ctypes.c_double),
                                     ctypes.POINTER(ctypes.c_int), _VP]),

@@ -136,6 +136,10 @@ struct sdd_plan {
   int* h_int;         // pinned host flags
   double *sv_F, *sv_x, *sv_X0, *sv_Xd, *sv_t, *sv_G, *sv_Jmu, *sv_g, *sv_base64, *sv_dev;
   float* sv_base32;
+  // diagnostics (sdd_diagnostics): FFT plan of length 3M and weight tables; part = per-radius sums
+  const FftPlan* dfft;
+  double *dg_ir, *dg_tw, *dg_wr, *dg_nuw, *dg_part, *dg_out;
+  double ke_scale;
   // CUDA graphs of repeated time steps (sdd_step): A -> xtmp -> A pairs, A = the caller's output
   StepGraph graphs[kStepGraphs];
   unsigned long long graph_clock;
@@ -233,7 +237,8 @@ static void free_plan(sdd_plan* p) {
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   double* d[] = {p->Dr, p->D2r2, p->ir4r2, p->D2s, p->ir2s, p->D2A4, p->ir2A4, p->ir4A4, p->rsq, p->dT0,
                  p->gr, p->LinvA4, p->LinvT, p->LinvS, p->out4, p->rhs, p->xtmp, p->coefA4, p->coefT, p->coefS, p->ABA4, p->hbuf,
-                 p->GA4, p->GT, p->GS, p->PhiA4, p->PhiT, p->PhiS, p->dbuf, p->cbuf};
+                 p->GA4, p->GT, p->GS, p->PhiA4, p->PhiT, p->PhiS, p->dbuf, p->cbuf,
+                 p->dg_ir, p->dg_tw, p->dg_wr, p->dg_nuw, p->dg_part, p->dg_out};
   for (double* x : d) cudaFree(x);
   cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232);
   cudaFree(p->base_tmp);
@@ -339,6 +344,43 @@ static int build_chunk_tables(sdd_plan* p, const double* AB, const double* LinvT
   return SDD_OK;
 }
 
+// Diagnostics tables (Main.py:41-134): 1/R and trapezoid weights over the interior radii, trapezoid
+// weight * sin(theta) on the 3M-point midpoint grid, Nusselt weights of the even modes, 1/(2V).  Left out
+// (diagnostics unsupported) when the descriptor has no radii or 3M has no FFT plan.
+static int build_diag_tables(sdd_plan* p, const sdd_plan_desc* d) {
+  if (!d->nu_w || !d->r_int) return SDD_OK;
+  const int M = p->M, nr = p->nr, L = 3 * M;
+  const FftPlan* fp = get_fft_plan(L);
+  int optin = 0;
+  SDD_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device));
+  if (!fp || diag_rows_smem_bytes(M, L) > (size_t)optin) return SDD_OK;
+  std::vector<double> ir(nr), wr(nr, 0.0), tw(L), nuw((size_t)((M + 1) / 2) * nr);
+  const double* x = d->r_int;
+  for (int n = 0; n < nr; ++n) ir[n] = 1.0 / x[n];
+  for (int n = 0; n + 1 < nr; ++n) {   // trapezoid over x = R[1:-1]
+    const double hh = 0.5 * (x[n + 1] - x[n]);
+    wr[n] += hh;
+    wr[n + 1] += hh;
+  }
+  const double h = M_PI / L;          // midpoint grid theta_i = pi (2i+1) / (2L)
+  for (int i = 0; i < L; ++i) {
+    const double th = M_PI * (2.0 * i + 1.0) / (2.0 * L);
+    const double w = (i == 0 || i == L - 1) ? 0.5 * h : h;
+    tw[i] = w * std::sin(th);
+  }
+  for (int kk = 0; kk < (M + 1) / 2; ++kk) {
+    const double k = 2.0 * kk;
+    for (int m = 0; m < nr; ++m) nuw[(size_t)kk * nr + m] = d->nu_w[m] / (1.0 - k * k);
+  }
+  int st;
+  if ((st = upload(&p->dg_ir, ir.data(), nr)) || (st = upload(&p->dg_wr, wr.data(), nr)) ||
+      (st = upload(&p->dg_tw, tw.data(), L)) || (st = upload(&p->dg_nuw, nuw.data(), nuw.size())))
+    return st;
+  p->ke_scale = 0.5 / ((2.0 / 3.0) * (d->r_o * d->r_o * d->r_o - d->r_i * d->r_i * d->r_i));
+  p->dfft = fp;
+  return SDD_OK;
+}
+
 int sdd_plan_create(const sdd_plan_desc* d, sdd_plan** out) {
   if (!d || !out) return SDD_ERR_ARG;
   *out = nullptr;
@@ -425,7 +467,8 @@ int sdd_plan_create(const sdd_plan_desc* d, sdd_plan** out) {
       }
     }
     if ((st = upload(&p->ABA4, AB.data(), AB.size())) ||
-        (st = build_chunk_tables(p, AB.data(), d->Linv_T, d->Linv_S, cA.data(), cT.data(), cS.data()))) {
+        (st = build_chunk_tables(p, AB.data(), d->Linv_T, d->Linv_S, cA.data(), cT.data(), cS.data())) ||
+        (st = build_diag_tables(p, d))) {
       free_plan(p);
       return st;
     }
@@ -464,6 +507,8 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   clear_step_graphs(p);   // the graphs bake in the workspace pointers
   cudaFree(p->out4); cudaFree(p->rhs); cudaFree(p->xtmp); cudaFree(p->base_tmp); cudaFree(p->hbuf);
   cudaFree(p->dbuf); cudaFree(p->cbuf); cudaFree(p->gridbuf); cudaFree(p->derivbuf);
+  cudaFree(p->dg_part); cudaFree(p->dg_out);
+  p->dg_part = p->dg_out = nullptr;
   p->out4 = p->rhs = p->xtmp = p->hbuf = p->dbuf = p->cbuf = nullptr;
   p->base_tmp = p->gridbuf = p->derivbuf = nullptr;
   p->ws_batch = 0;
@@ -476,6 +521,8 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   SDD_CUDA(cudaMalloc(&p->base_tmp, (size_t)max_batch * be * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->gridbuf, (size_t)max_batch * be * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->derivbuf, (size_t)max_batch * 5 * p->M * p->nr * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->dg_part, (size_t)max_batch * p->nr * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->dg_out, (size_t)max_batch * 4 * sizeof(double)));
   const size_t de = (size_t)6 * p->nch * p->ldd;
   SDD_CUDA(cudaMalloc(&p->dbuf, (size_t)max_batch * de * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->cbuf, (size_t)max_batch * de * sizeof(double)));
@@ -1181,6 +1228,50 @@ extern "C" int sdd_step_profile(sdd_plan* p, int B, const double* Ra, const doub
   }
   for (auto& e : ev) cudaEventDestroy(e);
   return rc;
+}
+
+static DiagArgs diag_args(const sdd_plan* p, const double* X, double* out) {
+  DiagArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.M = p->M; a.nr = p->nr; a.sym = p->sym; a.L = p->dfft->L;
+  a.st.L = p->dfft->L; a.st.nst = p->dfft->nst;
+  for (int i = 0; i < kMaxStages; ++i) a.st.rad[i] = p->dfft->rad[i];
+  a.w = p->dfft->w64; a.e = p->dfft->e64;
+  a.Dr = p->Dr; a.ir = p->dg_ir; a.tw = p->dg_tw; a.wr = p->dg_wr; a.nuw = p->dg_nuw;
+  a.ke_scale = p->ke_scale;
+  a.X = X; a.x_stride = shell_elems(p);
+  a.part = p->dg_part; a.out = out;
+  return a;
+}
+
+extern "C" int sdd_diagnostics(sdd_plan* p, int batch, const double* X, double* out, void* stream) {
+  int st = check_plan(p, batch);
+  if (st) return st;
+  if (!X || !out) return SDD_ERR_ARG;
+  if (!p->dfft) return SDD_ERR_UNSUPPORTED;
+  SDD_CUDA(launch_diag(diag_args(p, X, out), batch, (cudaStream_t)stream));
+  return SDD_OK;
+}
+
+extern "C" int sdd_step_diag(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X_in,
+                             double* X_out, int nsteps, int linear, double* diag, void* stream) {
+  int st = check_plan(p, batch);
+  if (st) return st;
+  if (!Ra || !Ras || !X_in || !X_out || !diag || nsteps < 0) return SDD_ERR_ARG;
+  if (!p->dfft) return SDD_ERR_UNSUPPORTED;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t bytes = (size_t)batch * shell_elems(p) * sizeof(double);
+  const double* cur = X_in;
+  for (int it = 0; it < nsteps; ++it) {
+    const int left = nsteps - it;
+    double* dst = (left % 2 == 1) ? X_out : p->xtmp;
+    if (dst == cur) dst = (dst == X_out) ? p->xtmp : X_out;
+    if ((st = apply_step(p, batch, Ra, Ras, cur, dst, nullptr, linear ? 2 : 0, nullptr, p->prec, s))) return st;
+    SDD_CUDA(launch_diag(diag_args(p, dst, diag + (size_t)it * batch * 4), batch, s));
+    cur = dst;
+  }
+  if (cur != X_out) SDD_CUDA(cudaMemcpyAsync(X_out, cur, bytes, cudaMemcpyDeviceToDevice, s));
+  return SDD_OK;
 }
 
 extern "C" const char* sdd_kernel_name(int id) {

@@ -175,7 +175,26 @@ struct ChainArgs {
   size_t d_stride;           // doubles per shell in dbuf / cbuf
 };
 
+struct DiagArgs {
+  int M, nr, sym, L;         // L = 3 M: the kinetic-energy grid
+  StageArgs st;              // FFT of length L
+  const double2* w;          // FFT twiddles of length L
+  const double2* e;          // DCT twiddles of length L
+  const double* Dr;          // nr*nr interior D
+  const double* ir;          // nr  1/R interior
+  const double* tw;          // L   trapezoid weight * sin(theta_i) on the L-point midpoint grid
+  const double* wr;          // nr  trapezoid weights over the interior radii
+  const double* nuw;         // ceil(M/2)*nr  Nusselt weights of the even modes
+  double ke_scale;           // 1/(2V), V = (2/3)(r_o^3 - r_i^3)
+  const double* X;           // states [shell][3][M][nr]
+  size_t x_stride;
+  double* part;              // [shell][nr] per-radius kinetic-energy sums
+  double* out;               // [shell][4]
+};
+
 // launchers (return cudaError_t of the launch)
+cudaError_t launch_diag(const DiagArgs& a, int batch, cudaStream_t s);
+size_t diag_rows_smem_bytes(int M, int L);
 cudaError_t launch_fx(const FxArgs& a, int batch, int mode, int prec, cudaStream_t s);
 // whether launch_fx takes the split path for these arguments
 bool fx_uses_split(const FxArgs& a, int batch, int mode);

@@ -131,5 +131,7 @@ def plan_arrays(N_fm, N_r, d, dt, Pr, Tau):
         Linv_A4=a4_tstep_mats(Pr * dt, N_fm, nr, D, R),
         Linv_T=nab2_tstep_mats(dt, N_fm, nr, D, R),
         Linv_S=nab2_tstep_mats(Tau * dt, N_fm, nr, D, R),
+        nu_w=np.ascontiguousarray((R[0] ** 2 / A_T) * D[0, 1:-1]),
+        r_int=np.ascontiguousarray(R[1:-1]),
     )
     return ops

@@ -67,6 +67,9 @@ class Plan:
         for name in ("Dr", "D2_r2", "ir4_r2", "D2_sine", "ir2_sine", "D2_A4", "ir2_A4", "ir4_A4", "rsq",
                      "dT0", "gr", "Linv_A4", "Linv_T", "Linv_S"):
             setattr(desc, name, _ptr(A[name]))
+        if "nu_w" in A and "r_int" in A and "R" in A:      # diagnostics tables (optional)
+            desc.nu_w, desc.r_int = _ptr(A["nu_w"]), _ptr(A["r_int"])
+            desc.r_i, desc.r_o = float(A["R"][0]), float(A["R"][-1])
         h = ctypes.c_void_p()
         L = _lib.lib()
         with torch.cuda.device(self.device):
@@ -211,6 +214,27 @@ class Plan:
         _lib.check(self._L.sdd_step_profile(self._h, B, _dptr(ra), _dptr(ras), _dptr(X), _dptr(out), int(nsteps),
                                             ms, _stream(self.device)), "sdd_step_profile")
         return list(ms), out
+
+    def diagnostics(self, X):
+        """(batch, 4) device tensor: |X|_2, Kinetic_Energy, Nusselt(T), Nusselt(S) of each shell
+        (Main.py:41-134, sdd_diagnostics)."""
+        torch = _torch()
+        B = self._chk(X, self.n_state, "X")
+        out = torch.empty((B, 4), dtype=torch.float64, device=self.device)
+        _lib.check(self._L.sdd_diagnostics(self._h, B, _dptr(X), _dptr(out), _stream(self.device)), "sdd_diagnostics")
+        return out
+
+    def step_diag(self, X, Ra, Ra_s, nsteps=1, linear=False, out=None):
+        """nsteps steps like ``step`` with the diagnostics of the state after every step:
+        returns (X_out, (nsteps, batch, 4) device tensor)."""
+        torch = _torch()
+        B = self._chk(X, self.n_state, "X")
+        out = out if out is not None else torch.empty_like(X)
+        ra, ras = self._vec(Ra, B), self._vec(Ra_s, B)
+        dg = torch.empty((max(int(nsteps), 0), B, 4), dtype=torch.float64, device=self.device)
+        _lib.check(self._L.sdd_step_diag(self._h, B, _dptr(ra), _dptr(ras), _dptr(X), _dptr(out), int(nsteps),
+                                         int(bool(linear)), _dptr(dg), _stream(self.device)), "sdd_step_diag")
+        return out, dg
 
     def chunks(self):
         """Chunks per chain of the chunked layout: kc = clamp(round(sqrt(N_fm)), 4, 32) steps each."""

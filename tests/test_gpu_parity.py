@@ -213,3 +213,49 @@ def test_full_eig_vec_dropin_matches_reference(cuda):
     for N_fm in (16, 32):
         assert rel(LP.Full_Eig_Vec(f, 2.0, N_fm, 19), Z[f"full_{N_fm}"]) < 1e-13
     assert rel(LP.Full_Eig_Vec(f, 2.0, 16, 19, symmetric=True), Z["full_sym_16"]) < 1e-13
+
+
+def _series_close(a, b, tol):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)) < tol
+
+
+@pytest.mark.parametrize("tag", ["c1", "tiny", "sym_lin"])
+def test_time_step_dropin_records_match_reference(cuda, tag):
+    """Main._Time_Step drop-in against the reference's own run: saved states, final state, and the
+    per-step |X|, KE, Nu_T, Nu_S series (computed on the device every step)."""
+    from spectraldoublediffusiveconvection_gb300 import Main
+    Z = load_golden(f"traj_{tag}.npz")
+    N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, sym, ns = Z["params"]
+    XN = Main._Time_Step(Z["X0"].copy(), Ra, Ra_s, Tau, Pr, d, int(N_fm), int(N_r), bool(sym), save_filename=None,
+                         Total_time=int(ns) * dt, dt=dt, linear=(tag == "sym_lin"))
+    rec = Main._Time_Step.last_record
+    assert rel(XN, Z["X_final"]) < 1e-11
+    assert len(rec["X_DATA"]) == len(Z["X_DATA"])
+    for a, b in zip(rec["X_DATA"], Z["X_DATA"]):
+        assert rel(a, b) < 1e-11
+    n = len(Z["KE"])
+    assert len(rec["KE"]) == n
+    assert _series_close(rec["Norm"], Z["Norm"], 1e-11)
+    assert _series_close(rec["KE"], Z["KE"], 1e-10)
+    assert _series_close(rec["Nu_T"], Z["NuT"], 1e-10)
+    assert _series_close(rec["Nu_S"], Z["NuS"], 1e-10)
+
+
+@pytest.mark.parametrize("N_r,N_fm,sym", [(30, 256, False), (20, 64, True), (48, 512, False)])
+def test_device_diagnostics_against_oracle(cuda, N_r, N_fm, sym):
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    nr = N_r - 1
+    ops = O.Operators(N_fm, N_r, 2.0, 1e-3, 1.0, 0.01)
+    Xs = [O.seeded_state(N_fm, nr, s, sym) * (1 + 50 * s) for s in range(3)]
+    p = Plan(N_fm, N_r, 2.0, 1e-3, 1.0, 0.01, symmetric=sym)
+    out = p.diagnostics(torch.from_numpy(np.stack(Xs)).cuda()).cpu().numpy()
+    N = N_fm * nr
+    for i, X in enumerate(Xs):
+        ref = [np.linalg.norm(X), O.Kinetic_Energy(X, ops.R, ops.D, N_fm, nr, sym),
+               O.Nusselt(X[N:2 * N], 2.0, ops.R, ops.D, N_fm, nr), O.Nusselt(X[2 * N:], 2.0, ops.R, ops.D, N_fm, nr)]
+        assert abs(out[i, 0] - ref[0]) <= 1e-13 * ref[0]
+        assert abs(out[i, 1] - ref[1]) <= 1e-11 * abs(ref[1])
+        assert abs(out[i, 2] - ref[2]) <= 1e-11 * (abs(ref[2]) + 1e-3)
+        assert abs(out[i, 3] - ref[3]) <= 1e-11 * (abs(ref[3]) + 1e-3)
