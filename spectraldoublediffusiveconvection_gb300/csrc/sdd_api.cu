@@ -26,6 +26,7 @@ void set_cuda_error(cudaError_t e) { g_last_cuda = (int)e; }
     cudaError_t e_ = (call);                   \
     if (e_ != cudaSuccess) {                   \
       set_cuda_error(e_);                      \
+      (void)cudaGetLastError(); /* not left for the caller's next runtime call */ \
       return e_ == cudaErrorMemoryAllocation ? SDD_ERR_NOMEM : SDD_ERR_CUDA; \
     }                                          \
   } while (0)
@@ -117,6 +118,7 @@ struct sdd_plan {
   int kc, nch, ldmA, ldmT, ldd;
   double *GA4, *GT, *GS, *PhiA4, *PhiT, *PhiS;
   double *dbuf, *cbuf;              // [B][3][2][nch][ldd] chunk end states / carried states
+  int* dcnt;                        // [B][6] chunk counters of the chunked chains
   // FP32 copies used by the mixed-precision nonlinear term
   float *Dr32, *D2r232, *ir4r232;
   // workspace
@@ -244,6 +246,7 @@ static void free_plan(sdd_plan* p) {
   cudaFree(p->base_tmp);
   cudaFree(p->gridbuf);
   cudaFree(p->derivbuf);
+  cudaFree(p->dcnt);
   solver_free(p);
   delete p;
 }
@@ -507,8 +510,9 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   clear_step_graphs(p);   // the graphs bake in the workspace pointers
   cudaFree(p->out4); cudaFree(p->rhs); cudaFree(p->xtmp); cudaFree(p->base_tmp); cudaFree(p->hbuf);
   cudaFree(p->dbuf); cudaFree(p->cbuf); cudaFree(p->gridbuf); cudaFree(p->derivbuf);
-  cudaFree(p->dg_part); cudaFree(p->dg_out);
+  cudaFree(p->dg_part); cudaFree(p->dg_out); cudaFree(p->dcnt);
   p->dg_part = p->dg_out = nullptr;
+  p->dcnt = nullptr;
   p->out4 = p->rhs = p->xtmp = p->hbuf = p->dbuf = p->cbuf = nullptr;
   p->base_tmp = p->gridbuf = p->derivbuf = nullptr;
   p->ws_batch = 0;
@@ -523,6 +527,8 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   SDD_CUDA(cudaMalloc(&p->derivbuf, (size_t)max_batch * 5 * p->M * p->nr * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->dg_part, (size_t)max_batch * p->nr * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->dg_out, (size_t)max_batch * 4 * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->dcnt, (size_t)max_batch * 6 * sizeof(int)));
+  SDD_CUDA(cudaMemset(p->dcnt, 0, (size_t)max_batch * 6 * sizeof(int)));
   const size_t de = (size_t)6 * p->nch * p->ldd;
   SDD_CUDA(cudaMalloc(&p->dbuf, (size_t)max_batch * de * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->cbuf, (size_t)max_batch * de * sizeof(double)));
@@ -585,7 +591,7 @@ static ChainArgs chain_args(const sdd_plan* p, const double* g, double* f, const
   a.dtA4 = p->Pr * p->dt; a.dtT = p->dt; a.dtS = p->Tau * p->dt;
   a.kc = p->kc; a.nch = p->nch; a.ldmA = p->ldmA; a.ldmT = p->ldmT; a.ldd = p->ldd;
   a.GA4 = p->GA4; a.GT = p->GT; a.GS = p->GS; a.PhiA4 = p->PhiA4; a.PhiT = p->PhiT; a.PhiS = p->PhiS;
-  a.dbuf = p->dbuf; a.cbuf = p->cbuf;
+  a.dbuf = p->dbuf; a.cbuf = p->cbuf; a.counter = p->dcnt;
   a.d_stride = (size_t)6 * p->nch * p->ldd;
   return a;
 }

@@ -26,12 +26,14 @@
 //     concurrently, each from a zero carried state (its own CTA, h = Linv g computed in its prologue).
 //     The chain's carried state s (psi: [f_e; bf_e], 2 nr; T/S: b, nr) enters every later step linearly,
 //     so with the plan's precomputed Phi_c (state over a whole chunk) and G_jj (state -> f_jj):
-//       s_1 = d_0,  s_{c+1} = Phi_c s_c + d_c   (k_chain_carry, one CTA per chain, nch - 2 matvecs)
+//       s_1 = d_0,  s_{c+1} = Phi_c s_c + d_c   (carry_run, by the chain's last-finishing chunk CTA)
 //       f_jj += G_jj s_c(jj)                    (k_mode_mv, all modes in parallel)
 //     The critical path drops from S dependent steps to kc + (nch - 2) carried matvecs + one matvec.
 // Matrices are stored transposed (column c contiguous, leading dimension ldl); the block of step s+2
 // streams global->shared with cp.async while step s runs (3-slot ring).  FP64 throughout.
 #include <cuda_runtime.h>
+#include <algorithm>
+
 #include "sdd_internal.cuh"
 
 namespace sdd {
@@ -76,7 +78,10 @@ __device__ __forceinline__ void chain_sync() {
 // CHUNK = false: the whole chain (s0 = 0, s1 = S).  CHUNK = true: chunk blockIdx.z of a.kc steps,
 // started from a zero carried state; its end state goes to dbuf (psi: [f_e; bf_e]; T/S: b + k_next f_last,
 // the b the next chunk's first step uses).  Both read h = Linv g (k_mode_mv) through a.g.
-template <int TPR, bool CHUNK>
+template <int TPR, int R>
+__device__ void carry_run(const ChainArgs& a, int field, int par, int b, double* csm);
+
+template <int TPR, bool CHUNK, int CR = 0>
 __global__ void k_chain(ChainArgs a) {
   extern __shared__ __align__(16) double csm[];
   const int field = a.field0 + (blockIdx.x >> 1);
@@ -193,6 +198,25 @@ __global__ void k_chain(ChainArgs a) {
       f[o] -= sub[o];
     }
   }
+  if (CHUNK && a.nch > 2) {
+    // the last chunk of this chain to finish runs the carried-state recurrence (no extra launch)
+    __shared__ int s_last;
+    __threadfence();                                   // this chunk's end state before the ticket
+    __syncthreads();
+    int* cnt = a.counter + (size_t)b * 6 + (field * 2 + par);
+    if (tid == 0) s_last = (atomicAdd(cnt, 1) == a.nch - 1);
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    if (tid == 0) *cnt = 0;                            // ready for the next launch
+    carry_run<(TPR == 4 ? 2 : 1), CR>(a, field, par, b, csm);
+  } else if (CHUNK && a.nch == 2) {                   // s_1 = d_0 only: the chain's first chunk copies it
+    if (chunk == 0 && lead) {
+      double* cb = a.cbuf + (size_t)b * a.d_stride + ((size_t)(field * 2 + par) * a.nch + 1) * a.ldd;
+      cb[i] = fe;
+      if (a4) cb[nr + i] = bfe;
+    }
+  }
 }
 
 size_t chain_smem_bytes(int M, int nr, int ldl) {
@@ -206,18 +230,14 @@ static size_t chunk_smem_bytes(int kc, int nr, int ldl) {
   return (3 * blk + (size_t)kc * nr + 4 * ((size_t)kc + 1) + 4 * (size_t)nr) * sizeof(double);
 }
 
-// Carried states of the chunked chains: s_1 = d_0, s_{c+1} = Phi_c s_c + d_c (c = 1 .. nch-2), one CTA per
-// chain.  Rows of Phi split over TPR lanes.  Phi_c streams into an R-slot shared-memory ring, R - 1 matrices
-// ahead of the one in use (R = 0: read through L2).  One barrier per step: the copy into the slot of
-// Phi_{c-1} is issued after the step-c barrier, when every thread is done with it.
+// Carried states of the chunked chains: s_1 = d_0, s_{c+1} = Phi_c s_c + d_c (c = 1 .. nch-2) of one chain,
+// run by the CTA of that chain's chunks that finishes last (see k_chain).  Rows of Phi split over TPR
+// lanes.  Phi_c streams into an R-slot shared-memory ring, R - 1 matrices ahead of the one in use (R = 0:
+// read through L2).  One barrier per step: the copy into the slot of Phi_{c-1} is issued after the step-c
+// barrier, when every thread is done with it.  The other chunks' end states are read through L2.
 template <int TPR, int R>
-__global__ void k_chain_carry(ChainArgs a) {
-  extern __shared__ __align__(16) double csm[];
-  const int field = a.field0 + (blockIdx.x >> 1);
-  const int par = blockIdx.x & 1;
-  const int b = blockIdx.y;
+__device__ void carry_run(const ChainArgs& a, int field, int par, int b, double* csm) {
   const bool a4 = (field == 0);
-  if (a.sym && !(a4 ? par == 0 : par == 1)) return;
   const int m = a4 ? 2 * a.nr : a.nr;
   const int ldm = a4 ? a.ldmA : a.ldmT;
   const int nch = a.nch;
@@ -234,6 +254,7 @@ __global__ void k_chain_carry(ChainArgs a) {
   const int last = nch - 2;                            // Phi_1 .. Phi_last are used
   constexpr int RR = R > 0 ? R : 1;
 
+  __syncthreads();                                     // the chunk's shared memory is free
   if (R > 0) {
 #pragma unroll
     for (int k = 1; k < RR; ++k) {                     // Phi_1 .. Phi_{R-1}
@@ -242,7 +263,7 @@ __global__ void k_chain_carry(ChainArgs a) {
     }
   }
   for (int e = tid; e < m; e += blockDim.x) {
-    const double v = d[e];                             // s_1 = d_0
+    const double v = __ldcg(d + e);                    // s_1 = d_0
     st[e] = v;
     cb[a.ldd + e] = v;
   }
@@ -267,7 +288,7 @@ __global__ void k_chain_carry(ChainArgs a) {
       for (int col = q; col < m; col += TPR) acc = fma(P[(size_t)col * ldm + rr], cur_in[col], acc);
       acc = group_sum<TPR>(acc);
       if (r < m && q == 0) {
-        const double v = acc + dc[r];
+        const double v = acc + __ldcg(dc + r);
         nxt[r] = v;
         cout[r] = v;
       }
@@ -424,45 +445,32 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
   ChainArgs a = a_in;
   a.g = a.h;
   a.g_stride = a.h_stride;
-  const size_t smem = chunk_smem_bytes(a.kc, a.nr, a.ldl);
-  const dim3 grid(2 * nfields, batch, a.nch);
-  if (a.nr <= 32) {
-    static unsigned long long done = 0;
-    if ((e = ensure_smem_attr(k_chain<4, true>, &done)) != cudaSuccess) return e;
-    if ((e = launch_kernel(k_chain<4, true>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e;
-  } else {
-    static unsigned long long done = 0;
-    if ((e = ensure_smem_attr(k_chain<2, true>, &done)) != cudaSuccess) return e;
-    if ((e = launch_kernel(k_chain<2, true>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e;
-  }
-  ktimer_mark(SDD_K_CHAIN, s);
-  if ((e = cudaGetLastError()) != cudaSuccess || a.nch < 2) return e;
-  // carried states: Phi of the psi chain (m = 2 nr) decides the ring depth for all fields of the launch
+  // the carry ring of the psi chain (m = 2 nr) decides the ring depth for all fields of the launch
   const int mmax = a.field0 == 0 ? 2 * a.nr : a.nr;
   const int ldmax = a.field0 == 0 ? a.ldmA : a.ldmT;
   const size_t blkb = (size_t)mmax * ldmax * sizeof(double);
   const size_t st = 2 * (size_t)a.ldd * sizeof(double);
   const int depth = (4 * blkb + st <= 200 * 1024) ? 4 : (2 * blkb + st <= 200 * 1024) ? 2 : 0;
-  const size_t smc = depth * blkb + st;
-  const dim3 cg(2 * nfields, batch);
-#define SDD_CARRY(TPR_, R_)                                                         \
-  do {                                                                              \
-    static unsigned long long done = 0;                                             \
-    if ((e = ensure_smem_attr(k_chain_carry<TPR_, R_>, &done)) != cudaSuccess) return e; \
-    if ((e = launch_kernel(k_chain_carry<TPR_, R_>, cg, dim3(128), smc, s, a)) != cudaSuccess) return e; \
+  const size_t smem = std::max(chunk_smem_bytes(a.kc, a.nr, a.ldl), depth * blkb + st);
+  const dim3 grid(2 * nfields, batch, a.nch);
+#define SDD_CHUNK(TPR_, R_)                                                              \
+  do {                                                                                   \
+    static unsigned long long done = 0;                                                  \
+    if ((e = ensure_smem_attr(k_chain<TPR_, true, R_>, &done)) != cudaSuccess) return e; \
+    if ((e = launch_kernel(k_chain<TPR_, true, R_>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e; \
   } while (0)
-  if (mmax <= 64) {
-    if (depth == 4) SDD_CARRY(2, 4);
-    else if (depth == 2) SDD_CARRY(2, 2);
-    else SDD_CARRY(2, 0);
+  if (a.nr <= 32) {
+    if (depth == 4) SDD_CHUNK(4, 4);
+    else if (depth == 2) SDD_CHUNK(4, 2);
+    else SDD_CHUNK(4, 0);
   } else {
-    if (depth == 4) SDD_CARRY(1, 4);
-    else if (depth == 2) SDD_CARRY(1, 2);
-    else SDD_CARRY(1, 0);
+    if (depth == 4) SDD_CHUNK(2, 4);
+    else if (depth == 2) SDD_CHUNK(2, 2);
+    else SDD_CHUNK(2, 0);
   }
-#undef SDD_CARRY
-  ktimer_mark(SDD_K_CHAIN_CARRY, s);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+#undef SDD_CHUNK
+  ktimer_mark(SDD_K_CHAIN, s);
+  if (a.nch < 2) return cudaSuccess;
   return launch_mode_mv<true>(a, batch, nfields, s, false);
 }
 

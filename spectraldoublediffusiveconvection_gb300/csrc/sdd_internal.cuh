@@ -59,7 +59,12 @@ inline cudaError_t ensure_smem_attr(F* fn, unsigned long long* done_mask) {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(reinterpret_cast<const void*>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(fn));
+  if (e != cudaSuccess) return e;
+  // the dynamic limit may not exceed the opt-in maximum less the kernel's static shared memory
+  e = cudaFuncSetAttribute(reinterpret_cast<const void*>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           optin - (int)fa.sharedSizeBytes);
   if (e == cudaSuccess) __atomic_fetch_or(done_mask, bit, __ATOMIC_ACQ_REL);
   return e;
 }
@@ -173,6 +178,7 @@ struct ChainArgs {
   double* dbuf;              // [shell][3][2][nch][ldd] chunk end states from a zero start
   double* cbuf;              // [shell][3][2][nch][ldd] carried states at the chunk starts (c >= 1)
   size_t d_stride;           // doubles per shell in dbuf / cbuf
+  int* counter;              // [shell][6] chunks finished per chain (the last one runs the carry), zeroed
 };
 
 struct DiagArgs {
