@@ -15,7 +15,7 @@ import numpy as np
 
 from .seeds import seeded_state
 
-from .plan import get_plan
+from .plan import Plan
 
 
 def _torch():
@@ -24,14 +24,15 @@ def _torch():
 
 
 class _Group:
-    def __init__(self, plan, idx, X, Ra, Ra_s, device):
+    def __init__(self, plan, idx, X, Ra, Ra_s, device, priority=0):
         torch = _torch()
         self.plan = plan
         self.idx = list(idx)                 # positions of the shells in the caller's list
         self.X = torch.from_numpy(np.ascontiguousarray(np.stack(X))).to(device)
         self.Ra = torch.tensor(Ra, dtype=torch.float64, device=device)
         self.Ras = torch.tensor(Ra_s, dtype=torch.float64, device=device)
-        self.stream = torch.cuda.Stream(device=device)
+        self.stream = torch.cuda.Stream(device=device, priority=priority)
+        self.priority = priority
 
     @property
     def shape(self):
@@ -43,7 +44,7 @@ class ShellBatch:
     flat numpy array in the reference layout; seeded if absent) and symmetric."""
 
     def __init__(self, shells, d=2.0, dt=1e-3, Pr=1.0, Tau=0.01, Ra_s=500.0, precision="mixed",
-                 device=None, seed=1234):
+                 device=None, seed=1234, max_group=None, priorities=False):
         torch = _torch()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.d, self.dt, self.Pr, self.Tau, self.precision = d, dt, Pr, Tau, precision
@@ -54,15 +55,27 @@ class ShellBatch:
             key = (int(s["N_r"]), int(s["N_theta"]), bool(s.get("symmetric", False)))
             groups.setdefault(key, []).append(i)
         self.groups = []
+        # every group has its own plan (its own workspace: groups run concurrently); groups larger than
+        # max_group are split into sub-groups on separate streams
+        parts = []
         for (N_r, M, sym), idx in sorted(groups.items(), key=lambda kv: -kv[0][1] * kv[0][0]):
-            plan = get_plan(M, N_r, d, dt, Pr, Tau, symmetric=sym, precision=precision, device=self.device)
+            step = max_group if max_group else len(idx)
+            parts += [((N_r, M, sym), idx[k:k + step]) for k in range(0, len(idx), step)]
+        # optional stream priorities: the costliest groups (M nr^2 per shell x shells) on high-priority
+        # streams, so the critical path of the graph is not delayed by the small groups
+        cost = [M * (N_r - 1) ** 2 * len(idx) for (N_r, M, _), idx in parts]
+        ranked = sorted(range(len(parts)), key=lambda k: -cost[k])
+        high = set(ranked[:max(1, len(parts) // 4)]) if priorities else set()
+        for k, ((N_r, M, sym), idx) in enumerate(parts):
+            plan = Plan(M, N_r, d, dt, Pr, Tau, symmetric=sym, precision=precision, device=self.device)
             X = []
             for i in idx:
                 x0 = shells[i].get("X")
                 X.append(np.asarray(x0, dtype=np.float64) if x0 is not None else
                          _seeded(M, N_r - 1, rng))
             g = _Group(plan, idx, X, [float(shells[i]["Ra"]) for i in idx],
-                       [float(shells[i].get("Ra_s", Ra_s)) for i in idx], self.device)
+                       [float(shells[i].get("Ra_s", Ra_s)) for i in idx], self.device,
+                       priority=-1 if k in high else 0)
             plan.reserve(len(idx))
             self.groups.append(g)
         # Starting point of the tuning (measured on the 64-shell mixed batch of N_r in {20..36}, N_theta in

@@ -145,6 +145,8 @@ class Server:
         self._groups = {}
         self._waiting = collections.OrderedDict()
         self._con_inflight = set()   # shapes a continuation worker is solving (one worker per plan)
+        self._int_joining = {}       # integration requests admitted, waiting for their group's boundary
+        self.worker_error = None
         self._running = False
         self._threads = []
         self.completed = []
@@ -239,12 +241,40 @@ class Server:
         """Wait until every submitted request has completed (or been rejected)."""
         t0 = time.perf_counter()
         with self._cv:
-            while any(self._pending.values()) or self._active:
+            while (any(self._pending.values()) or self._active) and self.worker_error is None:
                 left = None if timeout is None else timeout - (time.perf_counter() - t0)
                 if left is not None and left <= 0:
                     return False
                 self._cv.wait(timeout=0.05 if left is None else min(0.05, left))
-        return True
+        return self.worker_error is None
+
+    def _worker_failed(self, kind, exc):
+        """A worker thread hit an unexpected error: every request it holds or would take fails with it, and
+        ``worker_error`` records it (drain() returns instead of waiting)."""
+        msg = "%s worker failed: %r" % (kind, exc)
+        self.worker_error = msg
+        owned = []
+        with self._cv:
+            owned += list(self._pending[kind])
+            self._pending[kind].clear()
+            if kind == "integrate":
+                for g in self._groups.values():
+                    owned += list(g.reqs)
+                    g.reqs, g.left = [], []
+                for lst in self._int_joining.values():
+                    owned += list(lst)
+                self._int_joining.clear()
+            else:
+                for lst in self._waiting.values():
+                    owned += list(lst)
+                self._waiting.clear()
+        for req in owned:
+            if req.t_admit is None:                     # never admitted: no bytes to return
+                req.error = msg
+                req.t_done = time.perf_counter()
+                req.done.set()
+            else:
+                self._finish(req, error=msg)
 
     def _finish(self, req, result=None, error=None):
         req.result, req.error = result, error
@@ -282,9 +312,16 @@ class Server:
         completed requests are retired, the requests admitted for its shape since then join, and the next
         quantum is launched.  Groups of different shapes overlap on the device and never wait for each
         other."""
+        try:
+            self._int_loop_body()
+        except Exception as e:                          # noqa: BLE001 - a dead worker fails its requests
+            self._worker_failed("integrate", e)
+
+    def _int_loop_body(self):
         torch = _torch()
         torch.cuda.set_device(self.device)
-        streams, events, busy, joining = {}, {}, {}, {}
+        streams, events, busy = {}, {}, {}
+        joining = self._int_joining
         while True:
             with self._cv:
                 new = self._admit_kind("integrate")
@@ -352,6 +389,12 @@ class Server:
 
     # ---- continuation worker -------------------------------------------------------------------------
     def _con_loop(self):
+        try:
+            self._con_loop_body()
+        except Exception as e:                          # noqa: BLE001 - a dead worker fails its requests
+            self._worker_failed("continue", e)
+
+    def _con_loop_body(self):
         torch = _torch()
         torch.cuda.set_device(self.device)
         stream = torch.cuda.Stream(device=self.device)

@@ -53,3 +53,20 @@ def test_admit_kind_is_fifo_and_reports_rejections():
     n = len(got)
     assert got == reqs[:n] and n >= 1
     assert list(srv._pending["integrate"]) == reqs[n:]
+
+
+def test_failed_worker_fails_its_requests_and_drain_returns():
+    serve, srv = _server(10 ** 9)
+    a = serve.Request("continue", 20, 64, 9000.0)
+    b = serve.Request("continue", 20, 64, 9000.0)
+    srv.submit(a)
+    srv.submit(b)
+    got = srv._admit_kind("continue")                  # a and b admitted; move a into the waiting list
+    assert got == [a, b]
+    srv._waiting.setdefault(a.shape, []).append(a)
+    srv._pending["continue"].append(b)                 # b back in the queue (admitted bytes kept)
+    srv._worker_failed("continue", RuntimeError("device lost"))
+    assert a.done.is_set() and b.done.is_set()
+    assert "device lost" in a.error and "device lost" in b.error
+    assert srv.drain(timeout=1.0) is False and srv.worker_error
+    assert srv.used == 0
