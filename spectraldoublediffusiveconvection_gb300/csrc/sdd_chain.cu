@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(128) k_mode_mv(ChainArgs a) {
 
 // The same matvecs with one warp per (field, mode, shell) and one lane per row: the fewest FP64
 // instructions, for launches that share the GPU with many others (lane-per-row chain layout).
-template <bool FIX>
+template <bool FIX, int TPR>
 __global__ void __launch_bounds__(128) k_mode_mv_warp(ChainArgs a, int nfields) {
   const int M = a.M, nr = a.nr, ldl = a.ldl;
   const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
@@ -406,19 +406,33 @@ __global__ void __launch_bounds__(128) k_mode_mv_warp(ChainArgs a, int nfields) 
     }
   }
   for (int r = lane; r < nr; r += 32) {
-    double acc = 0.0;
-#pragma unroll 8
-    for (int col = 0; col < m; ++col) acc = fma(__ldg(A + (size_t)col * ldl + r), x[col], acc);
-    if (FIX) y[r] += acc;
-    else y[r] = acc;
+    // the TPR column-strided partial sums of k_mode_mv, combined in its shuffle-tree order: both kernels
+    // give the same bits, so the launcher may pick either by size
+    double acc[TPR];
+#pragma unroll
+    for (int q = 0; q < TPR; ++q) acc[q] = 0.0;
+    int col = 0;
+    for (; col + TPR <= m; col += TPR) {
+#pragma unroll
+      for (int q = 0; q < TPR; ++q) acc[q] = fma(__ldg(A + (size_t)(col + q) * ldl + r), x[col + q], acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < TPR; ++q)
+      if (col + q < m) acc[q] = fma(__ldg(A + (size_t)(col + q) * ldl + r), x[col + q], acc[q]);
+    double v;
+    if (TPR == 4) v = (acc[0] + acc[1]) + (acc[2 % TPR] + acc[3 % TPR]);
+    else v = acc[0] + acc[1 % TPR];
+    if (FIX) y[r] += v;
+    else y[r] = v;
   }
 }
 
 template <bool FIX>
 static cudaError_t launch_mode_mv(const ChainArgs& a, int batch, int nfields, cudaStream_t s, bool per_warp) {
   if (per_warp) {
-    const cudaError_t e = launch_kernel(k_mode_mv_warp<FIX>, dim3((nfields * a.M + 3) / 4, batch), dim3(128), 0, s, a,
-                                     nfields);
+    const dim3 wg((nfields * a.M + 3) / 4, batch);
+    const cudaError_t e = a.nr <= 32 ? launch_kernel(k_mode_mv_warp<FIX, 4>, wg, dim3(128), 0, s, a, nfields)
+                                     : launch_kernel(k_mode_mv_warp<FIX, 2>, wg, dim3(128), 0, s, a, nfields);
     ktimer_mark(FIX ? SDD_K_MODE_FIX : SDD_K_MODE_H, s);
     return e;
   }
@@ -427,6 +441,14 @@ static cudaError_t launch_mode_mv(const ChainArgs& a, int batch, int nfields, cu
                                    : launch_kernel(k_mode_mv<2, FIX>, grid, dim3(128), 0, s, a);
   ktimer_mark(FIX ? SDD_K_MODE_FIX : SDD_K_MODE_H, s);
   return e;
+}
+
+// The per-mode matvecs run one per CTA (rows split over lanes: the most lanes per matvec, for launches
+// that leave the GPU idle) until there are more than kMvPerCtaMax of them, then four per CTA, one per warp
+// (the fewest instructions; same bits).
+constexpr int kMvPerCtaMax = 2048;
+static bool mv_per_warp(const ChainArgs& a, int batch, int nfields) {
+  return (long long)nfields * a.M * batch > kMvPerCtaMax;
 }
 
 static int sm_count() {
@@ -441,7 +463,8 @@ static int sm_count() {
 
 static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields, cudaStream_t s) {
   cudaError_t e;
-  if ((e = launch_mode_mv<false>(a_in, batch, nfields, s, false)) != cudaSuccess) return e;   // h = Linv g
+  const bool pw = mv_per_warp(a_in, batch, nfields);
+  if ((e = launch_mode_mv<false>(a_in, batch, nfields, s, pw)) != cudaSuccess) return e;   // h = Linv g
   ChainArgs a = a_in;
   a.g = a.h;
   a.g_stride = a.h_stride;
@@ -471,7 +494,7 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
 #undef SDD_CHUNK
   ktimer_mark(SDD_K_CHAIN, s);
   if (a.nch < 2) return cudaSuccess;
-  return launch_mode_mv<true>(a, batch, nfields, s, false);
+  return launch_mode_mv<true>(a, batch, nfields, s, pw);
 }
 
 // One CTA per chain.  When the batch leaves SMs idle (2*nfields*batch <= #SMs) the 4-warp split-row
@@ -497,7 +520,7 @@ cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStre
     return launch_chunked(a, batch, nfields, s);
   }
   const bool split = layout == 4 || (layout == 0 && 2 * nfields * batch <= sms);
-  cudaError_t e = launch_mode_mv<false>(a, batch, nfields, s, !split);   // h = Linv g
+  cudaError_t e = launch_mode_mv<false>(a, batch, nfields, s, mv_per_warp(a, batch, nfields));   // h = Linv g
   if (e != cudaSuccess) return e;
   a.g = a.h;
   a.g_stride = a.h_stride;
