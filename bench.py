@@ -50,12 +50,14 @@ def algorithmic(M, nr):
     return step_flops, step_bytes, chain_flops, chain_bytes
 
 
-def kernel_algorithmic(name, M, nr, nch):
+def kernel_algorithmic(name, M, nr, nch, layout=3):
     """Algorithmic FP64 flops and bytes of ONE launch of a step kernel for one shell (one IMEX step),
-    P = 3M/2 grid points, nch chunks per chain (chunked layout):
+    P = 3M/2 grid points, nch chunks per chain (chunked layouts 2 and 3), np = (nch-1)(nch-2)/2:
       k_chain         the chain steps: flops 8 M nr^2 (psi [A B] 2nr x nr, T and S Linv nr x nr per mode),
-                      bytes 32 M nr^2 (those matrices) + 48 M nr (h in, f out)
-      k_chain_carry   (nch-2) carried matvecs per chain: flops 24 (nch-2) nr^2, bytes 96 (nch-2) nr^2
+                      bytes 32 M nr^2 (those matrices) + 48 M nr (h in, f out); under layout 2 plus the
+                      sequential carry run by the last chunk: (nch-2) carried matvecs per chain, flops
+                      24 (nch-2) nr^2, bytes 96 (nch-2) nr^2
+      k_chain_carry   layout 3: the np products per chain at once, flops 24 np nr^2, bytes 96 np nr^2
       k_mode_mv(h)    h = Linv g: flops 6 M nr^2, bytes 24 M nr^2 + 48 M nr
       k_mode_mv(fix)  f += G s: flops 8 M nr^2 (nch-1)/nch, bytes 32 M nr^2 (nch-1)/nch + 48 M nr
       k_fx_deriv      4 radial contractions: flops 8 M nr^2, bytes 56 M nr
@@ -67,9 +69,11 @@ def kernel_algorithmic(name, M, nr, nch):
     P = 3 * M // 2
     lg = math.log2(P)
     f = (nch - 1) / nch if nch > 0 else 0.0
+    npr = (nch - 1) * (nch - 2) // 2 if nch > 2 else 0
+    seq = max(nch - 2, 0) if layout == 2 else 0
     table = {
-        "k_chain": (8 * M * nr ** 2, 32 * M * nr ** 2 + 48 * M * nr),
-        "k_chain_carry": (24 * max(nch - 2, 0) * nr ** 2, 96 * max(nch - 2, 0) * nr ** 2),
+        "k_chain": (8 * M * nr ** 2 + 24 * seq * nr ** 2, 32 * M * nr ** 2 + 48 * M * nr + 96 * seq * nr ** 2),
+        "k_chain_carry": (24 * npr * nr ** 2, 96 * npr * nr ** 2),
         "k_mode_mv(h)": (6 * M * nr ** 2, 24 * M * nr ** 2 + 48 * M * nr),
         "k_mode_mv(fix)": (8 * M * nr ** 2 * f, 32 * M * nr ** 2 * f + 48 * M * nr),
         "k_fx_deriv": (8 * M * nr ** 2, 56 * M * nr),
@@ -430,7 +434,8 @@ def bench_gb300(args):
         traffic = tr.get(dom)
     except (OSError, ValueError):
         pass
-    kflops, kbytes = kernel_algorithmic(dom, M, nr, plan.chunks())
+    lay, _, nch_used = plan.chain_choice(1)
+    kflops, kbytes = kernel_algorithmic(dom, M, nr, nch_used, lay)
     dom_s = kavg[dom] * 1e-3
     achieved_gbs = kbytes / dom_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",

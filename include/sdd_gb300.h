@@ -95,10 +95,15 @@ int sdd_plan_destroy(sdd_plan* plan);
 /* Pre-allocates the plan's workspace for up to max_batch shells (otherwise grown on first use). */
 int sdd_plan_reserve(sdd_plan* plan, int max_batch);
 /* Chain-kernel layout of the implicit solves: 0 automatic (chunked while its CTAs fit the GPU at two per
- * SM, else split rows over 4 warps when the launch leaves SMs idle, else one lane per row), 1 one lane
- * per row, 2 chunked (each chain cut into chunks that run concurrently, joined by a short carried-state
- * recurrence), 4 split rows over 4 warps.  Set by the batch autotuner; no counterpart in the reference. */
+ * SM, layout 3 before 2, else split rows over 4 warps when the launch leaves SMs idle, else one lane per
+ * row), 1 one lane per row, 2 chunked (each chain cut into chunks that run concurrently, joined by a
+ * short sequential carried-state recurrence), 3 chunked with shorter chunks joined by a parallel carry
+ * (precomputed products of the chunk maps, all applied at once), 4 split rows over 4 warps.  Set by the
+ * batch autotuner; no counterpart in the reference. */
 int sdd_plan_set_chain_layout(sdd_plan* plan, int layout);
+/* The layout (1-4) a step of `batch` shells runs under the current setting, with its chunk length and
+ * chunks per chain (0 and 1 when not chunked). */
+int sdd_plan_chain_choice(const sdd_plan* plan, int batch, int* layout, int* kc, int* nch);
 /* Nonlinear-term kernel choice: 0 automatic (split while the fused kernel's nr*batch CTAs would fill
  * under half the SMs), 1 the fused row kernel (one CTA per radial row), 2 split (7 CTAs per radial row:
  * five paired inverse transforms, then two paired forward transforms).  Results are identical bit for

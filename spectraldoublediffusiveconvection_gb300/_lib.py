@@ -81,6 +81,7 @@ SIGNATURES = [
     ("sdd_plan_reserve", _I, [_VP, _I]),
     ("sdd_plan_set_chain_layout", _I, [_VP, _I]),
     ("sdd_plan_set_fx_split", _I, [_VP, _I]),
+    ("sdd_plan_chain_choice", _I, [_VP, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("sdd_plan_base_cache_elems", ctypes.c_size_t, [_VP]),
     ("sdd_nlin_fx", _I, [_VP, _I, _VP, _VP, _VP, _VP]),
     ("sdd_nlin_dfx", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP]),

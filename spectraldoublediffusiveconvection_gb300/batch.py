@@ -144,7 +144,7 @@ class ShellBatch:
         torch.cuda.synchronize(self.device)
         return (time.perf_counter() - t0) / reps
 
-    def autotune(self, steps_per_launch=5, reps=3, layouts=(1, 2, 4), fx_modes=(1, 2)):
+    def autotune(self, steps_per_launch=5, reps=3, layouts=(1, 2, 3, 4), fx_modes=(1, 2)):
         """Greedy per-group choice of the chain layout, then of the nonlinear-term kernel (fused or split),
         minimising the time of one graph launch.  The shells' states are restored afterwards: tuning does
         not advance them."""

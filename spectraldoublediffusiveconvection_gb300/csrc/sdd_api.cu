@@ -114,11 +114,14 @@ struct sdd_plan {
   double *LinvA4, *LinvT, *LinvS;
   double *ABA4;                     // transposed [A_j B_j] of the psi chain
   double *coefA4, *coefT, *coefS;   // per-step scalars of the chains
-  // chunked chains (layout 2): chunk length, chunk count, leading dimensions and tables
-  int kc, nch, ldmA, ldmT, ldd;
-  double *GA4, *GT, *GS, *PhiA4, *PhiT, *PhiS;
-  double *dbuf, *cbuf;              // [B][3][2][nch][ldd] chunk end states / carried states
-  int* dcnt;                        // [B][6] chunk counters of the chunked chains
+  // chunked chains: cs[0] the chunking of layout 2 (sequential carry), cs[1] of layout 3 (parallel
+  // carry); leading dimensions; workspaces sized for the larger chunk and product counts
+  ChunkSet cs[2];
+  int ldmA, ldmT, ldd, nch_alloc, np_alloc;
+  double *dbuf, *cbuf;              // [B][3][2][nch_alloc][ldd] chunk end states / carried states
+  int* dcnt;                        // [B][6] chunk counters of the sequential carry
+  double* pbuf;                     // [B][6][np_alloc][ldd] products of the parallel carry
+  int* pcnt;                        // [B][6][nch_alloc] row counters of the parallel carry
   // FP32 copies used by the mixed-precision nonlinear term
   float *Dr32, *D2r232, *ir4r232;
   // workspace
@@ -239,9 +242,14 @@ static void free_plan(sdd_plan* p) {
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   double* d[] = {p->Dr, p->D2r2, p->ir4r2, p->D2s, p->ir2s, p->D2A4, p->ir2A4, p->ir4A4, p->rsq, p->dT0,
                  p->gr, p->LinvA4, p->LinvT, p->LinvS, p->out4, p->rhs, p->xtmp, p->coefA4, p->coefT, p->coefS, p->ABA4, p->hbuf,
-                 p->GA4, p->GT, p->GS, p->PhiA4, p->PhiT, p->PhiS, p->dbuf, p->cbuf,
+                 p->dbuf, p->cbuf, p->pbuf,
                  p->dg_ir, p->dg_tw, p->dg_wr, p->dg_nuw, p->dg_part, p->dg_out};
   for (double* x : d) cudaFree(x);
+  for (ChunkSet& c : p->cs) {
+    const double* t[] = {c.GA4, c.GT, c.GS, c.PhiA4, c.PhiT, c.PhiS, c.PA4, c.PT, c.PS};
+    for (const double* x : t) cudaFree(const_cast<double*>(x));
+  }
+  cudaFree(p->pcnt);
   cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232);
   cudaFree(p->base_tmp);
   cudaFree(p->gridbuf);
@@ -271,17 +279,49 @@ static void matmul_rows(const double* A, const double* B, double* C, int n, int 
   }
 }
 
-static int build_chunk_tables(sdd_plan* p, const double* AB, const double* LinvT, const double* LinvS,
-                              const double* cA, const double* cT, const double* cS) {
+// Products of the parallel carry: P_{j,i} = Phi_{j-1} ... Phi_{i+1} for 2 <= j < nch, 0 <= i <= j-2,
+// built as P_{j,j-2} = Phi_{j-1}, P_{j,i} = Phi_{j-1} P_{j-1,i}; stored transposed like Phi, row j after
+// row j-1.  PhiT holds the Phi_c of both parities ([par][c][m cols][ldm]).
+static void carry_products(const std::vector<double>& PhiT, int nch, int m, int ldm, std::vector<double>& out) {
+  const int np = (nch - 1) * (nch - 2) / 2;
+  const size_t blk = (size_t)m * ldm;
+  out.assign((size_t)2 * std::max(np, 1) * blk, 0.0);
+  std::vector<double> Phi((size_t)m * m), Q((size_t)m * m), R((size_t)m * m);
+  std::vector<std::vector<double>> prev, cur;   // row-major P_{j-1,i}, P_{j,i}
+  for (int par = 0; par < 2; ++par) {
+    prev.clear();
+    for (int j = 2; j < nch; ++j) {
+      const double* src = PhiT.data() + ((size_t)par * nch + (j - 1)) * blk;   // Phi_{j-1}, transposed
+      for (int i = 0; i < m; ++i)
+        for (int col = 0; col < m; ++col) Phi[(size_t)i * m + col] = src[(size_t)col * ldm + i];
+      cur.assign(j - 1, std::vector<double>());
+      for (int i = 0; i <= j - 2; ++i) {
+        if (i == j - 2) {
+          cur[i] = Phi;
+        } else {
+          cur[i].resize((size_t)m * m);
+          matmul_rows(Phi.data(), prev[i].data(), cur[i].data(), m, m, m);
+        }
+        double* dst = out.data() + ((size_t)par * np + (size_t)(j - 1) * (j - 2) / 2 + i) * blk;
+        for (int r = 0; r < m; ++r)
+          for (int col = 0; col < m; ++col) dst[(size_t)col * ldm + r] = cur[i][(size_t)r * m + col];
+      }
+      prev.swap(cur);
+    }
+  }
+}
+
+// One chunking of the three chains' tables (see matmul_rows above for G and Phi): products for the
+// parallel carry (layout 3), else the per-chunk maps Phi_c (layout 2).
+static int build_chunk_set(sdd_plan* p, int kc, bool products, const double* AB, const double* LinvT,
+                           const double* LinvS, const double* cA, const double* cT, const double* cS,
+                           ChunkSet* cs) {
   const int M = p->M, nr = p->nr, ldl = p->ldl, S = M / 2;
-  int kc = (int)std::lround(std::sqrt(2.0 * S));
-  kc = std::max(4, std::min(32, kc));
   const int nch = (S + kc - 1) / kc;
-  p->kc = kc;
-  p->nch = nch;
-  p->ldmA = 2 * nr;
-  p->ldmT = nr + (nr & 1);
-  p->ldd = 2 * nr;
+  cs->kc = kc;
+  cs->nch = nch;
+  cs->np = products ? (nch - 1) * (nch - 2) / 2 : 0;
+  std::vector<double> Pr;
   {  // psi
     const int m = 2 * nr, ldm = p->ldmA;
     std::vector<double> G((size_t)M * m * ldl, 0.0), Phi((size_t)2 * nch * m * ldm, 0.0);
@@ -312,7 +352,18 @@ static int build_chunk_tables(sdd_plan* p, const double* AB, const double* LinvT
               Phi[(((size_t)par * nch + c) * m + col) * ldm + i] = Psi[(size_t)i * m + col];
       }
     int st;
-    if ((st = upload(&p->GA4, G.data(), G.size())) || (st = upload(&p->PhiA4, Phi.data(), Phi.size()))) return st;
+    double* g = nullptr;
+    double* t = nullptr;
+    if ((st = upload(&g, G.data(), G.size()))) return st;
+    cs->GA4 = g;
+    if (products) {
+      carry_products(Phi, nch, m, ldm, Pr);
+      if ((st = upload(&t, Pr.data(), Pr.size()))) return st;
+      cs->PA4 = t;
+    } else {
+      if ((st = upload(&t, Phi.data(), Phi.size()))) return st;
+      cs->PhiA4 = t;
+    }
   }
   for (int fld = 1; fld <= 2; ++fld) {  // T, S
     const int m = nr, ldm = p->ldmT;
@@ -340,10 +391,42 @@ static int build_chunk_tables(sdd_plan* p, const double* AB, const double* LinvT
               Phi[(((size_t)par * nch + c) * m + col) * ldm + i] = Psi[(size_t)i * m + col];
       }
     int st;
-    double** gd = fld == 1 ? &p->GT : &p->GS;
-    double** pd = fld == 1 ? &p->PhiT : &p->PhiS;
-    if ((st = upload(gd, G.data(), G.size())) || (st = upload(pd, Phi.data(), Phi.size()))) return st;
+    double* g = nullptr;
+    double* t = nullptr;
+    if ((st = upload(&g, G.data(), G.size()))) return st;
+    (fld == 1 ? cs->GT : cs->GS) = g;
+    if (products) {
+      carry_products(Phi, nch, m, ldm, Pr);
+      if ((st = upload(&t, Pr.data(), Pr.size()))) return st;
+      (fld == 1 ? cs->PT : cs->PS) = t;
+    } else {
+      if ((st = upload(&t, Phi.data(), Phi.size()))) return st;
+      (fld == 1 ? cs->PhiT : cs->PhiS) = t;
+    }
   }
+  return SDD_OK;
+}
+
+// Chunk lengths.  Layout 2 (sequential carry: kc local steps, then nch - 2 carried matvecs of twice the
+// width, on one SM per chain): kc ~ sqrt(2S).  Layout 3 (parallel carry: kc local steps, then all
+// (nch-1)(nch-2)/2 products at once, spread over the GPU): kc ~ sqrt(S/2), shorter chunks.
+static int chunk_len(int S, int layout) {
+  const double k = layout == 3 ? std::sqrt(0.5 * S) : std::sqrt(2.0 * S);
+  return std::max(layout == 3 ? 2 : 4, std::min(layout == 3 ? 16 : 32, (int)std::lround(k)));
+}
+
+static int build_chunk_tables(sdd_plan* p, const double* AB, const double* LinvT, const double* LinvS,
+                              const double* cA, const double* cT, const double* cS) {
+  const int S = p->M / 2, nr = p->nr;
+  p->ldmA = 2 * nr;
+  p->ldmT = nr + (nr & 1);
+  p->ldd = 2 * nr;
+  int st;
+  if ((st = build_chunk_set(p, chunk_len(S, 2), false, AB, LinvT, LinvS, cA, cT, cS, &p->cs[0])) ||
+      (st = build_chunk_set(p, chunk_len(S, 3), true, AB, LinvT, LinvS, cA, cT, cS, &p->cs[1])))
+    return st;
+  p->nch_alloc = std::max(p->cs[0].nch, p->cs[1].nch);
+  p->np_alloc = std::max(p->cs[1].np, 1);
   return SDD_OK;
 }
 
@@ -494,9 +577,21 @@ int sdd_plan_set_fx_split(sdd_plan* p, int mode) {
 }
 
 int sdd_plan_set_chain_layout(sdd_plan* p, int layout) {
-  if (!p || (layout != 0 && layout != 1 && layout != 2 && layout != 4)) return SDD_ERR_ARG;
+  if (!p || layout < 0 || layout > 4) return SDD_ERR_ARG;
   if (p->chain_layout != layout) clear_step_graphs(p);
   p->chain_layout = layout;
+  return SDD_OK;
+}
+
+static ChainArgs chain_args(const sdd_plan* p, const double* g, double* f, const double* sub);
+
+int sdd_plan_chain_choice(const sdd_plan* p, int batch, int* layout, int* kc, int* nch) {
+  if (!p || batch < 1 || !layout || !kc || !nch) return SDD_ERR_ARG;
+  const ChainArgs a = chain_args(p, nullptr, nullptr, nullptr);
+  *layout = resolve_chain_layout(a, batch, 3);
+  const bool chunked = *layout == 2 || *layout == 3;
+  *kc = chunked ? p->cs[*layout - 2].kc : 0;
+  *nch = chunked ? p->cs[*layout - 2].nch : 1;
   return SDD_OK;
 }
 
@@ -510,9 +605,10 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   clear_step_graphs(p);   // the graphs bake in the workspace pointers
   cudaFree(p->out4); cudaFree(p->rhs); cudaFree(p->xtmp); cudaFree(p->base_tmp); cudaFree(p->hbuf);
   cudaFree(p->dbuf); cudaFree(p->cbuf); cudaFree(p->gridbuf); cudaFree(p->derivbuf);
-  cudaFree(p->dg_part); cudaFree(p->dg_out); cudaFree(p->dcnt);
+  cudaFree(p->dg_part); cudaFree(p->dg_out); cudaFree(p->dcnt); cudaFree(p->pbuf); cudaFree(p->pcnt);
   p->dg_part = p->dg_out = nullptr;
-  p->dcnt = nullptr;
+  p->dcnt = p->pcnt = nullptr;
+  p->pbuf = nullptr;
   p->out4 = p->rhs = p->xtmp = p->hbuf = p->dbuf = p->cbuf = nullptr;
   p->base_tmp = p->gridbuf = p->derivbuf = nullptr;
   p->ws_batch = 0;
@@ -529,9 +625,12 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   SDD_CUDA(cudaMalloc(&p->dg_out, (size_t)max_batch * 4 * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->dcnt, (size_t)max_batch * 6 * sizeof(int)));
   SDD_CUDA(cudaMemset(p->dcnt, 0, (size_t)max_batch * 6 * sizeof(int)));
-  const size_t de = (size_t)6 * p->nch * p->ldd;
+  const size_t de = (size_t)6 * p->nch_alloc * p->ldd;
   SDD_CUDA(cudaMalloc(&p->dbuf, (size_t)max_batch * de * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->cbuf, (size_t)max_batch * de * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->pbuf, (size_t)max_batch * 6 * p->np_alloc * p->ldd * sizeof(double)));
+  SDD_CUDA(cudaMalloc(&p->pcnt, (size_t)max_batch * 6 * p->nch_alloc * sizeof(int)));
+  SDD_CUDA(cudaMemset(p->pcnt, 0, (size_t)max_batch * 6 * p->nch_alloc * sizeof(int)));
   p->ws_batch = max_batch;
   return SDD_OK;
 }
@@ -589,10 +688,13 @@ static ChainArgs chain_args(const sdd_plan* p, const double* g, double* f, const
   a.h_stride = shell_elems(p);
   a.coefA4 = p->coefA4; a.coefT = p->coefT; a.coefS = p->coefS;
   a.dtA4 = p->Pr * p->dt; a.dtT = p->dt; a.dtS = p->Tau * p->dt;
-  a.kc = p->kc; a.nch = p->nch; a.ldmA = p->ldmA; a.ldmT = p->ldmT; a.ldd = p->ldd;
-  a.GA4 = p->GA4; a.GT = p->GT; a.GS = p->GS; a.PhiA4 = p->PhiA4; a.PhiT = p->PhiT; a.PhiS = p->PhiS;
+  a.ldmA = p->ldmA; a.ldmT = p->ldmT; a.ldd = p->ldd;
+  a.cset[0] = p->cs[0];
+  a.cset[1] = p->cs[1];
   a.dbuf = p->dbuf; a.cbuf = p->cbuf; a.counter = p->dcnt;
-  a.d_stride = (size_t)6 * p->nch * p->ldd;
+  a.d_stride = (size_t)6 * p->nch_alloc * p->ldd;
+  a.pbuf = p->pbuf; a.pcounter = p->pcnt;
+  a.p_stride = (size_t)6 * p->np_alloc * p->ldd;
   return a;
 }
 

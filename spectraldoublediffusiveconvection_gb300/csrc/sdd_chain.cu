@@ -198,7 +198,7 @@ __global__ void k_chain(ChainArgs a) {
       f[o] -= sub[o];
     }
   }
-  if (CHUNK && a.nch > 2) {
+  if (CHUNK && a.nch > 2 && a.carry_seq) {
     // the last chunk of this chain to finish runs the carried-state recurrence (no extra launch)
     __shared__ int s_last;
     __threadfence();                                   // this chunk's end state before the ticket
@@ -210,7 +210,7 @@ __global__ void k_chain(ChainArgs a) {
     __threadfence();
     if (tid == 0) *cnt = 0;                            // ready for the next launch
     carry_run<(TPR == 4 ? 2 : 1), CR>(a, field, par, b, csm);
-  } else if (CHUNK && a.nch == 2) {                   // s_1 = d_0 only: the chain's first chunk copies it
+  } else if (CHUNK && a.nch >= 2) {                   // s_1 = d_0: the chain's first chunk copies it
     if (chunk == 0 && lead) {
       double* cb = a.cbuf + (size_t)b * a.d_stride + ((size_t)(field * 2 + par) * a.nch + 1) * a.ldd;
       cb[i] = fe;
@@ -295,6 +295,70 @@ __device__ void carry_run(const ChainArgs& a, int field, int par, int b, double*
     }
   }
   cp_async_wait<0>();
+}
+
+// y = P x for one m x m block P (transposed, leading dimension ldm) read through L2, x in shared memory;
+// rows over 128/TPR lanes groups, columns split over the TPR lanes of a group.
+template <int TPR>
+__device__ __forceinline__ void block_mv(const double* P, int ldm, const double* x, int m, double* y) {
+  const int q = threadIdx.x % TPR;
+  for (int r0 = 0; r0 < m; r0 += 128 / TPR) {
+    const int r = r0 + threadIdx.x / TPR;
+    const int rr = r < m ? r : 0;
+    double acc = 0.0;
+#pragma unroll 8
+    for (int col = q; col < m; col += TPR) acc = fma(__ldg(P + (size_t)col * ldm + rr), x[col], acc);
+    acc = group_sum<TPR>(acc);
+    if (r < m && q == 0) y[r] = acc;
+  }
+}
+
+// Parallel carry of the chunked chains (layout 3).  One CTA of 128 threads per (chain, shell, product
+// (j, i)), i <= j - 2: part_{j,i} = P_{j,i} d_i.  The last CTA of row j to finish (atomic ticket) forms
+//   s_j = d_{j-1} + part_{j,0} + part_{j,1} + ... + part_{j,j-2}
+// in that order (the same bits whichever CTA finishes last) and writes it to cbuf slot j; s_1 = d_0 is
+// written by the chain's first chunk.  Exact algebra of s_{c+1} = Phi_c s_c + d_c.
+__global__ void __launch_bounds__(128) k_carry_par(ChainArgs a) {
+  __shared__ double xs[2 * kMaxNr];
+  __shared__ int s_last;
+  const int field = a.field0 + (blockIdx.x >> 1), par = blockIdx.x & 1;
+  const int b = blockIdx.y, pidx = blockIdx.z;
+  const bool a4 = field == 0;
+  if (a.sym && !(a4 ? par == 0 : par == 1)) return;    // inactive chain: its carried states are not read
+  int j = 2;
+  while (j * (j - 1) / 2 <= pidx) ++j;                 // row j holds products (j-1)(j-2)/2 .. j(j-1)/2 - 1
+  const int i = pidx - (j - 1) * (j - 2) / 2;
+  const int m = a4 ? 2 * a.nr : a.nr;
+  const int ldm = a4 ? a.ldmA : a.ldmT;
+  const size_t chain = (size_t)(field * 2 + par);
+  const double* d = a.dbuf + (size_t)b * a.d_stride + chain * a.nch * a.ldd;
+  double* part = a.pbuf + (size_t)b * a.p_stride + chain * a.np * a.ldd;
+  const double* P = (a4 ? a.PA4 : (field == 1 ? a.PT : a.PS)) + ((size_t)par * a.np + pidx) * m * ldm;
+  for (int e = threadIdx.x; e < m; e += blockDim.x) xs[e] = d[(size_t)i * a.ldd + e];
+  __syncthreads();
+  double* y = part + (size_t)pidx * a.ldd;
+  if (a4) {
+    if (m <= 64) block_mv<2>(P, ldm, xs, m, y);
+    else block_mv<1>(P, ldm, xs, m, y);
+  } else {
+    if (m <= 32) block_mv<4>(P, ldm, xs, m, y);
+    else block_mv<2>(P, ldm, xs, m, y);
+  }
+  __threadfence();                                     // this product before the ticket
+  __syncthreads();
+  int* cnt = a.pcounter + ((size_t)b * 6 + chain) * a.nch + j;
+  if (threadIdx.x == 0) s_last = (atomicAdd(cnt, 1) == j - 2);
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  if (threadIdx.x == 0) *cnt = 0;                      // ready for the next launch
+  const double* row = part + (size_t)((j - 1) * (j - 2) / 2) * a.ldd;
+  double* cb = a.cbuf + (size_t)b * a.d_stride + (chain * a.nch + j) * a.ldd;
+  for (int e = threadIdx.x; e < m; e += blockDim.x) {
+    double v = __ldcg(d + (size_t)(j - 1) * a.ldd + e);
+    for (int k = 0; k <= j - 2; ++k) v += __ldcg(row + (size_t)k * a.ldd + e);
+    cb[e] = v;
+  }
 }
 
 // g of mode `row` for the fused right-hand side, element n (see ChainArgs::fuse_rhs): the roundings of
@@ -468,6 +532,27 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
   ChainArgs a = a_in;
   a.g = a.h;
   a.g_stride = a.h_stride;
+  if (!a.carry_seq) {   // layout 3: chunks, then the products in parallel, then the corrections
+    const dim3 grid(2 * nfields, batch, a.nch);
+    const size_t smem = chunk_smem_bytes(a.kc, a.nr, a.ldl);
+    if (a.nr <= 32) {
+      static unsigned long long done = 0;
+      if ((e = ensure_smem_attr(k_chain<4, true, 0>, &done)) != cudaSuccess) return e;
+      if ((e = launch_kernel(k_chain<4, true, 0>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e;
+    } else {
+      static unsigned long long done = 0;
+      if ((e = ensure_smem_attr(k_chain<2, true, 0>, &done)) != cudaSuccess) return e;
+      if ((e = launch_kernel(k_chain<2, true, 0>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e;
+    }
+    ktimer_mark(SDD_K_CHAIN, s);
+    if (a.nch < 2) return cudaSuccess;
+    if (a.np > 0) {
+      if ((e = launch_kernel(k_carry_par, dim3(2 * nfields, batch, a.np), dim3(128), 0, s, a)) != cudaSuccess)
+        return e;
+      ktimer_mark(SDD_K_CHAIN_CARRY, s);
+    }
+    return launch_mode_mv<true>(a, batch, nfields, s, pw);
+  }
   // the carry ring of the psi chain (m = 2 nr) decides the ring depth for all fields of the launch
   const int mmax = a.field0 == 0 ? 2 * a.nr : a.nr;
   const int ldmax = a.field0 == 0 ? a.ldmA : a.ldmT;
@@ -503,8 +588,7 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
 // carried-state recurrence and a parallel correction) is chosen automatically while all its CTAs fit
 // on the GPU at two per SM.  a.g holds the right-hand sides; a.h receives h = Linv g (k_mode_mv), which
 // is what the chains read.
-cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStream_t s) {
-  ChainArgs a = a_in;
+int resolve_chain_layout(const ChainArgs& a, int batch, int nfields) {
   const int sms = sm_count();
   static const int optin = [] {
     int dev = 0, n = 0;
@@ -513,13 +597,32 @@ cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStre
     return n;
   }();
   int layout = a.layout;
-  if (layout == 0 && a.nch > 1 && a.GA4 && 2 * nfields * batch * a.nch <= 2 * sms) layout = 2;
-  if (layout != 2 && chain_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin) layout = 2;  // whole chain too long
-  if (layout == 2) {
-    if (!a.GA4 || a.kc < 1 || a.nch < 1) return cudaErrorInvalidValue;
+  const ChunkSet& c2 = a.cset[0];
+  const ChunkSet& c3 = a.cset[1];
+  if (layout == 0 && c3.nch > 1 && c3.GA4 && 2 * nfields * batch * c3.nch <= 2 * sms) layout = 3;
+  if (layout == 0 && c2.nch > 1 && c2.GA4 && 2 * nfields * batch * c2.nch <= 2 * sms) layout = 2;
+  if (layout != 2 && layout != 3 && chain_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin)
+    layout = 2;   // whole chain too long for shared memory
+  if (layout == 0) layout = 2 * nfields * batch <= sms ? 4 : 1;
+  return layout;
+}
+
+cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStream_t s) {
+  ChainArgs a = a_in;
+  const int layout = resolve_chain_layout(a, batch, nfields);
+  const ChunkSet& c2 = a.cset[0];
+  const ChunkSet& c3 = a.cset[1];
+  if (layout == 2 || layout == 3) {
+    const ChunkSet& c = layout == 3 ? c3 : c2;
+    if (!c.GA4 || c.kc < 1 || c.nch < 1) return cudaErrorInvalidValue;
+    a.kc = c.kc; a.nch = c.nch; a.np = c.np;
+    a.GA4 = c.GA4; a.GT = c.GT; a.GS = c.GS;
+    a.PhiA4 = c.PhiA4; a.PhiT = c.PhiT; a.PhiS = c.PhiS;
+    a.PA4 = c.PA4; a.PT = c.PT; a.PS = c.PS;
+    a.carry_seq = layout == 2;
     return launch_chunked(a, batch, nfields, s);
   }
-  const bool split = layout == 4 || (layout == 0 && 2 * nfields * batch <= sms);
+  const bool split = layout == 4;
   cudaError_t e = launch_mode_mv<false>(a, batch, nfields, s, mv_per_warp(a, batch, nfields));   // h = Linv g
   if (e != cudaSuccess) return e;
   a.g = a.h;

@@ -140,10 +140,21 @@ struct FxArgs {
 
 
 
+// Tables of one chunking of the chains (see k_chain): chunk length kc, nch chunks per chain, the
+// corrections G_jj of every mode and the carried-state maps, either per chunk (Phi_c, the sequential
+// carry of layout 2) or as the products P_{j,i} = Phi_{j-1} ... Phi_{i+1}, i <= j - 2 (np per chain,
+// row j after row j-1; the parallel carry of layout 3).
+struct ChunkSet {
+  int kc, nch, np;
+  const double* GA4, *GT, *GS;        // [M][m cols][ldl] transposed G_jj (m = 2 nr for psi, nr for T/S)
+  const double* PhiA4, *PhiT, *PhiS;  // [2 parity][nch][m cols][ldm] transposed Phi_c
+  const double* PA4, *PT, *PS;        // [2 parity][np][m cols][ldm] transposed P_{j,i}
+};
+
 struct ChainArgs {
   int M, nr, ldl, sym;
   int field0;                // first field handled (blockIdx.x/2 + field0)
-  int layout;                // 1 one lane per row, 4 rows split over 4 warps, 2 chunked (resolved by the host)
+  int layout;                // 1 one lane per row, 4 rows split over 4 warps, 2/3 chunked (resolved by the host)
   size_t field_off;          // doubles between field blocks (N_fm*nr, or 0 when g/f point at one block)
   const double* g;           // rhs [shell][3][M][nr]
   size_t g_stride;
@@ -179,6 +190,16 @@ struct ChainArgs {
   double* cbuf;              // [shell][3][2][nch][ldd] carried states at the chunk starts (c >= 1)
   size_t d_stride;           // doubles per shell in dbuf / cbuf
   int* counter;              // [shell][6] chunks finished per chain (the last one runs the carry), zeroed
+  // layout 3 (parallel carry): the chunks only write their end states; k_carry_par forms
+  // part_{j,i} = P_{j,i} d_i for every product in parallel and the last CTA of row j sums
+  // s_j = d_{j-1} + sum_i part_{j,i} (index order) into cbuf
+  int carry_seq;             // 1: the last-finishing chunk CTA runs the sequential carry (layout 2)
+  int np;                    // products per chain
+  const double* PA4, *PT, *PS;
+  double* pbuf;              // [shell][6][np][ldd] products P_{j,i} d_i
+  size_t p_stride;           // doubles per shell in pbuf
+  int* pcounter;             // [shell][6][nch] products finished per row j, zeroed
+  ChunkSet cset[2];          // the chunkings of layouts 2 and 3 (launch_chain copies one into the fields above)
 };
 
 struct DiagArgs {
@@ -206,6 +227,8 @@ cudaError_t launch_fx(const FxArgs& a, int batch, int mode, int prec, cudaStream
 bool fx_uses_split(const FxArgs& a, int batch, int mode);
 cudaError_t launch_rhs(const RhsArgs& a, int batch, cudaStream_t s);
 cudaError_t launch_chain(const ChainArgs& a, int batch, int nfields, cudaStream_t s);
+// the chain layout (1, 2, 3 or 4) launch_chain runs for a.layout (0 = automatic) and this launch size
+int resolve_chain_layout(const ChainArgs& a, int batch, int nfields);
 cudaError_t launch_theta_op(int op, int M, int nr, int sym, const double* D2, const double* ir,
                             const double* dT0, const double* g, double* f, int batch,
                             cudaStream_t s);

@@ -128,7 +128,8 @@ class Plan:
             _lib.check(self._L.sdd_plan_reserve(self._h, int(batch)), "sdd_plan_reserve")
 
     def set_chain_layout(self, layout):
-        """0 automatic, 1 one lane per row, 2 chunked, 4 rows split over 4 warps (sdd_plan_set_chain_layout)."""
+        """0 automatic, 1 one lane per row, 2 chunked (sequential carry), 3 chunked (parallel carry), 4 rows
+        split over 4 warps (sdd_plan_set_chain_layout); the results agree to rounding."""
         _lib.check(self._L.sdd_plan_set_chain_layout(self._h, int(layout)), "sdd_plan_set_chain_layout")
         self.chain_layout = int(layout)
 
@@ -236,12 +237,16 @@ class Plan:
                                          int(bool(linear)), _dptr(dg), _stream(self.device)), "sdd_step_diag")
         return out, dg
 
-    def chunks(self):
-        """Chunks per chain of the chunked layout: kc = clamp(round(sqrt(N_fm)), 4, 32) steps each."""
-        import math
-        S = self.N_fm // 2
-        kc = max(4, min(32, int(math.floor(math.sqrt(2.0 * S) + 0.5))))
-        return (S + kc - 1) // kc
+    def chain_choice(self, batch=1):
+        """(layout, kc, nch) that a step of ``batch`` shells runs its chains with (sdd_plan_chain_choice)."""
+        lay, kc, nch = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _lib.check(self._L.sdd_plan_chain_choice(self._h, int(batch), ctypes.byref(lay), ctypes.byref(kc),
+                                                 ctypes.byref(nch)), "sdd_plan_chain_choice")
+        return lay.value, kc.value, nch.value
+
+    def chunks(self, batch=1):
+        """Chunks per chain of the chains a step of ``batch`` shells runs (1 when not chunked)."""
+        return self.chain_choice(batch)[2]
 
     def kernel_profile(self, X, Ra, Ra_s, nsteps):
         """{kernel name: (total milliseconds, launches)} over nsteps steps from X, with a CUDA event after

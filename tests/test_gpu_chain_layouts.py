@@ -1,7 +1,8 @@
-"""Every chain layout of the implicit solves (1 one lane per row, 2 chunked, 4 split rows) against the
-oracle's A4_BSub_TSTEP_V2 / NAB2_BSub_TSTEP_V2 chains (Matrix_Operators.py:1033-1194), alone and inside
-the step, the Newton residual and its Jacobian.  The chunked layout reorders the arithmetic (carried
-states through precomputed chunk maps), so it agrees with the sequential chain to rounding, not bitwise."""
+"""Every chain layout of the implicit solves (1 one lane per row, 2 chunked with a sequential carry, 3
+chunked with a parallel carry, 4 split rows) against the oracle's A4_BSub_TSTEP_V2 / NAB2_BSub_TSTEP_V2
+chains (Matrix_Operators.py:1033-1194), alone and inside the step, the Newton residual and its Jacobian.
+The chunked layouts reorder the arithmetic (carried states through precomputed chunk maps or their
+products), so they agree with the sequential chain to rounding, not bitwise."""
 import numpy as np
 import pytest
 
@@ -14,7 +15,7 @@ SHAPES = [(16, 16, False), (20, 64, False), (30, 256, False), (48, 512, False), 
 
 
 @pytest.mark.parametrize("N_r,N_fm,sym", SHAPES)
-@pytest.mark.parametrize("layout", [1, 2, 4])
+@pytest.mark.parametrize("layout", [1, 2, 3, 4])
 def test_chain_solves_against_oracle(cuda, N_r, N_fm, sym, layout):
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     torch = cuda
@@ -38,8 +39,9 @@ def test_chain_solves_against_oracle(cuda, N_r, N_fm, sym, layout):
         assert rel(fs[k], rs) < 1e-13
 
 
+@pytest.mark.parametrize("layout", [2, 3])
 @pytest.mark.parametrize("N_r,N_fm", [(20, 64), (30, 256), (48, 512)])
-def test_chunked_step_newton_operators_against_oracle(cuda, N_r, N_fm):
+def test_chunked_step_newton_operators_against_oracle(cuda, N_r, N_fm, layout):
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     torch = cuda
     nr = N_r - 1
@@ -49,7 +51,7 @@ def test_chunked_step_newton_operators_against_oracle(cuda, N_r, N_fm):
     dvt = torch.from_numpy(np.stack([dv, dv])).cuda()
     ops = O.Operators(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01)
     p = Plan(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01)
-    p.set_chain_layout(2)
+    p.set_chain_layout(layout)
     Y = p.step(Xt, 8000.0, 500.0, nsteps=3).cpu().numpy()
     for k, x in enumerate([X, 2 * X]):
         r = x
@@ -58,7 +60,7 @@ def test_chunked_step_newton_operators_against_oracle(cuda, N_r, N_fm):
         assert rel(Y[k], r) < 1e-12
     ops1 = O.Operators(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
     p1 = Plan(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
-    p1.set_chain_layout(2)
+    p1.set_chain_layout(layout)
     F = p1.pfx(Xt, 8000.0, 500.0).cpu().numpy()
     J = p1.pdfx(dvt, Xt, 8000.0, 500.0).cpu().numpy()
     for k, x in enumerate([X, 2 * X]):
@@ -66,13 +68,14 @@ def test_chunked_step_newton_operators_against_oracle(cuda, N_r, N_fm):
         assert rel(J[k], O.PDFX(ops1, dv, x, 8000.0, 500.0, False)) < 1e-12
 
 
-def test_chunked_batch_equals_alone(cuda):
-    """No arithmetic crosses shells in the chunked layout either: a batch equals its shells alone."""
+@pytest.mark.parametrize("layout", [2, 3])
+def test_chunked_batch_equals_alone(cuda, layout):
+    """No arithmetic crosses shells in the chunked layouts either: a batch equals its shells alone."""
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     torch = cuda
     N_fm, N_r = 128, 24
     p = Plan(N_fm, N_r, 2.0, 1e-3, 1.0, 0.01)
-    p.set_chain_layout(2)
+    p.set_chain_layout(layout)
     Xs = np.stack([O.seeded_state(N_fm, N_r - 1, s) for s in range(4)])
     Ra = torch.tensor([6000.0, 8000.0, 10000.0, 12000.0], dtype=torch.float64, device="cuda")
     Xb = p.step(torch.from_numpy(Xs).cuda(), Ra, 500.0, nsteps=4)
@@ -119,7 +122,7 @@ def test_forced_nonlinear_term_paths_agree(cuda):
         p.set_fx_split(3)
 
 
-@pytest.mark.parametrize("layout", [1, 2, 4])
+@pytest.mark.parametrize("layout", [1, 2, 3, 4])
 def test_matvec_variants_agree_across_batch_sizes(cuda, layout):
     """The per-mode h = Linv g (and chunk correction) kernels switch from one matvec per CTA to one per
     warp as the batch grows (3 fields x 256 modes x 4 shells crosses the switch); both sum in the same
@@ -133,3 +136,19 @@ def test_matvec_variants_agree_across_batch_sizes(cuda, layout):
     Xb = p.step(Xs, 8000.0, 500.0, nsteps=3)
     for i in range(4):
         assert torch.equal(p.step(Xs[i:i + 1], 8000.0, 500.0, nsteps=3), Xb[i:i + 1])
+
+
+def test_automatic_layout_choice(cuda):
+    """sdd_plan_chain_choice: one production shell runs the parallel-carry chunks (layout 3, kc ~ sqrt(S/2)),
+    a batch too large for its CTAs falls back to whole chains; forced layouts are reported as set."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    p = Plan(256, 30, 2.0, 5e-4, 1.0, 0.01)
+    assert p.chain_choice(1) == (3, 8, 16)
+    lay, kc, nch = p.chain_choice(64)
+    assert lay in (1, 4) and (kc, nch) == (0, 1)
+    p.set_chain_layout(2)
+    assert p.chain_choice(1) == (2, 16, 8)
+    p.set_chain_layout(3)
+    assert p.chain_choice(64) == (3, 8, 16)
+    with pytest.raises(Exception):
+        p.set_chain_layout(5)
