@@ -132,7 +132,8 @@ struct sdd_plan {
   double* hbuf;     // [B][3][M][nr] h = Linv g of the chains
   void* base_tmp;   // [B][nr][9][P] (T precision), for DFX without a caller cache
   void* gridbuf;    // [B][nr][9][P] (T precision), grid fields of the split nonlinear-term path
-  void* derivbuf;   // [B][4][M][nr] (T precision), radial derivatives of the split path
+  void* derivbuf;   // [B] x (5 M nr doubles of room), radial derivatives of the split path: 4 M nr of the
+                    // precision, then M nr doubles (D2s psi of the fused right-hand side)
   // Krylov / Newton / continuation workspace (grown on demand)
   int sv_B, sv_m;
   double *kv_V, *kv_w, *kv_r, *kv_part, *kv_nrm2, *kv_small, *kv_dot;
@@ -656,7 +657,9 @@ static FxArgs fx_args(const sdd_plan* p, int prec, const double* X, void* base, 
   a.out4 = out4; a.out_stride = (size_t)4 * p->M * p->nr;
   a.grid = p->gridbuf; a.grid_stride = sdd_plan_base_cache_elems(p);
   a.split = p->fx_split;
-  a.deriv = p->derivbuf; a.deriv_stride = (size_t)5 * p->M * p->nr;
+  // per shell: 4 M nr elements of the precision, then M nr doubles (the fused rhs's D2s psi)
+  a.deriv = p->derivbuf;
+  a.deriv_stride = (size_t)(prec == SDD_PREC_MIXED ? 6 : 5) * p->M * p->nr;
   return a;
 }
 
@@ -709,8 +712,9 @@ static int check_plan(sdd_plan* p, int batch) {
 // One application of Phi (the step map) or its Jacobian to X (or dv), into out.
 // mode 0: FX (nonlinear term of X); 1: DFX about the base in `base`; 2: linear only.
 // Same as apply_step with explicit strides (doubles between shells) of the input X, the output and sub.
-// With the FP64 split nonlinear term, the right-hand sides are not assembled by k_rhs: the grid kernel
-// writes their linear parts and the chains' h kernel adds the nonlinear parts (same roundings).
+// With the split nonlinear term, the right-hand sides are not assembled by k_rhs: the grid kernel writes
+// their linear parts (FP64 in both precisions) and the chains' h kernel adds the nonlinear parts (same
+// roundings).
 // ev (nullable): four events recorded around the nonlinear term, the rhs and the chains.
 static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X, size_t ldx,
                          double* out, size_t ldo, const double* sub, size_t lds, int mode, void* base, int prec,
@@ -723,7 +727,7 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
     FxArgs fa = fx_args(p, prec, X, base, p->out4);
     fa.x_stride = ldx;
     const int fm = mode == 1 ? 1 : 0;
-    fuse = prec == SDD_PREC_FP64 && fx_uses_split(fa, batch, fm);
+    fuse = fx_uses_split(fa, batch, fm);
     if (fuse) {
       fa.fuse_rhs = 1;
       fa.rl = ra;

@@ -74,6 +74,25 @@ __device__ __forceinline__ void chain_sync() {
   else __syncthreads();
 }
 
+// g of mode `row` for the fused right-hand side, element n (see ChainArgs::fuse_rhs): the roundings of
+// k_rhs, psi: (-dt (Dr Q - R)) + lin, T: (-dt NT) + lin, S: (-dt NS) + lin.
+__device__ __forceinline__ double fused_g(const ChainArgs& a, int b, int field, int row, int n) {
+  const int M = a.M, nr = a.nr;
+  const size_t N = (size_t)M * nr;
+  const double* o4 = a.out4 + (size_t)b * a.out_stride;
+  double nl;
+  if (field == 0) {
+    const double* qs = o4 + (size_t)row * nr;
+    const double* drn = a.Dr + (size_t)n * nr;
+    double dq = 0.0;
+    for (int c = 0; c < nr; ++c) dq = fma(drn[c], qs[c], dq);
+    nl = __dmul_rn(-a.dt, __dsub_rn(dq, o4[N + (size_t)row * nr + n]));
+  } else {
+    nl = __dmul_rn(-a.dt, o4[(size_t)(field + 1) * N + (size_t)row * nr + n]);
+  }
+  return __dadd_rn(nl, a.lin[(size_t)b * a.g_stride + (size_t)field * a.field_off + (size_t)row * nr + n]);
+}
+
 // One chain (field, parity) of one shell: steps [s0, s1) of the S = (M - par + 1)/2 chain steps.
 // CHUNK = false: the whole chain (s0 = 0, s1 = S).  CHUNK = true: chunk blockIdx.z of a.kc steps,
 // started from a zero carried state; its end state goes to dbuf (psi: [f_e; bf_e]; T/S: b + k_next f_last,
@@ -201,14 +220,19 @@ __global__ void k_chain(ChainArgs a) {
   if (CHUNK && a.nch > 2 && a.carry_seq) {
     // the last chunk of this chain to finish runs the carried-state recurrence (no extra launch)
     __shared__ int s_last;
-    __threadfence();                                   // this chunk's end state before the ticket
-    __syncthreads();
+    __syncthreads();                                   // this chunk's end state before the ticket (see k_carry_par)
     int* cnt = a.counter + (size_t)b * 6 + (field * 2 + par);
-    if (tid == 0) s_last = (atomicAdd(cnt, 1) == a.nch - 1);
+    if (tid == 0) {
+      __threadfence();
+      const int last = atomicAdd(cnt, 1) == a.nch - 1;
+      if (last) {
+        __threadfence();
+        *cnt = 0;                                      // ready for the next launch
+      }
+      s_last = last;
+    }
     __syncthreads();
     if (!s_last) return;
-    __threadfence();
-    if (tid == 0) *cnt = 0;                            // ready for the next launch
     carry_run<(TPR == 4 ? 2 : 1), CR>(a, field, par, b, csm);
   } else if (CHUNK && a.nch >= 2) {                   // s_1 = d_0: the chain's first chunk copies it
     if (chunk == 0 && lead) {
@@ -297,8 +321,8 @@ __device__ void carry_run(const ChainArgs& a, int field, int par, int b, double*
   cp_async_wait<0>();
 }
 
-// y = P x for one m x m block P (transposed, leading dimension ldm) read through L2, x in shared memory;
-// rows over 128/TPR lanes groups, columns split over the TPR lanes of a group.
+// y = P x for one m x m block P (transposed, leading dimension ldm) and x, both in shared memory; rows
+// over 128/TPR lane groups, columns split over the TPR lanes of a group.
 template <int TPR>
 __device__ __forceinline__ void block_mv(const double* P, int ldm, const double* x, int m, double* y) {
   const int q = threadIdx.x % TPR;
@@ -307,18 +331,27 @@ __device__ __forceinline__ void block_mv(const double* P, int ldm, const double*
     const int rr = r < m ? r : 0;
     double acc = 0.0;
 #pragma unroll 8
-    for (int col = q; col < m; col += TPR) acc = fma(__ldg(P + (size_t)col * ldm + rr), x[col], acc);
+    for (int col = q; col < m; col += TPR) acc = fma(P[(size_t)col * ldm + rr], x[col], acc);
     acc = group_sum<TPR>(acc);
     if (r < m && q == 0) y[r] = acc;
   }
 }
 
+size_t carry_par_smem_bytes(int nr, int ldmA, int nch) {
+  const size_t blk = (size_t)2 * nr * ldmA;             // the largest product block (psi)
+  const size_t rows = (size_t)nch * 2 * nr;             // d_{j-1} and up to nch - 2 products of row j
+  return std::max(blk, rows) * sizeof(double);
+}
+
 // Parallel carry of the chunked chains (layout 3).  One CTA of 128 threads per (chain, shell, product
-// (j, i)), i <= j - 2: part_{j,i} = P_{j,i} d_i.  The last CTA of row j to finish (atomic ticket) forms
+// (j, i)), i <= j - 2: part_{j,i} = P_{j,i} d_i, with P_{j,i} staged in shared memory by one round of
+// cp.async (every load in flight at once).  The last CTA of row j to finish (atomic ticket) loads the
+// row's terms in parallel and forms
 //   s_j = d_{j-1} + part_{j,0} + part_{j,1} + ... + part_{j,j-2}
-// in that order (the same bits whichever CTA finishes last) and writes it to cbuf slot j; s_1 = d_0 is
-// written by the chain's first chunk.  Exact algebra of s_{c+1} = Phi_c s_c + d_c.
+// in that order (the same bits whichever CTA finishes last) into cbuf slot j; s_1 = d_0 is written by
+// the chain's first chunk.  Exact algebra of s_{c+1} = Phi_c s_c + d_c.
 __global__ void __launch_bounds__(128) k_carry_par(ChainArgs a) {
+  extern __shared__ __align__(16) double psm[];
   __shared__ double xs[2 * kMaxNr];
   __shared__ int s_last;
   const int field = a.field0 + (blockIdx.x >> 1), par = blockIdx.x & 1;
@@ -334,50 +367,49 @@ __global__ void __launch_bounds__(128) k_carry_par(ChainArgs a) {
   const double* d = a.dbuf + (size_t)b * a.d_stride + chain * a.nch * a.ldd;
   double* part = a.pbuf + (size_t)b * a.p_stride + chain * a.np * a.ldd;
   const double* P = (a4 ? a.PA4 : (field == 1 ? a.PT : a.PS)) + ((size_t)par * a.np + pidx) * m * ldm;
+  copy_block(psm, P, m * ldm);                         // m * ldm is even (ldm even)
+  cp_async_commit();
   for (int e = threadIdx.x; e < m; e += blockDim.x) xs[e] = d[(size_t)i * a.ldd + e];
+  cp_async_wait<0>();
   __syncthreads();
   double* y = part + (size_t)pidx * a.ldd;
   if (a4) {
-    if (m <= 64) block_mv<2>(P, ldm, xs, m, y);
-    else block_mv<1>(P, ldm, xs, m, y);
+    if (m <= 64) block_mv<2>(psm, ldm, xs, m, y);
+    else block_mv<1>(psm, ldm, xs, m, y);
   } else {
-    if (m <= 32) block_mv<4>(P, ldm, xs, m, y);
-    else block_mv<2>(P, ldm, xs, m, y);
+    if (m <= 32) block_mv<4>(psm, ldm, xs, m, y);
+    else block_mv<2>(psm, ldm, xs, m, y);
   }
-  __threadfence();                                     // this product before the ticket
+  // ticket: the CTA barrier orders every thread's product stores before thread 0's device-scope fence
+  // and atomic (release); the last CTA's thread 0 fences again after its atomic (acquire) and the
+  // barrier passes that on to the CTA, whose loads of the other CTAs' products go through L2
   __syncthreads();
   int* cnt = a.pcounter + ((size_t)b * 6 + chain) * a.nch + j;
-  if (threadIdx.x == 0) s_last = (atomicAdd(cnt, 1) == j - 2);
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const int last = atomicAdd(cnt, 1) == j - 2;
+    if (last) {
+      __threadfence();
+      *cnt = 0;                                        // ready for the next launch
+    }
+    s_last = last;
+  }
   __syncthreads();
   if (!s_last) return;
-  __threadfence();
-  if (threadIdx.x == 0) *cnt = 0;                      // ready for the next launch
+  // terms of row j in shared memory: t = 0 is d_{j-1}, t = k + 1 is part_{j,k}
   const double* row = part + (size_t)((j - 1) * (j - 2) / 2) * a.ldd;
+  const int nt = j;
+  for (int e = threadIdx.x; e < nt * m; e += blockDim.x) {
+    const int t = e / m, c = e - t * m;
+    psm[e] = __ldcg(t == 0 ? d + (size_t)(j - 1) * a.ldd + c : row + (size_t)(t - 1) * a.ldd + c);
+  }
+  __syncthreads();
   double* cb = a.cbuf + (size_t)b * a.d_stride + (chain * a.nch + j) * a.ldd;
   for (int e = threadIdx.x; e < m; e += blockDim.x) {
-    double v = __ldcg(d + (size_t)(j - 1) * a.ldd + e);
-    for (int k = 0; k <= j - 2; ++k) v += __ldcg(row + (size_t)k * a.ldd + e);
+    double v = psm[e];
+    for (int t = 1; t < nt; ++t) v += psm[(size_t)t * m + e];
     cb[e] = v;
   }
-}
-
-// g of mode `row` for the fused right-hand side, element n (see ChainArgs::fuse_rhs): the roundings of
-// k_rhs, psi: (-dt (Dr Q - R)) + lin, T: (-dt NT) + lin, S: (-dt NS) + lin.
-__device__ __forceinline__ double fused_g(const ChainArgs& a, int b, int field, int row, int n) {
-  const int M = a.M, nr = a.nr;
-  const size_t N = (size_t)M * nr;
-  const double* o4 = a.out4 + (size_t)b * a.out_stride;
-  double nl;
-  if (field == 0) {
-    const double* qs = o4 + (size_t)row * nr;
-    const double* drn = a.Dr + (size_t)n * nr;
-    double dq = 0.0;
-    for (int c = 0; c < nr; ++c) dq = fma(drn[c], qs[c], dq);
-    nl = __dmul_rn(-a.dt, __dsub_rn(dq, o4[N + (size_t)row * nr + n]));
-  } else {
-    nl = __dmul_rn(-a.dt, o4[(size_t)(field + 1) * N + (size_t)row * nr + n]);
-  }
-  return __dadd_rn(nl, a.lin[(size_t)b * a.g_stride + (size_t)field * a.field_off + (size_t)row * nr + n]);
 }
 
 // Independent per-mode matvecs, one CTA of 128 threads per (field, mode, shell); matrix rows split over
@@ -547,7 +579,10 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
     ktimer_mark(SDD_K_CHAIN, s);
     if (a.nch < 2) return cudaSuccess;
     if (a.np > 0) {
-      if ((e = launch_kernel(k_carry_par, dim3(2 * nfields, batch, a.np), dim3(128), 0, s, a)) != cudaSuccess)
+      static unsigned long long done = 0;
+      if ((e = ensure_smem_attr(k_carry_par, &done)) != cudaSuccess) return e;
+      if ((e = launch_kernel(k_carry_par, dim3(2 * nfields, batch, a.np), dim3(128),
+                             carry_par_smem_bytes(a.nr, a.ldmA, a.nch), s, a)) != cudaSuccess)
         return e;
       ktimer_mark(SDD_K_CHAIN_CARRY, s);
     }

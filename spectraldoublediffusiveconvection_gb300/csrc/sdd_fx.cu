@@ -308,9 +308,14 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
 // Per element the operations and their order are those of k_fx_rows, so the results are identical.
 constexpr int kFxSplitThreads = 256;
 
-size_t fx_grid_smem_bytes(int M, int P, int prec) {
+// FP32 grid kernels of the fused right-hand side keep FP64 copies of the row's psi, T, S and psi's parity
+// suffix sums (4 M doubles) for the linear parts, after the T-typed arrays.
+__host__ __device__ inline size_t fx_grid_lin64_offset(int M, int P, int prec) {
   const size_t es = prec == SDD_PREC_MIXED ? sizeof(float) : sizeof(double);
-  return (8 * (size_t)P + P + 2 + 9 * (size_t)M + 32) * es + 2 * 32 * 8;
+  return (((8 * (size_t)P + P + 2 + 9 * (size_t)M + 32) * es + 2 * 32 * 8) + 15) / 16 * 16;
+}
+size_t fx_grid_smem_bytes(int M, int P, int prec) {
+  return fx_grid_lin64_offset(M, P, prec) + (prec == SDD_PREC_MIXED ? 4 * (size_t)M * sizeof(double) : 0);
 }
 size_t fx_prod_smem_bytes(int P, int prec) {
   const size_t es = prec == SDD_PREC_MIXED ? sizeof(float) : sizeof(double);
@@ -319,7 +324,9 @@ size_t fx_prod_smem_bytes(int P, int prec) {
 
 // Radial contractions of the split path (Derivatives, Matrix_Operators.py:698-729), one CTA per (mode,
 // shell): Dr psi_k, D2r2 psi_k, Dr T_k, Dr S_k for every radial row n, each a sequential fma chain over the
-// columns in the order of the fused kernel's (so both paths round identically).
+// columns in the order of the fused kernel's (so both paths round identically).  With the fused
+// right-hand side a fifth block, D2s psi_k in FP64, follows the four T-typed blocks (per shell:
+// 4 M nr T then M nr doubles).
 template <typename T>
 __global__ void __launch_bounds__(256) k_fx_deriv(FxArgs a, T* deriv, size_t deriv_stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -355,7 +362,7 @@ __global__ void __launch_bounds__(256) k_fx_deriv(FxArgs a, T* deriv, size_t der
       const double* row = a.rl.D2s + (size_t)n * nr;
       double acc = 0;
       for (int m = 0; m < nr; ++m) acc = fma(__ldg(row + m), __ldg(ps + m), acc);
-      reinterpret_cast<double*>(D)[(size_t)4 * M * nr + (size_t)k * nr + n] = acc;
+      reinterpret_cast<double*>(D)[(size_t)4 * M * nr * sizeof(T) / 8 + (size_t)k * nr + n] = acc;
     }
   }
 }
@@ -399,6 +406,11 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
   // which row quantities the pair's two fields need (fields: 0 JT_psi, 1 komega, 2 kDpsi, 3 DT, 4 DC,
   // 5 omega, 6 Dpsi, 7 kT, 8 kC)
   const bool need_psi = pr == 0 || pr == 2;            // pv (JT_psi, omega's A2 term) and D2 psi (omega)
+  // FP32 kernels: FP64 row values for the linear parts of the fused right-hand side (pair 0)
+  const bool lin = pr == 0 && a.fuse_rhs;
+  double* pv64 = nullptr;
+  if (sizeof(T) == 4 && lin)
+    pv64 = reinterpret_cast<double*>(smem_raw + fx_grid_lin64_offset(M, P, SDD_PREC_MIXED));
   const int N = M * nr;
   const double* Xs = a.X + (size_t)b * a.x_stride;
   const T* Dv = reinterpret_cast<const T*>(a.deriv) + (size_t)b * a.deriv_stride;   // k_fx_deriv
@@ -424,34 +436,43 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
     OM[k] = d2;
     DTv[k] = dtv;
     DCv[k] = dcv;
+    if (pv64) {
+      pv64[k] = psi_on ? __ldg(Xs + (size_t)k * nr + n) : 0.0;
+      pv64[2 * M + k] = ts_on ? __ldg(Xs + N + (size_t)k * nr + n) : 0.0;
+      pv64[3 * M + k] = ts_on ? __ldg(Xs + 2 * N + (size_t)k * nr + n) : 0.0;
+    }
   }
   __syncthreads();
   if (need_psi) {
     parity_suffix<T>(pv, Sc, M);
+    if (pv64) parity_suffix<double>(pv64, pv64 + M, M);
     __syncthreads();
-    if (sizeof(T) == 8 && pr == 0 && a.fuse_rhs) {
-      // the linear parts of the right-hand sides at row n (k_rhs's expressions, Main.py:262-280)
+    if (lin) {
+      // the linear parts of the right-hand sides at row n (k_rhs's expressions, Main.py:262-280), in FP64
+      const double* pvd = pv64 ? pv64 : reinterpret_cast<const double*>(pv);
+      const double* Scd = pv64 ? pv64 + M : reinterpret_cast<const double*>(Sc);
+      const double* Tvd = pv64 ? pv64 + 2 * M : reinterpret_cast<const double*>(Tv);
+      const double* Svd = pv64 ? pv64 + 3 * M : reinterpret_cast<const double*>(Sv);
       const RhsArgs& r = a.rl;
-      const double* D2p = reinterpret_cast<const double*>(Dv) + (size_t)4 * M * nr;
+      const double* D2p = reinterpret_cast<const double*>(Dv) + (size_t)4 * M * nr * sizeof(T) / 8;
       const double dt = r.dt, dtPr = r.dt * r.Pr;
       const double Ra = r.Ra[b], Ras = r.Ra_s[b];
       const double ir2 = r.ir2s[n], rsq = r.rsq[n], dT0 = r.dT0[n], gr = r.gr[n];
       double* R = r.rhs + (size_t)b * r.rhs_stride;
       for (int k = tid; k < M; k += bd) {
-        const double pk = (double)pv[k], pkm = k > 0 ? (double)pv[k - 1] : 0.0;
-        const double s1 = (k + 1 < M) ? (double)Sc[k + 1] : 0.0;
+        const double pk = pvd[k], pkm = k > 0 ? pvd[k - 1] : 0.0;
+        const double s1 = (k + 1 < M) ? Scd[k + 1] : 0.0;
         const double JPk = (k == 0) ? 1.0 * s1 : (k + 1.0) * pkm + 2.0 * s1;
-        const double s2 = (k + 2 < M) ? (double)Sc[k + 2] : 0.0;
+        const double s2 = (k + 2 < M) ? Scd[k + 2] : 0.0;
         const bool psi_on = !(a.sym && (k % 2 == 0));
         const double d2s = psi_on ? D2p[(size_t)k * nr + n] : 0.0;
         const double Om = d2s - (double)(k + 1) * ir2 * ((k + 2.0) * pk + 2.0 * s2);
-        const double grv = (k < M - 1) ? (-(double)(k + 1) * gr) * (Ra * (double)Tv[k + 1] - Ras * (double)Sv[k + 1])
-                                       : 0.0;
+        const double grv = (k < M - 1) ? (-(double)(k + 1) * gr) * (Ra * Tvd[k + 1] - Ras * Svd[k + 1]) : 0.0;
         const double psiT0 = dT0 * JPk;
         const size_t o = (size_t)k * nr + n;
         R[o] = Om + dtPr * grv;
-        R[N + o] = rsq * (double)Tv[k] - dt * psiT0;
-        R[2 * N + o] = rsq * (double)Sv[k] - dt * psiT0;
+        R[N + o] = rsq * Tvd[k] - dt * psiT0;
+        R[2 * N + o] = rsq * Svd[k] - dt * psiT0;
       }
     }
     for (int k = tid; k < M; k += bd) jp_om<T>(k, M, kf, pv, Sc, ir4n, JP[k], OM[k]);
@@ -882,7 +903,6 @@ static cudaError_t launch_fx_split_t(const FxArgs& a, int batch, cudaStream_t s)
   T* grid = reinterpret_cast<T*>((MODE != 1 && a.base) ? a.base : a.grid);
   const size_t gs = (MODE != 1 && a.base) ? a.base_stride : a.grid_stride;
   cudaError_t e;
-  if (sizeof(T) != 8 && a.fuse_rhs) return cudaErrorInvalidValue;   // the fused rhs is FP64-only
   e = launch_kernel(k_fx_deriv<T>, dim3(a.M, batch), dim3(256), (2 * a.nr * a.nr + 3 * a.nr) * sizeof(T), s, a,
                  reinterpret_cast<T*>(a.deriv), a.deriv_stride);
   ktimer_mark(SDD_K_FX_DERIV, s);
