@@ -121,7 +121,6 @@ struct sdd_plan {
   double *dbuf, *cbuf;              // [B][3][2][nch_alloc][ldd] chunk end states / carried states
   int* dcnt;                        // [B][6] chunk counters of the sequential carry
   double* pbuf;                     // [B][6][np_alloc][ldd] products of the parallel carry
-  int* pcnt;                        // [B][6][nch_alloc] row counters of the parallel carry
   // FP32 copies used by the mixed-precision nonlinear term
   float *Dr32, *D2r232, *ir4r232;
   // workspace
@@ -250,7 +249,6 @@ static void free_plan(sdd_plan* p) {
     const double* t[] = {c.GA4, c.GT, c.GS, c.PhiA4, c.PhiT, c.PhiS, c.PA4, c.PT, c.PS};
     for (const double* x : t) cudaFree(const_cast<double*>(x));
   }
-  cudaFree(p->pcnt);
   cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232);
   cudaFree(p->base_tmp);
   cudaFree(p->gridbuf);
@@ -606,9 +604,9 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   clear_step_graphs(p);   // the graphs bake in the workspace pointers
   cudaFree(p->out4); cudaFree(p->rhs); cudaFree(p->xtmp); cudaFree(p->base_tmp); cudaFree(p->hbuf);
   cudaFree(p->dbuf); cudaFree(p->cbuf); cudaFree(p->gridbuf); cudaFree(p->derivbuf);
-  cudaFree(p->dg_part); cudaFree(p->dg_out); cudaFree(p->dcnt); cudaFree(p->pbuf); cudaFree(p->pcnt);
+  cudaFree(p->dg_part); cudaFree(p->dg_out); cudaFree(p->dcnt); cudaFree(p->pbuf);
   p->dg_part = p->dg_out = nullptr;
-  p->dcnt = p->pcnt = nullptr;
+  p->dcnt = nullptr;
   p->pbuf = nullptr;
   p->out4 = p->rhs = p->xtmp = p->hbuf = p->dbuf = p->cbuf = nullptr;
   p->base_tmp = p->gridbuf = p->derivbuf = nullptr;
@@ -630,8 +628,6 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   SDD_CUDA(cudaMalloc(&p->dbuf, (size_t)max_batch * de * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->cbuf, (size_t)max_batch * de * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->pbuf, (size_t)max_batch * 6 * p->np_alloc * p->ldd * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->pcnt, (size_t)max_batch * 6 * p->nch_alloc * sizeof(int)));
-  SDD_CUDA(cudaMemset(p->pcnt, 0, (size_t)max_batch * 6 * p->nch_alloc * sizeof(int)));
   p->ws_batch = max_batch;
   return SDD_OK;
 }
@@ -696,7 +692,7 @@ static ChainArgs chain_args(const sdd_plan* p, const double* g, double* f, const
   a.cset[1] = p->cs[1];
   a.dbuf = p->dbuf; a.cbuf = p->cbuf; a.counter = p->dcnt;
   a.d_stride = (size_t)6 * p->nch_alloc * p->ldd;
-  a.pbuf = p->pbuf; a.pcounter = p->pcnt;
+  a.pbuf = p->pbuf;
   a.p_stride = (size_t)6 * p->np_alloc * p->ldd;
   return a;
 }

@@ -234,7 +234,7 @@ __global__ void k_chain(ChainArgs a) {
     __syncthreads();
     if (!s_last) return;
     carry_run<(TPR == 4 ? 2 : 1), CR>(a, field, par, b, csm);
-  } else if (CHUNK && a.nch >= 2) {                   // s_1 = d_0: the chain's first chunk copies it
+  } else if (CHUNK && a.nch == 2 && a.carry_seq) {    // s_1 = d_0 only: the chain's first chunk copies it
     if (chunk == 0 && lead) {
       double* cb = a.cbuf + (size_t)b * a.d_stride + ((size_t)(field * 2 + par) * a.nch + 1) * a.ldd;
       cb[i] = fe;
@@ -337,23 +337,16 @@ __device__ __forceinline__ void block_mv(const double* P, int ldm, const double*
   }
 }
 
-size_t carry_par_smem_bytes(int nr, int ldmA, int nch) {
-  const size_t blk = (size_t)2 * nr * ldmA;             // the largest product block (psi)
-  const size_t rows = (size_t)nch * 2 * nr;             // d_{j-1} and up to nch - 2 products of row j
-  return std::max(blk, rows) * sizeof(double);
-}
+size_t carry_par_smem_bytes(int nr, int ldmA) { return (size_t)2 * nr * ldmA * sizeof(double); }
 
 // Parallel carry of the chunked chains (layout 3).  One CTA of 128 threads per (chain, shell, product
 // (j, i)), i <= j - 2: part_{j,i} = P_{j,i} d_i, with P_{j,i} staged in shared memory by one round of
-// cp.async (every load in flight at once).  The last CTA of row j to finish (atomic ticket) loads the
-// row's terms in parallel and forms
-//   s_j = d_{j-1} + part_{j,0} + part_{j,1} + ... + part_{j,j-2}
-// in that order (the same bits whichever CTA finishes last) into cbuf slot j; s_1 = d_0 is written by
-// the chain's first chunk.  Exact algebra of s_{c+1} = Phi_c s_c + d_c.
+// cp.async (every load in flight at once).  The corrections sum each row (carried_state):
+//   s_j = d_{j-1} + part_{j,0} + part_{j,1} + ... + part_{j,j-2},
+// the exact algebra of s_{c+1} = Phi_c s_c + d_c.
 __global__ void __launch_bounds__(128) k_carry_par(ChainArgs a) {
   extern __shared__ __align__(16) double psm[];
   __shared__ double xs[2 * kMaxNr];
-  __shared__ int s_last;
   const int field = a.field0 + (blockIdx.x >> 1), par = blockIdx.x & 1;
   const int b = blockIdx.y, pidx = blockIdx.z;
   const bool a4 = field == 0;
@@ -380,36 +373,18 @@ __global__ void __launch_bounds__(128) k_carry_par(ChainArgs a) {
     if (m <= 32) block_mv<4>(psm, ldm, xs, m, y);
     else block_mv<2>(psm, ldm, xs, m, y);
   }
-  // ticket: the CTA barrier orders every thread's product stores before thread 0's device-scope fence
-  // and atomic (release); the last CTA's thread 0 fences again after its atomic (acquire) and the
-  // barrier passes that on to the CTA, whose loads of the other CTAs' products go through L2
-  __syncthreads();
-  int* cnt = a.pcounter + ((size_t)b * 6 + chain) * a.nch + j;
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const int last = atomicAdd(cnt, 1) == j - 2;
-    if (last) {
-      __threadfence();
-      *cnt = 0;                                        // ready for the next launch
-    }
-    s_last = last;
+}
+
+// Element e of the carried state s_c (c >= 1) of chain `chain` under layout 3: d_{c-1} plus the row's
+// products (k_carry_par), summed in index order.
+__device__ __forceinline__ double carried_state(const ChainArgs& a, int b, size_t chain, int c, int e) {
+  const double* d = a.dbuf + (size_t)b * a.d_stride + chain * a.nch * a.ldd;
+  double v = d[(size_t)(c - 1) * a.ldd + e];
+  if (c >= 2) {
+    const double* row = a.pbuf + (size_t)b * a.p_stride + (chain * a.np + (size_t)(c - 1) * (c - 2) / 2) * a.ldd;
+    for (int t = 0; t <= c - 2; ++t) v += row[(size_t)t * a.ldd + e];
   }
-  __syncthreads();
-  if (!s_last) return;
-  // terms of row j in shared memory: t = 0 is d_{j-1}, t = k + 1 is part_{j,k}
-  const double* row = part + (size_t)((j - 1) * (j - 2) / 2) * a.ldd;
-  const int nt = j;
-  for (int e = threadIdx.x; e < nt * m; e += blockDim.x) {
-    const int t = e / m, c = e - t * m;
-    psm[e] = __ldcg(t == 0 ? d + (size_t)(j - 1) * a.ldd + c : row + (size_t)(t - 1) * a.ldd + c);
-  }
-  __syncthreads();
-  double* cb = a.cbuf + (size_t)b * a.d_stride + (chain * a.nch + j) * a.ldd;
-  for (int e = threadIdx.x; e < m; e += blockDim.x) {
-    double v = psm[e];
-    for (int t = 1; t < nt; ++t) v += psm[(size_t)t * m + e];
-    cb[e] = v;
-  }
+  return v;
 }
 
 // Independent per-mode matvecs, one CTA of 128 threads per (field, mode, shell); matrix rows split over
@@ -434,8 +409,29 @@ __global__ void __launch_bounds__(128) k_mode_mv(ChainArgs a) {
     if (c == 0 || (a.sym && !(a4 ? par == 0 : par == 1))) return;
     m = a4 ? 2 * nr : nr;
     A = (a4 ? a.GA4 : (field == 1 ? a.GT : a.GS)) + (size_t)jj * m * ldl;
-    x = a.cbuf + (size_t)b * a.d_stride + ((size_t)(field * 2 + par) * a.nch + c) * a.ldd;
     y = a.f + (size_t)b * a.f_stride + foff + (size_t)row * nr;
+    const size_t chain = (size_t)(field * 2 + par);
+    if (a.carry_seq) {
+      x = a.cbuf + (size_t)b * a.d_stride + (chain * a.nch + c) * a.ldd;
+    } else {
+      // s_c: the row's terms loaded in parallel into shared memory, then summed in index order
+      extern __shared__ __align__(16) double tsm[];     // c * m doubles, then m for s_c
+      const double* d = a.dbuf + (size_t)b * a.d_stride + chain * a.nch * a.ldd;
+      const double* prow = a.pbuf + (size_t)b * a.p_stride + (chain * a.np + (size_t)(c - 1) * (c - 2) / 2) * a.ldd;
+      for (int e = threadIdx.x; e < c * m; e += blockDim.x) {
+        const int t = e / m, k = e - t * m;
+        tsm[e] = t == 0 ? d[(size_t)(c - 1) * a.ldd + k] : prow[(size_t)(t - 1) * a.ldd + k];
+      }
+      __syncthreads();
+      double* xs = tsm + (size_t)c * m;
+      for (int e = threadIdx.x; e < m; e += blockDim.x) {
+        double v = tsm[e];
+        for (int t = 1; t < c; ++t) v += tsm[(size_t)t * m + e];
+        xs[e] = v;
+      }
+      __syncthreads();
+      x = xs;
+    }
   } else {
     m = nr;
     A = (a4 ? a.LinvA4 : (field == 1 ? a.LinvT : a.LinvS)) + (size_t)jj * nr * ldl;
@@ -486,8 +482,16 @@ __global__ void __launch_bounds__(128) k_mode_mv_warp(ChainArgs a, int nfields) 
     if (c == 0 || (a.sym && !(a4 ? par == 0 : par == 1))) return;
     m = a4 ? 2 * nr : nr;
     A = (a4 ? a.GA4 : (field == 1 ? a.GT : a.GS)) + (size_t)jj * m * ldl;
-    x = a.cbuf + (size_t)b * a.d_stride + ((size_t)(field * 2 + par) * a.nch + c) * a.ldd;
     y = a.f + (size_t)b * a.f_stride + foff + (size_t)row * nr;
+    if (a.carry_seq) {
+      x = a.cbuf + (size_t)b * a.d_stride + ((size_t)(field * 2 + par) * a.nch + c) * a.ldd;
+    } else {   // s_c summed per lane in the index order of k_mode_mv
+      __shared__ double ssm[4][2 * kMaxNr];
+      double* sw = ssm[threadIdx.x >> 5];
+      for (int e = lane; e < m; e += 32) sw[e] = carried_state(a, b, (size_t)(field * 2 + par), c, e);
+      __syncwarp();
+      x = sw;
+    }
   } else {
     m = nr;
     A = (a4 ? a.LinvA4 : (field == 1 ? a.LinvT : a.LinvS)) + (size_t)jj * nr * ldl;
@@ -525,6 +529,8 @@ __global__ void __launch_bounds__(128) k_mode_mv_warp(ChainArgs a, int nfields) 
 
 template <bool FIX>
 static cudaError_t launch_mode_mv(const ChainArgs& a, int batch, int nfields, cudaStream_t s, bool per_warp) {
+  // layout-3 corrections stage the terms of s_c: up to nch vectors of 2 nr, then s_c
+  const size_t fsm = (FIX && !a.carry_seq) ? ((size_t)a.nch + 1) * 2 * a.nr * sizeof(double) : 0;
   if (per_warp) {
     const dim3 wg((nfields * a.M + 3) / 4, batch);
     const cudaError_t e = a.nr <= 32 ? launch_kernel(k_mode_mv_warp<FIX, 4>, wg, dim3(128), 0, s, a, nfields)
@@ -533,8 +539,16 @@ static cudaError_t launch_mode_mv(const ChainArgs& a, int batch, int nfields, cu
     return e;
   }
   const dim3 grid(nfields * a.M, batch);
-  const cudaError_t e = a.nr <= 32 ? launch_kernel(k_mode_mv<4, FIX>, grid, dim3(128), 0, s, a)
-                                   : launch_kernel(k_mode_mv<2, FIX>, grid, dim3(128), 0, s, a);
+  cudaError_t e;
+  if (a.nr <= 32) {
+    static unsigned long long done = 0;
+    if (fsm && (e = ensure_smem_attr(k_mode_mv<4, FIX>, &done)) != cudaSuccess) return e;
+    e = launch_kernel(k_mode_mv<4, FIX>, grid, dim3(128), fsm, s, a);
+  } else {
+    static unsigned long long done = 0;
+    if (fsm && (e = ensure_smem_attr(k_mode_mv<2, FIX>, &done)) != cudaSuccess) return e;
+    e = launch_kernel(k_mode_mv<2, FIX>, grid, dim3(128), fsm, s, a);
+  }
   ktimer_mark(FIX ? SDD_K_MODE_FIX : SDD_K_MODE_H, s);
   return e;
 }
@@ -580,9 +594,9 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
     if (a.nch < 2) return cudaSuccess;
     if (a.np > 0) {
       static unsigned long long done = 0;
-      if ((e = ensure_smem_attr(k_carry_par, &done)) != cudaSuccess) return e;
+      if ((e = ensure_smem_attr(k_carry_par, &done, true)) != cudaSuccess) return e;
       if ((e = launch_kernel(k_carry_par, dim3(2 * nfields, batch, a.np), dim3(128),
-                             carry_par_smem_bytes(a.nr, a.ldmA, a.nch), s, a)) != cudaSuccess)
+                             carry_par_smem_bytes(a.nr, a.ldmA), s, a)) != cudaSuccess)
         return e;
       ktimer_mark(SDD_K_CHAIN_CARRY, s);
     }

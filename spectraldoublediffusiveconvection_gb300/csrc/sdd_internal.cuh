@@ -48,9 +48,10 @@ inline void ktimer_mark(int id, cudaStream_t s) {
 }
 
 // Raises a kernel's dynamic shared-memory limit to the device's opt-in maximum once per device, so
-// launches do not pay a cudaFuncSetAttribute call each.
+// launches do not pay a cudaFuncSetAttribute call each.  max_carveout: also prefer the largest
+// shared-memory share of the L1/shared storage, for kernels whose many CTAs must be resident at once.
 template <typename F>
-inline cudaError_t ensure_smem_attr(F* fn, unsigned long long* done_mask) {
+inline cudaError_t ensure_smem_attr(F* fn, unsigned long long* done_mask, bool max_carveout = false) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
@@ -65,6 +66,9 @@ inline cudaError_t ensure_smem_attr(F* fn, unsigned long long* done_mask) {
   // the dynamic limit may not exceed the opt-in maximum less the kernel's static shared memory
   e = cudaFuncSetAttribute(reinterpret_cast<const void*>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
                            optin - (int)fa.sharedSizeBytes);
+  if (e == cudaSuccess && max_carveout)
+    e = cudaFuncSetAttribute(reinterpret_cast<const void*>(fn), cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
   if (e == cudaSuccess) __atomic_fetch_or(done_mask, bit, __ATOMIC_ACQ_REL);
   return e;
 }
@@ -191,14 +195,13 @@ struct ChainArgs {
   size_t d_stride;           // doubles per shell in dbuf / cbuf
   int* counter;              // [shell][6] chunks finished per chain (the last one runs the carry), zeroed
   // layout 3 (parallel carry): the chunks only write their end states; k_carry_par forms
-  // part_{j,i} = P_{j,i} d_i for every product in parallel and the last CTA of row j sums
-  // s_j = d_{j-1} + sum_i part_{j,i} (index order) into cbuf
+  // part_{j,i} = P_{j,i} d_i for every product in parallel and the corrections sum
+  // s_j = d_{j-1} + sum_i part_{j,i} (index order)
   int carry_seq;             // 1: the last-finishing chunk CTA runs the sequential carry (layout 2)
   int np;                    // products per chain
   const double* PA4, *PT, *PS;
   double* pbuf;              // [shell][6][np][ldd] products P_{j,i} d_i
   size_t p_stride;           // doubles per shell in pbuf
-  int* pcounter;             // [shell][6][nch] products finished per row j, zeroed
   ChunkSet cset[2];          // the chunkings of layouts 2 and 3 (launch_chain copies one into the fields above)
 };
 
