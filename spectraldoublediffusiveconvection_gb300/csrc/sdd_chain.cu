@@ -76,14 +76,16 @@ __device__ __forceinline__ void chain_sync() {
 
 // g of mode `row` for the fused right-hand side, element n (see ChainArgs::fuse_rhs): the roundings of
 // k_rhs, psi: (-dt (Dr Q - R)) + lin, T: (-dt NT) + lin, S: (-dt NS) + lin.
-__device__ __forceinline__ double fused_g(const ChainArgs& a, int b, int field, int row, int n) {
+// Dr and the Q row may be given in shared memory (Drs: nr x nr row-major, Qs: nr); nullptr reads global.
+__device__ __forceinline__ double fused_g(const ChainArgs& a, int b, int field, int row, int n,
+                                         const double* Drs = nullptr, const double* Qs = nullptr) {
   const int M = a.M, nr = a.nr;
   const size_t N = (size_t)M * nr;
   const double* o4 = a.out4 + (size_t)b * a.out_stride;
   double nl;
   if (field == 0) {
-    const double* qs = o4 + (size_t)row * nr;
-    const double* drn = a.Dr + (size_t)n * nr;
+    const double* qs = Qs ? Qs : o4 + (size_t)row * nr;
+    const double* drn = (Drs ? Drs : a.Dr) + (size_t)n * nr;
     double dq = 0.0;
     for (int c = 0; c < nr; ++c) dq = fma(drn[c], qs[c], dq);
     nl = __dmul_rn(-a.dt, __dsub_rn(dq, o4[N + (size_t)row * nr + n]));
@@ -391,8 +393,18 @@ __device__ __forceinline__ double carried_state(const ChainArgs& a, int b, size_
 // TPR lanes (TPR = 4 for nr <= 32, 2 for nr <= 64), every lane's column loads independent of each other:
 //   FIX = false:  h_jj = Linv_jj g_jj                          (the chains' right-hand sides)
 //   FIX = true:   f_jj += G_jj s_c(jj) for the modes of chunks c >= 1   (chunked chains' correction)
+// Shared memory of k_mode_mv: the matrix block (m x ldl), then the layout-3 terms of s_c ((nch + 1) 2 nr)
+// or the fused right-hand side's Dr and Q row (nr^2 + nr) and g (nr).
+size_t mode_mv_smem_bytes(const ChainArgs& a, bool fix) {
+  const size_t blk = (size_t)(fix ? 2 * a.nr : a.nr) * a.ldl;
+  const size_t rest = fix ? (a.carry_seq ? 0 : ((size_t)a.nch + 1) * 2 * a.nr)
+                          : (size_t)a.nr * a.nr + 2 * (size_t)a.nr;
+  return (blk + rest) * sizeof(double);
+}
+
 template <int TPR, bool FIX>
 __global__ void __launch_bounds__(128) k_mode_mv(ChainArgs a) {
+  extern __shared__ __align__(16) double msm[];
   const int M = a.M, nr = a.nr, ldl = a.ldl;
   const int fl = blockIdx.x / M, jj = blockIdx.x - fl * M;
   const int field = a.field0 + fl;
@@ -409,13 +421,16 @@ __global__ void __launch_bounds__(128) k_mode_mv(ChainArgs a) {
     if (c == 0 || (a.sym && !(a4 ? par == 0 : par == 1))) return;
     m = a4 ? 2 * nr : nr;
     A = (a4 ? a.GA4 : (field == 1 ? a.GT : a.GS)) + (size_t)jj * m * ldl;
+    copy_block(msm, A, m * ldl);                       // the block streams in while s_c is formed
+    cp_async_commit();
+    A = msm;
     y = a.f + (size_t)b * a.f_stride + foff + (size_t)row * nr;
     const size_t chain = (size_t)(field * 2 + par);
     if (a.carry_seq) {
       x = a.cbuf + (size_t)b * a.d_stride + (chain * a.nch + c) * a.ldd;
     } else {
       // s_c: the row's terms loaded in parallel into shared memory, then summed in index order
-      extern __shared__ __align__(16) double tsm[];     // c * m doubles, then m for s_c
+      double* tsm = msm + (size_t)2 * nr * ldl;          // c * m doubles, then m for s_c
       const double* d = a.dbuf + (size_t)b * a.d_stride + chain * a.nch * a.ldd;
       const double* prow = a.pbuf + (size_t)b * a.p_stride + (chain * a.np + (size_t)(c - 1) * (c - 2) / 2) * a.ldd;
       for (int e = threadIdx.x; e < c * m; e += blockDim.x) {
@@ -435,22 +450,34 @@ __global__ void __launch_bounds__(128) k_mode_mv(ChainArgs a) {
   } else {
     m = nr;
     A = (a4 ? a.LinvA4 : (field == 1 ? a.LinvT : a.LinvS)) + (size_t)jj * nr * ldl;
+    copy_block(msm, A, nr * ldl);                      // the block streams in while g is formed
+    cp_async_commit();
+    A = msm;
     x = a.g + (size_t)b * a.g_stride + foff + (size_t)row * nr;
     y = a.h + (size_t)b * a.h_stride + foff + (size_t)row * nr;
     if (a.fuse_rhs) {
-      __shared__ double gsm[kMaxNr];
-      for (int n = threadIdx.x; n < nr; n += blockDim.x) gsm[n] = fused_g(a, b, field, row, n);
-      __syncthreads();
+      double* Drs = msm + (size_t)nr * ldl;            // Dr (nr x nr), the Q row, then g
+      double* Qs = Drs + (size_t)nr * nr;
+      double* gsm = Qs + nr;
+      if (a4) {
+        for (int e = threadIdx.x; e < nr * nr; e += blockDim.x) Drs[e] = a.Dr[e];
+        const double* q4 = a.out4 + (size_t)b * a.out_stride + (size_t)row * nr;
+        for (int e = threadIdx.x; e < nr; e += blockDim.x) Qs[e] = q4[e];
+        __syncthreads();
+      }
+      for (int n = threadIdx.x; n < nr; n += blockDim.x) gsm[n] = fused_g(a, b, field, row, n, Drs, Qs);
       x = gsm;
     }
   }
+  cp_async_wait<0>();
+  __syncthreads();
   const int i = threadIdx.x / TPR, q = threadIdx.x % TPR;
   for (int r0 = 0; r0 < nr; r0 += 128 / TPR) {
     const int r = r0 + i;
     const int rr = r < nr ? r : 0;
     double acc = 0.0;
 #pragma unroll 8
-    for (int col = q; col < m; col += TPR) acc = fma(__ldg(A + (size_t)col * ldl + rr), x[col], acc);
+    for (int col = q; col < m; col += TPR) acc = fma(A[(size_t)col * ldl + rr], x[col], acc);
     acc = group_sum<TPR>(acc);
     if (r < nr && q == 0) {
       if (FIX) y[r] += acc;
@@ -529,8 +556,6 @@ __global__ void __launch_bounds__(128) k_mode_mv_warp(ChainArgs a, int nfields) 
 
 template <bool FIX>
 static cudaError_t launch_mode_mv(const ChainArgs& a, int batch, int nfields, cudaStream_t s, bool per_warp) {
-  // layout-3 corrections stage the terms of s_c: up to nch vectors of 2 nr, then s_c
-  const size_t fsm = (FIX && !a.carry_seq) ? ((size_t)a.nch + 1) * 2 * a.nr * sizeof(double) : 0;
   if (per_warp) {
     const dim3 wg((nfields * a.M + 3) / 4, batch);
     const cudaError_t e = a.nr <= 32 ? launch_kernel(k_mode_mv_warp<FIX, 4>, wg, dim3(128), 0, s, a, nfields)
@@ -539,15 +564,16 @@ static cudaError_t launch_mode_mv(const ChainArgs& a, int batch, int nfields, cu
     return e;
   }
   const dim3 grid(nfields * a.M, batch);
+  const size_t sm = mode_mv_smem_bytes(a, FIX);
   cudaError_t e;
   if (a.nr <= 32) {
     static unsigned long long done = 0;
-    if (fsm && (e = ensure_smem_attr(k_mode_mv<4, FIX>, &done)) != cudaSuccess) return e;
-    e = launch_kernel(k_mode_mv<4, FIX>, grid, dim3(128), fsm, s, a);
+    if ((e = ensure_smem_attr(k_mode_mv<4, FIX>, &done, true)) != cudaSuccess) return e;
+    e = launch_kernel(k_mode_mv<4, FIX>, grid, dim3(128), sm, s, a);
   } else {
     static unsigned long long done = 0;
-    if (fsm && (e = ensure_smem_attr(k_mode_mv<2, FIX>, &done)) != cudaSuccess) return e;
-    e = launch_kernel(k_mode_mv<2, FIX>, grid, dim3(128), fsm, s, a);
+    if ((e = ensure_smem_attr(k_mode_mv<2, FIX>, &done, true)) != cudaSuccess) return e;
+    e = launch_kernel(k_mode_mv<2, FIX>, grid, dim3(128), sm, s, a);
   }
   ktimer_mark(FIX ? SDD_K_MODE_FIX : SDD_K_MODE_H, s);
   return e;
