@@ -129,6 +129,7 @@ struct sdd_plan {
   double* rhs;      // [B][3][M][nr]
   double* xtmp;     // [B][3][M][nr]
   double* hbuf;     // [B][3][M][nr] h = Linv g of the chains
+  float* x32[2];    // mixed plans: [B][3][M][nr] FP32 copies of sdd_step's output buffer and of xtmp
   void* base_tmp;   // [B][nr][9][P] (T precision), for DFX without a caller cache
   void* gridbuf;    // [B][nr][9][P] (T precision), grid fields of the split nonlinear-term path
   void* derivbuf;   // [B] x (5 M nr doubles of room), radial derivatives of the split path: 4 M nr of the
@@ -250,6 +251,7 @@ static void free_plan(sdd_plan* p) {
     for (const double* x : t) cudaFree(const_cast<double*>(x));
   }
   cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232);
+  cudaFree(p->x32[0]); cudaFree(p->x32[1]);
   cudaFree(p->base_tmp);
   cudaFree(p->gridbuf);
   cudaFree(p->derivbuf);
@@ -605,6 +607,8 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   cudaFree(p->out4); cudaFree(p->rhs); cudaFree(p->xtmp); cudaFree(p->base_tmp); cudaFree(p->hbuf);
   cudaFree(p->dbuf); cudaFree(p->cbuf); cudaFree(p->gridbuf); cudaFree(p->derivbuf);
   cudaFree(p->dg_part); cudaFree(p->dg_out); cudaFree(p->dcnt); cudaFree(p->pbuf);
+  cudaFree(p->x32[0]); cudaFree(p->x32[1]);
+  p->x32[0] = p->x32[1] = nullptr;
   p->dg_part = p->dg_out = nullptr;
   p->dcnt = nullptr;
   p->pbuf = nullptr;
@@ -628,6 +632,8 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   SDD_CUDA(cudaMalloc(&p->dbuf, (size_t)max_batch * de * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->cbuf, (size_t)max_batch * de * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->pbuf, (size_t)max_batch * 6 * p->np_alloc * p->ldd * sizeof(double)));
+  if (p->prec == SDD_PREC_MIXED)
+    for (float*& x : p->x32) SDD_CUDA(cudaMalloc(&x, (size_t)max_batch * se * sizeof(float)));
   p->ws_batch = max_batch;
   return SDD_OK;
 }
@@ -712,9 +718,12 @@ static int check_plan(sdd_plan* p, int batch) {
 // their linear parts (FP64 in both precisions) and the chains' h kernel adds the nonlinear parts (same
 // roundings).
 // ev (nullable): four events recorded around the nonlinear term, the rhs and the chains.
+// x32_in / x32_out (mixed time steps only): the FP32 copy of X the nonlinear term reads instead of
+// converting X, and the one the chains write beside out for the next step (nullable).
 static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X, size_t ldx,
                          double* out, size_t ldo, const double* sub, size_t lds, int mode, void* base, int prec,
-                         cudaStream_t s, cudaEvent_t* ev = nullptr) {
+                         cudaStream_t s, cudaEvent_t* ev = nullptr, const float* x32_in = nullptr,
+                         float* x32_out = nullptr) {
   RhsArgs ra = rhs_args(p, X, p->out4, Ra, Ras, p->rhs, mode == 2);
   ra.x_stride = ldx;
   bool fuse = false;
@@ -722,6 +731,10 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
   if (mode != 2) {
     FxArgs fa = fx_args(p, prec, X, base, p->out4);
     fa.x_stride = ldx;
+    if (prec == SDD_PREC_MIXED && mode == 0) {
+      fa.X32 = x32_in;
+      fa.x32_stride = shell_elems(p);
+    }
     const int fm = mode == 1 ? 1 : 0;
     fuse = fx_uses_split(fa, batch, fm);
     if (fuse) {
@@ -736,6 +749,10 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
   ChainArgs ca = chain_args(p, p->rhs, out, sub);
   ca.f_stride = ldo;
   ca.sub_stride = lds;
+  if (prec == SDD_PREC_MIXED && mode == 0 && !sub) {
+    ca.f32 = x32_out;
+    ca.f32_stride = shell_elems(p);
+  }
   if (fuse) {
     ca.fuse_rhs = 1;
     ca.lin = p->rhs;
@@ -750,9 +767,10 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
 }
 
 static int apply_step(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X,
-                      double* out, const double* sub, int mode, void* base, int prec, cudaStream_t s) {
+                      double* out, const double* sub, int mode, void* base, int prec, cudaStream_t s,
+                      const float* x32_in = nullptr, float* x32_out = nullptr) {
   const size_t n = shell_elems(p);
-  return apply_step_ld(p, batch, Ra, Ras, X, n, out, n, sub, n, mode, base, prec, s);
+  return apply_step_ld(p, batch, Ra, Ras, X, n, out, n, sub, n, mode, base, prec, s, nullptr, x32_in, x32_out);
 }
 
 extern "C" {
@@ -847,9 +865,13 @@ static cudaGraphExec_t step_graph(sdd_plan* p, int batch, const double* Ra, cons
     return nullptr;
   }
   int st = SDD_OK;
+  // mixed: A's FP32 copy is current (the graph runs after a step into A); each step writes the other's
+  float* a32 = linear ? nullptr : p->x32[0];
+  float* t32 = linear ? nullptr : p->x32[1];
   for (int i = 0; i < pairs && st == SDD_OK; ++i) {
-    st = apply_step(p, batch, Ra, Ras, A, p->xtmp, nullptr, linear ? 2 : 0, nullptr, p->prec, cs);
-    if (st == SDD_OK) st = apply_step(p, batch, Ra, Ras, p->xtmp, A, nullptr, linear ? 2 : 0, nullptr, p->prec, cs);
+    st = apply_step(p, batch, Ra, Ras, A, p->xtmp, nullptr, linear ? 2 : 0, nullptr, p->prec, cs, a32, t32);
+    if (st == SDD_OK)
+      st = apply_step(p, batch, Ra, Ras, p->xtmp, A, nullptr, linear ? 2 : 0, nullptr, p->prec, cs, t32, a32);
   }
   cudaGraph_t graph = nullptr;
   const cudaError_t ec = cudaStreamEndCapture(cs, &graph);
@@ -874,8 +896,10 @@ int sdd_step(sdd_plan* p, int batch, const double* Ra, const double* Ras, const 
     if (X_out != X_in) SDD_CUDA(cudaMemcpyAsync(X_out, X_in, bytes, cudaMemcpyDeviceToDevice, s));
     return SDD_OK;
   }
-  // ping-pong so that the last step lands in X_out
+  // ping-pong so that the last step lands in X_out; mixed plans keep an FP32 copy of each step's output
+  // for the next step's nonlinear term (the caller's X_in has none)
   const double* cur = X_in;
+  const float* cur32 = nullptr;
   cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
   SDD_CUDA(cudaStreamIsCapturing(s, &cst));
   const bool graphs = cst == cudaStreamCaptureStatusNone && nsteps >= kGraphMinSteps && X_out != p->xtmp;
@@ -895,9 +919,11 @@ int sdd_step(sdd_plan* p, int batch, const double* Ra, const double* Ras, const 
     }
     double* dst = (left % 2 == 1) ? X_out : p->xtmp;
     if (dst == cur) dst = (dst == X_out) ? p->xtmp : X_out;  // never write the input in place
-    st = apply_step(p, batch, Ra, Ras, cur, dst, nullptr, linear ? 2 : 0, nullptr, p->prec, s);
+    float* dst32 = linear ? nullptr : p->x32[dst == p->xtmp ? 1 : 0];
+    st = apply_step(p, batch, Ra, Ras, cur, dst, nullptr, linear ? 2 : 0, nullptr, p->prec, s, cur32, dst32);
     if (st) return st;
     cur = dst;
+    cur32 = dst32;
   }
   if (cur != X_out) SDD_CUDA(cudaMemcpyAsync(X_out, cur, bytes, cudaMemcpyDeviceToDevice, s));
   return SDD_OK;

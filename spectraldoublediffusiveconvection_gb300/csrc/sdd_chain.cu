@@ -129,10 +129,12 @@ __global__ void k_chain(ChainArgs a) {
 
   // symmetric: only the "evens" loops run (A4 jj = 0,2,..; NAB2 jj = 1,3,..); other rows stay 0.
   const bool active = !a.sym || (a4 ? par == 0 : par == 1);
+  float* f32 = a.f32 ? a.f32 + (size_t)b * a.f32_stride + foff : nullptr;   // final values only (no sub)
   if (!active) {
     for (int e = tid; e < nsteps * nr; e += blockDim.x) {
       const int s = e / nr, c = e - s * nr;
       f[(size_t)(M - 1 - (par + 2 * (s0 + s))) * nr + c] = 0.0;
+      if (f32) f32[(size_t)(M - 1 - (par + 2 * (s0 + s))) * nr + c] = 0.0f;
     }
     if (CHUNK)
       for (int e = tid; e < a.ldd; e += blockDim.x) dout[e] = 0.0;
@@ -204,7 +206,10 @@ __global__ void k_chain(ChainArgs a) {
       fe = fma(cf[4 * (s + 1)], fi, fe);       // the b of the next step (of the next chunk after the last)
       if (lead) xn[i] = fe;
     }
-    if (lead) f[(size_t)row * nr + i] = fi;
+    if (lead) {
+      f[(size_t)row * nr + i] = fi;
+      if (f32 && chunk == 0) f32[(size_t)row * nr + i] = (float)fi;   // later chunks: final after the correction
+    }
   }
   cp_async_wait<0>();
   if (CHUNK && chunk + 1 < a.nch && lead) {    // end state of the chunk from a zero start
@@ -480,8 +485,13 @@ __global__ void __launch_bounds__(128) k_mode_mv(ChainArgs a) {
     for (int col = q; col < m; col += TPR) acc = fma(A[(size_t)col * ldl + rr], x[col], acc);
     acc = group_sum<TPR>(acc);
     if (r < nr && q == 0) {
-      if (FIX) y[r] += acc;
-      else y[r] = acc;
+      if (FIX) {
+        const double v = y[r] + acc;
+        y[r] = v;
+        if (a.f32) a.f32[(size_t)b * a.f32_stride + foff + (size_t)row * nr + r] = (float)v;
+      } else {
+        y[r] = acc;
+      }
     }
   }
 }
@@ -549,8 +559,13 @@ __global__ void __launch_bounds__(128) k_mode_mv_warp(ChainArgs a, int nfields) 
     double v;
     if (TPR == 4) v = (acc[0] + acc[1]) + (acc[2 % TPR] + acc[3 % TPR]);
     else v = acc[0] + acc[1 % TPR];
-    if (FIX) y[r] += v;
-    else y[r] = v;
+    if (FIX) {
+      const double w = y[r] + v;
+      y[r] = w;
+      if (a.f32) a.f32[(size_t)b * a.f32_stride + foff + (size_t)row * nr + r] = (float)w;
+    } else {
+      y[r] = v;
+    }
   }
 }
 

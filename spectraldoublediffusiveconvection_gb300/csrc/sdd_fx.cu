@@ -48,6 +48,21 @@ __device__ __forceinline__ T fx_x(int t, int k, int M, int P, const T* kf, const
   }
 }
 
+// Runs body(rd) with rd(e) = element e of shell b's state as T: FP32 kernels read the caller's FP32 copy
+// when there is one (the previous mixed step wrote it with the same rounding), else the FP64 state is
+// converted (an FP64-pipe instruction per element).  The choice is made once, outside the loops, so the
+// compiler cannot turn it into a per-element select that executes both loads and the conversion.
+template <typename T, typename F>
+__device__ __forceinline__ void with_x(const FxArgs& a, int b, F&& body) {
+  if (sizeof(T) == 4 && a.X32) {
+    const float* x = a.X32 + (size_t)b * a.x32_stride;
+    body([x](size_t e) { return (T)__ldg(x + e); });
+  } else {
+    const double* x = a.X + (size_t)b * a.x_stride;
+    body([x](size_t e) { return (T)__ldg(x + e); });
+  }
+}
+
 // Arithmetic shared by the fused and the split nonlinear-term kernels.  This file is compiled without
 // automatic fma contraction and every multiply-add below is an explicit fma, so both kernels round
 // identically.
@@ -148,29 +163,27 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
 
   // ---- 1. radial contractions of row n (Derivatives, :698-729) and the row values ----
   const int N = M * nr;
-  const double* Xs = a.X + (size_t)b * a.x_stride;
+  with_x<T>(a, b, [&](auto xr) {
   for (int k = tid; k < M; k += bd) {
-    const double* ps = Xs + (size_t)k * nr;
-    const double* ts = Xs + N + (size_t)k * nr;
-    const double* ss = Xs + 2 * N + (size_t)k * nr;
+    const size_t ps = (size_t)k * nr, ts = N + (size_t)k * nr, ss = 2 * (size_t)N + (size_t)k * nr;
     const bool psi_on = !(a.sym && (k % 2 == 0));
     const bool ts_on = !(a.sym && (k % 2 == 1));
     T dp = 0, d2 = 0, dtv = 0, dcv = 0, pn = 0, tn = 0, sn = 0;
     if (psi_on) {
       for (int m = 0; m < nr; ++m) {
-        const T x = (T)__ldg(ps + m);
+        const T x = xr(ps + m);
         dp = fma(opr[m], x, dp);
         d2 = fma(opr[nr + m], x, d2);
       }
-      pn = (T)__ldg(ps + n);
+      pn = xr(ps + n);
     }
     if (ts_on) {
       for (int m = 0; m < nr; ++m) {
-        dtv = fma(opr[m], (T)__ldg(ts + m), dtv);
-        dcv = fma(opr[m], (T)__ldg(ss + m), dcv);
+        dtv = fma(opr[m], xr(ts + m), dtv);
+        dcv = fma(opr[m], xr(ss + m), dcv);
       }
-      tn = (T)__ldg(ts + n);
-      sn = (T)__ldg(ss + n);
+      tn = xr(ts + n);
+      sn = xr(ss + n);
     }
     pv[k] = pn;
     Tv[k] = tn;
@@ -180,6 +193,7 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
     DTv[k] = dtv;
     DCv[k] = dcv;
   }
+  });
   __syncthreads();
   parity_suffix<T>(pv, Sc, M);
   __syncthreads();
@@ -341,11 +355,12 @@ __global__ void __launch_bounds__(256) k_fx_deriv(FxArgs a, T* deriv, size_t der
     ops[nr * nr + e] = D2g[e];
   }
   const int N = M * nr;
-  const double* Xs = a.X + (size_t)b * a.x_stride + (size_t)k * nr;
-  for (int e = threadIdx.x; e < 3 * nr; e += blockDim.x) {
-    const int f = e / nr, m = e - f * nr;
-    xv[e] = (T)__ldg(Xs + (size_t)f * N + m);
-  }
+  with_x<T>(a, b, [&](auto xr) {
+    for (int e = threadIdx.x; e < 3 * nr; e += blockDim.x) {
+      const int f = e / nr, m = e - f * nr;
+      xv[e] = xr((size_t)f * N + (size_t)k * nr + m);
+    }
+  });
   __syncthreads();
   T* D = deriv + (size_t)b * deriv_stride;
   const int nops = a.fuse_rhs ? 5 : 4;
@@ -414,6 +429,7 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
   const int N = M * nr;
   const double* Xs = a.X + (size_t)b * a.x_stride;
   const T* Dv = reinterpret_cast<const T*>(a.deriv) + (size_t)b * a.deriv_stride;   // k_fx_deriv
+  with_x<T>(a, b, [&](auto xr) {
   for (int k = tid; k < M; k += bd) {
     const bool psi_on = !(a.sym && (k % 2 == 0));
     const bool ts_on = !(a.sym && (k % 2 == 1));
@@ -421,13 +437,13 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
     if (psi_on) {
       dp = Dv[(size_t)k * nr + n];
       d2 = Dv[((size_t)M + k) * nr + n];
-      pn = (T)__ldg(Xs + (size_t)k * nr + n);
+      pn = xr((size_t)k * nr + n);
     }
     if (ts_on) {
       dtv = Dv[((size_t)2 * M + k) * nr + n];
       dcv = Dv[((size_t)3 * M + k) * nr + n];
-      tn = (T)__ldg(Xs + N + (size_t)k * nr + n);
-      sn = (T)__ldg(Xs + 2 * N + (size_t)k * nr + n);
+      tn = xr(N + (size_t)k * nr + n);
+      sn = xr(2 * (size_t)N + (size_t)k * nr + n);
     }
     pv[k] = pn;
     Tv[k] = tn;
@@ -442,6 +458,7 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
       pv64[3 * M + k] = ts_on ? __ldg(Xs + 2 * N + (size_t)k * nr + n) : 0.0;
     }
   }
+  });
   __syncthreads();
   if (need_psi) {
     parity_suffix<T>(pv, Sc, M);

@@ -123,6 +123,8 @@ struct FxArgs {
   FxOps ops;
   const double* X;           // state whose nonlinear term (FX) or perturbation (DFX) is formed
   size_t x_stride;           // doubles between shells in X
+  const float* X32;          // nullable: X rounded to FP32, read by the FP32 kernels instead of converting X
+  size_t x32_stride;         // floats between shells in X32
   void* base;                // base-state grid cache [shell][nr][9][P] (T precision), nullable
   size_t base_stride;        // elements between shells in base
   double* out4;              // [shell][4][M][nr] : Qhat, Rhat, NJ_T hat, NJ_S hat
@@ -164,6 +166,8 @@ struct ChainArgs {
   size_t g_stride;
   double* f;                 // solution [shell][3][M][nr]
   size_t f_stride;
+  float* f32;                // nullable: the final solution also rounded to FP32 (the next mixed step's X32)
+  size_t f32_stride;
   const double* sub;         // nullable: f -= sub (Newton residual), same layout
   size_t sub_stride;
   const double* LinvA4, *LinvT, *LinvS;  // [M][nr cols][ldl] transposed blocks
