@@ -645,8 +645,7 @@ static FxArgs fx_args(const sdd_plan* p, int prec, const double* X, void* base, 
   FxArgs a;
   std::memset(&a, 0, sizeof(a));
   a.M = p->M; a.nr = p->nr; a.P = p->P; a.sym = p->sym;
-  a.st.L = p->fft->L; a.st.nst = p->fft->nst;
-  for (int i = 0; i < kMaxStages; ++i) a.st.rad[i] = p->fft->rad[i];
+  a.st = stage_args(p->fft);
   if (prec == SDD_PREC_MIXED) {
     a.ops.Dr = p->Dr32; a.ops.D2r2 = p->D2r232; a.ops.ir4r2 = p->ir4r232;
     a.ops.w = p->fft->w32; a.ops.e = p->fft->e32;
@@ -1368,8 +1367,7 @@ static DiagArgs diag_args(const sdd_plan* p, const double* X, double* out) {
   DiagArgs a;
   std::memset(&a, 0, sizeof(a));
   a.M = p->M; a.nr = p->nr; a.sym = p->sym; a.L = p->dfft->L;
-  a.st.L = p->dfft->L; a.st.nst = p->dfft->nst;
-  for (int i = 0; i < kMaxStages; ++i) a.st.rad[i] = p->dfft->rad[i];
+  a.st = stage_args(p->dfft);
   a.w = p->dfft->w64; a.e = p->dfft->e64;
   a.Dr = p->Dr; a.ir = p->dg_ir; a.tw = p->dg_tw; a.wr = p->dg_wr; a.nuw = p->dg_nuw;
   a.ke_scale = p->ke_scale;

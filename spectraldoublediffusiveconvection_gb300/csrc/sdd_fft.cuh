@@ -88,21 +88,22 @@ __device__ __forceinline__ void butterfly(typename Cplx<T>::type (&v)[R], const 
   }
 }
 
-// One Stockham pass of radix R over nf FFTs of length L stored back to back (stride L).
+// One Stockham pass of radix R over nf FFTs of length L stored back to back (stride L); fnb, fns divide by
+// nb = L / R and by Ns, tws = L / (Ns R) (precomputed per stage).
 template <typename T, bool INV, int R>
 __device__ __forceinline__ void fft_pass_r(const typename Cplx<T>::type* __restrict__ in,
                                            typename Cplx<T>::type* __restrict__ out, int L, int nf, int Ns,
-                                           const typename Cplx<T>::type* w) {
+                                           const typename Cplx<T>::type* w, FastDiv fnb, FastDiv fns, int tws) {
   using C = typename Cplx<T>::type;
   const int nb = L / R;
   const int total = nf * nb;
-  const int tws = L / (Ns * R);
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
-    const int f = t / nb;
+    const int f = (int)fast_div((unsigned)t, fnb);
     const int j = t - f * nb;
     const C* src = in + f * L;
     C* dst = out + f * L;
-    const int k = j % Ns;
+    const int jq = (int)fast_div((unsigned)j, fns);
+    const int k = j - jq * Ns;
     C v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = src[j + r * nb];
@@ -111,7 +112,7 @@ __device__ __forceinline__ void fft_pass_r(const typename Cplx<T>::type* __restr
       for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw_at<T, INV>(w, k * r * tws));
     }
     butterfly<T, INV, R>(v, w, L);
-    const int idxD = (j / Ns) * Ns * R + k;
+    const int idxD = jq * Ns * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) dst[idxD + r * Ns] = v[r];
   }
@@ -120,13 +121,13 @@ __device__ __forceinline__ void fft_pass_r(const typename Cplx<T>::type* __restr
 template <typename T, bool INV>
 __device__ __forceinline__ void fft_pass(const typename Cplx<T>::type* __restrict__ in,
                                          typename Cplx<T>::type* __restrict__ out, int L, int nf, int R, int Ns,
-                                         const typename Cplx<T>::type* w) {
+                                         const typename Cplx<T>::type* w, FastDiv fnb, FastDiv fns, int tws) {
   switch (R) {
-    case 4: fft_pass_r<T, INV, 4>(in, out, L, nf, Ns, w); break;
-    case 2: fft_pass_r<T, INV, 2>(in, out, L, nf, Ns, w); break;
-    case 3: fft_pass_r<T, INV, 3>(in, out, L, nf, Ns, w); break;
-    case 5: fft_pass_r<T, INV, 5>(in, out, L, nf, Ns, w); break;
-    default: fft_pass_r<T, INV, 7>(in, out, L, nf, Ns, w); break;
+    case 4: fft_pass_r<T, INV, 4>(in, out, L, nf, Ns, w, fnb, fns, tws); break;
+    case 2: fft_pass_r<T, INV, 2>(in, out, L, nf, Ns, w, fnb, fns, tws); break;
+    case 3: fft_pass_r<T, INV, 3>(in, out, L, nf, Ns, w, fnb, fns, tws); break;
+    case 5: fft_pass_r<T, INV, 5>(in, out, L, nf, Ns, w, fnb, fns, tws); break;
+    default: fft_pass_r<T, INV, 7>(in, out, L, nf, Ns, w, fnb, fns, tws); break;
   }
 }
 
@@ -141,7 +142,7 @@ __device__ typename Cplx<T>::type* fft_rows(typename Cplx<T>::type* a, typename 
   int Ns = 1;
   for (int s = 0; s < st.nst; ++s) {
     const int R = st.rad[s];
-    fft_pass<T, INV>(in, out, st.L, nf, R, Ns, w);
+    fft_pass<T, INV>(in, out, st.L, nf, R, Ns, w, st.nb[s], st.ns[s], st.tws[s]);
     __syncthreads();
     Ns *= R;
     C* tmp = in; in = out; out = tmp;

@@ -1019,9 +1019,7 @@ cudaError_t launch_transform(int kind, int rows, int n_in, int n_out, const FftP
   a.n_in = n_in;
   a.n_out = n_out;
   a.L = fp->L;
-  a.st.L = fp->L;
-  a.st.nst = fp->nst;
-  for (int i = 0; i < kMaxStages; ++i) a.st.rad[i] = fp->rad[i];
+  a.st = stage_args(fp);
   a.w = fp->w64;
   a.e = fp->e64;
   a.in = in;

@@ -89,10 +89,48 @@ const FftPlan* get_fft_plan(int L);
 
 // Kernel argument blocks -----------------------------------------------------------------------
 
-struct StageArgs {           // radices passed by value
+// Division of n < 2^31 by an invariant d >= 1 with one multiply-high and a shift (Granlund and Montgomery,
+// "Division by invariant integers using multiplication", 1994): with l = ceil(log2 d) and p = 31 + l,
+// m = ceil(2^p / d) < 2^32 and floor(n / d) = floor(n m / 2^p), because m d - 2^p < d <= 2^l and
+// n < 2^31 keep the error below one.  m = 0 encodes d = 1.
+struct FastDiv {
+  unsigned m;
+  int s;                     // p - 32
+};
+inline FastDiv make_fastdiv(unsigned d) {
+  if (d <= 1) return FastDiv{0u, 0};
+  int l = 0;
+  while ((1ull << l) < d) ++l;
+  const int p = 31 + l;
+  return FastDiv{(unsigned)(((1ull << p) + d - 1) / d), p - 32};
+}
+__device__ __forceinline__ unsigned fast_div(unsigned n, FastDiv f) { return f.m ? (__umulhi(n, f.m) >> f.s) : n; }
+
+struct StageArgs {           // radices passed by value, with each stage's divisors precomputed
   int L, nst;
   int rad[kMaxStages];
+  int tws[kMaxStages];       // twiddle stride L / (Ns R) of the stage
+  FastDiv nb[kMaxStages];    // division by L / R (butterflies per transform)
+  FastDiv ns[kMaxStages];    // division by Ns (product of the earlier radices)
 };
+
+inline StageArgs stage_args(const FftPlan* fp) {
+  StageArgs st{};
+  st.L = fp->L;
+  st.nst = fp->nst;
+  int Ns = 1;
+  for (int i = 0; i < kMaxStages; ++i) {
+    st.rad[i] = fp->rad[i];
+    if (i < fp->nst) {
+      const int R = fp->rad[i];
+      st.tws[i] = fp->L / (Ns * R);
+      st.nb[i] = make_fastdiv((unsigned)(fp->L / R));
+      st.ns[i] = make_fastdiv((unsigned)Ns);
+      Ns *= R;
+    }
+  }
+  return st;
+}
 
 struct FxOps {               // FP64 or FP32 copies of the operators the nonlinear term needs
   const void* Dr;            // nr*nr
