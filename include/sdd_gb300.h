@@ -95,11 +95,12 @@ int sdd_plan_destroy(sdd_plan* plan);
 /* Pre-allocates the plan's workspace for up to max_batch shells (otherwise grown on first use). */
 int sdd_plan_reserve(sdd_plan* plan, int max_batch);
 /* Chain-kernel layout of the implicit solves: 0 automatic (chunked while its CTAs fit the GPU at two per
- * SM, layout 3 before 2, else split rows over 4 warps when the launch leaves SMs idle, else one lane per
- * row), 1 one lane per row, 2 chunked (each chain cut into chunks that run concurrently, joined by a
- * short sequential carried-state recurrence), 3 chunked with shorter chunks joined by a parallel carry
- * (precomputed products of the chunk maps, all applied at once), 4 split rows over 4 warps.  Set by the
- * batch autotuner; no counterpart in the reference. */
+ * SM, layout 3 before 2, else split rows over 4 warps when the launch leaves SMs idle, else layout 5),
+ * 1 one lane per row, 2 chunked (each chain cut into chunks that run concurrently, joined by a short
+ * sequential carried-state recurrence), 3 chunked with shorter chunks joined by a parallel carry
+ * (precomputed products of the chunk maps, all applied at once), 4 split rows over 4 warps, 5 split rows
+ * over 2 lanes in 2 warps (nr <= 32; 4 otherwise).  Set by the batch autotuner; no counterpart in the
+ * reference. */
 int sdd_plan_set_chain_layout(sdd_plan* plan, int layout);
 /* The layout (1-4) a step of `batch` shells runs under the current setting, with its chunk length and
  * chunks per chain (0 and 1 when not chunked). */

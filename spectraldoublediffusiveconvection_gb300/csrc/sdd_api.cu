@@ -130,6 +130,7 @@ struct sdd_plan {
   double* xtmp;     // [B][3][M][nr]
   double* hbuf;     // [B][3][M][nr] h = Linv g of the chains
   float* x32[2];    // mixed plans: [B][3][M][nr] FP32 copies of sdd_step's output buffer and of xtmp
+  float* q32;       // mixed plans: [B][M][nr] FP32 copy of the nonlinear term's Q block
   void* base_tmp;   // [B][nr][9][P] (T precision), for DFX without a caller cache
   void* gridbuf;    // [B][nr][9][P] (T precision), grid fields of the split nonlinear-term path
   void* derivbuf;   // [B] x (5 M nr doubles of room), radial derivatives of the split path: 4 M nr of the
@@ -251,7 +252,7 @@ static void free_plan(sdd_plan* p) {
     for (const double* x : t) cudaFree(const_cast<double*>(x));
   }
   cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232);
-  cudaFree(p->x32[0]); cudaFree(p->x32[1]);
+  cudaFree(p->x32[0]); cudaFree(p->x32[1]); cudaFree(p->q32);
   cudaFree(p->base_tmp);
   cudaFree(p->gridbuf);
   cudaFree(p->derivbuf);
@@ -578,7 +579,7 @@ int sdd_plan_set_fx_split(sdd_plan* p, int mode) {
 }
 
 int sdd_plan_set_chain_layout(sdd_plan* p, int layout) {
-  if (!p || layout < 0 || layout > 4) return SDD_ERR_ARG;
+  if (!p || layout < 0 || layout > 5) return SDD_ERR_ARG;
   if (p->chain_layout != layout) clear_step_graphs(p);
   p->chain_layout = layout;
   return SDD_OK;
@@ -607,8 +608,9 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   cudaFree(p->out4); cudaFree(p->rhs); cudaFree(p->xtmp); cudaFree(p->base_tmp); cudaFree(p->hbuf);
   cudaFree(p->dbuf); cudaFree(p->cbuf); cudaFree(p->gridbuf); cudaFree(p->derivbuf);
   cudaFree(p->dg_part); cudaFree(p->dg_out); cudaFree(p->dcnt); cudaFree(p->pbuf);
-  cudaFree(p->x32[0]); cudaFree(p->x32[1]);
+  cudaFree(p->x32[0]); cudaFree(p->x32[1]); cudaFree(p->q32);
   p->x32[0] = p->x32[1] = nullptr;
+  p->q32 = nullptr;
   p->dg_part = p->dg_out = nullptr;
   p->dcnt = nullptr;
   p->pbuf = nullptr;
@@ -632,8 +634,10 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   SDD_CUDA(cudaMalloc(&p->dbuf, (size_t)max_batch * de * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->cbuf, (size_t)max_batch * de * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->pbuf, (size_t)max_batch * 6 * p->np_alloc * p->ldd * sizeof(double)));
-  if (p->prec == SDD_PREC_MIXED)
+  if (p->prec == SDD_PREC_MIXED) {
     for (float*& x : p->x32) SDD_CUDA(cudaMalloc(&x, (size_t)max_batch * se * sizeof(float)));
+    SDD_CUDA(cudaMalloc(&p->q32, (size_t)max_batch * p->M * p->nr * sizeof(float)));
+  }
   p->ws_batch = max_batch;
   return SDD_OK;
 }
@@ -725,6 +729,10 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
                          float* x32_out = nullptr) {
   RhsArgs ra = rhs_args(p, X, p->out4, Ra, Ras, p->rhs, mode == 2);
   ra.x_stride = ldx;
+  if (prec == SDD_PREC_MIXED && mode != 2) {   // the FP32 nonlinear term's Q, for an FP32 Dr Q
+    ra.q32 = p->q32;
+    ra.Dr32 = p->Dr32;
+  }
   bool fuse = false;
   if (ev) SDD_CUDA(cudaEventRecord(ev[0], s));
   if (mode != 2) {
@@ -734,6 +742,7 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
       fa.X32 = x32_in;
       fa.x32_stride = shell_elems(p);
     }
+    if (prec == SDD_PREC_MIXED) fa.q32 = p->q32;
     const int fm = mode == 1 ? 1 : 0;
     fuse = fx_uses_split(fa, batch, fm);
     if (fuse) {
@@ -758,6 +767,8 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
     ca.out4 = p->out4;
     ca.out_stride = (size_t)4 * p->M * p->nr;
     ca.Dr = p->Dr;
+    ca.q32 = ra.q32;
+    ca.Dr32 = ra.Dr32;
     ca.dt = p->dt;
   }
   SDD_CUDA(launch_chain(ca, batch, 3, s));

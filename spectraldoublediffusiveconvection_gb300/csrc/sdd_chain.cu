@@ -84,10 +84,18 @@ __device__ __forceinline__ double fused_g(const ChainArgs& a, int b, int field, 
   const double* o4 = a.out4 + (size_t)b * a.out_stride;
   double nl;
   if (field == 0) {
-    const double* qs = Qs ? Qs : o4 + (size_t)row * nr;
-    const double* drn = (Drs ? Drs : a.Dr) + (size_t)n * nr;
     double dq = 0.0;
-    for (int c = 0; c < nr; ++c) dq = fma(drn[c], qs[c], dq);
+    if (a.q32) {            // FP32 nonlinear term: Dr Q in FP32, the order of k_rhs
+      const float* qs = a.q32 + (size_t)b * M * nr + (size_t)row * nr;
+      const float* drn = a.Dr32 + (size_t)n * nr;
+      float d = 0.0f;
+      for (int c = 0; c < nr; ++c) d = fmaf(__ldg(drn + c), __ldg(qs + c), d);
+      dq = (double)d;
+    } else {
+      const double* qs = Qs ? Qs : o4 + (size_t)row * nr;
+      const double* drn = (Drs ? Drs : a.Dr) + (size_t)n * nr;
+      for (int c = 0; c < nr; ++c) dq = fma(drn[c], qs[c], dq);
+    }
     nl = __dmul_rn(-a.dt, __dsub_rn(dq, o4[N + (size_t)row * nr + n]));
   } else {
     nl = __dmul_rn(-a.dt, o4[(size_t)(field + 1) * N + (size_t)row * nr + n]);
@@ -188,9 +196,22 @@ __global__ void k_chain(ChainArgs a) {
     if (a4) {
       const double pre = fma(cf[4 * s + 3], fe, bfe);   // bf_e + bjt f_e, off the matvec's path
       double acc = (q == 0) ? hi : 0.0;
-      if (s > 0)
+      if (TPR == 1) {                          // one lane per row: two interleaved partial sums
+        double acc1 = 0.0;
+        if (s > 0) {
+          int c = 0;
+#pragma unroll 4
+          for (; c + 1 < ncol; c += 2) {
+            acc = fma(cur[c * ldl + ir], xs[c], acc);
+            acc1 = fma(cur[(c + 1) * ldl + ir], xs[c + 1], acc1);
+          }
+          if (c < ncol) acc = fma(cur[c * ldl + ir], xs[c], acc);
+        }
+        acc += acc1;
+      } else if (s > 0) {
 #pragma unroll 8
         for (int c = q; c < ncol; c += TPR) acc = fma(cur[c * ldl + ir], xs[c], acc);
+      }
       fi = group_sum<TPR>(acc);
       fe += fi;
       bfe = fma(cf[4 * s + 2], fi, pre);
@@ -200,8 +221,20 @@ __global__ void k_chain(ChainArgs a) {
       }
     } else {
       double acc = 0.0;
+      if (TPR == 1) {                          // one lane per row: two interleaved partial sums
+        double acc1 = 0.0;
+        int c = 0;
+#pragma unroll 4
+        for (; c + 1 < nr; c += 2) {
+          acc = fma(cur[c * ldl + ir], xs[c], acc);
+          acc1 = fma(cur[(c + 1) * ldl + ir], xs[c + 1], acc1);
+        }
+        if (c < nr) acc = fma(cur[c * ldl + ir], xs[c], acc);
+        acc += acc1;
+      } else {
 #pragma unroll 8
-      for (int c = q; c < nr; c += TPR) acc = fma(cur[c * ldl + ir], xs[c], acc);
+        for (int c = q; c < nr; c += TPR) acc = fma(cur[c * ldl + ir], xs[c], acc);
+      }
       fi = fma(-cf[4 * s + 1], group_sum<TPR>(acc), hi);
       fe = fma(cf[4 * (s + 1)], fi, fe);       // the b of the next step (of the next chunk after the last)
       if (lead) xn[i] = fe;
@@ -464,7 +497,7 @@ __global__ void __launch_bounds__(128) k_mode_mv(ChainArgs a) {
       double* Drs = msm + (size_t)nr * ldl;            // Dr (nr x nr), the Q row, then g
       double* Qs = Drs + (size_t)nr * nr;
       double* gsm = Qs + nr;
-      if (a4) {
+      if (a4 && !a.q32) {
         for (int e = threadIdx.x; e < nr * nr; e += blockDim.x) Drs[e] = a.Dr[e];
         const double* q4 = a.out4 + (size_t)b * a.out_stride + (size_t)row * nr;
         for (int e = threadIdx.x; e < nr; e += blockDim.x) Qs[e] = q4[e];
@@ -673,8 +706,10 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
 }
 
 // One CTA per chain.  When the batch leaves SMs idle (2*nfields*batch <= #SMs) the 4-warp split-row
-// layout gives the shortest chain; otherwise the one-lane-per-row layout issues the fewest FP64
-// instructions and several chains share every SM.  Layout 2 (chunked: nch CTAs per chain, a short
+// layout gives the shortest chain; otherwise rows split over 2 lanes in 2 warps (layout 5, nr <= 32):
+// fewer FP64 instructions per step than 4 lanes (one shuffle-add level, half the warps repeating the
+// per-row updates), and two chains share an SM's sub-partitions (64-shell batch: 0.60 vs 0.63 ms per
+// step, and 0.79 with one lane per row).  Layout 2 (chunked: nch CTAs per chain, a short
 // carried-state recurrence and a parallel correction) is chosen automatically while all its CTAs fit
 // on the GPU at two per SM.  a.g holds the right-hand sides; a.h receives h = Linv g (k_mode_mv), which
 // is what the chains read.
@@ -693,7 +728,8 @@ int resolve_chain_layout(const ChainArgs& a, int batch, int nfields) {
   if (layout == 0 && c2.nch > 1 && c2.GA4 && 2 * nfields * batch * c2.nch <= 2 * sms) layout = 2;
   if (layout != 2 && layout != 3 && chain_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin)
     layout = 2;   // whole chain too long for shared memory
-  if (layout == 0) layout = 2 * nfields * batch <= sms ? 4 : 1;
+  if (layout == 0) layout = 2 * nfields * batch <= sms ? 4 : 5;
+  if (layout == 5 && a.nr > 32) layout = 4;
   return layout;
 }
 
@@ -713,6 +749,19 @@ cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStre
     return launch_chunked(a, batch, nfields, s);
   }
   const bool split = layout == 4;
+  if (layout == 5 && a.nr <= 32) {   // rows split over 2 lanes, 2 warps per chain
+    cudaError_t e = launch_mode_mv<false>(a, batch, nfields, s, mv_per_warp(a, batch, nfields));
+    if (e != cudaSuccess) return e;
+    a.g = a.h;
+    a.g_stride = a.h_stride;
+    static unsigned long long done = 0;
+    if ((e = ensure_smem_attr(k_chain<2, false>, &done)) != cudaSuccess) return e;
+    if ((e = launch_kernel(k_chain<2, false>, dim3(2 * nfields, batch), dim3(64), chain_smem_bytes(a.M, a.nr, a.ldl),
+                           s, a)) != cudaSuccess)
+      return e;
+    ktimer_mark(SDD_K_CHAIN, s);
+    return cudaGetLastError();
+  }
   cudaError_t e = launch_mode_mv<false>(a, batch, nfields, s, mv_per_warp(a, batch, nfields));   // h = Linv g
   if (e != cudaSuccess) return e;
   a.g = a.h;

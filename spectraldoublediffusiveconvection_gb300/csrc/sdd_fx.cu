@@ -308,6 +308,7 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
     const size_t q0 = (size_t)(2 * p) * N + (size_t)s * nr + n;
     o[q0] = (double)ya;
     o[q0 + N] = (double)yb;
+    if (sizeof(T) == 4 && p == 0 && a.q32) a.q32[(size_t)b * M * a.nr + (size_t)s * a.nr + n] = (float)ya;
   }
 }
 
@@ -608,6 +609,7 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_prod(FxArgs a, const T* 
     const size_t q0 = (size_t)(2 * p) * N + (size_t)s * nr + n;
     o[q0] = (double)ya;
     o[q0 + N] = (double)yb;
+    if (sizeof(T) == 4 && p == 0 && a.q32) a.q32[(size_t)b * M * a.nr + (size_t)s * a.nr + n] = (float)ya;
   }
 }
 
@@ -642,7 +644,13 @@ __global__ void __launch_bounds__(kFxThreads) k_rhs(RhsArgs a) {
       for (int m = 0; m < nr; ++m) d2 = fma(opr[nr + m], __ldg(ps + m), d2);
       pn = __ldg(ps + n);
     }
-    if (O4) {
+    if (O4 && a.q32) {         // FP32 nonlinear term: Dr Q in FP32 (the order of the chains' fused_g)
+      const float* qs = a.q32 + (size_t)b * M * nr + (size_t)k * nr;
+      const float* drn = a.Dr32 + (size_t)n * nr;
+      float d = 0.0f;
+      for (int m = 0; m < nr; ++m) d = fmaf(__ldg(drn + m), __ldg(qs + m), d);
+      q = (double)d;
+    } else if (O4) {
       const double* qs = O4 + (size_t)k * nr;
       for (int m = 0; m < nr; ++m) q = fma(opr[m], __ldg(qs + m), q);
     }

@@ -153,6 +153,10 @@ struct RhsArgs {
   const double* Ra, *Ra_s;   // per shell
   double* rhs;               // [shell][3][M][nr]
   size_t rhs_stride;
+  // mixed plans: Q (out4's first block) also in FP32, [shell][M][nr]; then Dr Q is an FP32 contraction
+  // (part of the FP32 nonlinear term) with Dr32, converted to FP64 once
+  const float* q32;
+  const float* Dr32;
 };
 
 struct FxArgs {
@@ -163,6 +167,7 @@ struct FxArgs {
   size_t x_stride;           // doubles between shells in X
   const float* X32;          // nullable: X rounded to FP32, read by the FP32 kernels instead of converting X
   size_t x32_stride;         // floats between shells in X32
+  float* q32;                // nullable (FP32 kernels): Q also written in FP32, [shell][M][nr]
   void* base;                // base-state grid cache [shell][nr][9][P] (T precision), nullable
   size_t base_stride;        // elements between shells in base
   double* out4;              // [shell][4][M][nr] : Qhat, Rhat, NJ_T hat, NJ_S hat
@@ -223,6 +228,7 @@ struct ChainArgs {
   const double* out4;        // [shell][4][M][nr]
   size_t out_stride;
   const double* Dr;          // nr*nr (FP64)
+  const float* q32, *Dr32;   // mixed plans: Dr Q in FP32 (see RhsArgs)
   double dt;                 // the step's dt
   // chunked (parallel-in-modes) chains, layout 2: every chain of S = N_fm/2 steps is cut into nch chunks
   // of kc steps.  Chunk c runs from a zero carried state (f_local, end state d_c); the carried states

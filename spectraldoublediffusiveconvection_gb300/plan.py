@@ -55,6 +55,8 @@ class Plan:
         self.nr = self.N_r - 1
         self.symmetric = bool(symmetric)
         self.precision = precision
+        self.chain_layout = 0          # automatic (sdd_plan_set_chain_layout)
+        self.fx_split = 0              # automatic (sdd_plan_set_fx_split)
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.arrays = arrays if arrays is not None else plan_arrays(N_fm, N_r, d, dt, Pr, Tau)
         A = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in self.arrays.items()
@@ -129,7 +131,8 @@ class Plan:
 
     def set_chain_layout(self, layout):
         """0 automatic, 1 one lane per row, 2 chunked (sequential carry), 3 chunked (parallel carry), 4 rows
-        split over 4 warps (sdd_plan_set_chain_layout); the results agree to rounding."""
+        split over 4 warps, 5 rows split over 2 lanes in 2 warps (sdd_plan_set_chain_layout); the results
+        agree to rounding."""
         _lib.check(self._L.sdd_plan_set_chain_layout(self._h, int(layout)), "sdd_plan_set_chain_layout")
         self.chain_layout = int(layout)
 
