@@ -726,9 +726,10 @@ static int check_plan(sdd_plan* p, int batch) {
 static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X, size_t ldx,
                          double* out, size_t ldo, const double* sub, size_t lds, int mode, void* base, int prec,
                          cudaStream_t s, cudaEvent_t* ev = nullptr, const float* x32_in = nullptr,
-                         float* x32_out = nullptr) {
+                         float* x32_out = nullptr, const int* active = nullptr) {
   RhsArgs ra = rhs_args(p, X, p->out4, Ra, Ras, p->rhs, mode == 2);
   ra.x_stride = ldx;
+  ra.active = active;
   if (prec == SDD_PREC_MIXED && mode != 2) {   // the FP32 nonlinear term's Q, for an FP32 Dr Q
     ra.q32 = p->q32;
     ra.Dr32 = p->Dr32;
@@ -738,6 +739,7 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
   if (mode != 2) {
     FxArgs fa = fx_args(p, prec, X, base, p->out4);
     fa.x_stride = ldx;
+    fa.active = active;
     if (prec == SDD_PREC_MIXED && mode == 0) {
       fa.X32 = x32_in;
       fa.x32_stride = shell_elems(p);
@@ -757,6 +759,7 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
   ChainArgs ca = chain_args(p, p->rhs, out, sub);
   ca.f_stride = ldo;
   ca.sub_stride = lds;
+  ca.active = active;
   if (prec == SDD_PREC_MIXED && mode == 0 && !sub) {
     ca.f32 = x32_out;
     ca.f32_stride = shell_elems(p);
@@ -976,6 +979,7 @@ static int solver_reserve(sdd_plan* p, int B, int m) {
   const size_t vb = (size_t)B * ld * sizeof(double);
   SDD_CUDA(cudaMalloc(&p->kv_V, (size_t)(m + 1) * vb));
   SDD_CUDA(cudaMalloc(&p->kv_w, vb));
+  SDD_CUDA(cudaMemset(p->kv_w, 0, vb));   // shells a masked matvec skips keep finite values here
   SDD_CUDA(cudaMalloc(&p->kv_r, vb));
   SDD_CUDA(cudaMalloc(&p->kv_part, (size_t)B * (m + 1) * nchunk * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->kv_nrm2, (size_t)B * sizeof(double)));
@@ -1020,8 +1024,9 @@ static GmresState gmres_state(sdd_plan* p, int B, int m) {
   return s;
 }
 
-// Device matvec on B shells: out = A v (vectors of stride ld).
-using MatVec = std::function<int(const double* v, double* out)>;
+// Device matvec on B shells: out = A v (vectors of stride ld); shells whose flag in `active` (device,
+// nullable) is 0 may be skipped, their part of out left as it was.
+using MatVec = std::function<int(const double* v, double* out, const int* active)>;
 
 // Restarted GMRES(m), CGS2, for the shells with solve[b] != 0: A x = rhs, x starts at 0, inner stop
 // |r_b| <= target[b] (absolute).  x, rhs have stride ld with nu used doubles.  resid (host) receives the
@@ -1040,7 +1045,7 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const double* rhs, double* 
   for (int cyc = 0; cyc < max_restarts; ++cyc) {
     const double* r = rhs;
     if (cyc > 0) {                                   // r = rhs - A x
-      if ((st = A(x, p->kv_w))) return st;
+      if ((st = A(x, p->kv_w, G.solve))) return st;
       ++*matvecs;
       SDD_CUDA(krylov_sub(rhs, p->kv_w, p->kv_r, vs, s));
       r = p->kv_r;
@@ -1050,7 +1055,7 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const double* rhs, double* 
     SDD_CUDA(krylov_scale(r, G.inv, p->kv_V, nu, ld, B, s));
     for (int j = 0; j < m; ++j) {
       double* Vj = p->kv_V + (size_t)j * vs;
-      if ((st = A(Vj, p->kv_w))) return st;
+      if ((st = A(Vj, p->kv_w, G.active))) return st;
       ++*matvecs;
       SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.hcol, m + 1, 0, s));
       SDD_CUDA(krylov_sub_combination(p->kv_V, vs, p->kv_w, G.hcol, m + 1, nu, ld, j + 1, B, s));
@@ -1106,8 +1111,9 @@ extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const doub
   std::vector<int> nmask(B, 0), iters(B, 0);
   int matvecs = 0;
   // the Jacobian of PFX about the cached base state, on vectors of stride ld
-  MatVec J = [&](const double* v, double* out) {
-    return apply_step_ld(p, B, Ra, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s);
+  MatVec J = [&](const double* v, double* out, const int* active) {
+    return apply_step_ld(p, B, Ra, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s, nullptr, nullptr, nullptr,
+                         active);
   };
   for (int it = 0;; ++it) {
     if ((st = apply_step_ld(p, B, Ra, Ras, X, n, p->sv_F, ld, X, n, 0, p->sv_base64, SDD_PREC_FP64, s)))
@@ -1193,12 +1199,14 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
     }
     return pdfmu(p, B, Xs, n, s);
   };
-  MatVec J = [&](const double* v, double* out) {
-    return apply_step_ld(p, B, mu_dev, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s);
+  MatVec J = [&](const double* v, double* out, const int* active) {
+    return apply_step_ld(p, B, mu_dev, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s, nullptr, nullptr, nullptr,
+                         active);
   };
   // bordered operator DG = [[DF_X, DF_mu], [delta X_dot^T, (1-delta) mu_dot]]  (Main.py:914-915)
-  MatVec DG = [&](const double* v, double* out) -> int {
-    int r = apply_step_ld(p, B, mu_dev, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s);
+  MatVec DG = [&](const double* v, double* out, const int* active) -> int {
+    int r = apply_step_ld(p, B, mu_dev, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s, nullptr, nullptr,
+                          nullptr, active);
     if (r) return r;
     SDD_CUDA(krylov_dots(p->sv_Xd, 0, v, n, ld, 1, B, p->kv_part, p->kv_dot, 1, 0, s));
     SDD_CUDA(contin_border(v, out, n, ld, p->sv_Jmu, n, Npsi, p->kv_dot, mudot_dev, delta, B, s));

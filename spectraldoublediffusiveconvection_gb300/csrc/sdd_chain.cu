@@ -116,6 +116,7 @@ __global__ void k_chain(ChainArgs a) {
   const int field = a.field0 + (blockIdx.x >> 1);
   const int par = blockIdx.x & 1;  // first jj of the chain
   const int b = blockIdx.y;
+  if (a.active && !a.active[b]) return;
   const int M = a.M, nr = a.nr, ldl = a.ldl;
   const bool a4 = (field == 0);
   const size_t foff = (size_t)field * a.field_off;
@@ -391,6 +392,7 @@ __global__ void __launch_bounds__(128) k_carry_par(ChainArgs a) {
   const int b = blockIdx.y, pidx = blockIdx.z;
   const bool a4 = field == 0;
   if (a.sym && !(a4 ? par == 0 : par == 1)) return;    // inactive chain: its carried states are not read
+  if (a.active && !a.active[b]) return;
   int j = 2;
   while (j * (j - 1) / 2 <= pidx) ++j;                 // row j holds products (j-1)(j-2)/2 .. j(j-1)/2 - 1
   const int i = pidx - (j - 1) * (j - 2) / 2;
@@ -447,6 +449,7 @@ __global__ void __launch_bounds__(128) k_mode_mv(ChainArgs a) {
   const int fl = blockIdx.x / M, jj = blockIdx.x - fl * M;
   const int field = a.field0 + fl;
   const int b = blockIdx.y;
+  if (a.active && !a.active[b]) return;
   const int row = M - 1 - jj;
   const size_t foff = (size_t)field * a.field_off;
   const bool a4 = field == 0;
@@ -540,6 +543,7 @@ __global__ void __launch_bounds__(128) k_mode_mv_warp(ChainArgs a, int nfields) 
   const int fl = wid / M, jj = wid - fl * M;
   const int field = a.field0 + fl;
   const int b = blockIdx.y;
+  if (a.active && !a.active[b]) return;
   const int row = M - 1 - jj;
   const size_t foff = (size_t)field * a.field_off;
   const bool a4 = field == 0;

@@ -157,6 +157,7 @@ struct RhsArgs {
   // (part of the FP32 nonlinear term) with Dr32, converted to FP64 once
   const float* q32;
   const float* Dr32;
+  const int* active;         // nullable: per-shell flags; kernels skip shells whose flag is 0
 };
 
 struct FxArgs {
@@ -168,6 +169,8 @@ struct FxArgs {
   const float* X32;          // nullable: X rounded to FP32, read by the FP32 kernels instead of converting X
   size_t x32_stride;         // floats between shells in X32
   float* q32;                // nullable (FP32 kernels): Q also written in FP32, [shell][M][nr]
+  const int* active;         // nullable: per-shell flags; kernels skip shells whose flag is 0 (their
+                             // outputs are left as they were: Krylov solves mask those shells out)
   void* base;                // base-state grid cache [shell][nr][9][P] (T precision), nullable
   size_t base_stride;        // elements between shells in base
   double* out4;              // [shell][4][M][nr] : Qhat, Rhat, NJ_T hat, NJ_S hat
@@ -251,6 +254,7 @@ struct ChainArgs {
   double* pbuf;              // [shell][6][np][ldd] products P_{j,i} d_i
   size_t p_stride;           // doubles per shell in pbuf
   ChunkSet cset[2];          // the chunkings of layouts 2 and 3 (launch_chain copies one into the fields above)
+  const int* active;         // nullable: per-shell flags; kernels skip shells whose flag is 0
 };
 
 struct DiagArgs {
