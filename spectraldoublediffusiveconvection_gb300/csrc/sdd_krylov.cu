@@ -16,27 +16,55 @@ namespace sdd {
 
 constexpr int kDotThreads = 256;
 
-// part[(b*(nv) + i)*nchunk + c] = sum over chunk c of V_i[b] . w[b],  i < nv
+// part[(b*(nv) + i)*nchunk + c] = sum over chunk c of V_i[b] . w[b],  i < nv.
+// The chunk of w sits in registers (kDotPer elements per thread); the vectors go kDotVecs at a time, so
+// each thread has kDotVecs * kDotPer independent loads in flight and a block reduction serves kDotVecs
+// dot products (the products are FP64-throughput bound on this GPU, about 5 TB/s of V).  Each partial is
+// a fixed-order sum: per thread over its elements in index order, then the shuffle tree, then the warps
+// in order.
+constexpr int kDotPer = kDotChunk / kDotThreads;
+constexpr int kDotVecs = 4;
+static_assert(kDotChunk % kDotThreads == 0, "dot chunk must be a multiple of the block");
+
 __global__ void __launch_bounds__(kDotThreads) k_dot_partials(const double* __restrict__ V, size_t vstride_i,
                                                              const double* __restrict__ w, int n, int ld, int nv,
                                                              int chunk, double* __restrict__ part) {
-  __shared__ double red[kDotThreads / 32];
+  __shared__ double red[kDotVecs][kDotThreads / 32];
   const int c = blockIdx.x, b = blockIdx.y, nchunk = gridDim.x;
-  const int e0 = c * chunk, e1 = min(n, e0 + chunk);
+  const int e0 = c * chunk;
   const double* wb = w + (size_t)b * ld;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int i = 0; i < nv; ++i) {
-    const double* vb = V + (size_t)i * vstride_i + (size_t)b * ld;
-    double s = 0.0;
-    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) s += vb[e] * wb[e];
+  double wr[kDotPer];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-    if (lane == 0) red[warp] = s;
+  for (int k = 0; k < kDotPer; ++k) {
+    const int e = e0 + threadIdx.x + k * kDotThreads;
+    wr[k] = e < n ? wb[e] : 0.0;
+  }
+  for (int i0 = 0; i0 < nv; i0 += kDotVecs) {
+    double sv[kDotVecs];
+#pragma unroll
+    for (int u = 0; u < kDotVecs; ++u) {
+      sv[u] = 0.0;
+      if (i0 + u < nv) {
+        const double* vb = V + (size_t)(i0 + u) * vstride_i + (size_t)b * ld;
+#pragma unroll
+        for (int k = 0; k < kDotPer; ++k) {
+          const int e = e0 + threadIdx.x + k * kDotThreads;
+          if (e < n) sv[u] = fma(vb[e], wr[k], sv[u]);
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kDotVecs; ++u) {
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) sv[u] += __shfl_xor_sync(0xffffffffu, sv[u], off);
+      if (lane == 0) red[u][warp] = sv[u];
+    }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < kDotVecs && i0 + threadIdx.x < nv) {
       double t = 0.0;
-      for (int q = 0; q < (int)(blockDim.x / 32); ++q) t += red[q];
-      part[((size_t)b * nv + i) * nchunk + c] = t;
+      for (int q = 0; q < kDotThreads / 32; ++q) t += red[threadIdx.x][q];
+      part[((size_t)b * nv + i0 + threadIdx.x) * nchunk + c] = t;
     }
     __syncthreads();
   }

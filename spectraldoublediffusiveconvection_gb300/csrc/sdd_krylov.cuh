@@ -5,7 +5,7 @@
 
 namespace sdd {
 
-constexpr int kDotChunk = 4096;   // elements per CTA in the two-level dot products
+constexpr int kDotChunk = 2048;   // elements per CTA in the two-level dot products
 
 struct GmresState {
   int m;            // restart length
