@@ -468,7 +468,7 @@ def bench_gb300(args):
         # space), FP32 nonlinear term inside the Jacobian products, FP64 residual <= 1e-10
         nb = 64
         planm = Plan(M, N_r, w["d"], 1.0, w["Pr"], w["Tau"], precision="mixed", device=device)
-        planm.set_chain_layout(5)      # whole chains, rows split over 2 lanes: the 64-shell batch layout
+        planm.set_chain_layout(4)      # whole chains, split rows: measured best for the 64-shell Newton batch
         pert = torch.from_numpy(np.stack([seeded_state(M, N_r - 1, 500 + i) for i in range(nb)])).to(device)
         Xb0 = X_after.reshape(1, -1) + pert
         Rab = torch.linspace(7000.0, 9000.0, nb, dtype=torch.float64, device=device)
