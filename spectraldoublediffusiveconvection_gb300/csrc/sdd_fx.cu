@@ -124,6 +124,7 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int M = a.M, nr = a.nr, P = a.P;
   const int n = blockIdx.x, b = blockIdx.y;
+  if (a.active && !a.active[b]) return;
   const int tid = threadIdx.x, bd = blockDim.x;
 
   C* RA = reinterpret_cast<C*>(smem_raw);
@@ -347,6 +348,7 @@ __global__ void __launch_bounds__(256) k_fx_deriv(FxArgs a, T* deriv, size_t der
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int M = a.M, nr = a.nr;
   const int k = blockIdx.x, b = blockIdx.y;
+  if (a.active && !a.active[b]) return;
   T* ops = reinterpret_cast<T*>(smem_raw);     // Dr, D2r2 (nr x nr each, row-major)
   T* xv = ops + 2 * nr * nr;                  // psi_k, T_k, S_k
   const T* Drg = reinterpret_cast<const T*>(a.ops.Dr);
@@ -389,6 +391,7 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int M = a.M, nr = a.nr, P = a.P;
   const int n = blockIdx.x, pr = blockIdx.y, b = blockIdx.z;
+  if (a.active && !a.active[b]) return;
   const int tid = threadIdx.x, bd = blockDim.x;
   const int ta = 2 * pr, tb = 2 * pr + 1;      // tb = 9 (absent) for the last pair
 
@@ -545,6 +548,7 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_prod(FxArgs a, const T* 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int M = a.M, nr = a.nr, P = a.P;
   const int n = blockIdx.x, p = blockIdx.y, b = blockIdx.z;
+  if (a.active && !a.active[b]) return;
   const int tid = threadIdx.x, bd = blockDim.x;
   C* RA = reinterpret_cast<C*>(smem_raw);
   C* RB = RA + P;
@@ -618,6 +622,7 @@ __global__ void __launch_bounds__(kFxThreads) k_rhs(RhsArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int M = a.M, nr = a.nr;
   const int n = blockIdx.x, b = blockIdx.y;
+  if (a.active && !a.active[b]) return;
   const int tid = threadIdx.x, bd = blockDim.x;
   double* sm = reinterpret_cast<double*>(smem_raw);
   double* pv = sm;
