@@ -1057,11 +1057,12 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const double* rhs, double* 
       double* Vj = p->kv_V + (size_t)j * vs;
       if ((st = A(Vj, p->kv_w, G.active))) return st;
       ++*matvecs;
-      SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.hcol, m + 1, 0, s));
-      SDD_CUDA(krylov_sub_combination(p->kv_V, vs, p->kv_w, G.hcol, m + 1, nu, ld, j + 1, B, s));
-      SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.h2, m + 1, 0, s));
-      SDD_CUDA(krylov_sub_combination(p->kv_V, vs, p->kv_w, G.h2, m + 1, nu, ld, j + 1, B, s));
-      SDD_CUDA(krylov_dots(p->kv_w, 0, p->kv_w, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s));
+      // shells whose Arnoldi process has stopped skip the Gram-Schmidt work (krylov_arnoldi_finish ignores them)
+      SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.hcol, m + 1, 0, s, G.active));
+      SDD_CUDA(krylov_sub_combination(p->kv_V, vs, p->kv_w, G.hcol, m + 1, nu, ld, j + 1, B, s, G.active));
+      SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.h2, m + 1, 0, s, G.active));
+      SDD_CUDA(krylov_sub_combination(p->kv_V, vs, p->kv_w, G.h2, m + 1, nu, ld, j + 1, B, s, G.active));
+      SDD_CUDA(krylov_dots(p->kv_w, 0, p->kv_w, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s, G.active));
       SDD_CUDA(krylov_arnoldi_finish(G, p->kv_nrm2, j, B, s));
       if (j + 1 < m) SDD_CUDA(krylov_scale(p->kv_w, G.inv, p->kv_V + (size_t)(j + 1) * vs, nu, ld, B, s));
       SDD_CUDA(cudaMemcpyAsync(p->h_int, G.active, B * sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -28,9 +28,14 @@ static_assert(kDotChunk % kDotThreads == 0, "dot chunk must be a multiple of the
 
 __global__ void __launch_bounds__(kDotThreads) k_dot_partials(const double* __restrict__ V, size_t vstride_i,
                                                              const double* __restrict__ w, int n, int ld, int nv,
-                                                             int chunk, double* __restrict__ part) {
+                                                             int chunk, double* __restrict__ part,
+                                                             const int* __restrict__ active) {
   __shared__ double red[kDotVecs][kDotThreads / 32];
   const int c = blockIdx.x, b = blockIdx.y, nchunk = gridDim.x;
+  if (active && !active[b]) {                         // skipped shell: zero partials (its results are unused)
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) part[((size_t)b * nv + i) * nchunk + c] = 0.0;
+    return;
+  }
   const int e0 = c * chunk;
   const double* wb = w + (size_t)b * ld;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -85,8 +90,10 @@ __global__ void k_dot_reduce(const double* __restrict__ part, int nv, int nchunk
 
 // w[b] -= sum_{i<nv} V_i[b] * coef[b*ldc + i]
 __global__ void k_sub_combination(const double* __restrict__ V, size_t vstride_i, double* __restrict__ w,
-                                  const double* __restrict__ coef, int ldc, int n, int ld, int nv) {
+                                  const double* __restrict__ coef, int ldc, int n, int ld, int nv,
+                                  const int* __restrict__ active) {
   const int b = blockIdx.y;
+  if (active && !active[b]) return;
   const double* cb = coef + (size_t)b * ldc;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
     double s = 0.0;
@@ -267,16 +274,16 @@ static int grid_x(int n) {
 }
 
 cudaError_t krylov_dots(const double* V, size_t vstride_i, const double* w, int n, int ld, int nv, int B,
-                        double* part, double* h, int ldh, int accumulate, cudaStream_t st) {
+                        double* part, double* h, int ldh, int accumulate, cudaStream_t st, const int* active) {
   const int nchunk = (n + kDotChunk - 1) / kDotChunk;
-  k_dot_partials<<<dim3(nchunk, B), kDotThreads, 0, st>>>(V, vstride_i, w, n, ld, nv, kDotChunk, part);
+  k_dot_partials<<<dim3(nchunk, B), kDotThreads, 0, st>>>(V, vstride_i, w, n, ld, nv, kDotChunk, part, active);
   k_dot_reduce<<<B, 64, 0, st>>>(part, nv, nchunk, h, ldh, accumulate);
   return cudaGetLastError();
 }
 
 cudaError_t krylov_sub_combination(const double* V, size_t vstride_i, double* w, const double* coef, int ldc,
-                                   int n, int ld, int nv, int B, cudaStream_t st) {
-  k_sub_combination<<<dim3(grid_x(n), B), 256, 0, st>>>(V, vstride_i, w, coef, ldc, n, ld, nv);
+                                   int n, int ld, int nv, int B, cudaStream_t st, const int* active) {
+  k_sub_combination<<<dim3(grid_x(n), B), 256, 0, st>>>(V, vstride_i, w, coef, ldc, n, ld, nv, active);
   return cudaGetLastError();
 }
 

@@ -25,11 +25,13 @@ struct GmresState {
   int* kb;          // [B] columns used
 };
 
-// n: used doubles per shell, ld: stride between shells (n <= ld)
+// n: used doubles per shell, ld: stride between shells (n <= ld); active (device, nullable): shells whose
+// flag is 0 are skipped (dots: zero results; combinations: w left as it was)
 cudaError_t krylov_dots(const double* V, size_t vstride_i, const double* w, int n, int ld, int nv, int B,
-                        double* part, double* h, int ldh, int accumulate, cudaStream_t st);
+                        double* part, double* h, int ldh, int accumulate, cudaStream_t st,
+                        const int* active = nullptr);
 cudaError_t krylov_sub_combination(const double* V, size_t vstride_i, double* w, const double* coef, int ldc,
-                                   int n, int ld, int nv, int B, cudaStream_t st);
+                                   int n, int ld, int nv, int B, cudaStream_t st, const int* active = nullptr);
 cudaError_t krylov_add_combination(const double* V, size_t vstride_i, double* x, const double* y, int ldy,
                                    const int* kb, int n, int ld, int B, cudaStream_t st);
 cudaError_t krylov_scale(const double* a, const double* scale, double* out, int n, int ld, int B, cudaStream_t st);
