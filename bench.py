@@ -411,6 +411,7 @@ def bench_gb300(args):
     # ---- per-kernel durations: a CUDA event after every kernel launch of each step (launched one by one) --
     nprof = min(200, args.steps * chunk)
     kp = plan.kernel_profile(X_after, Ra, Ras, nprof)
+    n_kp = sum(v[1] for v in kp.values())
     ms3, _ = plan.step_profile(X_after, Ra, Ras, nprof)
     ms3 = [m / nprof for m in ms3]
     kavg = {k: v[0] / v[1] for k, v in kp.items()}                 # ms per launch
@@ -561,7 +562,9 @@ def bench_gb300(args):
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                         "d2h_bytes_per_step": nbytes,
                         "api": "Plan.step on a pinned host state copied in/out every bench step"},
-                "gpu_launches": args.steps * chunk * sum(v[1] for v in kp.values()) // nprof,
+                # per bench step: the kernels of `chunk` steps, plus the one deferred chain correction that a
+                # multi-step call applies at its end (the profile's launches over nprof steps include it once)
+                "gpu_launches": args.steps * (chunk * (n_kp // nprof) + n_kp % nprof),
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": ck, "newton": newton, "mixed": mixed,
                 "batched": batched,
                 "served": served}

@@ -721,12 +721,30 @@ static int check_plan(sdd_plan* p, int batch) {
 // their linear parts (FP64 in both precisions) and the chains' h kernel adds the nonlinear parts (same
 // roundings).
 // ev (nullable): four events recorded around the nonlinear term, the rhs and the chains.
+// The pending layout-3 correction of a state X (and its FP32 copy x32, nullable), for FixArgs.
+static FixArgs fix_args(const sdd_plan* p, const double* X, const float* x32) {
+  FixArgs f;
+  std::memset(&f, 0, sizeof(f));
+  const ChunkSet& c = p->cs[1];
+  f.on = 1;
+  f.kc = c.kc; f.nch = c.nch; f.np = c.np; f.ldd = p->ldd; f.ldl = p->ldl;
+  f.GA4 = c.GA4; f.GT = c.GT; f.GS = c.GS;
+  f.dbuf = p->dbuf; f.pbuf = p->pbuf;
+  f.d_stride = (size_t)6 * p->nch_alloc * p->ldd;
+  f.p_stride = (size_t)6 * p->np_alloc * p->ldd;
+  f.X = const_cast<double*>(X);
+  f.X32 = const_cast<float*>(x32);
+  return f;
+}
+
 // x32_in / x32_out (mixed time steps only): the FP32 copy of X the nonlinear term reads instead of
-// converting X, and the one the chains write beside out for the next step (nullable).
+// converting X, and the one the chains write beside out for the next step (nullable).  defer: leave a
+// layout-3 chain correction pending (sdd_step); fix_in: X carries the previous step's pending correction,
+// applied by the nonlinear term's first kernel.
 static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X, size_t ldx,
                          double* out, size_t ldo, const double* sub, size_t lds, int mode, void* base, int prec,
                          cudaStream_t s, cudaEvent_t* ev = nullptr, const float* x32_in = nullptr,
-                         float* x32_out = nullptr, const int* active = nullptr) {
+                         float* x32_out = nullptr, const int* active = nullptr, int defer = 0, int fix_in = 0) {
   RhsArgs ra = rhs_args(p, X, p->out4, Ra, Ras, p->rhs, mode == 2);
   ra.x_stride = ldx;
   ra.active = active;
@@ -747,6 +765,10 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
     if (prec == SDD_PREC_MIXED) fa.q32 = p->q32;
     const int fm = mode == 1 ? 1 : 0;
     fuse = fx_uses_split(fa, batch, fm);
+    if (fix_in) {
+      if (!fuse || mode != 0) return SDD_ERR_ARG;   // only the split path's derivative kernel applies it
+      fa.fix = fix_args(p, X, x32_in);
+    }
     if (fuse) {
       fa.fuse_rhs = 1;
       fa.rl = ra;
@@ -760,6 +782,7 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
   ca.f_stride = ldo;
   ca.sub_stride = lds;
   ca.active = active;
+  ca.defer_fix = defer && mode == 0 && !sub;
   if (prec == SDD_PREC_MIXED && mode == 0 && !sub) {
     ca.f32 = x32_out;
     ca.f32_stride = shell_elems(p);
@@ -781,9 +804,28 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
 
 static int apply_step(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X,
                       double* out, const double* sub, int mode, void* base, int prec, cudaStream_t s,
-                      const float* x32_in = nullptr, float* x32_out = nullptr) {
+                      const float* x32_in = nullptr, float* x32_out = nullptr, int defer = 0, int fix_in = 0) {
   const size_t n = shell_elems(p);
-  return apply_step_ld(p, batch, Ra, Ras, X, n, out, n, sub, n, mode, base, prec, s, nullptr, x32_in, x32_out);
+  return apply_step_ld(p, batch, Ra, Ras, X, n, out, n, sub, n, mode, base, prec, s, nullptr, x32_in, x32_out,
+                       nullptr, defer, fix_in);
+}
+
+// Whether sdd_step's steps leave the chains' correction to the next step's nonlinear term: layout 3 with
+// the split nonlinear term, non-linear steps.
+static bool step_defers_fix(sdd_plan* p, int batch, int linear) {
+  if (linear || p->cs[1].nch < 2) return false;
+  if (resolve_chain_layout(chain_args(p, nullptr, nullptr, nullptr), batch, 3) != 3) return false;
+  const FxArgs fa = fx_args(p, p->prec, nullptr, nullptr, p->out4);
+  return fx_uses_split(fa, batch, 0);
+}
+
+// The correction left pending by the last step of a sequence, on the state X (and its FP32 copy).
+static int finish_fix(sdd_plan* p, int batch, double* X, float* x32, cudaStream_t s) {
+  ChainArgs ca = chain_args(p, nullptr, X, nullptr);
+  ca.f32 = x32;
+  ca.f32_stride = shell_elems(p);
+  SDD_CUDA(launch_chunk_fix(ca, batch, 3, s));
+  return SDD_OK;
 }
 
 extern "C" {
@@ -878,13 +920,17 @@ static cudaGraphExec_t step_graph(sdd_plan* p, int batch, const double* Ra, cons
     return nullptr;
   }
   int st = SDD_OK;
-  // mixed: A's FP32 copy is current (the graph runs after a step into A); each step writes the other's
+  // mixed: A's FP32 copy is current (the graph runs after a step into A); each step writes the other's.
+  // With deferred corrections every step applies its input's pending one and leaves its own.
   float* a32 = linear ? nullptr : p->x32[0];
   float* t32 = linear ? nullptr : p->x32[1];
+  const int dfix = step_defers_fix(p, batch, linear) ? 1 : 0;
   for (int i = 0; i < pairs && st == SDD_OK; ++i) {
-    st = apply_step(p, batch, Ra, Ras, A, p->xtmp, nullptr, linear ? 2 : 0, nullptr, p->prec, cs, a32, t32);
+    st = apply_step(p, batch, Ra, Ras, A, p->xtmp, nullptr, linear ? 2 : 0, nullptr, p->prec, cs, a32, t32, dfix,
+                    dfix);
     if (st == SDD_OK)
-      st = apply_step(p, batch, Ra, Ras, p->xtmp, A, nullptr, linear ? 2 : 0, nullptr, p->prec, cs, t32, a32);
+      st = apply_step(p, batch, Ra, Ras, p->xtmp, A, nullptr, linear ? 2 : 0, nullptr, p->prec, cs, t32, a32, dfix,
+                      dfix);
   }
   cudaGraph_t graph = nullptr;
   const cudaError_t ec = cudaStreamEndCapture(cs, &graph);
@@ -913,6 +959,9 @@ int sdd_step(sdd_plan* p, int batch, const double* Ra, const double* Ras, const 
   // for the next step's nonlinear term (the caller's X_in has none)
   const double* cur = X_in;
   const float* cur32 = nullptr;
+  // layout 3 with the split nonlinear term: each step's chain correction is applied by the next step's
+  // first kernel (one launch fewer per step); the last one runs on its own at the end
+  const int dfix = step_defers_fix(p, batch, linear) ? 1 : 0;
   cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
   SDD_CUDA(cudaStreamIsCapturing(s, &cst));
   const bool graphs = cst == cudaStreamCaptureStatusNone && nsteps >= kGraphMinSteps && X_out != p->xtmp;
@@ -927,17 +976,19 @@ int sdd_step(sdd_plan* p, int batch, const double* Ra, const double* Ras, const 
         int done = 0;
         for (; g8 && done + 8 <= npairs; done += 8) SDD_CUDA(cudaGraphLaunch(g8, s));
         for (; done < npairs; ++done) SDD_CUDA(cudaGraphLaunch(g1, s));
-        return SDD_OK;
+        return dfix ? finish_fix(p, batch, X_out, linear ? nullptr : p->x32[0], s) : SDD_OK;
       }
     }
     double* dst = (left % 2 == 1) ? X_out : p->xtmp;
     if (dst == cur) dst = (dst == X_out) ? p->xtmp : X_out;  // never write the input in place
     float* dst32 = linear ? nullptr : p->x32[dst == p->xtmp ? 1 : 0];
-    st = apply_step(p, batch, Ra, Ras, cur, dst, nullptr, linear ? 2 : 0, nullptr, p->prec, s, cur32, dst32);
+    st = apply_step(p, batch, Ra, Ras, cur, dst, nullptr, linear ? 2 : 0, nullptr, p->prec, s, cur32, dst32, dfix,
+                    dfix && it > 0);
     if (st) return st;
     cur = dst;
     cur32 = dst32;
   }
+  if (dfix && (st = finish_fix(p, batch, const_cast<double*>(cur), const_cast<float*>(cur32), s))) return st;
   if (cur != X_out) SDD_CUDA(cudaMemcpyAsync(X_out, cur, bytes, cudaMemcpyDeviceToDevice, s));
   return SDD_OK;
 }
@@ -1449,6 +1500,7 @@ extern "C" int sdd_step_kernel_profile(sdd_plan* p, int B, const double* Ra, con
   const double* cur = X_in;
   int rc = e == cudaSuccess ? SDD_OK : SDD_ERR_CUDA;
   if (rc) set_cuda_error(e);
+  const int dfix = step_defers_fix(p, B, 0) ? 1 : 0;   // the sequencing of sdd_step
   for (int it = 0; it < nsteps && rc == SDD_OK; ++it) {
     double* dst = ((nsteps - it) % 2 == 1) ? X_out : p->xtmp;
     t.n = 0;
@@ -1459,7 +1511,9 @@ extern "C" int sdd_step_kernel_profile(sdd_plan* p, int B, const double* Ra, con
     }
     g_ktimer = &t;
     const size_t n = shell_elems(p);
-    rc = apply_step_ld(p, B, Ra, Ras, cur, n, dst, n, nullptr, n, 0, nullptr, p->prec, s);
+    rc = apply_step_ld(p, B, Ra, Ras, cur, n, dst, n, nullptr, n, 0, nullptr, p->prec, s, nullptr, nullptr, nullptr,
+                       nullptr, dfix, dfix && it > 0);
+    if (rc == SDD_OK && dfix && it + 1 == nsteps) rc = finish_fix(p, B, dst, nullptr, s);
     g_ktimer = nullptr;
     if (rc != SDD_OK) break;
     if (t.n > 0 && (e = cudaEventSynchronize(t.ev[t.n - 1])) != cudaSuccess) {

@@ -678,6 +678,7 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
         return e;
       ktimer_mark(SDD_K_CHAIN_CARRY, s);
     }
+    if (a.defer_fix) return cudaSuccess;   // the next step's nonlinear term applies the correction
     return launch_mode_mv<true>(a, batch, nfields, s, pw);
   }
   // the carry ring of the psi chain (m = 2 nr) decides the ring depth for all fields of the launch
@@ -717,6 +718,19 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
 // carried-state recurrence and a parallel correction) is chosen automatically while all its CTAs fit
 // on the GPU at two per SM.  a.g holds the right-hand sides; a.h receives h = Linv g (k_mode_mv), which
 // is what the chains read.
+// The layout-3 correction f += G_jj s_c on its own (a correction left pending by the last step of a
+// sequence; a.f is the state, a.f32 its FP32 copy or null).
+cudaError_t launch_chunk_fix(const ChainArgs& a_in, int batch, int nfields, cudaStream_t s) {
+  ChainArgs a = a_in;
+  const ChunkSet& c = a.cset[1];
+  a.kc = c.kc; a.nch = c.nch; a.np = c.np;
+  a.GA4 = c.GA4; a.GT = c.GT; a.GS = c.GS;
+  a.PA4 = c.PA4; a.PT = c.PT; a.PS = c.PS;
+  a.carry_seq = 0;
+  if (a.nch < 2) return cudaSuccess;
+  return launch_mode_mv<true>(a, batch, nfields, s, mv_per_warp(a, batch, nfields));
+}
+
 int resolve_chain_layout(const ChainArgs& a, int batch, int nfields) {
   const int sms = sm_count();
   static const int optin = [] {

@@ -343,14 +343,81 @@ size_t fx_prod_smem_bytes(int P, int prec) {
 // columns in the order of the fused kernel's (so both paths round identically).  With the fused
 // right-hand side a fifth block, D2s psi_k in FP64, follows the four T-typed blocks (per shell:
 // 4 M nr T then M nr doubles).
+// sum over the TPR lanes of a row group (the order of the chains' group_sum)
+template <int TPR>
+__device__ __forceinline__ double lane_group_sum(double v) {
+#pragma unroll
+  for (int off = 1; off < TPR; off <<= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// The pending correction of mode k (see FixArgs) on xd (the mode's FP64 psi, T, S rows, in shared memory),
+// the three fields at once, each by its own 128 threads (threads 128 f .. 128 f + 127; the CTA has 384):
+// s_c = d_{c-1} + part_{c,0} + ... in index order, then xd += G_jj s_c with rows split over TPR lanes as
+// k_mode_mv<TPR, true> (the same bits); the corrected rows are written back to the state (and its FP32
+// copy).  sc holds the three carried states (4 nr doubles).
+template <int TPR>
+__device__ void apply_pending_fix(const FxArgs& a, int b, int k, double* xd, double* sc) {
+  const FixArgs& x = a.fix;
+  const int M = a.M, nr = a.nr, ldl = x.ldl;
+  const int jj = M - 1 - k, par = jj & 1, c = (jj >> 1) / x.kc;
+  if (c < 1) return;                                   // uniform over the CTA
+  const size_t N = (size_t)M * nr;
+  const int f = threadIdx.x >> 7, t = threadIdx.x & 127;
+  const bool a4 = f == 0;
+  const bool on = f < 3 && !(a.sym && !(a4 ? par == 0 : par == 1));
+  const int m = a4 ? 2 * nr : nr;
+  double* s = sc + (a4 ? 0 : (f == 1 ? 2 * nr : 3 * nr));
+  if (on) {
+    const size_t chain = (size_t)(f * 2 + par);
+    const double* d = x.dbuf + (size_t)b * x.d_stride + chain * x.nch * x.ldd;
+    const double* prow = x.pbuf + (size_t)b * x.p_stride + (chain * x.np + (size_t)(c - 1) * (c - 2) / 2) * x.ldd;
+    for (int e = t; e < m; e += 128) {
+      double v = d[(size_t)(c - 1) * x.ldd + e];
+      for (int u = 0; u <= c - 2; ++u) v += prow[(size_t)u * x.ldd + e];
+      s[e] = v;
+    }
+  }
+  __syncthreads();
+  if (on) {
+    const double* G = (a4 ? x.GA4 : (f == 1 ? x.GT : x.GS)) + (size_t)jj * m * ldl;
+    const int i = t / TPR, q = t % TPR;
+    for (int r0 = 0; r0 < nr; r0 += 128 / TPR) {
+      const int r = r0 + i;
+      const int rr = r < nr ? r : 0;
+      double acc = 0.0;
+#pragma unroll 8
+      for (int col = q; col < m; col += TPR) acc = fma(__ldg(G + (size_t)col * ldl + rr), s[col], acc);
+      acc = lane_group_sum<TPR>(acc);
+      if (r < nr && q == 0) {
+        const double v = xd[f * nr + r] + acc;
+        xd[f * nr + r] = v;
+        const size_t o = (size_t)b * a.x_stride + (size_t)f * N + (size_t)k * nr + r;
+        x.X[o] = v;
+        if (x.X32) x.X32[(size_t)b * a.x32_stride + (size_t)f * N + (size_t)k * nr + r] = (float)v;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+size_t fx_deriv_smem_bytes(int nr, int prec, bool fix) {
+  const size_t es = prec == SDD_PREC_MIXED ? sizeof(float) : sizeof(double);
+  const size_t t = ((2 * (size_t)nr * nr + 3 * (size_t)nr) * es + 15) / 16 * 16;
+  return fix ? t + 7 * (size_t)nr * sizeof(double) : t;
+}
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_fx_deriv(FxArgs a, T* deriv, size_t deriv_stride) {
+__global__ void __launch_bounds__(384) k_fx_deriv(FxArgs a, T* deriv, size_t deriv_stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int M = a.M, nr = a.nr;
   const int k = blockIdx.x, b = blockIdx.y;
   if (a.active && !a.active[b]) return;
   T* ops = reinterpret_cast<T*>(smem_raw);     // Dr, D2r2 (nr x nr each, row-major)
   T* xv = ops + 2 * nr * nr;                  // psi_k, T_k, S_k
+  // with a pending correction: the mode's FP64 rows (corrected here) and a carried state
+  double* xd = reinterpret_cast<double*>(smem_raw + ((2 * (size_t)nr * nr + 3 * (size_t)nr) * sizeof(T) + 15) / 16 * 16);
+  double* sc = xd + 3 * nr;
   const T* Drg = reinterpret_cast<const T*>(a.ops.Dr);
   const T* D2g = reinterpret_cast<const T*>(a.ops.D2r2);
   for (int e = threadIdx.x; e < nr * nr; e += blockDim.x) {
@@ -358,12 +425,23 @@ __global__ void __launch_bounds__(256) k_fx_deriv(FxArgs a, T* deriv, size_t der
     ops[nr * nr + e] = D2g[e];
   }
   const int N = M * nr;
-  with_x<T>(a, b, [&](auto xr) {
+  if (a.fix.on) {
     for (int e = threadIdx.x; e < 3 * nr; e += blockDim.x) {
       const int f = e / nr, m = e - f * nr;
-      xv[e] = xr((size_t)f * N + (size_t)k * nr + m);
+      xd[e] = a.fix.X[(size_t)b * a.x_stride + (size_t)f * N + (size_t)k * nr + m];
     }
-  });
+    __syncthreads();
+    if (nr <= 32) apply_pending_fix<4>(a, b, k, xd, sc);
+    else apply_pending_fix<2>(a, b, k, xd, sc);
+    for (int e = threadIdx.x; e < 3 * nr; e += blockDim.x) xv[e] = (T)xd[e];
+  } else {
+    with_x<T>(a, b, [&](auto xr) {
+      for (int e = threadIdx.x; e < 3 * nr; e += blockDim.x) {
+        const int f = e / nr, m = e - f * nr;
+        xv[e] = xr((size_t)f * N + (size_t)k * nr + m);
+      }
+    });
+  }
   __syncthreads();
   T* D = deriv + (size_t)b * deriv_stride;
   const int nops = a.fuse_rhs ? 5 : 4;
@@ -376,10 +454,14 @@ __global__ void __launch_bounds__(256) k_fx_deriv(FxArgs a, T* deriv, size_t der
       for (int m = 0; m < nr; ++m) acc = fma(row[m], x[m], acc);
       D[((size_t)op * M + k) * nr + n] = acc;
     } else {   // A2_SINE's D2 psi for the fused right-hand side (FP64; the order of k_rhs's dot)
-      const double* ps = a.X + (size_t)b * a.x_stride + (size_t)k * nr;
       const double* row = a.rl.D2s + (size_t)n * nr;
       double acc = 0;
-      for (int m = 0; m < nr; ++m) acc = fma(__ldg(row + m), __ldg(ps + m), acc);
+      if (a.fix.on) {          // the corrected rows (this kernel wrote them: not through the read-only path)
+        for (int m = 0; m < nr; ++m) acc = fma(__ldg(row + m), xd[m], acc);
+      } else {
+        const double* ps = a.X + (size_t)b * a.x_stride + (size_t)k * nr;
+        for (int m = 0; m < nr; ++m) acc = fma(__ldg(row + m), __ldg(ps + m), acc);
+      }
       reinterpret_cast<double*>(D)[(size_t)4 * M * nr * sizeof(T) / 8 + (size_t)k * nr + n] = acc;
     }
   }
@@ -933,7 +1015,8 @@ static cudaError_t launch_fx_split_t(const FxArgs& a, int batch, cudaStream_t s)
   T* grid = reinterpret_cast<T*>((MODE != 1 && a.base) ? a.base : a.grid);
   const size_t gs = (MODE != 1 && a.base) ? a.base_stride : a.grid_stride;
   cudaError_t e;
-  e = launch_kernel(k_fx_deriv<T>, dim3(a.M, batch), dim3(256), (2 * a.nr * a.nr + 3 * a.nr) * sizeof(T), s, a,
+  e = launch_kernel(k_fx_deriv<T>, dim3(a.M, batch), dim3(a.fix.on ? 384 : 256),
+                    fx_deriv_smem_bytes(a.nr, prec, a.fix.on != 0), s, a,
                  reinterpret_cast<T*>(a.deriv), a.deriv_stride);
   ktimer_mark(SDD_K_FX_DERIV, s);
   if (e != cudaSuccess) return e;

@@ -160,6 +160,21 @@ struct RhsArgs {
   const int* active;         // nullable: per-shell flags; kernels skip shells whose flag is 0
 };
 
+// A chunk correction of the state left pending by the previous time step (layout 3, sdd_step): the split
+// nonlinear term's k_fx_deriv applies X[jj] += G_jj s_c(jj) to its mode before using it, with the
+// arithmetic of k_mode_mv<TPR, true> (the same bits), and writes the corrected rows back (and their FP32
+// copy).  The previous step's chunk end states and carry products are still in dbuf / pbuf: this step's
+// chains overwrite them only after the nonlinear term.
+struct FixArgs {
+  int on;
+  int kc, nch, np, ldd, ldl;
+  const double* GA4, *GT, *GS;
+  const double* dbuf, *pbuf;
+  size_t d_stride, p_stride;
+  double* X;                 // the state being corrected in place (the nonlinear term's input)
+  float* X32;                // nullable: its FP32 copy
+};
+
 struct FxArgs {
   int M, nr, P, sym;
   StageArgs st;
@@ -188,6 +203,7 @@ struct FxArgs {
   // nonlinear parts from out4.  rl carries the operators, parameters and the rhs buffer.
   int fuse_rhs;
   RhsArgs rl;
+  FixArgs fix;               // split path: a pending correction of X (see FixArgs)
 };
 
 
@@ -254,6 +270,7 @@ struct ChainArgs {
   double* pbuf;              // [shell][6][np][ldd] products P_{j,i} d_i
   size_t p_stride;           // doubles per shell in pbuf
   ChunkSet cset[2];          // the chunkings of layouts 2 and 3 (launch_chain copies one into the fields above)
+  int defer_fix;             // layout 3: leave the correction to the next step's nonlinear term (FixArgs)
   const int* active;         // nullable: per-shell flags; kernels skip shells whose flag is 0
 };
 
@@ -284,6 +301,7 @@ cudaError_t launch_rhs(const RhsArgs& a, int batch, cudaStream_t s);
 cudaError_t launch_chain(const ChainArgs& a, int batch, int nfields, cudaStream_t s);
 // the chain layout (1, 2, 3 or 4) launch_chain runs for a.layout (0 = automatic) and this launch size
 int resolve_chain_layout(const ChainArgs& a, int batch, int nfields);
+cudaError_t launch_chunk_fix(const ChainArgs& a, int batch, int nfields, cudaStream_t s);
 cudaError_t launch_theta_op(int op, int M, int nr, int sym, const double* D2, const double* ir,
                             const double* dT0, const double* g, double* f, int batch,
                             cudaStream_t s);
