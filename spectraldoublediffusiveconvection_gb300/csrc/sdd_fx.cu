@@ -1015,6 +1015,10 @@ static cudaError_t launch_fx_split_t(const FxArgs& a, int batch, cudaStream_t s)
   T* grid = reinterpret_cast<T*>((MODE != 1 && a.base) ? a.base : a.grid);
   const size_t gs = (MODE != 1 && a.base) ? a.base_stride : a.grid_stride;
   cudaError_t e;
+  {
+    static unsigned long long done = 0;   // large nr with a pending correction can pass 48 KB
+    if ((e = ensure_smem_attr(k_fx_deriv<T>, &done)) != cudaSuccess) return e;
+  }
   e = launch_kernel(k_fx_deriv<T>, dim3(a.M, batch), dim3(a.fix.on ? 384 : 256),
                     fx_deriv_smem_bytes(a.nr, prec, a.fix.on != 0), s, a,
                  reinterpret_cast<T*>(a.deriv), a.deriv_stride);
