@@ -60,7 +60,8 @@ def kernel_algorithmic(name, M, nr, nch, layout=3):
       k_chain_carry   layout 3: the np products per chain at once, flops 24 np nr^2, bytes 96 np nr^2
       k_mode_mv(h)    h = Linv g: flops 6 M nr^2, bytes 24 M nr^2 + 48 M nr
       k_mode_mv(fix)  f += G s: flops 8 M nr^2 (nch-1)/nch, bytes 32 M nr^2 (nch-1)/nch + 48 M nr
-      k_fx_deriv      4 radial contractions: flops 8 M nr^2, bytes 56 M nr
+      k_fx_deriv      4 radial contractions: flops 8 M nr^2, bytes 56 M nr; under layout 3 (time steps) plus
+                      the previous step's chain correction, the k_mode_mv(fix) terms below
       k_fx_grid       9 inverse transforms (2.5 P log2 P each): flops 22.5 nr P log2 P, bytes 56 M nr + 72 nr P
       k_fx_prod       products + 3 forward transforms: flops 7.5 nr P log2 P + 11 nr P, bytes 72 nr P + 32 M nr
       k_fx_rows       fused nonlinear term: flops 8 M nr^2 + 30 nr P log2 P + 11 nr P, bytes 56 M nr
@@ -76,7 +77,8 @@ def kernel_algorithmic(name, M, nr, nch, layout=3):
         "k_chain_carry": (24 * npr * nr ** 2, 96 * npr * nr ** 2),
         "k_mode_mv(h)": (6 * M * nr ** 2, 24 * M * nr ** 2 + 48 * M * nr),
         "k_mode_mv(fix)": (8 * M * nr ** 2 * f, 32 * M * nr ** 2 * f + 48 * M * nr),
-        "k_fx_deriv": (8 * M * nr ** 2, 56 * M * nr),
+        "k_fx_deriv": (8 * M * nr ** 2 + (8 * M * nr ** 2 * f if layout == 3 else 0),
+                       56 * M * nr + ((32 * M * nr ** 2 * f + 48 * M * nr) if layout == 3 else 0)),
         "k_fx_grid": (22.5 * nr * P * lg, 56 * M * nr + 72 * nr * P),
         "k_fx_prod": (7.5 * nr * P * lg + 11 * nr * P, 72 * nr * P + 32 * M * nr),
         "k_fx_rows": (8 * M * nr ** 2 + 30 * nr * P * lg + 11 * nr * P, 56 * M * nr),
