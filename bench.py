@@ -146,8 +146,9 @@ class ClockSampler:
 # ------------------------------------------------------------------------------------------------
 # CPU baseline (the oracle), run in a child process so its BLAS/OpenMP threads are pinned at start-up
 # ------------------------------------------------------------------------------------------------
-def cpu_worker(seconds, threads, steps_per_sample):
-    """Times IMEX steps of the workload with the oracle; prints one JSON line."""
+def cpu_worker(seconds, threads, steps_per_sample, count=0):
+    """Times IMEX steps of the workload with the oracle, in samples of steps_per_sample steps: `count`
+    samples when count > 0, else samples until `seconds` have passed; prints one JSON line."""
     import numpy as np
     from oracle import sdd_oracle as O
     w = WORKLOAD
@@ -164,20 +165,20 @@ def cpu_worker(seconds, threads, steps_per_sample):
             X = O.step(ops, X, w["Ra_T"], w["Ra_S"], False)
         samples.append(time.perf_counter() - t0)
         n += steps_per_sample
-        if time.perf_counter() - t_start >= seconds:
+        if (count > 0 and len(samples) >= count) or (count <= 0 and time.perf_counter() - t_start >= seconds):
             break
     total = sum(samples)
     print(json.dumps({"steps": n, "seconds": total, "samples": samples, "threads": threads,
                       "finite": bool(np.isfinite(X).all())}))
 
 
-def run_cpu_baseline(seconds=12.0, threads=1, steps_per_sample=5):
+def run_cpu_baseline(seconds=12.0, threads=1, steps_per_sample=5, count=0):
     env = dict(os.environ)
     for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS", "NUMEXPR_NUM_THREADS"):
         env[v] = str(threads)
     env["CUDA_VISIBLE_DEVICES"] = ""
     cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--cpu-worker", str(seconds), str(threads),
-           str(steps_per_sample)]
+           str(steps_per_sample), str(count)]
     out = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=600)
     if out.returncode != 0:
         raise RuntimeError("cpu baseline failed: " + out.stderr[-2000:])
@@ -218,17 +219,17 @@ def bench_reference(args):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    # a bounded sample per bench step: 5 IMEX steps with all host threads available to BLAS
+    # one bench step = a bounded sample of the workload: 5 IMEX steps with all host threads available to
+    # BLAS; exactly W untimed then K timed samples
     per = 5
-    seconds = max(5.0, min(120.0, 0.02 * per * (args.steps + args.warmup)))
-    r = run_cpu_baseline(seconds=seconds, threads=threads, steps_per_sample=per)
+    r = run_cpu_baseline(threads=threads, steps_per_sample=per, count=args.warmup + args.steps)
     samples = r["samples"]
-    timed = samples[min(len(samples) - 1, args.warmup):] if len(samples) > args.warmup else samples
+    timed = samples[args.warmup:]
     tsec = sum(timed)
     nsteps = per * len(timed)
     value = nsteps / tsec
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": len(timed), "warmup": min(args.warmup, len(samples) - len(timed)),
+            "steps": len(timed), "warmup": args.warmup,
             "ms_per_step": 1e3 * tsec / len(timed), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian coefficients)",
             "config": dict(WORKLOAD, steps_per_bench_step=per, l2="n/a (host)"),
@@ -579,7 +580,8 @@ def bench_gb300(args):
 
 def main():
     if len(sys.argv) > 1 and sys.argv[1] == "--cpu-worker":
-        cpu_worker(float(sys.argv[2]), int(sys.argv[3]), int(sys.argv[4]))
+        cpu_worker(float(sys.argv[2]), int(sys.argv[3]), int(sys.argv[4]),
+                   int(sys.argv[5]) if len(sys.argv) > 5 else 0)
         return 0
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
