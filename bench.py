@@ -250,8 +250,12 @@ def bench_batched(device, precision, steps=1000, steps_per_launch=10, n_shells=6
     import torch
     from spectraldoublediffusiveconvection_gb300.batch import ShellBatch, config4_shells
     shells = config4_shells(n_shells, seed=1234)
-    b = ShellBatch(shells, d=2.0, dt=1e-3, Pr=1.0, Tau=0.01, Ra_s=500.0, precision=precision, device=device)
-    tuning = b.autotune(steps_per_launch=steps_per_launch, reps=2)
+    kw = dict(d=2.0, dt=1e-3, Pr=1.0, Tau=0.01, Ra_s=500.0, precision=precision, device=device)
+    # tune on a scratch batch, run a fresh one with its choices (see ShellBatch.apply_tuning)
+    tuning = ShellBatch(shells, **kw).autotune(steps_per_launch=steps_per_launch, reps=2)
+    torch.cuda.synchronize(device)
+    b = ShellBatch(shells, tuning=tuning, **kw)
+    b.capture(steps_per_launch)
     launches = max(1, steps // steps_per_launch)
     b.replay(1)
     torch.cuda.synchronize(device)

@@ -44,7 +44,7 @@ class ShellBatch:
     flat numpy array in the reference layout; seeded if absent) and symmetric."""
 
     def __init__(self, shells, d=2.0, dt=1e-3, Pr=1.0, Tau=0.01, Ra_s=500.0, precision="mixed",
-                 device=None, seed=1234, max_group=None, priorities=False):
+                 device=None, seed=1234, max_group=None, priorities=False, tuning=None):
         torch = _torch()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.d, self.dt, self.Pr, self.Tau, self.precision = d, dt, Pr, Tau, precision
@@ -92,6 +92,20 @@ class ShellBatch:
         self.graph = None
         self.steps_per_launch = 0
         self.tuning = {}
+        if tuning:
+            self.apply_tuning(tuning)
+
+    def apply_tuning(self, tuning):
+        """Per-shape kernel choices of an earlier autotune() (its returned dict), e.g. of a scratch batch
+        of the same shapes: a batch object that went through tuning itself was measured to run some 8%
+        slower afterwards with the same choices (cause not found), a fresh one with them does not."""
+        for g in self.groups:
+            c = tuning.get("N_r=%d,N_theta=%d" % g.shape)
+            if c:
+                g.plan.set_chain_layout(int(c["chain_layout"]))
+                g.plan.set_fx_split(int(c["fx_split"]))
+                self.tuning["N_r=%d,N_theta=%d" % g.shape] = dict(c)
+        self.graph = None
 
     # ---- eager ---------------------------------------------------------------------------------
     def step(self, nsteps=1):

@@ -153,8 +153,7 @@ __global__ void k_chain(ChainArgs a) {
   const int ncol = a4 ? 2 * nr : nr;           // columns of the step matrix ([A B] or Linv)
   const int blk = ncol * ldl;
   double* Lb0 = csm;                           // 3-slot ring of step matrices
-  double* hs = csm + 3 * blk;                  // the chunk's h rows, step-ordered
-  double* cf = hs + (size_t)nsteps * nr;       // per-step scalars (4 per step, one step past the chunk)
+  double* cf = csm + 3 * blk;                  // per-step scalars (4 per step, one step past the chunk)
   double* x2 = cf + 4 * (size_t)(nsteps + 1);  // 2 buffers of the matvec operand: A4 [f_e; bf_e], NAB2 b
   const double* Mat = a4 ? a.ABA4 : (field == 1 ? a.LinvT : a.LinvS);
   const double* coef = a4 ? a.coefA4 : (field == 1 ? a.coefT : a.coefS);   // [M][4] indexed by jj
@@ -169,13 +168,11 @@ __global__ void k_chain(ChainArgs a) {
     cf[e] = jj < M ? coef[(size_t)jj * 4 + (e & 3)] : 0.0;
   }
   for (int c = tid; c < 4 * nr; c += blockDim.x) x2[c] = 0.0;
-  {
-    const double* h = a.g + (size_t)b * a.g_stride + foff;       // h_j = Linv_j g_j (k_mode_mv)
-    for (int e = tid; e < nsteps * nr; e += blockDim.x) {
-      const int s = e / nr, c = e - s * nr;
-      hs[e] = h[(size_t)(M - 1 - (par + 2 * (s0 + s))) * nr + c];
-    }
-  }
+  // h_j = Linv_j g_j (k_mode_mv) of row ir, two steps ahead in registers (off the chain's critical path;
+  // no shared-memory copy of the chain's h rows, so long chains leave room for other CTAs on the SM)
+  const double* hrow = a.g + (size_t)b * a.g_stride + foff + ir;
+  auto h_at = [&](int s) { return s < nsteps ? hrow[(size_t)(M - 1 - (par + 2 * (s0 + s))) * nr] : 0.0; };
+  double hn0 = h_at(0), hn1 = h_at(1);
 
   // The lead lane of row i keeps the row's carried state in registers and publishes it to the other
   // buffer of x2 for the next step's matvec: one barrier per step.
@@ -192,7 +189,9 @@ __global__ void k_chain(ChainArgs a) {
     chain_sync();                              // block s landed; this step's x2 visible; step s-1 done
     if (s + 2 < nsteps) copy_block(Lb0 + ((s + 2) % 3) * blk, Mat + (size_t)(jj + 4) * blk, blk);
     cp_async_commit();
-    const double hi = hs[s * nr + ir];
+    const double hi = hn0;
+    hn0 = hn1;
+    hn1 = h_at(s + 2);
     double fi;
     if (a4) {
       const double pre = fma(cf[4 * s + 3], fe, bfe);   // bf_e + bjt f_e, off the matvec's path
@@ -287,12 +286,12 @@ __global__ void k_chain(ChainArgs a) {
 size_t chain_smem_bytes(int M, int nr, int ldl) {
   const size_t blk = (size_t)2 * nr * ldl;
   const size_t ns = (size_t)((M + 1) / 2);
-  return (3 * blk + ns * nr + 4 * (ns + 1) + 4 * (size_t)nr) * sizeof(double);
+  return (3 * blk + 4 * (ns + 1) + 4 * (size_t)nr) * sizeof(double);
 }
 
 static size_t chunk_smem_bytes(int kc, int nr, int ldl) {
   const size_t blk = (size_t)2 * nr * ldl;
-  return (3 * blk + (size_t)kc * nr + 4 * ((size_t)kc + 1) + 4 * (size_t)nr) * sizeof(double);
+  return (3 * blk + 4 * ((size_t)kc + 1) + 4 * (size_t)nr) * sizeof(double);
 }
 
 // Carried states of the chunked chains: s_1 = d_0, s_{c+1} = Phi_c s_c + d_c (c = 1 .. nch-2) of one chain,

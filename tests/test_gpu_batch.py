@@ -61,6 +61,14 @@ def test_autotune_records_choices(cuda):
     assert all(v["chain_layout"] in (0, 1, 2, 3, 4, 5) for k, v in t.items() if k.startswith("N_r"))
     b.replay(1)
     assert all(np.isfinite(x).all() for x in b.states())
+    # a fresh batch built with the tuned choices runs the same kernels: the same states after a launch
+    b2 = ShellBatch(SHELLS, precision="mixed", tuning=t)
+    assert all(b2.tuning[k] == {"chain_layout": v["chain_layout"], "fx_split": v["fx_split"]}
+               for k, v in t.items() if k.startswith("N_r"))
+    b2.capture(2)
+    b2.replay(1)
+    for x, y in zip(b2.states(), b.states()):
+        assert np.array_equal(x, y)
 
 
 def test_autotune_does_not_advance_states(cuda):
