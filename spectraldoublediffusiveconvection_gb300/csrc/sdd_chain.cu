@@ -22,13 +22,16 @@
 //     over 4 warps, one per SMSP.  Lowest latency for one chain on an otherwise idle SM.
 //   TPR = 1, ceil(nr/32) warps: one lane per row, no reduction adds.  Fewest FP64 instructions per
 //     chain, used when a batch puts several chains on every SM.
-//   chunked (layout 2): the S = N_fm/2 steps of a chain are cut into nch chunks of kc steps that run
-//     concurrently, each from a zero carried state (its own CTA, h = Linv g computed in its prologue).
-//     The chain's carried state s (psi: [f_e; bf_e], 2 nr; T/S: b, nr) enters every later step linearly,
-//     so with the plan's precomputed Phi_c (state over a whole chunk) and G_jj (state -> f_jj):
-//       s_1 = d_0,  s_{c+1} = Phi_c s_c + d_c   (carry_run, by the chain's last-finishing chunk CTA)
+//   chunked (layouts 2 and 3): the S = N_fm/2 steps of a chain are cut into nch chunks of kc steps that
+//     run concurrently, each from a zero carried state (its own CTA; h = Linv g from k_mode_mv).  The
+//     chain's carried state s (psi: [f_e; bf_e], 2 nr; T/S: b, nr) enters every later step linearly, so
+//     with the plan's precomputed Phi_c (state over a whole chunk) and G_jj (state -> f_jj):
+//       layout 2: s_1 = d_0,  s_{c+1} = Phi_c s_c + d_c   (carry_run, by the chain's last-finishing chunk CTA)
+//       layout 3: s_c = d_{c-1} + sum_{i<=c-2} P_{c,i} d_i, P_{c,i} = Phi_{c-1}...Phi_{i+1} precomputed,
+//                 every product at once (k_carry_par), the row sums in the corrections
 //       f_jj += G_jj s_c(jj)                    (k_mode_mv, all modes in parallel)
-//     The critical path drops from S dependent steps to kc + (nch - 2) carried matvecs + one matvec.
+//     The critical path drops from S dependent steps to kc + (nch - 2) carried matvecs + one matvec
+//     (layout 2), or kc steps + one product + one matvec (layout 3, shorter chunks).
 // Matrices are stored transposed (column c contiguous, leading dimension ldl); the block of step s+2
 // streams global->shared with cp.async while step s runs (3-slot ring).  FP64 throughout.
 #include <cuda_runtime.h>
