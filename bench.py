@@ -275,6 +275,55 @@ def bench_batched(device, precision, steps=1000, steps_per_launch=10, n_shells=6
             "groups": [f"N_r={a} N_theta={c} x{n}" for a, c, n in groups], "tuning": tuning, "finite": finite}
 
 
+def _cpu_batch_worker(job):
+    """One host process of the batched CPU baseline: IMEX steps of its shells of the 64-shell workload with
+    the oracle, round robin, for `seconds`; returns (shell-steps, seconds)."""
+    idx, seconds = job
+    from oracle import sdd_oracle as O
+    from spectraldoublediffusiveconvection_gb300.batch import config4_shells
+    shells = config4_shells(64, seed=1234)
+    ops, X = {}, {}
+    for i in idx:
+        s = shells[i]
+        key = (s["N_theta"], s["N_r"])
+        if key not in ops:
+            ops[key] = O.Operators(s["N_theta"], s["N_r"], 2.0, 1e-3, 1.0, 0.01)
+        X[i] = O.seeded_state(s["N_theta"], s["N_r"] - 1, 1234 + i)
+    n = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        for i in idx:
+            s = shells[i]
+            X[i] = O.step(ops[(s["N_theta"], s["N_r"])], X[i], s["Ra"], 500.0, False)
+            n += 1
+    return n, time.perf_counter() - t0
+
+
+def bench_batched_cpu(seconds=10.0):
+    """The batched workload on the host: one oracle process per core (spawned, one BLAS thread each), the
+    64 shells dealt round robin; shell-steps of all processes over the slowest process's time."""
+    import multiprocessing as mp
+    n = os.cpu_count() or 1
+    env_keys = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS", "NUMEXPR_NUM_THREADS")
+    saved = {k: os.environ.get(k) for k in env_keys}
+    for k in env_keys:
+        os.environ[k] = "1"
+    try:
+        with mp.get_context("spawn").Pool(n) as pool:
+            res = pool.map(_cpu_batch_worker, [(list(range(w, 64, n)), seconds) for w in range(n)])
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    steps = sum(r[0] for r in res)
+    t = max(r[1] for r in res)
+    return {"value": steps / t, "unit": "shell-steps/s", "cores": n, "kind": "port",
+            "sample": f"{steps} IMEX steps of the 64 shells (FP64 numpy oracle restating the reference), "
+                      f"{n} processes of one thread, {seconds:.0f} s each (reference un-JIT'd: numba unavailable)"}
+
+
 # ------------------------------------------------------------------------------------------------
 # served workload: Poisson arrivals of continuation steps and 500-step integrations
 # ------------------------------------------------------------------------------------------------
@@ -545,6 +594,7 @@ def bench_gb300(args):
         batched = {"mixed": bm, "fp64": bd,
                    "mixed_vs_plain_single_shell": bm["shell_steps_per_s"] / plain,
                    "fp64_vs_plain_single_shell": bd["shell_steps_per_s"] / plain,
+                   "cpu_baseline": None if args.no_cpu else bench_batched_cpu(),
                    "workload": "64 shells, N_r in {20,24,30,36}, N_theta in {64,128,256,384}, Ra_T ~ U[6000,12000],"
                                " Ra_S=500, Pr=1, Tau=0.01, dt=1e-3, 1000 steps each (seed 1234)"}
 
