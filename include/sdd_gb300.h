@@ -102,7 +102,7 @@ int sdd_plan_reserve(sdd_plan* plan, int max_batch);
  * over 2 lanes in 2 warps (nr <= 32; 4 otherwise).  Set by the batch autotuner; no counterpart in the
  * reference. */
 int sdd_plan_set_chain_layout(sdd_plan* plan, int layout);
-/* The layout (1-4) a step of `batch` shells runs under the current setting, with its chunk length and
+/* The layout (1-5) a step of `batch` shells runs under the current setting, with its chunk length and
  * chunks per chain (0 and 1 when not chunked). */
 int sdd_plan_chain_choice(const sdd_plan* plan, int batch, int* layout, int* kc, int* nch);
 /* Nonlinear-term kernel choice: 0 automatic (split while the fused kernel's nr*batch CTAs would fill
@@ -155,7 +155,8 @@ typedef struct sdd_newton_opts {
   int32_t restart;         /* GMRES restart length (<= 64)                                          */
   int32_t max_restarts;    /* GMRES cycles per Newton iteration                                     */
   int32_t max_newton;      /* Newton iteration cap                                                  */
-  int32_t mixed_matvec;    /* 1: FP32 nonlinear term inside the Jacobian products (plan must be mixed) */
+  int32_t mixed_matvec;    /* 1: FP32 nonlinear term inside the Jacobian products (plan must be mixed);
+                              2: also FP32 right-hand sides and h = Linv g matvecs (chains stay FP64) */
 } sdd_newton_opts;
 
 typedef struct sdd_newton_result {

@@ -123,6 +123,9 @@ struct sdd_plan {
   double* pbuf;                     // [B][6][np_alloc][ldd] products of the parallel carry
   // FP32 copies used by the mixed-precision nonlinear term
   float *Dr32, *D2r232, *ir4r232;
+  // mixed plans: FP32 copies for the FP32 right-hand sides and h matvecs of Newton's Jacobian products
+  float* D2s32;
+  float* Linv32[3];                 // LinvA4, LinvT, LinvS in their transposed layout
   // workspace
   int ws_batch;
   double* out4;     // [B][4][M][nr]
@@ -131,6 +134,7 @@ struct sdd_plan {
   double* hbuf;     // [B][3][M][nr] h = Linv g of the chains
   float* x32[2];    // mixed plans: [B][3][M][nr] FP32 copies of sdd_step's output buffer and of xtmp
   float* q32;       // mixed plans: [B][M][nr] FP32 copy of the nonlinear term's Q block
+  float* g32;       // mixed plans: [B][3][M][nr] FP32 right-hand sides (k_rhs32)
   void* base_tmp;   // [B][nr][9][P] (T precision), for DFX without a caller cache
   void* gridbuf;    // [B][nr][9][P] (T precision), grid fields of the split nonlinear-term path
   void* derivbuf;   // [B] x (5 M nr doubles of room), radial derivatives of the split path: 4 M nr of the
@@ -143,6 +147,7 @@ struct sdd_plan {
   int* h_int;         // pinned host flags
   double *sv_F, *sv_x, *sv_X0, *sv_Xd, *sv_t, *sv_G, *sv_Jmu, *sv_g, *sv_base64, *sv_dev;
   float* sv_base32;
+  float* kv_v32;      // mixed plans: [B][ld] FP32 copy of the Krylov vector the next product is applied to
   // diagnostics (sdd_diagnostics): FFT plan of length 3M and weight tables; part = per-radius sums
   const FftPlan* dfft;
   double *dg_ir, *dg_tw, *dg_wr, *dg_nuw, *dg_part, *dg_out;
@@ -212,12 +217,24 @@ static int upload_linv(double** dst, const double* src, int M, int nr, int ldl) 
   SDD_CUDA(cudaMemcpy(*dst, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
   return SDD_OK;
 }
+// The same transposed layout rounded to FP32.
+static int upload_linv32(float** dst, const double* src, int M, int nr, int ldl) {
+  if (!src) return SDD_ERR_ARG;
+  std::vector<float> h((size_t)M * nr * ldl, 0.0f);
+  for (int m = 0; m < M; ++m)
+    for (int i = 0; i < nr; ++i)
+      for (int c = 0; c < nr; ++c) h[((size_t)m * nr + c) * ldl + i] = (float)src[((size_t)m * nr + i) * nr + c];
+  SDD_CUDA(cudaMalloc(dst, h.size() * sizeof(float)));
+  SDD_CUDA(cudaMemcpy(*dst, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return SDD_OK;
+}
 
 static void solver_free(sdd_plan* p) {
   double* d[] = {p->kv_V, p->kv_w, p->kv_r, p->kv_part, p->kv_nrm2, p->kv_small, p->kv_dot, p->sv_F, p->sv_x,
                  p->sv_X0, p->sv_Xd, p->sv_t, p->sv_G, p->sv_Jmu, p->sv_g, p->sv_base64, p->sv_dev};
   for (double* x : d) cudaFree(x);
   cudaFree(p->sv_base32);
+  cudaFree(p->kv_v32);
   cudaFree(p->kv_ismall);
   cudaFreeHost(p->h_dbl);
   cudaFreeHost(p->h_int);
@@ -225,6 +242,7 @@ static void solver_free(sdd_plan* p) {
   p->sv_F = p->sv_x = p->sv_X0 = p->sv_Xd = p->sv_t = p->sv_G = p->sv_Jmu = p->sv_g = p->sv_base64 = nullptr;
   p->sv_dev = nullptr;
   p->sv_base32 = nullptr;
+  p->kv_v32 = nullptr;
   p->kv_ismall = nullptr;
   p->h_dbl = nullptr;
   p->h_int = nullptr;
@@ -251,8 +269,9 @@ static void free_plan(sdd_plan* p) {
     const double* t[] = {c.GA4, c.GT, c.GS, c.PhiA4, c.PhiT, c.PhiS, c.PA4, c.PT, c.PS};
     for (const double* x : t) cudaFree(const_cast<double*>(x));
   }
-  cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232);
-  cudaFree(p->x32[0]); cudaFree(p->x32[1]); cudaFree(p->q32);
+  cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232); cudaFree(p->D2s32);
+  for (float* x : p->Linv32) cudaFree(x);
+  cudaFree(p->x32[0]); cudaFree(p->x32[1]); cudaFree(p->q32); cudaFree(p->g32);
   cudaFree(p->base_tmp);
   cudaFree(p->gridbuf);
   cudaFree(p->derivbuf);
@@ -507,6 +526,14 @@ int sdd_plan_create(const sdd_plan_desc* d, sdd_plan** out) {
     free_plan(p);
     return st;
   }
+  if (p->prec == SDD_PREC_MIXED &&
+      ((st = upload32(&p->D2s32, d->D2_sine, nn)) ||
+       (st = upload_linv32(&p->Linv32[0], d->Linv_A4, M, nr, p->ldl)) ||
+       (st = upload_linv32(&p->Linv32[1], d->Linv_T, M, nr, p->ldl)) ||
+       (st = upload_linv32(&p->Linv32[2], d->Linv_S, M, nr, p->ldl)))) {
+    free_plan(p);
+    return st;
+  }
   (void)nm;
   {  // per-step scalars of the chains (Matrix_Operators.py:1143-1159 and 1056-1083)
     std::vector<double> cA((size_t)M * 4), cT((size_t)M * 4), cS((size_t)M * 4);
@@ -608,9 +635,9 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   cudaFree(p->out4); cudaFree(p->rhs); cudaFree(p->xtmp); cudaFree(p->base_tmp); cudaFree(p->hbuf);
   cudaFree(p->dbuf); cudaFree(p->cbuf); cudaFree(p->gridbuf); cudaFree(p->derivbuf);
   cudaFree(p->dg_part); cudaFree(p->dg_out); cudaFree(p->dcnt); cudaFree(p->pbuf);
-  cudaFree(p->x32[0]); cudaFree(p->x32[1]); cudaFree(p->q32);
+  cudaFree(p->x32[0]); cudaFree(p->x32[1]); cudaFree(p->q32); cudaFree(p->g32);
   p->x32[0] = p->x32[1] = nullptr;
-  p->q32 = nullptr;
+  p->q32 = p->g32 = nullptr;
   p->dg_part = p->dg_out = nullptr;
   p->dcnt = nullptr;
   p->pbuf = nullptr;
@@ -637,6 +664,7 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   if (p->prec == SDD_PREC_MIXED) {
     for (float*& x : p->x32) SDD_CUDA(cudaMalloc(&x, (size_t)max_batch * se * sizeof(float)));
     SDD_CUDA(cudaMalloc(&p->q32, (size_t)max_batch * p->M * p->nr * sizeof(float)));
+    SDD_CUDA(cudaMalloc(&p->g32, (size_t)max_batch * se * sizeof(float)));
   }
   p->ws_batch = max_batch;
   return SDD_OK;
@@ -740,11 +768,14 @@ static FixArgs fix_args(const sdd_plan* p, const double* X, const float* x32) {
 // x32_in / x32_out (mixed time steps only): the FP32 copy of X the nonlinear term reads instead of
 // converting X, and the one the chains write beside out for the next step (nullable).  defer: leave a
 // layout-3 chain correction pending (sdd_step); fix_in: X carries the previous step's pending correction,
-// applied by the nonlinear term's first kernel.
+// applied by the nonlinear term's first kernel.  v32 (mixed plans, mode 1, nullable): an FP32 copy of X
+// (stride ldx); the right-hand sides and h = Linv g are then formed in FP32 (k_rhs32, k_mode_mv32), for
+// Jacobian products inside a GMRES solve whose tolerance is far above FP32 rounding.
 static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X, size_t ldx,
                          double* out, size_t ldo, const double* sub, size_t lds, int mode, void* base, int prec,
                          cudaStream_t s, cudaEvent_t* ev = nullptr, const float* x32_in = nullptr,
-                         float* x32_out = nullptr, const int* active = nullptr, int defer = 0, int fix_in = 0) {
+                         float* x32_out = nullptr, const int* active = nullptr, int defer = 0, int fix_in = 0,
+                         const float* v32 = nullptr) {
   RhsArgs ra = rhs_args(p, X, p->out4, Ra, Ras, p->rhs, mode == 2);
   ra.x_stride = ldx;
   ra.active = active;
@@ -776,6 +807,13 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
     SDD_CUDA(launch_fx(fa, batch, fm, prec, s));
   }
   if (ev) SDD_CUDA(cudaEventRecord(ev[1], s));
+  const bool rhs32 = v32 && mode == 1 && prec == SDD_PREC_MIXED && !fuse && p->g32 && ra.q32;
+  if (rhs32) {
+    ra.X32 = v32;
+    ra.x32_stride = ldx;
+    ra.rhs32 = p->g32;
+    ra.D2s32 = p->D2s32;
+  }
   if (!fuse) SDD_CUDA(launch_rhs(ra, batch, s));
   if (ev) SDD_CUDA(cudaEventRecord(ev[2], s));
   ChainArgs ca = chain_args(p, p->rhs, out, sub);
@@ -783,6 +821,10 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
   ca.sub_stride = lds;
   ca.active = active;
   ca.defer_fix = defer && mode == 0 && !sub;
+  if (rhs32) {
+    ca.g32 = p->g32;
+    ca.Linv32A4 = p->Linv32[0]; ca.Linv32T = p->Linv32[1]; ca.Linv32S = p->Linv32[2];
+  }
   if (prec == SDD_PREC_MIXED && mode == 0 && !sub) {
     ca.f32 = x32_out;
     ca.f32_stride = shell_elems(p);
@@ -1047,6 +1089,7 @@ static int solver_reserve(sdd_plan* p, int B, int m) {
   SDD_CUDA(cudaMalloc(&p->sv_g, (size_t)B * n * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->sv_base64, (size_t)B * be * sizeof(double)));
   SDD_CUDA(cudaMalloc(&p->sv_base32, (size_t)B * be * sizeof(float)));
+  if (p->prec == SDD_PREC_MIXED) SDD_CUDA(cudaMalloc(&p->kv_v32, (size_t)B * ld * sizeof(float)));
   SDD_CUDA(cudaMalloc(&p->sv_dev, (size_t)8 * B * sizeof(double)));
   p->sv_B = B;
   p->sv_m = m;
@@ -1076,8 +1119,9 @@ static GmresState gmres_state(sdd_plan* p, int B, int m) {
 }
 
 // Device matvec on B shells: out = A v (vectors of stride ld); shells whose flag in `active` (device,
-// nullable) is 0 may be skipped, their part of out left as it was.
-using MatVec = std::function<int(const double* v, double* out, const int* active)>;
+// nullable) is 0 may be skipped, their part of out left as it was.  v32 (nullable): v rounded to FP32,
+// same strides, for matvecs that work in FP32.
+using MatVec = std::function<int(const double* v, double* out, const int* active, const float* v32)>;
 
 // Restarted GMRES(m), CGS2, for the shells with solve[b] != 0: A x = rhs, x starts at 0, inner stop
 // |r_b| <= target[b] (absolute).  x, rhs have stride ld with nu used doubles.  resid (host) receives the
@@ -1096,17 +1140,17 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const double* rhs, double* 
   for (int cyc = 0; cyc < max_restarts; ++cyc) {
     const double* r = rhs;
     if (cyc > 0) {                                   // r = rhs - A x
-      if ((st = A(x, p->kv_w, G.solve))) return st;
+      if ((st = A(x, p->kv_w, G.solve, nullptr))) return st;
       ++*matvecs;
       SDD_CUDA(krylov_sub(rhs, p->kv_w, p->kv_r, vs, s));
       r = p->kv_r;
     }
     SDD_CUDA(krylov_dots(r, 0, r, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s));
     SDD_CUDA(krylov_cycle_start(G, p->kv_nrm2, B, s));
-    SDD_CUDA(krylov_scale(r, G.inv, p->kv_V, nu, ld, B, s));
+    SDD_CUDA(krylov_scale(r, G.inv, p->kv_V, nu, ld, B, s, p->kv_v32));
     for (int j = 0; j < m; ++j) {
       double* Vj = p->kv_V + (size_t)j * vs;
-      if ((st = A(Vj, p->kv_w, G.active))) return st;
+      if ((st = A(Vj, p->kv_w, G.active, p->kv_v32))) return st;   // kv_v32: Vj in FP32
       ++*matvecs;
       // shells whose Arnoldi process has stopped skip the Gram-Schmidt work (krylov_arnoldi_finish ignores them)
       SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.hcol, m + 1, 0, s, G.active));
@@ -1115,7 +1159,7 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const double* rhs, double* 
       SDD_CUDA(krylov_sub_combination(p->kv_V, vs, p->kv_w, G.h2, m + 1, nu, ld, j + 1, B, s, G.active));
       SDD_CUDA(krylov_dots(p->kv_w, 0, p->kv_w, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s, G.active));
       SDD_CUDA(krylov_arnoldi_finish(G, p->kv_nrm2, j, B, s));
-      if (j + 1 < m) SDD_CUDA(krylov_scale(p->kv_w, G.inv, p->kv_V + (size_t)(j + 1) * vs, nu, ld, B, s));
+      if (j + 1 < m) SDD_CUDA(krylov_scale(p->kv_w, G.inv, p->kv_V + (size_t)(j + 1) * vs, nu, ld, B, s, p->kv_v32));
       SDD_CUDA(cudaMemcpyAsync(p->h_int, G.active, B * sizeof(int), cudaMemcpyDeviceToHost, s));
       SDD_CUDA(cudaStreamSynchronize(s));
       bool act = false;
@@ -1153,6 +1197,7 @@ extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const doub
   if (!Ra || !Ras || !X || !o || !res) return SDD_ERR_ARG;
   const int m = o->restart;
   if (m < 1 || m > 64 || o->max_newton < 0 || o->max_restarts < 1 || !(o->tol >= 0.0)) return SDD_ERR_ARG;
+  if (o->mixed_matvec < 0 || o->mixed_matvec > 2) return SDD_ERR_ARG;
   if (o->mixed_matvec && p->prec != SDD_PREC_MIXED) return SDD_ERR_ARG;
   if ((st = solver_reserve(p, B, m))) return st;
   cudaStream_t s = (cudaStream_t)stream;
@@ -1163,9 +1208,10 @@ extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const doub
   std::vector<int> nmask(B, 0), iters(B, 0);
   int matvecs = 0;
   // the Jacobian of PFX about the cached base state, on vectors of stride ld
-  MatVec J = [&](const double* v, double* out, const int* active) {
+  const bool fp32_rhs = o->mixed_matvec == 2;
+  MatVec J = [&](const double* v, double* out, const int* active, const float* v32) {
     return apply_step_ld(p, B, Ra, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s, nullptr, nullptr, nullptr,
-                         active);
+                         active, 0, 0, fp32_rhs ? v32 : nullptr);
   };
   for (int it = 0;; ++it) {
     if ((st = apply_step_ld(p, B, Ra, Ras, X, n, p->sv_F, ld, X, n, 0, p->sv_base64, SDD_PREC_FP64, s)))
@@ -1251,12 +1297,12 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
     }
     return pdfmu(p, B, Xs, n, s);
   };
-  MatVec J = [&](const double* v, double* out, const int* active) {
+  MatVec J = [&](const double* v, double* out, const int* active, const float*) {
     return apply_step_ld(p, B, mu_dev, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s, nullptr, nullptr, nullptr,
                          active);
   };
   // bordered operator DG = [[DF_X, DF_mu], [delta X_dot^T, (1-delta) mu_dot]]  (Main.py:914-915)
-  MatVec DG = [&](const double* v, double* out, const int* active) -> int {
+  MatVec DG = [&](const double* v, double* out, const int* active, const float*) -> int {
     int r = apply_step_ld(p, B, mu_dev, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s, nullptr, nullptr,
                           nullptr, active);
     if (r) return r;

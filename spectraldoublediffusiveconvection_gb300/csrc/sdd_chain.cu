@@ -608,8 +608,48 @@ __global__ void __launch_bounds__(128) k_mode_mv_warp(ChainArgs a, int nfields) 
   }
 }
 
+// h = Linv g in FP32 from the FP32 right-hand sides (k_rhs32) and the FP32 copies of the Linv blocks: one
+// warp per (field, mode, shell), one lane per row, four partial sums; h stored in FP64 for the chains.
+__global__ void __launch_bounds__(128) k_mode_mv32(ChainArgs a, int nfields) {
+  __shared__ float gsm[4][kMaxNr];
+  const int M = a.M, nr = a.nr, ldl = a.ldl;
+  const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  const int b = blockIdx.y;
+  if (wid >= nfields * M || (a.active && !a.active[b])) return;
+  const int fl = wid / M, jj = wid - fl * M;
+  const int field = a.field0 + fl;
+  const int row = M - 1 - jj;
+  const size_t foff = (size_t)field * a.field_off;
+  const float* A = (field == 0 ? a.Linv32A4 : (field == 1 ? a.Linv32T : a.Linv32S)) + (size_t)jj * nr * ldl;
+  const float* x = a.g32 + (size_t)b * a.g_stride + foff + (size_t)row * nr;
+  double* y = a.h + (size_t)b * a.h_stride + foff + (size_t)row * nr;
+  float* gw = gsm[threadIdx.x >> 5];
+  for (int c = lane; c < nr; c += 32) gw[c] = x[c];
+  __syncwarp();
+  for (int r = lane; r < nr; r += 32) {
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+    int col = 0;
+    for (; col + 4 <= nr; col += 4) {
+      a0 = fmaf(__ldg(A + (size_t)col * ldl + r), gw[col], a0);
+      a1 = fmaf(__ldg(A + (size_t)(col + 1) * ldl + r), gw[col + 1], a1);
+      a2 = fmaf(__ldg(A + (size_t)(col + 2) * ldl + r), gw[col + 2], a2);
+      a3 = fmaf(__ldg(A + (size_t)(col + 3) * ldl + r), gw[col + 3], a3);
+    }
+    for (; col < nr; ++col) a0 = fmaf(__ldg(A + (size_t)col * ldl + r), gw[col], a0);
+    y[r] = (double)((a0 + a1) + (a2 + a3));
+  }
+}
+
 template <bool FIX>
 static cudaError_t launch_mode_mv(const ChainArgs& a, int batch, int nfields, cudaStream_t s, bool per_warp) {
+  if (!FIX && a.g32) {   // FP32 right-hand sides: the FP32 matvecs, whatever the chain layout
+    if (!a.Linv32A4 || !a.Linv32T || !a.Linv32S || a.fuse_rhs) return cudaErrorInvalidValue;
+    const cudaError_t e = launch_kernel(k_mode_mv32, dim3((nfields * a.M + 3) / 4, batch), dim3(128), 0, s, a,
+                                        nfields);
+    ktimer_mark(SDD_K_MODE_H, s);
+    return e;
+  }
   if (per_warp) {
     const dim3 wg((nfields * a.M + 3) / 4, batch);
     const cudaError_t e = a.nr <= 32 ? launch_kernel(k_mode_mv_warp<FIX, 4>, wg, dim3(128), 0, s, a, nfields)

@@ -775,6 +775,78 @@ __global__ void __launch_bounds__(kFxThreads) k_rhs(RhsArgs a) {
   }
 }
 
+// The same right-hand sides in FP32, for Jacobian products inside GMRES solves whose tolerance is far
+// above FP32 rounding: X from its FP32 copy, D2s and Dr Q in FP32, the nonlinear-term outputs rounded once,
+// written to rhs32.  FP64 arithmetic (and FP64<->FP32 conversion) runs on the GPU's narrow FP64 pipe; here
+// only the three conversions of the nonlinear-term outputs per element remain on it.
+__global__ void __launch_bounds__(kFxThreads) k_rhs32(RhsArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int M = a.M, nr = a.nr;
+  const int n = blockIdx.x, b = blockIdx.y;
+  if (a.active && !a.active[b]) return;
+  const int tid = threadIdx.x, bd = blockDim.x;
+  float* sm = reinterpret_cast<float*>(smem_raw);
+  float* pv = sm;
+  float* Sc = pv + M;
+  float* D2p = Sc + M;
+  float* DrQ = D2p + M;
+  float* Tv = DrQ + M;
+  float* Sv = Tv + M;
+  float* opr = Sv + M;  // Dr row n, D2s row n
+  for (int m = tid; m < nr; m += bd) {
+    opr[m] = a.Dr32[n * nr + m];
+    opr[nr + m] = a.D2s32[n * nr + m];
+  }
+  __syncthreads();
+  const int N = M * nr;
+  const float* Xs = a.X32 + (size_t)b * a.x32_stride;
+  const double* O4 = a.linear ? nullptr : a.out4 + (size_t)b * a.out_stride;
+  for (int k = tid; k < M; k += bd) {
+    const bool psi_on = !(a.sym && (k % 2 == 0));
+    const bool ts_on = !(a.sym && (k % 2 == 1));
+    const float* ps = Xs + (size_t)k * nr;
+    float d2 = 0.0f, pn = 0.0f, q = 0.0f;
+    if (psi_on) {
+      for (int m = 0; m < nr; ++m) d2 = fmaf(opr[nr + m], __ldg(ps + m), d2);
+      pn = __ldg(ps + n);
+    }
+    if (O4) {
+      const float* qs = a.q32 + (size_t)b * M * nr + (size_t)k * nr;
+      for (int m = 0; m < nr; ++m) q = fmaf(opr[m], __ldg(qs + m), q);
+    }
+    pv[k] = pn;
+    D2p[k] = d2;
+    DrQ[k] = q;
+    Tv[k] = ts_on ? __ldg(Xs + N + (size_t)k * nr + n) : 0.0f;
+    Sv[k] = ts_on ? __ldg(Xs + 2 * N + (size_t)k * nr + n) : 0.0f;
+  }
+  __syncthreads();
+  parity_suffix<float>(pv, Sc, M);
+  __syncthreads();
+  const float dt = (float)a.dt, dtPr = (float)(a.dt * a.Pr);
+  const float Ra = (float)a.Ra[b], Ras = (float)a.Ra_s[b];
+  const float ir2 = (float)a.ir2s[n], rsq = (float)a.rsq[n], dT0 = (float)a.dT0[n], gr = (float)a.gr[n];
+  float* R = a.rhs32 + (size_t)b * a.rhs_stride;
+  for (int k = tid; k < M; k += bd) {
+    const float s1 = (k + 1 < M) ? Sc[k + 1] : 0.0f;
+    const float JP = (k == 0) ? s1 : (float)(k + 1) * pv[k - 1] + 2.0f * s1;                  // J_theta_RT
+    const float s2 = (k + 2 < M) ? Sc[k + 2] : 0.0f;
+    const float Om = D2p[k] - (float)(k + 1) * ir2 * ((float)(k + 2) * pv[k] + 2.0f * s2);   // A2_SINE
+    const float grv = (k < M - 1) ? (-(float)(k + 1) * gr) * (Ra * Tv[k + 1] - Ras * Sv[k + 1]) : 0.0f;
+    float nxp = 0.0f, nxt = 0.0f, nxs = 0.0f;
+    const size_t o = (size_t)k * nr + n;
+    if (O4) {
+      nxp = -dt * (DrQ[k] - (float)O4[N + o]);
+      nxt = -dt * (float)O4[2 * N + o];
+      nxs = -dt * (float)O4[3 * N + o];
+    }
+    const float psiT0 = dT0 * JP;                                                            // DT0_theta
+    R[o] = nxp + (Om + dtPr * grv);
+    R[N + o] = nxt + (rsq * Tv[k] - dt * psiT0);
+    R[2 * N + o] = nxs + (rsq * Sv[k] - dt * psiT0);
+  }
+}
+
 // ---- standalone theta recurrences (J_theta_RT, A2_SINE_R2, A2_SINE, DT0_theta) ------------------
 struct ThetaArgs {
   int op, M, nr, sym;
@@ -1083,6 +1155,17 @@ cudaError_t launch_fx(const FxArgs& a, int batch, int mode, int prec, cudaStream
 }
 
 cudaError_t launch_rhs(const RhsArgs& a, int batch, cudaStream_t s) {
+  if (a.rhs32) {   // needs X32, D2s32, Dr32 and (with a nonlinear term) q32
+    if (!a.X32 || !a.D2s32 || !a.Dr32 || (!a.linear && !a.q32)) return cudaErrorInvalidValue;
+    const size_t smem32 = (6 * (size_t)a.M + 2 * (size_t)a.nr) * sizeof(float);
+    static unsigned long long done32 = 0;
+    cudaError_t e = ensure_smem_attr(k_rhs32, &done32);
+    if (e != cudaSuccess) return e;
+    const cudaError_t er = launch_kernel(k_rhs32, dim3(a.nr, batch), dim3(kFxThreads), smem32, s, a);
+    ktimer_mark(SDD_K_RHS, s);
+    if (er != cudaSuccess) return er;
+    return cudaGetLastError();
+  }
   const size_t smem = (6 * (size_t)a.M + 2 * (size_t)a.nr) * sizeof(double);
   static unsigned long long done = 0;
   cudaError_t e = ensure_smem_attr(k_rhs, &done);

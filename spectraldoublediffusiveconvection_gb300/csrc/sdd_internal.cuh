@@ -158,6 +158,12 @@ struct RhsArgs {
   const float* q32;
   const float* Dr32;
   const int* active;         // nullable: per-shell flags; kernels skip shells whose flag is 0
+  // FP32 right-hand sides (Jacobian products of Newton solves whose GMRES tolerance is far above FP32
+  // rounding): k_rhs32 reads the FP32 copy X32 of X and writes rhs32 [shell][3][M][nr] instead of rhs
+  const float* X32;
+  size_t x32_stride;         // floats between shells in X32
+  float* rhs32;
+  const float* D2s32;        // nr*nr (A2_SINE) in FP32
 };
 
 // A chunk correction of the state left pending by the previous time step (layout 3, sdd_step): the split
@@ -272,6 +278,10 @@ struct ChainArgs {
   ChunkSet cset[2];          // the chunkings of layouts 2 and 3 (launch_chain copies one into the fields above)
   int defer_fix;             // layout 3: leave the correction to the next step's nonlinear term (FixArgs)
   const int* active;         // nullable: per-shell flags; kernels skip shells whose flag is 0
+  // nullable: FP32 right-hand sides (k_rhs32, stride g_stride): h = Linv g is then formed in FP32 with the
+  // FP32 copies of the Linv blocks (k_mode_mv32) and stored in FP64 for the chains
+  const float* g32;
+  const float* Linv32A4, *Linv32T, *Linv32S;
 };
 
 struct DiagArgs {

@@ -118,11 +118,14 @@ __global__ void k_add_combination(const double* __restrict__ V, size_t vstride_i
 
 // out[b] = a[b] * scale[b]  (scale may be per shell)
 __global__ void k_scale(const double* __restrict__ a, const double* __restrict__ scale, double* __restrict__ out,
-                        int n, int ld) {
+                        int n, int ld, float* __restrict__ out32) {
   const int b = blockIdx.y;
   const double s = scale[b];
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
-    out[(size_t)b * ld + e] = a[(size_t)b * ld + e] * s;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const double v = a[(size_t)b * ld + e] * s;
+    out[(size_t)b * ld + e] = v;
+    if (out32) out32[(size_t)b * ld + e] = (float)v;
+  }
 }
 
 // out = a - b
@@ -293,8 +296,9 @@ cudaError_t krylov_add_combination(const double* V, size_t vstride_i, double* x,
   return cudaGetLastError();
 }
 
-cudaError_t krylov_scale(const double* a, const double* scale, double* out, int n, int ld, int B, cudaStream_t st) {
-  k_scale<<<dim3(grid_x(n), B), 256, 0, st>>>(a, scale, out, n, ld);
+cudaError_t krylov_scale(const double* a, const double* scale, double* out, int n, int ld, int B, cudaStream_t st,
+                         float* out32) {
+  k_scale<<<dim3(grid_x(n), B), 256, 0, st>>>(a, scale, out, n, ld, out32);
   return cudaGetLastError();
 }
 

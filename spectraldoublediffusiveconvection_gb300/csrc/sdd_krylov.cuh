@@ -34,7 +34,9 @@ cudaError_t krylov_sub_combination(const double* V, size_t vstride_i, double* w,
                                    int n, int ld, int nv, int B, cudaStream_t st, const int* active = nullptr);
 cudaError_t krylov_add_combination(const double* V, size_t vstride_i, double* x, const double* y, int ldy,
                                    const int* kb, int n, int ld, int B, cudaStream_t st);
-cudaError_t krylov_scale(const double* a, const double* scale, double* out, int n, int ld, int B, cudaStream_t st);
+// out = a * scale[b]; out32 (nullable, same strides): the result also rounded to FP32
+cudaError_t krylov_scale(const double* a, const double* scale, double* out, int n, int ld, int B, cudaStream_t st,
+                         float* out32 = nullptr);
 cudaError_t krylov_sub(const double* a, const double* b, double* out, size_t n, cudaStream_t st);
 cudaError_t krylov_masked_sub(double* X, const double* dx, const int* mask, int n, int ldx, int ld, int B,
                               cudaStream_t st);

@@ -268,11 +268,15 @@ class Plan:
     def newton(self, X, Ra, Ra_s, tol=1e-10, restart=50, gmres_rtol=1e-4, max_newton=20, max_restarts=20,
                mixed_matvec=False, raise_on_fail=False):
         """Newton-GMRES on F(X) = Phi_dt(X) - X in place on X (batch x n_state); returns per-shell dicts
-        (residual0, residual, newton_iters, matvecs, converged).  The plan's dt should be 1 (Main.py:430)."""
+        (residual0, residual, newton_iters, matvecs, converged).  The plan's dt should be 1 (Main.py:430).
+        mixed_matvec (mixed plans): False/0 FP64 Jacobian products, True/1 with the FP32 nonlinear term,
+        2 also with FP32 right-hand sides and h = Linv g matvecs (the chains and the residual stay FP64)."""
         B = self._chk(X, self.n_state, "X")
         ra, ras = self._vec(Ra, B), self._vec(Ra_s, B)
-        o = _lib.NewtonOpts(float(tol), float(gmres_rtol), int(restart), int(max_restarts), int(max_newton),
-                            int(bool(mixed_matvec)))
+        mv = int(mixed_matvec)
+        if mv not in (0, 1, 2):
+            raise ValueError("mixed_matvec: expected False/True, 0, 1 or 2")
+        o = _lib.NewtonOpts(float(tol), float(gmres_rtol), int(restart), int(max_restarts), int(max_newton), mv)
         res = (_lib.NewtonResult * B)()
         st = self._L.sdd_newton_gmres(self._h, B, _dptr(ra), _dptr(ras), _dptr(X), ctypes.byref(o), res,
                                       _stream(self.device))

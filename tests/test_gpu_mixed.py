@@ -50,3 +50,42 @@ def test_mixed_newton_reaches_fp64_residual(cuda):
     assert r["converged"] and r["residual"] <= 1e-10, r
     ops1 = O.Operators(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
     assert np.linalg.norm(O.PFX(ops1, X.cpu().numpy().ravel(), 8000.0, 500.0, False)) <= 1.5e-10
+
+
+@pytest.mark.parametrize("layout", [0, 2, 4, 5])
+def test_fp32_rhs_newton_matches_mixed_newton(cuda, layout):
+    """mixed_matvec=2: FP32 right-hand sides and h = Linv g matvecs inside the Jacobian products as well (the
+    chains and the residual stay FP64).  A batch of shells (perturbed states, different Ra_T) reaches the
+    FP64 residual, the oracle's residual agrees, and the steady states equal those of mixed_matvec=1."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    N_fm, N_r, B = 64, 20, 4
+    p = Plan(N_fm, N_r, 2.0, 1.0, 1.0, 0.01, precision="mixed")
+    p.set_chain_layout(layout)
+    X0 = np.stack([O.seeded_state(N_fm, N_r - 1, 1234 + i) for i in range(B)])
+    Ra = torch.tensor([7000.0, 8000.0, 9000.0, 10000.0], dtype=torch.float64, device="cuda")
+    X1 = torch.from_numpy(X0).cuda()
+    X2 = X1.clone()
+    r1 = p.newton(X1, Ra, 500.0, tol=1e-10, mixed_matvec=1)
+    r2 = p.newton(X2, Ra, 500.0, tol=1e-10, mixed_matvec=2)
+    ops1 = O.Operators(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
+    for b in range(B):
+        assert r2[b]["converged"] and r2[b]["residual"] <= 1e-10, (b, r2[b])
+        assert np.linalg.norm(O.PFX(ops1, X2[b].cpu().numpy(), float(Ra[b]), 500.0, False)) <= 1.5e-10
+        assert r2[b]["newton_iters"] <= r1[b]["newton_iters"] + 1, (r1[b], r2[b])
+    # both converge to the same steady states (to the Newton tolerance)
+    d = (X2 - X1).norm().item()
+    assert d <= 1e-8 * max(1.0, X1.norm().item()), d
+    assert r2[0]["matvecs"] <= 1.25 * r1[0]["matvecs"] + 2, (r1[0]["matvecs"], r2[0]["matvecs"])
+
+
+def test_fp32_rhs_newton_requires_mixed_plan(cuda):
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    from spectraldoublediffusiveconvection_gb300 import _lib
+    torch = cuda
+    p = Plan(16, 8, 2.0, 1.0, 1.0, 0.01)
+    X = torch.from_numpy(O.seeded_state(16, 7, 3)).cuda().reshape(1, -1)
+    with pytest.raises(_lib.SDDError):
+        p.newton(X, 8000.0, 500.0, mixed_matvec=2)
+    with pytest.raises(ValueError):
+        p.newton(X, 8000.0, 500.0, mixed_matvec=3)
