@@ -522,21 +522,22 @@ def bench_gb300(args):
                   "matvecs": res["matvecs"], "residual0": res["residual0"], "residual": res["residual"],
                   "converged": res["converged"], "tol": 1e-10, "restart": 50}
         # batched: 64 shells of the same shape in one sdd_newton_gmres call (each shell its own Krylov
-        # space), FP32 nonlinear term inside the Jacobian products, FP64 residual <= 1e-10
+        # space), FP32 nonlinear term, right-hand sides and h matvecs inside the Jacobian products (FP64
+        # chains, Krylov basis and residual), FP64 residual <= 1e-10
         nb = 64
         planm = Plan(M, N_r, w["d"], 1.0, w["Pr"], w["Tau"], precision="mixed", device=device)
         planm.set_chain_layout(4)      # whole chains, split rows: measured best for the 64-shell Newton batch
         pert = torch.from_numpy(np.stack([seeded_state(M, N_r - 1, 500 + i) for i in range(nb)])).to(device)
         Xb0 = X_after.reshape(1, -1) + pert
         Rab = torch.linspace(7000.0, 9000.0, nb, dtype=torch.float64, device=device)
-        planm.newton(Xb0.clone(), Rab, Ras, tol=1e-10, restart=50, max_newton=1, mixed_matvec=True)  # warm-up
+        planm.newton(Xb0.clone(), Rab, Ras, tol=1e-10, restart=50, max_newton=1, mixed_matvec=2)  # warm-up
         Xb = Xb0.clone()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        rb = planm.newton(Xb, Rab, Ras, tol=1e-10, restart=50, gmres_rtol=1e-4, max_newton=20, mixed_matvec=True)
+        rb = planm.newton(Xb, Rab, Ras, tol=1e-10, restart=50, gmres_rtol=1e-4, max_newton=20, mixed_matvec=2)
         torch.cuda.synchronize()
         tb = time.perf_counter() - t0
-        newton["batched"] = {"solves_per_s": nb / tb, "seconds": tb, "shells": nb, "mixed_matvec": True,
+        newton["batched"] = {"solves_per_s": nb / tb, "seconds": tb, "shells": nb, "mixed_matvec": 2,
                              "converged": sum(r["converged"] for r in rb),
                              "max_residual": max(r["residual"] for r in rb), "matvecs": rb[0]["matvecs"],
                              "vs_plain_single_shell": (nb / tb) / (1.0 / tn),

@@ -609,35 +609,47 @@ __global__ void __launch_bounds__(128) k_mode_mv_warp(ChainArgs a, int nfields) 
 }
 
 // h = Linv g in FP32 from the FP32 right-hand sides (k_rhs32) and the FP32 copies of the Linv blocks: one
-// warp per (field, mode, shell), one lane per row, four partial sums; h stored in FP64 for the chains.
-__global__ void __launch_bounds__(128) k_mode_mv32(ChainArgs a, int nfields) {
-  __shared__ float gsm[4][kMaxNr];
+// warp per (field, mode) and group of up to kMv32Shells shells, one lane per row.  The lane keeps its row
+// of the block in registers for all shells of the group (the block is read once per group, not once per
+// shell); each shell's g row is loaded once per lane and broadcast by shuffles.  h is stored in FP64 for
+// the chains.  NP: passes of 32 rows (nr <= 32 NP).
+constexpr int kMv32Shells = 16;
+
+template <int NP>
+__global__ void __launch_bounds__(128) k_mode_mv32(ChainArgs a, int nfields, int batch) {
   const int M = a.M, nr = a.nr, ldl = a.ldl;
   const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  const int b = blockIdx.y;
-  if (wid >= nfields * M || (a.active && !a.active[b])) return;
+  if (wid >= nfields * M) return;
   const int fl = wid / M, jj = wid - fl * M;
   const int field = a.field0 + fl;
-  const int row = M - 1 - jj;
-  const size_t foff = (size_t)field * a.field_off;
+  const size_t foff = (size_t)field * a.field_off + (size_t)(M - 1 - jj) * nr;   // this mode's row
   const float* A = (field == 0 ? a.Linv32A4 : (field == 1 ? a.Linv32T : a.Linv32S)) + (size_t)jj * nr * ldl;
-  const float* x = a.g32 + (size_t)b * a.g_stride + foff + (size_t)row * nr;
-  double* y = a.h + (size_t)b * a.h_stride + foff + (size_t)row * nr;
-  float* gw = gsm[threadIdx.x >> 5];
-  for (int c = lane; c < nr; c += 32) gw[c] = x[c];
-  __syncwarp();
-  for (int r = lane; r < nr; r += 32) {
-    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
-    int col = 0;
-    for (; col + 4 <= nr; col += 4) {
-      a0 = fmaf(__ldg(A + (size_t)col * ldl + r), gw[col], a0);
-      a1 = fmaf(__ldg(A + (size_t)(col + 1) * ldl + r), gw[col + 1], a1);
-      a2 = fmaf(__ldg(A + (size_t)(col + 2) * ldl + r), gw[col + 2], a2);
-      a3 = fmaf(__ldg(A + (size_t)(col + 3) * ldl + r), gw[col + 3], a3);
+  const int b0 = blockIdx.y * kMv32Shells;
+  const int b1 = min(batch, b0 + kMv32Shells);
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    const int r = p * 32 + lane;
+    const bool rok = r < nr;
+    float Ar[32 * NP];
+#pragma unroll
+    for (int c = 0; c < 32 * NP; ++c) Ar[c] = (rok && c < nr) ? __ldg(A + (size_t)c * ldl + r) : 0.0f;
+    for (int b = b0; b < b1; ++b) {
+      if (a.active && !a.active[b]) continue;
+      const float* x = a.g32 + (size_t)b * a.g_stride + foff;
+      float xv[NP];
+#pragma unroll
+      for (int q = 0; q < NP; ++q) xv[q] = (q * 32 + lane < nr) ? x[q * 32 + lane] : 0.0f;
+      float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+#pragma unroll
+      for (int c = 0; c < 32 * NP; c += 4) {
+        s0 = fmaf(Ar[c], __shfl_sync(0xffffffffu, xv[c / 32], c % 32), s0);
+        s1 = fmaf(Ar[c + 1], __shfl_sync(0xffffffffu, xv[(c + 1) / 32], (c + 1) % 32), s1);
+        s2 = fmaf(Ar[c + 2], __shfl_sync(0xffffffffu, xv[(c + 2) / 32], (c + 2) % 32), s2);
+        s3 = fmaf(Ar[c + 3], __shfl_sync(0xffffffffu, xv[(c + 3) / 32], (c + 3) % 32), s3);
+      }
+      if (rok) a.h[(size_t)b * a.h_stride + foff + r] = (double)((s0 + s1) + (s2 + s3));
     }
-    for (; col < nr; ++col) a0 = fmaf(__ldg(A + (size_t)col * ldl + r), gw[col], a0);
-    y[r] = (double)((a0 + a1) + (a2 + a3));
   }
 }
 
@@ -645,8 +657,9 @@ template <bool FIX>
 static cudaError_t launch_mode_mv(const ChainArgs& a, int batch, int nfields, cudaStream_t s, bool per_warp) {
   if (!FIX && a.g32) {   // FP32 right-hand sides: the FP32 matvecs, whatever the chain layout
     if (!a.Linv32A4 || !a.Linv32T || !a.Linv32S || a.fuse_rhs) return cudaErrorInvalidValue;
-    const cudaError_t e = launch_kernel(k_mode_mv32, dim3((nfields * a.M + 3) / 4, batch), dim3(128), 0, s, a,
-                                        nfields);
+    const dim3 grid((nfields * a.M + 3) / 4, (batch + kMv32Shells - 1) / kMv32Shells);
+    const cudaError_t e = a.nr <= 32 ? launch_kernel(k_mode_mv32<1>, grid, dim3(128), 0, s, a, nfields, batch)
+                                     : launch_kernel(k_mode_mv32<2>, grid, dim3(128), 0, s, a, nfields, batch);
     ktimer_mark(SDD_K_MODE_H, s);
     return e;
   }

@@ -778,9 +778,12 @@ __global__ void __launch_bounds__(kFxThreads) k_rhs(RhsArgs a) {
 // The same right-hand sides in FP32, for Jacobian products inside GMRES solves whose tolerance is far
 // above FP32 rounding: X from its FP32 copy, D2s and Dr Q in FP32, the nonlinear-term outputs rounded once,
 // written to rhs32.  FP64 arithmetic (and FP64<->FP32 conversion) runs on the GPU's narrow FP64 pipe; here
-// only the three conversions of the nonlinear-term outputs per element remain on it.
+// only the conversions of the nonlinear-term outputs and of the per-CTA scalars remain on it.  (Staging the
+// psi and Q rows in shared memory was measured slower: the 66 KB per CTA cut the resident CTAs that hide
+// the latency of these row reads.)
 __global__ void __launch_bounds__(kFxThreads) k_rhs32(RhsArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ float scal[8];
   const int M = a.M, nr = a.nr;
   const int n = blockIdx.x, b = blockIdx.y;
   if (a.active && !a.active[b]) return;
@@ -792,15 +795,25 @@ __global__ void __launch_bounds__(kFxThreads) k_rhs32(RhsArgs a) {
   float* DrQ = D2p + M;
   float* Tv = DrQ + M;
   float* Sv = Tv + M;
-  float* opr = Sv + M;  // Dr row n, D2s row n
+  float* opr = Sv + M;                      // Dr row n, D2s row n
   for (int m = tid; m < nr; m += bd) {
     opr[m] = a.Dr32[n * nr + m];
     opr[nr + m] = a.D2s32[n * nr + m];
   }
-  __syncthreads();
+  if (tid == 0) {
+    scal[0] = (float)a.dt;
+    scal[1] = (float)(a.dt * a.Pr);
+    scal[2] = (float)a.Ra[b];
+    scal[3] = (float)a.Ra_s[b];
+    scal[4] = (float)a.ir2s[n];
+    scal[5] = (float)a.rsq[n];
+    scal[6] = (float)a.dT0[n];
+    scal[7] = (float)a.gr[n];
+  }
   const int N = M * nr;
   const float* Xs = a.X32 + (size_t)b * a.x32_stride;
   const double* O4 = a.linear ? nullptr : a.out4 + (size_t)b * a.out_stride;
+  __syncthreads();                          // opr / scal are visible
   for (int k = tid; k < M; k += bd) {
     const bool psi_on = !(a.sym && (k % 2 == 0));
     const bool ts_on = !(a.sym && (k % 2 == 1));
@@ -823,16 +836,17 @@ __global__ void __launch_bounds__(kFxThreads) k_rhs32(RhsArgs a) {
   __syncthreads();
   parity_suffix<float>(pv, Sc, M);
   __syncthreads();
-  const float dt = (float)a.dt, dtPr = (float)(a.dt * a.Pr);
-  const float Ra = (float)a.Ra[b], Ras = (float)a.Ra_s[b];
-  const float ir2 = (float)a.ir2s[n], rsq = (float)a.rsq[n], dT0 = (float)a.dT0[n], gr = (float)a.gr[n];
+  const float dt = scal[0], dtPr = scal[1], Ra = scal[2], Ras = scal[3];
+  const float ir2 = scal[4], rsq = scal[5], dT0 = scal[6], gr = scal[7];
   float* R = a.rhs32 + (size_t)b * a.rhs_stride;
   for (int k = tid; k < M; k += bd) {
+    // k as a float without an int->float conversion: the bits of 2^23 + k, minus 2^23 (exact for k < 2^23)
+    const float k1 = (__int_as_float(0x4B000000 | k) - 8388608.0f) + 1.0f;
     const float s1 = (k + 1 < M) ? Sc[k + 1] : 0.0f;
-    const float JP = (k == 0) ? s1 : (float)(k + 1) * pv[k - 1] + 2.0f * s1;                  // J_theta_RT
+    const float JP = (k == 0) ? s1 : k1 * pv[k - 1] + 2.0f * s1;                                // J_theta_RT
     const float s2 = (k + 2 < M) ? Sc[k + 2] : 0.0f;
-    const float Om = D2p[k] - (float)(k + 1) * ir2 * ((float)(k + 2) * pv[k] + 2.0f * s2);   // A2_SINE
-    const float grv = (k < M - 1) ? (-(float)(k + 1) * gr) * (Ra * Tv[k + 1] - Ras * Sv[k + 1]) : 0.0f;
+    const float Om = D2p[k] - k1 * ir2 * ((k1 + 1.0f) * pv[k] + 2.0f * s2);                    // A2_SINE
+    const float grv = (k < M - 1) ? (-k1 * gr) * (Ra * Tv[k + 1] - Ras * Sv[k + 1]) : 0.0f;
     float nxp = 0.0f, nxt = 0.0f, nxs = 0.0f;
     const size_t o = (size_t)k * nr + n;
     if (O4) {

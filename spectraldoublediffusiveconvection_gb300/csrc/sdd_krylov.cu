@@ -20,11 +20,29 @@ constexpr int kDotThreads = 256;
 // The chunk of w sits in registers (kDotPer elements per thread); the vectors go kDotVecs at a time, so
 // each thread has kDotVecs * kDotPer independent loads in flight and a block reduction serves kDotVecs
 // dot products (the products are FP64-throughput bound on this GPU, about 5 TB/s of V).  Each partial is
-// a fixed-order sum: per thread over its elements in index order, then the shuffle tree, then the warps
-// in order.
+// a fixed-order sum: per thread over its elements in index order, then the warp's transposed shuffle
+// tree (warp_sum4), then the warps in order.
 constexpr int kDotPer = kDotChunk / kDotThreads;
 constexpr int kDotVecs = 4;
 static_assert(kDotChunk % kDotThreads == 0, "dot chunk must be a multiple of the block");
+
+// Warp sums of four values per lane in 6 FP64 additions per lane instead of 4 x 5: the first two shuffle
+// levels exchange halves of the set (lanes with bit 4 set keep vectors 2-3, then lanes with bit 3 set
+// keep the odd one), the last three are a plain tree.  Lanes 8v..8v+7 return the sum of vector v.
+__device__ __forceinline__ double warp_sum4(const double (&sv)[4], int lane) {
+  const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0;
+  double k0 = h16 ? sv[2] : sv[0], k1 = h16 ? sv[3] : sv[1];
+  const double s0 = h16 ? sv[0] : sv[2], s1 = h16 ? sv[1] : sv[3];
+  k0 += __shfl_xor_sync(0xffffffffu, s0, 16);
+  k1 += __shfl_xor_sync(0xffffffffu, s1, 16);
+  double k = h8 ? k1 : k0;
+  const double t = h8 ? k0 : k1;
+  k += __shfl_xor_sync(0xffffffffu, t, 8);
+  k += __shfl_xor_sync(0xffffffffu, k, 4);
+  k += __shfl_xor_sync(0xffffffffu, k, 2);
+  k += __shfl_xor_sync(0xffffffffu, k, 1);
+  return k;
+}
 
 __global__ void __launch_bounds__(kDotThreads) k_dot_partials(const double* __restrict__ V, size_t vstride_i,
                                                              const double* __restrict__ w, int n, int ld, int nv,
@@ -59,12 +77,9 @@ __global__ void __launch_bounds__(kDotThreads) k_dot_partials(const double* __re
         }
       }
     }
-#pragma unroll
-    for (int u = 0; u < kDotVecs; ++u) {
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) sv[u] += __shfl_xor_sync(0xffffffffu, sv[u], off);
-      if (lane == 0) red[u][warp] = sv[u];
-    }
+    static_assert(kDotVecs == 4, "warp_sum4 reduces four vectors");
+    const double ws = warp_sum4(sv, lane);
+    if ((lane & 7) == 0) red[lane >> 3][warp] = ws;
     __syncthreads();
     if (threadIdx.x < kDotVecs && i0 + threadIdx.x < nv) {
       double t = 0.0;
@@ -163,8 +178,13 @@ __global__ void k_cycle_start(GmresState s, const double* __restrict__ nrm2, int
 
 // After CGS2 for column j: hcol[b][0..j] holds the projections, nrm2[b] = ||w||^2.  Stores the column in H,
 // applies the previous Givens rotations, makes the new one, updates g and the residual estimate.
-__global__ void k_arnoldi_finish(GmresState s, const double* __restrict__ nrm2, int j, int B) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(32) k_arnoldi_finish(GmresState s, const double* __restrict__ nrm2, int j,
+                                                        int B) {
+  // one warp per shell: the lanes stage the column (hcol + h2) and the previous rotations in shared memory,
+  // lane 0 applies the rotations (the rotated entry of row i + 1 carried in a register, the only dependent
+  // chain) and makes the new one, the lanes write the column back
+  __shared__ double col[kMaxRestart + 1], csv[kMaxRestart], snv[kMaxRestart];
+  const int b = blockIdx.x, lane = threadIdx.x;
   if (b >= B) return;
   const int m = s.m;
   double* H = s.H + (size_t)b * (m + 1) * m;   // H[row*m + col]
@@ -173,37 +193,48 @@ __global__ void k_arnoldi_finish(GmresState s, const double* __restrict__ nrm2, 
   double* cs = s.cs + (size_t)b * m;
   double* sn = s.sn + (size_t)b * m;
   double* g = s.g + (size_t)b * (m + 1);
-  const double hnext = sqrt(nrm2[b]);
   if (!s.active[b]) {
-    s.inv[b] = 0.0;
+    if (lane == 0) s.inv[b] = 0.0;
     return;
   }
-  for (int i = 0; i <= j; ++i) H[i * m + j] = hc[i] + hd[i];
-  H[(j + 1) * m + j] = hnext;
-  for (int i = 0; i < j; ++i) {
-    const double a = H[i * m + j], c = H[(i + 1) * m + j];
-    H[i * m + j] = cs[i] * a + sn[i] * c;
-    H[(i + 1) * m + j] = -sn[i] * a + cs[i] * c;
+  for (int i = lane; i <= j; i += 32) col[i] = hc[i] + hd[i];
+  for (int i = lane; i < j; i += 32) {
+    csv[i] = cs[i];
+    snv[i] = sn[i];
   }
-  const double a = H[j * m + j], c = H[(j + 1) * m + j];
-  const double r = hypot(a, c);
-  double cj = 1.0, sj = 0.0;
-  if (r > 0.0) {
-    cj = a / r;
-    sj = c / r;
+  __syncwarp();
+  if (lane == 0) {
+    const double hnext = sqrt(nrm2[b]);
+    double a = col[0];
+    for (int i = 0; i < j; ++i) {
+      const double c = col[i + 1];
+      col[i] = fma(csv[i], a, snv[i] * c);
+      a = fma(-snv[i], a, csv[i] * c);
+    }
+    const double c = hnext;
+    const double r = hypot(a, c);
+    double cj = 1.0, sj = 0.0;
+    if (r > 0.0) {
+      cj = a / r;
+      sj = c / r;
+    }
+    cs[j] = cj;
+    sn[j] = sj;
+    H[j * m + j] = r;
+    H[(j + 1) * m + j] = 0.0;
+    g[j + 1] = -sj * g[j];
+    g[j] = cj * g[j];
+    const double res = fabs(g[j + 1]);
+    s.resid[b] = res;
+    s.kb[b] = j + 1;
+    const bool breakdown = !(hnext > 1e-300 * s.beta[b]);
+    int act = 1;
+    if (res <= s.target[b] || breakdown || j + 1 == m) act = 0;
+    s.active[b] = act;
+    s.inv[b] = (act && hnext > 0.0) ? 1.0 / hnext : 0.0;
   }
-  cs[j] = cj;
-  sn[j] = sj;
-  H[j * m + j] = r;
-  H[(j + 1) * m + j] = 0.0;
-  g[j + 1] = -sj * g[j];
-  g[j] = cj * g[j];
-  const double res = fabs(g[j + 1]);
-  s.resid[b] = res;
-  s.kb[b] = j + 1;
-  const bool breakdown = !(hnext > 1e-300 * s.beta[b]);
-  if (res <= s.target[b] || breakdown || j + 1 == m) s.active[b] = 0;
-  s.inv[b] = (s.active[b] && hnext > 0.0) ? 1.0 / hnext : 0.0;
+  __syncwarp();
+  for (int i = lane; i < j; i += 32) H[i * m + j] = col[i];
 }
 
 // Back substitution R y = g over the first kb[b] columns.
@@ -319,7 +350,8 @@ cudaError_t krylov_cycle_start(const GmresState& s, const double* nrm2, int B, c
 }
 
 cudaError_t krylov_arnoldi_finish(const GmresState& s, const double* nrm2, int j, int B, cudaStream_t st) {
-  k_arnoldi_finish<<<(B + 63) / 64, 64, 0, st>>>(s, nrm2, j, B);
+  if (s.m > kMaxRestart || j >= s.m) return cudaErrorInvalidValue;
+  k_arnoldi_finish<<<B, 32, 0, st>>>(s, nrm2, j, B);
   return cudaGetLastError();
 }
 

@@ -6,6 +6,7 @@
 namespace sdd {
 
 constexpr int kDotChunk = 2048;   // elements per CTA in the two-level dot products
+constexpr int kMaxRestart = 64;   // GMRES restart length limit (Newton and continuation check it)
 
 struct GmresState {
   int m;            // restart length
