@@ -633,6 +633,38 @@ def bench_gb300(args):
     return 0
 
 
+def profile_newton_batch():
+    """One Newton iteration (residual, one GMRES(50) solve, update) of the 64-shell batched Newton workload
+    inside an NVTX range "newton_batched", for a kernel launch list of the batched Jacobian products:
+    ncu --nvtx --nvtx-include "newton_batched/" ... python bench.py --profile-newton-batch.  The start: the
+    seeded shell after 2000 IMEX steps of dt=5e-4 plus the 64 seeded perturbations of the bench workload."""
+    import numpy as np
+    import torch
+    from spectraldoublediffusiveconvection_gb300.seeds import seeded_state
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    w = WORKLOAD
+    M, N_r = w["N_theta"], w["N_r"]
+    device = torch.device("cuda", 0)
+    p = Plan(M, N_r, w["d"], w["dt"], w["Pr"], w["Tau"], device=device)
+    X0 = torch.from_numpy(seeded_state(M, N_r - 1, w["seed"])).to(device).reshape(1, -1)
+    Xa = p.step(X0, w["Ra_T"], w["Ra_S"], nsteps=2000)
+    nb = 64
+    pert = torch.from_numpy(np.stack([seeded_state(M, N_r - 1, 500 + i) for i in range(nb)])).to(device)
+    Xb0 = Xa.reshape(1, -1) + pert
+    Rab = torch.linspace(7000.0, 9000.0, nb, dtype=torch.float64, device=device)
+    Ras = torch.full((nb,), w["Ra_S"], dtype=torch.float64, device=device)
+    q = Plan(M, N_r, w["d"], 1.0, w["Pr"], w["Tau"], precision="mixed", device=device)
+    q.set_chain_layout(4)
+    q.newton(Xb0.clone(), Rab, Ras, tol=1e-10, restart=50, max_newton=1, mixed_matvec=2)   # warm-up
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("newton_batched")
+    r = q.newton(Xb0.clone(), Rab, Ras, tol=1e-10, restart=50, max_newton=1, mixed_matvec=2)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    print(json.dumps({"profile": "newton_batched", "shells": nb, "jacobian_products": r[0]["matvecs"]}))
+    return 0
+
+
 def main():
     if len(sys.argv) > 1 and sys.argv[1] == "--cpu-worker":
         cpu_worker(float(sys.argv[2]), int(sys.argv[3]), int(sys.argv[4]),
@@ -649,7 +681,10 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--served-requests", type=int, default=1000)
+    ap.add_argument("--profile-newton-batch", action="store_true")
     args = ap.parse_args()
+    if args.profile_newton_batch:
+        return profile_newton_batch()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
