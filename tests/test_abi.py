@@ -39,3 +39,34 @@ def test_argument_errors_need_no_gpu(built_lib):
     h = ctypes.c_void_p()
     assert lib.sdd_plan_create(ctypes.byref(d), ctypes.byref(h)) == _lib.SDD_ERR_ODD_NFM
     assert lib.sdd_step(None, 1, None, None, None, None, 1, 0, None) == _lib.SDD_ERR_ARG
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors of the option/result structs have the C header's field offsets and sizes (a C
+    program compiled against include/sdd_gb300.h prints them)."""
+    import shutil
+    import subprocess
+    import pytest
+    from spectraldoublediffusiveconvection_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"sdd_plan_desc": _lib.PlanDesc, "sdd_newton_opts": _lib.NewtonOpts,
+               "sdd_newton_result": _lib.NewtonResult, "sdd_contin_opts": _lib.ContinOpts,
+               "sdd_contin_result": _lib.ContinResult}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "sdd_gb300.h"', "int main(void) {"]
+    for cname, cls in mirrors.items():
+        lines.append('  printf("%s sizeof %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _ in cls._fields_:
+            lines.append('  printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, cls in mirrors.items():
+        assert got[(cname, "sizeof")] == ctypes.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert got[(cname, fname)] == getattr(cls, fname).offset, (cname, fname)
