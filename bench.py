@@ -38,7 +38,9 @@ L2_FLUSH_BYTES = 512 << 20
 
 
 def algorithmic(M, nr):
-    """Per IMEX step of one shell: FP64 flops and bytes of the reference's algorithm:
+    """Per IMEX step of one shell: FP64 flops and bytes of the reference's algorithm (the radial
+    contractions, 12 real transforms of length P per radius at 2.5 P log2 P, the pointwise products and
+    the theta recurrences; the state in and out plus the three Linv sets read once):
     flops = 21 M nr^2 + 12 nr 2.5 P log2 P + 11 nr P + 40 nr M, bytes = 48 M nr + 24 M nr^2.
     Chain kernel alone: flops 8 M nr^2, bytes 24 M nr^2 + 48 M nr."""
     import math
