@@ -118,3 +118,25 @@ def test_linear_problem_matches_reference():
     for N_fm in (16, 32):
         assert rel(O.Full_Eig_Vec(f, 2.0, N_fm, 19), Z[f"full_{N_fm}"]) < 1e-13
     assert rel(O.Full_Eig_Vec(f, 2.0, 16, 19, symmetric=True), Z["full_sym_16"]) < 1e-13
+
+
+def test_oracle_on_continuation_golden():
+    """The reference's steady convective state (Ra_T = 9000, N_r = N_fm = 16, Tau = 1) and the point its
+    _ContinC step reached (tests/golden/cont_tau1.npz) are zeros of the oracle's PFX, and the oracle's
+    diagnostics of both equal the Norm / Kinetic_Energy / Nusselt values the reference reported."""
+    import numpy as np
+    Z = load_golden("cont_tau1.npz")
+    N_r, N_fm, dt, d, Pr, Tau, Ra0, Ra_s, sym = Z["params"]
+    N_r, N_fm = int(N_r), int(N_fm)
+    nr, N = N_r - 1, N_fm * (N_r - 1)
+    ops1 = O.Operators(N_fm, N_r, d, 1.0, Pr, Tau)
+    D, R = O.cheb_radial(N_r, d)
+    X, Y = Z["X_steady"], Z["Y"]
+    assert np.linalg.norm(O.PFX(ops1, X, Ra0, Ra_s, False)) <= 1e-12
+    assert np.linalg.norm(O.PFX(ops1, Y[:-1], Y[-1], Ra_s, False)) <= 1e-12
+
+    def diag(v):
+        return np.array([np.linalg.norm(v), O.Kinetic_Energy(v, R, D, N_fm, nr, False),
+                         O.Nusselt(v[N:2 * N], d, R, D, N_fm, nr), O.Nusselt(v[2 * N:], d, R, D, N_fm, nr)])
+    assert np.allclose(diag(X), Z["steady_diag"], rtol=1e-12, atol=0)
+    assert np.allclose(diag(Y[:-1]), [Z["Norm"], Z["KE"], Z["NuT"], Z["NuS"]], rtol=1e-12, atol=0)
