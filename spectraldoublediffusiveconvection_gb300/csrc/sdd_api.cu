@@ -1079,7 +1079,7 @@ static int solver_reserve(sdd_plan* p, int B, int m) {
   SDD_CUDA(cudaMalloc(&p->kv_dot, (size_t)B * sizeof(double)));
   const size_t small = (size_t)B * ((size_t)(m + 1) * m + 3 * (m + 1) + 3 * m + 4);
   SDD_CUDA(cudaMalloc(&p->kv_small, small * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->kv_ismall, (size_t)4 * B * sizeof(int)));
+  SDD_CUDA(cudaMalloc(&p->kv_ismall, (size_t)5 * B * sizeof(int)));
   SDD_CUDA(cudaMallocHost(&p->h_dbl, (size_t)2 * B * sizeof(double)));
   SDD_CUDA(cudaMallocHost(&p->h_int, (size_t)B * sizeof(int)));
   double** v[] = {&p->sv_F, &p->sv_x, &p->sv_Xd, &p->sv_t, &p->sv_G};
@@ -1115,6 +1115,7 @@ static GmresState gmres_state(sdd_plan* p, int B, int m) {
   s.active = iq; iq += B;
   s.solve = iq; iq += B;
   s.kb = iq; iq += B;
+  s.reo = p->kv_ismall + (size_t)4 * B;   // (block 3 is the Newton update mask)
   return s;
 }
 
@@ -1123,9 +1124,9 @@ static GmresState gmres_state(sdd_plan* p, int B, int m) {
 // same strides, for matvecs that work in FP32.
 using MatVec = std::function<int(const double* v, double* out, const int* active, const float* v32)>;
 
-// Restarted GMRES(m), CGS2, for the shells with solve[b] != 0: A x = rhs, x starts at 0, inner stop
-// |r_b| <= target[b] (absolute).  x, rhs have stride ld with nu used doubles.  resid (host) receives the
-// final residual estimates.
+// Restarted GMRES(m), classical Gram-Schmidt with a conditional second pass, for the shells with
+// solve[b] != 0: A x = rhs, x starts at 0, inner stop |r_b| <= target[b] (absolute).  x, rhs have stride
+// ld with nu used doubles.  resid (host) receives the final residual estimates.
 static int gmres_solve(sdd_plan* p, const MatVec& A, const double* rhs, double* x, int B, int nu, int ld, int m,
                        int max_restarts, const std::vector<double>& target, const std::vector<int>& solve,
                        cudaStream_t s, int* matvecs, std::vector<double>& resid) {
@@ -1155,8 +1156,12 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const double* rhs, double* 
       // shells whose Arnoldi process has stopped skip the Gram-Schmidt work (krylov_arnoldi_finish ignores them)
       SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.hcol, m + 1, 0, s, G.active));
       SDD_CUDA(krylov_sub_combination(p->kv_V, vs, p->kv_w, G.hcol, m + 1, nu, ld, j + 1, B, s, G.active));
-      SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.h2, m + 1, 0, s, G.active));
-      SDD_CUDA(krylov_sub_combination(p->kv_V, vs, p->kv_w, G.h2, m + 1, nu, ld, j + 1, B, s, G.active));
+      // the second pass only for the shells whose first pass cancelled w below kReorthEta of its norm
+      // (the others get zero second projections)
+      SDD_CUDA(krylov_dots(p->kv_w, 0, p->kv_w, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s, G.active));
+      SDD_CUDA(krylov_reorth_mask(G, p->kv_nrm2, j, kReorthEta, B, s));
+      SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.h2, m + 1, 0, s, G.reo));
+      SDD_CUDA(krylov_sub_combination(p->kv_V, vs, p->kv_w, G.h2, m + 1, nu, ld, j + 1, B, s, G.reo));
       SDD_CUDA(krylov_dots(p->kv_w, 0, p->kv_w, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s, G.active));
       SDD_CUDA(krylov_arnoldi_finish(G, p->kv_nrm2, j, B, s));
       if (j + 1 < m) SDD_CUDA(krylov_scale(p->kv_w, G.inv, p->kv_V + (size_t)(j + 1) * vs, nu, ld, B, s, p->kv_v32));

@@ -1,6 +1,7 @@
 // Device Krylov kernels for the matrix-free Newton-GMRES of Main.py:523-536 (the reference calls
 // scipy.sparse.linalg.lgmres on a LinearOperator wrapping PDFX).  Here: restarted GMRES(m) with
-// classical Gram-Schmidt applied twice (CGS2), FP64 throughout, one Krylov space per shell of a batch.
+// classical Gram-Schmidt, the pass repeated for a column only where the first one cancelled w below
+// kReorthEta of its norm, FP64 throughout, one Krylov space per shell of a batch.
 //
 // Reductions are deterministic: every dot product is a fixed-order two-level sum (per-CTA partials over
 // fixed element chunks, then a fixed-order sum of the partials), so a shell's result does not depend
@@ -176,8 +177,8 @@ __global__ void k_cycle_start(GmresState s, const double* __restrict__ nrm2, int
   s.resid[b] = beta;
 }
 
-// After CGS2 for column j: hcol[b][0..j] holds the projections, nrm2[b] = ||w||^2.  Stores the column in H,
-// applies the previous Givens rotations, makes the new one, updates g and the residual estimate.
+// After Gram-Schmidt for column j: hcol + h2 [b][0..j] hold the projections, nrm2[b] = ||w||^2.  Stores the
+// column in H, applies the previous Givens rotations, makes the new one, updates g and the residual estimate.
 __global__ void __launch_bounds__(32) k_arnoldi_finish(GmresState s, const double* __restrict__ nrm2, int j,
                                                         int B) {
   // one warp per shell: the lanes stage the column (hcol + h2) and the previous rotations in shared memory,
@@ -235,6 +236,22 @@ __global__ void __launch_bounds__(32) k_arnoldi_finish(GmresState s, const doubl
   }
   __syncwarp();
   for (int i = lane; i < j; i += 32) H[i * m + j] = col[i];
+}
+
+// Whether shell b repeats the Gram-Schmidt pass of column j: |w'|^2 = nrm2[b] after the first pass,
+// |w|^2 = |w'|^2 + |h|^2 for an orthonormal basis.
+__global__ void k_reorth_mask(GmresState s, const double* __restrict__ nrm2, int j, double eta2, int B) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  int r = 0;
+  if (s.active[b]) {
+    const double* hc = s.hcol + (size_t)b * (s.m + 1);
+    double h2 = 0.0;
+    for (int i = 0; i <= j; ++i) h2 = fma(hc[i], hc[i], h2);
+    const double n1 = nrm2[b];
+    r = n1 < eta2 * (n1 + h2) ? 1 : 0;
+  }
+  s.reo[b] = r;
 }
 
 // Back substitution R y = g over the first kb[b] columns.
@@ -352,6 +369,11 @@ cudaError_t krylov_cycle_start(const GmresState& s, const double* nrm2, int B, c
 cudaError_t krylov_arnoldi_finish(const GmresState& s, const double* nrm2, int j, int B, cudaStream_t st) {
   if (s.m > kMaxRestart || j >= s.m) return cudaErrorInvalidValue;
   k_arnoldi_finish<<<B, 32, 0, st>>>(s, nrm2, j, B);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_reorth_mask(const GmresState& s, const double* nrm2, int j, double eta, int B, cudaStream_t st) {
+  k_reorth_mask<<<(B + 63) / 64, 64, 0, st>>>(s, nrm2, j, eta * eta, B);
   return cudaGetLastError();
 }
 

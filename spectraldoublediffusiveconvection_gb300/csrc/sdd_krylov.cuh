@@ -24,7 +24,12 @@ struct GmresState {
   int* active;      // [B] still iterating in the current cycle
   int* solve;       // [B] shell takes part in this solve
   int* kb;          // [B] columns used
+  int* reo;         // [B] shell repeats the Gram-Schmidt pass for the current column
 };
+
+// The second Gram-Schmidt pass of a column runs only where the first one left less than this fraction of
+// w's norm (|w'| < eta |w|): the loss of orthogonality of one pass is then at most ~eps/eta.
+constexpr double kReorthEta = 1e-2;
 
 // n: used doubles per shell, ld: stride between shells (n <= ld); active (device, nullable): shells whose
 // flag is 0 are skipped (dots: zero results; combinations: w left as it was)
@@ -43,6 +48,8 @@ cudaError_t krylov_masked_sub(double* X, const double* dx, const int* mask, int 
                               cudaStream_t st);
 cudaError_t krylov_cycle_start(const GmresState& s, const double* nrm2, int B, cudaStream_t st);
 cudaError_t krylov_arnoldi_finish(const GmresState& s, const double* nrm2, int j, int B, cudaStream_t st);
+// s.reo[b] = active and nrm2[b] < eta^2 (nrm2[b] + sum_{i<=j} hcol[b][i]^2) (|w|^2 = |w'|^2 + |h|^2)
+cudaError_t krylov_reorth_mask(const GmresState& s, const double* nrm2, int j, double eta, int B, cudaStream_t st);
 cudaError_t krylov_solve_y(const GmresState& s, int B, cudaStream_t st);
 cudaError_t krylov_copy_scaled(const double* src, int lds, double* dst, int ldd, int n, double a, const double* last,
                                int B, cudaStream_t st);
