@@ -190,7 +190,8 @@ typedef struct sdd_contin_opts {
   int32_t restart, max_restarts;
   int32_t max_corrector;   /* corrector iterations before ds is halved (5)                         */
   int32_t max_halvings;
-  int32_t mixed_matvec;
+  int32_t mixed_matvec;    /* as in sdd_newton_opts: 0 FP64 products, 1 FP32 nonlinear term, 2 also FP32
+                              right-hand sides and h matvecs (mixed plans)                           */
   int32_t pad;
 } sdd_contin_opts;
 
@@ -252,6 +253,11 @@ const char* sdd_kernel_name(int id);
 int sdd_step_kernel_profile(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s,
                             const double* X_in, double* X_out, int nsteps, double* ms, int* launches,
                             void* stream);
+/* Test hook (no counterpart in the reference): the next `after` workspace allocations (sdd_plan_reserve, and
+ * the Krylov workspace of sdd_newton_gmres / sdd_contin_step) succeed and every later one fails on the host,
+ * before cudaMalloc is called, as if the device were out of memory, so that a caller can check how
+ * SDD_ERR_NOMEM reaches it.  after < 0 removes the limit.  Process-wide. */
+int sdd_debug_fail_allocations(long long after);
 /* Measured FP64 FMA throughput of the current device in GFLOP/s (a register-resident FMA loop over
  * all SMs, a few milliseconds).  The roofline denominator of the FP64-bound kernels. */
 int sdd_measure_fp64_peak(double* gflops, void* stream);

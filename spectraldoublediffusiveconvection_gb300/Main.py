@@ -20,7 +20,6 @@ import numpy as np
 
 from . import Matrix_Operators as MO
 from . import operators as _ops
-from .Transforms import IDCT, IDST, grid
 from .plan import get_plan
 
 
@@ -39,40 +38,57 @@ def Base_State_Coeffs(d):
     return _ops.base_state_coeffs(d)
 
 
-def Nusselt(T_hat, d, R, D, N_fm, nr, check=True):
-    """Main.py:41-68: convective Nusselt number from the even cosine modes of T (or S)."""
-    T_hat = np.asarray(T_hat.cpu() if hasattr(T_hat, "cpu") else T_hat, dtype=np.float64)
+def _diag_plan(D, R, N_fm, nr, symmetric, d, wall=0):
+    """A device plan holding only the diagnostics tables for the caller's (D, R): Nusselt weights of the
+    inner (wall = 0) or outer (wall = -1) boundary row of D (Main.py:55-62) and the radii of the kinetic
+    energy's trapezoid rule (Main.py:124-132).  Cached by content, like the other drop-ins' plans."""
+    D = np.asarray(D, dtype=np.float64)
+    R = np.asarray(R, dtype=np.float64)
     A_T = _ops.base_state_coeffs(d)[0]
-    TT = np.zeros((N_fm // 2 + N_fm % 2, len(R)))
-    ks = np.arange(0, N_fm, 2)
-    TT[:, 1:-1] = T_hat.reshape(N_fm, nr)[ks]
-    NuM1 = ((TT @ D.T) / (1.0 - ks[:, None] ** 2)).sum(axis=0)
-    NuM1 = ((R ** 2) / A_T) * NuM1
-    error = abs(NuM1[-1] - NuM1[0]) / abs(NuM1[-1])
-    if check and error > 1e-03:
-        raise ValueError("|Nu(R_1) - Nu(R_2)|/|Nu(R_1)| = ", error, " > .1%, Increase Nr \n")
-    return NuM1[0]
+    arrays = _ops.theta_operators(D, R)
+    arrays.update(nu_w=np.ascontiguousarray((R[wall] ** 2 / A_T) * D[wall, 1:-1]),
+                  r_int=np.ascontiguousarray(R[1:-1]), R=R)
+    return MO._plan_from(N_fm, nr, symmetric, **arrays)
+
+
+def _device_diag(plan, X):
+    """sdd_diagnostics of one host or device state: (|X|_2, KE, Nu of T, Nu of S)."""
+    import torch
+    if isinstance(X, torch.Tensor):
+        Xd = X.to(device=plan.device, dtype=torch.float64).reshape(1, -1).contiguous()
+    else:
+        Xd = torch.from_numpy(np.ascontiguousarray(X, dtype=np.float64)).to(plan.device).reshape(1, -1)
+    return plan.diagnostics(Xd)[0].tolist()
+
+
+def Nusselt(T_hat, d, R, D, N_fm, nr, check=True):
+    """Main.py:41-68: convective Nusselt number from the even cosine modes of T (or S), on the GPU
+    (sdd_diagnostics).  With check, the value at the outer wall is formed too and a difference above 0.1%
+    raises ValueError as the reference does."""
+    import torch
+    T = T_hat.reshape(-1) if isinstance(T_hat, torch.Tensor) else np.asarray(T_hat, dtype=np.float64).reshape(-1)
+    N = N_fm * nr
+    if isinstance(T, torch.Tensor):
+        X = torch.zeros(3 * N, dtype=torch.float64, device=T.device if T.is_cuda else "cuda")
+        X[N:2 * N] = T.to(X.device, torch.float64)
+    else:
+        X = np.zeros(3 * N)
+        X[N:2 * N] = T
+    nu_in = _device_diag(_diag_plan(D, R, N_fm, nr, False, d, 0), X)[2]
+    if check:
+        nu_out = _device_diag(_diag_plan(D, R, N_fm, nr, False, d, -1), X)[2]
+        error = abs(nu_out - nu_in) / abs(nu_out)
+        if error > 1e-03:
+            raise ValueError("|Nu(R_1) - Nu(R_2)|/|Nu(R_1)| = ", error, " > .1%, Increase Nr \n")
+    return nu_in
 
 
 def Kinetic_Energy(X_hat, R, D, N_fm, nr, symmetric):
-    """Main.py:71-134: volume-averaged kinetic energy; the transforms run on the GPU."""
-    X_hat = np.asarray(X_hat.cpu() if hasattr(X_hat, "cpu") else X_hat, dtype=np.float64)
-    N = N_fm * nr
-    Dr = D[1:-1, 1:-1]
-    JPSI = np.asarray(MO.J_theta_RT(X_hat[0:N], nr, N_fm, symmetric)).reshape(N_fm, nr)
-    PSI = X_hat[0:N].reshape(N_fm, nr)
-    Dpsi_h = (PSI @ Dr.T).T
-    Jpsi_h = (JPSI / R[1:-1][None, :]).T
-    Dpsi_s = np.zeros_like(Dpsi_h)
-    Dpsi_s[:, 1:] = Dpsi_h[:, :-1]
-    th = grid(3 * N_fm)
-    Jpsi = IDCT(Jpsi_h, n=3 * N_fm)
-    Dpsi = IDST(Dpsi_s, n=3 * N_fm)
-    KE_rt = Jpsi ** 2 + Dpsi ** 2
-    KE_t = np.trapezoid(KE_rt, x=R[1:-1], axis=0)
-    KE = np.trapezoid(KE_t * np.sin(th), x=th, axis=-1)
-    V = (2.0 / 3.0) * (R[-1] ** 3 - R[0] ** 3)
-    return (0.5 / V) * KE
+    """Main.py:71-134: volume-averaged kinetic energy (IDCT/IDST of J_theta psi / r and Dr psi to the 3 N_fm
+    grid, trapezoid rules in r and theta), on the GPU (sdd_diagnostics)."""
+    R = np.asarray(R, dtype=np.float64)
+    d = 1.0 / R[0]
+    return _device_diag(_diag_plan(D, R, N_fm, nr, symmetric, d, 0), X_hat)[1]
 
 
 def Eq_SYM(X1, R):
@@ -214,19 +230,56 @@ class result():
                 + '\n' + 'KE                = ' + str(self.KE[i]) + '\n')
 
 
+def _cont_plan(kw):
+    """The dt = 1 plan of a continuation (Main.py:742, 430: the drivers' default dt)."""
+    return get_plan(kw["N_fm"], kw["N_r"], kw["d"], kw.get("dt", 1), kw["Pr"], kw["Tau"], kw.get("symmetric", False))
+
+
+def _newtonc_dev(plan, X, Ra, sign, ds, Ra_s, tol_newton=1e-08, tol_gmres=1e-04, Krylov_Space_Size=300):
+    """_NewtonC (Main.py:717-739) on a device state X (1 x n): Newton at Ra + sign*ds from X.  Returns
+    (X_new, Ra_new, ds, diagnostics or None, converged); X itself is not modified."""
+    Ra_new = float(Ra) + sign * ds
+    Xn = X.clone()
+    r = plan.newton(Xn, Ra_new, Ra_s, tol=tol_newton, restart=min(int(Krylov_Space_Size), 50),
+                    gmres_rtol=tol_gmres)[0]
+    if r["converged"]:
+        return Xn, Ra_new, ds * 2, _diagnostics(plan, Xn), True
+    print('Newton iteration could not converge')
+    return X, float(Ra), ds * 0.5, None, False
+
+
+def _continc_dev(plan, X, Ra, sign, ds, Ra_s, symmetric, tol_newton=1e-08, tol_gmres=1e-04, Krylov_Space_Size=300):
+    """_ContinC (Main.py:742-955) on a device state: X (1 x n) and Ra (device, 1) are updated in place.
+    Returns (X_dot device tensor, Ra_dot, ds, diagnostics); raises ValueError when ds becomes too small
+    (Main.py:895)."""
+    import torch
+    if symmetric:
+        X.mul_(torch.from_numpy(Eq_SYM(np.zeros(plan.n_state), plan.arrays["R"])).to(plan.device).reshape(1, -1))
+    Xd, res = plan.contin_step(X, Ra, Ra_s, sign, ds, tol=tol_newton, restart=min(int(Krylov_Space_Size), 50),
+                               gmres_rtol=tol_gmres, tangent_rtol=tol_newton)
+    r = res[0]
+    if not r["converged"]:
+        raise ValueError("\n Step-size ds has become too small terminating \n")
+    return Xd, r["Ra_dot"], r["ds"], _diagnostics(plan, X)
+
+
 def _NewtonC(Y, sign, ds, **kwargs_f):
     """Main.py:717-739: natural-parameter step Ra -> Ra + sign*ds solved by Newton; ds doubles on success
     and halves on failure."""
     Y = np.asarray(Y.cpu() if hasattr(Y, "cpu") else Y, dtype=np.float64)
-    X = Y[0:-1].copy()
-    Ra = Y[-1] + sign * ds
-    kwargs_f = dict(kwargs_f)
-    kwargs_f["Ra"] = Ra
-    kwargs_f.setdefault("tol_newton", 1e-08)
-    X_new, Norm, KE, NuT, NuS, exitcode = _Newton(X, **kwargs_f)
-    if exitcode:
-        return np.hstack((X_new, Ra)), sign, ds * 2, Norm, KE, NuT, NuS, exitcode
-    return Y, sign, ds * 0.5, Norm, KE, NuT, NuS, exitcode
+    kw = dict(kwargs_f)
+    plan = _cont_plan(kw)
+    X = torch_state(Y[0:-1], plan)
+    Xn, Ra, ds, dg, ok = _newtonc_dev(plan, X, Y[-1], sign, ds, kw["Ra_s"], kw.get("tol_newton", 1e-08),
+                                      kw.get("tol_gmres", 1e-04), kw.get("Krylov_Space_Size", 300))
+    if ok:
+        return np.hstack((Xn.cpu().numpy().ravel(), Ra)), sign, ds, dg[0], dg[1], dg[2], dg[3], ok
+    return Y, sign, ds, None, None, None, None, ok
+
+
+def torch_state(X, plan):
+    """A host state as a (1 x n) float64 tensor on the plan's device."""
+    return _to_state(np.asarray(X, dtype=np.float64).copy(), plan)[0]
 
 
 def _ContinC(Y_0_dot, Y_0, sign, ds, Ra, Ra_s, Tau, Pr, d, N_fm, N_r, symmetric, dt=1, tol_newton=1e-08,
@@ -239,61 +292,77 @@ def _ContinC(Y_0_dot, Y_0, sign, ds, Ra, Ra_s, Tau, Pr, d, N_fm, N_r, symmetric,
     import torch
     plan = get_plan(N_fm, N_r, d, dt, Pr, Tau, symmetric)
     Y_0 = np.asarray(Y_0.cpu() if hasattr(Y_0, "cpu") else Y_0, dtype=np.float64)
-    X = torch.from_numpy(Y_0[0:-1].copy()).to(plan.device).reshape(1, -1)
-    if symmetric:
-        X = X * torch.from_numpy(Eq_SYM(Y_0[0:-1], plan.arrays["R"])).to(plan.device).reshape(1, -1)
+    X = torch_state(Y_0[0:-1], plan)
     Ra_d = torch.tensor([float(Y_0[-1])], dtype=torch.float64, device=plan.device)
-    Xd, res = plan.contin_step(X, Ra_d, Ra_s, sign, ds, tol=tol_newton, restart=min(int(Krylov_Space_Size), 50),
-                               gmres_rtol=tol_gmres, tangent_rtol=tol_newton)
-    r = res[0]
-    if not r["converged"]:
-        raise ValueError("\n Step-size ds has become too small terminating \n")
-    Xh = X.cpu().numpy().ravel()
-    Y = np.hstack((Xh, float(Ra_d.item())))
-    Y_dot = np.hstack((Xd.cpu().numpy().ravel(), r["Ra_dot"]))
-    Norm, KE, NuT, NuS = _diagnostics(plan, X)
-    return Y_dot, Y, sign, r["ds"], Norm, KE, NuT, NuS, True
+    Xd, Ra_dot, ds, dg = _continc_dev(plan, X, Ra_d, sign, ds, Ra_s, symmetric, tol_newton, tol_gmres,
+                                      Krylov_Space_Size)
+    Y = np.hstack((X.cpu().numpy().ravel(), float(Ra_d.item())))
+    Y_dot = np.hstack((Xd.cpu().numpy().ravel(), Ra_dot))
+    return Y_dot, Y, sign, ds, dg[0], dg[1], dg[2], dg[3], True
 
 
 def _Continuation(filename, N_steps, sign, Y, **kwargs):
     """Main.py:958-1045: branch following; natural-parameter Newton steps while ds > 1, pseudo-arclength
-    steps otherwise, fold detection by a sign change of Ra_dot.  Returns the ``result`` record (the reference
-    returns None and writes it to ``filename``; the file is written here only if h5py is importable)."""
-    Y = np.array(Y, dtype=np.float64, copy=True)
-    Y_dot = 0.0 * Y
+    steps otherwise, fold detection by a sign change of Ra_dot.  The state and the tangent stay on the GPU
+    for the whole run: only the scalar records (Ra, Ra_dot, Norm, KE, Nu) come back every step, and the
+    state every 5th step for the checkpoint record (Checkpoints/X_DATA, as the reference).  Returns the
+    ``result`` record (the reference returns None and writes it to ``filename``; the file is written here
+    only if h5py is importable)."""
+    import torch
+    kw = dict(kwargs)
+    plan = _cont_plan(kw)
+    Ra_s, sym = kw["Ra_s"], kw.get("symmetric", False)
+    opts = {k: kw[k] for k in ("tol_gmres", "Krylov_Space_Size") if k in kw}
+    Y = np.asarray(Y.cpu() if hasattr(Y, "cpu") else Y, dtype=np.float64)
+    X = torch_state(Y[0:-1], plan)               # the branch point, resident on the device
+    Ra = torch.tensor([float(Y[-1])], dtype=torch.float64, device=plan.device)
+    Ra_h = float(Y[-1])
+    X_dot = torch.zeros_like(X)                  # tangent (state part) and its parameter part
+    Ra_dot = 0.0
     ds, ds_min, ds_max = 0.01, 1.0, 10.0
     Result = result()
     while Result.Iterations < N_steps:
-        Y_dot_new = None
+        new_dot = None
         if ds > ds_min:
-            OUT = _NewtonC(Y, sign, ds, **kwargs)
-            if OUT[-1] is False:
+            Xn, Ra_n, ds, dg, ok = _newtonc_dev(plan, X, Ra_h, sign, ds, Ra_s, **opts)
+            if not ok:
                 print('Switching to arc-length \n')
-                Y_dot_new, Y_new, sign, ds, Norm, KE, NuT, NuS, _ = _ContinC(Y_dot, Y, sign, ds, **kwargs)
+                new_dot = _continc_dev(plan, X, Ra, sign, ds, Ra_s, sym, **opts)
+                Ra_n = float(Ra.item())
+                ds, dg = new_dot[2], new_dot[3]
             else:
-                Y_new, sign, ds, Norm, KE, NuT, NuS = OUT[0], OUT[1], OUT[2], OUT[3], OUT[4], OUT[5], OUT[6]
+                X = Xn
+                Ra.fill_(Ra_n)
             if ds > ds_max:
                 ds = ds_max
         else:
-            Y_dot_new, Y_new, sign, ds, Norm, KE, NuT, NuS, _ = _ContinC(Y_dot, Y, sign, ds, **kwargs)
-            if (Y_dot_new[-1] * Y_dot[-1]) < 0:
-                Result.Y_FOLD.append(Y_new)
-            sign = 1.0 if Y_new[-1] > Y[-1] else -1.0
-        Y = Y_new.copy()
-        Y_dot = Y_dot_new.copy() if Y_dot_new is not None else 0.0 * Y
-        Result.Ra.append(Y[-1])
-        Result.Ra_dot.append(Y_dot[-1])
+            new_dot = _continc_dev(plan, X, Ra, sign, ds, Ra_s, sym, **opts)
+            Ra_n = float(Ra.item())
+            ds, dg = new_dot[2], new_dot[3]
+            if new_dot[1] * Ra_dot < 0:          # saddle-node: Ra_dot changed sign (Main.py:995-997)
+                Result.Y_FOLD.append(np.hstack((X.cpu().numpy().ravel(), Ra_n)))
+            sign = 1.0 if Ra_n > Ra_h else -1.0
+        Ra_h = Ra_n
+        # a natural-parameter step keeps the last pseudo-arclength tangent (the reference's Y_dot_new outlives
+        # the loop iteration that set it, Main.py:1006-1010); it stays zero until the first arclength step
+        if new_dot is not None:
+            X_dot, Ra_dot = new_dot[0], new_dot[1]
+        Norm, KE, NuT, NuS = dg
+        Result.Ra.append(Ra_h)
+        Result.Ra_dot.append(Ra_dot)
         Result.Norm.append(Norm)
         Result.KE.append(KE)
         Result.NuT.append(NuT)
         Result.NuS.append(NuS)
         if Result.Iterations % 5 == 0:
-            Result.X_DATA.append(Y[0:-1])
-            Result.Ra_DATA.append(Y[-1])
+            Result.X_DATA.append(X.cpu().numpy().ravel())
+            Result.Ra_DATA.append(Ra_h)
             if filename:
                 _write_continuation_h5(filename, Result, kwargs)
         print(Result, flush=True)
         Result.Iterations += 1
+    Result.X = X.reshape(-1)                     # the last branch point, on the device
+    Result.X_dot = X_dot.reshape(-1)
     return Result
 
 

@@ -104,6 +104,7 @@ SIGNATURES = [
     ("sdd_step_kernel_profile", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, ctypes.POINTER(ctypes.c_double),
                                     ctypes.POINTER(ctypes.c_int), _VP]),
     ("sdd_measure_fp64_peak", _I, [ctypes.POINTER(ctypes.c_double), _VP]),
+    ("sdd_debug_fail_allocations", _I, [ctypes.c_longlong]),
 ]
 
 _lib = None
@@ -118,6 +119,10 @@ class SDDError(RuntimeError):
         if status == SDD_ERR_CUDA:
             msg += f" (cudaError {lib().sdd_last_cuda_error()})"
         super().__init__(f"{where}: {msg} [status {status}]")
+
+
+class SDDMemoryError(SDDError, MemoryError):
+    """SDD_ERR_NOMEM: a device allocation of the library failed."""
 
 
 def load(path=LIB_PATH):
@@ -146,5 +151,7 @@ def check(status, where):
     if status != SDD_OK:
         if status == SDD_ERR_ODD_NFM:
             raise ValueError(f"The number of Fourier modes is not even ({where})")
+        if status == SDD_ERR_NOMEM:
+            raise SDDMemoryError(status, where)
         raise SDDError(status, where)
     return status

@@ -7,6 +7,7 @@
 #include <cstring>
 #include <functional>
 #include <map>
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -157,6 +158,25 @@ struct sdd_plan {
   unsigned long long graph_clock;
   cudaStream_t cap_stream;          // private capture stream (created on first use)
 };
+
+// Workspace allocations (sdd_plan_reserve and the Krylov workspace) go through ws_malloc, so that a test can
+// make them fail on the host (sdd_debug_fail_allocations) and check that SDD_ERR_NOMEM reaches the caller.
+static std::atomic<long long> g_alloc_left{-1};   // allocations that still succeed; -1: no limit
+static cudaError_t ws_malloc(void** ptr, size_t bytes, bool pinned_host = false) {
+  long long left = g_alloc_left.load();
+  while (left >= 0) {
+    if (left == 0) {
+      *ptr = nullptr;
+      return cudaErrorMemoryAllocation;
+    }
+    if (g_alloc_left.compare_exchange_weak(left, left - 1)) break;
+  }
+  return pinned_host ? cudaMallocHost(ptr, bytes) : cudaMalloc(ptr, bytes);
+}
+template <typename T>
+static cudaError_t ws_malloc(T** ptr, size_t bytes, bool pinned_host = false) {
+  return ws_malloc(reinterpret_cast<void**>(ptr), bytes, pinned_host);
+}
 
 extern "C" {
 
@@ -628,6 +648,7 @@ size_t sdd_plan_base_cache_elems(const sdd_plan* p) { return p ? (size_t)9 * p->
 
 static size_t shell_elems(const sdd_plan* p) { return (size_t)3 * p->M * p->nr; }
 
+
 int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   if (!p || max_batch < 1) return SDD_ERR_ARG;
   if (max_batch <= p->ws_batch) return SDD_OK;
@@ -646,25 +667,25 @@ int sdd_plan_reserve(sdd_plan* p, int max_batch) {
   p->ws_batch = 0;
   const size_t se = shell_elems(p);
   const size_t be = sdd_plan_base_cache_elems(p);
-  SDD_CUDA(cudaMalloc(&p->out4, (size_t)max_batch * 4 * p->M * p->nr * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->rhs, (size_t)max_batch * se * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->xtmp, (size_t)max_batch * se * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->hbuf, (size_t)max_batch * se * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->base_tmp, (size_t)max_batch * be * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->gridbuf, (size_t)max_batch * be * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->derivbuf, (size_t)max_batch * 5 * p->M * p->nr * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->dg_part, (size_t)max_batch * p->nr * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->dg_out, (size_t)max_batch * 4 * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->dcnt, (size_t)max_batch * 6 * sizeof(int)));
+  SDD_CUDA(ws_malloc(&p->out4, (size_t)max_batch * 4 * p->M * p->nr * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->rhs, (size_t)max_batch * se * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->xtmp, (size_t)max_batch * se * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->hbuf, (size_t)max_batch * se * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->base_tmp, (size_t)max_batch * be * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->gridbuf, (size_t)max_batch * be * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->derivbuf, (size_t)max_batch * 5 * p->M * p->nr * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->dg_part, (size_t)max_batch * p->nr * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->dg_out, (size_t)max_batch * 4 * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->dcnt, (size_t)max_batch * 6 * sizeof(int)));
   SDD_CUDA(cudaMemset(p->dcnt, 0, (size_t)max_batch * 6 * sizeof(int)));
   const size_t de = (size_t)6 * p->nch_alloc * p->ldd;
-  SDD_CUDA(cudaMalloc(&p->dbuf, (size_t)max_batch * de * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->cbuf, (size_t)max_batch * de * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->pbuf, (size_t)max_batch * 6 * p->np_alloc * p->ldd * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->dbuf, (size_t)max_batch * de * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->cbuf, (size_t)max_batch * de * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->pbuf, (size_t)max_batch * 6 * p->np_alloc * p->ldd * sizeof(double)));
   if (p->prec == SDD_PREC_MIXED) {
-    for (float*& x : p->x32) SDD_CUDA(cudaMalloc(&x, (size_t)max_batch * se * sizeof(float)));
-    SDD_CUDA(cudaMalloc(&p->q32, (size_t)max_batch * p->M * p->nr * sizeof(float)));
-    SDD_CUDA(cudaMalloc(&p->g32, (size_t)max_batch * se * sizeof(float)));
+    for (float*& x : p->x32) SDD_CUDA(ws_malloc(&x, (size_t)max_batch * se * sizeof(float)));
+    SDD_CUDA(ws_malloc(&p->q32, (size_t)max_batch * p->M * p->nr * sizeof(float)));
+    SDD_CUDA(ws_malloc(&p->g32, (size_t)max_batch * se * sizeof(float)));
   }
   p->ws_batch = max_batch;
   return SDD_OK;
@@ -1070,27 +1091,27 @@ static int solver_reserve(sdd_plan* p, int B, int m) {
   const size_t n = shell_elems(p), ld = n + 1, be = sdd_plan_base_cache_elems(p);
   const int nchunk = (int)((ld + kDotChunk - 1) / kDotChunk);
   const size_t vb = (size_t)B * ld * sizeof(double);
-  SDD_CUDA(cudaMalloc(&p->kv_V, (size_t)(m + 1) * vb));
-  SDD_CUDA(cudaMalloc(&p->kv_w, vb));
+  SDD_CUDA(ws_malloc(&p->kv_V, (size_t)(m + 1) * vb));
+  SDD_CUDA(ws_malloc(&p->kv_w, vb));
   SDD_CUDA(cudaMemset(p->kv_w, 0, vb));   // shells a masked matvec skips keep finite values here
-  SDD_CUDA(cudaMalloc(&p->kv_r, vb));
-  SDD_CUDA(cudaMalloc(&p->kv_part, (size_t)B * (m + 1) * nchunk * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->kv_nrm2, (size_t)B * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->kv_dot, (size_t)B * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->kv_r, vb));
+  SDD_CUDA(ws_malloc(&p->kv_part, (size_t)B * (m + 1) * nchunk * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->kv_nrm2, (size_t)B * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->kv_dot, (size_t)B * sizeof(double)));
   const size_t small = (size_t)B * ((size_t)(m + 1) * m + 3 * (m + 1) + 3 * m + 4);
-  SDD_CUDA(cudaMalloc(&p->kv_small, small * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->kv_ismall, (size_t)5 * B * sizeof(int)));
-  SDD_CUDA(cudaMallocHost(&p->h_dbl, (size_t)2 * B * sizeof(double)));
-  SDD_CUDA(cudaMallocHost(&p->h_int, (size_t)B * sizeof(int)));
+  SDD_CUDA(ws_malloc(&p->kv_small, small * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->kv_ismall, (size_t)5 * B * sizeof(int)));
+  SDD_CUDA(ws_malloc(&p->h_dbl, (size_t)2 * B * sizeof(double), true));
+  SDD_CUDA(ws_malloc(&p->h_int, (size_t)B * sizeof(int), true));
   double** v[] = {&p->sv_F, &p->sv_x, &p->sv_Xd, &p->sv_t, &p->sv_G};
-  for (double** q : v) SDD_CUDA(cudaMalloc(q, vb));
-  SDD_CUDA(cudaMalloc(&p->sv_X0, (size_t)B * n * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->sv_Jmu, (size_t)B * n * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->sv_g, (size_t)B * n * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->sv_base64, (size_t)B * be * sizeof(double)));
-  SDD_CUDA(cudaMalloc(&p->sv_base32, (size_t)B * be * sizeof(float)));
-  if (p->prec == SDD_PREC_MIXED) SDD_CUDA(cudaMalloc(&p->kv_v32, (size_t)B * ld * sizeof(float)));
-  SDD_CUDA(cudaMalloc(&p->sv_dev, (size_t)8 * B * sizeof(double)));
+  for (double** q : v) SDD_CUDA(ws_malloc(q, vb));
+  SDD_CUDA(ws_malloc(&p->sv_X0, (size_t)B * n * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->sv_Jmu, (size_t)B * n * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->sv_g, (size_t)B * n * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->sv_base64, (size_t)B * be * sizeof(double)));
+  SDD_CUDA(ws_malloc(&p->sv_base32, (size_t)B * be * sizeof(float)));
+  if (p->prec == SDD_PREC_MIXED) SDD_CUDA(ws_malloc(&p->kv_v32, (size_t)B * ld * sizeof(float)));
+  SDD_CUDA(ws_malloc(&p->sv_dev, (size_t)8 * B * sizeof(double)));
   p->sv_B = B;
   p->sv_m = m;
   return SDD_OK;
@@ -1226,7 +1247,9 @@ extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const doub
     for (int b = 0; b < B; ++b) {
       resF[b] = std::sqrt(p->h_dbl[b]);
       if (it == 0) res[b].residual0 = resF[b];
-      nmask[b] = (resF[b] > o->tol) ? 1 : 0;
+      // a non-finite residual (a NaN/Inf state or a diverged update) stops that shell at once: it is
+      // reported as not converged instead of iterating to the caps
+      nmask[b] = (std::isfinite(resF[b]) && resF[b] > o->tol) ? 1 : 0;
       any = any || nmask[b];
     }
     if (!any || it >= o->max_newton) break;
@@ -1273,10 +1296,12 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
   const int m = o->restart;
   if (m < 1 || m > 64 || o->max_restarts < 1 || o->max_corrector < 1 || o->max_halvings < 0 || !(o->tol > 0.0))
     return SDD_ERR_ARG;
+  if (o->mixed_matvec < 0 || o->mixed_matvec > 2) return SDD_ERR_ARG;
   if (o->mixed_matvec && p->prec != SDD_PREC_MIXED) return SDD_ERR_ARG;
   if ((st = solver_reserve(p, B, m))) return st;
   cudaStream_t s = (cudaStream_t)stream;
   const int n = (int)shell_elems(p), ld = n + 1, Npsi = p->M * p->nr;
+  const bool fp32_rhs = o->mixed_matvec == 2;   // FP32 right-hand sides and h matvecs in the products too
   const double delta = 1.0 / n;                         // 1/(3N), Main.py:771
   const int mv_prec = o->mixed_matvec ? SDD_PREC_MIXED : SDD_PREC_FP64;
   void* base_mv = o->mixed_matvec ? (void*)p->sv_base32 : (void*)p->sv_base64;
@@ -1302,14 +1327,14 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
     }
     return pdfmu(p, B, Xs, n, s);
   };
-  MatVec J = [&](const double* v, double* out, const int* active, const float*) {
+  MatVec J = [&](const double* v, double* out, const int* active, const float* v32) {
     return apply_step_ld(p, B, mu_dev, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s, nullptr, nullptr, nullptr,
-                         active);
+                         active, 0, 0, fp32_rhs ? v32 : nullptr);
   };
   // bordered operator DG = [[DF_X, DF_mu], [delta X_dot^T, (1-delta) mu_dot]]  (Main.py:914-915)
-  MatVec DG = [&](const double* v, double* out, const int* active, const float*) -> int {
+  MatVec DG = [&](const double* v, double* out, const int* active, const float* v32) -> int {
     int r = apply_step_ld(p, B, mu_dev, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s, nullptr, nullptr,
-                          nullptr, active);
+                          nullptr, active, 0, 0, fp32_rhs ? v32 : nullptr);
     if (r) return r;
     SDD_CUDA(krylov_dots(p->sv_Xd, 0, v, n, ld, 1, B, p->kv_part, p->kv_dot, 1, 0, s));
     SDD_CUDA(contin_border(v, out, n, ld, p->sv_Jmu, n, Npsi, p->kv_dot, mudot_dev, delta, B, s));
@@ -1368,6 +1393,10 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
       gl[b] = delta * p->h_dbl[B + b] + (1.0 - delta) * mudot[b] * (mu[b] - mu0[b]) - ds[b];
       solve[b] = 0;
       if (conv[b] || fail[b]) continue;
+      if (!std::isfinite(resF[b]) || !std::isfinite(gl[b]) || !std::isfinite(mu[b])) {   // NaN/Inf: give up
+        fail[b] = 1;
+        continue;
+      }
       if (resF[b] <= o->tol && std::fabs(gl[b]) <= o->tol) {
         conv[b] = 1;
         continue;
@@ -1599,6 +1628,11 @@ __global__ void k_fp64_fma_loop(double* out, int iters, double a, double b) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 }  // namespace sdd
+
+extern "C" int sdd_debug_fail_allocations(long long after) {
+  g_alloc_left.store(after < 0 ? -1 : after);
+  return SDD_OK;
+}
 
 extern "C" int sdd_measure_fp64_peak(double* gflops, void* stream) {
   if (!gflops) return SDD_ERR_ARG;

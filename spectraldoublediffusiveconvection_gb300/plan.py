@@ -289,7 +289,8 @@ class Plan:
     def contin_step(self, X, Ra, Ra_s, sign, ds, tol=1e-10, restart=50, gmres_rtol=1e-4, tangent_rtol=1e-8,
                     max_restarts=20, max_corrector=5, max_halvings=8, mixed_matvec=False):
         """One pseudo-arclength step (sdd_contin_step) in place on X (batch x n_state) and Ra (device,
-        batch).  Returns (X_dot tensor, per-shell result dicts)."""
+        batch).  mixed_matvec as in ``newton`` (mixed plans).  Returns (X_dot tensor, per-shell result
+        dicts)."""
         torch = _torch()
         B = self._chk(X, self.n_state, "X")
         if not (isinstance(Ra, torch.Tensor) and Ra.dtype == torch.float64 and Ra.device == self.device
@@ -299,8 +300,11 @@ class Plan:
         Xd = torch.empty_like(X)
         sg = (ctypes.c_double * B)(*[float(v) for v in np.broadcast_to(np.asarray(sign, dtype=float), (B,))])
         dd = (ctypes.c_double * B)(*[float(v) for v in np.broadcast_to(np.asarray(ds, dtype=float), (B,))])
+        mv = int(mixed_matvec)
+        if mv not in (0, 1, 2):
+            raise ValueError("mixed_matvec: expected False/True, 0, 1 or 2")
         o = _lib.ContinOpts(float(tol), float(gmres_rtol), float(tangent_rtol), int(restart), int(max_restarts),
-                            int(max_corrector), int(max_halvings), int(bool(mixed_matvec)), 0)
+                            int(max_corrector), int(max_halvings), mv, 0)
         res = (_lib.ContinResult * B)()
         st = self._L.sdd_contin_step(self._h, B, _dptr(X), _dptr(Ra), _dptr(ras), _dptr(Xd), sg, dd,
                                      ctypes.byref(o), res, _stream(self.device))

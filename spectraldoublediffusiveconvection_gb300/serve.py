@@ -17,8 +17,14 @@ process drives one GPU:
 * Results do not depend on the mix: no arithmetic crosses shells, every reduction has a fixed order, and
   the plans' chain layout is fixed (the automatic choice would depend on the batch size).
 
-Latency of a request = completion time - submission time; the server records admission and completion
-times for p50/p99 reporting.
+Latency of a request = completion time - submission time; the server records admission, start (first
+device work) and completion times, so a latency splits into queue time (submission to start) and device
+time (start to completion) for p50/p99 reporting.
+
+Failure paths (the reference's own exits are Main.py:541-544, 888-899, 923): a request whose state is or
+becomes non-finite completes with an error instead of a result; a continuation step whose corrector does
+not converge completes with an error; ``cancel`` retires a queued request at once and an in-flight one at
+its next quantum boundary (integrations) or when its batched call returns (continuations).
 """
 import collections
 import itertools
@@ -47,9 +53,10 @@ class Request:
         self.id = next(Request._ids)
         self.kind, self.N_r, self.N_theta, self.Ra = kind, int(N_r), int(N_theta), float(Ra)
         self.X, self.n_steps, self.sign, self.ds, self.seed = X, int(n_steps), float(sign), float(ds), seed
-        self.t_submit = self.t_admit = self.t_done = None
+        self.t_submit = self.t_admit = self.t_start = self.t_done = None
         self.result = None
         self.error = None
+        self.cancelled = False
         self._bytes = 0
         self.done = threading.Event()
 
@@ -60,6 +67,16 @@ class Request:
     @property
     def latency(self):
         return None if self.t_done is None else self.t_done - self.t_submit
+
+    @property
+    def queue_time(self):
+        """Submission to the start of the request's first device work."""
+        return None if self.t_start is None else self.t_start - self.t_submit
+
+    @property
+    def device_time(self):
+        """Start of the request's first device work to completion."""
+        return None if self.t_start is None or self.t_done is None else self.t_done - self.t_start
 
 
 def _seeded(M, nr, seed):
@@ -114,7 +131,8 @@ class _IntGroup:
 class Server:
     """Request server over one GPU.  Integrations use plans with step dt and nonlinear-term precision
     ``int_precision``; continuation steps use plans with dt = 1 (Main.py:430, PFX over one unit of time),
-    FP32 nonlinear term inside the Jacobian products when ``con_mixed`` and an FP64 residual <= tol.
+    an FP64 residual <= tol, and inside the Jacobian products the FP32 nonlinear term when ``con_mixed`` is
+    1 (or True), and FP32 right-hand sides and h = Linv g matvecs as well when it is 2.
     Integrations default to the mixed form (FP32 nonlinear term, FP64 implicit solves: 1.7x the served
     integration throughput of FP64 at these sizes; its trajectory error against FP64 is checked by the
     mixed-precision tests).  Every plan has the fixed chain layout ``chain_layout`` (default: chunked, the
@@ -127,7 +145,9 @@ class Server:
         torch = _torch()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.d, self.Pr, self.Tau, self.Ra_s, self.dt = d, Pr, Tau, Ra_s, dt
-        self.int_precision, self.con_mixed = int_precision, bool(con_mixed)
+        self.int_precision, self.con_mixed = int_precision, int(con_mixed)
+        if self.con_mixed not in (0, 1, 2):
+            raise ValueError("con_mixed: expected False/True, 0, 1 or 2")
         self.quantum, self.max_batch, self.con_workers = int(quantum), int(max_batch), int(con_workers)
         self.chain_layout, self.tol, self.restart, self.tangent_rtol = chain_layout, tol, restart, tangent_rtol
         if memory_budget is None:
@@ -220,6 +240,31 @@ class Server:
             self._pending[req.kind].append(req)
             self._cv.notify_all()
         return req
+
+    def cancel(self, req):
+        """Retires a request: a queued one (not yet admitted, or admitted and waiting for its batch) at once,
+        an integration in flight at its group's next quantum boundary, a continuation in flight when its
+        batched call returns.  The request completes with error "cancelled".  Returns True if it was still
+        pending or in flight."""
+        with self._cv:
+            if req.done.is_set():
+                return False
+            req.cancelled = True
+            q = self._pending[req.kind]
+            if req in q:                                  # never admitted: no bytes to return
+                q.remove(req)
+                req.error = "cancelled"
+                req.t_done = time.perf_counter()
+                req.done.set()
+                self._cv.notify_all()
+                return True
+            lst = (self._waiting if req.kind == "continue" else self._int_joining).get(req.shape, [])
+            waiting = req in lst
+            if waiting:
+                lst.remove(req)
+        if waiting:
+            self._finish(req, error="cancelled")
+        return True
 
     def start(self):
         self._running = True
@@ -332,8 +377,9 @@ class Server:
                         return
                     self._cv.wait(timeout=0.01)
                     continue
-            for req in new:
-                joining.setdefault(req.shape, []).append(req)
+            with self._cv:
+                for req in new:
+                    joining.setdefault(req.shape, []).append(req)
             progressed = False
             for shape in list(set(self._groups) | set(joining)):
                 g = self._groups.get(shape)
@@ -345,14 +391,25 @@ class Server:
                     with torch.cuda.stream(streams[shape]):
                         i = 0
                         while i < len(g.reqs):
-                            if g.left[i] <= 0:
-                                req = g.reqs[i]
+                            req = g.reqs[i]
+                            if req.cancelled:
+                                g.remove(i)
+                                self._finish(req, error="cancelled")
+                            elif g.left[i] <= 0:
                                 X = g.X[i].cpu().numpy().copy()
                                 g.remove(i)
-                                self._finish(req, result={"X": X, "Ra": req.Ra, "steps": req.n_steps})
+                                if np.isfinite(X).all():
+                                    self._finish(req, result={"X": X, "Ra": req.Ra, "steps": req.n_steps})
+                                else:
+                                    self._finish(req, error="non-finite state after %d steps" % req.n_steps)
                             else:
                                 i += 1
-                for req in joining.pop(shape, []):
+                with self._cv:
+                    joined = joining.pop(shape, [])
+                for req in joined:
+                    if req.cancelled:
+                        self._finish(req, error="cancelled")
+                        continue
                     try:
                         if g is None:
                             g = _IntGroup(self._plan("integrate", req.N_r, req.N_theta), self.device)
@@ -369,6 +426,10 @@ class Server:
                     continue
                 na = len(g.reqs)
                 q = min(self.quantum, min(g.left))
+                now = time.perf_counter()
+                for req in g.reqs:
+                    if req.t_start is None:
+                        req.t_start = now
                 try:
                     with torch.cuda.stream(streams[shape]):
                         g.plan.step(g.X[:na], g.Ra[:na], g.Ras[:na], nsteps=q, out=g.X[:na])
@@ -416,6 +477,9 @@ class Server:
                     batch = self._waiting[shape][:self.max_batch]
                     del self._waiting[shape][:len(batch)]
                     self._con_inflight.add(shape)
+                t0 = time.perf_counter()
+                for req in batch:
+                    req.t_start = t0
                 try:
                     plan = self._plan("continue", *shape)
                     X = torch.from_numpy(np.stack([np.asarray(r.X, dtype=np.float64) for r in batch])).to(self.device)
@@ -428,8 +492,16 @@ class Server:
                         self.stats["con_calls"] += 1
                         self.stats["con_shells"] += len(batch)
                     for k, req in enumerate(batch):
-                        self._finish(req, result={"X": Xh[k].copy(), "Ra": float(Rah[k]), "X_dot": Xdh[k].copy(),
-                                                  **res[k]})
+                        if req.cancelled:
+                            self._finish(req, error="cancelled")
+                        elif not (np.isfinite(Xh[k]).all() and np.isfinite(Rah[k])):
+                            self._finish(req, error="non-finite state")
+                        elif not res[k]["converged"]:
+                            self._finish(req, error="corrector did not converge (|F| = %.3e after %d halvings)"
+                                         % (res[k]["residual"], res[k]["halvings"]))
+                        else:
+                            self._finish(req, result={"X": Xh[k].copy(), "Ra": float(Rah[k]),
+                                                      "X_dot": Xdh[k].copy(), **res[k]})
                 except Exception as e:              # noqa: BLE001 - report per request
                     for req in batch:
                         self._finish(req, error=repr(e))
@@ -508,8 +580,18 @@ def run_workload(server, workload):
 
 
 def latency_report(reqs):
-    lat = np.array([r.latency for r in reqs if r.latency is not None and r.error is None])
+    """p50/p99/mean/max of the latency of the completed requests, and of its two parts: queue time
+    (submission to first device work) and device time (first device work to completion)."""
+    ok = [r for r in reqs if r.latency is not None and r.error is None]
+    lat = np.array([r.latency for r in ok])
     if lat.size == 0:
         return {}
-    return {"n": int(lat.size), "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
-            "mean_ms": float(lat.mean() * 1e3), "max_ms": float(lat.max() * 1e3)}
+    out = {"n": int(lat.size), "p50_ms": float(np.percentile(lat, 50) * 1e3),
+           "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3),
+           "max_ms": float(lat.max() * 1e3)}
+    for name in ("queue", "device"):
+        v = np.array([getattr(r, name + "_time") for r in ok if getattr(r, name + "_time") is not None])
+        if v.size:
+            out[name + "_p50_ms"] = float(np.percentile(v, 50) * 1e3)
+            out[name + "_p99_ms"] = float(np.percentile(v, 99) * 1e3)
+    return out

@@ -13,8 +13,8 @@ shims, so that the reference's own source runs unmodified:
                                diagnostics can be read back;
 * ``np.RankWarning`` / ``np.trapz`` -> numpy-2 aliases (``Matrix_Operators.py:6``, ``Main.py:9,129``).
 
-Run:  python tests/golden/make_golden.py [REF_DIR]
-It writes small ``.npz`` fixtures beside this script.  They are inputs/outputs of the reference's own
+Run:  python tests/golden/make_golden.py REF_DIR [--only-<case>]
+(or with REF_DIR in the environment variable SDD_REFERENCE_DIR).  It writes small ``.npz`` fixtures beside this script.  They are inputs/outputs of the reference's own
 functions on seeded synthetic states (amplitude 1e-3*exp(-k/8)*exp(-n/4), default_rng seeds below).
 """
 import os
@@ -25,7 +25,11 @@ sys.dont_write_bytecode = True      # never write __pycache__ into the (read-onl
 import numpy as np  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DIR = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF_DIR = sys.argv[1] if len(sys.argv) > 1 and not sys.argv[1].startswith("--") else \
+    os.environ.get("SDD_REFERENCE_DIR")
+if not REF_DIR:
+    sys.exit("usage: make_golden.py REF_DIR [--only-<case>]  (or set SDD_REFERENCE_DIR)")
+OPTS = [a for a in sys.argv[1:] if a.startswith("--")]
 
 
 # ----------------------------------------------------------------------------------------------
@@ -289,15 +293,95 @@ def transform_case():
     print("wrote transforms")
 
 
+def trajectory_c2_case():
+    """The production-size plain configuration: N_r = 30, N_fm = 256, dt = 5e-4, 10^4 steps of the reference's
+    own _Time_Step (Main.py:228-329) from the seed-1234 state.  Kept small: the seed, the saved states after
+    steps 1, 5001 and 9001 (X_DATA[0], [5], [9]), the final state, and every 10th entry of the per-step
+    Norm / KE / Nu_T / Nu_S series."""
+    d, Pr, Tau, Ra, Ra_s = (PARAMS[k] for k in ("d", "Pr", "Tau", "Ra", "Ra_s"))
+    N_r, N_fm, dt, n_steps = 30, 256, 5e-4, 10000
+    nr = N_r - 1
+    X0 = seeded_state(N_fm, nr, 1234)
+    fname = "golden_c2.h5"
+    assert int(n_steps * dt / dt) == n_steps
+    XN = Main._Time_Step(X0.copy(), Ra, Ra_s, Tau, Pr, d, N_fm, N_r, False, save_filename=fname,
+                         start_time=0, Total_time=n_steps * dt, dt=dt, linear=False, Verbose=False)
+    f = H5.File.files[fname]
+    XD = np.asarray(f["Checkpoints"]["X_DATA"])
+    sd = f["Scalar_Data"]
+    out = dict(X_DATA=XD[[0, 5, 9]], saved_steps=np.array([1, 5001, 9001]), X_final=XN,
+               Norm=np.asarray(sd["Norm"])[::10], KE=np.asarray(sd["KE"])[::10],
+               NuT=np.asarray(sd["Nu_T"])[::10], NuS=np.asarray(sd["Nu_S"])[::10],
+               params=np.array([N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, 0.0, n_steps, 1234]))
+    np.savez(os.path.join(HERE, "traj_c2.npz"), **out)
+    print("wrote traj_c2", XD.shape, "|X_N| %.6e" % np.linalg.norm(XN))
+
+
+def layout_case():
+    """Matrix_Operators.py:529-627 Vecs_to_X / X_to_Vecs on seeded fields, symmetric and not."""
+    rng = np.random.default_rng(51)
+    N_fm, nr = 10, 7
+    PSI, T, C = (rng.standard_normal((nr, N_fm)) for _ in range(3))
+    out = dict(PSI=PSI, T=T, C=C)
+    for sym in (False, True):
+        X = MO.Vecs_to_X(PSI, T, C, N_fm, nr, sym)
+        out[f"X_{int(sym)}"] = X
+        P2, T2, C2 = MO.X_to_Vecs(X, N_fm, nr, sym)
+        out[f"PSI_{int(sym)}"], out[f"T_{int(sym)}"], out[f"C_{int(sym)}"] = P2, T2, C2
+    Xr = rng.standard_normal(3 * N_fm * nr)
+    out["X_raw"] = Xr
+    for sym in (False, True):
+        P2, T2, C2 = MO.X_to_Vecs(Xr, N_fm, nr, sym)
+        out[f"PSI_raw_{int(sym)}"], out[f"T_raw_{int(sym)}"], out[f"C_raw_{int(sym)}"] = P2, T2, C2
+    np.savez(os.path.join(HERE, "layout.npz"), **out)
+    print("wrote layout")
+
+
+def continuation_run_case(n_steps=11):
+    """The reference's branch-following loop _Continuation (Main.py:958-1045) as written, from the
+    steady convective state of cont_tau1.npz (N_r = 16, N_fm = 16, Tau = 1, Ra_T = 9000): it starts at
+    ds = 0.01 with pseudo-arclength steps (_ContinC), doubling ds after each step that needs <= 4 corrector
+    iterations, and switches to natural-parameter Newton steps (_NewtonC, ds doubling up to ds_max = 10) once
+    ds > 1.  The record it writes every 5 iterations (Checkpoints/*, Bifurcation/*) comes back through the
+    fake h5py File; n_steps = 11 so that the last write holds all 11 iterations."""
+    Z = np.load(os.path.join(HERE, "cont_tau1.npz"))
+    N_r, N_fm, _, d, Pr, Tau, Ra0, Ra_s, _ = Z["params"]
+    kwargs = {"Ra": float(Ra0), "Ra_s": float(Ra_s), "Tau": float(Tau), "Pr": float(Pr), "d": float(d),
+              "N_fm": int(N_fm), "N_r": int(N_r), "symmetric": False}
+    Y = np.hstack((Z["X_steady"], float(Ra0)))
+    fname = "golden_contrun.h5"
+    Main._Continuation(fname, n_steps, 1.0, Y, **kwargs)
+    f = H5.File.files[fname]
+    bif, chk = f["Bifurcation"], f["Checkpoints"]
+    out = {k: np.asarray(bif[k]) for k in ("Ra", "Ra_dot", "Norm", "KE", "NuT", "NuS")}
+    out["n_folds"] = np.array(len(bif["Y_FOLD"]))
+    out["X_DATA"] = np.asarray(chk["X_DATA"])
+    out["Ra_DATA"] = np.asarray(chk["Ra_DATA"])
+    out["Y0"] = Y
+    out["params"] = Z["params"]
+    out["n_steps"] = np.array(n_steps)
+    np.savez(os.path.join(HERE, "contrun_tau1.npz"), **out)
+    print("wrote contrun", "Ra:", np.array2string(out["Ra"], precision=6))
+
+
 if __name__ == "__main__":
-    if len(sys.argv) > 2 and sys.argv[2] == "--only-eigen":
+    if "--only-eigen" in OPTS:
         eigen_case()
         sys.exit(0)
-    if len(sys.argv) > 2 and sys.argv[2] == "--only-interp":
+    if "--only-interp" in OPTS:
         interp_case()
         sys.exit(0)
-    if len(sys.argv) > 2 and sys.argv[2] == "--only-continuation":
+    if "--only-continuation" in OPTS:
         continuation_case("tau1", N_r=16, N_fm=16, Ra0=9000.0, Tau=1.0, ds=50.0, n_steps=40000, dt_ts=5e-3, seed=31)
+        sys.exit(0)
+    if "--only-continuation-run" in OPTS:
+        continuation_run_case()
+        sys.exit(0)
+    if "--only-c2" in OPTS:
+        trajectory_c2_case()
+        sys.exit(0)
+    if "--only-layout" in OPTS:
+        layout_case()
         sys.exit(0)
     # the reference's own known-answer tests must pass before anything is recorded (Transforms.py:132-374)
     for k in range(4):
@@ -318,3 +402,6 @@ if __name__ == "__main__":
     trajectory_case("sym_lin", N_r=8, N_fm=10, dt=5e-3, n_steps=100, symmetric=True, seed=22, linear=True)
     continuation_case("tau1", N_r=16, N_fm=16, Ra0=9000.0, Tau=1.0, ds=50.0, n_steps=40000, dt_ts=5e-3, seed=31)
     interp_case()
+    layout_case()
+    continuation_run_case()
+    trajectory_c2_case()

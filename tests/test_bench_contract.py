@@ -20,6 +20,8 @@ def test_reference_arm_prints_one_contract_line():
     assert d["metric"] == "time-steps/s" and d["unit"] == "time-steps/s" and d["higher_is_better"] is True
     assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 3 and d["n_gpus"] == 1
     assert d["config"]["N_r"] == 30 and d["config"]["N_theta"] == 256
+    # the same bench step as the GPU arm (100 IMEX steps of the shell)
+    assert d["config"]["steps_per_bench_step"] == 100
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
     e = d["e2e"]

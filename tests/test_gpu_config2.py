@@ -1,0 +1,114 @@
+"""The production-size plain configuration end to end: one shell N_r = 30, N_theta = 256, d = 2, Pr = 1,
+Tau = 0.01, Ra_T = 8000, Ra_S = 500, dt = 5e-4, 10^4 IMEX steps from the seed-1234 state, then
+Newton-GMRES(50) with the dt = 1 operators to |F|_2 <= 1e-10.
+
+The trajectory is compared with the reference's own 10^4-step _Time_Step run (tests/golden/traj_c2.npz,
+made by tests/golden/make_golden.py): the saved states after steps 1, 5001 and 9001 and the final state to
+1e-11 relative, and the per-step Norm / KE / Nu series.  The Newton solutions are compared with the oracle's
+Newton-GMRES from the same start: from the time-stepped state (which converges to the conduction state
+X = 0: absolute distance) and from a nontrivial start (a steady convective state interpolated to a larger
+shape and perturbed, which converges to a convective state of norm ~3): relative distance <= 1e-10.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel
+from oracle import sdd_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _c2():
+    Z = load_golden("traj_c2.npz")
+    N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, sym, ns, seed = Z["params"]
+    return Z, int(N_r), int(N_fm), float(dt), float(d), float(Pr), float(Tau), float(Ra), float(Ra_s), int(ns), int(seed)
+
+
+@pytest.fixture(scope="module")
+def c2_final(cuda):
+    """The 10^4-step state of Plan.step (the benchmarked path: captured step graphs), checked on the way."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    Z, N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, ns, seed = _c2()
+    p = Plan(N_fm, N_r, d, dt, Pr, Tau)
+    X = torch.from_numpy(O.seeded_state(N_fm, N_r - 1, seed)).cuda().reshape(1, -1)
+    done, errs = 0, []
+    for target, ref in zip(Z["saved_steps"], Z["X_DATA"]):
+        X = p.step(X, Ra, Ra_s, nsteps=int(target) - done)
+        done = int(target)
+        errs.append(rel(X.cpu().numpy().ravel(), ref))
+    X = p.step(X, Ra, Ra_s, nsteps=ns - done)
+    errs.append(rel(X.cpu().numpy().ravel(), Z["X_final"]))
+    return X, errs
+
+
+def test_c2_trajectory_matches_reference(c2_final):
+    X, errs = c2_final
+    print("relative error vs the reference after steps 1, 5001, 9001, 10000:", ["%.2e" % e for e in errs])
+    assert max(errs) <= 1e-11, errs
+
+
+def test_c2_time_step_dropin_series_match_reference(cuda):
+    """Main._Time_Step (per-step diagnostics on the device) for the same 10^4 steps."""
+    from spectraldoublediffusiveconvection_gb300 import Main
+    Z, N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, ns, seed = _c2()
+    X0 = O.seeded_state(N_fm, N_r - 1, seed)
+    XN = Main._Time_Step(X0, Ra, Ra_s, Tau, Pr, d, N_fm, N_r, False, save_filename=None, Total_time=ns * dt, dt=dt)
+    assert rel(XN, Z["X_final"]) <= 1e-11
+    rec = Main._Time_Step.last_record
+    s = rec["series"][::10]
+    for q, key in enumerate(("Norm", "KE", "NuT", "NuS")):
+        ref = Z[key]
+        n = len(ref)
+        assert np.abs(s[:n, q] - ref).max() <= 1e-10 * np.abs(ref).max(), key
+
+
+def test_c2_newton_from_trajectory_matches_oracle(cuda, c2_final):
+    """Newton from the 10^4-step state: the GPU's and the oracle's solutions (both at |F| <= 1e-10) are the
+    conduction state to within 1e-10 of each other, and the oracle's residual at the GPU's solution is
+    <= 1.5e-10."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    Z, N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, ns, seed = _c2()
+    Xs, _ = c2_final
+    X0 = Xs.cpu().numpy().ravel()
+    p1 = Plan(N_fm, N_r, d, 1.0, Pr, Tau)
+    Xg = Xs.clone()
+    r = p1.newton(Xg, Ra, Ra_s, tol=1e-10, restart=50)[0]
+    assert r["converged"] and r["residual"] <= 1e-10, r
+    ops1 = O.Operators(N_fm, N_r, d, 1.0, Pr, Tau)
+    Xo, hist, mv = O.newton_gmres(ops1, X0, Ra, Ra_s, False, tol=1e-10, restart=50)
+    assert hist[-1] <= 1e-10
+    xg = Xg.cpu().numpy().ravel()
+    print("GPU: %d Newton iterations, %d products; oracle: %d iterations, %d products; |Xg - Xo| = %.2e"
+          % (r["newton_iters"], r["matvecs"], len(hist) - 1, mv, np.linalg.norm(xg - Xo)))
+    assert np.linalg.norm(xg - Xo) <= 1e-10
+    assert np.linalg.norm(O.PFX(ops1, xg, Ra, Ra_s, False)) <= 1.5e-10
+    assert abs(r["newton_iters"] - (len(hist) - 1)) <= 1
+
+
+@pytest.mark.parametrize("N_r,N_fm", [(24, 32), (30, 64)])
+def test_newton_from_nontrivial_start_matches_oracle(cuda, N_r, N_fm):
+    """A steady convective state of the reference (tests/golden/cont_tau1.npz: N_r = 16, N_fm = 16, Tau = 1,
+    Ra_T = 9000) interpolated to a larger shape (INTERP_RADIAL / INTERP_THETAS) and perturbed: Newton
+    converges to a convective state (|X| ~ 3), not to X = 0.  The GPU's and the oracle's solutions from the
+    same start agree to 1e-10 relative (two oracle solves at 1e-10 and 1e-12 agree to ~1e-12)."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    G = load_golden("cont_tau1.npz")
+    _, _, _, d, Pr, Tau, Ra, Ra_s, _ = G["params"]
+    X = O.INTERP_THETAS(N_fm, 16, O.INTERP_RADIAL(N_r, 16, G["X_steady"], d))
+    rng = np.random.default_rng(5)
+    X = X + 1e-3 * np.linalg.norm(X) / np.sqrt(X.size) * rng.standard_normal(X.size)
+    ops1 = O.Operators(N_fm, N_r, d, 1.0, Pr, Tau)
+    Xo, hist, mv = O.newton_gmres(ops1, X, Ra, Ra_s, False, tol=1e-11, restart=50)
+    assert hist[-1] <= 1e-11 and np.linalg.norm(Xo) > 1.0
+    p1 = Plan(N_fm, N_r, d, 1.0, Pr, Tau)
+    Xg = torch.from_numpy(X.copy()).cuda().reshape(1, -1)
+    r = p1.newton(Xg, Ra, Ra_s, tol=1e-11, restart=50)[0]
+    assert r["converged"] and r["residual"] <= 1e-11, r
+    xg = Xg.cpu().numpy().ravel()
+    e = rel(xg, Xo)
+    print("N_r=%d N_fm=%d: |X| = %.4f, GPU %d iterations / %d products, oracle %d / %d, relative distance %.2e"
+          % (N_r, N_fm, np.linalg.norm(Xo), r["newton_iters"], r["matvecs"], len(hist) - 1, mv, e))
+    assert e <= 1e-10
+    assert np.linalg.norm(O.PFX(ops1, xg, Ra, Ra_s, False)) <= 1.5e-11

@@ -81,3 +81,35 @@ def test_main_contin_and_continuation_dropins(cuda):
     kw2 = {k: v for k, v in kw.items() if k != "Ra"}
     R = Main._Continuation(None, 3, 1.0, Y0, Ra=Ra0, **kw2)
     assert len(R.Ra) == 3 and R.Ra[-1] > Ra0
+
+
+def test_continuation_run_matches_reference_run(cuda):
+    """Main._Continuation (Main.py:958-1045) against 11 iterations of the reference's own loop from the same
+    steady state (tests/golden/contrun_tau1.npz): 7 pseudo-arclength steps with ds doubling 0.01 -> 1.28, the
+    switch to natural-parameter Newton steps once ds > 1, and ds doubling up to ds_max = 10.  The Ra
+    sequence, the scalar records, the checkpointed states (iterations 0, 5, 10) and the tangent's parameter
+    component carried through the natural steps all agree at the reference's own accuracy: its correctors and
+    Newton stop on a relative step of 1e-8, this build's on an absolute residual of 1e-8, so states agree to
+    about 1e-7 and the parameter to 1e-9 of its increments (checked at 1e-6 and 1e-6)."""
+    from spectraldoublediffusiveconvection_gb300 import Main
+    Z = load_golden("contrun_tau1.npz")
+    N_r, N_fm, _, d, Pr, Tau, Ra0, Ra_s, _ = Z["params"]
+    kw = dict(Ra=float(Ra0), Ra_s=float(Ra_s), Tau=float(Tau), Pr=float(Pr), d=float(d), N_fm=int(N_fm),
+              N_r=int(N_r), symmetric=False)
+    R = Main._Continuation(None, int(Z["n_steps"]), 1.0, Z["Y0"], **kw)
+    Ra = np.array(R.Ra)
+    assert Ra.shape == Z["Ra"].shape
+    # arclength steps: Ra to 1e-6 of its distance from Ra0 (9000.01 .. 9001.27) and 1e-9 relative overall
+    assert np.all(np.abs(Ra - Z["Ra"]) <= 1e-6 * np.abs(Z["Ra"] - Ra0) + 1e-9 * Ra0), (Ra, Z["Ra"])
+    # then natural-parameter steps of ds = 1.28, 2.56, 5.12 and ds_max = 10
+    assert np.allclose(np.diff(Ra)[-4:], [1.28, 2.56, 5.12, 10.0], rtol=0, atol=1e-9)
+    assert np.allclose(R.Ra_dot, Z["Ra_dot"], rtol=1e-6, atol=0)
+    for k in ("Norm", "KE", "NuT", "NuS"):
+        assert np.allclose(getattr(R, k), Z[k], rtol=1e-6, atol=0), k
+    assert len(R.Y_FOLD) == int(Z["n_folds"])
+    assert len(R.X_DATA) == len(Z["X_DATA"])
+    for a, b in zip(R.X_DATA, Z["X_DATA"]):
+        assert rel(a, b) <= 1e-6
+    assert np.allclose(R.Ra_DATA, Z["Ra_DATA"], rtol=1e-12, atol=1e-6)
+    # the state stays on the device: the record's last branch point is a CUDA tensor
+    assert R.X.is_cuda and rel(R.X.cpu().numpy(), R.X_DATA[-1]) == 0.0

@@ -259,3 +259,21 @@ def test_device_diagnostics_against_oracle(cuda, N_r, N_fm, sym):
         assert abs(out[i, 1] - ref[1]) <= 1e-11 * abs(ref[1])
         assert abs(out[i, 2] - ref[2]) <= 1e-11 * (abs(ref[2]) + 1e-3)
         assert abs(out[i, 3] - ref[3]) <= 1e-11 * (abs(ref[3]) + 1e-3)
+
+
+@pytest.mark.parametrize("tag", OPS_CASES)
+def test_main_diagnostics_dropins_match_reference(cuda, tag):
+    """Main.Kinetic_Energy / Main.Nusselt (Main.py:41-134) run on the device and match the reference's values
+    on the golden states; Nusselt's wall-consistency check raises ValueError like the reference's."""
+    from spectraldoublediffusiveconvection_gb300 import Main
+    Z, N_r, N_fm, dt, d, Pr, Tau, Ra, Ra_s, sym = _case(tag)
+    nr = N_r - 1
+    N = N_fm * nr
+    X, D, R = Z["X"], Z["D"], Z["R"]
+    assert abs(Main.Kinetic_Energy(X, R, D, N_fm, nr, sym) - float(Z["KE"])) <= 1e-11 * abs(float(Z["KE"]))
+    for key, blk in (("NuT", X[N:2 * N]), ("NuS", X[2 * N:])):
+        ref = float(Z[key])
+        assert abs(Main.Nusselt(blk, d, R, D, N_fm, nr, check=False) - ref) <= 1e-11 * (abs(ref) + 1e-3)
+    # a seeded (non-steady) temperature field has different fluxes at the two walls
+    with pytest.raises(ValueError):
+        Main.Nusselt(X[N:2 * N] * 1e3, d, R, D, N_fm, nr, check=True)

@@ -70,3 +70,48 @@ def test_failed_worker_fails_its_requests_and_drain_returns():
     assert "device lost" in a.error and "device lost" in b.error
     assert srv.drain(timeout=1.0) is False and srv.worker_error
     assert srv.used == 0
+
+
+def test_cancel_queued_and_waiting_requests():
+    """Server.cancel on the host: a request still in the queue is retired at once without touching the
+    budget; an admitted request waiting for its batch (continuation) or its group's boundary (integration)
+    returns its bytes; a request in flight is only marked (its worker retires it)."""
+    serve, srv = _server(10 ** 9)
+    q = serve.Request("integrate", 20, 64, 9000.0)
+    srv.submit(q)
+    assert srv.cancel(q) is True
+    assert q.done.is_set() and q.error == "cancelled" and not srv._pending["integrate"] and srv.used == 0
+    assert srv.cancel(q) is False                      # already completed
+    a = serve.Request("continue", 20, 64, 9000.0)
+    b = serve.Request("integrate", 24, 128, 9000.0)
+    srv.submit(a)
+    srv.submit(b)
+    assert srv._admit_kind("continue") == [a] and srv._admit_kind("integrate") == [b]
+    srv._waiting.setdefault(a.shape, []).append(a)
+    srv._int_joining.setdefault(b.shape, []).append(b)
+    assert srv.used == srv.request_bytes(a) + srv.request_bytes(b) and srv._active == 2
+    assert srv.cancel(a) and srv.cancel(b)
+    assert a.error == b.error == "cancelled" and a.done.is_set() and b.done.is_set()
+    assert srv.used == 0 and srv._active == 0 and not srv._waiting[a.shape] and not srv._int_joining[b.shape]
+    c = serve.Request("integrate", 20, 64, 9000.0)
+    srv.submit(c)
+    srv._admit_kind("integrate")                       # admitted and handed to a group (in flight)
+    assert srv.cancel(c) is True and c.cancelled and not c.done.is_set()
+    srv._finish(c, error="cancelled")                  # what the worker does at the next boundary
+    assert srv.used == 0 and srv._active == 0
+
+
+def test_latency_report_splits_queue_and_device_time():
+    serve, _ = _server(10 ** 9)
+    reqs = []
+    for i in range(10):
+        r = serve.Request("integrate", 20, 64, 9000.0)
+        r.t_submit, r.t_start, r.t_done = 0.0, 0.01 * i, 0.01 * i + 0.1
+        reqs.append(r)
+    bad = serve.Request("integrate", 20, 64, 9000.0)
+    bad.t_submit, bad.t_start, bad.t_done, bad.error = 0.0, 0.0, 5.0, "non-finite state"
+    rep = serve.latency_report(reqs + [bad])
+    assert rep["n"] == 10
+    assert rep["device_p50_ms"] == pytest.approx(100.0) and rep["device_p99_ms"] == pytest.approx(100.0)
+    assert rep["queue_p50_ms"] == pytest.approx(45.0)
+    assert rep["max_ms"] == pytest.approx(190.0)

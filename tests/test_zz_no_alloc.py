@@ -52,3 +52,28 @@ def test_noalloc_rejects_batches_beyond_its_scratch(cuda):
     X = torch.zeros((too_many, 3 * N_fm * (N_r - 1)), dtype=torch.float64, device="cuda")
     F = torch.empty_like(X)
     assert _noalloc(p, X, F) == _lib.SDD_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("sym", [False, True])
+def test_noalloc_at_the_largest_accepted_batch(cuda, sym):
+    """batch * 4 * N_fm * nr equal to (at most one shell below) the scratch size: the last shell's outputs
+    sit at the end of the fixed array, where a wrong stride would run past it."""
+    from spectraldoublediffusiveconvection_gb300 import _lib
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    N_fm, N_r = 64, 20
+    nr = N_r - 1
+    p = Plan(N_fm, N_r, 2.0, 1e-3, 1.0, 0.01, symmetric=sym)
+    B = _lib.SDD_NOALLOC_SCRATCH_DOUBLES // (4 * N_fm * nr)            # 215 shells
+    assert (B + 1) * 4 * N_fm * nr > _lib.SDD_NOALLOC_SCRATCH_DOUBLES
+    seeds = [O.seeded_state(N_fm, nr, s, sym) for s in range(4)]
+    X = torch.from_numpy(np.stack([seeds[b % 4] * (1.0 + 0.01 * b) for b in range(B)])).cuda()
+    ref = p.nlin_fx(X)
+    for _ in range(2):
+        F = torch.full_like(X, float("nan"))
+        assert _noalloc(p, X, F) == _lib.SDD_OK
+        torch.cuda.synchronize()
+        for b in (0, B // 2, B - 1):
+            err = float(torch.linalg.norm(F[b] - ref[b]) / torch.linalg.norm(ref[b]))
+            assert err <= 1e-12, (b, err)
+        assert bool(torch.isfinite(F).all())
