@@ -300,6 +300,36 @@ def bench_batched(device, precision, steps=1000, steps_per_launch=10, n_shells=6
             "tuning_chain_layout_fx_split": tune, "finite": finite}
 
 
+def bench_batched_plain_alone(device, steps=100):
+    """The plain FP64 path on the batched workload's shells one at a time (each shell's own plan, the
+    automatic kernel choices of a single shell): shell-steps/s of the whole set stepped sequentially, the
+    same-workload denominator of the batched forms."""
+    import torch
+    from spectraldoublediffusiveconvection_gb300.batch import config4_shells
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    from spectraldoublediffusiveconvection_gb300.seeds import seeded_state
+    shells = config4_shells(64, seed=1234)
+    plans, total = {}, 0.0
+    stream = torch.cuda.current_stream(device)
+    for i, sh in enumerate(shells):
+        key = (sh["N_theta"], sh["N_r"])
+        if key not in plans:
+            plans[key] = Plan(sh["N_theta"], sh["N_r"], 2.0, 1e-3, 1.0, 0.01, device=device)
+        p = plans[key]
+        X = torch.from_numpy(seeded_state(sh["N_theta"], sh["N_r"] - 1, 1234 + i)).to(device).reshape(1, -1)
+        Y = p.step(X, sh["Ra"], 500.0, nsteps=steps)          # warm-up (graphs, workspace)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        p.step(Y, sh["Ra"], 500.0, nsteps=steps, out=X)
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        total += e0.elapsed_time(e1) * 1e-3
+    for p in plans.values():
+        p.close()
+    return {"shell_steps_per_s": 64 * steps / total, "steps_per_shell": steps,
+            "how": "each of the 64 shells alone on the plain FP64 path, %d steps, one after the other" % steps}
+
+
 def _cpu_batch_worker(job):
     """One host process of the batched CPU baseline: IMEX steps of its shells of the 64-shell workload with
     the oracle, round robin, for `seconds`; returns (shell-steps, seconds)."""
@@ -615,6 +645,17 @@ def bench_gb300(args):
         rb = planm.newton(Xb, Rab, Ras, tol=1e-10, restart=50, gmres_rtol=1e-4, max_newton=20, mixed_matvec=2)
         torch.cuda.synchronize()
         tb = time.perf_counter() - t0
+        # the plain FP64 path on the same problems: a sample of 8 of the 64 shells solved one at a time with
+        # FP64 Jacobian products (the single-shell automatic kernel choices)
+        sample = list(range(0, nb, nb // 8))
+        Xs = Xb0[sample].clone()
+        plan1.newton(Xs[0:1].clone(), Rab[0:1], Ras, tol=1e-10, restart=50, max_newton=1)      # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rp = [plan1.newton(Xs[i:i + 1], Rab[sample[i]:sample[i] + 1], Ras, tol=1e-10, restart=50, gmres_rtol=1e-4,
+                           max_newton=20)[0] for i in range(len(sample))]
+        torch.cuda.synchronize()
+        tp = time.perf_counter() - t0
         n_st = 3 * M * nr
         # per Jacobian product and shell: the FP64 chains (8 M nr^2) and one classical Gram-Schmidt pass
         # against on average m/2 = 25 basis vectors (4 * 25 * n); every shell counted for every product (the
@@ -624,6 +665,12 @@ def bench_gb300(args):
                              "converged": sum(r["converged"] for r in rb),
                              "max_residual": max(r["residual"] for r in rb), "matvecs": rb[0]["matvecs"],
                              "vs_plain_single_shell": (nb / tb) / (1.0 / tn),
+                             "plain_same_workload": {"solves_per_s": len(sample) / tp, "shells": len(sample),
+                                                     "converged": sum(r["converged"] for r in rp),
+                                                     "matvecs_mean": sum(r["matvecs"] for r in rp) / len(rp),
+                                                     "how": "8 of the 64 problems, one at a time, FP64 plan "
+                                                            "and FP64 Jacobian products"},
+                             "vs_plain_same_workload": (nb / tb) / (len(sample) / tp),
                              "roofline": {"bound": "fp64", "achieved": f64_b / tb / 1e12, "peak": fp64_peak_tf,
                                           "unit": "TFLOP/s", "frac": f64_b / tb / 1e12 / fp64_peak_tf,
                                           "note": "FP64 chains + Gram-Schmidt flops of every product of every "
@@ -679,9 +726,12 @@ def bench_gb300(args):
         bm = bench_batched(device, "mixed", fp64_peak=fp64_peak_tf)
         bd = bench_batched(device, "fp64", fp64_peak=fp64_peak_tf)
         plain = value / ws
+        alone = bench_batched_plain_alone(device)
         batched = {"mixed": bm, "fp64": bd,
                    "mixed_vs_plain_single_shell": bm["shell_steps_per_s"] / plain,
                    "fp64_vs_plain_single_shell": bd["shell_steps_per_s"] / plain,
+                   "plain_same_shells_alone": alone,
+                   "mixed_vs_plain_same_shells": bm["shell_steps_per_s"] / alone["shell_steps_per_s"],
                    "cpu_baseline": None if args.no_cpu else bench_batched_cpu(),
                    "workload": "64 shells, N_r in {20,24,30,36}, N_theta in {64,128,256,384}, Ra_T ~ U[6000,12000],"
                                " Ra_S=500, Pr=1, Tau=0.01, dt=1e-3, 1000 steps each (seed 1234)"}

@@ -105,6 +105,14 @@ int sdd_plan_set_chain_layout(sdd_plan* plan, int layout);
 /* The layout (1-5) a step of `batch` shells runs under the current setting, with its chunk length and
  * chunks per chain (0 and 1 when not chunked). */
 int sdd_plan_chain_choice(const sdd_plan* plan, int batch, int* layout, int* kc, int* nch);
+/* Mixed plans: the FP32 radial contractions of the nonlinear term (Derivatives, Matrix_Operators.py:698-729)
+ * on the tensor cores (1, the default: 3xTF32 split products with tcgen05.mma, FP32-level accuracy) or as FP32
+ * multiply-adds on the CUDA cores (0).  SDD_ERR_UNSUPPORTED for FP64 plans.  No counterpart in the
+ * reference. */
+int sdd_plan_set_tensor_cores(sdd_plan* plan, int on);
+/* 1 in *timed_out if a tensor-core kernel of this plan gave up waiting for its matrix products (its outputs
+ * were then NaN); 0 otherwise.  Synchronous. */
+int sdd_plan_tensor_core_status(const sdd_plan* plan, int* timed_out);
 /* Nonlinear-term kernel choice: 0 automatic (split while the fused kernel's nr*batch CTAs would fill
  * under half the SMs), 1 the fused row kernel (one CTA per radial row), 2 split (7 CTAs per radial row:
  * five paired inverse transforms, then two paired forward transforms).  Results are identical bit for
@@ -221,6 +229,15 @@ int sdd_contin_step(sdd_plan* plan, int batch, double* X, double* Ra, const doub
 #define SDD_NOALLOC_SCRATCH_DOUBLES (1 << 20)
 int sdd_nlin_fx_noalloc(sdd_plan* plan, int batch, const double* X, double* F, void* stream);
 
+/* ---- radial contractions on the tensor cores ------------------------------------------------- */
+/* The four radial contractions of Derivatives (Matrix_Operators.py:698-729: Dr psi_k, (D^2/r^2) psi_k
+ * (A2_SINE_R2 :498), Dr T_k, Dr S_k) of every mode of every shell, as the mixed plans' nonlinear term forms
+ * them: 3xTF32 products on the tensor cores (tcgen05.mma, TMEM accumulators), FP32-level accuracy.
+ * X32: batch x 3*N_fm*nr floats (the state in FP32, reference layout); out: batch x 4*nr*N_fm floats,
+ * out[shell][op][n][k] (op 0..3 in the order above, radial row n, mode k contiguous).  Rows outside the
+ * symmetric subspace give zeros.  Mixed plans only (SDD_ERR_UNSUPPORTED otherwise). */
+int sdd_deriv_tc(sdd_plan* plan, int batch, const float* X32, float* out, void* stream);
+
 /* ---- instrumentation (no counterpart in the reference) ---------------------------------------- */
 /* Runs nsteps steps like sdd_step (launched one by one, not from graphs) with CUDA events between the
  * three stages of each step and adds the elapsed milliseconds to ms[0] (nonlinear term), ms[1]
@@ -246,7 +263,8 @@ int sdd_step_diag(sdd_plan* plan, int batch, const double* Ra, const double* Ra_
 #define SDD_K_CHAIN 6        /* the chains (whole, or the concurrent chunks) */
 #define SDD_K_CHAIN_CARRY 7  /* chunked chains: carried states */
 #define SDD_K_MODE_FIX 8     /* chunked chains: correction per mode */
-#define SDD_NUM_KERNELS 9
+#define SDD_K_DERIV_TC 9     /* mixed plans: radial contractions on the tensor cores (3xTF32) */
+#define SDD_NUM_KERNELS 10
 const char* sdd_kernel_name(int id);
 /* Like sdd_step_profile, but with an event after every kernel launch: adds the elapsed milliseconds of
  * each kernel to ms[id] and counts its launches in launches[id] (arrays of SDD_NUM_KERNELS). */

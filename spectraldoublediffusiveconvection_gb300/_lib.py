@@ -81,6 +81,8 @@ SIGNATURES = [
     ("sdd_plan_reserve", _I, [_VP, _I]),
     ("sdd_plan_set_chain_layout", _I, [_VP, _I]),
     ("sdd_plan_set_fx_split", _I, [_VP, _I]),
+    ("sdd_plan_set_tensor_cores", _I, [_VP, _I]),
+    ("sdd_plan_tensor_core_status", _I, [_VP, ctypes.POINTER(_I)]),
     ("sdd_plan_chain_choice", _I, [_VP, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("sdd_plan_base_cache_elems", ctypes.c_size_t, [_VP]),
     ("sdd_nlin_fx", _I, [_VP, _I, _VP, _VP, _VP, _VP]),
@@ -97,6 +99,7 @@ SIGNATURES = [
                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ContinOpts),
                              ctypes.POINTER(ContinResult), _VP]),
     ("sdd_nlin_fx_noalloc", _I, [_VP, _I, _VP, _VP, _VP]),
+    ("sdd_deriv_tc", _I, [_VP, _I, _VP, _VP, _VP]),
     ("sdd_step_profile", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, ctypes.POINTER(ctypes.c_double), _VP]),
     ("sdd_diagnostics", _I, [_VP, _I, _VP, _VP, _VP]),
     ("sdd_step_diag", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, _I, _VP, _VP]),

@@ -127,6 +127,11 @@ struct sdd_plan {
   // mixed plans: FP32 copies for the FP32 right-hand sides and h matvecs of Newton's Jacobian products
   float* D2s32;
   float* Linv32[3];                 // LinvA4, LinvT, LinvS in their transposed layout
+  // mixed plans: the radial contractions on the tensor cores (k_deriv_tc): split operator tiles
+  float* tcB;                       // [hi | lo] of [Dr ; D^2/r^2], tensor-core layout (build_tc_operator)
+  int tcKP, tcNP;                   // nr rounded up to 8
+  int use_tc;                       // 1: k_deriv_tc forms the FP32 contractions (sdd_plan_set_tensor_cores)
+  int* tc_err;                      // device word set by a tensor-core kernel whose wait timed out
   // workspace
   int ws_batch;
   double* out4;     // [B][4][M][nr]
@@ -290,6 +295,7 @@ static void free_plan(sdd_plan* p) {
     for (const double* x : t) cudaFree(const_cast<double*>(x));
   }
   cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232); cudaFree(p->D2s32);
+  cudaFree(p->tcB); cudaFree(p->tc_err);
   for (float* x : p->Linv32) cudaFree(x);
   cudaFree(p->x32[0]); cudaFree(p->x32[1]); cudaFree(p->q32); cudaFree(p->g32);
   cudaFree(p->base_tmp);
@@ -555,6 +561,22 @@ int sdd_plan_create(const sdd_plan_desc* d, sdd_plan** out) {
     return st;
   }
   (void)nm;
+  if (p->prec == SDD_PREC_MIXED) {   // 3xTF32 operator tiles of the tensor-core contractions
+    p->tcKP = p->tcNP = (nr + 7) / 8 * 8;
+    std::vector<float> tb((size_t)2 * 2 * p->tcNP * p->tcKP);
+    build_tc_operator(d->Dr, d->D2_r2, nr, p->tcKP, p->tcNP, tb.data());
+    cudaError_t e = cudaMalloc(&p->tcB, tb.size() * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(p->tcB, tb.data(), tb.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&p->tc_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(p->tc_err, 0, sizeof(int));
+    if (e != cudaSuccess) {
+      set_cuda_error(e);
+      cudaGetLastError();
+      free_plan(p);
+      return e == cudaErrorMemoryAllocation ? SDD_ERR_NOMEM : SDD_ERR_CUDA;
+    }
+    p->use_tc = 1;
+  }
   {  // per-step scalars of the chains (Matrix_Operators.py:1143-1159 and 1056-1083)
     std::vector<double> cA((size_t)M * 4), cT((size_t)M * 4), cS((size_t)M * 4);
     const double dA = d->Pr * d->dt, dT = d->dt, dS = d->Tau * d->dt;
@@ -622,6 +644,21 @@ int sdd_plan_set_fx_split(sdd_plan* p, int mode) {
   if (!p || mode < 0 || mode > 2) return SDD_ERR_ARG;
   if (p->fx_split != mode) clear_step_graphs(p);
   p->fx_split = mode;
+  return SDD_OK;
+}
+
+int sdd_plan_set_tensor_cores(sdd_plan* p, int on) {
+  if (!p || on < 0 || on > 1) return SDD_ERR_ARG;
+  if (on && !p->tcB) return SDD_ERR_UNSUPPORTED;
+  if (p->use_tc != on) clear_step_graphs(p);   // the captured graphs hold the other kernels
+  p->use_tc = on;
+  return SDD_OK;
+}
+
+int sdd_plan_tensor_core_status(const sdd_plan* p, int* timed_out) {
+  if (!p || !timed_out) return SDD_ERR_ARG;
+  *timed_out = 0;
+  if (p->tc_err) SDD_CUDA(cudaMemcpy(timed_out, p->tc_err, sizeof(int), cudaMemcpyDeviceToHost));
   return SDD_OK;
 }
 
@@ -714,6 +751,12 @@ static FxArgs fx_args(const sdd_plan* p, int prec, const double* X, void* base, 
   // per shell: 4 M nr elements of the precision, then M nr doubles (the fused rhs's D2s psi)
   a.deriv = p->derivbuf;
   a.deriv_stride = (size_t)(prec == SDD_PREC_MIXED ? 6 : 5) * p->M * p->nr;
+  if (prec == SDD_PREC_MIXED && p->use_tc) {
+    a.tcB = p->tcB;
+    a.tcKP = p->tcKP;
+    a.tcNP = p->tcNP;
+    a.tc_err = p->tc_err;
+  }
   return a;
 }
 
@@ -790,13 +833,14 @@ static FixArgs fix_args(const sdd_plan* p, const double* X, const float* x32) {
 // converting X, and the one the chains write beside out for the next step (nullable).  defer: leave a
 // layout-3 chain correction pending (sdd_step); fix_in: X carries the previous step's pending correction,
 // applied by the nonlinear term's first kernel.  v32 (mixed plans, mode 1, nullable): an FP32 copy of X
-// (stride ldx); the right-hand sides and h = Linv g are then formed in FP32 (k_rhs32, k_mode_mv32), for
-// Jacobian products inside a GMRES solve whose tolerance is far above FP32 rounding.
+// (stride ldx), read by the FP32 nonlinear term instead of converting X (the same values); with v32_rhs
+// the right-hand sides and h = Linv g are then formed in FP32 as well (k_rhs32, k_mode_mv32), for Jacobian
+// products inside a GMRES solve whose tolerance is far above FP32 rounding.
 static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X, size_t ldx,
                          double* out, size_t ldo, const double* sub, size_t lds, int mode, void* base, int prec,
                          cudaStream_t s, cudaEvent_t* ev = nullptr, const float* x32_in = nullptr,
                          float* x32_out = nullptr, const int* active = nullptr, int defer = 0, int fix_in = 0,
-                         const float* v32 = nullptr) {
+                         const float* v32 = nullptr, bool v32_rhs = true) {
   RhsArgs ra = rhs_args(p, X, p->out4, Ra, Ras, p->rhs, mode == 2);
   ra.x_stride = ldx;
   ra.active = active;
@@ -814,6 +858,10 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
       fa.X32 = x32_in;
       fa.x32_stride = shell_elems(p);
     }
+    if (prec == SDD_PREC_MIXED && mode == 1 && v32) {   // the Krylov vector's FP32 copy: no conversions
+      fa.X32 = v32;
+      fa.x32_stride = ldx;
+    }
     if (prec == SDD_PREC_MIXED) fa.q32 = p->q32;
     const int fm = mode == 1 ? 1 : 0;
     fuse = fx_uses_split(fa, batch, fm);
@@ -828,7 +876,7 @@ static int apply_step_ld(sdd_plan* p, int batch, const double* Ra, const double*
     SDD_CUDA(launch_fx(fa, batch, fm, prec, s));
   }
   if (ev) SDD_CUDA(cudaEventRecord(ev[1], s));
-  const bool rhs32 = v32 && mode == 1 && prec == SDD_PREC_MIXED && !fuse && p->g32 && ra.q32;
+  const bool rhs32 = v32 && v32_rhs && mode == 1 && prec == SDD_PREC_MIXED && !fuse && p->g32 && ra.q32;
   if (rhs32) {
     ra.X32 = v32;
     ra.x32_stride = ldx;
@@ -1237,7 +1285,7 @@ extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const doub
   const bool fp32_rhs = o->mixed_matvec == 2;
   MatVec J = [&](const double* v, double* out, const int* active, const float* v32) {
     return apply_step_ld(p, B, Ra, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s, nullptr, nullptr, nullptr,
-                         active, 0, 0, fp32_rhs ? v32 : nullptr);
+                         active, 0, 0, o->mixed_matvec ? v32 : nullptr, fp32_rhs);
   };
   for (int it = 0;; ++it) {
     if ((st = apply_step_ld(p, B, Ra, Ras, X, n, p->sv_F, ld, X, n, 0, p->sv_base64, SDD_PREC_FP64, s)))
@@ -1329,12 +1377,12 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
   };
   MatVec J = [&](const double* v, double* out, const int* active, const float* v32) {
     return apply_step_ld(p, B, mu_dev, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s, nullptr, nullptr, nullptr,
-                         active, 0, 0, fp32_rhs ? v32 : nullptr);
+                         active, 0, 0, o->mixed_matvec ? v32 : nullptr, fp32_rhs);
   };
   // bordered operator DG = [[DF_X, DF_mu], [delta X_dot^T, (1-delta) mu_dot]]  (Main.py:914-915)
   MatVec DG = [&](const double* v, double* out, const int* active, const float* v32) -> int {
     int r = apply_step_ld(p, B, mu_dev, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s, nullptr, nullptr,
-                          nullptr, active, 0, 0, fp32_rhs ? v32 : nullptr);
+                          nullptr, active, 0, 0, o->mixed_matvec ? v32 : nullptr, fp32_rhs);
     if (r) return r;
     SDD_CUDA(krylov_dots(p->sv_Xd, 0, v, n, ld, 1, B, p->kv_part, p->kv_dot, 1, 0, s));
     SDD_CUDA(contin_border(v, out, n, ld, p->sv_Jmu, n, Npsi, p->kv_dot, mudot_dev, delta, B, s));
@@ -1559,7 +1607,8 @@ extern "C" int sdd_step_diag(sdd_plan* p, int batch, const double* Ra, const dou
 
 extern "C" const char* sdd_kernel_name(int id) {
   static const char* names[SDD_NUM_KERNELS] = {"k_fx_rows", "k_fx_deriv", "k_fx_grid", "k_fx_prod", "k_rhs",
-                                               "k_mode_mv(h)", "k_chain", "k_chain_carry", "k_mode_mv(fix)"};
+                                               "k_mode_mv(h)", "k_chain", "k_chain_carry", "k_mode_mv(fix)",
+                                               "k_deriv_tc"};
   return (id >= 0 && id < SDD_NUM_KERNELS) ? names[id] : "unknown";
 }
 
@@ -1628,6 +1677,26 @@ __global__ void k_fp64_fma_loop(double* out, int iters, double a, double b) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 }  // namespace sdd
+
+extern "C" int sdd_deriv_tc(sdd_plan* p, int batch, const float* X32, float* out, void* stream) {
+  if (!p || batch < 1 || !X32 || !out) return SDD_ERR_ARG;
+  if (!p->tcB) return SDD_ERR_UNSUPPORTED;
+  int dev = 0;
+  SDD_CUDA(cudaGetDevice(&dev));
+  if (dev != p->device) return SDD_ERR_ARG;
+  TcArgs t;
+  std::memset(&t, 0, sizeof(t));
+  t.M = p->M; t.nr = p->nr; t.sym = p->sym; t.KP = p->tcKP; t.NP = p->tcNP;
+  t.rows = batch * 3 * p->M;
+  t.X32 = X32;
+  t.x32_stride = shell_elems(p);
+  t.B = p->tcB;
+  t.out = out;
+  t.out_stride = (size_t)4 * p->M * p->nr;
+  t.err = p->tc_err;
+  SDD_CUDA(launch_deriv_tc(t, (cudaStream_t)stream));
+  return SDD_OK;
+}
 
 extern "C" int sdd_debug_fail_allocations(long long after) {
   g_alloc_left.store(after < 0 ? -1 : after);

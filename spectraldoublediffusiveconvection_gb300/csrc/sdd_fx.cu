@@ -164,6 +164,9 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
 
   // ---- 1. radial contractions of row n (Derivatives, :698-729) and the row values ----
   const int N = M * nr;
+  // mixed plans with tensor cores: the four contractions were formed by k_deriv_tc ([op][n][k] blocks)
+  const T* Dt = (sizeof(T) == 4 && a.deriv_t) ? reinterpret_cast<const T*>(a.deriv) + (size_t)b * a.deriv_stride
+                                              : nullptr;
   with_x<T>(a, b, [&](auto xr) {
   for (int k = tid; k < M; k += bd) {
     const size_t ps = (size_t)k * nr, ts = N + (size_t)k * nr, ss = 2 * (size_t)N + (size_t)k * nr;
@@ -171,17 +174,27 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
     const bool ts_on = !(a.sym && (k % 2 == 1));
     T dp = 0, d2 = 0, dtv = 0, dcv = 0, pn = 0, tn = 0, sn = 0;
     if (psi_on) {
-      for (int m = 0; m < nr; ++m) {
-        const T x = xr(ps + m);
-        dp = fma(opr[m], x, dp);
-        d2 = fma(opr[nr + m], x, d2);
+      if (Dt) {
+        dp = Dt[(size_t)n * M + k];
+        d2 = Dt[((size_t)nr + n) * M + k];
+      } else {
+        for (int m = 0; m < nr; ++m) {
+          const T x = xr(ps + m);
+          dp = fma(opr[m], x, dp);
+          d2 = fma(opr[nr + m], x, d2);
+        }
       }
       pn = xr(ps + n);
     }
     if (ts_on) {
-      for (int m = 0; m < nr; ++m) {
-        dtv = fma(opr[m], xr(ts + m), dtv);
-        dcv = fma(opr[m], xr(ss + m), dcv);
+      if (Dt) {
+        dtv = Dt[((size_t)2 * nr + n) * M + k];
+        dcv = Dt[((size_t)3 * nr + n) * M + k];
+      } else {
+        for (int m = 0; m < nr; ++m) {
+          dtv = fma(opr[m], xr(ts + m), dtv);
+          dcv = fma(opr[m], xr(ss + m), dcv);
+        }
       }
       tn = xr(ts + n);
       sn = xr(ss + n);
@@ -445,7 +458,8 @@ __global__ void __launch_bounds__(384) k_fx_deriv(FxArgs a, T* deriv, size_t der
   __syncthreads();
   T* D = deriv + (size_t)b * deriv_stride;
   const int nops = a.fuse_rhs ? 5 : 4;
-  for (int e = threadIdx.x; e < nops * nr; e += blockDim.x) {
+  const int op0 = a.deriv_t ? 4 : 0;    // tensor cores: only the pending correction and the FP64 block here
+  for (int e = threadIdx.x + op0 * nr; e < nops * nr; e += blockDim.x) {
     const int op = e / nr, n = e - op * nr;
     if (op < 4) {
       const T* row = ops + (op == 1 ? nr * nr : 0) + (size_t)n * nr;
@@ -520,14 +534,17 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
     const bool psi_on = !(a.sym && (k % 2 == 0));
     const bool ts_on = !(a.sym && (k % 2 == 1));
     T dp = 0, d2 = 0, dtv = 0, dcv = 0, pn = 0, tn = 0, sn = 0;
+    // k_fx_deriv writes [op][k][n]; k_deriv_tc (deriv_t) the transposed [op][n][k]
+    const size_t o0 = a.deriv_t ? (size_t)n * M + k : (size_t)k * nr + n;
+    const size_t ob = (size_t)M * nr;
     if (psi_on) {
-      dp = Dv[(size_t)k * nr + n];
-      d2 = Dv[((size_t)M + k) * nr + n];
+      dp = Dv[o0];
+      d2 = Dv[ob + o0];
       pn = xr((size_t)k * nr + n);
     }
     if (ts_on) {
-      dtv = Dv[((size_t)2 * M + k) * nr + n];
-      dcv = Dv[((size_t)3 * M + k) * nr + n];
+      dtv = Dv[2 * ob + o0];
+      dcv = Dv[3 * ob + o0];
       tn = xr(N + (size_t)k * nr + n);
       sn = xr(2 * (size_t)N + (size_t)k * nr + n);
     }
@@ -1083,12 +1100,28 @@ __global__ void __launch_bounds__(kFxThreads) k_fx_finish(FinishArgs a) {
 }
 
 // ---- launchers ---------------------------------------------------------------------------------
+// The tensor-core contractions of a mixed launch (a.deriv_t): every state row of the batch at once.
+static cudaError_t launch_tc_for(const FxArgs& a, int batch, cudaStream_t s) {
+  TcArgs t;
+  t.M = a.M; t.nr = a.nr; t.sym = a.sym; t.KP = a.tcKP; t.NP = a.tcNP;
+  t.rows = batch * 3 * a.M;
+  t.X32 = a.X32; t.x32_stride = a.x32_stride;
+  t.X = a.X; t.x_stride = a.x_stride;
+  t.active = a.active;
+  t.B = a.tcB;
+  t.out = reinterpret_cast<float*>(a.deriv);
+  t.out_stride = a.deriv_stride;
+  t.err = a.tc_err;
+  return launch_deriv_tc(t, s);
+}
+
 template <typename T, int MODE>
 static cudaError_t launch_fx_t(const FxArgs& a, int batch, cudaStream_t s) {
   const size_t smem = fx_smem_bytes(a.M, a.P, sizeof(T) == 4 ? SDD_PREC_MIXED : SDD_PREC_FP64);
   static unsigned long long done = 0;
   cudaError_t e = ensure_smem_attr(k_fx_rows<T, MODE>, &done);
   if (e != cudaSuccess) return e;
+  if (sizeof(T) == 4 && a.deriv_t && (e = launch_tc_for(a, batch, s)) != cudaSuccess) return e;
   e = launch_kernel(k_fx_rows<T, MODE>, dim3(a.nr, batch), dim3(kFxRowThreads), smem, s, a);
   ktimer_mark(SDD_K_FX_ROWS, s);
   return e;
@@ -1105,11 +1138,17 @@ static cudaError_t launch_fx_split_t(const FxArgs& a, int batch, cudaStream_t s)
     static unsigned long long done = 0;   // large nr with a pending correction can pass 48 KB
     if ((e = ensure_smem_attr(k_fx_deriv<T>, &done)) != cudaSuccess) return e;
   }
-  e = launch_kernel(k_fx_deriv<T>, dim3(a.M, batch), dim3(a.fix.on ? 384 : 256),
-                    fx_deriv_smem_bytes(a.nr, prec, a.fix.on != 0), s, a,
-                 reinterpret_cast<T*>(a.deriv), a.deriv_stride);
-  ktimer_mark(SDD_K_FX_DERIV, s);
-  if (e != cudaSuccess) return e;
+  // with tensor cores the per-mode kernel only applies a pending chain correction and forms the fused
+  // right-hand side's FP64 block; the contractions follow on the corrected state
+  const bool tc = sizeof(T) == 4 && a.deriv_t;
+  if (!tc || a.fix.on || a.fuse_rhs) {
+    e = launch_kernel(k_fx_deriv<T>, dim3(a.M, batch), dim3(a.fix.on ? 384 : 256),
+                      fx_deriv_smem_bytes(a.nr, prec, a.fix.on != 0), s, a,
+                      reinterpret_cast<T*>(a.deriv), a.deriv_stride);
+    ktimer_mark(SDD_K_FX_DERIV, s);
+    if (e != cudaSuccess) return e;
+  }
+  if (tc && (e = launch_tc_for(a, batch, s)) != cudaSuccess) return e;
   {
     static unsigned long long done = 0;
     if ((e = ensure_smem_attr(k_fx_grid<T>, &done)) != cudaSuccess) return e;
@@ -1147,7 +1186,10 @@ bool fx_uses_split(const FxArgs& a, int batch, int mode) {
   return a.split == 2 || 2 * a.nr * batch <= fx_sm_count();
 }
 
-cudaError_t launch_fx(const FxArgs& a, int batch, int mode, int prec, cudaStream_t s) {
+cudaError_t launch_fx(const FxArgs& a_in, int batch, int mode, int prec, cudaStream_t s) {
+  FxArgs a = a_in;
+  // mixed plans with tensor-core tables: the radial contractions go to k_deriv_tc (needs the deriv scratch)
+  a.deriv_t = (prec == SDD_PREC_MIXED && a.tcB && a.deriv) ? 1 : 0;
   if (fx_uses_split(a, batch, mode)) {
     if (prec == SDD_PREC_MIXED) {
       if (mode == 0) return launch_fx_split_t<float, 0>(a, batch, s);

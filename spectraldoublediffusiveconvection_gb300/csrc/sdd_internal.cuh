@@ -210,6 +210,30 @@ struct FxArgs {
   int fuse_rhs;
   RhsArgs rl;
   FixArgs fix;               // split path: a pending correction of X (see FixArgs)
+  // mixed plans: the FP32 radial contractions on the tensor cores (k_deriv_tc, 3xTF32).  tcB: the plan's
+  // split operator tiles (nullable: CUDA-core FP32 contractions); tcKP / tcNP: nr rounded up to 8.  When
+  // they are used, deriv's four FP32 blocks hold the transposed layout [op][n][k] (deriv_t, set by
+  // launch_fx) and the row kernels read them instead of contracting.
+  const float* tcB;
+  int tcKP, tcNP;
+  int* tc_err;               // nullable: set by a tensor-core kernel whose wait timed out
+  int deriv_t;
+};
+
+// k_deriv_tc: the four radial contractions of Derivatives for every state row of a batch, 3xTF32 on the
+// tensor cores, into out[shell][op][n][k] (op 0 Dr psi, 1 (D^2/r^2) psi, 2 Dr T, 3 Dr S; FP32).
+struct TcArgs {
+  int M, nr, sym, KP, NP;
+  int rows;                  // batch * 3 * M state rows
+  const float* X32;          // the state in FP32 (nullable: X is converted)
+  size_t x32_stride;
+  const double* X;
+  size_t x_stride;
+  const int* active;         // nullable: per-shell flags; rows of shells whose flag is 0 are skipped
+  const float* B;            // [hi | lo] operator tiles (build_tc_operator), 16-byte aligned
+  float* out;
+  size_t out_stride;         // floats between shells in out
+  int* err;                  // nullable: set to 1 when a wait for the tensor cores timed out
 };
 
 
@@ -305,6 +329,11 @@ struct DiagArgs {
 cudaError_t launch_diag(const DiagArgs& a, int batch, cudaStream_t s);
 size_t diag_rows_smem_bytes(int M, int L);
 cudaError_t launch_fx(const FxArgs& a, int batch, int mode, int prec, cudaStream_t s);
+cudaError_t launch_deriv_tc(const TcArgs& a, cudaStream_t s);
+size_t tc_smem_bytes(int KP, int NP);
+// [hi | lo] tiles of B = [Dr ; D^2/r^2] (2 NP rows of KP) in the tensor cores' canonical shared-memory
+// layout: 2 * 2 NP * KP floats
+void build_tc_operator(const double* Dr, const double* D2r2, int nr, int KP, int NP, float* out);
 // whether launch_fx takes the split path for these arguments
 bool fx_uses_split(const FxArgs& a, int batch, int mode);
 cudaError_t launch_rhs(const RhsArgs& a, int batch, cudaStream_t s);

@@ -57,6 +57,7 @@ class Plan:
         self.precision = precision
         self.chain_layout = 0          # automatic (sdd_plan_set_chain_layout)
         self.fx_split = 0              # automatic (sdd_plan_set_fx_split)
+        self.tensor_cores = precision == "mixed"   # sdd_plan_set_tensor_cores
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.arrays = arrays if arrays is not None else plan_arrays(N_fm, N_r, d, dt, Pr, Tau)
         A = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in self.arrays.items()
@@ -141,6 +142,18 @@ class Plan:
         _lib.check(self._L.sdd_plan_set_fx_split(self._h, int(mode)), "sdd_plan_set_fx_split")
         self.fx_split = int(mode)
 
+    def set_tensor_cores(self, on):
+        """Mixed plans: FP32 radial contractions on the tensor cores (True, the default; 3xTF32 tcgen05 products)
+        or on the CUDA cores (False) (sdd_plan_set_tensor_cores)."""
+        _lib.check(self._L.sdd_plan_set_tensor_cores(self._h, int(bool(on))), "sdd_plan_set_tensor_cores")
+        self.tensor_cores = bool(on)
+
+    def tensor_core_timed_out(self):
+        """True if a tensor-core kernel of this plan gave up waiting for its products (sdd_plan_tensor_core_status)."""
+        v = ctypes.c_int(0)
+        _lib.check(self._L.sdd_plan_tensor_core_status(self._h, ctypes.byref(v)), "sdd_plan_tensor_core_status")
+        return bool(v.value)
+
     def new_state(self, batch=1):
         torch = _torch()
         return torch.zeros((batch, self.n_state), dtype=torch.float64, device=self.device)
@@ -209,6 +222,19 @@ class Plan:
         return out
 
 
+    def deriv_tc(self, X32, out=None):
+        """The four radial contractions of every mode (Dr psi, (D^2/r^2) psi, Dr T, Dr S) of a batch of FP32
+        states on the tensor cores (sdd_deriv_tc, mixed plans): (batch, 4, nr, N_fm) float32."""
+        torch = _torch()
+        if not isinstance(X32, torch.Tensor) or X32.dtype != torch.float32 or X32.device != self.device or \
+                not X32.is_contiguous() or X32.numel() % self.n_state:
+            raise TypeError("X32: expected a contiguous float32 tensor of batch x n_state on the plan's device")
+        B = X32.numel() // self.n_state
+        if out is None:
+            out = torch.empty((B, 4, self.nr, self.N_fm), dtype=torch.float32, device=self.device)
+        _lib.check(self._L.sdd_deriv_tc(self._h, B, _dptr(X32), _dptr(out), _stream(self.device)), "sdd_deriv_tc")
+        return out
+
     def step_profile(self, X, Ra, Ra_s, nsteps):
         """Per-kernel milliseconds (fx, rhs, chain) summed over nsteps steps from X (CUDA events)."""
         B = self._chk(X, self.n_state, "X")
@@ -257,7 +283,7 @@ class Plan:
         B = self._chk(X, self.n_state, "X")
         ra, ras = self._vec(Ra, B), self._vec(Ra_s, B)
         out = _torch().empty_like(X)
-        n = 9
+        n = 10                         # SDD_NUM_KERNELS
         ms = (ctypes.c_double * n)(*([0.0] * n))
         cnt = (ctypes.c_int * n)(*([0] * n))
         _lib.check(self._L.sdd_step_kernel_profile(self._h, B, _dptr(ra), _dptr(ras), _dptr(X), _dptr(out),
