@@ -145,6 +145,16 @@ int sdd_theta_op(sdd_plan* plan, int op, int batch, const double* g, double* f, 
  * linear != 0 drops the nonlinear term (Main.py:261-264). */
 int sdd_step(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, const double* X_in,
              double* X_out, int nsteps, int linear, void* stream);
+/* One Crank-Nicolson / Adams-Bashforth-2 step (an opt-in scheme; the reference and sdd_step are IMEX Euler,
+ * "CNAB1", Main.py:255-283).  The plan is built with HALF the step, dt_plan = dt/2 (its blocks invert
+ * A^2 - (dt/2) Pr A^4 and r^2 - (dt/2) r^2 Lap, Matrix_Operators.py:1014-1112): composed of the reference's
+ * own operations, psi' = A4_BSub(2 A2_SINE(psi) + dt E~_psi) - psi and T' = NAB2_BSub(2 r^2 T + dt E~_T) - T
+ * (S alike with Tau), where E are the explicit terms per unit time (psi: -NLIN_FX_psi + Pr gr_k(Ra T - Ra_s S);
+ * T/S: -NLIN_FX_T/S - DT0_theta(psi)) and E~ = 3/2 E - 1/2 E_prev.  hist (device, batch x 3*N_fm*nr) holds
+ * E_prev on entry when hist_valid (else E~ = E: the first step), and this step's E on exit.  X_in, X_out
+ * and hist must not alias. */
+int sdd_step_cnab2(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, const double* X_in,
+                   double* X_out, double* hist, int hist_valid, void* stream);
 /* Newton residual F(X) = Phi_dt(X) - X, Main.py:473-496 PFX.  base_cache as in sdd_nlin_fx. */
 int sdd_pfx(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, const double* X,
             double* F, double* base_cache, void* stream);
@@ -181,6 +191,15 @@ typedef struct sdd_newton_result {
  * residuals back to decide convergence).  Returns SDD_ERR_NOT_CONVERGED if a shell misses tol. */
 int sdd_newton_gmres(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, double* X,
                      const sdd_newton_opts* opts, sdd_newton_result* results, void* stream);
+
+/* The classical Gram-Schmidt pass of a GMRES column is repeated where the first pass left less than eta of
+ * the column's norm (|w'| < eta |w|); default 1e-2; eta >= 1 repeats it on every column, 0 never.  No
+ * counterpart in the reference (scipy's lgmres). */
+int sdd_plan_set_reorth_eta(sdd_plan* plan, double eta);
+/* Copies the Krylov basis vectors V_0 .. V_{k-1} of the last GMRES cycle of the last solve of this plan
+ * (sdd_newton_gmres / sdd_contin_step) for one shell into out (device, max_cols x 3*N_fm*nr doubles);
+ * *ncols = k (at most max_cols).  Synchronous.  For checking the basis' orthogonality. */
+int sdd_krylov_basis(const sdd_plan* plan, int shell, int max_cols, double* out, int* ncols, void* stream);
 
 /* ---- pseudo-arclength continuation step (Main.py:742-955 _ContinC) ------------------------------ */
 /* One step along the branch of steady states in Ra_T.  Predictor: with dt = 1 the reference always

@@ -524,6 +524,31 @@ def time_step(ops, X, Ra, Ra_s, symmetric, n_steps, linear=False, every=None):
     return (Xn, snaps) if every else Xn
 
 
+def step_cnab2(ops_half, Xn, E_prev, Ra, Ra_s, symmetric, dt):
+    """A Crank-Nicolson / Adams-Bashforth-2 step of dt composed of the reference's own operations
+    (NLIN_FX Matrix_Operators.py:743, DT0_theta :131, A2_SINE :192, kGR_RT :97, A4_BSub_TSTEP_V2 :1115,
+    NAB2_BSub_TSTEP_V2 :1033), with ops_half the operators of dt/2 (Main.py:179-225 at dt/2):
+      psi' = A4_BSub_{dt/2}(2 A2_SINE(psi) + dt E~_psi) - psi,   T' = NAB2_BSub_{dt/2}(2 r^2 T + dt E~_T) - T,
+    E the explicit terms per unit time (psi: -F_psi + Pr gr_k(Ra T - Ra_s S); T/S: -F_T/S - DT0_theta(psi)),
+    E~ = 3/2 E - 1/2 E_prev (E_prev None: E).  Returns (X', E)."""
+    N_fm, nr, Pr, Tau = ops_half.N_fm, ops_half.nr, ops_half.Pr, ops_half.Tau
+    h = ops_half.dt
+    N = N_fm * nr
+    psi, T, S = Xn[0:N], Xn[N:2 * N], Xn[2 * N:3 * N]
+    F = NLIN_FX(Xn, ops_half.D, ops_half.R, N_fm, nr, symmetric)
+    psi_T0 = DT0_theta(psi, ops_half.DT0, N_fm, nr, symmetric)
+    E = np.hstack((-F[0:N] + Pr * _gr_apply(ops_half, Ra * T - Ra_s * S), -F[N:2 * N] - psi_T0,
+                   -F[2 * N:3 * N] - psi_T0))
+    Et = E if E_prev is None else 1.5 * E - 0.5 * E_prev
+    rsq = np.tile(ops_half.rsq, N_fm)
+    Om = A2_SINE(psi, ops_half.D, ops_half.R, N_fm, nr, symmetric)
+    a = A4_BSub_TSTEP_V2(2.0 * Om + dt * Et[0:N], ops_half.Linv_A4, ops_half.D2_A4, ops_half.IR4_A4,
+                         ops_half.IR2_A4, N_fm, nr, Pr * h, symmetric) - psi
+    b = NAB2_BSub_TSTEP_V2(2.0 * rsq * T + dt * Et[N:2 * N], ops_half.Linv_T, N_fm, nr, h, symmetric) - T
+    c = NAB2_BSub_TSTEP_V2(2.0 * rsq * S + dt * Et[2 * N:], ops_half.Linv_S, N_fm, nr, Tau * h, symmetric) - S
+    return np.hstack((a, b, c)), E
+
+
 def PFX(ops, Xn, Ra, Ra_s, symmetric):
     """Main.py:473-496: Newton residual F(X) = Phi_dt(X) - X."""
     NX = -1.0 * ops.dt * NLIN_FX(Xn, ops.D, ops.R, ops.N_fm, ops.nr, symmetric)

@@ -91,10 +91,13 @@ SIGNATURES = [
     ("sdd_nab2_bsub", _I, [_VP, _I, _I, _VP, _VP, _VP]),
     ("sdd_theta_op", _I, [_VP, _I, _I, _VP, _VP, _VP]),
     ("sdd_step", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, _I, _VP]),
+    ("sdd_step_cnab2", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _I, _VP]),
     ("sdd_pfx", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP]),
     ("sdd_pdfx", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     ("sdd_newton_gmres", _I, [_VP, _I, _VP, _VP, _VP, ctypes.POINTER(NewtonOpts), ctypes.POINTER(NewtonResult),
                               _VP]),
+    ("sdd_plan_set_reorth_eta", _I, [_VP, _D]),
+    ("sdd_krylov_basis", _I, [_VP, _I, _I, _VP, ctypes.POINTER(_I), _VP]),
     ("sdd_contin_step", _I, [_VP, _I, _VP, _VP, _VP, _VP, ctypes.POINTER(ctypes.c_double),
                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ContinOpts),
                              ctypes.POINTER(ContinResult), _VP]),

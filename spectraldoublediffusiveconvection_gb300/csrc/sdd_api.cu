@@ -147,6 +147,8 @@ struct sdd_plan {
                     // precision, then M nr doubles (D2s psi of the fused right-hand side)
   // Krylov / Newton / continuation workspace (grown on demand)
   int sv_B, sv_m;
+  double reorth_eta;  // second Gram-Schmidt pass where |w'| < reorth_eta |w| (sdd_plan_set_reorth_eta)
+  int kv_last_B;      // batch of the last GMRES solve (the layout sdd_krylov_basis reads)
   double *kv_V, *kv_w, *kv_r, *kv_part, *kv_nrm2, *kv_small, *kv_dot;
   int* kv_ismall;
   double* h_dbl;      // pinned host scalars
@@ -535,6 +537,7 @@ int sdd_plan_create(const sdd_plan_desc* d, sdd_plan** out) {
   std::memset(p, 0, sizeof(*p));
   p->M = M; p->nr = nr; p->P = P; p->ldl = nr + (nr & 1); p->sym = d->symmetric ? 1 : 0;
   p->prec = d->precision; p->device = dev;
+  p->reorth_eta = kReorthEta;
   p->dt = d->dt; p->Pr = d->Pr; p->Tau = d->Tau;
   p->fft = fp;
   const size_t nn = (size_t)nr * nr, nm = (size_t)M * nr * nr;
@@ -659,6 +662,28 @@ int sdd_plan_tensor_core_status(const sdd_plan* p, int* timed_out) {
   if (!p || !timed_out) return SDD_ERR_ARG;
   *timed_out = 0;
   if (p->tc_err) SDD_CUDA(cudaMemcpy(timed_out, p->tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+  return SDD_OK;
+}
+
+int sdd_plan_set_reorth_eta(sdd_plan* p, double eta) {
+  if (!p || !(eta >= 0.0)) return SDD_ERR_ARG;
+  p->reorth_eta = eta;
+  return SDD_OK;
+}
+
+int sdd_krylov_basis(const sdd_plan* p, int shell, int max_cols, double* out, int* ncols, void* stream) {
+  if (!p || !out || !ncols || max_cols < 1 || shell < 0 || shell >= p->kv_last_B || !p->kv_V) return SDD_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int B = p->kv_last_B;
+  int kb = 0;
+  SDD_CUDA(cudaMemcpyAsync(&kb, p->kv_ismall + 2 * (size_t)B + shell, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SDD_CUDA(cudaStreamSynchronize(s));
+  const size_t n = (size_t)3 * p->M * p->nr, ld = n + 1, vs = (size_t)B * ld;
+  const int c = kb < max_cols ? kb : max_cols;
+  for (int j = 0; j < c; ++j)
+    SDD_CUDA(cudaMemcpyAsync(out + (size_t)j * n, p->kv_V + (size_t)j * vs + (size_t)shell * ld, n * sizeof(double),
+                             cudaMemcpyDeviceToDevice, s));
+  *ncols = c;
   return SDD_OK;
 }
 
@@ -1104,6 +1129,33 @@ int sdd_step(sdd_plan* p, int batch, const double* Ra, const double* Ras, const 
   return SDD_OK;
 }
 
+// Crank-Nicolson / Adams-Bashforth 2 step (no counterpart in the reference, which steps IMEX Euler): the plan
+// holds the operators of dt/2, the step is dt = 2 plan dt.  psi' = A4_BSub_{dt/2}(2 A2 psi + dt E~) - psi,
+// T' = NAB2_BSub_{dt/2}(2 r^2 T + dt E~_T) - T (and S with Tau), E~ = 3/2 E - 1/2 E_prev (E when !hist_valid).
+int sdd_step_cnab2(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X_in, double* X_out,
+                   double* hist, int hist_valid, void* stream) {
+  int st = check_plan(p, batch);
+  if (st) return st;
+  if (!Ra || !Ras || !X_in || !X_out || !hist || X_in == X_out || hist == X_in || hist == X_out) return SDD_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  FxArgs fa = fx_args(p, p->prec, X_in, nullptr, p->out4);
+  if (p->prec == SDD_PREC_MIXED) fa.q32 = p->q32;
+  SDD_CUDA(launch_fx(fa, batch, 0, p->prec, s));
+  RhsArgs ra = rhs_args(p, X_in, p->out4, Ra, Ras, p->rhs, 0);
+  ra.dt = 2.0 * p->dt;
+  if (p->prec == SDD_PREC_MIXED) {
+    ra.q32 = p->q32;
+    ra.Dr32 = p->Dr32;
+  }
+  ra.cnab2 = 1;
+  ra.hist_valid = hist_valid ? 1 : 0;
+  ra.hist = hist;
+  SDD_CUDA(launch_rhs(ra, batch, s));
+  ChainArgs ca = chain_args(p, p->rhs, X_out, X_in);   // the chains' "f -= sub": minus the old state
+  SDD_CUDA(launch_chain(ca, batch, 3, s));
+  return SDD_OK;
+}
+
 int sdd_pfx(sdd_plan* p, int batch, const double* Ra, const double* Ras, const double* X, double* F,
             double* base_cache, void* stream) {
   int st = check_plan(p, batch);
@@ -1200,6 +1252,7 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const double* rhs, double* 
                        int max_restarts, const std::vector<double>& target, const std::vector<int>& solve,
                        cudaStream_t s, int* matvecs, std::vector<double>& resid) {
   GmresState G = gmres_state(p, B, m);
+  p->kv_last_B = B;
   const size_t vs = (size_t)B * ld;
   int st;
   resid.assign(B, 0.0);
@@ -1228,7 +1281,7 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const double* rhs, double* 
       // the second pass only for the shells whose first pass cancelled w below kReorthEta of its norm
       // (the others get zero second projections)
       SDD_CUDA(krylov_dots(p->kv_w, 0, p->kv_w, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s, G.active));
-      SDD_CUDA(krylov_reorth_mask(G, p->kv_nrm2, j, kReorthEta, B, s));
+      SDD_CUDA(krylov_reorth_mask(G, p->kv_nrm2, j, p->reorth_eta, B, s));
       SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.h2, m + 1, 0, s, G.reo));
       SDD_CUDA(krylov_sub_combination(p->kv_V, vs, p->kv_w, G.h2, m + 1, nu, ld, j + 1, B, s, G.reo));
       SDD_CUDA(krylov_dots(p->kv_w, 0, p->kv_w, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s, G.active));

@@ -786,6 +786,27 @@ __global__ void __launch_bounds__(kFxThreads) k_rhs(RhsArgs a) {
     }
     const double psiT0 = dT0 * JP;                                              // DT0_theta
     const size_t o = (size_t)k * nr + n;
+    if (a.cnab2) {
+      // explicit terms per unit time at this step, and the Adams-Bashforth 2 extrapolation
+      const size_t ko = (size_t)k * nr + n;
+      const double ep = (O4 ? -(DrQ[k] - O4[N + ko]) : 0.0) + a.Pr * grv;
+      const double et = (O4 ? -O4[2 * N + ko] : 0.0) - psiT0;
+      const double es = (O4 ? -O4[3 * N + ko] : 0.0) - psiT0;
+      double* H = a.hist + (size_t)b * a.rhs_stride;
+      double xp = ep, xt = et, xs = es;
+      if (a.hist_valid) {
+        xp = fma(1.5, ep, -0.5 * H[o]);
+        xt = fma(1.5, et, -0.5 * H[N + o]);
+        xs = fma(1.5, es, -0.5 * H[2 * N + o]);
+      }
+      H[o] = ep;
+      H[N + o] = et;
+      H[2 * N + o] = es;
+      R[o] = fma(dt, xp, 2.0 * Om);
+      R[N + o] = fma(dt, xt, 2.0 * (rsq * Tv[k]));
+      R[2 * N + o] = fma(dt, xs, 2.0 * (rsq * Sv[k]));
+      continue;
+    }
     R[o] = nxp + (Om + dtPr * grv);
     R[N + o] = nxt + (rsq * Tv[k] - dt * psiT0);
     R[2 * N + o] = nxs + (rsq * Sv[k] - dt * psiT0);

@@ -164,6 +164,14 @@ struct RhsArgs {
   size_t x32_stride;         // floats between shells in X32
   float* rhs32;
   const float* D2s32;        // nr*nr (A2_SINE) in FP32
+  // Crank-Nicolson / Adams-Bashforth 2 (cnab2 != 0; the plan's operators are those of dt/2, dt above is
+  // the full step): rhs = 2 lin + dt (3/2 E - 1/2 E_prev) with E the explicit terms per unit time
+  // (psi: -(Dr Q - R) + Pr gr_k(Ra T - Ra_s S); T/S: -N - psi_T0), lin = A2_SINE(psi), r^2 T, r^2 S.
+  // hist [shell][3][M][nr] (stride rhs_stride) holds E_prev on entry when hist_valid (else the explicit
+  // part is Euler, dt E) and E of this step on exit.
+  int cnab2;
+  int hist_valid;
+  double* hist;
 };
 
 // A chunk correction of the state left pending by the previous time step (layout 3, sdd_step): the split

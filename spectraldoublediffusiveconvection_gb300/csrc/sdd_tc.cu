@@ -43,7 +43,7 @@ __host__ __device__ inline uint32_t tc_canon_off(int r, int k, int KP) {
 
 size_t tc_smem_bytes(int KP, int NP) {
   const size_t a = (size_t)kTcRows * KP * 4, b = (size_t)2 * NP * KP * 4;
-  size_t n = 2 * a + 2 * b + 64;
+  size_t n = 3 * a + 2 * b + 64;   // A hi, A lo, the raw FP32 rows of a tile, B hi, B lo, barrier + TMEM slot
   // at most three CTAs per SM with 128 TMEM columns each (five with 64): TMEM (512 columns) never runs out
   const size_t floor_bytes = (2 * NP > 64) ? (size_t)60 * 1024 : (size_t)46 * 1024;
   return n < floor_bytes ? floor_bytes : n;
@@ -126,7 +126,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_deriv_tc(TcArgs a) {
   unsigned char* Alo = Ahi + abytes;
   unsigned char* Bhi = Alo + abytes;
   unsigned char* Blo = Bhi + bbytes;
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(Blo + bbytes);
+  float* raw = reinterpret_cast<float*>(Blo + bbytes);          // the tile's rows as loaded, [128][nr]
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(raw) + abytes);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
   __shared__ int s_timeout;
   const uint32_t ncols = N > 64 ? 128u : 64u;
@@ -158,14 +159,30 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_deriv_tc(TcArgs a) {
   uint32_t phase = 0;
 
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    // ---- stage A: thread = tile row (kTcThreads == kTcRows); split into TF32 hi / lo, zero in the
-    // padding and in rows the symmetric subspace leaves out; 16-byte stores (one core-matrix row each) ----
+    // ---- stage A.  1: the tile's rows with coalesced loads, all in flight at once.  The rows of one shell
+    // are contiguous, so the tile is at most a few contiguous segments (one per shell it touches). ----
+    for (int r0 = 0; r0 < kTcRows;) {
+      const int R = tile * kTcRows + r0;
+      if (R >= a.rows) break;
+      const int b = R / rows3, fk = R - b * rows3;
+      const int cnt = min(min(kTcRows - r0, rows3 - fk), a.rows - R);
+      float* dst = raw + (size_t)r0 * nr;
+      if (a.X32) {
+        const float* src = a.X32 + (size_t)b * a.x32_stride + (size_t)fk * nr;
+        for (int e = tid; e < cnt * nr; e += kTcThreads) dst[e] = __ldg(src + e);
+      } else {
+        const double* src = a.X + (size_t)b * a.x_stride + (size_t)fk * nr;
+        for (int e = tid; e < cnt * nr; e += kTcThreads) dst[e] = (float)__ldg(src + e);
+      }
+      r0 += cnt;
+    }
+    __syncthreads();
+    // 2: thread = tile row (kTcThreads == kTcRows): split into TF32 hi / lo, zero in the padding and in
+    // rows the symmetric subspace leaves out; 16-byte stores (one core-matrix row each) ----
     const int r = tid;
     const int R = tile * kTcRows + r;
     int b = 0, f = 0, kk = 0;
     bool valid = R < a.rows, load = false;
-    const float* xs32 = nullptr;
-    const double* xs64 = nullptr;
     if (valid) {
       b = R / rows3;
       const int fk = R - b * rows3;
@@ -173,16 +190,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_deriv_tc(TcArgs a) {
       kk = fk - f * M;
       valid = !a.active || a.active[b];
       load = valid && !(a.sym && (f == 0 ? (kk % 2 == 0) : (kk % 2 == 1)));
-      if (a.X32) xs32 = a.X32 + (size_t)b * a.x32_stride + (size_t)fk * nr;
-      else xs64 = a.X + (size_t)b * a.x_stride + (size_t)fk * nr;
     }
+    const float* xr = raw + (size_t)r * nr;     // stride nr words between threads: conflict-free for odd nr
     for (int k4 = 0; k4 < KP / 4; ++k4) {
       uint32_t h[4], l[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int k = 4 * k4 + j;
-        float v = 0.f;
-        if (load && k < nr) v = xs32 ? __ldg(xs32 + k) : (float)__ldg(xs64 + k);
+        const float v = (load && k < nr) ? xr[k] : 0.f;
         h[j] = tf32_rna(v);
         l[j] = tf32_rna(v - __uint_as_float(h[j]));
       }
@@ -274,7 +289,26 @@ cudaError_t launch_deriv_tc(const TcArgs& a, cudaStream_t s) {
   cudaError_t e = ensure_smem_attr(k_deriv_tc, &done);
   if (e != cudaSuccess) return e;
   const int ntiles = (a.rows + kTcRows - 1) / kTcRows;
-  const int grid = ntiles < 2 * tc_sm_count() ? ntiles : 2 * tc_sm_count();
+  // persistent: as many CTAs as fit on the GPU at once (their shared memory bounds the count per SM)
+  static int occ_smem[8] = {0}, occ_val[8] = {0};
+  int per_sm = 0;
+  for (int i = 0; i < 8 && occ_smem[i]; ++i)
+    if (occ_smem[i] == (int)smem) per_sm = occ_val[i];
+  if (!per_sm) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_deriv_tc, kTcThreads, smem) != cudaSuccess ||
+        per_sm < 1) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
+    for (int i = 0; i < 8; ++i)
+      if (!occ_smem[i]) {
+        occ_val[i] = per_sm;              // the value before its key: a concurrent reader never sees 0
+        occ_smem[i] = (int)smem;
+        break;
+      }
+  }
+  const int slots = per_sm * tc_sm_count();
+  const int grid = ntiles < slots ? ntiles : slots;
   e = launch_kernel(k_deriv_tc, dim3(grid), dim3(kTcThreads), smem, s, a);
   ktimer_mark(SDD_K_DERIV_TC, s);
   return e;

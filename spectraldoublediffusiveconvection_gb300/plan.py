@@ -205,6 +205,18 @@ class Plan:
                                     int(bool(linear)), _stream(self.device)), "sdd_step")
         return out
 
+    def step_cnab2(self, X, Ra, Ra_s, hist, hist_valid, out=None):
+        """One Crank-Nicolson / Adams-Bashforth-2 step of dt = 2 * self.dt (the plan holds the operators of
+        the half step; sdd_step_cnab2).  hist: device tensor like X holding the previous step's explicit terms
+        when hist_valid, overwritten with this step's.  Returns the new state."""
+        B = self._chk(X, self.n_state, "X")
+        self._chk(hist, self.n_state, "hist")
+        out = out if out is not None else _torch().empty_like(X)
+        ra, ras = self._vec(Ra, B), self._vec(Ra_s, B)
+        _lib.check(self._L.sdd_step_cnab2(self._h, B, _dptr(ra), _dptr(ras), _dptr(X), _dptr(out), _dptr(hist),
+                                          int(bool(hist_valid)), _stream(self.device)), "sdd_step_cnab2")
+        return out
+
     def pfx(self, X, Ra, Ra_s, out=None, base=None):
         B = self._chk(X, self.n_state, "X")
         out = out if out is not None else _torch().empty_like(X)
@@ -312,6 +324,20 @@ class Plan:
                      matvecs=r.matvecs, converged=bool(r.converged)) for r in res]
 
 
+    def set_reorth_eta(self, eta):
+        """GMRES: repeat a column's Gram-Schmidt pass where the first left |w'| < eta |w| (default 1e-2)."""
+        _lib.check(self._L.sdd_plan_set_reorth_eta(self._h, float(eta)), "sdd_plan_set_reorth_eta")
+
+    def krylov_basis(self, shell, max_cols=64):
+        """(k x n_state) device tensor: the basis vectors of the last GMRES cycle of the last solve for one
+        shell (sdd_krylov_basis)."""
+        torch = _torch()
+        out = torch.empty((max_cols, self.n_state), dtype=torch.float64, device=self.device)
+        k = ctypes.c_int(0)
+        _lib.check(self._L.sdd_krylov_basis(self._h, int(shell), int(max_cols), _dptr(out), ctypes.byref(k),
+                                            _stream(self.device)), "sdd_krylov_basis")
+        return out[:k.value]
+
     def contin_step(self, X, Ra, Ra_s, sign, ds, tol=1e-10, restart=50, gmres_rtol=1e-4, tangent_rtol=1e-8,
                     max_restarts=20, max_corrector=5, max_halvings=8, mixed_matvec=False):
         """One pseudo-arclength step (sdd_contin_step) in place on X (batch x n_state) and Ra (device,
@@ -363,3 +389,32 @@ def clear_plans():
         for p in _cache.values():
             p.close()
         _cache.clear()
+
+
+class CNAB2Stepper:
+    """Crank-Nicolson (implicit terms) / Adams-Bashforth 2 (explicit terms) time stepping of a batch of
+    shells: an opt-in, second-order scheme beside the reference's IMEX Euler ("CNAB1", Main.py:255-283,
+    which Plan.step reproduces).  The first step's explicit part is Euler; the explicit terms of the last
+    step are kept on the device for the next.  Uses a plan of dt/2 (sdd_step_cnab2)."""
+
+    def __init__(self, N_fm, N_r, d, dt, Pr, Tau, symmetric=False, precision="fp64", device=None):
+        self.plan = Plan(N_fm, N_r, d, 0.5 * float(dt), Pr, Tau, symmetric=symmetric, precision=precision,
+                         device=device)
+        self.dt = float(dt)
+        self.hist = None
+        self.valid = False
+
+    def reset(self):
+        self.valid = False
+
+    def step(self, X, Ra, Ra_s, nsteps=1):
+        torch = _torch()
+        if self.hist is None or self.hist.shape != X.shape:
+            self.hist = torch.empty_like(X)
+            self.valid = False
+        a, b = X, torch.empty_like(X)
+        for _ in range(int(nsteps)):
+            self.plan.step_cnab2(a, Ra, Ra_s, self.hist, self.valid, out=b)
+            self.valid = True
+            a, b = b, (a if a is not X else torch.empty_like(X))
+        return a

@@ -317,6 +317,18 @@ def trajectory_c2_case():
     print("wrote traj_c2", XD.shape, "|X_N| %.6e" % np.linalg.norm(XN))
 
 
+def c2_operators_case():
+    """The reference's own psi-solve blocks (Build_Matrix_Operators' L_inv_A4, Main.py:205, i.e. numpy's
+    LAPACK inverses of A4_TSTEP_MATS, Matrix_Operators.py:1089-1112) for the N_r = 30, N_fm = 256,
+    dt = 5e-4 configuration.  These blocks are ill-conditioned: another platform's LAPACK inverts them
+    differently by up to ~1e-13 relative, and over 10^4 steps that alone moves the trajectory by ~5e-11, so
+    the trajectory check builds its plan from the blocks the reference itself used."""
+    d, Pr, Tau = PARAMS["d"], PARAMS["Pr"], PARAMS["Tau"]
+    ops = Main.Build_Matrix_Operators(256, 30, d, 5e-4, Pr, Tau)
+    np.savez(os.path.join(HERE, "traj_c2_linv_a4.npz"), Linv_A4=np.asarray(ops[5]))
+    print("wrote traj_c2_linv_a4")
+
+
 def layout_case():
     """Matrix_Operators.py:529-627 Vecs_to_X / X_to_Vecs on seeded fields, symmetric and not."""
     rng = np.random.default_rng(51)
@@ -380,6 +392,9 @@ if __name__ == "__main__":
     if "--only-c2" in OPTS:
         trajectory_c2_case()
         sys.exit(0)
+    if "--only-c2-operators" in OPTS:
+        c2_operators_case()
+        sys.exit(0)
     if "--only-layout" in OPTS:
         layout_case()
         sys.exit(0)
@@ -405,3 +420,4 @@ if __name__ == "__main__":
     layout_case()
     continuation_run_case()
     trajectory_c2_case()
+    c2_operators_case()

@@ -99,3 +99,33 @@ def test_main_build_matrix_operators_matches_reference_tuple(cuda):
     assert rel(np.array(LT), Z["Linv_T"]) < 1e-14
     assert rel(args_A4[0], Z["D2_A4"]) < 1e-14
     assert Rsq.shape == (8 * 5, 8 * 5) and gr_k.shape == (8 * 5, 8 * 5)
+
+
+@pytest.mark.parametrize("eta", [1e-2, 0.7071067811865476])
+def test_krylov_basis_stays_orthonormal(cuda, eta):
+    """The GMRES basis after full 50-column cycles of a batched mixed-precision Newton solve (FP32 nonlinear
+    term, right-hand sides and h in the products; FP64 basis): |V^T V - I|_max <= 1e-10 for the conditional
+    second Gram-Schmidt pass at the default eta = 1e-2 (loss per column <= ~eps/eta, accumulated over the
+    cycle) and at the usual 1/sqrt(2).  A nontrivial start (a convective steady state interpolated and
+    perturbed) and a tight inner tolerance keep every cycle at its full length."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    G = load_golden("cont_tau1.npz")
+    _, _, _, d, Pr, Tau, Ra, Ra_s, _ = G["params"]
+    N_r, N_fm, B = 24, 32, 3
+    X = O.INTERP_THETAS(N_fm, 16, O.INTERP_RADIAL(N_r, 16, G["X_steady"], d))
+    rng = np.random.default_rng(9)
+    Xs = np.stack([X + 1e-2 * np.linalg.norm(X) / np.sqrt(X.size) * rng.standard_normal(X.size) for _ in range(B)])
+    p = Plan(N_fm, N_r, d, 1.0, Pr, Tau, precision="mixed")
+    p.set_reorth_eta(eta)
+    Xt = torch.from_numpy(Xs).cuda()
+    Ra_t = torch.tensor([Ra - 100.0, Ra, Ra + 100.0], dtype=torch.float64, device="cuda")
+    p.newton(Xt, Ra_t, Ra_s, tol=1e-12, restart=50, gmres_rtol=1e-13, max_newton=1, max_restarts=2, mixed_matvec=2)
+    worst = 0.0
+    for b in range(B):
+        V = p.krylov_basis(b, 64)
+        assert V.shape[0] == 50, V.shape
+        err = float((V @ V.T - torch.eye(V.shape[0], dtype=torch.float64, device="cuda")).abs().max())
+        worst = max(worst, err)
+    print(f"eta={eta:.3g}: max |V^T V - I| over {B} shells, 50 columns: {worst:.2e}")
+    assert worst <= 1e-10
