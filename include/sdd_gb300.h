@@ -99,10 +99,13 @@ int sdd_plan_reserve(sdd_plan* plan, int max_batch);
  * 1 one lane per row, 2 chunked (each chain cut into chunks that run concurrently, joined by a short
  * sequential carried-state recurrence), 3 chunked with shorter chunks joined by a parallel carry
  * (precomputed products of the chunk maps, all applied at once), 4 split rows over 4 warps, 5 split rows
- * over 2 lanes in 2 warps (nr <= 32; 4 otherwise).  Set by the batch autotuner; no counterpart in the
- * reference. */
+ * over 2 lanes in 2 warps (nr <= 32; 4 otherwise), 6 / 7 the chains in the reference's own order of
+ * operations (Matrix_Operators.py:1139-1164, 1056-1083: per step D2 f_e, then Linv_j (g_j + b)), without the
+ * h = Linv g pre-pass of the other layouts: 4 nr^2 multiply-adds per mode instead of 7, rows over 2 / 4
+ * lanes; they need the full FP64 right-hand side, so launches with the fused or the FP32 right-hand side run
+ * layout 5.  Set by the batch autotuner; no counterpart in the reference. */
 int sdd_plan_set_chain_layout(sdd_plan* plan, int layout);
-/* The layout (1-5) a step of `batch` shells runs under the current setting, with its chunk length and
+/* The layout (1-7) a step of `batch` shells runs under the current setting, with its chunk length and
  * chunks per chain (0 and 1 when not chunked). */
 int sdd_plan_chain_choice(const sdd_plan* plan, int batch, int* layout, int* kc, int* nch);
 /* Mixed plans: the FP32 radial contractions of the nonlinear term (Derivatives, Matrix_Operators.py:698-729)
@@ -193,8 +196,9 @@ int sdd_newton_gmres(sdd_plan* plan, int batch, const double* Ra, const double* 
                      const sdd_newton_opts* opts, sdd_newton_result* results, void* stream);
 
 /* The classical Gram-Schmidt pass of a GMRES column is repeated where the first pass left less than eta of
- * the column's norm (|w'| < eta |w|); default 1e-2; eta >= 1 repeats it on every column, 0 never.  No
- * counterpart in the reference (scipy's lgmres). */
+ * the column's norm (|w'| < eta |w|); default 1/sqrt(2); eta >= 1 repeats it on every column, 0 never.
+ * Thresholds well below the default lose the basis' orthogonality over long cycles.  No counterpart in
+ * the reference (scipy's lgmres). */
 int sdd_plan_set_reorth_eta(sdd_plan* plan, double eta);
 /* Copies the Krylov basis vectors V_0 .. V_{k-1} of the last GMRES cycle of the last solve of this plan
  * (sdd_newton_gmres / sdd_contin_step) for one shell into out (device, max_cols x 3*N_fm*nr doubles);

@@ -688,7 +688,7 @@ int sdd_krylov_basis(const sdd_plan* p, int shell, int max_cols, double* out, in
 }
 
 int sdd_plan_set_chain_layout(sdd_plan* p, int layout) {
-  if (!p || layout < 0 || layout > 5) return SDD_ERR_ARG;
+  if (!p || layout < 0 || layout > 7) return SDD_ERR_ARG;
   if (p->chain_layout != layout) clear_step_graphs(p);
   p->chain_layout = layout;
   return SDD_OK;
@@ -808,7 +808,7 @@ static ChainArgs chain_args(const sdd_plan* p, const double* g, double* f, const
   a.f = f; a.f_stride = shell_elems(p);
   a.sub = sub; a.sub_stride = shell_elems(p);
   a.LinvA4 = p->LinvA4; a.LinvT = p->LinvT; a.LinvS = p->LinvS;
-  a.ABA4 = p->ABA4; a.ir2A4 = p->ir2A4; a.ir4A4 = p->ir4A4;
+  a.ABA4 = p->ABA4; a.D2A4 = p->D2A4; a.ir2A4 = p->ir2A4; a.ir4A4 = p->ir4A4;
   a.h = p->hbuf;
   a.h_stride = shell_elems(p);
   a.coefA4 = p->coefA4; a.coefT = p->coefT; a.coefS = p->coefS;
@@ -1278,7 +1278,7 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const double* rhs, double* 
       // shells whose Arnoldi process has stopped skip the Gram-Schmidt work (krylov_arnoldi_finish ignores them)
       SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.hcol, m + 1, 0, s, G.active));
       SDD_CUDA(krylov_sub_combination(p->kv_V, vs, p->kv_w, G.hcol, m + 1, nu, ld, j + 1, B, s, G.active));
-      // the second pass only for the shells whose first pass cancelled w below kReorthEta of its norm
+      // the second pass only for the shells whose first pass cancelled w below reorth_eta of its norm
       // (the others get zero second projections)
       SDD_CUDA(krylov_dots(p->kv_w, 0, p->kv_w, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s, G.active));
       SDD_CUDA(krylov_reorth_mask(G, p->kv_nrm2, j, p->reorth_eta, B, s));

@@ -286,6 +286,137 @@ __global__ void k_chain(ChainArgs a) {
   }
 }
 
+// Layouts 6 and 7: the chains in the reference's own order of operations, without the h = Linv g pre-pass:
+//   psi (Matrix_Operators.py:1139-1164):  f_e += f_{j+2};  L1f = D2 f_e + bj IR4 f_e;
+//          b = dt bjt (L1f + IR4 bf_e) - bjt IR2 f_e;  f_j = Linv_j (g_j + b);  bf_e += bj f_j + bjt f_e
+//   T, S (Matrix_Operators.py:1056-1083):  b += 2 dt (j+2) f_{j+2};  f_j = Linv_j (g_j - w b)
+// Per mode 4 nr^2 multiply-adds instead of the 7 nr^2 of the pre-pass form (h, then [A B] for psi and
+// Linv b for T/S), at the price of a second dependent matvec per psi step: the form for batches that fill
+// the GPU, where the FP64 work and not a chain's latency sets the time.  Rows split over TPR lanes, one CTA
+// per (field, parity, shell); the Linv blocks stream through a 3-slot cp.async ring, D2 sits in shared
+// memory.  g is the full right-hand side (not the fused form).
+template <int TPR>
+__global__ void k_chain_ref(ChainArgs a) {
+  extern __shared__ __align__(16) double csm[];
+  const int field = a.field0 + (blockIdx.x >> 1);
+  const int par = blockIdx.x & 1;
+  const int b = blockIdx.y;
+  if (a.active && !a.active[b]) return;
+  const int M = a.M, nr = a.nr, ldl = a.ldl;
+  const bool a4 = (field == 0);
+  const size_t foff = (size_t)field * a.field_off;
+  double* f = a.f + (size_t)b * a.f_stride + foff;
+  const double* sub = a.sub ? a.sub + (size_t)b * a.sub_stride + foff : nullptr;
+  float* f32 = a.f32 ? a.f32 + (size_t)b * a.f32_stride + foff : nullptr;
+  const int tid = threadIdx.x;
+  const int i = tid / TPR, q = tid % TPR;
+  const bool row_ok = i < nr;
+  const bool lead = row_ok && q == 0;
+  const int ir = row_ok ? i : 0;
+  const int S = (M - par + 1) / 2;
+  if (a.sym && !(a4 ? par == 0 : par == 1)) {          // symmetric: the other parity's rows are zero
+    for (int e = tid; e < S * nr; e += blockDim.x) {
+      const int st = e / nr, c = e - st * nr;
+      f[(size_t)(M - 1 - (par + 2 * st)) * nr + c] = 0.0;
+      if (f32) f32[(size_t)(M - 1 - (par + 2 * st)) * nr + c] = 0.0f;
+    }
+    return;
+  }
+  const int blk = nr * ldl;
+  double* Lb0 = csm;                                   // 3-slot ring of Linv blocks
+  double* D2s = Lb0 + 3 * blk;                         // psi: D2 (transposed), nr x ldl
+  double* cf = D2s + (a4 ? blk : 0);                   // per-step scalars, 4 per step
+  double* xv = cf + 4 * (size_t)(S + 1);               // 2 buffers of f_e (psi)
+  double* yv = xv + 2 * nr;                            // 2 buffers of the Linv matvec's operand
+  const double* Mat = a4 ? a.LinvA4 : (field == 1 ? a.LinvT : a.LinvS);
+  const double* coef = a4 ? a.coefA4 : (field == 1 ? a.coefT : a.coefS);
+  copy_block(Lb0, Mat + (size_t)par * blk, blk);
+  if (a4) copy_block(D2s, a.D2A4, blk);
+  cp_async_commit();
+  if (S > 1) copy_block(Lb0 + blk, Mat + (size_t)(par + 2) * blk, blk);
+  cp_async_commit();
+  for (int e = tid; e < 4 * (S + 1); e += blockDim.x) {
+    const int jj = par + 2 * (e >> 2);
+    cf[e] = jj < M ? coef[(size_t)jj * 4 + (e & 3)] : 0.0;
+  }
+  const double ir4 = a4 ? a.ir4A4[ir] : 0.0, ir2 = a4 ? a.ir2A4[ir] : 0.0;
+  const double* grow = a.g + (size_t)b * a.g_stride + foff + ir;
+  auto g_at = [&](int st) { return st < S ? grow[(size_t)(M - 1 - (par + 2 * st)) * nr] : 0.0; };
+  double gn0 = g_at(0), gn1 = g_at(1);
+  double fe = 0.0, bfe = 0.0, fprev = 0.0;             // psi: f_e_i, bf_e_i; T/S: b_i in fe
+  for (int st = 0; st < S; ++st) {
+    const int jj = par + 2 * st;
+    const int row = M - 1 - jj;
+    const double* cur = Lb0 + (st % 3) * blk;
+    double* yb = yv + (st & 1) * nr;
+    cp_async_wait<1>();
+    chain_sync();                                      // Linv_jj (and D2) landed; step st-1 done
+    if (st + 2 < S) copy_block(Lb0 + ((st + 2) % 3) * blk, Mat + (size_t)(jj + 4) * blk, blk);
+    cp_async_commit();
+    const double gi = gn0;
+    gn0 = gn1;
+    gn1 = g_at(st + 2);
+    if (a4) {
+      const double bj = cf[4 * st + 2], bjt = cf[4 * st + 3], c1 = cf[4 * st];
+      double y = gi;
+      if (st > 0) {
+        fe += fprev;                                   // f_e += f_{j+2}
+        double* xb = xv + (st & 1) * nr;
+        if (lead) xb[i] = fe;
+        chain_sync();
+        double z = 0.0;
+#pragma unroll 8
+        for (int c = q; c < nr; c += TPR) z = fma(D2s[c * ldl + ir], xb[c], z);
+        z = group_sum<TPR>(z);
+        const double L1f = fma(bj * ir4, fe, z);      // (D2 + bj IR4) f_e
+        const double t = fma(ir4, bfe, L1f);           // + IR4 bf_e
+        const double bt = fma(c1, t, -(bjt * ir2 * fe));
+        y = gi + bt;
+      }
+      if (lead) yb[i] = y;
+      chain_sync();
+      double acc = 0.0;
+#pragma unroll 8
+      for (int c = q; c < nr; c += TPR) acc = fma(cur[c * ldl + ir], yb[c], acc);
+      const double fi = group_sum<TPR>(acc);
+      bfe = st > 0 ? fma(bj, fi, fma(bjt, fe, bfe)) : fma(bj, fi, bfe);
+      fprev = fi;
+      if (lead) {
+        f[(size_t)row * nr + i] = fi;
+        if (f32) f32[(size_t)row * nr + i] = (float)fi;
+      }
+    } else {
+      const double y = fma(-cf[4 * st + 1], fe, gi);  // g - w b
+      if (lead) yb[i] = y;
+      chain_sync();
+      double acc = 0.0;
+#pragma unroll 8
+      for (int c = q; c < nr; c += TPR) acc = fma(cur[c * ldl + ir], yb[c], acc);
+      const double fi = group_sum<TPR>(acc);
+      fe = fma(cf[4 * (st + 1)], fi, fe);             // the b of the next step
+      if (lead) {
+        f[(size_t)row * nr + i] = fi;
+        if (f32) f32[(size_t)row * nr + i] = (float)fi;
+      }
+    }
+  }
+  cp_async_wait<0>();
+  if (sub) {  // Newton residual: f -= sub (the block's own writes are visible after the barrier)
+    __syncthreads();
+    for (int e = tid; e < S * nr; e += blockDim.x) {
+      const int st = e / nr, c = e - st * nr;
+      const size_t o = (size_t)(M - 1 - (par + 2 * st)) * nr + c;
+      f[o] -= sub[o];
+    }
+  }
+}
+
+static size_t chain_ref_smem_bytes(int M, int nr, int ldl) {
+  const size_t blk = (size_t)nr * ldl;
+  const size_t ns = (size_t)((M + 1) / 2);
+  return (4 * blk + 4 * (ns + 1) + 4 * (size_t)nr) * sizeof(double);
+}
+
 size_t chain_smem_bytes(int M, int nr, int ldl) {
   const size_t blk = (size_t)2 * nr * ldl;
   const size_t ns = (size_t)((M + 1) / 2);
@@ -799,7 +930,10 @@ int resolve_chain_layout(const ChainArgs& a, int batch, int nfields) {
   const ChunkSet& c3 = a.cset[1];
   if (layout == 0 && c3.nch > 1 && c3.GA4 && 2 * nfields * batch * c3.nch <= 2 * sms) layout = 3;
   if (layout == 0 && c2.nch > 1 && c2.GA4 && 2 * nfields * batch * c2.nch <= 2 * sms) layout = 2;
-  if (layout != 2 && layout != 3 && chain_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin)
+  // layouts 6 / 7 need the full right-hand side in FP64: with the fused or the FP32 one, the pre-pass form
+  if ((layout == 6 || layout == 7) && (a.fuse_rhs || a.g32)) layout = 5;
+  if ((layout == 6 || layout == 7) && chain_ref_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin) layout = 2;
+  if (layout != 2 && layout != 3 && layout != 6 && layout != 7 && chain_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin)
     layout = 2;   // whole chain too long for shared memory
   if (layout == 0) layout = 2 * nfields * batch <= sms ? 4 : 5;
   if (layout == 5 && a.nr > 32) layout = 4;
@@ -809,6 +943,25 @@ int resolve_chain_layout(const ChainArgs& a, int batch, int nfields) {
 cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStream_t s) {
   ChainArgs a = a_in;
   const int layout = resolve_chain_layout(a, batch, nfields);
+  if (layout == 6 || layout == 7) {   // the reference's order, no h pre-pass (full right-hand sides only)
+    if (a.fuse_rhs || a.g32 || !a.D2A4) return cudaErrorInvalidValue;
+    const int tpr = layout == 6 ? 2 : 4;
+    const int threads = ((a.nr * tpr + 31) / 32) * 32;
+    const size_t smem = chain_ref_smem_bytes(a.M, a.nr, a.ldl);
+    cudaError_t e;
+    if (tpr == 2) {
+      static unsigned long long done = 0;
+      if ((e = ensure_smem_attr(k_chain_ref<2>, &done)) != cudaSuccess) return e;
+      e = launch_kernel(k_chain_ref<2>, dim3(2 * nfields, batch), dim3(threads), smem, s, a);
+    } else {
+      static unsigned long long done = 0;
+      if ((e = ensure_smem_attr(k_chain_ref<4>, &done)) != cudaSuccess) return e;
+      e = launch_kernel(k_chain_ref<4>, dim3(2 * nfields, batch), dim3(threads), smem, s, a);
+    }
+    ktimer_mark(SDD_K_CHAIN, s);
+    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+  }
   const ChunkSet& c2 = a.cset[0];
   const ChunkSet& c3 = a.cset[1];
   if (layout == 2 || layout == 3) {

@@ -731,10 +731,14 @@ __global__ void __launch_bounds__(kFxThreads) k_rhs(RhsArgs a) {
   double* Tv = DrQ + M;
   double* Sv = Tv + M;
   double* opr = Sv + M;  // Dr row n, D2s row n
+  // kd[k] = k: the mode numbers as doubles, read instead of converted (a conversion is an FP64-pipe
+  // instruction on this GPU); the same exact values, so the same bits
+  double* kd = opr + 2 * nr;
   for (int m = tid; m < nr; m += bd) {
     opr[m] = a.Dr[n * nr + m];
     opr[nr + m] = a.D2s[n * nr + m];
   }
+  for (int k = tid; k < M + 3; k += bd) kd[k] = (double)k;
   __syncthreads();
   const int N = M * nr;
   const double* Xs = a.X + (size_t)b * a.x_stride;
@@ -773,10 +777,11 @@ __global__ void __launch_bounds__(kFxThreads) k_rhs(RhsArgs a) {
   double* R = a.rhs + (size_t)b * a.rhs_stride;
   for (int k = tid; k < M; k += bd) {
     const double s1 = (k + 1 < M) ? Sc[k + 1] : 0.0;
-    const double JP = (k == 0) ? 1.0 * s1 : (k + 1.0) * pv[k - 1] + 2.0 * s1;    // J_theta_RT
+    const double k1 = kd[k + 1], k2 = kd[k + 2];
+    const double JP = (k == 0) ? 1.0 * s1 : k1 * pv[k - 1] + 2.0 * s1;    // J_theta_RT
     const double s2 = (k + 2 < M) ? Sc[k + 2] : 0.0;
-    const double Om = D2p[k] - (double)(k + 1) * ir2 * ((k + 2.0) * pv[k] + 2.0 * s2);  // A2_SINE
-    const double grv = (k < M - 1) ? (-(double)(k + 1) * gr) * (Ra * Tv[k + 1] - Ras * Sv[k + 1]) : 0.0;
+    const double Om = D2p[k] - k1 * ir2 * (k2 * pv[k] + 2.0 * s2);       // A2_SINE
+    const double grv = (k < M - 1) ? (-k1 * gr) * (Ra * Tv[k + 1] - Ras * Sv[k + 1]) : 0.0;
     double nxp = 0, nxt = 0, nxs = 0;
     if (O4) {
       const size_t o = (size_t)k * nr + n;
@@ -1243,7 +1248,7 @@ cudaError_t launch_rhs(const RhsArgs& a, int batch, cudaStream_t s) {
     if (er != cudaSuccess) return er;
     return cudaGetLastError();
   }
-  const size_t smem = (6 * (size_t)a.M + 2 * (size_t)a.nr) * sizeof(double);
+  const size_t smem = (7 * (size_t)a.M + 3 + 2 * (size_t)a.nr) * sizeof(double);
   static unsigned long long done = 0;
   cudaError_t e = ensure_smem_attr(k_rhs, &done);
   if (e != cudaSuccess) return e;

@@ -260,7 +260,8 @@ struct ChunkSet {
 struct ChainArgs {
   int M, nr, ldl, sym;
   int field0;                // first field handled (blockIdx.x/2 + field0)
-  int layout;                // 1 one lane per row, 4 rows split over 4 warps, 2/3 chunked (resolved by the host)
+  int layout;                // 1 one lane per row, 4 rows split over 4 warps, 2/3 chunked, 6/7 the reference's
+                             // order (resolved by the host)
   size_t field_off;          // doubles between field blocks (N_fm*nr, or 0 when g/f point at one block)
   const double* g;           // rhs [shell][3][M][nr]
   size_t g_stride;
@@ -272,6 +273,7 @@ struct ChainArgs {
   size_t sub_stride;
   const double* LinvA4, *LinvT, *LinvS;  // [M][nr cols][ldl] transposed blocks
   const double* ABA4;        // [M][2 nr cols][ldl]: transposed [A_j B_j] of the psi chain
+  const double* D2A4;        // [nr cols][ldl]: transposed D2 of the psi operator (layouts 6 and 7)
   double* h;                 // [shell][3][M][nr] h = Linv g
   size_t h_stride;           // doubles between shells in h
   const double* ir2A4, *ir4A4;

@@ -108,6 +108,10 @@ static __device__ __forceinline__ bool mbar_wait_bounded(uint32_t addr, uint32_t
   }
 }
 
+static __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_u32(smem)), "l"(gmem));
+}
+
 static __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
@@ -158,24 +162,32 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_deriv_tc(TcArgs a) {
   const int ntiles = (a.rows + kTcRows - 1) / kTcRows;
   uint32_t phase = 0;
 
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    // ---- stage A.  1: the tile's rows with coalesced loads, all in flight at once.  The rows of one shell
-    // are contiguous, so the tile is at most a few contiguous segments (one per shell it touches). ----
+  // The rows of a tile go to `raw` in contiguous segments (one per shell the tile touches: a shell's rows
+  // are contiguous).  FP32 input: cp.async, issued for the next tile as soon as this tile's rows are split,
+  // so the loads overlap this tile's MMAs and epilogue.  FP64 input: converted through registers.
+  auto stage = [&](int t) {
     for (int r0 = 0; r0 < kTcRows;) {
-      const int R = tile * kTcRows + r0;
+      const int R = t * kTcRows + r0;
       if (R >= a.rows) break;
       const int b = R / rows3, fk = R - b * rows3;
       const int cnt = min(min(kTcRows - r0, rows3 - fk), a.rows - R);
       float* dst = raw + (size_t)r0 * nr;
       if (a.X32) {
         const float* src = a.X32 + (size_t)b * a.x32_stride + (size_t)fk * nr;
-        for (int e = tid; e < cnt * nr; e += kTcThreads) dst[e] = __ldg(src + e);
+        for (int e = tid; e < cnt * nr; e += kTcThreads) cp_async4(dst + e, src + e);
       } else {
         const double* src = a.X + (size_t)b * a.x_stride + (size_t)fk * nr;
         for (int e = tid; e < cnt * nr; e += kTcThreads) dst[e] = (float)__ldg(src + e);
       }
       r0 += cnt;
     }
+    asm volatile("cp.async.commit_group;\n" ::);
+  };
+  if ((int)blockIdx.x < ntiles) stage(blockIdx.x);
+
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    // ---- stage A.  1: this tile's rows have landed in `raw` ----
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
     __syncthreads();
     // 2: thread = tile row (kTcThreads == kTcRows): split into TF32 hi / lo, zero in the padding and in
     // rows the symmetric subspace leaves out; 16-byte stores (one core-matrix row each) ----
@@ -209,6 +221,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_deriv_tc(TcArgs a) {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
+    // `raw` is free again: the next tile's rows stream in while this tile's products run
+    if (tile + (int)gridDim.x < ntiles) stage(tile + gridDim.x);
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t ah = smem_u32(Ahi), al = smem_u32(Alo), bh = smem_u32(Bhi), bl = smem_u32(Blo);
@@ -257,6 +271,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_deriv_tc(TcArgs a) {
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
   }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");   // a prefetch left in flight by a timed-out tile
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (s_timeout) {
@@ -289,24 +304,19 @@ cudaError_t launch_deriv_tc(const TcArgs& a, cudaStream_t s) {
   cudaError_t e = ensure_smem_attr(k_deriv_tc, &done);
   if (e != cudaSuccess) return e;
   const int ntiles = (a.rows + kTcRows - 1) / kTcRows;
-  // persistent: as many CTAs as fit on the GPU at once (their shared memory bounds the count per SM)
-  static int occ_smem[8] = {0}, occ_val[8] = {0};
-  int per_sm = 0;
-  for (int i = 0; i < 8 && occ_smem[i]; ++i)
-    if (occ_smem[i] == (int)smem) per_sm = occ_val[i];
-  if (!per_sm) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_deriv_tc, kTcThreads, smem) != cudaSuccess ||
-        per_sm < 1) {
-      cudaGetLastError();
-      per_sm = 1;
-    }
-    for (int i = 0; i < 8; ++i)
-      if (!occ_smem[i]) {
-        occ_val[i] = per_sm;              // the value before its key: a concurrent reader never sees 0
-        occ_smem[i] = (int)smem;
-        break;
-      }
+  // persistent: as many CTAs as fit on an SM at once (their shared memory bounds the count; at most 4)
+  static int smem_sm = 0, smem_rsv = 0;
+  if (!smem_sm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int v = 0, r = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&r, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    smem_rsv = r;
+    smem_sm = v > 0 ? v : 1;
   }
+  int per_sm = smem_sm / (int)(smem + 1024 + smem_rsv);   // 1 KB of static shared memory per CTA
+  per_sm = per_sm < 1 ? 1 : (per_sm > 4 ? 4 : per_sm);
   const int slots = per_sm * tc_sm_count();
   const int grid = ntiles < slots ? ntiles : slots;
   e = launch_kernel(k_deriv_tc, dim3(grid), dim3(kTcThreads), smem, s, a);

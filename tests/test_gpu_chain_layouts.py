@@ -1,5 +1,6 @@
 """Every chain layout of the implicit solves (1 one lane per row, 2 chunked with a sequential carry, 3
-chunked with a parallel carry, 4 rows split over 4 lanes, 5 over 2 lanes) against the oracle's A4_BSub_TSTEP_V2 / NAB2_BSub_TSTEP_V2
+chunked with a parallel carry, 4 rows split over 4 lanes, 5 over 2 lanes, 6 and 7 the reference's own order
+of operations with rows over 2 or 4 lanes) against the oracle's A4_BSub_TSTEP_V2 / NAB2_BSub_TSTEP_V2
 chains (Matrix_Operators.py:1033-1194), alone and inside the step, the Newton residual and its Jacobian.
 The chunked layouts reorder the arithmetic (carried states through precomputed chunk maps or their
 products), so they agree with the sequential chain to rounding, not bitwise."""
@@ -15,7 +16,7 @@ SHAPES = [(16, 16, False), (20, 64, False), (30, 256, False), (48, 512, False), 
 
 
 @pytest.mark.parametrize("N_r,N_fm,sym", SHAPES)
-@pytest.mark.parametrize("layout", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("layout", [1, 2, 3, 4, 5, 6, 7])
 def test_chain_solves_against_oracle(cuda, N_r, N_fm, sym, layout):
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     torch = cuda
@@ -64,6 +65,44 @@ def test_chunked_step_newton_operators_against_oracle(cuda, N_r, N_fm, layout):
     F = p1.pfx(Xt, 8000.0, 500.0).cpu().numpy()
     J = p1.pdfx(dvt, Xt, 8000.0, 500.0).cpu().numpy()
     for k, x in enumerate([X, 2 * X]):
+        assert rel(F[k], O.PFX(ops1, x, 8000.0, 500.0, False)) < 1e-12
+        assert rel(J[k], O.PDFX(ops1, dv, x, 8000.0, 500.0, False)) < 1e-12
+
+
+@pytest.mark.parametrize("layout", [6, 7])
+@pytest.mark.parametrize("N_r,N_fm,prec", [(20, 64, "fp64"), (30, 256, "fp64"), (48, 512, "fp64"), (30, 256, "mixed")])
+def test_reference_order_chains_in_steps_and_newton_operators(cuda, N_r, N_fm, prec, layout):
+    """Layouts 6/7 (no h pre-pass; they need the full right-hand side, so the fused row kernel): steps, the
+    Newton residual and its Jacobian against the oracle, and a batch equal to its shells alone."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    nr = N_r - 1
+    X = O.seeded_state(N_fm, nr, 1234)
+    dv = O.seeded_state(N_fm, nr, 77)
+    Xt = torch.from_numpy(np.stack([X, 2 * X, 0.5 * X])).cuda()
+    ops = O.Operators(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01)
+    p = Plan(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01, precision=prec)
+    p.set_chain_layout(layout)
+    p.set_fx_split(1)
+    assert p.chain_choice(3)[0] == layout
+    Y = p.step(Xt, 8000.0, 500.0, nsteps=3).cpu().numpy()
+    for k, x in enumerate([X, 2 * X, 0.5 * X]):
+        r = x
+        for _ in range(3):
+            r = O.step(ops, r, 8000.0, 500.0, False)
+        assert rel(Y[k], r) < (1e-12 if prec == "fp64" else 1e-6)
+        Yk = p.step(Xt[k:k + 1].clone(), 8000.0, 500.0, nsteps=3).cpu().numpy()
+        assert np.array_equal(Yk[0], Y[k])
+    if prec != "fp64":
+        return
+    ops1 = O.Operators(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
+    p1 = Plan(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
+    p1.set_chain_layout(layout)
+    p1.set_fx_split(1)
+    dvt = torch.from_numpy(np.stack([dv, dv, dv])).cuda()
+    F = p1.pfx(Xt, 8000.0, 500.0).cpu().numpy()
+    J = p1.pdfx(dvt, Xt, 8000.0, 500.0).cpu().numpy()
+    for k, x in enumerate([X, 2 * X, 0.5 * X]):
         assert rel(F[k], O.PFX(ops1, x, 8000.0, 500.0, False)) < 1e-12
         assert rel(J[k], O.PDFX(ops1, dv, x, 8000.0, 500.0, False)) < 1e-12
 
@@ -151,4 +190,4 @@ def test_automatic_layout_choice(cuda):
     p.set_chain_layout(3)
     assert p.chain_choice(64) == (3, 8, 16)
     with pytest.raises(Exception):
-        p.set_chain_layout(6)
+        p.set_chain_layout(8)

@@ -101,13 +101,13 @@ def test_main_build_matrix_operators_matches_reference_tuple(cuda):
     assert Rsq.shape == (8 * 5, 8 * 5) and gr_k.shape == (8 * 5, 8 * 5)
 
 
-@pytest.mark.parametrize("eta", [1e-2, 0.7071067811865476])
-def test_krylov_basis_stays_orthonormal(cuda, eta):
-    """The GMRES basis after full 50-column cycles of a batched mixed-precision Newton solve (FP32 nonlinear
-    term, right-hand sides and h in the products; FP64 basis): |V^T V - I|_max <= 1e-10 for the conditional
-    second Gram-Schmidt pass at the default eta = 1e-2 (loss per column <= ~eps/eta, accumulated over the
-    cycle) and at the usual 1/sqrt(2).  A nontrivial start (a convective steady state interpolated and
-    perturbed) and a tight inner tolerance keep every cycle at its full length."""
+def test_krylov_basis_stays_orthonormal(cuda):
+    """The GMRES basis after 40-50-column cycles of a batched mixed-precision Newton solve (FP32 nonlinear term,
+    right-hand sides and h in the products; FP64 basis) stays orthonormal, |V^T V - I|_max <= 1e-10, with the
+    default conditional second Gram-Schmidt pass (|w'| < |w|/sqrt(2)).  A nontrivial start (a convective
+    steady state interpolated and perturbed) and a tight inner tolerance keep the cycles long.  A threshold of
+    1e-2 was measured to lose orthogonality entirely on this problem (|V^T V - I| = 1): classical Gram-Schmidt
+    compounds each skipped pass's loss."""
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     torch = cuda
     G = load_golden("cont_tau1.npz")
@@ -117,15 +117,14 @@ def test_krylov_basis_stays_orthonormal(cuda, eta):
     rng = np.random.default_rng(9)
     Xs = np.stack([X + 1e-2 * np.linalg.norm(X) / np.sqrt(X.size) * rng.standard_normal(X.size) for _ in range(B)])
     p = Plan(N_fm, N_r, d, 1.0, Pr, Tau, precision="mixed")
-    p.set_reorth_eta(eta)
     Xt = torch.from_numpy(Xs).cuda()
     Ra_t = torch.tensor([Ra - 100.0, Ra, Ra + 100.0], dtype=torch.float64, device="cuda")
     p.newton(Xt, Ra_t, Ra_s, tol=1e-12, restart=50, gmres_rtol=1e-13, max_newton=1, max_restarts=2, mixed_matvec=2)
     worst = 0.0
     for b in range(B):
         V = p.krylov_basis(b, 64)
-        assert V.shape[0] == 50, V.shape
+        assert V.shape[0] >= 40, V.shape                 # a cycle stops early only once the target is met
         err = float((V @ V.T - torch.eye(V.shape[0], dtype=torch.float64, device="cuda")).abs().max())
         worst = max(worst, err)
-    print(f"eta={eta:.3g}: max |V^T V - I| over {B} shells, 50 columns: {worst:.2e}")
+    print(f"max |V^T V - I| over {B} shells, cycles of 40-50 columns: {worst:.2e}")
     assert worst <= 1e-10
