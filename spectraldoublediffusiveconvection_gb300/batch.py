@@ -80,14 +80,15 @@ class ShellBatch:
             self.groups.append(g)
         # Starting point of the tuning (measured on the 64-shell mixed batch of N_r in {20..36}, N_theta in
         # {64..384}): the groups' launches share the GPU inside one graph, so the nonlinear term runs as the
-        # fused row kernel once the batch fills the SMs; the chains use the split-row layout, and chunked
-        # chains for N_theta >= 256 with the FP32 nonlinear term, where the long chains of the largest
-        # shells set the critical path (84k vs 77k shell-steps/s); in FP64 the nonlinear term dominates
-        # and chunking does not pay.
+        # fused row kernel once the batch fills the SMs; the chains run in the reference's order of
+        # operations (layout 6: 4 nr^2 multiply-adds per mode instead of 7; the library runs layout 5 where
+        # the right-hand side is fused or FP32), and chunked chains for N_theta >= 256 with the FP32
+        # nonlinear term, where the long chains of the largest shells set the critical path (84k vs 77k
+        # shell-steps/s); in FP64 the nonlinear term dominates and chunking does not pay.
         sms = _torch().cuda.get_device_properties(self.device).multi_processor_count
         total_rows = sum(g.plan.nr * len(g.idx) for g in self.groups)
         for g in self.groups:
-            g.plan.set_chain_layout(2 if (precision == "mixed" and g.plan.N_fm >= 256) else 5)
+            g.plan.set_chain_layout(2 if (precision == "mixed" and g.plan.N_fm >= 256) else 6)
             g.plan.set_fx_split(1 if 2 * total_rows > sms else 0)
         self.graph = None
         self.steps_per_launch = 0
@@ -97,8 +98,9 @@ class ShellBatch:
 
     def apply_tuning(self, tuning):
         """Per-shape kernel choices of an earlier autotune() (its returned dict), e.g. of a scratch batch
-        of the same shapes: a batch object that went through tuning itself was measured to run some 8%
-        slower afterwards with the same choices (cause not found), a fresh one with them does not."""
+        of the same shapes.  A batch timed straight after its own tuning ran some 8% slower than a fresh
+        batch with the same choices; timed again later it ran at the fresh batch's speed (6.65 vs 6.66 ms a
+        launch), so the difference was the GPU's clock state after the tuning bursts, not the batch."""
         for g in self.groups:
             c = tuning.get("N_r=%d,N_theta=%d" % g.shape)
             if c:

@@ -103,6 +103,10 @@ struct StepGraph {
 };
 constexpr int kStepGraphs = 8;
 constexpr int kGraphMinSteps = 8;   // sdd_step replays captured graphs from this many steps on
+// The Arnoldi loop reads the shells' activity flags kFlagLag columns late, so that the host never waits on
+// the column the GPU is computing: the columns run past the last active one are fully masked (no shell takes
+// part) and are not counted as Jacobian products.
+constexpr int kFlagLag = 2;
 
 struct sdd_plan {
   int M, nr, P, ldl, sym, prec, device;
@@ -152,7 +156,8 @@ struct sdd_plan {
   double *kv_V, *kv_w, *kv_r, *kv_part, *kv_nrm2, *kv_small, *kv_dot;
   int* kv_ismall;
   double* h_dbl;      // pinned host scalars
-  int* h_int;         // pinned host flags
+  int* h_int;         // pinned host flags: kFlagLag + 1 slots of B
+  cudaEvent_t flag_ev[kFlagLag + 1];   // one per slot: its flags have arrived
   double *sv_F, *sv_x, *sv_X0, *sv_Xd, *sv_t, *sv_G, *sv_Jmu, *sv_g, *sv_base64, *sv_dev;
   float* sv_base32;
   float* kv_v32;      // mixed plans: [B][ld] FP32 copy of the Krylov vector the next product is applied to
@@ -265,6 +270,10 @@ static void solver_free(sdd_plan* p) {
   cudaFree(p->kv_ismall);
   cudaFreeHost(p->h_dbl);
   cudaFreeHost(p->h_int);
+  for (cudaEvent_t& e : p->flag_ev) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
   p->kv_V = p->kv_w = p->kv_r = p->kv_part = p->kv_nrm2 = p->kv_small = p->kv_dot = nullptr;
   p->sv_F = p->sv_x = p->sv_X0 = p->sv_Xd = p->sv_t = p->sv_G = p->sv_Jmu = p->sv_g = p->sv_base64 = nullptr;
   p->sv_dev = nullptr;
@@ -1202,7 +1211,8 @@ static int solver_reserve(sdd_plan* p, int B, int m) {
   SDD_CUDA(ws_malloc(&p->kv_small, small * sizeof(double)));
   SDD_CUDA(ws_malloc(&p->kv_ismall, (size_t)5 * B * sizeof(int)));
   SDD_CUDA(ws_malloc(&p->h_dbl, (size_t)2 * B * sizeof(double), true));
-  SDD_CUDA(ws_malloc(&p->h_int, (size_t)B * sizeof(int), true));
+  SDD_CUDA(ws_malloc(&p->h_int, (size_t)(kFlagLag + 1) * B * sizeof(int), true));
+  for (cudaEvent_t& e : p->flag_ev) SDD_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   double** v[] = {&p->sv_F, &p->sv_x, &p->sv_Xd, &p->sv_t, &p->sv_G};
   for (double** q : v) SDD_CUDA(ws_malloc(q, vb));
   SDD_CUDA(ws_malloc(&p->sv_X0, (size_t)B * n * sizeof(double)));
@@ -1287,11 +1297,20 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const double* rhs, double* 
       SDD_CUDA(krylov_dots(p->kv_w, 0, p->kv_w, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s, G.active));
       SDD_CUDA(krylov_arnoldi_finish(G, p->kv_nrm2, j, B, s));
       if (j + 1 < m) SDD_CUDA(krylov_scale(p->kv_w, G.inv, p->kv_V + (size_t)(j + 1) * vs, nu, ld, B, s, p->kv_v32));
-      SDD_CUDA(cudaMemcpyAsync(p->h_int, G.active, B * sizeof(int), cudaMemcpyDeviceToHost, s));
-      SDD_CUDA(cudaStreamSynchronize(s));
-      bool act = false;
-      for (int b = 0; b < B; ++b) act = act || p->h_int[b];
-      if (!act) break;
+      // the flags after column j go to slot j; the host reads those of column j - kFlagLag
+      const int slot = j % (kFlagLag + 1);
+      SDD_CUDA(cudaMemcpyAsync(p->h_int + (size_t)slot * B, G.active, B * sizeof(int), cudaMemcpyDeviceToHost, s));
+      SDD_CUDA(cudaEventRecord(p->flag_ev[slot], s));
+      if (j >= kFlagLag) {
+        const int old = (j - kFlagLag) % (kFlagLag + 1);
+        SDD_CUDA(cudaEventSynchronize(p->flag_ev[old]));
+        bool act = false;
+        for (int b = 0; b < B; ++b) act = act || p->h_int[(size_t)old * B + b];
+        if (!act) {                // every shell stopped after column j - kFlagLag: the later columns were void
+          *matvecs -= kFlagLag;
+          break;
+        }
+      }
     }
     SDD_CUDA(krylov_solve_y(G, B, s));
     SDD_CUDA(krylov_add_combination(p->kv_V, vs, x, G.y, m, G.kb, nu, ld, B, s));

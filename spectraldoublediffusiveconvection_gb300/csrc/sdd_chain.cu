@@ -935,7 +935,8 @@ int resolve_chain_layout(const ChainArgs& a, int batch, int nfields) {
   if ((layout == 6 || layout == 7) && chain_ref_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin) layout = 2;
   if (layout != 2 && layout != 3 && layout != 6 && layout != 7 && chain_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin)
     layout = 2;   // whole chain too long for shared memory
-  if (layout == 0) layout = 2 * nfields * batch <= sms ? 4 : 5;
+  // a launch that fills the SMs: the reference-order chains (4 nr^2 multiply-adds per mode instead of 7)
+  if (layout == 0) layout = 2 * nfields * batch <= sms ? 4 : ((a.fuse_rhs || a.g32) ? 5 : 6);
   if (layout == 5 && a.nr > 32) layout = 4;
   return layout;
 }

@@ -23,7 +23,9 @@ def test_mixed_nlin_fx_error_is_fp32_level(cuda):
 
 def test_mixed_trajectory_to_t5(cuda):
     """Config 'mixed precision, N_r=20, N_theta=64': 5000 steps of dt=1e-3 (t = 5); the error against the FP64
-    path (which matches the oracle to 1e-11) is reported and bounded."""
+    path (which matches the oracle to 1e-11) is reported and bounded.  The FP32 nonlinear term enters each step
+    through dt * F, so the drift stays near FP32 rounding times the step's nonlinear share (measured ~1e-8 on
+    GB300, tensor-core contractions included); 5e-8 leaves room for rounding-order changes only."""
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     torch = cuda
     N_fm, N_r = 64, 20
@@ -34,7 +36,7 @@ def test_mixed_trajectory_to_t5(cuda):
     Xd = pd.step(X, 8000.0, 500.0, nsteps=5000)
     e = rel(Xm.cpu().numpy(), Xd.cpu().numpy())
     print(f"mixed vs FP64 relative error at t=5: {e:.3e}")
-    assert e < 1e-5
+    assert e < 5e-8
 
 
 def test_mixed_newton_reaches_fp64_residual(cuda):
