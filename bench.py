@@ -832,6 +832,66 @@ def profile_newton_batch():
     return 0
 
 
+def profile_deriv_tc(batch):
+    """k_deriv_tc alone (the mixed form's 3xTF32 radial contractions) on `batch` FP32 shells of N_r=30,
+    N_theta=256: three warm-up launches, then ten timed with CUDA events.  For
+    ncu --set full -k regex:k_deriv_tc -s 3 -c 1 ... python bench.py --profile-deriv-tc <batch>."""
+    import torch
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    M, N_r = 256, 30
+    nr = N_r - 1
+    device = torch.device("cuda", 0)
+    p = Plan(M, N_r, 2.0, 5e-4, 1.0, 0.01, precision="mixed", device=device)
+    g = torch.Generator(device="cpu").manual_seed(1)
+    X = torch.randn((batch, p.n_state), generator=g, dtype=torch.float32).to(device)
+    out = torch.empty((batch, 4, nr, M), dtype=torch.float32, device=device)
+    for _ in range(3):
+        p.deriv_tc(X, out)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        p.deriv_tc(X, out)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 10
+    io = batch * (3 * M * nr + 4 * nr * M) * 4
+    print(json.dumps({"profile": "deriv_tc", "shells": batch, "ms_per_launch": ms, "algorithmic_bytes": io,
+                      "GB_per_s": io / ms / 1e6, "timed_out": p.tensor_core_timed_out()}))
+    return 0
+
+
+def profile_step_batch(precision, layout, batch=64, steps=1):
+    """The kernels of `steps` IMEX steps of `batch` shells N_r=30, N_theta=256 sharing one plan (dt=1e-3,
+    Ra_T 6000..12000, seeded states 1000+i), launched one by one with an event after each kernel
+    (Plan.kernel_profile) after two warm-up steps; chain layout `layout` (0 automatic), the fused row kernel.
+    For ncu launch lists and per-kernel captures of the batched time step:
+    ncu ... -k regex:<kernel> -c 1 ... python bench.py --profile-step-batch <precision> <layout>."""
+    import numpy as np
+    import torch
+    from spectraldoublediffusiveconvection_gb300.seeds import seeded_state
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    M, N_r = 256, 30
+    device = torch.device("cuda", 0)
+    p = Plan(M, N_r, 2.0, 1e-3, 1.0, 0.01, precision=precision, device=device)
+    p.set_chain_layout(layout)
+    p.set_fx_split(1)
+    X = torch.from_numpy(np.stack([seeded_state(M, N_r - 1, 1000 + i) for i in range(batch)])).to(device)
+    Ra = torch.linspace(6000.0, 12000.0, batch, dtype=torch.float64, device=device)
+    X = p.step(X, Ra, 500.0, nsteps=2)
+    torch.cuda.synchronize()
+    prof = p.kernel_profile(X, Ra, 500.0, steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    p.step(X, Ra, 500.0, nsteps=20)
+    e1.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "step_batch", "precision": precision, "shells": batch,
+                      "chain_layout": p.chain_choice(batch)[0], "graph_ms_per_step": e0.elapsed_time(e1) / 20,
+                      "kernels_ms": {k: v[0] / steps for k, v in prof.items()}}))
+    return 0
+
+
 def main():
     if len(sys.argv) > 1 and sys.argv[1] == "--cpu-worker":
         cpu_worker(float(sys.argv[2]), int(sys.argv[3]), int(sys.argv[4]),
@@ -849,9 +909,15 @@ def main():
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--served-requests", type=int, default=1000)
     ap.add_argument("--profile-newton-batch", action="store_true")
+    ap.add_argument("--profile-deriv-tc", type=int, metavar="SHELLS")
+    ap.add_argument("--profile-step-batch", nargs=2, metavar=("PRECISION", "LAYOUT"))
     args = ap.parse_args()
     if args.profile_newton_batch:
         return profile_newton_batch()
+    if args.profile_deriv_tc:
+        return profile_deriv_tc(args.profile_deriv_tc)
+    if args.profile_step_batch:
+        return profile_step_batch(args.profile_step_batch[0], int(args.profile_step_batch[1]))
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

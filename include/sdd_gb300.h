@@ -104,9 +104,11 @@ int sdd_plan_reserve(sdd_plan* plan, int max_batch);
  * operations (Matrix_Operators.py:1139-1164, 1056-1083: per step D2 f_e, then Linv_j (g_j + b)), without the
  * h = Linv g pre-pass of the other layouts: 4 nr^2 multiply-adds per mode instead of 7, rows over 2 / 4
  * lanes; they need the full FP64 right-hand side, so launches with the fused or the FP32 right-hand side run
- * layout 5.  Set by the batch autotuner; no counterpart in the reference. */
+ * layout 5.  8: the same order of operations with the three chains of one (parity, shell) in one CTA, psi
+ * rows over 2 lanes, T and S one lane per row, so every warp carries about the same work per step (launches
+ * of fewer than three fields run layout 6).  Set by the batch autotuner; no counterpart in the reference. */
 int sdd_plan_set_chain_layout(sdd_plan* plan, int layout);
-/* The layout (1-7) a step of `batch` shells runs under the current setting, with its chunk length and
+/* The layout (1-8) a step of `batch` shells runs under the current setting, with its chunk length and
  * chunks per chain (0 and 1 when not chunked). */
 int sdd_plan_chain_choice(const sdd_plan* plan, int batch, int* layout, int* kc, int* nch);
 /* Mixed plans: the FP32 radial contractions of the nonlinear term (Derivatives, Matrix_Operators.py:698-729)

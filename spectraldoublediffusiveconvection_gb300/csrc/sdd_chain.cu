@@ -286,36 +286,52 @@ __global__ void k_chain(ChainArgs a) {
   }
 }
 
-// Layouts 6 and 7: the chains in the reference's own order of operations, without the h = Linv g pre-pass:
+// Layouts 6, 7 and 8: the chains in the reference's own order of operations, without the h = Linv g pre-pass:
 //   psi (Matrix_Operators.py:1139-1164):  f_e += f_{j+2};  L1f = D2 f_e + bj IR4 f_e;
 //          b = dt bjt (L1f + IR4 bf_e) - bjt IR2 f_e;  f_j = Linv_j (g_j + b);  bf_e += bj f_j + bjt f_e
 //   T, S (Matrix_Operators.py:1056-1083):  b += 2 dt (j+2) f_{j+2};  f_j = Linv_j (g_j - w b)
 // Per mode 4 nr^2 multiply-adds instead of the 7 nr^2 of the pre-pass form (h, then [A B] for psi and
 // Linv b for T/S), at the price of a second dependent matvec per psi step: the form for batches that fill
-// the GPU, where the FP64 work and not a chain's latency sets the time.  Rows split over TPR lanes, one CTA
-// per (field, parity, shell); the Linv blocks stream through a 3-slot cp.async ring, D2 sits in shared
-// memory.  g is the full right-hand side (not the fused form).
+// the GPU, where the FP64 work and not a chain's latency sets the time.  g is the full right-hand side (not
+// the fused form).
+//
+// ref_chain runs one chain (field, parity) of shell b on `nt` threads (whole warps) of a CTA, thread t of
+// them, rows split over TPR lanes, synchronising on named barrier `bar` (nt > 32) or the warp; its own
+// shared memory `sm` (ref_group_doubles): a 3-slot cp.async ring of Linv blocks, D2 (psi), the per-step
+// scalars and two operand buffers.  Every cp.async of the chain is issued and waited for by the chain's own
+// threads, so chains sharing a CTA never wait on one another.
+__device__ __forceinline__ void group_sync(int bar, int nt) {
+  if (nt <= 32) __syncwarp();
+  else asm volatile("bar.sync %0, %1;\n" ::"r"(bar), "r"(nt) : "memory");
+}
+
+__device__ __forceinline__ void copy_block_g(double* dst, const double* src, int ndouble, int t, int nt) {
+  const int nchunk = ndouble / 2;  // ndouble is even (ldl even)
+  for (int c = t; c < nchunk; c += nt) cp_async16(dst + 2 * c, src + 2 * c);
+}
+
+__host__ __device__ inline size_t ref_group_doubles(int M, int nr, int ldl, bool a4) {
+  const size_t blk = (size_t)nr * ldl;
+  const size_t ns = (size_t)((M + 1) / 2);
+  return (a4 ? 4 : 3) * blk + 4 * (ns + 1) + (a4 ? 4 : 2) * (size_t)nr;
+}
+
 template <int TPR>
-__global__ void k_chain_ref(ChainArgs a) {
-  extern __shared__ __align__(16) double csm[];
-  const int field = a.field0 + (blockIdx.x >> 1);
-  const int par = blockIdx.x & 1;
-  const int b = blockIdx.y;
-  if (a.active && !a.active[b]) return;
+__device__ __forceinline__ void ref_chain(const ChainArgs& a, int field, int par, int b, int t, int nt, int bar,
+                                          double* sm) {
   const int M = a.M, nr = a.nr, ldl = a.ldl;
   const bool a4 = (field == 0);
   const size_t foff = (size_t)field * a.field_off;
   double* f = a.f + (size_t)b * a.f_stride + foff;
   const double* sub = a.sub ? a.sub + (size_t)b * a.sub_stride + foff : nullptr;
   float* f32 = a.f32 ? a.f32 + (size_t)b * a.f32_stride + foff : nullptr;
-  const int tid = threadIdx.x;
-  const int i = tid / TPR, q = tid % TPR;
+  const int i = t / TPR, q = t % TPR;
   const bool row_ok = i < nr;
   const bool lead = row_ok && q == 0;
   const int ir = row_ok ? i : 0;
   const int S = (M - par + 1) / 2;
   if (a.sym && !(a4 ? par == 0 : par == 1)) {          // symmetric: the other parity's rows are zero
-    for (int e = tid; e < S * nr; e += blockDim.x) {
+    for (int e = t; e < S * nr; e += nt) {
       const int st = e / nr, c = e - st * nr;
       f[(size_t)(M - 1 - (par + 2 * st)) * nr + c] = 0.0;
       if (f32) f32[(size_t)(M - 1 - (par + 2 * st)) * nr + c] = 0.0f;
@@ -323,19 +339,19 @@ __global__ void k_chain_ref(ChainArgs a) {
     return;
   }
   const int blk = nr * ldl;
-  double* Lb0 = csm;                                   // 3-slot ring of Linv blocks
+  double* Lb0 = sm;                                    // 3-slot ring of Linv blocks
   double* D2s = Lb0 + 3 * blk;                         // psi: D2 (transposed), nr x ldl
   double* cf = D2s + (a4 ? blk : 0);                   // per-step scalars, 4 per step
   double* xv = cf + 4 * (size_t)(S + 1);               // 2 buffers of f_e (psi)
-  double* yv = xv + 2 * nr;                            // 2 buffers of the Linv matvec's operand
+  double* yv = xv + (a4 ? 2 * nr : 0);                 // 2 buffers of the Linv matvec's operand
   const double* Mat = a4 ? a.LinvA4 : (field == 1 ? a.LinvT : a.LinvS);
   const double* coef = a4 ? a.coefA4 : (field == 1 ? a.coefT : a.coefS);
-  copy_block(Lb0, Mat + (size_t)par * blk, blk);
-  if (a4) copy_block(D2s, a.D2A4, blk);
+  copy_block_g(Lb0, Mat + (size_t)par * blk, blk, t, nt);
+  if (a4) copy_block_g(D2s, a.D2A4, blk, t, nt);
   cp_async_commit();
-  if (S > 1) copy_block(Lb0 + blk, Mat + (size_t)(par + 2) * blk, blk);
+  if (S > 1) copy_block_g(Lb0 + blk, Mat + (size_t)(par + 2) * blk, blk, t, nt);
   cp_async_commit();
-  for (int e = tid; e < 4 * (S + 1); e += blockDim.x) {
+  for (int e = t; e < 4 * (S + 1); e += nt) {
     const int jj = par + 2 * (e >> 2);
     cf[e] = jj < M ? coef[(size_t)jj * 4 + (e & 3)] : 0.0;
   }
@@ -350,8 +366,8 @@ __global__ void k_chain_ref(ChainArgs a) {
     const double* cur = Lb0 + (st % 3) * blk;
     double* yb = yv + (st & 1) * nr;
     cp_async_wait<1>();
-    chain_sync();                                      // Linv_jj (and D2) landed; step st-1 done
-    if (st + 2 < S) copy_block(Lb0 + ((st + 2) % 3) * blk, Mat + (size_t)(jj + 4) * blk, blk);
+    group_sync(bar, nt);                               // Linv_jj (and D2) landed; step st-1 done
+    if (st + 2 < S) copy_block_g(Lb0 + ((st + 2) % 3) * blk, Mat + (size_t)(jj + 4) * blk, blk, t, nt);
     cp_async_commit();
     const double gi = gn0;
     gn0 = gn1;
@@ -363,18 +379,18 @@ __global__ void k_chain_ref(ChainArgs a) {
         fe += fprev;                                   // f_e += f_{j+2}
         double* xb = xv + (st & 1) * nr;
         if (lead) xb[i] = fe;
-        chain_sync();
+        group_sync(bar, nt);
         double z = 0.0;
 #pragma unroll 8
         for (int c = q; c < nr; c += TPR) z = fma(D2s[c * ldl + ir], xb[c], z);
         z = group_sum<TPR>(z);
         const double L1f = fma(bj * ir4, fe, z);      // (D2 + bj IR4) f_e
-        const double t = fma(ir4, bfe, L1f);           // + IR4 bf_e
-        const double bt = fma(c1, t, -(bjt * ir2 * fe));
+        const double tt = fma(ir4, bfe, L1f);          // + IR4 bf_e
+        const double bt = fma(c1, tt, -(bjt * ir2 * fe));
         y = gi + bt;
       }
       if (lead) yb[i] = y;
-      chain_sync();
+      group_sync(bar, nt);
       double acc = 0.0;
 #pragma unroll 8
       for (int c = q; c < nr; c += TPR) acc = fma(cur[c * ldl + ir], yb[c], acc);
@@ -388,7 +404,7 @@ __global__ void k_chain_ref(ChainArgs a) {
     } else {
       const double y = fma(-cf[4 * st + 1], fe, gi);  // g - w b
       if (lead) yb[i] = y;
-      chain_sync();
+      group_sync(bar, nt);
       double acc = 0.0;
 #pragma unroll 8
       for (int c = q; c < nr; c += TPR) acc = fma(cur[c * ldl + ir], yb[c], acc);
@@ -401,9 +417,9 @@ __global__ void k_chain_ref(ChainArgs a) {
     }
   }
   cp_async_wait<0>();
-  if (sub) {  // Newton residual: f -= sub (the block's own writes are visible after the barrier)
-    __syncthreads();
-    for (int e = tid; e < S * nr; e += blockDim.x) {
+  if (sub) {  // Newton residual: f -= sub (the group's own writes are visible after the barrier)
+    group_sync(bar, nt);
+    for (int e = t; e < S * nr; e += nt) {
       const int st = e / nr, c = e - st * nr;
       const size_t o = (size_t)(M - 1 - (par + 2 * st)) * nr + c;
       f[o] -= sub[o];
@@ -411,10 +427,38 @@ __global__ void k_chain_ref(ChainArgs a) {
   }
 }
 
+// Layouts 6 / 7: one chain per CTA (field, parity, shell), rows over TPR = 2 / 4 lanes.
+template <int TPR>
+__global__ void k_chain_ref(ChainArgs a) {
+  extern __shared__ __align__(16) double csm[];
+  const int b = blockIdx.y;
+  if (a.active && !a.active[b]) return;
+  ref_chain<TPR>(a, a.field0 + (blockIdx.x >> 1), blockIdx.x & 1, b, threadIdx.x, blockDim.x, 0, csm);
+}
+
+// Layout 8: the three chains of one (parity, shell) in one CTA, each on its own warps: psi on wp warps with
+// rows over 2 lanes (two dependent matvecs of nr/2 multiply-adds per lane and step), T and S on wt warps each
+// with one lane per row (one matvec of nr multiply-adds).  Every warp then carries about the same dependent
+// FP64 work per step, and a CTA puts one warp on each SM sub-partition (nr <= 32: 2 + 1 + 1 warps), where
+// one CTA per (field, parity, shell) leaves the T/S warps idle half the time and stacks psi warps on shared
+// sub-partitions.  Named barriers 1-3, one per chain.
+__global__ void k_chain_shell(ChainArgs a, int wp, int wt) {
+  extern __shared__ __align__(16) double csm[];
+  const int par = blockIdx.x, b = blockIdx.y;
+  if (a.active && !a.active[b]) return;
+  const int w = threadIdx.x >> 5;
+  const size_t sp = ref_group_doubles(a.M, a.nr, a.ldl, true), sg = ref_group_doubles(a.M, a.nr, a.ldl, false);
+  if (w < wp) ref_chain<2>(a, 0, par, b, threadIdx.x, 32 * wp, 1, csm);
+  else if (w < wp + wt) ref_chain<1>(a, 1, par, b, threadIdx.x - 32 * wp, 32 * wt, 2, csm + sp);
+  else ref_chain<1>(a, 2, par, b, threadIdx.x - 32 * (wp + wt), 32 * wt, 3, csm + sp + sg);
+}
+
 static size_t chain_ref_smem_bytes(int M, int nr, int ldl) {
-  const size_t blk = (size_t)nr * ldl;
-  const size_t ns = (size_t)((M + 1) / 2);
-  return (4 * blk + 4 * (ns + 1) + 4 * (size_t)nr) * sizeof(double);
+  return ref_group_doubles(M, nr, ldl, true) * sizeof(double);
+}
+
+static size_t chain_shell_smem_bytes(int M, int nr, int ldl) {
+  return (ref_group_doubles(M, nr, ldl, true) + 2 * ref_group_doubles(M, nr, ldl, false)) * sizeof(double);
 }
 
 size_t chain_smem_bytes(int M, int nr, int ldl) {
@@ -928,6 +972,10 @@ int resolve_chain_layout(const ChainArgs& a, int batch, int nfields) {
   int layout = a.layout;
   const ChunkSet& c2 = a.cset[0];
   const ChunkSet& c3 = a.cset[1];
+  // layout 8 needs all three fields of a step with full right-hand sides, and its three rings in one CTA
+  if (layout == 8 && (nfields != 3 || a.field0 != 0 || a.fuse_rhs || a.g32 ||
+                      chain_shell_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin))
+    layout = 6;
   if (layout == 0 && c3.nch > 1 && c3.GA4 && 2 * nfields * batch * c3.nch <= 2 * sms) layout = 3;
   if (layout == 0 && c2.nch > 1 && c2.GA4 && 2 * nfields * batch * c2.nch <= 2 * sms) layout = 2;
   // layouts 6 / 7 need the full right-hand side in FP64: with the fused or the FP32 one, the pre-pass form
@@ -944,6 +992,18 @@ int resolve_chain_layout(const ChainArgs& a, int batch, int nfields) {
 cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStream_t s) {
   ChainArgs a = a_in;
   const int layout = resolve_chain_layout(a, batch, nfields);
+  if (layout == 8) {                  // the reference's order, three chains per CTA
+    if (a.fuse_rhs || a.g32 || !a.D2A4 || nfields != 3 || a.field0 != 0) return cudaErrorInvalidValue;
+    const int wp = (2 * a.nr + 31) / 32, wt = (a.nr + 31) / 32;
+    static unsigned long long done = 0;
+    cudaError_t e;
+    if ((e = ensure_smem_attr(k_chain_shell, &done)) != cudaSuccess) return e;
+    e = launch_kernel(k_chain_shell, dim3(2, batch), dim3(32 * (wp + 2 * wt)), chain_shell_smem_bytes(a.M, a.nr, a.ldl),
+                      s, a, wp, wt);
+    ktimer_mark(SDD_K_CHAIN, s);
+    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+  }
   if (layout == 6 || layout == 7) {   // the reference's order, no h pre-pass (full right-hand sides only)
     if (a.fuse_rhs || a.g32 || !a.D2A4) return cudaErrorInvalidValue;
     const int tpr = layout == 6 ? 2 : 4;
