@@ -95,8 +95,9 @@ int sdd_plan_destroy(sdd_plan* plan);
 /* Pre-allocates the plan's workspace for up to max_batch shells (otherwise grown on first use). */
 int sdd_plan_reserve(sdd_plan* plan, int max_batch);
 /* Chain-kernel layout of the implicit solves: 0 automatic (chunked while its CTAs fit the GPU at two per
- * SM, layout 3 before 2, else split rows over 4 warps when the launch leaves SMs idle, else layout 6, or 5
- * where the right-hand side is fused or FP32),
+ * SM, layout 3 before 2, else split rows over 4 warps when the launch leaves SMs idle, else layout 8 (6 for
+ * launches of fewer than three fields or where its shared memory does not fit, 5 where the right-hand side
+ * is fused or FP32)),
  * 1 one lane per row, 2 chunked (each chain cut into chunks that run concurrently, joined by a short
  * sequential carried-state recurrence), 3 chunked with shorter chunks joined by a parallel carry
  * (precomputed products of the chunk maps, all applied at once), 4 split rows over 4 warps, 5 split rows

@@ -81,14 +81,15 @@ class ShellBatch:
         # Starting point of the tuning (measured on the 64-shell mixed batch of N_r in {20..36}, N_theta in
         # {64..384}): the groups' launches share the GPU inside one graph, so the nonlinear term runs as the
         # fused row kernel once the batch fills the SMs; the chains run in the reference's order of
-        # operations (layout 6: 4 nr^2 multiply-adds per mode instead of 7; the library runs layout 5 where
-        # the right-hand side is fused or FP32), and chunked chains for N_theta >= 256 with the FP32
+        # operations, a shell's three chains of one parity per CTA (layout 8: 4 nr^2 multiply-adds per mode
+        # instead of 7; the library runs layout 5 where the right-hand side is fused or FP32, and layout 6
+        # where the three rings do not fit a CTA), and chunked chains for N_theta >= 256 with the FP32
         # nonlinear term, where the long chains of the largest shells set the critical path (84k vs 77k
         # shell-steps/s); in FP64 the nonlinear term dominates and chunking does not pay.
         sms = _torch().cuda.get_device_properties(self.device).multi_processor_count
         total_rows = sum(g.plan.nr * len(g.idx) for g in self.groups)
         for g in self.groups:
-            g.plan.set_chain_layout(2 if (precision == "mixed" and g.plan.N_fm >= 256) else 6)
+            g.plan.set_chain_layout(2 if (precision == "mixed" and g.plan.N_fm >= 256) else 8)
             g.plan.set_fx_split(1 if 2 * total_rows > sms else 0)
         self.graph = None
         self.steps_per_launch = 0

@@ -184,13 +184,13 @@ def test_matvec_variants_agree_across_batch_sizes(cuda, layout):
 
 def test_automatic_layout_choice(cuda):
     """sdd_plan_chain_choice: one production shell runs the parallel-carry chunks (layout 3, kc ~ sqrt(S/2)),
-    a batch too large for its CTAs falls back to whole chains in the reference's order (layout 6); forced
-    layouts are reported as set."""
+    a batch too large for its CTAs falls back to whole chains in the reference's order, three per CTA
+    (layout 8); forced layouts are reported as set."""
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     p = Plan(256, 30, 2.0, 5e-4, 1.0, 0.01)
     assert p.chain_choice(1) == (3, 8, 16)
     lay, kc, nch = p.chain_choice(64)
-    assert lay == 6 and (kc, nch) == (0, 1)
+    assert lay == 8 and (kc, nch) == (0, 1)
     p.set_chain_layout(2)
     assert p.chain_choice(1) == (2, 16, 8)
     p.set_chain_layout(3)
