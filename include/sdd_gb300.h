@@ -120,6 +120,15 @@ int sdd_plan_set_tensor_cores(sdd_plan* plan, int on);
 /* 1 in *timed_out if a tensor-core kernel of this plan gave up waiting for its matrix products (its outputs
  * were then NaN); 0 otherwise.  Synchronous. */
 int sdd_plan_tensor_core_status(const sdd_plan* plan, int* timed_out);
+/* How the Newton / continuation GMRES products of this plan ran so far: captured into a CUDA graph (and
+ * launched), replayed from a captured graph, or launched kernel by kernel (a product that could not be
+ * captured).  The products of every Arnoldi column read one fixed vector, so a solve captures a product
+ * once per batch size and kind and replays it for the other columns and later solves.  No counterpart in
+ * the reference. */
+int sdd_plan_product_graph_stats(const sdd_plan* plan, long long* captured, long long* replayed, long long* direct);
+/* 1 (the default): the GMRES products run as captured CUDA graphs; 0: kernel by kernel (the same kernels
+ * and arguments, so the same results).  No counterpart in the reference. */
+int sdd_plan_set_product_graphs(sdd_plan* plan, int on);
 /* Nonlinear-term kernel choice: 0 automatic (split while the fused kernel's nr*batch CTAs would fill
  * under half the SMs), 1 the fused row kernel (one CTA per radial row), 2 split (7 CTAs per radial row:
  * five paired inverse transforms, then two paired forward transforms).  Results are identical bit for

@@ -83,6 +83,9 @@ SIGNATURES = [
     ("sdd_plan_set_fx_split", _I, [_VP, _I]),
     ("sdd_plan_set_tensor_cores", _I, [_VP, _I]),
     ("sdd_plan_tensor_core_status", _I, [_VP, ctypes.POINTER(_I)]),
+    ("sdd_plan_set_product_graphs", _I, [_VP, _I]),
+    ("sdd_plan_product_graph_stats", _I, [_VP, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+                                          ctypes.POINTER(ctypes.c_longlong)]),
     ("sdd_plan_chain_choice", _I, [_VP, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     ("sdd_plan_base_cache_elems", ctypes.c_size_t, [_VP]),
     ("sdd_nlin_fx", _I, [_VP, _I, _VP, _VP, _VP, _VP]),

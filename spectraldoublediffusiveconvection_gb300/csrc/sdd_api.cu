@@ -102,6 +102,15 @@ struct StepGraph {
   unsigned long long last_use;
 };
 constexpr int kStepGraphs = 8;
+// CUDA graphs of the GMRES products: the launches of one Jacobian (or bordered) product, keyed by what they
+// bake in (the kind of product, the batch, every pointer it reads or writes, the plan's kernel choices)
+struct MvGraph {
+  cudaGraphExec_t exec;
+  int kind, batch, layout, fx_split, use_tc;
+  const void* ptr[7];               // v, out, active, v32, Ra, Ras, base
+  unsigned long long last_use;
+};
+constexpr int kMvGraphs = 8;
 constexpr int kGraphMinSteps = 8;   // sdd_step replays captured graphs from this many steps on
 // The Arnoldi loop reads the shells' activity flags kFlagLag columns late, so that the host never waits on
 // the column the GPU is computing: the columns run past the last active one are fully masked (no shell takes
@@ -155,6 +164,7 @@ struct sdd_plan {
   int kv_last_B;      // batch of the last GMRES solve (the layout sdd_krylov_basis reads)
   double *kv_V, *kv_w, *kv_r, *kv_part, *kv_nrm2, *kv_small, *kv_dot;
   int* kv_ismall;
+  int* kv_ticket;     // [B] per-shell CTA counters of the one-launch reductions (zero between launches)
   double* h_dbl;      // pinned host scalars
   int* h_int;         // pinned host flags: kFlagLag + 1 slots of B
   cudaEvent_t flag_ev[kFlagLag + 1];   // one per slot: its flags have arrived
@@ -167,6 +177,10 @@ struct sdd_plan {
   double ke_scale;
   // CUDA graphs of repeated time steps (sdd_step): A -> xtmp -> A pairs, A = the caller's output
   StepGraph graphs[kStepGraphs];
+  MvGraph mv_graphs[kMvGraphs];
+  long long mv_count[3];            // GMRES products: captured into a graph, replayed from one, run directly
+  int mv_graphs_off;                // 1: run the GMRES products kernel by kernel (sdd_plan_set_product_graphs)
+  double* kv_vin;     // [B][ld] the Krylov vector the next product reads (a fixed address for its graph)
   unsigned long long graph_clock;
   cudaStream_t cap_stream;          // private capture stream (created on first use)
 };
@@ -261,13 +275,19 @@ static int upload_linv32(float** dst, const double* src, int M, int nr, int ldl)
   return SDD_OK;
 }
 
+static void clear_mv_graphs(sdd_plan* p);
+
 static void solver_free(sdd_plan* p) {
+  clear_mv_graphs(p);               // they bake in the solver workspace
+  cudaFree(p->kv_vin);
+  p->kv_vin = nullptr;
   double* d[] = {p->kv_V, p->kv_w, p->kv_r, p->kv_part, p->kv_nrm2, p->kv_small, p->kv_dot, p->sv_F, p->sv_x,
                  p->sv_X0, p->sv_Xd, p->sv_t, p->sv_G, p->sv_Jmu, p->sv_g, p->sv_base64, p->sv_dev};
   for (double* x : d) cudaFree(x);
   cudaFree(p->sv_base32);
   cudaFree(p->kv_v32);
   cudaFree(p->kv_ismall);
+  cudaFree(p->kv_ticket);
   cudaFreeHost(p->h_dbl);
   cudaFreeHost(p->h_int);
   for (cudaEvent_t& e : p->flag_ev) {
@@ -280,9 +300,17 @@ static void solver_free(sdd_plan* p) {
   p->sv_base32 = nullptr;
   p->kv_v32 = nullptr;
   p->kv_ismall = nullptr;
+  p->kv_ticket = nullptr;
   p->h_dbl = nullptr;
   p->h_int = nullptr;
   p->sv_B = p->sv_m = 0;
+}
+
+static void clear_mv_graphs(sdd_plan* p) {
+  for (MvGraph& g : p->mv_graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g.exec = nullptr;
+  }
 }
 
 static void clear_step_graphs(sdd_plan* p) {
@@ -290,6 +318,7 @@ static void clear_step_graphs(sdd_plan* p) {
     if (p->graphs[i].exec) cudaGraphExecDestroy(p->graphs[i].exec);
     p->graphs[i].exec = nullptr;
   }
+  clear_mv_graphs(p);
 }
 
 static void free_plan(sdd_plan* p) {
@@ -671,6 +700,20 @@ int sdd_plan_tensor_core_status(const sdd_plan* p, int* timed_out) {
   if (!p || !timed_out) return SDD_ERR_ARG;
   *timed_out = 0;
   if (p->tc_err) SDD_CUDA(cudaMemcpy(timed_out, p->tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+  return SDD_OK;
+}
+
+int sdd_plan_set_product_graphs(sdd_plan* p, int on) {
+  if (!p || on < 0 || on > 1) return SDD_ERR_ARG;
+  p->mv_graphs_off = !on;
+  return SDD_OK;
+}
+
+int sdd_plan_product_graph_stats(const sdd_plan* p, long long* captured, long long* replayed, long long* direct) {
+  if (!p || !captured || !replayed || !direct) return SDD_ERR_ARG;
+  *captured = p->mv_count[0];
+  *replayed = p->mv_count[1];
+  *direct = p->mv_count[2];
   return SDD_OK;
 }
 
@@ -1204,12 +1247,16 @@ static int solver_reserve(sdd_plan* p, int B, int m) {
   SDD_CUDA(ws_malloc(&p->kv_w, vb));
   SDD_CUDA(cudaMemset(p->kv_w, 0, vb));   // shells a masked matvec skips keep finite values here
   SDD_CUDA(ws_malloc(&p->kv_r, vb));
-  SDD_CUDA(ws_malloc(&p->kv_part, (size_t)B * (m + 1) * nchunk * sizeof(double)));
+  const size_t nsub = (ld + kSubChunk - 1) / kSubChunk;       // partials of the fused update-and-norm
+  SDD_CUDA(ws_malloc(&p->kv_part, (size_t)B * std::max((size_t)(m + 1) * nchunk, nsub) * sizeof(double)));
   SDD_CUDA(ws_malloc(&p->kv_nrm2, (size_t)B * sizeof(double)));
   SDD_CUDA(ws_malloc(&p->kv_dot, (size_t)B * sizeof(double)));
   const size_t small = (size_t)B * ((size_t)(m + 1) * m + 3 * (m + 1) + 3 * m + 4);
   SDD_CUDA(ws_malloc(&p->kv_small, small * sizeof(double)));
   SDD_CUDA(ws_malloc(&p->kv_ismall, (size_t)5 * B * sizeof(int)));
+  SDD_CUDA(ws_malloc(&p->kv_ticket, (size_t)B * sizeof(int)));
+  SDD_CUDA(ws_malloc(&p->kv_vin, vb));
+  SDD_CUDA(cudaMemset(p->kv_ticket, 0, (size_t)B * sizeof(int)));
   SDD_CUDA(ws_malloc(&p->h_dbl, (size_t)2 * B * sizeof(double), true));
   SDD_CUDA(ws_malloc(&p->h_int, (size_t)(kFlagLag + 1) * B * sizeof(int), true));
   for (cudaEvent_t& e : p->flag_ev) SDD_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1253,14 +1300,77 @@ static GmresState gmres_state(sdd_plan* p, int B, int m) {
 // Device matvec on B shells: out = A v (vectors of stride ld); shells whose flag in `active` (device,
 // nullable) is 0 may be skipped, their part of out left as it was.  v32 (nullable): v rounded to FP32,
 // same strides, for matvecs that work in FP32.
-using MatVec = std::function<int(const double* v, double* out, const int* active, const float* v32)>;
+using MatVec = std::function<int(const double* v, double* out, const int* active, const float* v32, cudaStream_t st)>;
+
+// What a product graph bakes in besides its operands: its kind (0: never captured) and the parameter / base
+// state pointers the product reads.
+struct MvSpec {
+  int kind;
+  const void* Ra;
+  const void* Ras;
+  const void* base;
+};
+
+// Runs A on stream s.  A product of a nonzero kind is captured once per key on the plan's private stream
+// (thread-local capture: other host threads are unaffected) and replayed as one graph launch; a product
+// that cannot be captured runs its launches directly.
+static int run_mv(sdd_plan* p, const MatVec& A, const MvSpec& spec, int B, const double* v, double* out,
+                  const int* active, const float* v32, cudaStream_t s) {
+  auto direct = [&]() {
+    ++p->mv_count[2];
+    return A(v, out, active, v32, s);
+  };
+  if (!spec.kind || p->mv_graphs_off) return direct();
+  const void* key[7] = {v, out, active, v32, spec.Ra, spec.Ras, spec.base};
+  MvGraph* slot = nullptr;
+  for (MvGraph& g : p->mv_graphs) {
+    if (g.exec && g.kind == spec.kind && g.batch == B && g.layout == p->chain_layout && g.fx_split == p->fx_split &&
+        g.use_tc == p->use_tc && std::equal(key, key + 7, g.ptr)) {
+      g.last_use = ++p->graph_clock;
+      ++p->mv_count[1];
+      SDD_CUDA(cudaGraphLaunch(g.exec, s));
+      return SDD_OK;
+    }
+    if (!slot || !g.exec || (slot->exec && g.last_use < slot->last_use)) slot = &g;
+  }
+  if (!p->cap_stream && cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    p->cap_stream = nullptr;
+    cudaGetLastError();
+    return direct();
+  }
+  cudaStream_t cs = p->cap_stream;
+  if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return direct();
+  }
+  const int st = A(v, out, active, v32, cs);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(cs, &graph);
+  cudaGraphExec_t exec = nullptr;
+  if (st != SDD_OK || ec != cudaSuccess || !graph || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) exec = nullptr;
+  if (graph) cudaGraphDestroy(graph);
+  cudaGetLastError();
+  if (st != SDD_OK || !exec) return direct();   // not capturable: the launches themselves
+  if (slot->exec) cudaGraphExecDestroy(slot->exec);
+  slot->exec = exec;
+  slot->kind = spec.kind;
+  slot->batch = B;
+  slot->layout = p->chain_layout;
+  slot->fx_split = p->fx_split;
+  slot->use_tc = p->use_tc;
+  std::copy(key, key + 7, slot->ptr);
+  slot->last_use = ++p->graph_clock;
+  ++p->mv_count[0];
+  SDD_CUDA(cudaGraphLaunch(exec, s));
+  return SDD_OK;
+}
 
 // Restarted GMRES(m), classical Gram-Schmidt with a conditional second pass, for the shells with
 // solve[b] != 0: A x = rhs, x starts at 0, inner stop |r_b| <= target[b] (absolute).  x, rhs have stride
 // ld with nu used doubles.  resid (host) receives the final residual estimates.
-static int gmres_solve(sdd_plan* p, const MatVec& A, const double* rhs, double* x, int B, int nu, int ld, int m,
-                       int max_restarts, const std::vector<double>& target, const std::vector<int>& solve,
-                       cudaStream_t s, int* matvecs, std::vector<double>& resid) {
+static int gmres_solve(sdd_plan* p, const MatVec& A, const MvSpec& spec, const double* rhs, double* x, int B, int nu,
+                       int ld, int m, int max_restarts, const std::vector<double>& target,
+                       const std::vector<int>& solve, cudaStream_t s, int* matvecs, std::vector<double>& resid) {
   GmresState G = gmres_state(p, B, m);
   p->kv_last_B = B;
   const size_t vs = (size_t)B * ld;
@@ -1273,30 +1383,33 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const double* rhs, double* 
   for (int cyc = 0; cyc < max_restarts; ++cyc) {
     const double* r = rhs;
     if (cyc > 0) {                                   // r = rhs - A x
-      if ((st = A(x, p->kv_w, G.solve, nullptr))) return st;
+      if ((st = run_mv(p, A, spec, B, x, p->kv_w, G.solve, nullptr, s))) return st;
       ++*matvecs;
       SDD_CUDA(krylov_sub(rhs, p->kv_w, p->kv_r, vs, s));
       r = p->kv_r;
     }
-    SDD_CUDA(krylov_dots(r, 0, r, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s));
+    SDD_CUDA(krylov_dots(r, 0, r, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s, nullptr, p->kv_ticket));
     SDD_CUDA(krylov_cycle_start(G, p->kv_nrm2, B, s));
-    SDD_CUDA(krylov_scale(r, G.inv, p->kv_V, nu, ld, B, s, p->kv_v32));
+    SDD_CUDA(krylov_scale(r, G.inv, p->kv_V, nu, ld, B, s, p->kv_v32, p->kv_vin));
     for (int j = 0; j < m; ++j) {
-      double* Vj = p->kv_V + (size_t)j * vs;
-      if ((st = A(Vj, p->kv_w, G.active, p->kv_v32))) return st;   // kv_v32: Vj in FP32
+      // kv_vin (and kv_v32 in FP32) hold V_j: a fixed address, so one captured graph serves every column
+      if ((st = run_mv(p, A, spec, B, p->kv_vin, p->kv_w, G.active, p->kv_v32, s))) return st;
       ++*matvecs;
-      // shells whose Arnoldi process has stopped skip the Gram-Schmidt work (krylov_arnoldi_finish ignores them)
-      SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.hcol, m + 1, 0, s, G.active));
-      SDD_CUDA(krylov_sub_combination(p->kv_V, vs, p->kv_w, G.hcol, m + 1, nu, ld, j + 1, B, s, G.active));
-      // the second pass only for the shells whose first pass cancelled w below reorth_eta of its norm
-      // (the others get zero second projections)
-      SDD_CUDA(krylov_dots(p->kv_w, 0, p->kv_w, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s, G.active));
-      SDD_CUDA(krylov_reorth_mask(G, p->kv_nrm2, j, p->reorth_eta, B, s));
-      SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.h2, m + 1, 0, s, G.reo));
-      SDD_CUDA(krylov_sub_combination(p->kv_V, vs, p->kv_w, G.h2, m + 1, nu, ld, j + 1, B, s, G.reo));
-      SDD_CUDA(krylov_dots(p->kv_w, 0, p->kv_w, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s, G.active));
+      // shells whose Arnoldi process has stopped skip the Gram-Schmidt work (krylov_arnoldi_finish ignores them);
+      // each pass is two launches: the projections, then the update with the new norm (and after the first
+      // pass the flag of the shells that repeat it: those whose first pass cancelled w below reorth_eta of
+      // its norm; the others get zero second projections)
+      SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.hcol, m + 1, 0, s, G.active,
+                           p->kv_ticket));
+      SDD_CUDA(krylov_sub_norm(p->kv_V, vs, p->kv_w, G.hcol, m + 1, nu, ld, j + 1, B, G.active, G.active, p->kv_part,
+                               p->kv_ticket, p->kv_nrm2, &G, j, p->reorth_eta, s));
+      SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.h2, m + 1, 0, s, G.reo,
+                           p->kv_ticket));
+      SDD_CUDA(krylov_sub_norm(p->kv_V, vs, p->kv_w, G.h2, m + 1, nu, ld, j + 1, B, G.reo, G.active, p->kv_part,
+                               p->kv_ticket, p->kv_nrm2, nullptr, j, p->reorth_eta, s));
       SDD_CUDA(krylov_arnoldi_finish(G, p->kv_nrm2, j, B, s));
-      if (j + 1 < m) SDD_CUDA(krylov_scale(p->kv_w, G.inv, p->kv_V + (size_t)(j + 1) * vs, nu, ld, B, s, p->kv_v32));
+      if (j + 1 < m)
+        SDD_CUDA(krylov_scale(p->kv_w, G.inv, p->kv_V + (size_t)(j + 1) * vs, nu, ld, B, s, p->kv_v32, p->kv_vin));
       // the flags after column j go to slot j; the host reads those of column j - kFlagLag
       const int slot = j % (kFlagLag + 1);
       SDD_CUDA(cudaMemcpyAsync(p->h_int + (size_t)slot * B, G.active, B * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1330,7 +1443,7 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const double* rhs, double* 
 
 // |v_b|^2 over nu doubles at stride ld -> host h_dbl[0..B)
 static int host_norms2(sdd_plan* p, const double* v, int nu, int ld, int B, cudaStream_t s) {
-  SDD_CUDA(krylov_dots(v, 0, v, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s));
+  SDD_CUDA(krylov_dots(v, 0, v, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s, nullptr, p->kv_ticket));
   SDD_CUDA(cudaMemcpyAsync(p->h_dbl, p->kv_nrm2, B * sizeof(double), cudaMemcpyDeviceToHost, s));
   SDD_CUDA(cudaStreamSynchronize(s));
   return SDD_OK;
@@ -1353,14 +1466,20 @@ extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const doub
   std::vector<double> resF(B, 0.0), target(B, 0.0), resid;
   std::vector<int> nmask(B, 0), iters(B, 0);
   int matvecs = 0;
+  // the parameters in the plan's own buffers: the captured products read them there whatever the caller passes
+  double* Ra_d = p->sv_dev + 6 * (size_t)B;
+  double* Ras_d = p->sv_dev + 7 * (size_t)B;
+  SDD_CUDA(cudaMemcpyAsync(Ra_d, Ra, B * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  SDD_CUDA(cudaMemcpyAsync(Ras_d, Ras, B * sizeof(double), cudaMemcpyDeviceToDevice, s));
   // the Jacobian of PFX about the cached base state, on vectors of stride ld
   const bool fp32_rhs = o->mixed_matvec == 2;
-  MatVec J = [&](const double* v, double* out, const int* active, const float* v32) {
-    return apply_step_ld(p, B, Ra, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s, nullptr, nullptr, nullptr,
+  MatVec J = [&](const double* v, double* out, const int* active, const float* v32, cudaStream_t sm) {
+    return apply_step_ld(p, B, Ra_d, Ras_d, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, sm, nullptr, nullptr, nullptr,
                          active, 0, 0, o->mixed_matvec ? v32 : nullptr, fp32_rhs);
   };
+  const MvSpec Jspec{1 + o->mixed_matvec, Ra_d, Ras_d, base_mv};
   for (int it = 0;; ++it) {
-    if ((st = apply_step_ld(p, B, Ra, Ras, X, n, p->sv_F, ld, X, n, 0, p->sv_base64, SDD_PREC_FP64, s)))
+    if ((st = apply_step_ld(p, B, Ra_d, Ras_d, X, n, p->sv_F, ld, X, n, 0, p->sv_base64, SDD_PREC_FP64, s)))
       return st;                                                         // F = PFX(X), base cached
     if ((st = host_norms2(p, p->sv_F, n, ld, B, s))) return st;
     bool any = false;
@@ -1378,7 +1497,8 @@ extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const doub
       SDD_CUDA(launch_fx(ga, B, 2, SDD_PREC_MIXED, s));
     }
     for (int b = 0; b < B; ++b) target[b] = o->gmres_rtol * resF[b];
-    if ((st = gmres_solve(p, J, p->sv_F, p->sv_x, B, n, ld, m, o->max_restarts, target, nmask, s, &matvecs, resid)))
+    if ((st = gmres_solve(p, J, Jspec, p->sv_F, p->sv_x, B, n, ld, m, o->max_restarts, target, nmask, s, &matvecs,
+                          resid)))
       return st;
     int* mask_dev = p->kv_ismall + 3 * B;
     SDD_CUDA(cudaMemcpyAsync(mask_dev, nmask.data(), B * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -1429,9 +1549,11 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
   double* mudot_dev = p->sv_dev + B;
   double* c_dev = p->sv_dev + 2 * B;     // per-shell scalars
   double* last_dev = p->sv_dev + 3 * B;
+  double* Ras_d = p->sv_dev + 7 * (size_t)B;   // Ra_s in the plan's own buffer (read by the captured products)
   std::vector<double> mu0(B), mu(B), mudot(B), ds(ds_in, ds_in + B), resF(B, 0.0), gl(B, 0.0), c(B), tgt(B), resid;
   std::vector<int> it(B, 0), halv(B, 0), conv(B, 0), fail(B, 0), solve(B, 0);
   int matvecs = 0;
+  SDD_CUDA(cudaMemcpyAsync(Ras_d, Ras, B * sizeof(double), cudaMemcpyDeviceToDevice, s));
   SDD_CUDA(cudaMemcpyAsync(mu0.data(), Ra, B * sizeof(double), cudaMemcpyDeviceToHost, s));
   SDD_CUDA(cudaStreamSynchronize(s));
   mu = mu0;
@@ -1447,19 +1569,21 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
     }
     return pdfmu(p, B, Xs, n, s);
   };
-  MatVec J = [&](const double* v, double* out, const int* active, const float* v32) {
-    return apply_step_ld(p, B, mu_dev, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s, nullptr, nullptr, nullptr,
-                         active, 0, 0, o->mixed_matvec ? v32 : nullptr, fp32_rhs);
+  MatVec J = [&](const double* v, double* out, const int* active, const float* v32, cudaStream_t sm) {
+    return apply_step_ld(p, B, mu_dev, Ras_d, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, sm, nullptr, nullptr,
+                         nullptr, active, 0, 0, o->mixed_matvec ? v32 : nullptr, fp32_rhs);
   };
   // bordered operator DG = [[DF_X, DF_mu], [delta X_dot^T, (1-delta) mu_dot]]  (Main.py:914-915)
-  MatVec DG = [&](const double* v, double* out, const int* active, const float* v32) -> int {
-    int r = apply_step_ld(p, B, mu_dev, Ras, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, s, nullptr, nullptr,
+  MatVec DG = [&](const double* v, double* out, const int* active, const float* v32, cudaStream_t sm) -> int {
+    int r = apply_step_ld(p, B, mu_dev, Ras_d, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, sm, nullptr, nullptr,
                           nullptr, active, 0, 0, o->mixed_matvec ? v32 : nullptr, fp32_rhs);
     if (r) return r;
-    SDD_CUDA(krylov_dots(p->sv_Xd, 0, v, n, ld, 1, B, p->kv_part, p->kv_dot, 1, 0, s));
-    SDD_CUDA(contin_border(v, out, n, ld, p->sv_Jmu, n, Npsi, p->kv_dot, mudot_dev, delta, B, s));
+    SDD_CUDA(krylov_dots(p->sv_Xd, 0, v, n, ld, 1, B, p->kv_part, p->kv_dot, 1, 0, sm, nullptr, p->kv_ticket));
+    SDD_CUDA(contin_border(v, out, n, ld, p->sv_Jmu, n, Npsi, p->kv_dot, mudot_dev, delta, B, sm));
     return SDD_OK;
   };
+  const MvSpec Jspec{4 + o->mixed_matvec, mu_dev, Ras_d, base_mv};
+  const MvSpec DGspec{8 + o->mixed_matvec, mu_dev, Ras_d, base_mv};
 
   // ---- predictor (Main.py:839-876; with dt < 10 the tangent is always recomputed) ----
   SDD_CUDA(upload(mu_dev, mu));
@@ -1471,7 +1595,7 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
     tgt[b] = o->tangent_rtol * nj;
     solve[b] = nj > 0.0;
   }
-  if ((st = gmres_solve(p, J, p->sv_G, p->sv_x, B, n, ld, m, o->max_restarts, tgt, solve, s, &matvecs, resid)))
+  if ((st = gmres_solve(p, J, Jspec, p->sv_G, p->sv_x, B, n, ld, m, o->max_restarts, tgt, solve, s, &matvecs, resid)))
     return st;
   if ((st = host_norms2(p, p->sv_x, n, ld, B, s))) return st;
   for (int b = 0; b < B; ++b) {
@@ -1504,7 +1628,7 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
     for (int b = 0; b < B; ++b) c[b] = -1.0;
     SDD_CUDA(upload(c_dev, c));
     SDD_CUDA(krylov_axpy_shell(p->sv_t, ld, p->sv_X0, n, c_dev, p->sv_t, ld, n, B, s));
-    SDD_CUDA(krylov_dots(p->sv_Xd, 0, p->sv_t, n, ld, 1, B, p->kv_part, p->kv_dot, 1, 0, s));
+    SDD_CUDA(krylov_dots(p->sv_Xd, 0, p->sv_t, n, ld, 1, B, p->kv_part, p->kv_dot, 1, 0, s, nullptr, p->kv_ticket));
     SDD_CUDA(cudaMemcpyAsync(p->h_dbl + B, p->kv_dot, B * sizeof(double), cudaMemcpyDeviceToHost, s));
     if ((st = host_norms2(p, p->sv_F, n, ld, B, s))) return st;
     bool pending = false;
@@ -1544,7 +1668,7 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
     SDD_CUDA(krylov_copy_scaled(p->sv_F, ld, p->sv_G, ld, n, 1.0, last_dev, B, s));     // G = [F; p]
     for (int b = 0; b < B; ++b)
       tgt[b] = o->gmres_rtol * std::sqrt(delta * resF[b] * resF[b] + (1.0 - delta) * gl[b] * gl[b]);  // :919
-    if ((st = gmres_solve(p, DG, p->sv_G, p->sv_x, B, n + 1, ld, m, o->max_restarts, tgt, solve, s, &matvecs,
+    if ((st = gmres_solve(p, DG, DGspec, p->sv_G, p->sv_x, B, n + 1, ld, m, o->max_restarts, tgt, solve, s, &matvecs,
                           resid)))
       return st;
     int* mask_dev = p->kv_ismall + 3 * B;
@@ -1569,7 +1693,8 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
     tgt[b] = o->tangent_rtol;
     solve[b] = conv[b];
   }
-  if ((st = gmres_solve(p, DG, p->sv_G, p->sv_x, B, n + 1, ld, m, o->max_restarts, tgt, solve, s, &matvecs, resid)))
+  if ((st = gmres_solve(p, DG, DGspec, p->sv_G, p->sv_x, B, n + 1, ld, m, o->max_restarts, tgt, solve, s, &matvecs,
+                        resid)))
     return st;
   if ((st = host_norms2(p, p->sv_x, n, ld, B, s))) return st;
   std::vector<double> yx2(p->h_dbl, p->h_dbl + B);

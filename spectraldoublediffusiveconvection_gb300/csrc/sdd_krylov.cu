@@ -11,6 +11,8 @@
 // for Newton, n+1 with the continuation parameter appended for the bordered arclength system).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "sdd_krylov.cuh"
 
 namespace sdd {
@@ -24,6 +26,8 @@ constexpr int kDotThreads = 256;
 // a fixed-order sum: per thread over its elements in index order, then the warp's transposed shuffle
 // tree (warp_sum4), then the warps in order.
 constexpr int kDotPer = kDotChunk / kDotThreads;
+constexpr int kSubPer = kSubChunk / kDotThreads;
+static_assert(kSubChunk % kDotThreads == 0, "update chunk must be a multiple of the block");
 constexpr int kDotVecs = 4;
 static_assert(kDotChunk % kDotThreads == 0, "dot chunk must be a multiple of the block");
 
@@ -45,49 +49,145 @@ __device__ __forceinline__ double warp_sum4(const double (&sv)[4], int lane) {
   return k;
 }
 
+// The last CTA of a shell to finish (ticket[b], one counter per shell, zero between launches) sums the
+// shell's partials in chunk order and writes h: the reduction of k_dot_reduce, without its launch.
+__device__ __forceinline__ bool last_chunk_of_shell(int* ticket, int b, int nblocks) {
+  __shared__ int s_last;
+  __syncthreads();                                   // this CTA's partials are written
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const int last = atomicAdd(ticket + b, 1) == nblocks - 1;
+    if (last) {
+      __threadfence();
+      ticket[b] = 0;                                 // ready for the next launch
+    }
+    s_last = last;
+  }
+  __syncthreads();
+  return s_last != 0;
+}
+
+__device__ __forceinline__ void reduce_partials(const double* part, int b, int nv, int nchunk, double* h, int ldh,
+                                                int accumulate) {
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    double t = 0.0;
+    const volatile double* p = part + ((size_t)b * nv + i) * nchunk;
+    for (int c = 0; c < nchunk; ++c) t += p[c];
+    if (accumulate) h[(size_t)b * ldh + i] += t;
+    else h[(size_t)b * ldh + i] = t;
+  }
+}
+
+// blockIdx.z selects the vectors [z vpb, (z+1) vpb) of the CTA (vpb a multiple of kDotVecs): small batches
+// spread the vectors over more CTAs; every partial is summed the same way whatever the split.
 __global__ void __launch_bounds__(kDotThreads) k_dot_partials(const double* __restrict__ V, size_t vstride_i,
                                                              const double* __restrict__ w, int n, int ld, int nv,
-                                                             int chunk, double* __restrict__ part,
-                                                             const int* __restrict__ active) {
+                                                             int chunk, double* part,
+                                                             const int* __restrict__ active, int* ticket,
+                                                             double* h, int ldh, int accumulate, int vpb) {
   __shared__ double red[kDotVecs][kDotThreads / 32];
   const int c = blockIdx.x, b = blockIdx.y, nchunk = gridDim.x;
+  const int ib = blockIdx.z * vpb, ie = min(nv, ib + vpb);
   if (active && !active[b]) {                         // skipped shell: zero partials (its results are unused)
-    for (int i = threadIdx.x; i < nv; i += blockDim.x) part[((size_t)b * nv + i) * nchunk + c] = 0.0;
-    return;
-  }
-  const int e0 = c * chunk;
-  const double* wb = w + (size_t)b * ld;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double wr[kDotPer];
+    for (int i = ib + threadIdx.x; i < ie; i += blockDim.x) part[((size_t)b * nv + i) * nchunk + c] = 0.0;
+  } else {
+    const int e0 = c * chunk;
+    const double* wb = w + (size_t)b * ld;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double wr[kDotPer];
 #pragma unroll
-  for (int k = 0; k < kDotPer; ++k) {
-    const int e = e0 + threadIdx.x + k * kDotThreads;
-    wr[k] = e < n ? wb[e] : 0.0;
-  }
-  for (int i0 = 0; i0 < nv; i0 += kDotVecs) {
-    double sv[kDotVecs];
+    for (int k = 0; k < kDotPer; ++k) {
+      const int e = e0 + threadIdx.x + k * kDotThreads;
+      wr[k] = e < n ? wb[e] : 0.0;
+    }
+    for (int i0 = ib; i0 < ie; i0 += kDotVecs) {
+      double sv[kDotVecs];
 #pragma unroll
-    for (int u = 0; u < kDotVecs; ++u) {
-      sv[u] = 0.0;
-      if (i0 + u < nv) {
-        const double* vb = V + (size_t)(i0 + u) * vstride_i + (size_t)b * ld;
+      for (int u = 0; u < kDotVecs; ++u) {
+        sv[u] = 0.0;
+        if (i0 + u < ie) {
+          const double* vb = V + (size_t)(i0 + u) * vstride_i + (size_t)b * ld;
 #pragma unroll
-        for (int k = 0; k < kDotPer; ++k) {
-          const int e = e0 + threadIdx.x + k * kDotThreads;
-          if (e < n) sv[u] = fma(vb[e], wr[k], sv[u]);
+          for (int k = 0; k < kDotPer; ++k) {
+            const int e = e0 + threadIdx.x + k * kDotThreads;
+            if (e < n) sv[u] = fma(vb[e], wr[k], sv[u]);
+          }
         }
       }
+      static_assert(kDotVecs == 4, "warp_sum4 reduces four vectors");
+      const double ws = warp_sum4(sv, lane);
+      if ((lane & 7) == 0) red[lane >> 3][warp] = ws;
+      __syncthreads();
+      if (threadIdx.x < kDotVecs && i0 + threadIdx.x < ie) {
+        double t = 0.0;
+        for (int q = 0; q < kDotThreads / 32; ++q) t += red[threadIdx.x][q];
+        part[((size_t)b * nv + i0 + threadIdx.x) * nchunk + c] = t;
+      }
+      __syncthreads();
     }
-    static_assert(kDotVecs == 4, "warp_sum4 reduces four vectors");
-    const double ws = warp_sum4(sv, lane);
-    if ((lane & 7) == 0) red[lane >> 3][warp] = ws;
-    __syncthreads();
-    if (threadIdx.x < kDotVecs && i0 + threadIdx.x < nv) {
-      double t = 0.0;
-      for (int q = 0; q < kDotThreads / 32; ++q) t += red[threadIdx.x][q];
-      part[((size_t)b * nv + i0 + threadIdx.x) * nchunk + c] = t;
+  }
+  if (ticket && last_chunk_of_shell(ticket, b, nchunk * gridDim.z))
+    reduce_partials(part, b, nv, nchunk, h, ldh, accumulate);
+}
+
+// w[b] -= sum_{i<nv} V_i[b] coef[b*ldc + i] for the shells with sub_mask[b] (k_sub_combination's arithmetic),
+// then nrm2[b] = |w[b]|^2 for the shells with norm_mask[b] (0 for the others): per thread over its elements
+// in index order, the warp tree of k_dot_partials, the warps in order, the chunks of kSubChunk elements in
+// order.  The chunks are a quarter of the dot products' (the update's dependent multiply-adds over the
+// basis dominate, so one shell's update spreads over four times the CTAs).  With reo != nullptr the shell's
+// last CTA also sets the second-pass flag of column j (k_reorth_mask's test).
+__global__ void __launch_bounds__(kDotThreads) k_sub_norm(const double* __restrict__ V, size_t vstride_i, double* w,
+                                                         const double* __restrict__ coef, int ldc, int n, int ld,
+                                                         int nv, const int* __restrict__ sub_mask,
+                                                         const int* __restrict__ norm_mask, double* part,
+                                                         int* ticket, double* nrm2, GmresState gs, int j,
+                                                         double eta2, int set_reo) {
+  __shared__ double red[kDotVecs][kDotThreads / 32];
+  const int c = blockIdx.x, b = blockIdx.y, nchunk = gridDim.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int e0 = c * kSubChunk;
+  double* wb = w + (size_t)b * ld;
+  const bool sub = !sub_mask || sub_mask[b];
+  const bool nrm = !norm_mask || norm_mask[b];
+  const double* cb = coef + (size_t)b * ldc;
+  double sv[kDotVecs] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+  for (int k = 0; k < kSubPer; ++k) {
+    const int e = e0 + threadIdx.x + k * kDotThreads;
+    if (e < n) {
+      double x = wb[e];
+      if (sub) {
+        double t = 0.0;
+        for (int i = 0; i < nv; ++i) t += V[(size_t)i * vstride_i + (size_t)b * ld + e] * cb[i];
+        x -= t;
+        wb[e] = x;
+      }
+      if (nrm) sv[0] = fma(x, x, sv[0]);
     }
-    __syncthreads();
+  }
+  const double ws = warp_sum4(sv, lane);
+  if ((lane & 7) == 0) red[lane >> 3][warp] = ws;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < kDotThreads / 32; ++q) t += red[0][q];
+    part[(size_t)b * nchunk + c] = nrm ? t : 0.0;
+  }
+  if (last_chunk_of_shell(ticket, b, nchunk) && threadIdx.x == 0) {
+    double t = 0.0;
+    const volatile double* p = part + (size_t)b * nchunk;
+    for (int q = 0; q < nchunk; ++q) t += p[q];
+    nrm2[b] = t;
+    if (set_reo) {
+      int r = 0;
+      if (gs.active[b]) {
+        const double* hc = gs.hcol + (size_t)b * (gs.m + 1);
+        double h2 = 0.0;
+        for (int i = 0; i <= j; ++i) h2 = fma(hc[i], hc[i], h2);
+        r = t < eta2 * (t + h2) ? 1 : 0;
+      }
+      gs.reo[b] = r;
+    }
   }
 }
 
@@ -132,15 +232,16 @@ __global__ void k_add_combination(const double* __restrict__ V, size_t vstride_i
   }
 }
 
-// out[b] = a[b] * scale[b]  (scale may be per shell)
+// out[b] = a[b] * scale[b]  (scale may be per shell); out32 / out2 (nullable): FP32 and FP64 copies
 __global__ void k_scale(const double* __restrict__ a, const double* __restrict__ scale, double* __restrict__ out,
-                        int n, int ld, float* __restrict__ out32) {
+                        int n, int ld, float* __restrict__ out32, double* __restrict__ out2) {
   const int b = blockIdx.y;
   const double s = scale[b];
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
     const double v = a[(size_t)b * ld + e] * s;
     out[(size_t)b * ld + e] = v;
     if (out32) out32[(size_t)b * ld + e] = (float)v;
+    if (out2) out2[(size_t)b * ld + e] = v;
   }
 }
 
@@ -324,11 +425,44 @@ static int grid_x(int n) {
   return g < 1 ? 1 : (g > 1024 ? 1024 : g);
 }
 
+static int sm_count_dev() {
+  static int n = [] {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+  }();
+  return n;
+}
+
 cudaError_t krylov_dots(const double* V, size_t vstride_i, const double* w, int n, int ld, int nv, int B,
-                        double* part, double* h, int ldh, int accumulate, cudaStream_t st, const int* active) {
+                        double* part, double* h, int ldh, int accumulate, cudaStream_t st, const int* active,
+                        int* ticket) {
   const int nchunk = (n + kDotChunk - 1) / kDotChunk;
-  k_dot_partials<<<dim3(nchunk, B), kDotThreads, 0, st>>>(V, vstride_i, w, n, ld, nv, kDotChunk, part, active);
-  k_dot_reduce<<<B, 64, 0, st>>>(part, nv, nchunk, h, ldh, accumulate);
+  // with the one-launch reduction, spread the vectors over CTAs until the launch has ~2 CTAs per SM
+  int nvg = 1;
+  if (ticket) {
+    const int want = (2 * sm_count_dev() + B * nchunk - 1) / (B * nchunk);
+    nvg = std::max(1, std::min((nv + kDotVecs - 1) / kDotVecs, want));
+  }
+  int vpb = (nv + nvg - 1) / nvg;
+  vpb = (vpb + kDotVecs - 1) / kDotVecs * kDotVecs;
+  nvg = (nv + vpb - 1) / vpb;
+  k_dot_partials<<<dim3(nchunk, B, nvg), kDotThreads, 0, st>>>(V, vstride_i, w, n, ld, nv, kDotChunk, part, active,
+                                                               ticket, h, ldh, accumulate, vpb);
+  if (!ticket) k_dot_reduce<<<B, 64, 0, st>>>(part, nv, nchunk, h, ldh, accumulate);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_sub_norm(const double* V, size_t vstride_i, double* w, const double* coef, int ldc, int n, int ld,
+                            int nv, int B, const int* sub_mask, const int* norm_mask, double* part, int* ticket,
+                            double* nrm2, const GmresState* reo_of, int j, double eta, cudaStream_t st) {
+  if (!ticket) return cudaErrorInvalidValue;
+  const int nchunk = (n + kSubChunk - 1) / kSubChunk;
+  GmresState gs{};
+  if (reo_of) gs = *reo_of;
+  k_sub_norm<<<dim3(nchunk, B), kDotThreads, 0, st>>>(V, vstride_i, w, coef, ldc, n, ld, nv, sub_mask, norm_mask,
+                                                      part, ticket, nrm2, gs, j, eta * eta, reo_of ? 1 : 0);
   return cudaGetLastError();
 }
 
@@ -345,8 +479,8 @@ cudaError_t krylov_add_combination(const double* V, size_t vstride_i, double* x,
 }
 
 cudaError_t krylov_scale(const double* a, const double* scale, double* out, int n, int ld, int B, cudaStream_t st,
-                         float* out32) {
-  k_scale<<<dim3(grid_x(n), B), 256, 0, st>>>(a, scale, out, n, ld, out32);
+                         float* out32, double* out2) {
+  k_scale<<<dim3(grid_x(n), B), 256, 0, st>>>(a, scale, out, n, ld, out32, out2);
   return cudaGetLastError();
 }
 

@@ -6,6 +6,7 @@
 namespace sdd {
 
 constexpr int kDotChunk = 2048;   // elements per CTA in the two-level dot products
+constexpr int kSubChunk = 512;    // elements per CTA of the fused Gram-Schmidt update and norm
 constexpr int kMaxRestart = 64;   // GMRES restart length limit (Newton and continuation check it)
 
 struct GmresState {
@@ -36,16 +37,23 @@ constexpr double kReorthEta = 0.70710678118654752440;
 
 // n: used doubles per shell, ld: stride between shells (n <= ld); active (device, nullable): shells whose
 // flag is 0 are skipped (dots: zero results; combinations: w left as it was)
+// ticket (nullable): B zeroed counters; with it the partials are reduced by each shell's last CTA (one launch)
 cudaError_t krylov_dots(const double* V, size_t vstride_i, const double* w, int n, int ld, int nv, int B,
                         double* part, double* h, int ldh, int accumulate, cudaStream_t st,
-                        const int* active = nullptr);
+                        const int* active = nullptr, int* ticket = nullptr);
+// One launch for a Gram-Schmidt pass's update and the new norm: w -= V coef where sub_mask (nullable: all),
+// nrm2 = |w|^2 where norm_mask (nullable: all; 0 elsewhere), with the sums of krylov_dots; reo_of
+// (nullable): also set reo_of->reo for column j as krylov_reorth_mask does.  ticket: B zeroed counters.
+cudaError_t krylov_sub_norm(const double* V, size_t vstride_i, double* w, const double* coef, int ldc, int n, int ld,
+                            int nv, int B, const int* sub_mask, const int* norm_mask, double* part, int* ticket,
+                            double* nrm2, const GmresState* reo_of, int j, double eta, cudaStream_t st);
 cudaError_t krylov_sub_combination(const double* V, size_t vstride_i, double* w, const double* coef, int ldc,
                                    int n, int ld, int nv, int B, cudaStream_t st, const int* active = nullptr);
 cudaError_t krylov_add_combination(const double* V, size_t vstride_i, double* x, const double* y, int ldy,
                                    const int* kb, int n, int ld, int B, cudaStream_t st);
-// out = a * scale[b]; out32 (nullable, same strides): the result also rounded to FP32
+// out = a * scale[b]; out32 / out2 (nullable, same strides): the result also rounded to FP32 / copied
 cudaError_t krylov_scale(const double* a, const double* scale, double* out, int n, int ld, int B, cudaStream_t st,
-                         float* out32 = nullptr);
+                         float* out32 = nullptr, double* out2 = nullptr);
 cudaError_t krylov_sub(const double* a, const double* b, double* out, size_t n, cudaStream_t st);
 cudaError_t krylov_masked_sub(double* X, const double* dx, const int* mask, int n, int ldx, int ld, int B,
                               cudaStream_t st);

@@ -156,6 +156,19 @@ class Plan:
         _lib.check(self._L.sdd_plan_tensor_core_status(self._h, ctypes.byref(v)), "sdd_plan_tensor_core_status")
         return bool(v.value)
 
+    def set_product_graphs(self, on):
+        """True (the default): Newton / continuation GMRES products replay captured CUDA graphs; False: launched
+        kernel by kernel, with identical results (sdd_plan_set_product_graphs)."""
+        _lib.check(self._L.sdd_plan_set_product_graphs(self._h, int(bool(on))), "sdd_plan_set_product_graphs")
+
+    def product_graph_stats(self):
+        """{"captured", "replayed", "direct"}: how this plan's GMRES products ran so far
+        (sdd_plan_product_graph_stats)."""
+        v = [ctypes.c_longlong(0) for _ in range(3)]
+        _lib.check(self._L.sdd_plan_product_graph_stats(self._h, *[ctypes.byref(x) for x in v]),
+                   "sdd_plan_product_graph_stats")
+        return dict(zip(("captured", "replayed", "direct"), (x.value for x in v)))
+
     def new_state(self, batch=1):
         torch = _torch()
         return torch.zeros((batch, self.n_state), dtype=torch.float64, device=self.device)

@@ -128,3 +128,51 @@ def test_krylov_basis_stays_orthonormal(cuda):
         worst = max(worst, err)
     print(f"max |V^T V - I| over {B} shells, cycles of 40-50 columns: {worst:.2e}")
     assert worst <= 1e-10
+
+
+def test_product_graphs_replay_and_match_direct_launches(cuda):
+    """The GMRES products of Newton and of the pseudo-arclength step run as captured CUDA graphs (one capture
+    per batch size and kind; every Arnoldi column reads the same fixed vector), with exactly the results of
+    the same kernels launched one by one; a kernel-choice change recaptures."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    from conftest import load_golden
+    torch = cuda
+    N_fm, N_r = 64, 20
+    X0 = np.stack([O.seeded_state(N_fm, N_r - 1, s) for s in (4, 5)])
+    out = []
+    for graphs in (True, False):
+        p = Plan(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
+        p.set_product_graphs(graphs)
+        X = torch.from_numpy(X0.copy()).cuda()
+        r = p.newton(X, 8000.0, 500.0, tol=1e-10)
+        st = p.product_graph_stats()
+        if graphs:
+            assert st["direct"] == 0 and 1 <= st["captured"] <= 2 and st["replayed"] >= r[0]["matvecs"] - 2
+            X2 = torch.from_numpy(X0.copy()).cuda()
+            p.newton(X2, 8000.0, 500.0, tol=1e-10)
+            assert p.product_graph_stats()["captured"] == st["captured"]      # the second solve replays
+            assert torch.equal(X2, X)
+            p.set_chain_layout(1)                                             # a kernel choice: recaptured
+            X3 = torch.from_numpy(X0.copy()).cuda()
+            p.newton(X3, 8000.0, 500.0, tol=1e-10)
+            assert p.product_graph_stats()["captured"] > st["captured"]
+        else:
+            assert st["captured"] == 0 and st["replayed"] == 0 and st["direct"] >= r[0]["matvecs"]
+        out.append((X.cpu().numpy(), [x["matvecs"] for x in r]))
+    assert np.array_equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
+    # the bordered products of a continuation step
+    Z = load_golden("cont_tau1.npz")
+    N_r2, N_fm2, _, d, Pr, Tau, Ra0, Ra_s, _ = Z["params"]
+    res = []
+    for graphs in (True, False):
+        p = Plan(int(N_fm2), int(N_r2), d, 1.0, Pr, Tau)
+        p.set_product_graphs(graphs)
+        X = torch.from_numpy(Z["X_steady"].copy()).cuda().reshape(1, -1)
+        Ra = torch.tensor([Ra0], dtype=torch.float64, device="cuda")
+        Xd, r = p.contin_step(X, Ra, Ra_s, sign=1.0, ds=50.0, tol=1e-10)
+        assert r[0]["converged"]
+        if graphs:
+            assert p.product_graph_stats()["direct"] == 0
+        res.append((X.cpu().numpy(), Ra.cpu().numpy(), Xd.cpu().numpy()))
+    for a, b in zip(*res):
+        assert np.array_equal(a, b)
