@@ -168,6 +168,7 @@ struct sdd_plan {
   double* h_dbl;      // pinned host scalars
   int* h_int;         // pinned host flags: kFlagLag + 1 slots of B
   cudaEvent_t flag_ev[kFlagLag + 1];   // one per slot: its flags have arrived
+  cudaEvent_t wait_ev;                 // the solvers' host waits (blocking: the waiting thread sleeps)
   double *sv_F, *sv_x, *sv_X0, *sv_Xd, *sv_t, *sv_G, *sv_Jmu, *sv_g, *sv_base64, *sv_dev;
   float* sv_base32;
   float* kv_v32;      // mixed plans: [B][ld] FP32 copy of the Krylov vector the next product is applied to
@@ -294,6 +295,8 @@ static void solver_free(sdd_plan* p) {
     if (e) cudaEventDestroy(e);
     e = nullptr;
   }
+  if (p->wait_ev) cudaEventDestroy(p->wait_ev);
+  p->wait_ev = nullptr;
   p->kv_V = p->kv_w = p->kv_r = p->kv_part = p->kv_nrm2 = p->kv_small = p->kv_dot = nullptr;
   p->sv_F = p->sv_x = p->sv_X0 = p->sv_Xd = p->sv_t = p->sv_G = p->sv_Jmu = p->sv_g = p->sv_base64 = nullptr;
   p->sv_dev = nullptr;
@@ -1259,7 +1262,11 @@ static int solver_reserve(sdd_plan* p, int B, int m) {
   SDD_CUDA(cudaMemset(p->kv_ticket, 0, (size_t)B * sizeof(int)));
   SDD_CUDA(ws_malloc(&p->h_dbl, (size_t)2 * B * sizeof(double), true));
   SDD_CUDA(ws_malloc(&p->h_int, (size_t)(kFlagLag + 1) * B * sizeof(int), true));
-  for (cudaEvent_t& e : p->flag_ev) SDD_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  // blocking-sync events: a solver thread waiting for the GPU sleeps instead of spinning, so that many
+  // solver threads (a server's workers) do not take the host cores from each other
+  for (cudaEvent_t& e : p->flag_ev)
+    SDD_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming | cudaEventBlockingSync));
+  SDD_CUDA(cudaEventCreateWithFlags(&p->wait_ev, cudaEventDisableTiming | cudaEventBlockingSync));
   double** v[] = {&p->sv_F, &p->sv_x, &p->sv_Xd, &p->sv_t, &p->sv_G};
   for (double** q : v) SDD_CUDA(ws_malloc(q, vb));
   SDD_CUDA(ws_malloc(&p->sv_X0, (size_t)B * n * sizeof(double)));
@@ -1365,6 +1372,13 @@ static int run_mv(sdd_plan* p, const MatVec& A, const MvSpec& spec, int B, const
   return SDD_OK;
 }
 
+// The solvers' host waits: until the work queued on s so far is done, sleeping on a blocking event.
+static int solver_wait(sdd_plan* p, cudaStream_t s) {
+  SDD_CUDA(cudaEventRecord(p->wait_ev, s));
+  SDD_CUDA(cudaEventSynchronize(p->wait_ev));
+  return SDD_OK;
+}
+
 // Restarted GMRES(m), classical Gram-Schmidt with a conditional second pass, for the shells with
 // solve[b] != 0: A x = rhs, x starts at 0, inner stop |r_b| <= target[b] (absolute).  x, rhs have stride
 // ld with nu used doubles.  resid (host) receives the final residual estimates.
@@ -1428,7 +1442,7 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const MvSpec& spec, const d
     SDD_CUDA(krylov_solve_y(G, B, s));
     SDD_CUDA(krylov_add_combination(p->kv_V, vs, x, G.y, m, G.kb, nu, ld, B, s));
     SDD_CUDA(cudaMemcpyAsync(p->h_dbl, G.resid, B * sizeof(double), cudaMemcpyDeviceToHost, s));
-    SDD_CUDA(cudaStreamSynchronize(s));
+    if ((st = solver_wait(p, s))) return st;
     bool more = false;
     for (int b = 0; b < B; ++b) {
       if (again[b]) resid[b] = p->h_dbl[b];
@@ -1445,8 +1459,7 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const MvSpec& spec, const d
 static int host_norms2(sdd_plan* p, const double* v, int nu, int ld, int B, cudaStream_t s) {
   SDD_CUDA(krylov_dots(v, 0, v, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s, nullptr, p->kv_ticket));
   SDD_CUDA(cudaMemcpyAsync(p->h_dbl, p->kv_nrm2, B * sizeof(double), cudaMemcpyDeviceToHost, s));
-  SDD_CUDA(cudaStreamSynchronize(s));
-  return SDD_OK;
+  return solver_wait(p, s);
 }
 
 extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const double* Ras, double* X,
@@ -1555,7 +1568,7 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
   int matvecs = 0;
   SDD_CUDA(cudaMemcpyAsync(Ras_d, Ras, B * sizeof(double), cudaMemcpyDeviceToDevice, s));
   SDD_CUDA(cudaMemcpyAsync(mu0.data(), Ra, B * sizeof(double), cudaMemcpyDeviceToHost, s));
-  SDD_CUDA(cudaStreamSynchronize(s));
+  if ((st = solver_wait(p, s))) return st;
   mu = mu0;
   auto upload = [&](double* dst, const std::vector<double>& v) {
     return cudaMemcpyAsync(dst, v.data(), B * sizeof(double), cudaMemcpyHostToDevice, s);
@@ -1676,7 +1689,7 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
     SDD_CUDA(krylov_masked_sub(X, p->sv_x, mask_dev, n, n, ld, B, s));                   // Y -= dY
     SDD_CUDA(cudaMemcpy2DAsync(p->h_dbl, sizeof(double), p->sv_x + n, ld * sizeof(double), sizeof(double), B,
                                cudaMemcpyDeviceToHost, s));
-    SDD_CUDA(cudaStreamSynchronize(s));
+    if ((st = solver_wait(p, s))) return st;
     for (int b = 0; b < B; ++b)
       if (solve[b]) {
         mu[b] -= p->h_dbl[b];
@@ -1700,7 +1713,7 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
   std::vector<double> yx2(p->h_dbl, p->h_dbl + B);
   SDD_CUDA(cudaMemcpy2DAsync(p->h_dbl, sizeof(double), p->sv_x + n, ld * sizeof(double), sizeof(double), B,
                              cudaMemcpyDeviceToHost, s));
-  SDD_CUDA(cudaStreamSynchronize(s));
+  if ((st = solver_wait(p, s))) return st;
   for (int b = 0; b < B; ++b) {
     const double yl = p->h_dbl[b];
     const double nrm = std::sqrt(delta * yx2[b] + (1.0 - delta) * yl * yl);
@@ -1711,7 +1724,7 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
   SDD_CUDA(krylov_scale(p->sv_x, c_dev, p->sv_t, n, ld, B, s));
   SDD_CUDA(krylov_copy_scaled(p->sv_t, ld, X_dot, n, n, 1.0, nullptr, B, s));
   SDD_CUDA(upload(Ra, mu));
-  SDD_CUDA(cudaStreamSynchronize(s));
+  if ((st = solver_wait(p, s))) return st;
   bool all = true;
   for (int b = 0; b < B; ++b) {
     res[b].residual = resF[b];
