@@ -408,6 +408,7 @@ def _served_stats(srv, reqs, wall, rate, st0):
                                                                      if r.result])) if ok_con else None),
             "integration": dict(serve.latency_report(itg), n=len(itg), finite=len(ok_int)),
             "errors": sum(r.error is not None for r in reqs),
+            "error_samples": sorted({"%s %dx%d: %s" % (r.kind, r.N_r, r.N_theta, r.error) for r in reqs if r.error})[:5],
             "batching": {k: srv.stats[k] - st0[k] for k in srv.stats}}
 
 
@@ -457,6 +458,8 @@ def bench_served(device, n_requests=1000, rate=200.0, seed=2024, frac_continue=0
         same = run(rate, sweep_requests, seed + 99, server_kw["con_mixed"])
     finally:
         srv.stop()
+    # plans whose tensor-core kernel gave up waiting for its products (outputs NaN: such requests fail)
+    tc_timeouts = sum(1 for p_ in srv._plans.values() if getattr(p_, "tensor_cores", False) and p_.tensor_core_timed_out())
     # the plain FP64 path on the same request mix: a sample of the continuation requests, each solved alone
     # (one shell, FP64 plan and FP64 Jacobian products), one after the other
     from spectraldoublediffusiveconvection_gb300.plan import Plan
@@ -495,8 +498,9 @@ def bench_served(device, n_requests=1000, rate=200.0, seed=2024, frac_continue=0
         "capacity_vs_plain_same_workload": (cap["continuation_solves_per_s"] / plain_rate) if cap else None,
         "saturation_vs_plain_same_workload": max(c["continuation_solves_per_s"] for c in curve) / plain_rate,
         "sweep": [{k: c[k] for k in ("offered_rate_per_s", "continuation_solves_per_s", "integration_steps_per_s",
-                                      "p50_ms", "p99_ms", "queue_p99_ms", "device_p99_ms", "errors")}
+                                      "p50_ms", "p99_ms", "queue_p99_ms", "device_p99_ms", "errors", "error_samples")}
                   for c in curve],
+        "tensor_core_timeouts": tc_timeouts,
         "continuation_matvec_compare": {
             "mixed_matvec_%d" % server_kw["con_mixed"]: {k: same[k] for k in ("continuation_solves_per_s", "p50_ms",
                                                                             "p99_ms")},

@@ -601,7 +601,15 @@ __device__ __forceinline__ double carried_state(const ChainArgs& a, int b, size_
   double v = d[(size_t)(c - 1) * a.ldd + e];
   if (c >= 2) {
     const double* row = a.pbuf + (size_t)b * a.p_stride + (chain * a.np + (size_t)(c - 1) * (c - 2) / 2) * a.ldd;
-    for (int t = 0; t <= c - 2; ++t) v += row[(size_t)t * a.ldd + e];
+    const int nt = c - 1;                              // in index order, the terms loaded eight at a time
+    for (int u0 = 0; u0 < nt; u0 += 8) {
+      double tv[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) tv[k] = (u0 + k < nt) ? row[(size_t)(u0 + k) * a.ldd + e] : 0.0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        if (u0 + k < nt) v += tv[k];
+    }
   }
   return v;
 }

@@ -386,8 +386,18 @@ __device__ void apply_pending_fix(const FxArgs& a, int b, int k, double* xd, dou
     const double* d = x.dbuf + (size_t)b * x.d_stride + chain * x.nch * x.ldd;
     const double* prow = x.pbuf + (size_t)b * x.p_stride + (chain * x.np + (size_t)(c - 1) * (c - 2) / 2) * x.ldd;
     for (int e = t; e < m; e += 128) {
+      // d_{c-1} + part_0 + ... + part_{c-2} in index order, the terms loaded eight at a time (a load
+      // after each addition would wait out one L2 round trip per term)
       double v = d[(size_t)(c - 1) * x.ldd + e];
-      for (int u = 0; u <= c - 2; ++u) v += prow[(size_t)u * x.ldd + e];
+      const int nt = c - 1;
+      for (int u0 = 0; u0 < nt; u0 += 8) {
+        double tv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) tv[k] = (u0 + k < nt) ? prow[(size_t)(u0 + k) * x.ldd + e] : 0.0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          if (u0 + k < nt) v += tv[k];
+      }
       s[e] = v;
     }
   }
@@ -399,7 +409,7 @@ __device__ void apply_pending_fix(const FxArgs& a, int b, int k, double* xd, dou
       const int r = r0 + i;
       const int rr = r < nr ? r : 0;
       double acc = 0.0;
-#pragma unroll 8
+#pragma unroll 16
       for (int col = q; col < m; col += TPR) acc = fma(__ldg(G + (size_t)col * ldl + rr), s[col], acc);
       acc = lane_group_sum<TPR>(acc);
       if (r < nr && q == 0) {
