@@ -424,10 +424,12 @@ __device__ void apply_pending_fix(const FxArgs& a, int b, int k, double* xd, dou
   __syncthreads();
 }
 
-size_t fx_deriv_smem_bytes(int nr, int prec, bool fix) {
+// T-typed Dr, D2r2 and the mode's rows; then (FP64) the corrected rows and carried states of a pending fix
+// (7 nr); then the fused right-hand side's D2s (nr^2) and the mode's FP64 psi row (nr)
+size_t fx_deriv_smem_bytes(int nr, int prec, bool fix, bool fuse) {
   const size_t es = prec == SDD_PREC_MIXED ? sizeof(float) : sizeof(double);
   const size_t t = ((2 * (size_t)nr * nr + 3 * (size_t)nr) * es + 15) / 16 * 16;
-  return fix ? t + 7 * (size_t)nr * sizeof(double) : t;
+  return t + (fix ? 7 * (size_t)nr * sizeof(double) : 0) + (fuse ? ((size_t)nr * nr + nr) * sizeof(double) : 0);
 }
 
 template <typename T>
@@ -441,11 +443,13 @@ __global__ void __launch_bounds__(384) k_fx_deriv(FxArgs a, T* deriv, size_t der
   // with a pending correction: the mode's FP64 rows (corrected here) and a carried state
   double* xd = reinterpret_cast<double*>(smem_raw + ((2 * (size_t)nr * nr + 3 * (size_t)nr) * sizeof(T) + 15) / 16 * 16);
   double* sc = xd + 3 * nr;
+  double* D2sm = xd + (a.fix.on ? 7 * nr : 0);        // fused right-hand side: A2_SINE's D2 (FP64)
   const T* Drg = reinterpret_cast<const T*>(a.ops.Dr);
   const T* D2g = reinterpret_cast<const T*>(a.ops.D2r2);
   for (int e = threadIdx.x; e < nr * nr; e += blockDim.x) {
     ops[e] = Drg[e];
     ops[nr * nr + e] = D2g[e];
+    if (a.fuse_rhs) D2sm[e] = __ldg(a.rl.D2s + e);
   }
   const int N = M * nr;
   if (a.fix.on) {
@@ -464,6 +468,9 @@ __global__ void __launch_bounds__(384) k_fx_deriv(FxArgs a, T* deriv, size_t der
         xv[e] = xr((size_t)f * N + (size_t)k * nr + m);
       }
     });
+    if (a.fuse_rhs)
+      for (int e = threadIdx.x; e < nr; e += blockDim.x)
+        D2sm[nr * nr + e] = __ldg(a.X + (size_t)b * a.x_stride + (size_t)k * nr + e);
   }
   __syncthreads();
   T* D = deriv + (size_t)b * deriv_stride;
@@ -478,13 +485,13 @@ __global__ void __launch_bounds__(384) k_fx_deriv(FxArgs a, T* deriv, size_t der
       for (int m = 0; m < nr; ++m) acc = fma(row[m], x[m], acc);
       D[((size_t)op * M + k) * nr + n] = acc;
     } else {   // A2_SINE's D2 psi for the fused right-hand side (FP64; the order of k_rhs's dot)
-      const double* row = a.rl.D2s + (size_t)n * nr;
+      const double* row = D2sm + (size_t)n * nr;
       double acc = 0;
       if (a.fix.on) {          // the corrected rows (this kernel wrote them: not through the read-only path)
-        for (int m = 0; m < nr; ++m) acc = fma(__ldg(row + m), xd[m], acc);
+        for (int m = 0; m < nr; ++m) acc = fma(row[m], xd[m], acc);
       } else {
-        const double* ps = a.X + (size_t)b * a.x_stride + (size_t)k * nr;
-        for (int m = 0; m < nr; ++m) acc = fma(__ldg(row + m), __ldg(ps + m), acc);
+        const double* ps = D2sm + nr * nr;     // the mode's FP64 psi row
+        for (int m = 0; m < nr; ++m) acc = fma(row[m], ps[m], acc);
       }
       reinterpret_cast<double*>(D)[(size_t)4 * M * nr * sizeof(T) / 8 + (size_t)k * nr + n] = acc;
     }
@@ -1179,7 +1186,7 @@ static cudaError_t launch_fx_split_t(const FxArgs& a, int batch, cudaStream_t s)
   const bool tc = sizeof(T) == 4 && a.deriv_t;
   if (!tc || a.fix.on || a.fuse_rhs) {
     e = launch_kernel(k_fx_deriv<T>, dim3(a.M, batch), dim3(a.fix.on ? 384 : 256),
-                      fx_deriv_smem_bytes(a.nr, prec, a.fix.on != 0), s, a,
+                      fx_deriv_smem_bytes(a.nr, prec, a.fix.on != 0, a.fuse_rhs != 0), s, a,
                       reinterpret_cast<T*>(a.deriv), a.deriv_stride);
     ktimer_mark(SDD_K_FX_DERIV, s);
     if (e != cudaSuccess) return e;
