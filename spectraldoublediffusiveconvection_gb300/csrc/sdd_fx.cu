@@ -533,19 +533,37 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
   }
   for (int i = tid; i < P + 2; i += bd) kf[i] = (T)i;
   const T ir4n = reinterpret_cast<const T*>(a.ops.ir4r2)[n];
-  __syncthreads();
+  // (no barrier: the row loads below do not read the tables, the barrier after them covers both)
 
   // which row quantities the pair's two fields need (fields: 0 JT_psi, 1 komega, 2 kDpsi, 3 DT, 4 DC,
   // 5 omega, 6 Dpsi, 7 kT, 8 kC)
   const bool need_psi = pr == 0 || pr == 2;            // pv (JT_psi, omega's A2 term) and D2 psi (omega)
-  // FP32 kernels: FP64 row values for the linear parts of the fused right-hand side (pair 0)
-  const bool lin = pr == 0 && a.fuse_rhs;
+  // The linear parts of the fused right-hand sides: FP64 kernels split them between the two pairs that form
+  // psi's parity sums anyway (pair 0 the psi part, pair 2 the T and S parts: pair 0 carries the most work
+  // and sets the kernel's length); FP32 kernels form all three in pair 0 from FP64 copies of the row.
+  const bool lin = a.fuse_rhs && (pr == 0 || (sizeof(T) == 8 && pr == 2));
+  const bool lin_psi = lin && pr == 0;
+  const bool lin_ts = lin && (pr == 2 || sizeof(T) == 4);
   double* pv64 = nullptr;
   if (sizeof(T) == 4 && lin)
     pv64 = reinterpret_cast<double*>(smem_raw + fx_grid_lin64_offset(M, P, SDD_PREC_MIXED));
   const int N = M * nr;
   const double* Xs = a.X + (size_t)b * a.x_stride;
   const T* Dv = reinterpret_cast<const T*>(a.deriv) + (size_t)b * a.deriv_stride;   // k_fx_deriv
+  // the psi part's FP64 D2 psi (k_fx_deriv's fifth block) for this thread's first mode, loaded with the row
+  const double* D2p = reinterpret_cast<const double*>(Dv) + (size_t)4 * M * nr * sizeof(T) / 8;
+  double d2s0 = 0.0;
+  if (lin_psi && tid < M && !(a.sym && (tid % 2 == 0))) d2s0 = D2p[(size_t)tid * nr + n];
+  // the linear parts' per-row scalars, also loaded with the row (read after the parity sums)
+  double lRa = 0.0, lRas = 0.0, lir2 = 0.0, lrsq = 0.0, ldT0 = 0.0, lgr = 0.0;
+  if (lin) {
+    lRa = a.rl.Ra[b];
+    lRas = a.rl.Ra_s[b];
+    lir2 = a.rl.ir2s[n];
+    lrsq = a.rl.rsq[n];
+    ldT0 = a.rl.dT0[n];
+    lgr = a.rl.gr[n];
+  }
   with_x<T>(a, b, [&](auto xr) {
   for (int k = tid; k < M; k += bd) {
     const bool psi_on = !(a.sym && (k % 2 == 0));
@@ -581,38 +599,41 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
   });
   __syncthreads();
   if (need_psi) {
-    parity_suffix<T>(pv, Sc, M);
+    parity_suffix<T>(pv, Sc, M);                       // (ends with a barrier)
     if (pv64) parity_suffix<double>(pv64, pv64 + M, M);
-    __syncthreads();
-    if (lin) {
-      // the linear parts of the right-hand sides at row n (k_rhs's expressions, Main.py:262-280), in FP64
-      const double* pvd = pv64 ? pv64 : reinterpret_cast<const double*>(pv);
-      const double* Scd = pv64 ? pv64 + M : reinterpret_cast<const double*>(Sc);
-      const double* Tvd = pv64 ? pv64 + 2 * M : reinterpret_cast<const double*>(Tv);
-      const double* Svd = pv64 ? pv64 + 3 * M : reinterpret_cast<const double*>(Sv);
-      const RhsArgs& r = a.rl;
-      const double* D2p = reinterpret_cast<const double*>(Dv) + (size_t)4 * M * nr * sizeof(T) / 8;
-      const double dt = r.dt, dtPr = r.dt * r.Pr;
-      const double Ra = r.Ra[b], Ras = r.Ra_s[b];
-      const double ir2 = r.ir2s[n], rsq = r.rsq[n], dT0 = r.dT0[n], gr = r.gr[n];
-      double* R = r.rhs + (size_t)b * r.rhs_stride;
-      for (int k = tid; k < M; k += bd) {
+    // one loop: the linear parts of the right-hand sides at row n (k_rhs's expressions, Main.py:262-280, in
+    // FP64) and J_theta_RT / A2_SINE_R2 of the row, independent per k
+    const double* pvd = pv64 ? pv64 : reinterpret_cast<const double*>(pv);
+    const double* Scd = pv64 ? pv64 + M : reinterpret_cast<const double*>(Sc);
+    const double* Tvd = pv64 ? pv64 + 2 * M : reinterpret_cast<const double*>(Tv);
+    const double* Svd = pv64 ? pv64 + 3 * M : reinterpret_cast<const double*>(Sv);
+    const RhsArgs& r = a.rl;
+    const double dt = r.dt, dtPr = r.dt * r.Pr;
+    const double Ra = lRa, Ras = lRas;
+    const double ir2 = lir2, rsq = lrsq, dT0 = ldT0, gr = lgr;
+    double* R = lin ? r.rhs + (size_t)b * r.rhs_stride : nullptr;
+    for (int k = tid; k < M; k += bd) {
+      jp_om<T>(k, M, kf, pv, Sc, ir4n, JP[k], OM[k]);
+      if (lin) {
         const double pk = pvd[k], pkm = k > 0 ? pvd[k - 1] : 0.0;
         const double s1 = (k + 1 < M) ? Scd[k + 1] : 0.0;
         const double JPk = (k == 0) ? 1.0 * s1 : (k + 1.0) * pkm + 2.0 * s1;
-        const double s2 = (k + 2 < M) ? Scd[k + 2] : 0.0;
-        const bool psi_on = !(a.sym && (k % 2 == 0));
-        const double d2s = psi_on ? D2p[(size_t)k * nr + n] : 0.0;
-        const double Om = d2s - (double)(k + 1) * ir2 * ((k + 2.0) * pk + 2.0 * s2);
-        const double grv = (k < M - 1) ? (-(double)(k + 1) * gr) * (Ra * Tvd[k + 1] - Ras * Svd[k + 1]) : 0.0;
-        const double psiT0 = dT0 * JPk;
         const size_t o = (size_t)k * nr + n;
-        R[o] = Om + dtPr * grv;
-        R[N + o] = rsq * Tvd[k] - dt * psiT0;
-        R[2 * N + o] = rsq * Svd[k] - dt * psiT0;
+        if (lin_psi) {
+          const double s2 = (k + 2 < M) ? Scd[k + 2] : 0.0;
+          const bool psi_on = !(a.sym && (k % 2 == 0));
+          const double d2s = k == tid ? d2s0 : (psi_on ? D2p[(size_t)k * nr + n] : 0.0);
+          const double Om = d2s - (double)(k + 1) * ir2 * ((k + 2.0) * pk + 2.0 * s2);
+          const double grv = (k < M - 1) ? (-(double)(k + 1) * gr) * (Ra * Tvd[k + 1] - Ras * Svd[k + 1]) : 0.0;
+          R[o] = Om + dtPr * grv;
+        }
+        if (lin_ts) {
+          const double psiT0 = dT0 * JPk;
+          R[N + o] = rsq * Tvd[k] - dt * psiT0;
+          R[2 * N + o] = rsq * Svd[k] - dt * psiT0;
+        }
       }
     }
-    for (int k = tid; k < M; k += bd) jp_om<T>(k, M, kf, pv, Sc, ir4n, JP[k], OM[k]);
     __syncthreads();
   }
   // the pair's two DCT3 input rows (in RB, free until the FFT) and their maxima

@@ -6,27 +6,44 @@
 
 namespace sdd {
 
-// S[m] = sum_{m' >= m, m' = m mod 2} v[m'] for m < M (warps 0 and 1; caller syncs).
+// S[m] = sum_{m' >= m, m' = m mod 2} v[m'] for m < M.  Called by every thread of the block; returns after a
+// barrier (S and the block's shared totals are then free to reuse), the caller syncs before reading S.
+// Each parity's values go in chunks of 32 (one warp-wide suffix scan per chunk, all chunks of both parities
+// at once over the block's warps); chunk c then adds the carried total of the chunks above it,
+// carry_c = T_{c+1} + (T_{c+2} + (... + T_last)), the association of a sequential carry from the top chunk
+// down, so the sums are those of one warp scanning the chunks one after another.
+constexpr int kSuffixChunks = 64;   // per parity: M <= 4096
 template <typename T>
 __device__ void parity_suffix(const T* v, T* S, int M) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp < 2) {
-    const int p = warp;
-    const int cnt = (M - p + 1) / 2;
-    T carry = (T)0;
-    for (int t0 = ((cnt - 1) / 32) * 32; t0 >= 0; t0 -= 32) {
-      const int t = t0 + lane;
-      T x = (t < cnt) ? v[p + 2 * t] : (T)0;
+  __shared__ T tot[2][kSuffixChunks];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int cnt0 = (M + 1) / 2, cnt1 = M / 2;
+  const int nc0 = (cnt0 + 31) / 32, nc1 = (cnt1 + 31) / 32;
+  for (int item = warp; item < nc0 + nc1; item += nw) {
+    const int p = item < nc0 ? 0 : 1;
+    const int c = item - (p ? nc0 : 0);
+    const int cnt = p ? cnt1 : cnt0;
+    const int t = c * 32 + lane;
+    T x = (t < cnt) ? v[p + 2 * t] : (T)0;
 #pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        T y = __shfl_down_sync(0xffffffffu, x, off);
-        if (lane + off < 32) x += y;
-      }
-      x += carry;
-      if (t < cnt) S[p + 2 * t] = x;
-      carry = __shfl_sync(0xffffffffu, x, 0);
+    for (int off = 1; off < 32; off <<= 1) {
+      T y = __shfl_down_sync(0xffffffffu, x, off);
+      if (lane + off < 32) x += y;
     }
+    if (t < cnt) S[p + 2 * t] = x;
+    if (lane == 0) tot[p][c] = x;
   }
+  __syncthreads();
+  for (int item = warp; item < nc0 + nc1; item += nw) {
+    const int p = item < nc0 ? 0 : 1;
+    const int c = item - (p ? nc0 : 0);
+    const int cnt = p ? cnt1 : cnt0, nc = p ? nc1 : nc0;
+    T carry = (T)0;
+    for (int cc = nc - 1; cc > c; --cc) carry = tot[p][cc] + carry;
+    const int t = c * 32 + lane;
+    if (t < cnt) S[p + 2 * t] = S[p + 2 * t] + carry;
+  }
+  __syncthreads();
 }
 
 // Exact power-of-two balancing of the rows that share one complex FFT.  The two rows of a pair ride in
