@@ -432,6 +432,24 @@ size_t fx_deriv_smem_bytes(int nr, int prec, bool fix, bool fuse) {
   return t + (fix ? 7 * (size_t)nr * sizeof(double) : 0) + (fuse ? ((size_t)nr * nr + nr) * sizeof(double) : 0);
 }
 
+// One asynchronous global -> shared copy of an element of 4, 8 or 16 bytes (the issuing thread does not
+// wait for the data: a loop of such copies has all its loads in flight at once).
+template <int BYTES>
+__device__ __forceinline__ void cp_async_bytes(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (BYTES == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem));
+  else if constexpr (BYTES == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem));
+  else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
+}
+template <typename E>
+__device__ __forceinline__ void cp_async_elem(E* smem, const E* gmem) {
+  static_assert(sizeof(E) == 4 || sizeof(E) == 8 || sizeof(E) == 16, "element size");
+  cp_async_bytes<(int)sizeof(E)>(smem, gmem);
+}
+__device__ __forceinline__ void cp_async_all_done() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_all;\n" ::: "memory");
+}
+
 template <typename T>
 __global__ void __launch_bounds__(384) k_fx_deriv(FxArgs a, T* deriv, size_t deriv_stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -446,17 +464,20 @@ __global__ void __launch_bounds__(384) k_fx_deriv(FxArgs a, T* deriv, size_t der
   double* D2sm = xd + (a.fix.on ? 7 * nr : 0);        // fused right-hand side: A2_SINE's D2 (FP64)
   const T* Drg = reinterpret_cast<const T*>(a.ops.Dr);
   const T* D2g = reinterpret_cast<const T*>(a.ops.D2r2);
+  // the operators (and the rows of a pending fix) stream in asynchronously: one L2 round trip, not one per
+  // element each thread copies
   for (int e = threadIdx.x; e < nr * nr; e += blockDim.x) {
-    ops[e] = Drg[e];
-    ops[nr * nr + e] = D2g[e];
-    if (a.fuse_rhs) D2sm[e] = __ldg(a.rl.D2s + e);
+    cp_async_elem(ops + e, Drg + e);
+    cp_async_elem(ops + nr * nr + e, D2g + e);
+    if (a.fuse_rhs) cp_async_elem(D2sm + e, a.rl.D2s + e);
   }
   const int N = M * nr;
   if (a.fix.on) {
     for (int e = threadIdx.x; e < 3 * nr; e += blockDim.x) {
       const int f = e / nr, m = e - f * nr;
-      xd[e] = a.fix.X[(size_t)b * a.x_stride + (size_t)f * N + (size_t)k * nr + m];
+      cp_async_elem(xd + e, a.fix.X + (size_t)b * a.x_stride + (size_t)f * N + (size_t)k * nr + m);
     }
+    cp_async_all_done();
     __syncthreads();
     if (nr <= 32) apply_pending_fix<4>(a, b, k, xd, sc);
     else apply_pending_fix<2>(a, b, k, xd, sc);
@@ -470,7 +491,8 @@ __global__ void __launch_bounds__(384) k_fx_deriv(FxArgs a, T* deriv, size_t der
     });
     if (a.fuse_rhs)
       for (int e = threadIdx.x; e < nr; e += blockDim.x)
-        D2sm[nr * nr + e] = __ldg(a.X + (size_t)b * a.x_stride + (size_t)k * nr + e);
+        cp_async_elem(D2sm + nr * nr + e, a.X + (size_t)b * a.x_stride + (size_t)k * nr + e);
+    cp_async_all_done();
   }
   __syncthreads();
   T* D = deriv + (size_t)b * deriv_stride;
@@ -527,13 +549,13 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
   U* red = reinterpret_cast<U*>(scl + 32);
   const C* wg = reinterpret_cast<const C*>(a.ops.w);
   const C* eg = reinterpret_cast<const C*>(a.ops.e);
-  for (int i = tid; i < P; i += bd) {
-    Wt[i] = wg[i];
-    Et[i] = eg[i];
+  for (int i = tid; i < P; i += bd) {               // asynchronous: in flight while the row loads
+    cp_async_elem(Wt + i, wg + i);
+    cp_async_elem(Et + i, eg + i);
   }
   for (int i = tid; i < P + 2; i += bd) kf[i] = (T)i;
   const T ir4n = reinterpret_cast<const T*>(a.ops.ir4r2)[n];
-  // (no barrier: the row loads below do not read the tables, the barrier after them covers both)
+  // (no barrier: the row loads below do not read the tables; the one after them covers both)
 
   // which row quantities the pair's two fields need (fields: 0 JT_psi, 1 komega, 2 kDpsi, 3 DT, 4 DC,
   // 5 omega, 6 Dpsi, 7 kT, 8 kC)
@@ -597,6 +619,7 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
     }
   }
   });
+  cp_async_all_done();
   __syncthreads();
   if (need_psi) {
     parity_suffix<T>(pv, Sc, M);                       // (ends with a barrier)
@@ -697,9 +720,9 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_prod(FxArgs a, const T* 
   U* red = reinterpret_cast<U*>(scl + 32);
   const C* wg = reinterpret_cast<const C*>(a.ops.w);
   const C* eg = reinterpret_cast<const C*>(a.ops.e);
-  for (int i = tid; i < P; i += bd) {
-    Wt[i] = wg[i];
-    Et[i] = eg[i];
+  for (int i = tid; i < P; i += bd) {               // asynchronous: in flight while the products load
+    cp_async_elem(Wt + i, wg + i);
+    cp_async_elem(Et + i, eg + i);
   }
   const T* RG = grid + (size_t)b * grid_stride + (size_t)n * 9 * P;
   const T* bs = (MODE == 1) ? reinterpret_cast<const T*>(a.base) + (size_t)b * a.base_stride + (size_t)n * 9 * P
@@ -725,6 +748,7 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_prod(FxArgs a, const T* 
     const int src = makhoul_src(nn, P);
     RB[nn] = cmk<C>(scl[0] * PR[src], scl[1] * PR[P + src]);
   }
+  cp_async_all_done();
   __syncthreads();
   C* Z = fft_rows<T, false>(RB, RA, 1, a.st, Wt);
   const int N = M * nr;
