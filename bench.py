@@ -484,6 +484,24 @@ def bench_served(device, n_requests=1000, rate=200.0, seed=2024, frac_continue=0
     plain_rate = len(sample) / (time.perf_counter() - t0)
     for p_ in plans.values():
         p_.close()
+    # ... and a sample of the mix's integrations (500 steps of dt=1e-3 from seeded states), each alone on an
+    # FP64 plan, so that the whole request mix has a plain-path rate: requests/s = 1 / (0.7 t_con + 0.3 t_int)
+    from spectraldoublediffusiveconvection_gb300.seeds import seeded_state
+    isample = [shapes[int(i)] for i in rng.integers(len(shapes), size=8)]
+    iplans = {sh: Plan(sh[1], sh[0], 2.0, 1e-3, 1.0, 1.0, device=device) for sh in sorted(set(isample))}
+    for sh, p_ in iplans.items():                                      # warm-up: workspace and step graphs
+        p_.step(torch.from_numpy(seeded_state(sh[1], sh[0] - 1, 1)).to(device).reshape(1, -1), 9000.0, 500.0,
+                nsteps=20)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    for k, sh in enumerate(isample):
+        Xi = torch.from_numpy(seeded_state(sh[1], sh[0] - 1, 100 + k)).to(device).reshape(1, -1)
+        iplans[sh].step(Xi, float(rng.uniform(8500.0, 9500.0)), 500.0, nsteps=500)
+    torch.cuda.synchronize(device)
+    t_int = (time.perf_counter() - t0) / len(isample)
+    for p_ in iplans.values():
+        p_.close()
+    plain_mix = 1.0 / (frac_continue / plain_rate + (1.0 - frac_continue) * t_int)
     ok = [c for c in curve if c["p99_ms"] is not None and c["p99_ms"] <= P99_BOUND_MS]
     cap = max(ok, key=lambda c: c["offered_rate_per_s"]) if ok else None
     main.update({
@@ -496,8 +514,16 @@ def bench_served(device, n_requests=1000, rate=200.0, seed=2024, frac_continue=0
                                 "how": "24 continuation requests of the mix, each alone on an FP64 plan with FP64 "
                                        "Jacobian products, one after the other"},
         "capacity_vs_plain_same_workload": (cap["continuation_solves_per_s"] / plain_rate) if cap else None,
+        "capacity_requests_per_s": (cap["continuation_solves_per_s"] + cap["integration_requests_per_s"]) if cap else None,
+        "plain_same_mix": {"requests_per_s": plain_mix, "integration_seconds_per_request": t_int,
+                           "continuation_seconds_per_request": 1.0 / plain_rate,
+                           "how": "the mix's two kinds on the plain FP64 path one request at a time: 24 continuation "
+                                  "requests and 8 of its 500-step integrations, combined 70/30 as the mix"},
+        "capacity_vs_plain_same_mix": ((cap["continuation_solves_per_s"] + cap["integration_requests_per_s"])
+                                       / plain_mix) if cap else None,
         "saturation_vs_plain_same_workload": max(c["continuation_solves_per_s"] for c in curve) / plain_rate,
-        "sweep": [{k: c[k] for k in ("offered_rate_per_s", "continuation_solves_per_s", "integration_steps_per_s",
+        "sweep": [{k: c[k] for k in ("offered_rate_per_s", "continuation_solves_per_s", "integration_requests_per_s",
+                                      "integration_steps_per_s",
                                       "p50_ms", "p99_ms", "queue_p99_ms", "device_p99_ms", "errors", "error_samples")}
                   for c in curve],
         "tensor_core_timeouts": tc_timeouts,
