@@ -168,7 +168,7 @@ class ShellBatch:
             best = min(best, e0.elapsed_time(e1) * 1e-3 / reps)
         return best
 
-    def autotune(self, steps_per_launch=5, reps=3, layouts=(1, 2, 3, 4, 5, 6, 7, 8), fx_modes=(1, 2), min_gain=0.015):
+    def autotune(self, steps_per_launch=5, reps=3, layouts=(1, 2, 3, 4, 5, 6, 7, 8, 9), fx_modes=(1, 2), min_gain=0.015):
         """Greedy per-group choice of the chain layout, then of the nonlinear-term kernel (fused or split),
         minimising the time of one graph launch; a change is kept only if it gains more than min_gain (the
         groups share the GPU, so single timings are noisy), and the starting choices are kept when the

@@ -743,7 +743,7 @@ int sdd_krylov_basis(const sdd_plan* p, int shell, int max_cols, double* out, in
 }
 
 int sdd_plan_set_chain_layout(sdd_plan* p, int layout) {
-  if (!p || layout < 0 || layout > 8) return SDD_ERR_ARG;
+  if (!p || layout < 0 || layout > 9) return SDD_ERR_ARG;
   if (p->chain_layout != layout) clear_step_graphs(p);
   p->chain_layout = layout;
   return SDD_OK;

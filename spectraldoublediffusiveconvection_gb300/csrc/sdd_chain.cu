@@ -453,6 +453,150 @@ __global__ void k_chain_shell(ChainArgs a, int wp, int wt) {
   else ref_chain<1>(a, 2, par, b, threadIdx.x - 32 * (wp + wt), 32 * wt, 3, csm + sp + sg);
 }
 
+// Layout 9: the pre-pass form (f_j = h_j + A_j f_e + B_j bf_e for psi, f_j = h_j - w Linv_j b for T and S;
+// h = Linv g from k_mode_mv / k_mode_mv32, so the fused and the FP32 right-hand sides work) with the three
+// chains of one (parity, shell) in one CTA, each on its own warps, named barrier and cp.async ring: psi rows
+// over 2 lanes (one matvec of 2 nr columns: nr multiply-adds per lane and step), T and S one lane per row
+// (nr multiply-adds).  The arithmetic of each chain is that of k_chain<2> (psi) and k_chain<1> (T, S).
+__host__ __device__ inline size_t pre_group_doubles(int M, int nr, int ldl, bool a4) {
+  const size_t blk = (size_t)(a4 ? 2 * nr : nr) * ldl;
+  const size_t ns = (size_t)((M + 1) / 2);
+  return 3 * blk + 4 * (ns + 1) + 4 * (size_t)nr;
+}
+
+template <int TPR>
+__device__ __forceinline__ void pre_chain(const ChainArgs& a, int field, int par, int b, int t, int nt, int bar,
+                                          double* sm) {
+  const int M = a.M, nr = a.nr, ldl = a.ldl;
+  const bool a4 = (field == 0);
+  const size_t foff = (size_t)field * a.field_off;
+  double* f = a.f + (size_t)b * a.f_stride + foff;
+  const double* sub = a.sub ? a.sub + (size_t)b * a.sub_stride + foff : nullptr;
+  float* f32 = a.f32 ? a.f32 + (size_t)b * a.f32_stride + foff : nullptr;
+  const int i = t / TPR, q = t % TPR;
+  const bool row_ok = i < nr;
+  const bool lead = row_ok && q == 0;
+  const int ir = row_ok ? i : 0;
+  const int S = (M - par + 1) / 2;
+  if (a.sym && !(a4 ? par == 0 : par == 1)) {          // symmetric: the other parity's rows are zero
+    for (int e = t; e < S * nr; e += nt) {
+      const int st = e / nr, c = e - st * nr;
+      f[(size_t)(M - 1 - (par + 2 * st)) * nr + c] = 0.0;
+      if (f32) f32[(size_t)(M - 1 - (par + 2 * st)) * nr + c] = 0.0f;
+    }
+    return;
+  }
+  const int ncol = a4 ? 2 * nr : nr;
+  const int blk = ncol * ldl;
+  double* Lb0 = sm;                                    // 3-slot ring of step matrices
+  double* cf = sm + 3 * blk;                           // per-step scalars, 4 per step, one step past the end
+  double* x2 = cf + 4 * (size_t)(S + 1);               // 2 buffers of the matvec operand ([f_e; bf_e] or b)
+  const double* Mat = a4 ? a.ABA4 : (field == 1 ? a.LinvT : a.LinvS);
+  const double* coef = a4 ? a.coefA4 : (field == 1 ? a.coefT : a.coefS);
+  copy_block_g(Lb0, Mat + (size_t)par * blk, blk, t, nt);
+  cp_async_commit();
+  if (S > 1) copy_block_g(Lb0 + blk, Mat + (size_t)(par + 2) * blk, blk, t, nt);
+  cp_async_commit();
+  for (int e = t; e < 4 * (S + 1); e += nt) {
+    const int jj = par + 2 * (e >> 2);
+    cf[e] = jj < M ? coef[(size_t)jj * 4 + (e & 3)] : 0.0;
+  }
+  for (int c = t; c < 4 * nr; c += nt) x2[c] = 0.0;
+  const double* hrow = a.g + (size_t)b * a.g_stride + foff + ir;
+  auto h_at = [&](int st) { return st < S ? hrow[(size_t)(M - 1 - (par + 2 * st)) * nr] : 0.0; };
+  double hn0 = h_at(0), hn1 = h_at(1);
+  double fe = 0.0, bfe = 0.0;                          // psi: f_e_i, bf_e_i;  T/S: b_i in fe
+  for (int st = 0; st < S; ++st) {
+    const int jj = par + 2 * st;
+    const int row = M - 1 - jj;
+    const double* cur = Lb0 + (st % 3) * blk;
+    const double* xs = x2 + (st & 1) * 2 * nr;
+    double* xn = x2 + ((st + 1) & 1) * 2 * nr;
+    cp_async_wait<1>();
+    group_sync(bar, nt);                               // block st landed; this step's x2 visible
+    if (st + 2 < S) copy_block_g(Lb0 + ((st + 2) % 3) * blk, Mat + (size_t)(jj + 4) * blk, blk, t, nt);
+    cp_async_commit();
+    const double hi = hn0;
+    hn0 = hn1;
+    hn1 = h_at(st + 2);
+    double fi;
+    if (a4) {
+      const double pre = fma(cf[4 * st + 3], fe, bfe);   // bf_e + bjt f_e, off the matvec's path
+      double acc = (q == 0) ? hi : 0.0;
+      if (TPR == 1) {
+        double acc1 = 0.0;
+        if (st > 0) {
+          int c = 0;
+#pragma unroll 4
+          for (; c + 1 < ncol; c += 2) {
+            acc = fma(cur[c * ldl + ir], xs[c], acc);
+            acc1 = fma(cur[(c + 1) * ldl + ir], xs[c + 1], acc1);
+          }
+          if (c < ncol) acc = fma(cur[c * ldl + ir], xs[c], acc);
+        }
+        acc += acc1;
+      } else if (st > 0) {
+#pragma unroll 8
+        for (int c = q; c < ncol; c += TPR) acc = fma(cur[c * ldl + ir], xs[c], acc);
+      }
+      fi = group_sum<TPR>(acc);
+      fe += fi;
+      bfe = fma(cf[4 * st + 2], fi, pre);
+      if (lead) {
+        xn[i] = fe;
+        xn[nr + i] = bfe;
+      }
+    } else {
+      double acc = 0.0;
+      if (TPR == 1) {
+        double acc1 = 0.0;
+        int c = 0;
+#pragma unroll 4
+        for (; c + 1 < nr; c += 2) {
+          acc = fma(cur[c * ldl + ir], xs[c], acc);
+          acc1 = fma(cur[(c + 1) * ldl + ir], xs[c + 1], acc1);
+        }
+        if (c < nr) acc = fma(cur[c * ldl + ir], xs[c], acc);
+        acc += acc1;
+      } else {
+#pragma unroll 8
+        for (int c = q; c < nr; c += TPR) acc = fma(cur[c * ldl + ir], xs[c], acc);
+      }
+      fi = fma(-cf[4 * st + 1], group_sum<TPR>(acc), hi);
+      fe = fma(cf[4 * (st + 1)], fi, fe);             // the b of the next step
+      if (lead) xn[i] = fe;
+    }
+    if (lead) {
+      f[(size_t)row * nr + i] = fi;
+      if (f32) f32[(size_t)row * nr + i] = (float)fi;
+    }
+  }
+  cp_async_wait<0>();
+  if (sub) {  // Newton residual: f -= sub (the group's own writes are visible after the barrier)
+    group_sync(bar, nt);
+    for (int e = t; e < S * nr; e += nt) {
+      const int st = e / nr, c = e - st * nr;
+      const size_t o = (size_t)(M - 1 - (par + 2 * st)) * nr + c;
+      f[o] -= sub[o];
+    }
+  }
+}
+
+__global__ void k_chain_shell_pre(ChainArgs a, int wp, int wt) {
+  extern __shared__ __align__(16) double csm[];
+  const int par = blockIdx.x, b = blockIdx.y;
+  if (a.active && !a.active[b]) return;
+  const int w = threadIdx.x >> 5;
+  const size_t sp = pre_group_doubles(a.M, a.nr, a.ldl, true), sg = pre_group_doubles(a.M, a.nr, a.ldl, false);
+  if (w < wp) pre_chain<2>(a, 0, par, b, threadIdx.x, 32 * wp, 1, csm);
+  else if (w < wp + wt) pre_chain<1>(a, 1, par, b, threadIdx.x - 32 * wp, 32 * wt, 2, csm + sp);
+  else pre_chain<1>(a, 2, par, b, threadIdx.x - 32 * (wp + wt), 32 * wt, 3, csm + sp + sg);
+}
+
+static size_t chain_shell_pre_smem_bytes(int M, int nr, int ldl) {
+  return (pre_group_doubles(M, nr, ldl, true) + 2 * pre_group_doubles(M, nr, ldl, false)) * sizeof(double);
+}
+
 static size_t chain_ref_smem_bytes(int M, int nr, int ldl) {
   return ref_group_doubles(M, nr, ldl, true) * sizeof(double);
 }
@@ -984,12 +1128,15 @@ int resolve_chain_layout(const ChainArgs& a, int batch, int nfields) {
   if (layout == 8 && (nfields != 3 || a.field0 != 0 || a.fuse_rhs || a.g32 ||
                       chain_shell_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin))
     layout = 6;
+  // layout 9 needs all three fields and its three rings in one CTA
+  if (layout == 9 && (nfields != 3 || a.field0 != 0 || chain_shell_pre_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin))
+    layout = 5;
   if (layout == 0 && c3.nch > 1 && c3.GA4 && 2 * nfields * batch * c3.nch <= 2 * sms) layout = 3;
   if (layout == 0 && c2.nch > 1 && c2.GA4 && 2 * nfields * batch * c2.nch <= 2 * sms) layout = 2;
   // layouts 6 / 7 need the full right-hand side in FP64: with the fused or the FP32 one, the pre-pass form
   if ((layout == 6 || layout == 7) && (a.fuse_rhs || a.g32)) layout = 5;
   if ((layout == 6 || layout == 7) && chain_ref_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin) layout = 2;
-  if (layout != 2 && layout != 3 && layout != 6 && layout != 7 && chain_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin)
+  if (layout != 2 && layout != 3 && layout < 6 && chain_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin)
     layout = 2;   // whole chain too long for shared memory
   // a launch that fills the SMs: the reference-order chains (4 nr^2 multiply-adds per mode instead of 7), a
   // step's three chains per CTA where they fit (64 shells N_r=30 N_theta=256: 287 us against 301 us)
@@ -1006,6 +1153,21 @@ int resolve_chain_layout(const ChainArgs& a, int batch, int nfields) {
 cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStream_t s) {
   ChainArgs a = a_in;
   const int layout = resolve_chain_layout(a, batch, nfields);
+  if (layout == 9) {                  // the pre-pass form, three chains per CTA
+    if (nfields != 3 || a.field0 != 0) return cudaErrorInvalidValue;
+    cudaError_t e = launch_mode_mv<false>(a, batch, nfields, s, mv_per_warp(a, batch, nfields));   // h = Linv g
+    if (e != cudaSuccess) return e;
+    a.g = a.h;
+    a.g_stride = a.h_stride;
+    const int wp = (2 * a.nr + 31) / 32, wt = (a.nr + 31) / 32;
+    static unsigned long long done = 0;
+    if ((e = ensure_smem_attr(k_chain_shell_pre, &done)) != cudaSuccess) return e;
+    e = launch_kernel(k_chain_shell_pre, dim3(2, batch), dim3(32 * (wp + 2 * wt)),
+                      chain_shell_pre_smem_bytes(a.M, a.nr, a.ldl), s, a, wp, wt);
+    ktimer_mark(SDD_K_CHAIN, s);
+    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+  }
   if (layout == 8) {                  // the reference's order, three chains per CTA
     if (a.fuse_rhs || a.g32 || !a.D2A4 || nfields != 3 || a.field0 != 0) return cudaErrorInvalidValue;
     const int wp = (2 * a.nr + 31) / 32, wt = (a.nr + 31) / 32;

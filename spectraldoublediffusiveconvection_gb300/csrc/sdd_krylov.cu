@@ -130,12 +130,13 @@ __global__ void __launch_bounds__(kDotThreads) k_dot_partials(const double* __re
     reduce_partials(part, b, nv, nchunk, h, ldh, accumulate);
 }
 
-// w[b] -= sum_{i<nv} V_i[b] coef[b*ldc + i] for the shells with sub_mask[b] (k_sub_combination's arithmetic),
-// then nrm2[b] = |w[b]|^2 for the shells with norm_mask[b] (0 for the others): per thread over its elements
+// w[b] -= sum_{i<nv} V_i[b] coef[b*ldc + i] for the shells with sub_mask[b] (per element, the products summed
+// in index order), then nrm2[b] = |w[b]|^2 for the shells with norm_mask[b] (0 for the others): per thread over its elements
 // in index order, the warp tree of k_dot_partials, the warps in order, the chunks of kSubChunk elements in
 // order.  The chunks are a quarter of the dot products' (the update's dependent multiply-adds over the
 // basis dominate, so one shell's update spreads over four times the CTAs).  With reo != nullptr the shell's
-// last CTA also sets the second-pass flag of column j (k_reorth_mask's test).
+// last CTA also sets the second-pass flag of column j: active and |w'|^2 < eta^2 (|w'|^2 + |h|^2), where
+// |w|^2 = |w'|^2 + |h|^2 for an orthonormal basis.
 __global__ void __launch_bounds__(kDotThreads) k_sub_norm(const double* __restrict__ V, size_t vstride_i, double* w,
                                                          const double* __restrict__ coef, int ldc, int n, int ld,
                                                          int nv, const int* __restrict__ sub_mask,
@@ -201,20 +202,6 @@ __global__ void k_dot_reduce(const double* __restrict__ part, int nv, int nchunk
     for (int c = 0; c < nchunk; ++c) t += p[c];
     if (accumulate) h[(size_t)b * ldh + i] += t;
     else h[(size_t)b * ldh + i] = t;
-  }
-}
-
-// w[b] -= sum_{i<nv} V_i[b] * coef[b*ldc + i]
-__global__ void k_sub_combination(const double* __restrict__ V, size_t vstride_i, double* __restrict__ w,
-                                  const double* __restrict__ coef, int ldc, int n, int ld, int nv,
-                                  const int* __restrict__ active) {
-  const int b = blockIdx.y;
-  if (active && !active[b]) return;
-  const double* cb = coef + (size_t)b * ldc;
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int i = 0; i < nv; ++i) s += V[(size_t)i * vstride_i + (size_t)b * ld + e] * cb[i];
-    w[(size_t)b * ld + e] -= s;
   }
 }
 
@@ -339,22 +326,6 @@ __global__ void __launch_bounds__(32) k_arnoldi_finish(GmresState s, const doubl
   for (int i = lane; i < j; i += 32) H[i * m + j] = col[i];
 }
 
-// Whether shell b repeats the Gram-Schmidt pass of column j: |w'|^2 = nrm2[b] after the first pass,
-// |w|^2 = |w'|^2 + |h|^2 for an orthonormal basis.
-__global__ void k_reorth_mask(GmresState s, const double* __restrict__ nrm2, int j, double eta2, int B) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B) return;
-  int r = 0;
-  if (s.active[b]) {
-    const double* hc = s.hcol + (size_t)b * (s.m + 1);
-    double h2 = 0.0;
-    for (int i = 0; i <= j; ++i) h2 = fma(hc[i], hc[i], h2);
-    const double n1 = nrm2[b];
-    r = n1 < eta2 * (n1 + h2) ? 1 : 0;
-  }
-  s.reo[b] = r;
-}
-
 // Back substitution R y = g over the first kb[b] columns.
 __global__ void k_solve_y(GmresState s, int B) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -466,12 +437,6 @@ cudaError_t krylov_sub_norm(const double* V, size_t vstride_i, double* w, const 
   return cudaGetLastError();
 }
 
-cudaError_t krylov_sub_combination(const double* V, size_t vstride_i, double* w, const double* coef, int ldc,
-                                   int n, int ld, int nv, int B, cudaStream_t st, const int* active) {
-  k_sub_combination<<<dim3(grid_x(n), B), 256, 0, st>>>(V, vstride_i, w, coef, ldc, n, ld, nv, active);
-  return cudaGetLastError();
-}
-
 cudaError_t krylov_add_combination(const double* V, size_t vstride_i, double* x, const double* y, int ldy,
                                    const int* kb, int n, int ld, int B, cudaStream_t st) {
   k_add_combination<<<dim3(grid_x(n), B), 256, 0, st>>>(V, vstride_i, x, y, ldy, kb, n, ld);
@@ -503,11 +468,6 @@ cudaError_t krylov_cycle_start(const GmresState& s, const double* nrm2, int B, c
 cudaError_t krylov_arnoldi_finish(const GmresState& s, const double* nrm2, int j, int B, cudaStream_t st) {
   if (s.m > kMaxRestart || j >= s.m) return cudaErrorInvalidValue;
   k_arnoldi_finish<<<B, 32, 0, st>>>(s, nrm2, j, B);
-  return cudaGetLastError();
-}
-
-cudaError_t krylov_reorth_mask(const GmresState& s, const double* nrm2, int j, double eta, int B, cudaStream_t st) {
-  k_reorth_mask<<<(B + 63) / 64, 64, 0, st>>>(s, nrm2, j, eta * eta, B);
   return cudaGetLastError();
 }
 

@@ -43,12 +43,11 @@ cudaError_t krylov_dots(const double* V, size_t vstride_i, const double* w, int 
                         const int* active = nullptr, int* ticket = nullptr);
 // One launch for a Gram-Schmidt pass's update and the new norm: w -= V coef where sub_mask (nullable: all),
 // nrm2 = |w|^2 where norm_mask (nullable: all; 0 elsewhere), with the sums of krylov_dots; reo_of
-// (nullable): also set reo_of->reo for column j as krylov_reorth_mask does.  ticket: B zeroed counters.
+// (nullable): also set reo_of->reo for column j (active and |w'|^2 < eta^2 (|w'|^2 + |h|^2), the shells
+// whose first pass cancelled w below eta of its norm).  ticket: B zeroed counters.
 cudaError_t krylov_sub_norm(const double* V, size_t vstride_i, double* w, const double* coef, int ldc, int n, int ld,
                             int nv, int B, const int* sub_mask, const int* norm_mask, double* part, int* ticket,
                             double* nrm2, const GmresState* reo_of, int j, double eta, cudaStream_t st);
-cudaError_t krylov_sub_combination(const double* V, size_t vstride_i, double* w, const double* coef, int ldc,
-                                   int n, int ld, int nv, int B, cudaStream_t st, const int* active = nullptr);
 cudaError_t krylov_add_combination(const double* V, size_t vstride_i, double* x, const double* y, int ldy,
                                    const int* kb, int n, int ld, int B, cudaStream_t st);
 // out = a * scale[b]; out32 / out2 (nullable, same strides): the result also rounded to FP32 / copied
@@ -59,8 +58,6 @@ cudaError_t krylov_masked_sub(double* X, const double* dx, const int* mask, int 
                               cudaStream_t st);
 cudaError_t krylov_cycle_start(const GmresState& s, const double* nrm2, int B, cudaStream_t st);
 cudaError_t krylov_arnoldi_finish(const GmresState& s, const double* nrm2, int j, int B, cudaStream_t st);
-// s.reo[b] = active and nrm2[b] < eta^2 (nrm2[b] + sum_{i<=j} hcol[b][i]^2) (|w|^2 = |w'|^2 + |h|^2)
-cudaError_t krylov_reorth_mask(const GmresState& s, const double* nrm2, int j, double eta, int B, cudaStream_t st);
 cudaError_t krylov_solve_y(const GmresState& s, int B, cudaStream_t st);
 cudaError_t krylov_copy_scaled(const double* src, int lds, double* dst, int ldd, int n, double a, const double* last,
                                int B, cudaStream_t st);

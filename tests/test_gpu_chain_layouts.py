@@ -1,7 +1,7 @@
 """Every chain layout of the implicit solves (1 one lane per row, 2 chunked with a sequential carry, 3
 chunked with a parallel carry, 4 rows split over 4 lanes, 5 over 2 lanes, 6 and 7 the reference's own order
 of operations with rows over 2 or 4 lanes, 8 that order with the three chains of a (parity, shell) in one
-CTA) against the oracle's A4_BSub_TSTEP_V2 / NAB2_BSub_TSTEP_V2
+CTA, 9 the h pre-pass form with the three chains of a (parity, shell) in one CTA) against the oracle's A4_BSub_TSTEP_V2 / NAB2_BSub_TSTEP_V2
 chains (Matrix_Operators.py:1033-1194), alone and inside the step, the Newton residual and its Jacobian.
 The chunked layouts reorder the arithmetic (carried states through precomputed chunk maps or their
 products), so they agree with the sequential chain to rounding, not bitwise."""
@@ -17,7 +17,7 @@ SHAPES = [(16, 16, False), (20, 64, False), (30, 256, False), (48, 512, False), 
 
 
 @pytest.mark.parametrize("N_r,N_fm,sym", SHAPES)
-@pytest.mark.parametrize("layout", [1, 2, 3, 4, 5, 6, 7, 8])
+@pytest.mark.parametrize("layout", [1, 2, 3, 4, 5, 6, 7, 8, 9])
 def test_chain_solves_against_oracle(cuda, N_r, N_fm, sym, layout):
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     torch = cuda
@@ -197,5 +197,56 @@ def test_automatic_layout_choice(cuda):
     assert p.chain_choice(64) == (3, 8, 16)
     p.set_chain_layout(8)
     assert p.chain_choice(64)[0] == 8
+    p.set_chain_layout(9)
+    assert p.chain_choice(64)[0] == 9
     with pytest.raises(Exception):
-        p.set_chain_layout(9)
+        p.set_chain_layout(10)
+
+
+@pytest.mark.parametrize("N_r,N_fm,split", [(20, 64, 1), (30, 256, 2), (48, 512, 1), (12, 16, 2), (65, 32, 1)])
+def test_prepass_three_chain_layout_in_steps_and_newton(cuda, N_r, N_fm, split):
+    """Layout 9 (h pre-pass, the three chains of a (parity, shell) per CTA; with the fused right-hand side of
+    the split nonlinear term too): steps, the Newton residual and Jacobian against the oracle, a batch equal
+    to its shells alone, and mixed Jacobian products with FP32 right-hand sides (mixed_matvec 2) reaching the
+    FP64 residual.  N_r = 48 with N_theta = 512 and nr = 64 do not fit their three rings in a CTA: layout 5 runs,
+    rows over 4 warps for nr > 32 (layout 4)."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    nr = N_r - 1
+    X = O.seeded_state(N_fm, nr, 1234)
+    dv = O.seeded_state(N_fm, nr, 77)
+    Xt = torch.from_numpy(np.stack([X, 2 * X, 0.5 * X])).cuda()
+    ops = O.Operators(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01)
+    p = Plan(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01)
+    p.set_chain_layout(9)
+    p.set_fx_split(split)
+    assert p.chain_choice(3)[0] == (4 if (N_r, N_fm) in ((48, 512), (65, 32)) else 9)
+    Y = p.step(Xt, 8000.0, 500.0, nsteps=3).cpu().numpy()
+    for k, x in enumerate([X, 2 * X, 0.5 * X]):
+        r = x
+        for _ in range(3):
+            r = O.step(ops, r, 8000.0, 500.0, False)
+        assert rel(Y[k], r) < 1e-12
+        Yk = p.step(Xt[k:k + 1].clone(), 8000.0, 500.0, nsteps=3).cpu().numpy()
+        assert np.array_equal(Yk[0], Y[k])
+    ops1 = O.Operators(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
+    p1 = Plan(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
+    p1.set_chain_layout(9)
+    p1.set_fx_split(split)
+    dvt = torch.from_numpy(np.stack([dv, dv, dv])).cuda()
+    F = p1.pfx(Xt, 8000.0, 500.0).cpu().numpy()
+    J = p1.pdfx(dvt, Xt, 8000.0, 500.0).cpu().numpy()
+    for k, x in enumerate([X, 2 * X, 0.5 * X]):
+        assert rel(F[k], O.PFX(ops1, x, 8000.0, 500.0, False)) < 1e-12
+        assert rel(J[k], O.PDFX(ops1, dv, x, 8000.0, 500.0, False)) < 1e-12
+    if N_fm > 256:
+        return
+    pm = Plan(N_fm, N_r, 2.0, 1.0, 1.0, 0.01, precision="mixed")
+    pm.set_chain_layout(9)
+    X0 = np.stack([O.seeded_state(N_fm, nr, 40 + s) for s in range(4)])
+    Xm = torch.from_numpy(X0.copy()).cuda()
+    res = pm.newton(Xm, torch.linspace(7000.0, 9000.0, 4, dtype=torch.float64, device="cuda"), 500.0, tol=1e-10,
+                    mixed_matvec=2)
+    for b in range(4):
+        assert res[b]["converged"] and res[b]["residual"] <= 1e-10
+        assert np.linalg.norm(O.PFX(ops1, Xm[b].cpu().numpy(), 7000.0 + 2000.0 * b / 3, 500.0, False)) <= 1.5e-10
