@@ -45,6 +45,10 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
 }
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
@@ -830,9 +834,12 @@ __global__ void __launch_bounds__(128) k_mode_mv(ChainArgs a) {
       double* Qs = Drs + (size_t)nr * nr;
       double* gsm = Qs + nr;
       if (a4 && !a.q32) {
-        for (int e = threadIdx.x; e < nr * nr; e += blockDim.x) Drs[e] = a.Dr[e];
+        // asynchronous copies (the Linv block's are in flight too): one L2 round trip for all of them
         const double* q4 = a.out4 + (size_t)b * a.out_stride + (size_t)row * nr;
-        for (int e = threadIdx.x; e < nr; e += blockDim.x) Qs[e] = q4[e];
+        for (int e = threadIdx.x; e < nr * nr; e += blockDim.x) cp_async8(Drs + e, a.Dr + e);
+        for (int e = threadIdx.x; e < nr; e += blockDim.x) cp_async8(Qs + e, q4 + e);
+        cp_async_commit();
+        cp_async_wait<0>();
         __syncthreads();
       }
       for (int n = threadIdx.x; n < nr; n += blockDim.x) gsm[n] = fused_g(a, b, field, row, n, Drs, Qs);

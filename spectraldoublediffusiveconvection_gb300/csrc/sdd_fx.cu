@@ -728,7 +728,8 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_prod(FxArgs a, const T* 
   const T* bs = (MODE == 1) ? reinterpret_cast<const T*>(a.base) + (size_t)b * a.base_stride + (size_t)n * 9 * P
                             : nullptr;
   U m2[2] = {0, 0};
-  for (int i = tid; i < P; i += bd) {
+#pragma unroll 2
+  for (int i = tid; i < P; i += bd) {               // (unrolled: both iterations' grid loads in flight)
     T v0, v1;
     grid_products<T, MODE>(p, RG, bs, i, P, v0, v1);
     if (p == 0) {
