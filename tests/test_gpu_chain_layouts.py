@@ -250,3 +250,33 @@ def test_prepass_three_chain_layout_in_steps_and_newton(cuda, N_r, N_fm, split):
     for b in range(4):
         assert res[b]["converged"] and res[b]["residual"] <= 1e-10
         assert np.linalg.norm(O.PFX(ops1, Xm[b].cpu().numpy(), 7000.0 + 2000.0 * b / 3, 500.0, False)) <= 1.5e-10
+
+
+@pytest.mark.parametrize("layout", [8, 9])
+@pytest.mark.parametrize("N_r,N_fm", [(16, 16), (36, 384)])
+def test_three_chain_layouts_symmetric(cuda, N_r, N_fm, layout):
+    """Symmetric plans under layouts 8 and 9: in each (parity, shell) CTA one or two of the three chains are
+    inactive (their rows are zero) and leave at once while the others run on their own barriers; steps and
+    the Newton residual against the oracle's symmetric solves, a batch equal to its shells alone."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    nr = N_r - 1
+    Xs = [O.seeded_state(N_fm, nr, 60 + s, True) for s in range(3)]
+    ops = O.Operators(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01)
+    p = Plan(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01, symmetric=True)
+    p.set_chain_layout(layout)
+    p.set_fx_split(1)
+    Xt = torch.from_numpy(np.stack(Xs)).cuda()
+    Y = p.step(Xt, 8000.0, 500.0, nsteps=2).cpu().numpy()
+    for k, x in enumerate(Xs):
+        r = x
+        for _ in range(2):
+            r = O.step(ops, r, 8000.0, 500.0, True)
+        assert rel(Y[k], r) < 1e-12
+        assert np.array_equal(p.step(Xt[k:k + 1].clone(), 8000.0, 500.0, nsteps=2).cpu().numpy()[0], Y[k])
+    ops1 = O.Operators(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
+    p1 = Plan(N_fm, N_r, 2.0, 1.0, 1.0, 0.01, symmetric=True)
+    p1.set_chain_layout(layout)
+    F = p1.pfx(Xt, 8000.0, 500.0).cpu().numpy()
+    for k, x in enumerate(Xs):
+        assert rel(F[k], O.PFX(ops1, x, 8000.0, 500.0, True)) < 1e-12
