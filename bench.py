@@ -922,6 +922,34 @@ def profile_step_batch(precision, layout, batch=64, steps=1):
     return 0
 
 
+def probe_phase_boundaries():
+    """The cost of a phase boundary inside a captured CUDA graph (a kernel boundary) against a grid-wide
+    barrier inside one persistent cooperative kernel (sdd_probe_phase_boundaries): 64 phases over one CTA
+    per SM (the single-shell step's kernels fill at most about one SM each) and over four CTAs per SM,
+    without work (the boundary alone) and with 256 dependent FP64 multiply-adds per thread per phase."""
+    import ctypes
+    import torch
+    from spectraldoublediffusiveconvection_gb300 import _lib
+    device = torch.device("cuda", 0)
+    torch.cuda.set_device(device)
+    L = _lib.lib()
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    stream = ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+    out = []
+    for ctas in (sms, 4 * sms):
+        for work in (0, 256):
+            g, pz, to = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_int(0)
+            nph = 64
+            _lib.check(L.sdd_probe_phase_boundaries(ctas, 256, nph, work, 5, ctypes.byref(g), ctypes.byref(pz),
+                                                    ctypes.byref(to), stream), "sdd_probe_phase_boundaries")
+            out.append({"ctas": ctas, "threads": 256, "phases": nph, "fp64_fma_per_thread_per_phase": work,
+                        "graph_us": g.value, "persistent_us": pz.value,
+                        "graph_us_per_phase": g.value / nph, "persistent_us_per_phase": pz.value / nph,
+                        "barrier_timed_out": bool(to.value)})
+    print(json.dumps({"probe": "phase_boundaries", "results": out}))
+    return 0
+
+
 def main():
     if len(sys.argv) > 1 and sys.argv[1] == "--cpu-worker":
         cpu_worker(float(sys.argv[2]), int(sys.argv[3]), int(sys.argv[4]),
@@ -941,7 +969,10 @@ def main():
     ap.add_argument("--profile-newton-batch", action="store_true")
     ap.add_argument("--profile-deriv-tc", type=int, metavar="SHELLS")
     ap.add_argument("--profile-step-batch", nargs=2, metavar=("PRECISION", "LAYOUT"))
+    ap.add_argument("--probe-phase-boundaries", action="store_true")
     args = ap.parse_args()
+    if args.probe_phase_boundaries:
+        return probe_phase_boundaries()
     if args.profile_newton_batch:
         return profile_newton_batch()
     if args.profile_deriv_tc:

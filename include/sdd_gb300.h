@@ -123,6 +123,14 @@ int sdd_plan_set_tensor_cores(sdd_plan* plan, int on);
 /* 1 in *timed_out if a tensor-core kernel of this plan gave up waiting for its matrix products (its outputs
  * were then NaN); 0 otherwise.  Synchronous. */
 int sdd_plan_tensor_core_status(const sdd_plan* plan, int* timed_out);
+/* Phase-boundary probe (no plan): `nphase` phases of `work` dependent FP64 multiply-adds per thread over
+ * ctas x threads threads, once as a captured CUDA graph of nphase kernel launches and once as one
+ * cooperative (persistent) kernel with nphase - 1 grid-wide barriers of its own (bounded spins: a barrier
+ * that runs out sets *barrier_timed_out and the kernel returns).  Best of `reps` timed runs of each, in
+ * microseconds.  SDD_ERR_UNSUPPORTED if the CTAs cannot all be resident at once.  Measures what a persistent
+ * step kernel could save over the captured step graphs; no counterpart in the reference. */
+int sdd_probe_phase_boundaries(int ctas, int threads, int nphase, int work, int reps, double* graph_us,
+                               double* persistent_us, int* barrier_timed_out, void* stream);
 /* How the Newton / continuation GMRES products of this plan ran so far: captured into a CUDA graph (and
  * launched), replayed from a captured graph, or launched kernel by kernel (a product that could not be
  * captured).  The products of every Arnoldi column read one fixed vector, so a solve captures a product

@@ -84,6 +84,8 @@ SIGNATURES = [
     ("sdd_plan_set_tensor_cores", _I, [_VP, _I]),
     ("sdd_plan_tensor_core_status", _I, [_VP, ctypes.POINTER(_I)]),
     ("sdd_plan_set_product_graphs", _I, [_VP, _I]),
+    ("sdd_probe_phase_boundaries", _I, [_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_double),
+                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I), _VP]),
     ("sdd_plan_product_graph_stats", _I, [_VP, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
                                           ctypes.POINTER(ctypes.c_longlong)]),
     ("sdd_plan_chain_choice", _I, [_VP, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
