@@ -105,7 +105,7 @@ def kernel_algorithmic(name, M, nr, nch, layout=3):
 # ------------------------------------------------------------------------------------------------
 class ClockSampler:
     """nvidia-smi clock / throttle-reason samples every 200 ms while the timed region runs."""
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -113,11 +113,16 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.window = None      # (t0, t1) wall-clock bounds of the timed region (mark())
+
+    def mark(self, t0, t1):
+        """The timed region: samples stamped inside it (with a margin of one sampling period) are kept."""
+        self.window = (t0, t1)
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -136,24 +141,32 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
+        import datetime
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
-            if len(f) < 9:
+            if len(f) < 10:
                 continue
             try:
-                sm.append(float(f[1]))
-                smax.append(float(f[2]))
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                ts = None
+            try:
+                rows.append((ts, float(f[2]), float(f[3]), [nm for nm, v in zip(names, f[6:10])
+                                                          if v.lower() == "active"]))
             except ValueError:
                 continue
-            for nm, v in zip(names, f[5:9]):
-                if v.lower() == "active":
-                    reasons.add(nm)
-        sm.sort()
+        inside = rows
+        if self.window and rows:
+            t0, t1 = self.window
+            inside = [r for r in rows if r[0] is not None and t0 - 0.1 <= r[0] <= t1 + 0.1] or rows
+        sm = sorted(r[1] for r in inside)
+        smax = [r[2] for r in inside]
+        reasons = sorted({nm for r in inside for nm in r[3]})
         med = sm[len(sm) // 2] if sm else None
-        return {"sm_mhz": med, "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": med, "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(sm), "samples_in_timed_region": len(inside) if inside is not rows else None}
 
 
 # ------------------------------------------------------------------------------------------------
@@ -575,6 +588,9 @@ def bench_gb300(args):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
 
+    # clocks sampled from before the warm-up (nvidia-smi takes a moment to start), kept for the timed region
+    clocks = ClockSampler(device.index or 0)
+    clocks.start()
     # warm-up
     for _ in range(args.warmup):
         plan.step(Xa, Ra, Ras, nsteps=chunk, out=Xb)
@@ -582,10 +598,9 @@ def bench_gb300(args):
     torch.cuda.synchronize()
 
     # ---- timed region (device-resident): K bench steps, L2 flushed between them (outside the events) --
-    clocks = ClockSampler(device.index or 0)
-    clocks.start()
     barrier(ws)
     torch.cuda.synchronize()
+    wall0 = time.time()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for i in range(args.steps):
         flush.zero_()
@@ -595,6 +610,8 @@ def bench_gb300(args):
         Xa, Xb = Xb, Xa
     torch.cuda.synchronize()
     barrier(ws)
+    clocks.mark(wall0, time.time())
+    time.sleep(0.15)                  # one more sampling period past the region
     ms_total = sum(a.elapsed_time(b) for a, b in evs)
     ck = clocks.stop()
     ms_total = max_over_ranks(ms_total, ws, device)
