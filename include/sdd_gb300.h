@@ -110,9 +110,11 @@ int sdd_plan_reserve(sdd_plan* plan, int max_batch);
  * of fewer than three fields run layout 6).  9: the h pre-pass form (any right-hand side: fused, FP32) with
  * the three chains of one (parity, shell) in one CTA, psi rows over 2 lanes, T and S one lane per row
  * (launches of fewer than three fields, or whose three rings exceed a CTA's shared memory, run layout 5).
- * Set by the batch autotuner; no counterpart in the reference. */
+ * 10 / 11: the chunks of layouts 2 / 3 with each chunk in the reference's order of operations (no h
+ * pre-pass; full FP64 right-hand sides only, else layouts 2 / 3).  Set by the batch autotuner; no
+ * counterpart in the reference. */
 int sdd_plan_set_chain_layout(sdd_plan* plan, int layout);
-/* The layout (1-9) a step of `batch` shells runs under the current setting, with its chunk length and
+/* The layout (1-11) a step of `batch` shells runs under the current setting, with its chunk length and
  * chunks per chain (0 and 1 when not chunked). */
 int sdd_plan_chain_choice(const sdd_plan* plan, int batch, int* layout, int* kc, int* nch);
 /* Mixed plans: the FP32 radial contractions of the nonlinear term (Derivatives, Matrix_Operators.py:698-729)

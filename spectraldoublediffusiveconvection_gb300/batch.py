@@ -84,12 +84,14 @@ class ShellBatch:
         # operations, a shell's three chains of one parity per CTA (layout 8: 4 nr^2 multiply-adds per mode
         # instead of 7; the library runs layout 5 where the right-hand side is fused or FP32, and layout 6
         # where the three rings do not fit a CTA), and chunked chains for N_theta >= 256 with the FP32
-        # nonlinear term, where the long chains of the largest shells set the critical path (84k vs 77k
-        # shell-steps/s); in FP64 the nonlinear term dominates and chunking does not pay.
+        # nonlinear term, where the long chains of the largest shells set the critical path, each chunk in
+        # the reference's order too (layout 10: 96.0k shell-steps/s with it on every group against 88.3k
+        # for the pre-pass chunks of layout 2); in FP64 the nonlinear term dominates and chunking does not
+        # pay.
         sms = _torch().cuda.get_device_properties(self.device).multi_processor_count
         total_rows = sum(g.plan.nr * len(g.idx) for g in self.groups)
         for g in self.groups:
-            g.plan.set_chain_layout(2 if (precision == "mixed" and g.plan.N_fm >= 256) else 8)
+            g.plan.set_chain_layout(10 if (precision == "mixed" and g.plan.N_fm >= 256) else 8)
             g.plan.set_fx_split(1 if 2 * total_rows > sms else 0)
         self.graph = None
         self.steps_per_launch = 0
@@ -168,7 +170,7 @@ class ShellBatch:
             best = min(best, e0.elapsed_time(e1) * 1e-3 / reps)
         return best
 
-    def autotune(self, steps_per_launch=5, reps=3, layouts=(1, 2, 3, 4, 5, 6, 7, 8, 9), fx_modes=(1, 2), min_gain=0.015):
+    def autotune(self, steps_per_launch=5, reps=3, layouts=(1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11), fx_modes=(1, 2), min_gain=0.015):
         """Greedy per-group choice of the chain layout, then of the nonlinear-term kernel (fused or split),
         minimising the time of one graph launch; a change is kept only if it gains more than min_gain (the
         groups share the GPU, so single timings are noisy), and the starting choices are kept when the

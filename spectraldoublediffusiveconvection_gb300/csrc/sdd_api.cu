@@ -743,21 +743,23 @@ int sdd_krylov_basis(const sdd_plan* p, int shell, int max_cols, double* out, in
 }
 
 int sdd_plan_set_chain_layout(sdd_plan* p, int layout) {
-  if (!p || layout < 0 || layout > 9) return SDD_ERR_ARG;
+  if (!p || layout < 0 || layout > 11) return SDD_ERR_ARG;
   if (p->chain_layout != layout) clear_step_graphs(p);
   p->chain_layout = layout;
   return SDD_OK;
 }
 
 static ChainArgs chain_args(const sdd_plan* p, const double* g, double* f, const double* sub);
+static ChainArgs step_chain_args(const sdd_plan* p, int batch);
 
 int sdd_plan_chain_choice(const sdd_plan* p, int batch, int* layout, int* kc, int* nch) {
   if (!p || batch < 1 || !layout || !kc || !nch) return SDD_ERR_ARG;
-  const ChainArgs a = chain_args(p, nullptr, nullptr, nullptr);
+  const ChainArgs a = step_chain_args(p, batch);
   *layout = resolve_chain_layout(a, batch, 3);
-  const bool chunked = *layout == 2 || *layout == 3;
-  *kc = chunked ? p->cs[*layout - 2].kc : 0;
-  *nch = chunked ? p->cs[*layout - 2].nch : 1;
+  const bool chunked = *layout == 2 || *layout == 3 || *layout == 10 || *layout == 11;
+  const int set = (*layout == 3 || *layout == 11) ? 1 : 0;
+  *kc = chunked ? p->cs[set].kc : 0;
+  *nch = chunked ? p->cs[set].nch : 1;
   return SDD_OK;
 }
 
@@ -1001,13 +1003,22 @@ static int apply_step(sdd_plan* p, int batch, const double* Ra, const double* Ra
                        nullptr, defer, fix_in);
 }
 
+// The chain arguments of a plain step of `batch` shells as sdd_step launches them: the right-hand side fused
+// into the split nonlinear term when the step runs that form, so that the layout resolves as in the step.
+// The step reserves its scratch (the grid and derivative buffers the split form needs) before it launches,
+// so the rule is applied as if they were there.
+static ChainArgs step_chain_args(const sdd_plan* p, int batch) {
+  ChainArgs ca = chain_args(p, nullptr, nullptr, nullptr);
+  ca.fuse_rhs = fx_split_rule(p->fx_split, p->nr, batch) ? 1 : 0;
+  return ca;
+}
+
 // Whether sdd_step's steps leave the chains' correction to the next step's nonlinear term: layout 3 with
 // the split nonlinear term, non-linear steps.
 static bool step_defers_fix(sdd_plan* p, int batch, int linear) {
   if (linear || p->cs[1].nch < 2) return false;
-  if (resolve_chain_layout(chain_args(p, nullptr, nullptr, nullptr), batch, 3) != 3) return false;
-  const FxArgs fa = fx_args(p, p->prec, nullptr, nullptr, p->out4);
-  return fx_uses_split(fa, batch, 0);
+  const ChainArgs ca = step_chain_args(p, batch);
+  return ca.fuse_rhs && resolve_chain_layout(ca, batch, 3) == 3;
 }
 
 // The correction left pending by the last step of a sequence, on the state X (and its FP32 copy).

@@ -290,6 +290,166 @@ __global__ void k_chain(ChainArgs a) {
   }
 }
 
+// Layouts 10 and 11: the chunked chains of layouts 2 and 3 with each chunk in the reference's order of
+// operations (the step of ref_chain below: per psi step D2 f_e, then Linv_j (g_j + b); per T/S step
+// Linv_j (g_j - w b)), so that no h = Linv g pre-pass runs: each chunk starts from a zero carried state
+// exactly as in layouts 2 and 3 (the carried state [f_e; bf_e] or b is the same quantity), writes the same
+// end state (psi: f_e after its last f, bf_e), and the same carries and corrections follow.  g is the full
+// right-hand side.  One CTA per (field, parity, chunk, shell), rows over TPR lanes.
+template <int TPR, int CR>
+__global__ void k_chain_cref(ChainArgs a) {
+  extern __shared__ __align__(16) double csm[];
+  const int field = a.field0 + (blockIdx.x >> 1);
+  const int par = blockIdx.x & 1;
+  const int b = blockIdx.y;
+  if (a.active && !a.active[b]) return;
+  const int M = a.M, nr = a.nr, ldl = a.ldl;
+  const bool a4 = (field == 0);
+  const size_t foff = (size_t)field * a.field_off;
+  double* f = a.f + (size_t)b * a.f_stride + foff;
+  const double* sub = a.sub ? a.sub + (size_t)b * a.sub_stride + foff : nullptr;
+  const int tid = threadIdx.x;
+  const int i = tid / TPR, q = tid % TPR;
+  const bool row_ok = i < nr;
+  const bool lead = row_ok && q == 0;
+  const int ir = row_ok ? i : 0;
+  const int S = (M - par + 1) / 2;
+  const int chunk = (int)blockIdx.z;
+  const int s0 = chunk * a.kc;
+  const int s1 = min(S, s0 + a.kc);
+  if (s0 >= S) return;
+  const int nsteps = s1 - s0;
+  double* dout = a.dbuf + (size_t)b * a.d_stride + ((size_t)(field * 2 + par) * a.nch + chunk) * a.ldd;
+  const bool active = !a.sym || (a4 ? par == 0 : par == 1);
+  float* f32 = a.f32 ? a.f32 + (size_t)b * a.f32_stride + foff : nullptr;   // final values only (no sub)
+  if (!active) {
+    for (int e = tid; e < nsteps * nr; e += blockDim.x) {
+      const int st = e / nr, c = e - st * nr;
+      f[(size_t)(M - 1 - (par + 2 * (s0 + st))) * nr + c] = 0.0;
+      if (f32) f32[(size_t)(M - 1 - (par + 2 * (s0 + st))) * nr + c] = 0.0f;
+    }
+    for (int e = tid; e < a.ldd; e += blockDim.x) dout[e] = 0.0;
+    return;
+  }
+  const int blk = nr * ldl;
+  double* Lb0 = csm;                                   // 3-slot ring of Linv blocks
+  double* D2s = Lb0 + 3 * blk;                         // psi: D2 (transposed)
+  double* cf = D2s + (a4 ? blk : 0);                   // per-step scalars, 4 per step, one step past the chunk
+  double* xv = cf + 4 * (size_t)(nsteps + 1);          // 2 buffers of f_e (psi)
+  double* yv = xv + 2 * nr;                            // 2 buffers of the Linv matvec's operand
+  const double* Mat = a4 ? a.LinvA4 : (field == 1 ? a.LinvT : a.LinvS);
+  const double* coef = a4 ? a.coefA4 : (field == 1 ? a.coefT : a.coefS);
+  const int jj0 = par + 2 * s0;
+  copy_block(Lb0, Mat + (size_t)jj0 * blk, blk);
+  if (a4) copy_block(D2s, a.D2A4, blk);
+  cp_async_commit();
+  if (nsteps > 1) copy_block(Lb0 + blk, Mat + (size_t)(jj0 + 2) * blk, blk);
+  cp_async_commit();
+  for (int e = tid; e < 4 * (nsteps + 1); e += blockDim.x) {
+    const int jj = jj0 + 2 * (e >> 2);
+    cf[e] = jj < M ? coef[(size_t)jj * 4 + (e & 3)] : 0.0;
+  }
+  const double ir4 = a4 ? a.ir4A4[ir] : 0.0, ir2 = a4 ? a.ir2A4[ir] : 0.0;
+  const double* grow = a.g + (size_t)b * a.g_stride + foff + ir;
+  auto g_at = [&](int st) { return st < nsteps ? grow[(size_t)(M - 1 - (par + 2 * (s0 + st))) * nr] : 0.0; };
+  double gn0 = g_at(0), gn1 = g_at(1);
+  double fe = 0.0, bfe = 0.0, fprev = 0.0;             // psi: f_e_i, bf_e_i; T/S: b_i in fe
+  for (int st = 0; st < nsteps; ++st) {
+    const int jj = jj0 + 2 * st;
+    const int row = M - 1 - jj;
+    const double* cur = Lb0 + (st % 3) * blk;
+    double* yb = yv + (st & 1) * nr;
+    cp_async_wait<1>();
+    chain_sync();                                      // Linv_jj (and D2) landed; step st-1 done
+    if (st + 2 < nsteps) copy_block(Lb0 + ((st + 2) % 3) * blk, Mat + (size_t)(jj + 4) * blk, blk);
+    cp_async_commit();
+    const double gi = gn0;
+    gn0 = gn1;
+    gn1 = g_at(st + 2);
+    if (a4) {
+      const double bj = cf[4 * st + 2], bjt = cf[4 * st + 3], c1 = cf[4 * st];
+      double y = gi;
+      if (st > 0) {
+        fe += fprev;                                   // f_e += f_{j+2}
+        double* xb = xv + (st & 1) * nr;
+        if (lead) xb[i] = fe;
+        chain_sync();
+        double z = 0.0;
+#pragma unroll 8
+        for (int c = q; c < nr; c += TPR) z = fma(D2s[c * ldl + ir], xb[c], z);
+        z = group_sum<TPR>(z);
+        const double L1f = fma(bj * ir4, fe, z);      // (D2 + bj IR4) f_e
+        const double tt = fma(ir4, bfe, L1f);          // + IR4 bf_e
+        const double bt = fma(c1, tt, -(bjt * ir2 * fe));
+        y = gi + bt;
+      }
+      if (lead) yb[i] = y;
+      chain_sync();
+      double acc = 0.0;
+#pragma unroll 8
+      for (int c = q; c < nr; c += TPR) acc = fma(cur[c * ldl + ir], yb[c], acc);
+      const double fi = group_sum<TPR>(acc);
+      bfe = st > 0 ? fma(bj, fi, fma(bjt, fe, bfe)) : fma(bj, fi, bfe);
+      fprev = fi;
+      if (lead) {
+        f[(size_t)row * nr + i] = fi;
+        if (f32 && chunk == 0) f32[(size_t)row * nr + i] = (float)fi;   // later chunks: after the correction
+      }
+    } else {
+      const double y = fma(-cf[4 * st + 1], fe, gi);  // g - w b
+      if (lead) yb[i] = y;
+      chain_sync();
+      double acc = 0.0;
+#pragma unroll 8
+      for (int c = q; c < nr; c += TPR) acc = fma(cur[c * ldl + ir], yb[c], acc);
+      const double fi = group_sum<TPR>(acc);
+      fe = fma(cf[4 * (st + 1)], fi, fe);             // the b of the next step (of the next chunk after the last)
+      if (lead) {
+        f[(size_t)row * nr + i] = fi;
+        if (f32 && chunk == 0) f32[(size_t)row * nr + i] = (float)fi;
+      }
+    }
+  }
+  cp_async_wait<0>();
+  if (a4) fe += fprev;                                 // the carried f_e after the chunk's last f
+  if (chunk + 1 < a.nch && lead) {                     // end state of the chunk from a zero start
+    dout[i] = fe;
+    if (a4) dout[nr + i] = bfe;
+  }
+  if (sub) {  // Newton residual: f -= sub over the chunk's rows (the block's own writes are visible)
+    __syncthreads();
+    for (int e = tid; e < nsteps * nr; e += blockDim.x) {
+      const int st = e / nr, c = e - st * nr;
+      const size_t o = (size_t)(M - 1 - (par + 2 * (s0 + st))) * nr + c;
+      f[o] -= sub[o];
+    }
+  }
+  if (a.nch > 2 && a.carry_seq) {
+    // the last chunk of this chain to finish runs the carried-state recurrence (no extra launch)
+    __shared__ int s_last;
+    __syncthreads();
+    int* cnt = a.counter + (size_t)b * 6 + (field * 2 + par);
+    if (tid == 0) {
+      __threadfence();
+      const int last = atomicAdd(cnt, 1) == a.nch - 1;
+      if (last) {
+        __threadfence();
+        *cnt = 0;                                      // ready for the next launch
+      }
+      s_last = last;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    carry_run<(TPR == 4 ? 2 : 1), CR>(a, field, par, b, csm);
+  } else if (a.nch == 2 && a.carry_seq) {              // s_1 = d_0 only: the chain's first chunk copies it
+    if (chunk == 0 && lead) {
+      double* cb = a.cbuf + (size_t)b * a.d_stride + ((size_t)(field * 2 + par) * a.nch + 1) * a.ldd;
+      cb[i] = fe;
+      if (a4) cb[nr + i] = bfe;
+    }
+  }
+}
+
 // Layouts 6, 7 and 8: the chains in the reference's own order of operations, without the h = Linv g pre-pass:
 //   psi (Matrix_Operators.py:1139-1164):  f_e += f_{j+2};  L1f = D2 f_e + bj IR4 f_e;
 //          b = dt bjt (L1f + IR4 bf_e) - bjt IR2 f_e;  f_j = Linv_j (g_j + b);  bf_e += bj f_j + bjt f_e
@@ -1038,17 +1198,29 @@ static int sm_count() {
   return sms;
 }
 
-static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields, cudaStream_t s) {
+static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields, cudaStream_t s, bool ref = false) {
   cudaError_t e;
   const bool pw = mv_per_warp(a_in, batch, nfields);
-  if ((e = launch_mode_mv<false>(a_in, batch, nfields, s, pw)) != cudaSuccess) return e;   // h = Linv g
   ChainArgs a = a_in;
-  a.g = a.h;
-  a.g_stride = a.h_stride;
-  if (!a.carry_seq) {   // layout 3: chunks, then the products in parallel, then the corrections
+  if (!ref) {               // the pre-pass form: h = Linv g, read by the chunks
+    if ((e = launch_mode_mv<false>(a_in, batch, nfields, s, pw)) != cudaSuccess) return e;
+    a.g = a.h;
+    a.g_stride = a.h_stride;
+  }
+  if (!a.carry_seq) {   // layouts 3 / 11: chunks, then the products in parallel, then the corrections
     const dim3 grid(2 * nfields, batch, a.nch);
     const size_t smem = chunk_smem_bytes(a.kc, a.nr, a.ldl);
-    if (a.nr <= 32) {
+    if (ref) {
+      if (a.nr <= 32) {
+        static unsigned long long done = 0;
+        if ((e = ensure_smem_attr(k_chain_cref<4, 0>, &done)) != cudaSuccess) return e;
+        if ((e = launch_kernel(k_chain_cref<4, 0>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e;
+      } else {
+        static unsigned long long done = 0;
+        if ((e = ensure_smem_attr(k_chain_cref<2, 0>, &done)) != cudaSuccess) return e;
+        if ((e = launch_kernel(k_chain_cref<2, 0>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e;
+      }
+    } else if (a.nr <= 32) {
       static unsigned long long done = 0;
       if ((e = ensure_smem_attr(k_chain<4, true, 0>, &done)) != cudaSuccess) return e;
       if ((e = launch_kernel(k_chain<4, true, 0>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e;
@@ -1078,11 +1250,17 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
   const int depth = (4 * blkb + st <= 200 * 1024) ? 4 : (2 * blkb + st <= 200 * 1024) ? 2 : 0;
   const size_t smem = std::max(chunk_smem_bytes(a.kc, a.nr, a.ldl), depth * blkb + st);
   const dim3 grid(2 * nfields, batch, a.nch);
-#define SDD_CHUNK(TPR_, R_)                                                              \
-  do {                                                                                   \
-    static unsigned long long done = 0;                                                  \
-    if ((e = ensure_smem_attr(k_chain<TPR_, true, R_>, &done)) != cudaSuccess) return e; \
-    if ((e = launch_kernel(k_chain<TPR_, true, R_>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e; \
+#define SDD_CHUNK(TPR_, R_)                                                                      \
+  do {                                                                                           \
+    if (ref) {                                                                                   \
+      static unsigned long long done = 0;                                                        \
+      if ((e = ensure_smem_attr(k_chain_cref<TPR_, R_>, &done)) != cudaSuccess) return e;        \
+      if ((e = launch_kernel(k_chain_cref<TPR_, R_>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e; \
+    } else {                                                                                     \
+      static unsigned long long done = 0;                                                        \
+      if ((e = ensure_smem_attr(k_chain<TPR_, true, R_>, &done)) != cudaSuccess) return e;       \
+      if ((e = launch_kernel(k_chain<TPR_, true, R_>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e; \
+    }                                                                                            \
   } while (0)
   if (a.nr <= 32) {
     if (depth == 4) SDD_CHUNK(4, 4);
@@ -1138,8 +1316,12 @@ int resolve_chain_layout(const ChainArgs& a, int batch, int nfields) {
   // layout 9 needs all three fields and its three rings in one CTA
   if (layout == 9 && (nfields != 3 || a.field0 != 0 || chain_shell_pre_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin))
     layout = 5;
+  // layouts 10 / 11 (chunks in the reference's order) need the full FP64 right-hand side: else layouts 2 / 3
+  if ((layout == 10 || layout == 11) && (a.fuse_rhs || a.g32 || !a.D2A4)) layout -= 8;
   if (layout == 0 && c3.nch > 1 && c3.GA4 && 2 * nfields * batch * c3.nch <= 2 * sms) layout = 3;
   if (layout == 0 && c2.nch > 1 && c2.GA4 && 2 * nfields * batch * c2.nch <= 2 * sms) layout = 2;
+  // chosen chunks run in the reference's order where the full FP64 right-hand side is there (no pre-pass)
+  if (a.layout == 0 && (layout == 2 || layout == 3) && !a.fuse_rhs && !a.g32 && a.D2A4) layout += 8;
   // layouts 6 / 7 need the full right-hand side in FP64: with the fused or the FP32 one, the pre-pass form
   if ((layout == 6 || layout == 7) && (a.fuse_rhs || a.g32)) layout = 5;
   if ((layout == 6 || layout == 7) && chain_ref_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin) layout = 2;
@@ -1208,15 +1390,16 @@ cudaError_t launch_chain(const ChainArgs& a_in, int batch, int nfields, cudaStre
   }
   const ChunkSet& c2 = a.cset[0];
   const ChunkSet& c3 = a.cset[1];
-  if (layout == 2 || layout == 3) {
-    const ChunkSet& c = layout == 3 ? c3 : c2;
+  if (layout == 2 || layout == 3 || layout == 10 || layout == 11) {
+    const bool ref = layout >= 10;
+    const ChunkSet& c = (layout == 3 || layout == 11) ? c3 : c2;
     if (!c.GA4 || c.kc < 1 || c.nch < 1) return cudaErrorInvalidValue;
     a.kc = c.kc; a.nch = c.nch; a.np = c.np;
     a.GA4 = c.GA4; a.GT = c.GT; a.GS = c.GS;
     a.PhiA4 = c.PhiA4; a.PhiT = c.PhiT; a.PhiS = c.PhiS;
     a.PA4 = c.PA4; a.PT = c.PT; a.PS = c.PS;
-    a.carry_seq = layout == 2;
-    return launch_chunked(a, batch, nfields, s);
+    a.carry_seq = layout == 2 || layout == 10;
+    return launch_chunked(a, batch, nfields, s, ref);
   }
   const bool split = layout == 4;
   if (layout == 5 && a.nr <= 32) {   // rows split over 2 lanes, 2 warps per chain

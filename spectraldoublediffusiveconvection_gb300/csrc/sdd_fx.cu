@@ -1269,10 +1269,15 @@ static int fx_sm_count() {
 // most SMs idle (nr * batch CTAs below half the SMs); it needs a grid scratch (or none: mode 2 and
 // cached mode 0 write the cache).  A batch that shares the GPU with other launches (the captured
 // multi-group graphs) is better served by the fused kernel; its autotuner sets the choice per plan.
+bool fx_split_rule(int split, int nr, int batch) {
+  if (split == 1) return false;
+  return split == 2 || 2 * nr * batch <= fx_sm_count();
+}
+
 bool fx_uses_split(const FxArgs& a, int batch, int mode) {
   const bool has_grid = (mode != 1 && a.base) || a.grid;
-  if (!has_grid || !a.deriv || a.split == 1) return false;
-  return a.split == 2 || 2 * a.nr * batch <= fx_sm_count();
+  if (!has_grid || !a.deriv) return false;
+  return fx_split_rule(a.split, a.nr, batch);
 }
 
 cudaError_t launch_fx(const FxArgs& a_in, int batch, int mode, int prec, cudaStream_t s) {

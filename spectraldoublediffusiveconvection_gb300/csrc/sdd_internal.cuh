@@ -346,6 +346,9 @@ size_t tc_smem_bytes(int KP, int NP);
 void build_tc_operator(const double* Dr, const double* D2r2, int nr, int KP, int NP, float* out);
 // whether launch_fx takes the split path for these arguments
 bool fx_uses_split(const FxArgs& a, int batch, int mode);
+// the split-or-fused rule alone (split: 0 automatic, 1 fused, 2 split), for a plan whose scratch is not yet
+// reserved
+bool fx_split_rule(int split, int nr, int batch);
 cudaError_t launch_rhs(const RhsArgs& a, int batch, cudaStream_t s);
 cudaError_t launch_chain(const ChainArgs& a, int batch, int nfields, cudaStream_t s);
 // the chain layout (1, 2, 3 or 4) launch_chain runs for a.layout (0 = automatic) and this launch size

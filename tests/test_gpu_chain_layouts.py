@@ -1,7 +1,8 @@
 """Every chain layout of the implicit solves (1 one lane per row, 2 chunked with a sequential carry, 3
 chunked with a parallel carry, 4 rows split over 4 lanes, 5 over 2 lanes, 6 and 7 the reference's own order
 of operations with rows over 2 or 4 lanes, 8 that order with the three chains of a (parity, shell) in one
-CTA, 9 the h pre-pass form with the three chains of a (parity, shell) in one CTA) against the oracle's A4_BSub_TSTEP_V2 / NAB2_BSub_TSTEP_V2
+CTA, 9 the h pre-pass form with the three chains of a (parity, shell) in one CTA, 10 / 11 the chunks of 2 / 3
+in the reference's order) against the oracle's A4_BSub_TSTEP_V2 / NAB2_BSub_TSTEP_V2
 chains (Matrix_Operators.py:1033-1194), alone and inside the step, the Newton residual and its Jacobian.
 The chunked layouts reorder the arithmetic (carried states through precomputed chunk maps or their
 products), so they agree with the sequential chain to rounding, not bitwise."""
@@ -17,7 +18,7 @@ SHAPES = [(16, 16, False), (20, 64, False), (30, 256, False), (48, 512, False), 
 
 
 @pytest.mark.parametrize("N_r,N_fm,sym", SHAPES)
-@pytest.mark.parametrize("layout", [1, 2, 3, 4, 5, 6, 7, 8, 9])
+@pytest.mark.parametrize("layout", [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11])
 def test_chain_solves_against_oracle(cuda, N_r, N_fm, sym, layout):
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     torch = cuda
@@ -41,9 +42,11 @@ def test_chain_solves_against_oracle(cuda, N_r, N_fm, sym, layout):
         assert rel(fs[k], rs) < 1e-13
 
 
-@pytest.mark.parametrize("layout", [2, 3])
+@pytest.mark.parametrize("layout", [2, 3, 10, 11])
 @pytest.mark.parametrize("N_r,N_fm", [(20, 64), (30, 256), (48, 512)])
 def test_chunked_step_newton_operators_against_oracle(cuda, N_r, N_fm, layout):
+    """Chunked chains: 2 / 3 (h pre-pass, sequential / parallel carry) and 10 / 11 (each chunk in the
+    reference's order, no pre-pass; they need the full right-hand side, so the fused row kernel)."""
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     torch = cuda
     nr = N_r - 1
@@ -54,6 +57,9 @@ def test_chunked_step_newton_operators_against_oracle(cuda, N_r, N_fm, layout):
     ops = O.Operators(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01)
     p = Plan(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01)
     p.set_chain_layout(layout)
+    if layout >= 10:
+        p.set_fx_split(1)
+        assert p.chain_choice(2)[0] == layout
     Y = p.step(Xt, 8000.0, 500.0, nsteps=3).cpu().numpy()
     for k, x in enumerate([X, 2 * X]):
         r = x
@@ -63,6 +69,8 @@ def test_chunked_step_newton_operators_against_oracle(cuda, N_r, N_fm, layout):
     ops1 = O.Operators(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
     p1 = Plan(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
     p1.set_chain_layout(layout)
+    if layout >= 10:
+        p1.set_fx_split(1)
     F = p1.pfx(Xt, 8000.0, 500.0).cpu().numpy()
     J = p1.pdfx(dvt, Xt, 8000.0, 500.0).cpu().numpy()
     for k, x in enumerate([X, 2 * X]):
@@ -112,7 +120,7 @@ def test_reference_order_chains_in_steps_and_newton_operators(cuda, N_r, N_fm, p
         assert rel(J[k], O.PDFX(ops1, dv, x, 8000.0, 500.0, False)) < 1e-12
 
 
-@pytest.mark.parametrize("layout", [2, 3])
+@pytest.mark.parametrize("layout", [2, 3, 10, 11])
 def test_chunked_batch_equals_alone(cuda, layout):
     """No arithmetic crosses shells in the chunked layouts either: a batch equals its shells alone."""
     from spectraldoublediffusiveconvection_gb300.plan import Plan
@@ -120,6 +128,8 @@ def test_chunked_batch_equals_alone(cuda, layout):
     N_fm, N_r = 128, 24
     p = Plan(N_fm, N_r, 2.0, 1e-3, 1.0, 0.01)
     p.set_chain_layout(layout)
+    if layout >= 10:
+        p.set_fx_split(1)
     Xs = np.stack([O.seeded_state(N_fm, N_r - 1, s) for s in range(4)])
     Ra = torch.tensor([6000.0, 8000.0, 10000.0, 12000.0], dtype=torch.float64, device="cuda")
     Xb = p.step(torch.from_numpy(Xs).cuda(), Ra, 500.0, nsteps=4)
@@ -149,11 +159,14 @@ def test_split_nonlinear_term_equals_fused(cuda, precision):
 
 
 def test_forced_nonlinear_term_paths_agree(cuda):
-    """sdd_plan_set_fx_split: the forced fused and forced split kernels give the same bits on one batch."""
+    """sdd_plan_set_fx_split: the forced fused and forced split kernels give the same bits on one batch (under
+    one chain layout: the automatic choice runs chunks in the reference's order where the right-hand side is
+    not fused into the split nonlinear term, and the pre-pass chunks where it is)."""
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     torch = cuda
     N_fm, N_r = 128, 24
     p = Plan(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
+    p.set_chain_layout(3)
     Xs = torch.from_numpy(np.stack([O.seeded_state(N_fm, N_r - 1, s) for s in range(5)])).cuda()
     dvs = torch.from_numpy(np.stack([O.seeded_state(N_fm, N_r - 1, 20 + s) for s in range(5)])).cuda()
     out = []
@@ -183,9 +196,10 @@ def test_matvec_variants_agree_across_batch_sizes(cuda, layout):
 
 
 def test_automatic_layout_choice(cuda):
-    """sdd_plan_chain_choice: one production shell runs the parallel-carry chunks (layout 3, kc ~ sqrt(S/2)),
-    a batch too large for its CTAs falls back to whole chains in the reference's order, three per CTA
-    (layout 8); forced layouts are reported as set."""
+    """sdd_plan_chain_choice (as the step launches: the right-hand side fused into the split nonlinear term
+    for one shell): one production shell runs the parallel-carry chunks (layout 3, kc ~ sqrt(S/2)), a batch
+    too large for its CTAs falls back to whole chains in the reference's order, three per CTA (layout 8);
+    forced layouts are reported as they run."""
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     p = Plan(256, 30, 2.0, 5e-4, 1.0, 0.01)
     assert p.chain_choice(1) == (3, 8, 16)
@@ -199,8 +213,13 @@ def test_automatic_layout_choice(cuda):
     assert p.chain_choice(64)[0] == 8
     p.set_chain_layout(9)
     assert p.chain_choice(64)[0] == 9
+    p.set_chain_layout(10)                 # 64 shells: the fused row kernel, full right-hand sides
+    assert p.chain_choice(64) == (10, 16, 8)
+    assert p.chain_choice(1)[0] == 2       # one shell: the split nonlinear term fuses the right-hand side
+    p.set_chain_layout(11)
+    assert p.chain_choice(64) == (11, 8, 16)
     with pytest.raises(Exception):
-        p.set_chain_layout(10)
+        p.set_chain_layout(12)
 
 
 @pytest.mark.parametrize("N_r,N_fm,split", [(20, 64, 1), (30, 256, 2), (48, 512, 1), (12, 16, 2), (65, 32, 1)])
