@@ -111,8 +111,10 @@ int sdd_plan_reserve(sdd_plan* plan, int max_batch);
  * the three chains of one (parity, shell) in one CTA, psi rows over 2 lanes, T and S one lane per row
  * (launches of fewer than three fields, or whose three rings exceed a CTA's shared memory, run layout 5).
  * 10 / 11: the chunks of layouts 2 / 3 with each chunk in the reference's order of operations (no h
- * pre-pass; full FP64 right-hand sides only, else layouts 2 / 3).  Set by the batch autotuner; no
- * counterpart in the reference. */
+ * pre-pass; with the right-hand side fused into the split nonlinear term each chunk forms its own; FP32
+ * right-hand sides run layouts 2 / 3).  The automatic choice runs its chunked layout as 10 / 11 where the
+ * full FP64 right-hand side is there, and as 2 / 3 where it is fused (one shell: the pre-pass form is
+ * faster there).  Set by the batch autotuner; no counterpart in the reference. */
 int sdd_plan_set_chain_layout(sdd_plan* plan, int layout);
 /* The layout (1-11) a step of `batch` shells runs under the current setting, with its chunk length and
  * chunks per chain (0 and 1 when not chunked). */

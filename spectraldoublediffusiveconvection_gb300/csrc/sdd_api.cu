@@ -1013,12 +1013,13 @@ static ChainArgs step_chain_args(const sdd_plan* p, int batch) {
   return ca;
 }
 
-// Whether sdd_step's steps leave the chains' correction to the next step's nonlinear term: layout 3 with
-// the split nonlinear term, non-linear steps.
+// Whether sdd_step's steps leave the chains' correction to the next step's nonlinear term: layout 3 or 11
+// (chunk set 1, parallel carries) with the split nonlinear term, non-linear steps.
 static bool step_defers_fix(sdd_plan* p, int batch, int linear) {
   if (linear || p->cs[1].nch < 2) return false;
   const ChainArgs ca = step_chain_args(p, batch);
-  return ca.fuse_rhs && resolve_chain_layout(ca, batch, 3) == 3;
+  const int layout = resolve_chain_layout(ca, batch, 3);
+  return ca.fuse_rhs && (layout == 3 || layout == 11);
 }
 
 // The correction left pending by the last step of a sequence, on the state X (and its FP32 copy).

@@ -295,7 +295,9 @@ __global__ void k_chain(ChainArgs a) {
 // Linv_j (g_j - w b)), so that no h = Linv g pre-pass runs: each chunk starts from a zero carried state
 // exactly as in layouts 2 and 3 (the carried state [f_e; bf_e] or b is the same quantity), writes the same
 // end state (psi: f_e after its last f, bf_e), and the same carries and corrections follow.  g is the full
-// right-hand side.  One CTA per (field, parity, chunk, shell), rows over TPR lanes.
+// right-hand side, or with fuse_rhs formed by the CTA itself before its chain from the linear parts and the
+// nonlinear-term outputs (fused_g, the roundings of k_rhs: the same bits), so that the single shell's step
+// needs no right-hand-side kernel either.  One CTA per (field, parity, chunk, shell), rows over TPR lanes.
 template <int TPR, int CR>
 __global__ void k_chain_cref(ChainArgs a) {
   extern __shared__ __align__(16) double csm[];
@@ -337,11 +339,16 @@ __global__ void k_chain_cref(ChainArgs a) {
   double* cf = D2s + (a4 ? blk : 0);                   // per-step scalars, 4 per step, one step past the chunk
   double* xv = cf + 4 * (size_t)(nsteps + 1);          // 2 buffers of f_e (psi)
   double* yv = xv + 2 * nr;                            // 2 buffers of the Linv matvec's operand
+  double* gs = yv + 2 * nr;                            // fuse_rhs: g of the chunk's steps, then Dr (psi)
+  double* Drs = gs + (size_t)nsteps * nr;
+  const bool stage_dr = a.fuse_rhs && a4 && !a.q32;
   const double* Mat = a4 ? a.LinvA4 : (field == 1 ? a.LinvT : a.LinvS);
   const double* coef = a4 ? a.coefA4 : (field == 1 ? a.coefT : a.coefS);
   const int jj0 = par + 2 * s0;
   copy_block(Lb0, Mat + (size_t)jj0 * blk, blk);
   if (a4) copy_block(D2s, a.D2A4, blk);
+  if (stage_dr)
+    for (int e = tid; e < nr * nr; e += blockDim.x) cp_async8(Drs + e, a.Dr + e);
   cp_async_commit();
   if (nsteps > 1) copy_block(Lb0 + blk, Mat + (size_t)(jj0 + 2) * blk, blk);
   cp_async_commit();
@@ -350,8 +357,20 @@ __global__ void k_chain_cref(ChainArgs a) {
     cf[e] = jj < M ? coef[(size_t)jj * 4 + (e & 3)] : 0.0;
   }
   const double ir4 = a4 ? a.ir4A4[ir] : 0.0, ir2 = a4 ? a.ir2A4[ir] : 0.0;
+  if (a.fuse_rhs) {
+    if (stage_dr) cp_async_wait<1>();                  // Dr landed (with the first Linv block and D2)
+    __syncthreads();
+    for (int e = tid; e < nsteps * nr; e += blockDim.x) {
+      const int st = e / nr, n = e - st * nr;
+      gs[e] = fused_g(a, b, field, M - 1 - (par + 2 * (s0 + st)), n, stage_dr ? Drs : nullptr);
+    }
+    __syncthreads();
+  }
   const double* grow = a.g + (size_t)b * a.g_stride + foff + ir;
-  auto g_at = [&](int st) { return st < nsteps ? grow[(size_t)(M - 1 - (par + 2 * (s0 + st))) * nr] : 0.0; };
+  auto g_at = [&](int st) {
+    if (st >= nsteps) return 0.0;
+    return a.fuse_rhs ? gs[st * nr + ir] : grow[(size_t)(M - 1 - (par + 2 * (s0 + st))) * nr];
+  };
   double gn0 = g_at(0), gn1 = g_at(1);
   double fe = 0.0, bfe = 0.0, fprev = 0.0;             // psi: f_e_i, bf_e_i; T/S: b_i in fe
   for (int st = 0; st < nsteps; ++st) {
@@ -778,6 +797,14 @@ size_t chain_smem_bytes(int M, int nr, int ldl) {
 static size_t chunk_smem_bytes(int kc, int nr, int ldl) {
   const size_t blk = (size_t)2 * nr * ldl;
   return (3 * blk + 4 * ((size_t)kc + 1) + 4 * (size_t)nr) * sizeof(double);
+}
+
+// k_chain_cref: the Linv ring and D2 (4 nr ldl), the step scalars and operand buffers, and with fuse_rhs
+// the chunk's g (kc nr) and Dr (nr nr)
+static size_t chunk_ref_smem_bytes(int kc, int nr, int ldl, bool fuse) {
+  const size_t blk = (size_t)nr * ldl;
+  return (4 * blk + 4 * ((size_t)kc + 1) + 4 * (size_t)nr + (fuse ? (size_t)kc * nr + (size_t)nr * nr : 0)) *
+         sizeof(double);
 }
 
 // Carried states of the chunked chains: s_1 = d_0, s_{c+1} = Phi_c s_c + d_c (c = 1 .. nch-2) of one chain,
@@ -1209,7 +1236,7 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
   }
   if (!a.carry_seq) {   // layouts 3 / 11: chunks, then the products in parallel, then the corrections
     const dim3 grid(2 * nfields, batch, a.nch);
-    const size_t smem = chunk_smem_bytes(a.kc, a.nr, a.ldl);
+    const size_t smem = ref ? chunk_ref_smem_bytes(a.kc, a.nr, a.ldl, a.fuse_rhs) : chunk_smem_bytes(a.kc, a.nr, a.ldl);
     if (ref) {
       if (a.nr <= 32) {
         static unsigned long long done = 0;
@@ -1248,7 +1275,8 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
   const size_t blkb = (size_t)mmax * ldmax * sizeof(double);
   const size_t st = 2 * (size_t)a.ldd * sizeof(double);
   const int depth = (4 * blkb + st <= 200 * 1024) ? 4 : (2 * blkb + st <= 200 * 1024) ? 2 : 0;
-  const size_t smem = std::max(chunk_smem_bytes(a.kc, a.nr, a.ldl), depth * blkb + st);
+  const size_t smem = std::max(ref ? chunk_ref_smem_bytes(a.kc, a.nr, a.ldl, a.fuse_rhs)
+                                   : chunk_smem_bytes(a.kc, a.nr, a.ldl), depth * blkb + st);
   const dim3 grid(2 * nfields, batch, a.nch);
 #define SDD_CHUNK(TPR_, R_)                                                                      \
   do {                                                                                           \
@@ -1316,8 +1344,8 @@ int resolve_chain_layout(const ChainArgs& a, int batch, int nfields) {
   // layout 9 needs all three fields and its three rings in one CTA
   if (layout == 9 && (nfields != 3 || a.field0 != 0 || chain_shell_pre_smem_bytes(a.M, a.nr, a.ldl) > (size_t)optin))
     layout = 5;
-  // layouts 10 / 11 (chunks in the reference's order) need the full FP64 right-hand side: else layouts 2 / 3
-  if ((layout == 10 || layout == 11) && (a.fuse_rhs || a.g32 || !a.D2A4)) layout -= 8;
+  // layouts 10 / 11 (chunks in the reference's order) need an FP64 right-hand side (full or fused): else 2 / 3
+  if ((layout == 10 || layout == 11) && (a.g32 || !a.D2A4)) layout -= 8;
   if (layout == 0 && c3.nch > 1 && c3.GA4 && 2 * nfields * batch * c3.nch <= 2 * sms) layout = 3;
   if (layout == 0 && c2.nch > 1 && c2.GA4 && 2 * nfields * batch * c2.nch <= 2 * sms) layout = 2;
   // chosen chunks run in the reference's order where the full FP64 right-hand side is there (no pre-pass)

@@ -135,8 +135,8 @@ class Plan:
         split over 4 warps, 5 rows split over 2 lanes in 2 warps, 6 / 7 the reference's order of operations
         without the h pre-pass, rows over 2 / 4 lanes (full right-hand sides only; otherwise 5), 8 the same
         with a (parity, shell)'s three chains in one CTA, 9 the pre-pass form with a (parity, shell)'s three
-        chains in one CTA, 10 / 11 the chunks of 2 / 3 in the reference's order (full right-hand sides only;
-        otherwise 2 / 3) (sdd_plan_set_chain_layout); the results agree to rounding."""
+        chains in one CTA, 10 / 11 the chunks of 2 / 3 in the reference's order (FP64 right-hand sides, full
+        or fused; otherwise 2 / 3) (sdd_plan_set_chain_layout); the results agree to rounding."""
         _lib.check(self._L.sdd_plan_set_chain_layout(self._h, int(layout)), "sdd_plan_set_chain_layout")
         self.chain_layout = int(layout)
 

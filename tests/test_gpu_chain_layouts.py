@@ -46,7 +46,8 @@ def test_chain_solves_against_oracle(cuda, N_r, N_fm, sym, layout):
 @pytest.mark.parametrize("N_r,N_fm", [(20, 64), (30, 256), (48, 512)])
 def test_chunked_step_newton_operators_against_oracle(cuda, N_r, N_fm, layout):
     """Chunked chains: 2 / 3 (h pre-pass, sequential / parallel carry) and 10 / 11 (each chunk in the
-    reference's order, no pre-pass; they need the full right-hand side, so the fused row kernel)."""
+    reference's order, no pre-pass), the latter under the fused row kernel (full right-hand sides) and under
+    the split nonlinear term (the chunks form their right-hand side themselves): the same bits."""
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     torch = cuda
     nr = N_r - 1
@@ -58,9 +59,14 @@ def test_chunked_step_newton_operators_against_oracle(cuda, N_r, N_fm, layout):
     p = Plan(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01)
     p.set_chain_layout(layout)
     if layout >= 10:
+        p.set_fx_split(2)
+        assert p.chain_choice(2)[0] == layout
+        Y2 = p.step(Xt, 8000.0, 500.0, nsteps=3).cpu().numpy()
         p.set_fx_split(1)
         assert p.chain_choice(2)[0] == layout
     Y = p.step(Xt, 8000.0, 500.0, nsteps=3).cpu().numpy()
+    if layout >= 10:
+        assert np.array_equal(Y, Y2)
     for k, x in enumerate([X, 2 * X]):
         r = x
         for _ in range(3):
@@ -161,20 +167,26 @@ def test_split_nonlinear_term_equals_fused(cuda, precision):
 def test_forced_nonlinear_term_paths_agree(cuda):
     """sdd_plan_set_fx_split: the forced fused and forced split kernels give the same bits on one batch (under
     one chain layout: the automatic choice runs chunks in the reference's order where the right-hand side is
-    not fused into the split nonlinear term, and the pre-pass chunks where it is)."""
+    not fused into the split nonlinear term, and the pre-pass chunks where it is).  Layouts 3 and 11 (the
+    parallel-carry chunks whose correction the split form's steps leave to the next step's nonlinear term)."""
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     torch = cuda
     N_fm, N_r = 128, 24
-    p = Plan(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
-    p.set_chain_layout(3)
     Xs = torch.from_numpy(np.stack([O.seeded_state(N_fm, N_r - 1, s) for s in range(5)])).cuda()
     dvs = torch.from_numpy(np.stack([O.seeded_state(N_fm, N_r - 1, 20 + s) for s in range(5)])).cuda()
-    out = []
-    for mode in (1, 2):
-        p.set_fx_split(mode)
-        out.append((p.nlin_fx(Xs), p.nlin_dfx(dvs, Xs), p.pfx(Xs, 9000.0, 500.0), p.pdfx(dvs, Xs, 9000.0, 500.0)))
-    for a, b in zip(*out):
-        assert torch.equal(a, b)
+    for layout in (3, 11):
+        p = Plan(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
+        p.set_chain_layout(layout)
+        q = Plan(N_fm, N_r, 2.0, 1e-3, 1.0, 0.01)
+        q.set_chain_layout(layout)
+        out = []
+        for mode in (1, 2):
+            p.set_fx_split(mode)
+            q.set_fx_split(mode)
+            out.append((p.nlin_fx(Xs), p.nlin_dfx(dvs, Xs), p.pfx(Xs, 9000.0, 500.0),
+                        p.pdfx(dvs, Xs, 9000.0, 500.0), q.step(Xs, 9000.0, 500.0, nsteps=5)))
+        for a, b in zip(*out):
+            assert torch.equal(a, b)
     with pytest.raises(Exception):
         p.set_fx_split(3)
 
@@ -215,9 +227,10 @@ def test_automatic_layout_choice(cuda):
     assert p.chain_choice(64)[0] == 9
     p.set_chain_layout(10)                 # 64 shells: the fused row kernel, full right-hand sides
     assert p.chain_choice(64) == (10, 16, 8)
-    assert p.chain_choice(1)[0] == 2       # one shell: the split nonlinear term fuses the right-hand side
+    assert p.chain_choice(1) == (10, 16, 8)   # one shell: the split nonlinear term, the chunks form g
     p.set_chain_layout(11)
     assert p.chain_choice(64) == (11, 8, 16)
+    assert p.chain_choice(1) == (11, 8, 16)
     with pytest.raises(Exception):
         p.set_chain_layout(12)
 
