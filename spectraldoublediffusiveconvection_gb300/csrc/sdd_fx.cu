@@ -336,6 +336,7 @@ __global__ void __launch_bounds__(kFxRowThreads) k_fx_rows(FxArgs a) {
 //     sine-type Q, R; p = 1: the cosine-type NT, NS) and runs their paired forward transform into out4.
 // Per element the operations and their order are those of k_fx_rows, so the results are identical.
 constexpr int kFxSplitThreads = 256;
+constexpr size_t kFxDerivStageMaxBytes = 110 * 1024;   // two derivative CTAs per SM
 
 // FP32 grid kernels of the fused right-hand side keep FP64 copies of the row's psi, T, S and psi's parity
 // suffix sums (4 M doubles) for the linear parts, after the T-typed arrays.
@@ -364,74 +365,6 @@ __device__ __forceinline__ double lane_group_sum(double v) {
   return v;
 }
 
-// The pending correction of mode k (see FixArgs) on xd (the mode's FP64 psi, T, S rows, in shared memory),
-// the three fields at once, each by its own 128 threads (threads 128 f .. 128 f + 127; the CTA has 384):
-// s_c = d_{c-1} + part_{c,0} + ... in index order, then xd += G_jj s_c with rows split over TPR lanes as
-// k_mode_mv<TPR, true> (the same bits); the corrected rows are written back to the state (and its FP32
-// copy).  sc holds the three carried states (4 nr doubles).
-template <int TPR>
-__device__ void apply_pending_fix(const FxArgs& a, int b, int k, double* xd, double* sc) {
-  const FixArgs& x = a.fix;
-  const int M = a.M, nr = a.nr, ldl = x.ldl;
-  const int jj = M - 1 - k, par = jj & 1, c = (jj >> 1) / x.kc;
-  if (c < 1) return;                                   // uniform over the CTA
-  const size_t N = (size_t)M * nr;
-  const int f = threadIdx.x >> 7, t = threadIdx.x & 127;
-  const bool a4 = f == 0;
-  const bool on = f < 3 && !(a.sym && !(a4 ? par == 0 : par == 1));
-  const int m = a4 ? 2 * nr : nr;
-  double* s = sc + (a4 ? 0 : (f == 1 ? 2 * nr : 3 * nr));
-  if (on) {
-    const size_t chain = (size_t)(f * 2 + par);
-    const double* d = x.dbuf + (size_t)b * x.d_stride + chain * x.nch * x.ldd;
-    const double* prow = x.pbuf + (size_t)b * x.p_stride + (chain * x.np + (size_t)(c - 1) * (c - 2) / 2) * x.ldd;
-    for (int e = t; e < m; e += 128) {
-      // d_{c-1} + part_0 + ... + part_{c-2} in index order, the terms loaded eight at a time (a load
-      // after each addition would wait out one L2 round trip per term)
-      double v = d[(size_t)(c - 1) * x.ldd + e];
-      const int nt = c - 1;
-      for (int u0 = 0; u0 < nt; u0 += 8) {
-        double tv[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) tv[k] = (u0 + k < nt) ? prow[(size_t)(u0 + k) * x.ldd + e] : 0.0;
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-          if (u0 + k < nt) v += tv[k];
-      }
-      s[e] = v;
-    }
-  }
-  __syncthreads();
-  if (on) {
-    const double* G = (a4 ? x.GA4 : (f == 1 ? x.GT : x.GS)) + (size_t)jj * m * ldl;
-    const int i = t / TPR, q = t % TPR;
-    for (int r0 = 0; r0 < nr; r0 += 128 / TPR) {
-      const int r = r0 + i;
-      const int rr = r < nr ? r : 0;
-      double acc = 0.0;
-#pragma unroll 16
-      for (int col = q; col < m; col += TPR) acc = fma(__ldg(G + (size_t)col * ldl + rr), s[col], acc);
-      acc = lane_group_sum<TPR>(acc);
-      if (r < nr && q == 0) {
-        const double v = xd[f * nr + r] + acc;
-        xd[f * nr + r] = v;
-        const size_t o = (size_t)b * a.x_stride + (size_t)f * N + (size_t)k * nr + r;
-        x.X[o] = v;
-        if (x.X32) x.X32[(size_t)b * a.x32_stride + (size_t)f * N + (size_t)k * nr + r] = (float)v;
-      }
-    }
-  }
-  __syncthreads();
-}
-
-// T-typed Dr, D2r2 and the mode's rows; then (FP64) the corrected rows and carried states of a pending fix
-// (7 nr); then the fused right-hand side's D2s (nr^2) and the mode's FP64 psi row (nr)
-size_t fx_deriv_smem_bytes(int nr, int prec, bool fix, bool fuse) {
-  const size_t es = prec == SDD_PREC_MIXED ? sizeof(float) : sizeof(double);
-  const size_t t = ((2 * (size_t)nr * nr + 3 * (size_t)nr) * es + 15) / 16 * 16;
-  return t + (fix ? 7 * (size_t)nr * sizeof(double) : 0) + (fuse ? ((size_t)nr * nr + nr) * sizeof(double) : 0);
-}
-
 // One asynchronous global -> shared copy of an element of 4, 8 or 16 bytes (the issuing thread does not
 // wait for the data: a loop of such copies has all its loads in flight at once).
 template <int BYTES>
@@ -450,6 +383,127 @@ __device__ __forceinline__ void cp_async_all_done() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_all;\n" ::: "memory");
 }
 
+// Shared memory for a staged pending correction (FixArgs::stage): the G blocks of the mode's three chains
+// (2 nr + nr + nr columns of ldl) and, per chain, d_{c-1} and the carry terms of its chunk c (at most
+// nch - 1 vectors of 2 nr / nr / nr doubles).
+__host__ __device__ inline size_t fix_stage_doubles(int nr, int ldl, int nch) {
+  return (size_t)4 * nr * ldl + (size_t)(nch > 1 ? nch - 1 : 0) * 4 * nr;
+}
+
+// The asynchronous copies of a staged correction of mode k into st (16-byte aligned): the G blocks of the
+// three chains at st, st + 2 nr ldl, st + 3 nr ldl; then per chain f, from st + 4 nr ldl + c o_f
+// (o = 0, 2 nr, 3 nr), the c vectors d_{c-1}, part_{c,0}, ..., part_{c,c-2} of m_f doubles each.  The
+// caller commits and waits.
+__device__ __forceinline__ void stage_pending_fix(const FxArgs& a, int b, int k, double* st) {
+  const FixArgs& x = a.fix;
+  const int M = a.M, nr = a.nr, ldl = x.ldl;
+  const int jj = M - 1 - k, par = jj & 1, c = (jj >> 1) / x.kc;
+  if (c < 1) return;
+  for (int f = 0; f < 3; ++f) {
+    const bool a4 = f == 0;
+    if (a.sym && !(a4 ? par == 0 : par == 1)) continue;
+    const int m = a4 ? 2 * nr : nr;
+    const int o = a4 ? 0 : (f == 1 ? 2 * nr : 3 * nr);
+    const double* G = (a4 ? x.GA4 : (f == 1 ? x.GT : x.GS)) + (size_t)jj * m * ldl;
+    double* Gs = st + (size_t)o * ldl;
+    for (int e = threadIdx.x; e < m * ldl / 2; e += blockDim.x)   // m ldl is even (ldl even)
+      cp_async_bytes<16>(Gs + 2 * e, G + 2 * e);
+    const size_t chain = (size_t)(f * 2 + par);
+    const double* d = x.dbuf + (size_t)b * x.d_stride + chain * x.nch * x.ldd + (size_t)(c - 1) * x.ldd;
+    const double* prow = x.pbuf + (size_t)b * x.p_stride + (chain * x.np + (size_t)(c - 1) * (c - 2) / 2) * x.ldd;
+    double* Ts = st + (size_t)4 * nr * ldl + (size_t)c * o;
+    for (int e = threadIdx.x; e < c * m; e += blockDim.x) {
+      const int v = e / m, i = e - v * m;
+      cp_async_bytes<8>(Ts + e, v == 0 ? d + i : prow + (size_t)(v - 1) * x.ldd + i);
+    }
+  }
+}
+
+// The pending correction of mode k (see FixArgs) on xd (the mode's FP64 psi, T, S rows, in shared memory),
+// the three fields at once, each by its own 128 threads (threads 128 f .. 128 f + 127; the CTA has 384):
+// s_c = d_{c-1} + part_{c,0} + ... in index order, then xd += G_jj s_c with rows split over TPR lanes as
+// k_mode_mv<TPR, true> (the same bits); the corrected rows are written back to the state (and its FP32
+// copy).  sc holds the three carried states (4 nr doubles).  st: the staged G blocks and terms
+// (stage_pending_fix, landed), or null to read them from global memory.
+template <int TPR>
+__device__ void apply_pending_fix(const FxArgs& a, int b, int k, double* xd, double* sc, const double* st) {
+  const FixArgs& x = a.fix;
+  const int M = a.M, nr = a.nr, ldl = x.ldl;
+  const int jj = M - 1 - k, par = jj & 1, c = (jj >> 1) / x.kc;
+  if (c < 1) return;                                   // uniform over the CTA
+  const size_t N = (size_t)M * nr;
+  const int f = threadIdx.x >> 7, t = threadIdx.x & 127;
+  const bool a4 = f == 0;
+  const bool on = f < 3 && !(a.sym && !(a4 ? par == 0 : par == 1));
+  const int m = a4 ? 2 * nr : nr;
+  const int o = a4 ? 0 : (f == 1 ? 2 * nr : 3 * nr);
+  double* s = sc + o;
+  if (on) {
+    const size_t chain = (size_t)(f * 2 + par);
+    const int nt = c - 1;
+    if (st) {
+      const double* Ts = st + (size_t)4 * nr * ldl + (size_t)c * o;
+      for (int e = t; e < m; e += 128) {
+        double v = Ts[e];                              // d_{c-1} + part_0 + ... + part_{c-2} in index order
+        for (int u = 0; u < nt; ++u) v += Ts[(size_t)(u + 1) * m + e];
+        s[e] = v;
+      }
+    } else {
+      const double* d = x.dbuf + (size_t)b * x.d_stride + chain * x.nch * x.ldd;
+      const double* prow = x.pbuf + (size_t)b * x.p_stride + (chain * x.np + (size_t)(c - 1) * (c - 2) / 2) * x.ldd;
+      for (int e = t; e < m; e += 128) {
+        // d_{c-1} + part_0 + ... + part_{c-2} in index order, the terms loaded eight at a time (a load
+        // after each addition would wait out one L2 round trip per term)
+        double v = d[(size_t)(c - 1) * x.ldd + e];
+        for (int u0 = 0; u0 < nt; u0 += 8) {
+          double tv[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k) tv[k] = (u0 + k < nt) ? prow[(size_t)(u0 + k) * x.ldd + e] : 0.0;
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            if (u0 + k < nt) v += tv[k];
+        }
+        s[e] = v;
+      }
+    }
+  }
+  __syncthreads();
+  if (on) {
+    const double* G = st ? st + (size_t)o * ldl : (a4 ? x.GA4 : (f == 1 ? x.GT : x.GS)) + (size_t)jj * m * ldl;
+    const int i = t / TPR, q = t % TPR;
+    for (int r0 = 0; r0 < nr; r0 += 128 / TPR) {
+      const int r = r0 + i;
+      const int rr = r < nr ? r : 0;
+      double acc = 0.0;
+#pragma unroll 16
+      for (int col = q; col < m; col += TPR) acc = fma(G[(size_t)col * ldl + rr], s[col], acc);
+      acc = lane_group_sum<TPR>(acc);
+      if (r < nr && q == 0) {
+        const double v = xd[f * nr + r] + acc;
+        xd[f * nr + r] = v;
+        const size_t o = (size_t)b * a.x_stride + (size_t)f * N + (size_t)k * nr + r;
+        x.X[o] = v;
+        if (x.X32) x.X32[(size_t)b * a.x32_stride + (size_t)f * N + (size_t)k * nr + r] = (float)v;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// T-typed Dr, D2r2 and the mode's rows; then (FP64) the corrected rows and carried states of a pending fix
+// (7 nr); then the fused right-hand side's D2s (nr^2) and the mode's FP64 psi row (nr); then, 16-byte
+// aligned, the staged correction (stage_doubles, fix_stage_doubles, or 0)
+__host__ __device__ inline size_t fx_deriv_stage_offset(int nr, int prec, bool fix, bool fuse) {
+  const size_t es = prec == SDD_PREC_MIXED ? sizeof(float) : sizeof(double);
+  const size_t t = ((2 * (size_t)nr * nr + 3 * (size_t)nr) * es + 15) / 16 * 16;
+  return (t + (fix ? 7 * (size_t)nr * sizeof(double) : 0) + (fuse ? ((size_t)nr * nr + nr) * sizeof(double) : 0) +
+          15) / 16 * 16;
+}
+size_t fx_deriv_smem_bytes(int nr, int prec, bool fix, bool fuse, size_t stage_doubles) {
+  return fx_deriv_stage_offset(nr, prec, fix, fuse) + stage_doubles * sizeof(double);
+}
+
+
 template <typename T>
 __global__ void __launch_bounds__(384) k_fx_deriv(FxArgs a, T* deriv, size_t deriv_stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -464,8 +518,14 @@ __global__ void __launch_bounds__(384) k_fx_deriv(FxArgs a, T* deriv, size_t der
   double* D2sm = xd + (a.fix.on ? 7 * nr : 0);        // fused right-hand side: A2_SINE's D2 (FP64)
   const T* Drg = reinterpret_cast<const T*>(a.ops.Dr);
   const T* D2g = reinterpret_cast<const T*>(a.ops.D2r2);
-  // the operators (and the rows of a pending fix) stream in asynchronously: one L2 round trip, not one per
-  // element each thread copies
+  double* stg = (a.fix.on && a.fix.stage)
+                    ? reinterpret_cast<double*>(smem_raw + fx_deriv_stage_offset(nr, sizeof(T) == 4 ? SDD_PREC_MIXED
+                                                                                                    : SDD_PREC_FP64,
+                                                                                 true, a.fuse_rhs != 0))
+                    : nullptr;
+  // the operators (and the rows, G blocks and carry terms of a pending fix) stream in asynchronously: one
+  // L2 round trip, not one per element each thread copies
+  if (stg) stage_pending_fix(a, b, k, stg);
   for (int e = threadIdx.x; e < nr * nr; e += blockDim.x) {
     cp_async_elem(ops + e, Drg + e);
     cp_async_elem(ops + nr * nr + e, D2g + e);
@@ -479,8 +539,8 @@ __global__ void __launch_bounds__(384) k_fx_deriv(FxArgs a, T* deriv, size_t der
     }
     cp_async_all_done();
     __syncthreads();
-    if (nr <= 32) apply_pending_fix<4>(a, b, k, xd, sc);
-    else apply_pending_fix<2>(a, b, k, xd, sc);
+    if (nr <= 32) apply_pending_fix<4>(a, b, k, xd, sc, stg);
+    else apply_pending_fix<2>(a, b, k, xd, sc, stg);
     for (int e = threadIdx.x; e < 3 * nr; e += blockDim.x) xv[e] = (T)xd[e];
   } else {
     with_x<T>(a, b, [&](auto xr) {
@@ -1231,8 +1291,14 @@ static cudaError_t launch_fx_split_t(const FxArgs& a, int batch, cudaStream_t s)
   // right-hand side's FP64 block; the contractions follow on the corrected state
   const bool tc = sizeof(T) == 4 && a.deriv_t;
   if (!tc || a.fix.on || a.fuse_rhs) {
+    // a pending correction's G blocks and terms are staged with the operators while the CTA still fits
+    // twice on an SM (the per-mode CTAs of one shell outnumber the SMs)
+    FxArgs ad = a;
+    size_t sd = a.fix.on ? fix_stage_doubles(a.nr, a.fix.ldl, a.fix.nch) : 0;
+    if (fx_deriv_smem_bytes(a.nr, prec, a.fix.on != 0, a.fuse_rhs != 0, sd) > kFxDerivStageMaxBytes) sd = 0;
+    ad.fix.stage = sd > 0 ? 1 : 0;
     e = launch_kernel(k_fx_deriv<T>, dim3(a.M, batch), dim3(a.fix.on ? 384 : 256),
-                      fx_deriv_smem_bytes(a.nr, prec, a.fix.on != 0, a.fuse_rhs != 0), s, a,
+                      fx_deriv_smem_bytes(a.nr, prec, a.fix.on != 0, a.fuse_rhs != 0, sd), s, ad,
                       reinterpret_cast<T*>(a.deriv), a.deriv_stride);
     ktimer_mark(SDD_K_FX_DERIV, s);
     if (e != cudaSuccess) return e;

@@ -187,6 +187,8 @@ struct FixArgs {
   size_t d_stride, p_stride;
   double* X;                 // the state being corrected in place (the nonlinear term's input)
   float* X32;                // nullable: its FP32 copy
+  int stage;                 // set by the launcher: the mode's G blocks and carried-state terms are staged
+                             // in shared memory when they fit (fix_stage_doubles)
 };
 
 struct FxArgs {
