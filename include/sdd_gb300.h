@@ -205,7 +205,9 @@ typedef struct sdd_newton_opts {
   int32_t max_restarts;    /* GMRES cycles per Newton iteration                                     */
   int32_t max_newton;      /* Newton iteration cap                                                  */
   int32_t mixed_matvec;    /* 1: FP32 nonlinear term inside the Jacobian products (plan must be mixed);
-                              2: also FP32 right-hand sides and h = Linv g matvecs (chains stay FP64) */
+                              2: also FP32 right-hand sides and h = Linv g matvecs (chains stay FP64);
+                              3: as 2 with the GMRES basis stored and orthogonalised in FP32 (the
+                              residual, its norm and the update stay FP64)                          */
 } sdd_newton_opts;
 
 typedef struct sdd_newton_result {
@@ -250,7 +252,7 @@ typedef struct sdd_contin_opts {
   int32_t max_corrector;   /* corrector iterations before ds is halved (5)                         */
   int32_t max_halvings;
   int32_t mixed_matvec;    /* as in sdd_newton_opts: 0 FP64 products, 1 FP32 nonlinear term, 2 also FP32
-                              right-hand sides and h matvecs (mixed plans)                           */
+                              right-hand sides and h matvecs, 3 also an FP32 Krylov basis (mixed plans) */
   int32_t pad;
 } sdd_contin_opts;
 

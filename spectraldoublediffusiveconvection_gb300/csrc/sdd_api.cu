@@ -162,6 +162,7 @@ struct sdd_plan {
   int sv_B, sv_m;
   double reorth_eta;  // second Gram-Schmidt pass where |w'| < reorth_eta |w| (sdd_plan_set_reorth_eta)
   int kv_last_B;      // batch of the last GMRES solve (the layout sdd_krylov_basis reads)
+  int kv_basis32;     // the last GMRES solve kept its basis in FP32 (in kv_V's storage)
   double *kv_V, *kv_w, *kv_r, *kv_part, *kv_nrm2, *kv_small, *kv_dot;
   int* kv_ismall;
   int* kv_ticket;     // [B] per-shell CTA counters of the one-launch reductions (zero between launches)
@@ -735,9 +736,15 @@ int sdd_krylov_basis(const sdd_plan* p, int shell, int max_cols, double* out, in
   SDD_CUDA(cudaStreamSynchronize(s));
   const size_t n = (size_t)3 * p->M * p->nr, ld = n + 1, vs = (size_t)B * ld;
   const int c = kb < max_cols ? kb : max_cols;
-  for (int j = 0; j < c; ++j)
-    SDD_CUDA(cudaMemcpyAsync(out + (size_t)j * n, p->kv_V + (size_t)j * vs + (size_t)shell * ld, n * sizeof(double),
-                             cudaMemcpyDeviceToDevice, s));
+  for (int j = 0; j < c; ++j) {
+    if (p->kv_basis32) {   // FP32 basis: widened to FP64 on the way out
+      const float* src = reinterpret_cast<const float*>(p->kv_V) + (size_t)j * vs + (size_t)shell * ld;
+      SDD_CUDA(krylov_widen(src, out + (size_t)j * n, n, s));
+    } else {
+      SDD_CUDA(cudaMemcpyAsync(out + (size_t)j * n, p->kv_V + (size_t)j * vs + (size_t)shell * ld,
+                               n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
+  }
   *ncols = c;
   return SDD_OK;
 }
@@ -1396,10 +1403,28 @@ static int solver_wait(sdd_plan* p, cudaStream_t s) {
 // ld with nu used doubles.  resid (host) receives the final residual estimates.
 static int gmres_solve(sdd_plan* p, const MatVec& A, const MvSpec& spec, const double* rhs, double* x, int B, int nu,
                        int ld, int m, int max_restarts, const std::vector<double>& target,
-                       const std::vector<int>& solve, cudaStream_t s, int* matvecs, std::vector<double>& resid) {
+                       const std::vector<int>& solve, cudaStream_t s, int* matvecs, std::vector<double>& resid,
+                       bool basis32 = false) {
   GmresState G = gmres_state(p, B, m);
   p->kv_last_B = B;
+  p->kv_basis32 = basis32 ? 1 : 0;
   const size_t vs = (size_t)B * ld;
+  // the FP32 basis lives in the FP64 basis's storage (half of it)
+  float* V32 = reinterpret_cast<float*>(p->kv_V);
+  auto dots = [&](double* h, int nv, const int* mask) {
+    return basis32 ? krylov_dots(V32, vs, p->kv_w, nu, ld, nv, B, p->kv_part, h, m + 1, 0, s, mask, p->kv_ticket)
+                   : krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, nv, B, p->kv_part, h, m + 1, 0, s, mask, p->kv_ticket);
+  };
+  auto sub_norm = [&](const double* h, int nv, const int* sub_mask, const GmresState* reo_of, int j) {
+    return basis32 ? krylov_sub_norm(V32, vs, p->kv_w, h, m + 1, nu, ld, nv, B, sub_mask, G.active, p->kv_part,
+                                     p->kv_ticket, p->kv_nrm2, reo_of, j, p->reorth_eta, s)
+                   : krylov_sub_norm(p->kv_V, vs, p->kv_w, h, m + 1, nu, ld, nv, B, sub_mask, G.active, p->kv_part,
+                                     p->kv_ticket, p->kv_nrm2, reo_of, j, p->reorth_eta, s);
+  };
+  auto to_basis = [&](const double* src, int col) {
+    return basis32 ? krylov_scale(src, G.inv, V32 + (size_t)col * vs, nu, ld, B, s, p->kv_v32, p->kv_vin)
+                   : krylov_scale(src, G.inv, p->kv_V + (size_t)col * vs, nu, ld, B, s, p->kv_v32, p->kv_vin);
+  };
   int st;
   resid.assign(B, 0.0);
   SDD_CUDA(cudaMemcpyAsync(G.target, target.data(), B * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -1416,7 +1441,7 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const MvSpec& spec, const d
     }
     SDD_CUDA(krylov_dots(r, 0, r, nu, ld, 1, B, p->kv_part, p->kv_nrm2, 1, 0, s, nullptr, p->kv_ticket));
     SDD_CUDA(krylov_cycle_start(G, p->kv_nrm2, B, s));
-    SDD_CUDA(krylov_scale(r, G.inv, p->kv_V, nu, ld, B, s, p->kv_v32, p->kv_vin));
+    SDD_CUDA(to_basis(r, 0));
     for (int j = 0; j < m; ++j) {
       // kv_vin (and kv_v32 in FP32) hold V_j: a fixed address, so one captured graph serves every column
       if ((st = run_mv(p, A, spec, B, p->kv_vin, p->kv_w, G.active, p->kv_v32, s))) return st;
@@ -1425,17 +1450,12 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const MvSpec& spec, const d
       // each pass is two launches: the projections, then the update with the new norm (and after the first
       // pass the flag of the shells that repeat it: those whose first pass cancelled w below reorth_eta of
       // its norm; the others get zero second projections)
-      SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.hcol, m + 1, 0, s, G.active,
-                           p->kv_ticket));
-      SDD_CUDA(krylov_sub_norm(p->kv_V, vs, p->kv_w, G.hcol, m + 1, nu, ld, j + 1, B, G.active, G.active, p->kv_part,
-                               p->kv_ticket, p->kv_nrm2, &G, j, p->reorth_eta, s));
-      SDD_CUDA(krylov_dots(p->kv_V, vs, p->kv_w, nu, ld, j + 1, B, p->kv_part, G.h2, m + 1, 0, s, G.reo,
-                           p->kv_ticket));
-      SDD_CUDA(krylov_sub_norm(p->kv_V, vs, p->kv_w, G.h2, m + 1, nu, ld, j + 1, B, G.reo, G.active, p->kv_part,
-                               p->kv_ticket, p->kv_nrm2, nullptr, j, p->reorth_eta, s));
+      SDD_CUDA(dots(G.hcol, j + 1, G.active));
+      SDD_CUDA(sub_norm(G.hcol, j + 1, G.active, &G, j));
+      SDD_CUDA(dots(G.h2, j + 1, G.reo));
+      SDD_CUDA(sub_norm(G.h2, j + 1, G.reo, nullptr, j));
       SDD_CUDA(krylov_arnoldi_finish(G, p->kv_nrm2, j, B, s));
-      if (j + 1 < m)
-        SDD_CUDA(krylov_scale(p->kv_w, G.inv, p->kv_V + (size_t)(j + 1) * vs, nu, ld, B, s, p->kv_v32, p->kv_vin));
+      if (j + 1 < m) SDD_CUDA(to_basis(p->kv_w, j + 1));
       // the flags after column j go to slot j; the host reads those of column j - kFlagLag
       const int slot = j % (kFlagLag + 1);
       SDD_CUDA(cudaMemcpyAsync(p->h_int + (size_t)slot * B, G.active, B * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1452,7 +1472,8 @@ static int gmres_solve(sdd_plan* p, const MatVec& A, const MvSpec& spec, const d
       }
     }
     SDD_CUDA(krylov_solve_y(G, B, s));
-    SDD_CUDA(krylov_add_combination(p->kv_V, vs, x, G.y, m, G.kb, nu, ld, B, s));
+    if (basis32) SDD_CUDA(krylov_add_combination(V32, vs, x, G.y, m, G.kb, nu, ld, B, s));
+    else SDD_CUDA(krylov_add_combination(p->kv_V, vs, x, G.y, m, G.kb, nu, ld, B, s));
     SDD_CUDA(cudaMemcpyAsync(p->h_dbl, G.resid, B * sizeof(double), cudaMemcpyDeviceToHost, s));
     if ((st = solver_wait(p, s))) return st;
     bool more = false;
@@ -1481,7 +1502,7 @@ extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const doub
   if (!Ra || !Ras || !X || !o || !res) return SDD_ERR_ARG;
   const int m = o->restart;
   if (m < 1 || m > 64 || o->max_newton < 0 || o->max_restarts < 1 || !(o->tol >= 0.0)) return SDD_ERR_ARG;
-  if (o->mixed_matvec < 0 || o->mixed_matvec > 2) return SDD_ERR_ARG;
+  if (o->mixed_matvec < 0 || o->mixed_matvec > 3) return SDD_ERR_ARG;
   if (o->mixed_matvec && p->prec != SDD_PREC_MIXED) return SDD_ERR_ARG;
   if ((st = solver_reserve(p, B, m))) return st;
   cudaStream_t s = (cudaStream_t)stream;
@@ -1497,12 +1518,13 @@ extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const doub
   SDD_CUDA(cudaMemcpyAsync(Ra_d, Ra, B * sizeof(double), cudaMemcpyDeviceToDevice, s));
   SDD_CUDA(cudaMemcpyAsync(Ras_d, Ras, B * sizeof(double), cudaMemcpyDeviceToDevice, s));
   // the Jacobian of PFX about the cached base state, on vectors of stride ld
-  const bool fp32_rhs = o->mixed_matvec == 2;
+  const bool fp32_rhs = o->mixed_matvec >= 2;
+  const bool basis32 = o->mixed_matvec == 3;
   MatVec J = [&](const double* v, double* out, const int* active, const float* v32, cudaStream_t sm) {
     return apply_step_ld(p, B, Ra_d, Ras_d, v, ld, out, ld, v, ld, 1, base_mv, mv_prec, sm, nullptr, nullptr, nullptr,
                          active, 0, 0, o->mixed_matvec ? v32 : nullptr, fp32_rhs);
   };
-  const MvSpec Jspec{1 + o->mixed_matvec, Ra_d, Ras_d, base_mv};
+  const MvSpec Jspec{1 + (fp32_rhs ? 2 : o->mixed_matvec), Ra_d, Ras_d, base_mv};
   for (int it = 0;; ++it) {
     if ((st = apply_step_ld(p, B, Ra_d, Ras_d, X, n, p->sv_F, ld, X, n, 0, p->sv_base64, SDD_PREC_FP64, s)))
       return st;                                                         // F = PFX(X), base cached
@@ -1523,7 +1545,7 @@ extern "C" int sdd_newton_gmres(sdd_plan* p, int B, const double* Ra, const doub
     }
     for (int b = 0; b < B; ++b) target[b] = o->gmres_rtol * resF[b];
     if ((st = gmres_solve(p, J, Jspec, p->sv_F, p->sv_x, B, n, ld, m, o->max_restarts, target, nmask, s, &matvecs,
-                          resid)))
+                          resid, basis32)))
       return st;
     int* mask_dev = p->kv_ismall + 3 * B;
     SDD_CUDA(cudaMemcpyAsync(mask_dev, nmask.data(), B * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -1561,12 +1583,13 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
   const int m = o->restart;
   if (m < 1 || m > 64 || o->max_restarts < 1 || o->max_corrector < 1 || o->max_halvings < 0 || !(o->tol > 0.0))
     return SDD_ERR_ARG;
-  if (o->mixed_matvec < 0 || o->mixed_matvec > 2) return SDD_ERR_ARG;
+  if (o->mixed_matvec < 0 || o->mixed_matvec > 3) return SDD_ERR_ARG;
   if (o->mixed_matvec && p->prec != SDD_PREC_MIXED) return SDD_ERR_ARG;
   if ((st = solver_reserve(p, B, m))) return st;
   cudaStream_t s = (cudaStream_t)stream;
   const int n = (int)shell_elems(p), ld = n + 1, Npsi = p->M * p->nr;
-  const bool fp32_rhs = o->mixed_matvec == 2;   // FP32 right-hand sides and h matvecs in the products too
+  const bool fp32_rhs = o->mixed_matvec >= 2;   // FP32 right-hand sides and h matvecs in the products too
+  const bool basis32 = o->mixed_matvec == 3;    // and an FP32 Krylov basis
   const double delta = 1.0 / n;                         // 1/(3N), Main.py:771
   const int mv_prec = o->mixed_matvec ? SDD_PREC_MIXED : SDD_PREC_FP64;
   void* base_mv = o->mixed_matvec ? (void*)p->sv_base32 : (void*)p->sv_base64;
@@ -1607,8 +1630,9 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
     SDD_CUDA(contin_border(v, out, n, ld, p->sv_Jmu, n, Npsi, p->kv_dot, mudot_dev, delta, B, sm));
     return SDD_OK;
   };
-  const MvSpec Jspec{4 + o->mixed_matvec, mu_dev, Ras_d, base_mv};
-  const MvSpec DGspec{8 + o->mixed_matvec, mu_dev, Ras_d, base_mv};
+  const int mv_kind = fp32_rhs ? 2 : o->mixed_matvec;   // the products of modes 2 and 3 are the same
+  const MvSpec Jspec{4 + mv_kind, mu_dev, Ras_d, base_mv};
+  const MvSpec DGspec{8 + mv_kind, mu_dev, Ras_d, base_mv};
 
   // ---- predictor (Main.py:839-876; with dt < 10 the tangent is always recomputed) ----
   SDD_CUDA(upload(mu_dev, mu));
@@ -1620,7 +1644,8 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
     tgt[b] = o->tangent_rtol * nj;
     solve[b] = nj > 0.0;
   }
-  if ((st = gmres_solve(p, J, Jspec, p->sv_G, p->sv_x, B, n, ld, m, o->max_restarts, tgt, solve, s, &matvecs, resid)))
+  if ((st = gmres_solve(p, J, Jspec, p->sv_G, p->sv_x, B, n, ld, m, o->max_restarts, tgt, solve, s, &matvecs, resid,
+                        basis32)))
     return st;
   if ((st = host_norms2(p, p->sv_x, n, ld, B, s))) return st;
   for (int b = 0; b < B; ++b) {
@@ -1694,7 +1719,7 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
     for (int b = 0; b < B; ++b)
       tgt[b] = o->gmres_rtol * std::sqrt(delta * resF[b] * resF[b] + (1.0 - delta) * gl[b] * gl[b]);  // :919
     if ((st = gmres_solve(p, DG, DGspec, p->sv_G, p->sv_x, B, n + 1, ld, m, o->max_restarts, tgt, solve, s, &matvecs,
-                          resid)))
+                          resid, basis32)))
       return st;
     int* mask_dev = p->kv_ismall + 3 * B;
     SDD_CUDA(cudaMemcpyAsync(mask_dev, solve.data(), B * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -1719,7 +1744,7 @@ extern "C" int sdd_contin_step(sdd_plan* p, int B, double* X, double* Ra, const 
     solve[b] = conv[b];
   }
   if ((st = gmres_solve(p, DG, DGspec, p->sv_G, p->sv_x, B, n + 1, ld, m, o->max_restarts, tgt, solve, s, &matvecs,
-                        resid)))
+                        resid, basis32)))
     return st;
   if ((st = host_norms2(p, p->sv_x, n, ld, B, s))) return st;
   std::vector<double> yx2(p->h_dbl, p->h_dbl + B);

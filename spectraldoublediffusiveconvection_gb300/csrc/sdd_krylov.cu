@@ -9,6 +9,13 @@
 //
 // Vector layout: V[i][b][ld]: Krylov vector i of shell b has n used doubles at stride ld (n = 3*N_fm*nr
 // for Newton, n+1 with the continuation parameter appended for the bordered arclength system).
+//
+// FP32 basis (the VT = float instances): the Krylov vectors are stored rounded to FP32 and the
+// Gram-Schmidt products run in FP32 arithmetic (per-thread FP32 partial sums over a few elements, the
+// cross-thread sums in FP64); w, the norms, the Hessenberg matrix and the rotations stay FP64.  For inner
+// solves whose tolerance (relative 1e-4 in Newton) is far above FP32 rounding: the outer residual is FP64,
+// so the converged state is unchanged in accuracy.  The FP64 products are bound by the FP64 multiply-add
+// rate (one per element of V), the FP32 ones by the bytes of V, half as many.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -80,7 +87,8 @@ __device__ __forceinline__ void reduce_partials(const double* part, int b, int n
 
 // blockIdx.z selects the vectors [z vpb, (z+1) vpb) of the CTA (vpb a multiple of kDotVecs): small batches
 // spread the vectors over more CTAs; every partial is summed the same way whatever the split.
-__global__ void __launch_bounds__(kDotThreads) k_dot_partials(const double* __restrict__ V, size_t vstride_i,
+template <typename VT>
+__global__ void __launch_bounds__(kDotThreads) k_dot_partials(const VT* __restrict__ V, size_t vstride_i,
                                                              const double* __restrict__ w, int n, int ld, int nv,
                                                              int chunk, double* part,
                                                              const int* __restrict__ active, int* ticket,
@@ -94,26 +102,29 @@ __global__ void __launch_bounds__(kDotThreads) k_dot_partials(const double* __re
     const int e0 = c * chunk;
     const double* wb = w + (size_t)b * ld;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double wr[kDotPer];
+    VT wr[kDotPer];
 #pragma unroll
     for (int k = 0; k < kDotPer; ++k) {
       const int e = e0 + threadIdx.x + k * kDotThreads;
-      wr[k] = e < n ? wb[e] : 0.0;
+      wr[k] = e < n ? (VT)wb[e] : (VT)0;
     }
     for (int i0 = ib; i0 < ie; i0 += kDotVecs) {
-      double sv[kDotVecs];
+      VT sp[kDotVecs];
 #pragma unroll
       for (int u = 0; u < kDotVecs; ++u) {
-        sv[u] = 0.0;
+        sp[u] = (VT)0;
         if (i0 + u < ie) {
-          const double* vb = V + (size_t)(i0 + u) * vstride_i + (size_t)b * ld;
+          const VT* vb = V + (size_t)(i0 + u) * vstride_i + (size_t)b * ld;
 #pragma unroll
           for (int k = 0; k < kDotPer; ++k) {
             const int e = e0 + threadIdx.x + k * kDotThreads;
-            if (e < n) sv[u] = fma(vb[e], wr[k], sv[u]);
+            if (e < n) sp[u] = fma(vb[e], wr[k], sp[u]);
           }
         }
       }
+      double sv[kDotVecs];
+#pragma unroll
+      for (int u = 0; u < kDotVecs; ++u) sv[u] = (double)sp[u];
       static_assert(kDotVecs == 4, "warp_sum4 reduces four vectors");
       const double ws = warp_sum4(sv, lane);
       if ((lane & 7) == 0) red[lane >> 3][warp] = ws;
@@ -137,13 +148,15 @@ __global__ void __launch_bounds__(kDotThreads) k_dot_partials(const double* __re
 // basis dominate, so one shell's update spreads over four times the CTAs).  With reo != nullptr the shell's
 // last CTA also sets the second-pass flag of column j: active and |w'|^2 < eta^2 (|w'|^2 + |h|^2), where
 // |w|^2 = |w'|^2 + |h|^2 for an orthonormal basis.
-__global__ void __launch_bounds__(kDotThreads) k_sub_norm(const double* __restrict__ V, size_t vstride_i, double* w,
+template <typename VT>
+__global__ void __launch_bounds__(kDotThreads) k_sub_norm(const VT* __restrict__ V, size_t vstride_i, double* w,
                                                          const double* __restrict__ coef, int ldc, int n, int ld,
                                                          int nv, const int* __restrict__ sub_mask,
                                                          const int* __restrict__ norm_mask, double* part,
                                                          int* ticket, double* nrm2, GmresState gs, int j,
                                                          double eta2, int set_reo) {
   __shared__ double red[kDotVecs][kDotThreads / 32];
+  __shared__ VT cs[kMaxRestart + 1];                   // the coefficients in the basis's precision
   const int c = blockIdx.x, b = blockIdx.y, nchunk = gridDim.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int e0 = c * kSubChunk;
@@ -151,6 +164,8 @@ __global__ void __launch_bounds__(kDotThreads) k_sub_norm(const double* __restri
   const bool sub = !sub_mask || sub_mask[b];
   const bool nrm = !norm_mask || norm_mask[b];
   const double* cb = coef + (size_t)b * ldc;
+  for (int i = threadIdx.x; i < nv && i <= kMaxRestart; i += blockDim.x) cs[i] = (VT)cb[i];
+  __syncthreads();
   double sv[kDotVecs] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
   for (int k = 0; k < kSubPer; ++k) {
@@ -158,9 +173,9 @@ __global__ void __launch_bounds__(kDotThreads) k_sub_norm(const double* __restri
     if (e < n) {
       double x = wb[e];
       if (sub) {
-        double t = 0.0;
-        for (int i = 0; i < nv; ++i) t += V[(size_t)i * vstride_i + (size_t)b * ld + e] * cb[i];
-        x -= t;
+        VT t = (VT)0;
+        for (int i = 0; i < nv; ++i) t += V[(size_t)i * vstride_i + (size_t)b * ld + e] * cs[i];
+        x -= (double)t;
         wb[e] = x;
       }
       if (nrm) sv[0] = fma(x, x, sv[0]);
@@ -205,17 +220,21 @@ __global__ void k_dot_reduce(const double* __restrict__ part, int nv, int nchunk
   }
 }
 
-// x[b] += sum_{i<k_b} V_i[b] * y[b*ldy + i]
-__global__ void k_add_combination(const double* __restrict__ V, size_t vstride_i, double* __restrict__ x,
+// x[b] += sum_{i<k_b} V_i[b] * y[b*ldy + i]  (the sum in the basis's precision)
+template <typename VT>
+__global__ void k_add_combination(const VT* __restrict__ V, size_t vstride_i, double* __restrict__ x,
                                   const double* __restrict__ y, int ldy, const int* __restrict__ kb, int n,
                                   int ld) {
+  __shared__ VT ys[kMaxRestart];
   const int b = blockIdx.y;
-  const int k = kb[b];
+  const int k = min(kb[b], kMaxRestart);
   const double* yb = y + (size_t)b * ldy;
+  for (int i = threadIdx.x; i < k; i += blockDim.x) ys[i] = (VT)yb[i];
+  __syncthreads();
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int i = 0; i < k; ++i) s += V[(size_t)i * vstride_i + (size_t)b * ld + e] * yb[i];
-    x[(size_t)b * ld + e] += s;
+    VT s = (VT)0;
+    for (int i = 0; i < k; ++i) s += V[(size_t)i * vstride_i + (size_t)b * ld + e] * ys[i];
+    x[(size_t)b * ld + e] += (double)s;
   }
 }
 
@@ -230,6 +249,26 @@ __global__ void k_scale(const double* __restrict__ a, const double* __restrict__
     if (out32) out32[(size_t)b * ld + e] = (float)v;
     if (out2) out2[(size_t)b * ld + e] = v;
   }
+}
+
+// FP32 basis: out[b] = fl32(a[b] * scale[b]); out32 (nullable) the same FP32 values, out2 (nullable) them
+// in FP64 (the vector the next product reads is exactly the stored basis vector)
+__global__ void k_scale_to32(const double* __restrict__ a, const double* __restrict__ scale, float* __restrict__ out,
+                             int n, int ld, float* __restrict__ out32, double* __restrict__ out2) {
+  const int b = blockIdx.y;
+  const double s = scale[b];
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const float v = (float)(a[(size_t)b * ld + e] * s);
+    out[(size_t)b * ld + e] = v;
+    if (out32) out32[(size_t)b * ld + e] = v;
+    if (out2) out2[(size_t)b * ld + e] = (double)v;
+  }
+}
+
+// out[e] = (double)in[e]
+__global__ void k_widen(const float* __restrict__ in, double* __restrict__ out, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    out[e] = (double)in[e];
 }
 
 // out = a - b
@@ -406,9 +445,10 @@ static int sm_count_dev() {
   return n;
 }
 
-cudaError_t krylov_dots(const double* V, size_t vstride_i, const double* w, int n, int ld, int nv, int B,
-                        double* part, double* h, int ldh, int accumulate, cudaStream_t st, const int* active,
-                        int* ticket) {
+template <typename VT>
+static cudaError_t krylov_dots_t(const VT* V, size_t vstride_i, const double* w, int n, int ld, int nv, int B,
+                                 double* part, double* h, int ldh, int accumulate, cudaStream_t st, const int* active,
+                                 int* ticket) {
   const int nchunk = (n + kDotChunk - 1) / kDotChunk;
   // with the one-launch reduction, spread the vectors over CTAs until the launch has ~2 CTAs per SM
   int nvg = 1;
@@ -419,33 +459,72 @@ cudaError_t krylov_dots(const double* V, size_t vstride_i, const double* w, int 
   int vpb = (nv + nvg - 1) / nvg;
   vpb = (vpb + kDotVecs - 1) / kDotVecs * kDotVecs;
   nvg = (nv + vpb - 1) / vpb;
-  k_dot_partials<<<dim3(nchunk, B, nvg), kDotThreads, 0, st>>>(V, vstride_i, w, n, ld, nv, kDotChunk, part, active,
-                                                               ticket, h, ldh, accumulate, vpb);
+  k_dot_partials<VT><<<dim3(nchunk, B, nvg), kDotThreads, 0, st>>>(V, vstride_i, w, n, ld, nv, kDotChunk, part,
+                                                                   active, ticket, h, ldh, accumulate, vpb);
   if (!ticket) k_dot_reduce<<<B, 64, 0, st>>>(part, nv, nchunk, h, ldh, accumulate);
   return cudaGetLastError();
 }
+cudaError_t krylov_dots(const double* V, size_t vstride_i, const double* w, int n, int ld, int nv, int B,
+                        double* part, double* h, int ldh, int accumulate, cudaStream_t st, const int* active,
+                        int* ticket) {
+  return krylov_dots_t(V, vstride_i, w, n, ld, nv, B, part, h, ldh, accumulate, st, active, ticket);
+}
+cudaError_t krylov_dots(const float* V, size_t vstride_i, const double* w, int n, int ld, int nv, int B,
+                        double* part, double* h, int ldh, int accumulate, cudaStream_t st, const int* active,
+                        int* ticket) {
+  return krylov_dots_t(V, vstride_i, w, n, ld, nv, B, part, h, ldh, accumulate, st, active, ticket);
+}
 
-cudaError_t krylov_sub_norm(const double* V, size_t vstride_i, double* w, const double* coef, int ldc, int n, int ld,
-                            int nv, int B, const int* sub_mask, const int* norm_mask, double* part, int* ticket,
-                            double* nrm2, const GmresState* reo_of, int j, double eta, cudaStream_t st) {
-  if (!ticket) return cudaErrorInvalidValue;
+template <typename VT>
+static cudaError_t krylov_sub_norm_t(const VT* V, size_t vstride_i, double* w, const double* coef, int ldc, int n,
+                                     int ld, int nv, int B, const int* sub_mask, const int* norm_mask, double* part,
+                                     int* ticket, double* nrm2, const GmresState* reo_of, int j, double eta,
+                                     cudaStream_t st) {
+  if (!ticket || nv > kMaxRestart + 1) return cudaErrorInvalidValue;
   const int nchunk = (n + kSubChunk - 1) / kSubChunk;
   GmresState gs{};
   if (reo_of) gs = *reo_of;
-  k_sub_norm<<<dim3(nchunk, B), kDotThreads, 0, st>>>(V, vstride_i, w, coef, ldc, n, ld, nv, sub_mask, norm_mask,
-                                                      part, ticket, nrm2, gs, j, eta * eta, reo_of ? 1 : 0);
+  k_sub_norm<VT><<<dim3(nchunk, B), kDotThreads, 0, st>>>(V, vstride_i, w, coef, ldc, n, ld, nv, sub_mask, norm_mask,
+                                                          part, ticket, nrm2, gs, j, eta * eta, reo_of ? 1 : 0);
   return cudaGetLastError();
+}
+cudaError_t krylov_sub_norm(const double* V, size_t vstride_i, double* w, const double* coef, int ldc, int n, int ld,
+                            int nv, int B, const int* sub_mask, const int* norm_mask, double* part, int* ticket,
+                            double* nrm2, const GmresState* reo_of, int j, double eta, cudaStream_t st) {
+  return krylov_sub_norm_t(V, vstride_i, w, coef, ldc, n, ld, nv, B, sub_mask, norm_mask, part, ticket, nrm2, reo_of,
+                           j, eta, st);
+}
+cudaError_t krylov_sub_norm(const float* V, size_t vstride_i, double* w, const double* coef, int ldc, int n, int ld,
+                            int nv, int B, const int* sub_mask, const int* norm_mask, double* part, int* ticket,
+                            double* nrm2, const GmresState* reo_of, int j, double eta, cudaStream_t st) {
+  return krylov_sub_norm_t(V, vstride_i, w, coef, ldc, n, ld, nv, B, sub_mask, norm_mask, part, ticket, nrm2, reo_of,
+                           j, eta, st);
 }
 
 cudaError_t krylov_add_combination(const double* V, size_t vstride_i, double* x, const double* y, int ldy,
                                    const int* kb, int n, int ld, int B, cudaStream_t st) {
-  k_add_combination<<<dim3(grid_x(n), B), 256, 0, st>>>(V, vstride_i, x, y, ldy, kb, n, ld);
+  k_add_combination<double><<<dim3(grid_x(n), B), 256, 0, st>>>(V, vstride_i, x, y, ldy, kb, n, ld);
+  return cudaGetLastError();
+}
+cudaError_t krylov_add_combination(const float* V, size_t vstride_i, double* x, const double* y, int ldy,
+                                   const int* kb, int n, int ld, int B, cudaStream_t st) {
+  k_add_combination<float><<<dim3(grid_x(n), B), 256, 0, st>>>(V, vstride_i, x, y, ldy, kb, n, ld);
   return cudaGetLastError();
 }
 
 cudaError_t krylov_scale(const double* a, const double* scale, double* out, int n, int ld, int B, cudaStream_t st,
                          float* out32, double* out2) {
   k_scale<<<dim3(grid_x(n), B), 256, 0, st>>>(a, scale, out, n, ld, out32, out2);
+  return cudaGetLastError();
+}
+cudaError_t krylov_scale(const double* a, const double* scale, float* out, int n, int ld, int B, cudaStream_t st,
+                         float* out32, double* out2) {
+  k_scale_to32<<<dim3(grid_x(n), B), 256, 0, st>>>(a, scale, out, n, ld, out32, out2);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_widen(const float* in, double* out, size_t n, cudaStream_t st) {
+  k_widen<<<grid_x((int)(n > (1u << 30) ? (1u << 30) : n)), 256, 0, st>>>(in, out, n);
   return cudaGetLastError();
 }
 

@@ -41,6 +41,18 @@ constexpr double kReorthEta = 0.70710678118654752440;
 cudaError_t krylov_dots(const double* V, size_t vstride_i, const double* w, int n, int ld, int nv, int B,
                         double* part, double* h, int ldh, int accumulate, cudaStream_t st,
                         const int* active = nullptr, int* ticket = nullptr);
+// The FP32-basis forms (V stored in FP32, the products in FP32 arithmetic, see sdd_krylov.cu) of krylov_dots,
+// krylov_sub_norm, krylov_add_combination and krylov_scale (out rounded to FP32; out2 = the FP32 values).
+cudaError_t krylov_dots(const float* V, size_t vstride_i, const double* w, int n, int ld, int nv, int B,
+                        double* part, double* h, int ldh, int accumulate, cudaStream_t st,
+                        const int* active = nullptr, int* ticket = nullptr);
+cudaError_t krylov_sub_norm(const float* V, size_t vstride_i, double* w, const double* coef, int ldc, int n, int ld,
+                            int nv, int B, const int* sub_mask, const int* norm_mask, double* part, int* ticket,
+                            double* nrm2, const GmresState* reo_of, int j, double eta, cudaStream_t st);
+cudaError_t krylov_add_combination(const float* V, size_t vstride_i, double* x, const double* y, int ldy,
+                                   const int* kb, int n, int ld, int B, cudaStream_t st);
+cudaError_t krylov_scale(const double* a, const double* scale, float* out, int n, int ld, int B, cudaStream_t st,
+                         float* out32 = nullptr, double* out2 = nullptr);
 // One launch for a Gram-Schmidt pass's update and the new norm: w -= V coef where sub_mask (nullable: all),
 // nrm2 = |w|^2 where norm_mask (nullable: all; 0 elsewhere), with the sums of krylov_dots; reo_of
 // (nullable): also set reo_of->reo for column j (active and |w'|^2 < eta^2 (|w'|^2 + |h|^2), the shells
@@ -54,6 +66,7 @@ cudaError_t krylov_add_combination(const double* V, size_t vstride_i, double* x,
 cudaError_t krylov_scale(const double* a, const double* scale, double* out, int n, int ld, int B, cudaStream_t st,
                          float* out32 = nullptr, double* out2 = nullptr);
 cudaError_t krylov_sub(const double* a, const double* b, double* out, size_t n, cudaStream_t st);
+cudaError_t krylov_widen(const float* in, double* out, size_t n, cudaStream_t st);   // out = (double)in
 cudaError_t krylov_masked_sub(double* X, const double* dx, const int* mask, int n, int ldx, int ld, int B,
                               cudaStream_t st);
 cudaError_t krylov_cycle_start(const GmresState& s, const double* nrm2, int B, cudaStream_t st);

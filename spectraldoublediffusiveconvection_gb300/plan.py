@@ -324,12 +324,13 @@ class Plan:
         """Newton-GMRES on F(X) = Phi_dt(X) - X in place on X (batch x n_state); returns per-shell dicts
         (residual0, residual, newton_iters, matvecs, converged).  The plan's dt should be 1 (Main.py:430).
         mixed_matvec (mixed plans): False/0 FP64 Jacobian products, True/1 with the FP32 nonlinear term,
-        2 also with FP32 right-hand sides and h = Linv g matvecs (the chains and the residual stay FP64)."""
+        2 also with FP32 right-hand sides and h = Linv g matvecs (the chains and the residual stay FP64),
+        3 as 2 with the GMRES basis stored and orthogonalised in FP32 (the Newton residual stays FP64)."""
         B = self._chk(X, self.n_state, "X")
         ra, ras = self._vec(Ra, B), self._vec(Ra_s, B)
         mv = int(mixed_matvec)
-        if mv not in (0, 1, 2):
-            raise ValueError("mixed_matvec: expected False/True, 0, 1 or 2")
+        if mv not in (0, 1, 2, 3):
+            raise ValueError("mixed_matvec: expected False/True, 0, 1, 2 or 3")
         o = _lib.NewtonOpts(float(tol), float(gmres_rtol), int(restart), int(max_restarts), int(max_newton), mv)
         res = (_lib.NewtonResult * B)()
         st = self._L.sdd_newton_gmres(self._h, B, _dptr(ra), _dptr(ras), _dptr(X), ctypes.byref(o), res,
@@ -369,8 +370,8 @@ class Plan:
         sg = (ctypes.c_double * B)(*[float(v) for v in np.broadcast_to(np.asarray(sign, dtype=float), (B,))])
         dd = (ctypes.c_double * B)(*[float(v) for v in np.broadcast_to(np.asarray(ds, dtype=float), (B,))])
         mv = int(mixed_matvec)
-        if mv not in (0, 1, 2):
-            raise ValueError("mixed_matvec: expected False/True, 0, 1 or 2")
+        if mv not in (0, 1, 2, 3):
+            raise ValueError("mixed_matvec: expected False/True, 0, 1, 2 or 3")
         o = _lib.ContinOpts(float(tol), float(gmres_rtol), float(tangent_rtol), int(restart), int(max_restarts),
                             int(max_corrector), int(max_halvings), mv, 0)
         res = (_lib.ContinResult * B)()

@@ -132,7 +132,8 @@ class Server:
     """Request server over one GPU.  Integrations use plans with step dt and nonlinear-term precision
     ``int_precision``; continuation steps use plans with dt = 1 (Main.py:430, PFX over one unit of time),
     an FP64 residual <= tol, and inside the Jacobian products the FP32 nonlinear term when ``con_mixed`` is
-    1 (or True), and FP32 right-hand sides and h = Linv g matvecs as well when it is 2.
+    1 (or True), FP32 right-hand sides and h = Linv g matvecs as well when it is 2, and an FP32 Krylov basis
+    too when it is 3.
     Integrations default to the mixed form (FP32 nonlinear term, FP64 implicit solves: 1.7x the served
     integration throughput of FP64 at these sizes; its trajectory error against FP64 is checked by the
     mixed-precision tests).  Every plan has the fixed chain layout ``chain_layout`` (default: chunked, the
@@ -146,8 +147,8 @@ class Server:
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.d, self.Pr, self.Tau, self.Ra_s, self.dt = d, Pr, Tau, Ra_s, dt
         self.int_precision, self.con_mixed = int_precision, int(con_mixed)
-        if self.con_mixed not in (0, 1, 2):
-            raise ValueError("con_mixed: expected False/True, 0, 1 or 2")
+        if self.con_mixed not in (0, 1, 2, 3):
+            raise ValueError("con_mixed: expected False/True, 0, 1, 2 or 3")
         self.quantum, self.max_batch, self.con_workers = int(quantum), int(max_batch), int(con_workers)
         self.chain_layout, self.tol, self.restart, self.tangent_rtol = chain_layout, tol, restart, tangent_rtol
         if memory_budget is None:
