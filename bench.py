@@ -856,11 +856,12 @@ def bench_gb300(args):
     return 0
 
 
-def profile_newton_batch():
+def profile_newton_batch(mixed_matvec=2):
     """One Newton iteration (residual, one GMRES(50) solve, update) of the 64-shell batched Newton workload
     inside an NVTX range "newton_batched", for a kernel launch list of the batched Jacobian products:
-    ncu --nvtx --nvtx-include "newton_batched/" ... python bench.py --profile-newton-batch.  The start: the
-    seeded shell after 2000 IMEX steps of dt=5e-4 plus the 64 seeded perturbations of the bench workload."""
+    ncu --nvtx --nvtx-include "newton_batched/" ... python bench.py --profile-newton-batch [MODE].  The start:
+    the seeded shell after 2000 IMEX steps of dt=5e-4 plus the 64 seeded perturbations of the bench workload;
+    MODE the mixed_matvec value (2: FP64 Krylov basis, 3: FP32 basis)."""
     import numpy as np
     import torch
     from spectraldoublediffusiveconvection_gb300.seeds import seeded_state
@@ -878,13 +879,14 @@ def profile_newton_batch():
     Ras = torch.full((nb,), w["Ra_S"], dtype=torch.float64, device=device)
     q = Plan(M, N_r, w["d"], 1.0, w["Pr"], w["Tau"], precision="mixed", device=device)
     q.set_chain_layout(4)
-    q.newton(Xb0.clone(), Rab, Ras, tol=1e-10, restart=50, max_newton=1, mixed_matvec=2)   # warm-up
+    q.newton(Xb0.clone(), Rab, Ras, tol=1e-10, restart=50, max_newton=1, mixed_matvec=mixed_matvec)   # warm-up
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_push("newton_batched")
-    r = q.newton(Xb0.clone(), Rab, Ras, tol=1e-10, restart=50, max_newton=1, mixed_matvec=2)
+    r = q.newton(Xb0.clone(), Rab, Ras, tol=1e-10, restart=50, max_newton=1, mixed_matvec=mixed_matvec)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
-    print(json.dumps({"profile": "newton_batched", "shells": nb, "jacobian_products": r[0]["matvecs"]}))
+    print(json.dumps({"profile": "newton_batched", "shells": nb, "mixed_matvec": mixed_matvec,
+                      "jacobian_products": r[0]["matvecs"]}))
     return 0
 
 
@@ -992,15 +994,15 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--served-requests", type=int, default=1000)
-    ap.add_argument("--profile-newton-batch", action="store_true")
+    ap.add_argument("--profile-newton-batch", nargs="?", type=int, const=2, default=None, metavar="MODE")
     ap.add_argument("--profile-deriv-tc", type=int, metavar="SHELLS")
     ap.add_argument("--profile-step-batch", nargs=2, metavar=("PRECISION", "LAYOUT"))
     ap.add_argument("--probe-phase-boundaries", action="store_true")
     args = ap.parse_args()
     if args.probe_phase_boundaries:
         return probe_phase_boundaries()
-    if args.profile_newton_batch:
-        return profile_newton_batch()
+    if args.profile_newton_batch is not None:
+        return profile_newton_batch(args.profile_newton_batch)
     if args.profile_deriv_tc:
         return profile_deriv_tc(args.profile_deriv_tc)
     if args.profile_step_batch:

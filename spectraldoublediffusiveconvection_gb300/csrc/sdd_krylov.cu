@@ -56,6 +56,23 @@ __device__ __forceinline__ double warp_sum4(const double (&sv)[4], int lane) {
   return k;
 }
 
+// warp_sum4 in FP32 (the FP32 basis's projections: conversions and FP64 additions hold the FP64 pipe, the
+// FP32 ones do not); the same lane pattern.
+__device__ __forceinline__ float warp_sum4f(const float (&sv)[4], int lane) {
+  const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0;
+  float k0 = h16 ? sv[2] : sv[0], k1 = h16 ? sv[3] : sv[1];
+  const float s0 = h16 ? sv[0] : sv[2], s1 = h16 ? sv[1] : sv[3];
+  k0 += __shfl_xor_sync(0xffffffffu, s0, 16);
+  k1 += __shfl_xor_sync(0xffffffffu, s1, 16);
+  float k = h8 ? k1 : k0;
+  const float t = h8 ? k0 : k1;
+  k += __shfl_xor_sync(0xffffffffu, t, 8);
+  k += __shfl_xor_sync(0xffffffffu, k, 4);
+  k += __shfl_xor_sync(0xffffffffu, k, 2);
+  k += __shfl_xor_sync(0xffffffffu, k, 1);
+  return k;
+}
+
 // The last CTA of a shell to finish (ticket[b], one counter per shell, zero between launches) sums the
 // shell's partials in chunk order and writes h: the reduction of k_dot_reduce, without its launch.
 __device__ __forceinline__ bool last_chunk_of_shell(int* ticket, int b, int nblocks) {
@@ -122,11 +139,13 @@ __global__ void __launch_bounds__(kDotThreads) k_dot_partials(const VT* __restri
           }
         }
       }
-      double sv[kDotVecs];
-#pragma unroll
-      for (int u = 0; u < kDotVecs; ++u) sv[u] = (double)sp[u];
       static_assert(kDotVecs == 4, "warp_sum4 reduces four vectors");
-      const double ws = warp_sum4(sv, lane);
+      double ws;
+      if constexpr (sizeof(VT) == 4) {
+        ws = (double)warp_sum4f(sp, lane);             // the warp's 256 products in FP32, then FP64
+      } else {
+        ws = warp_sum4(sp, lane);
+      }
       if ((lane & 7) == 0) red[lane >> 3][warp] = ws;
       __syncthreads();
       if (threadIdx.x < kDotVecs && i0 + threadIdx.x < ie) {
@@ -167,15 +186,32 @@ __global__ void __launch_bounds__(kDotThreads) k_sub_norm(const VT* __restrict__
   for (int i = threadIdx.x; i < nv && i <= kMaxRestart; i += blockDim.x) cs[i] = (VT)cb[i];
   __syncthreads();
   double sv[kDotVecs] = {0.0, 0.0, 0.0, 0.0};
+  // per element the products summed in index order; the thread's elements side by side, so that their
+  // loads of one basis vector are in flight together
+  VT t[kSubPer];
+#pragma unroll
+  for (int k = 0; k < kSubPer; ++k) t[k] = (VT)0;
+  if (sub) {
+    const VT* vb = V + (size_t)b * ld + e0 + threadIdx.x;
+    const int kmax = min(kSubPer, max(0, (n - e0 - (int)threadIdx.x + kDotThreads - 1) / kDotThreads));
+    if (kmax == kSubPer) {
+#pragma unroll 4
+      for (int i = 0; i < nv; ++i) {
+#pragma unroll
+        for (int k = 0; k < kSubPer; ++k) t[k] += vb[(size_t)i * vstride_i + k * kDotThreads] * cs[i];
+      }
+    } else {
+      for (int i = 0; i < nv; ++i)
+        for (int k = 0; k < kmax; ++k) t[k] += vb[(size_t)i * vstride_i + k * kDotThreads] * cs[i];
+    }
+  }
 #pragma unroll
   for (int k = 0; k < kSubPer; ++k) {
     const int e = e0 + threadIdx.x + k * kDotThreads;
     if (e < n) {
       double x = wb[e];
       if (sub) {
-        VT t = (VT)0;
-        for (int i = 0; i < nv; ++i) t += V[(size_t)i * vstride_i + (size_t)b * ld + e] * cs[i];
-        x -= (double)t;
+        x -= (double)t[k];
         wb[e] = x;
       }
       if (nrm) sv[0] = fma(x, x, sv[0]);
