@@ -902,7 +902,8 @@ static int check_plan(sdd_plan* p, int batch) {
 // their linear parts (FP64 in both precisions) and the chains' h kernel adds the nonlinear parts (same
 // roundings).
 // ev (nullable): four events recorded around the nonlinear term, the rhs and the chains.
-// The pending layout-3 correction of a state X (and its FP32 copy x32, nullable), for FixArgs.
+// The pending correction of layouts 3 / 11 (chunk set 1) of a state X (and its FP32 copy x32, nullable),
+// for FixArgs.
 static FixArgs fix_args(const sdd_plan* p, const double* X, const float* x32) {
   FixArgs f;
   std::memset(&f, 0, sizeof(f));
@@ -920,7 +921,7 @@ static FixArgs fix_args(const sdd_plan* p, const double* X, const float* x32) {
 
 // x32_in / x32_out (mixed time steps only): the FP32 copy of X the nonlinear term reads instead of
 // converting X, and the one the chains write beside out for the next step (nullable).  defer: leave a
-// layout-3 chain correction pending (sdd_step); fix_in: X carries the previous step's pending correction,
+// layout-3 / 11 chain correction pending (sdd_step); fix_in: X carries the previous step's pending correction,
 // applied by the nonlinear term's first kernel.  v32 (mixed plans, mode 1, nullable): an FP32 copy of X
 // (stride ldx), read by the FP32 nonlinear term instead of converting X (the same values); with v32_rhs
 // the right-hand sides and h = Linv g are then formed in FP32 as well (k_rhs32, k_mode_mv32), for Jacobian
@@ -1169,7 +1170,7 @@ int sdd_step(sdd_plan* p, int batch, const double* Ra, const double* Ras, const 
   // for the next step's nonlinear term (the caller's X_in has none)
   const double* cur = X_in;
   const float* cur32 = nullptr;
-  // layout 3 with the split nonlinear term: each step's chain correction is applied by the next step's
+  // layout 3 or 11 with the split nonlinear term: each step's chain correction is applied by the next step's
   // first kernel (one launch fewer per step); the last one runs on its own at the end
   const int dfix = step_defers_fix(p, batch, linear) ? 1 : 0;
   cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;

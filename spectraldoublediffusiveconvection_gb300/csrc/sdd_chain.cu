@@ -892,7 +892,7 @@ __device__ __forceinline__ void block_mv(const double* P, int ldm, const double*
 
 size_t carry_par_smem_bytes(int nr, int ldmA) { return (size_t)2 * nr * ldmA * sizeof(double); }
 
-// Parallel carry of the chunked chains (layout 3).  One CTA of 128 threads per (chain, shell, product
+// Parallel carry of the chunked chains (layouts 3 and 11).  One CTA of 128 threads per (chain, shell, product
 // (j, i)), i <= j - 2: part_{j,i} = P_{j,i} d_i, with P_{j,i} staged in shared memory by one round of
 // cp.async (every load in flight at once).  The corrections sum each row (carried_state):
 //   s_j = d_{j-1} + part_{j,0} + part_{j,1} + ... + part_{j,j-2},
@@ -929,7 +929,7 @@ __global__ void __launch_bounds__(128) k_carry_par(ChainArgs a) {
   }
 }
 
-// Element e of the carried state s_c (c >= 1) of chain `chain` under layout 3: d_{c-1} plus the row's
+// Element e of the carried state s_c (c >= 1) of chain `chain` under layouts 3 / 11: d_{c-1} plus the row's
 // products (k_carry_par), summed in index order.
 __device__ __forceinline__ double carried_state(const ChainArgs& a, int b, size_t chain, int c, int e) {
   const double* d = a.dbuf + (size_t)b * a.d_stride + chain * a.nch * a.ldd;
@@ -1313,7 +1313,7 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
 // carried-state recurrence and a parallel correction) is chosen automatically while all its CTAs fit
 // on the GPU at two per SM.  a.g holds the right-hand sides; a.h receives h = Linv g (k_mode_mv), which
 // is what the chains read.
-// The layout-3 correction f += G_jj s_c on its own (a correction left pending by the last step of a
+// The layout-3 / 11 correction f += G_jj s_c on its own (a correction left pending by the last step of a
 // sequence; a.f is the state, a.f32 its FP32 copy or null).
 cudaError_t launch_chunk_fix(const ChainArgs& a_in, int batch, int nfields, cudaStream_t s) {
   ChainArgs a = a_in;

@@ -174,7 +174,7 @@ struct RhsArgs {
   double* hist;
 };
 
-// A chunk correction of the state left pending by the previous time step (layout 3, sdd_step): the split
+// A chunk correction of the state left pending by the previous time step (layouts 3 / 11, sdd_step): the split
 // nonlinear term's k_fx_deriv applies X[jj] += G_jj s_c(jj) to its mode before using it, with the
 // arithmetic of k_mode_mv<TPR, true> (the same bits), and writes the corrected rows back (and their FP32
 // copy).  The previous step's chunk end states and carry products are still in dbuf / pbuf: this step's
@@ -303,16 +303,16 @@ struct ChainArgs {
   double* cbuf;              // [shell][3][2][nch][ldd] carried states at the chunk starts (c >= 1)
   size_t d_stride;           // doubles per shell in dbuf / cbuf
   int* counter;              // [shell][6] chunks finished per chain (the last one runs the carry), zeroed
-  // layout 3 (parallel carry): the chunks only write their end states; k_carry_par forms
+  // layouts 3 / 11 (parallel carry): the chunks only write their end states; k_carry_par forms
   // part_{j,i} = P_{j,i} d_i for every product in parallel and the corrections sum
   // s_j = d_{j-1} + sum_i part_{j,i} (index order)
-  int carry_seq;             // 1: the last-finishing chunk CTA runs the sequential carry (layout 2)
+  int carry_seq;             // 1: the last-finishing chunk CTA runs the sequential carry (layouts 2 / 10)
   int np;                    // products per chain
   const double* PA4, *PT, *PS;
   double* pbuf;              // [shell][6][np][ldd] products P_{j,i} d_i
   size_t p_stride;           // doubles per shell in pbuf
   ChunkSet cset[2];          // the chunkings of layouts 2 and 3 (launch_chain copies one into the fields above)
-  int defer_fix;             // layout 3: leave the correction to the next step's nonlinear term (FixArgs)
+  int defer_fix;             // layouts 3 / 11: leave the correction to the next step's nonlinear term (FixArgs)
   const int* active;         // nullable: per-shell flags; kernels skip shells whose flag is 0
   // nullable: FP32 right-hand sides (k_rhs32, stride g_stride): h = Linv g is then formed in FP32 with the
   // FP32 copies of the Linv blocks (k_mode_mv32) and stored in FP64 for the chains
