@@ -284,12 +284,14 @@ def test_prepass_three_chain_layout_in_steps_and_newton(cuda, N_r, N_fm, split):
         assert np.linalg.norm(O.PFX(ops1, Xm[b].cpu().numpy(), 7000.0 + 2000.0 * b / 3, 500.0, False)) <= 1.5e-10
 
 
-@pytest.mark.parametrize("layout", [8, 9])
+@pytest.mark.parametrize("layout", [8, 9, 10, 11])
 @pytest.mark.parametrize("N_r,N_fm", [(16, 16), (36, 384)])
 def test_three_chain_layouts_symmetric(cuda, N_r, N_fm, layout):
-    """Symmetric plans under layouts 8 and 9: in each (parity, shell) CTA one or two of the three chains are
-    inactive (their rows are zero) and leave at once while the others run on their own barriers; steps and
-    the Newton residual against the oracle's symmetric solves, a batch equal to its shells alone."""
+    """Symmetric plans under layouts 8 and 9 (in each (parity, shell) CTA one or two of the three chains are
+    inactive, their rows are zero, and leave at once while the others run on their own barriers) and under
+    the reference-order chunks of layouts 10 and 11 (inactive chains' chunks write zeros; with the split
+    nonlinear term the active chunks form their own right-hand sides, the same bits as the full form): steps
+    and the Newton residual against the oracle's symmetric solves, a batch equal to its shells alone."""
     from spectraldoublediffusiveconvection_gb300.plan import Plan
     torch = cuda
     nr = N_r - 1
@@ -300,6 +302,11 @@ def test_three_chain_layouts_symmetric(cuda, N_r, N_fm, layout):
     p.set_fx_split(1)
     Xt = torch.from_numpy(np.stack(Xs)).cuda()
     Y = p.step(Xt, 8000.0, 500.0, nsteps=2).cpu().numpy()
+    if layout >= 10:
+        p.set_fx_split(2)
+        assert p.chain_choice(3)[0] == layout
+        assert np.array_equal(p.step(Xt, 8000.0, 500.0, nsteps=2).cpu().numpy(), Y)
+        p.set_fx_split(1)
     for k, x in enumerate(Xs):
         r = x
         for _ in range(2):
