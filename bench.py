@@ -950,6 +950,32 @@ def profile_step_batch(precision, layout, batch=64, steps=1):
     return 0
 
 
+def profile_uneven_batch(precision):
+    """One launch (10 steps of every shape group) of the batched workload's captured graph (64 shells, N_r in
+    {20,24,30,36}, N_theta in {64,128,256,384}, the default per-group choices) inside an NVTX range
+    "uneven_batch", after two warm-up launches, for a kernel launch list of the batched time step:
+    ncu --nvtx --nvtx-include "uneven_batch/" ... python bench.py --profile-uneven-batch <precision>."""
+    import torch
+    from spectraldoublediffusiveconvection_gb300.batch import ShellBatch, config4_shells
+    device = torch.device("cuda", 0)
+    b = ShellBatch(config4_shells(64, seed=1234), d=2.0, dt=1e-3, Pr=1.0, Tau=0.01, Ra_s=500.0,
+                   precision=precision, device=device)
+    b.capture(10)
+    b.replay(2)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("uneven_batch")
+    e0.record()
+    b.replay(1)
+    e1.record()
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    groups = [(g.plan.N_r, g.plan.N_fm, len(g.idx), g.plan.chain_choice(len(g.idx))[0]) for g in b.groups]
+    print(json.dumps({"profile": "uneven_batch", "precision": precision, "ms_per_launch": e0.elapsed_time(e1),
+                      "groups_Nr_Ntheta_shells_layout": groups}))
+    return 0
+
+
 def probe_phase_boundaries():
     """The cost of a phase boundary inside a captured CUDA graph (a kernel boundary) against a grid-wide
     barrier inside one persistent cooperative kernel (sdd_probe_phase_boundaries): 64 phases over one CTA
@@ -997,6 +1023,7 @@ def main():
     ap.add_argument("--profile-newton-batch", nargs="?", type=int, const=2, default=None, metavar="MODE")
     ap.add_argument("--profile-deriv-tc", type=int, metavar="SHELLS")
     ap.add_argument("--profile-step-batch", nargs=2, metavar=("PRECISION", "LAYOUT"))
+    ap.add_argument("--profile-uneven-batch", metavar="PRECISION")
     ap.add_argument("--probe-phase-boundaries", action="store_true")
     args = ap.parse_args()
     if args.probe_phase_boundaries:
@@ -1007,6 +1034,8 @@ def main():
         return profile_deriv_tc(args.profile_deriv_tc)
     if args.profile_step_batch:
         return profile_step_batch(args.profile_step_batch[0], int(args.profile_step_batch[1]))
+    if args.profile_uneven_batch:
+        return profile_uneven_batch(args.profile_uneven_batch)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
