@@ -429,7 +429,7 @@ P99_BOUND_MS = 1000.0
 
 
 def bench_served(device, n_requests=1000, rate=200.0, seed=2024, frac_continue=0.7, con_workers=4, branch=None,
-                 sweep=(100.0, 150.0, 200.0, 250.0, 300.0, 400.0), sweep_requests=600, **server_kw):
+                 sweep=(100.0, 150.0, 200.0, 250.0, 275.0, 300.0, 400.0), sweep_requests=600, **server_kw):
     """The served mix at `rate` arrivals/s (the headline block), then an arrival-rate sweep on the same
     server: capacity = the highest swept rate whose p99 latency stays under P99_BOUND_MS over a run of
     `sweep_requests` requests (past saturation the queue, and with it p99, grows with the run), and the
