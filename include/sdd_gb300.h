@@ -176,6 +176,22 @@ int sdd_theta_op(sdd_plan* plan, int op, int batch, const double* g, double* f, 
  * linear != 0 drops the nonlinear term (Main.py:261-264). */
 int sdd_step(sdd_plan* plan, int batch, const double* Ra, const double* Ra_s, const double* X_in,
              double* X_out, int nsteps, int linear, void* stream);
+/* One group of a batched call: `batch` shells of one plan (device arrays as in sdd_step). */
+typedef struct sdd_batch_group {
+  sdd_plan* plan;
+  int32_t batch;
+  int32_t pad;
+  const double* Ra;
+  const double* Ra_s;
+  const double* X_in;
+  double* X_out;
+} sdd_batch_group;
+/* sdd_step for several plans at once (shells of different shapes, one plan per shape group; no counterpart
+ * in the reference, which steps one shell per process): every group runs on its plan's own branch stream,
+ * forked from and joined back into `stream` by events, so the groups run concurrently and the call is
+ * ordered on `stream` like one sdd_step.  Captured on `stream`, it becomes one graph with a branch per group.
+ * Each plan may appear once per call (SDD_ERR_ARG otherwise); a group's result equals its sdd_step alone. */
+int sdd_batch_step(const sdd_batch_group* groups, int ngroups, int nsteps, int linear, void* stream);
 /* One Crank-Nicolson / Adams-Bashforth-2 step (an opt-in scheme; the reference and sdd_step are IMEX Euler,
  * "CNAB1", Main.py:255-283).  The plan is built with HALF the step, dt_plan = dt/2 (its blocks invert
  * A^2 - (dt/2) Pr A^4 and r^2 - (dt/2) r^2 Lap, Matrix_Operators.py:1014-1112): composed of the reference's

@@ -67,6 +67,13 @@ class ContinResult(ctypes.Structure):
                 ("matvecs", ctypes.c_int32), ("converged", ctypes.c_int32)]
 
 
+class BatchGroup(ctypes.Structure):
+    """Mirror of ``sdd_batch_group``."""
+    _fields_ = [("plan", ctypes.c_void_p), ("batch", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("Ra", ctypes.c_void_p), ("Ra_s", ctypes.c_void_p), ("X_in", ctypes.c_void_p),
+                ("X_out", ctypes.c_void_p)]
+
+
 # (name, restype, argtypes) of every exported symbol; the CPU test checks the header declares these.
 _VP = ctypes.c_void_p
 _I = ctypes.c_int
@@ -96,6 +103,7 @@ SIGNATURES = [
     ("sdd_nab2_bsub", _I, [_VP, _I, _I, _VP, _VP, _VP]),
     ("sdd_theta_op", _I, [_VP, _I, _I, _VP, _VP, _VP]),
     ("sdd_step", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, _I, _VP]),
+    ("sdd_batch_step", _I, [ctypes.POINTER(BatchGroup), _I, _I, _I, _VP]),
     ("sdd_step_cnab2", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _I, _VP]),
     ("sdd_pfx", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP]),
     ("sdd_pdfx", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),

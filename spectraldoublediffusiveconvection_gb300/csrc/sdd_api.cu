@@ -185,6 +185,8 @@ struct sdd_plan {
   double* kv_vin;     // [B][ld] the Krylov vector the next product reads (a fixed address for its graph)
   unsigned long long graph_clock;
   cudaStream_t cap_stream;          // private capture stream (created on first use)
+  cudaStream_t branch_stream;       // sdd_batch_step: this plan's branch of a batched call (created on first use)
+  cudaEvent_t branch_ev[2];         // sdd_batch_step: the fork (recorded on the caller's stream) and the join
 };
 
 // Workspace allocations (sdd_plan_reserve and the Krylov workspace) go through ws_malloc, so that a test can
@@ -329,6 +331,9 @@ static void free_plan(sdd_plan* p) {
   if (!p) return;
   clear_step_graphs(p);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
+  if (p->branch_stream) cudaStreamDestroy(p->branch_stream);
+  for (cudaEvent_t e : p->branch_ev)
+    if (e) cudaEventDestroy(e);
   double* d[] = {p->Dr, p->D2r2, p->ir4r2, p->D2s, p->ir2s, p->D2A4, p->ir2A4, p->ir4A4, p->rsq, p->dT0,
                  p->gr, p->LinvA4, p->LinvT, p->LinvS, p->out4, p->rhs, p->xtmp, p->coefA4, p->coefT, p->coefS, p->ABA4, p->hbuf,
                  p->dbuf, p->cbuf, p->pbuf,
@@ -1202,6 +1207,51 @@ int sdd_step(sdd_plan* p, int batch, const double* Ra, const double* Ras, const 
   if (dfix && (st = finish_fix(p, batch, const_cast<double*>(cur), const_cast<float*>(cur32), s))) return st;
   if (cur != X_out) SDD_CUDA(cudaMemcpyAsync(X_out, cur, bytes, cudaMemcpyDeviceToDevice, s));
   return SDD_OK;
+}
+
+// Several plans' shells advanced in one call (the C form of a batch of uneven shells: one plan per shape
+// group): every group runs sdd_step on its plan's own branch stream, forked from and joined back into the
+// caller's stream by events, so the groups run concurrently and the call is stream-ordered like sdd_step.
+// On a stream that is being captured the fork and join become graph dependencies (one graph with a branch
+// per group).  A plan may appear once per call (its workspace serves one stream at a time).
+int sdd_batch_step(const sdd_batch_group* groups, int ngroups, int nsteps, int linear, void* stream) {
+  if (!groups || ngroups < 1 || nsteps < 0) return SDD_ERR_ARG;
+  for (int g = 0; g < ngroups; ++g) {
+    const sdd_batch_group& q = groups[g];
+    if (!q.plan || q.batch < 1 || !q.Ra || !q.Ra_s || !q.X_in || !q.X_out) return SDD_ERR_ARG;
+    for (int h = 0; h < g; ++h)
+      if (groups[h].plan == q.plan) return SDD_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  for (int g = 0; g < ngroups; ++g) {
+    sdd_plan* p = groups[g].plan;
+    if (!p->branch_stream) SDD_CUDA(cudaStreamCreateWithFlags(&p->branch_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : p->branch_ev)
+      if (!e) SDD_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  cudaEvent_t fork = groups[0].plan->branch_ev[0];
+  SDD_CUDA(cudaEventRecord(fork, s));
+  int st = SDD_OK;
+  for (int g = 0; g < ngroups && st == SDD_OK; ++g) {
+    const sdd_batch_group& q = groups[g];
+    cudaStream_t bs = q.plan->branch_stream;
+    cudaError_t e = cudaStreamWaitEvent(bs, fork, 0);
+    if (e != cudaSuccess) {
+      set_cuda_error(e);
+      st = SDD_ERR_CUDA;
+      break;
+    }
+    st = sdd_step(q.plan, q.batch, q.Ra, q.Ra_s, q.X_in, q.X_out, nsteps, linear, bs);
+    // the join is recorded whatever the step returned, so that the caller's stream (and a capture on it)
+    // never ends with a branch left open
+    e = cudaEventRecord(q.plan->branch_ev[1], bs);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, q.plan->branch_ev[1], 0);
+    if (e != cudaSuccess && st == SDD_OK) {
+      set_cuda_error(e);
+      st = SDD_ERR_CUDA;
+    }
+  }
+  return st;
 }
 
 // Crank-Nicolson / Adams-Bashforth 2 step (no counterpart in the reference, which steps IMEX Euler): the plan

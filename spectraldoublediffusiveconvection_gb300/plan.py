@@ -384,6 +384,34 @@ class Plan:
                          converged=bool(r.converged)) for r in res]
 
 
+def batch_step(groups, nsteps=1, linear=False):
+    """Advance several plans' shells at once (sdd_batch_step): ``groups`` is a list of (plan, X, Ra, Ra_s) or
+    (plan, X, Ra, Ra_s, out) with X a (shells x n_state) device tensor of that plan, one entry per distinct
+    plan, all on one device.  Every group runs sdd_step on its plan's own branch stream, forked from and joined
+    back into the current stream, so the groups run concurrently; each group's result equals its
+    ``plan.step`` alone.  Returns the output tensors in the order of ``groups``."""
+    torch = _torch()
+    if not groups:
+        raise ValueError("batch_step: no groups")
+    dev = groups[0][0].device
+    arr = (_lib.BatchGroup * len(groups))()
+    outs, keep = [], []
+    for k, g in enumerate(groups):
+        plan, X, Ra, Ra_s = g[:4]
+        if plan.device != dev:
+            raise ValueError("batch_step: every plan must be on one device")
+        B = plan._chk(X, plan.n_state, "X")
+        out = g[4] if len(g) > 4 and g[4] is not None else torch.empty_like(X)
+        plan._chk(out, plan.n_state, "out")
+        ra, ras = plan._vec(Ra, B), plan._vec(Ra_s, B)
+        keep += [ra, ras]
+        arr[k] = _lib.BatchGroup(plan._h.value, B, 0, ra.data_ptr(), ras.data_ptr(), X.data_ptr(), out.data_ptr())
+        outs.append(out)
+    L = groups[0][0]._L
+    _lib.check(L.sdd_batch_step(arr, len(groups), int(nsteps), int(bool(linear)), _stream(dev)), "sdd_batch_step")
+    return outs
+
+
 _cache = {}
 _cache_lock = threading.Lock()
 

@@ -39,6 +39,10 @@ def test_argument_errors_need_no_gpu(built_lib):
     h = ctypes.c_void_p()
     assert lib.sdd_plan_create(ctypes.byref(d), ctypes.byref(h)) == _lib.SDD_ERR_ODD_NFM
     assert lib.sdd_step(None, 1, None, None, None, None, 1, 0, None) == _lib.SDD_ERR_ARG
+    assert lib.sdd_batch_step(None, 1, 1, 0, None) == _lib.SDD_ERR_ARG
+    g = (_lib.BatchGroup * 1)()
+    assert lib.sdd_batch_step(g, 1, 1, 0, None) == _lib.SDD_ERR_ARG      # no plan
+    assert lib.sdd_batch_step(g, 0, 1, 0, None) == _lib.SDD_ERR_ARG
 
 
 def test_struct_layouts_match_header(tmp_path):
@@ -53,7 +57,7 @@ def test_struct_layouts_match_header(tmp_path):
         pytest.skip("no C compiler")
     mirrors = {"sdd_plan_desc": _lib.PlanDesc, "sdd_newton_opts": _lib.NewtonOpts,
                "sdd_newton_result": _lib.NewtonResult, "sdd_contin_opts": _lib.ContinOpts,
-               "sdd_contin_result": _lib.ContinResult}
+               "sdd_contin_result": _lib.ContinResult, "sdd_batch_group": _lib.BatchGroup}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "sdd_gb300.h"', "int main(void) {"]
     for cname, cls in mirrors.items():
         lines.append('  printf("%s sizeof %%zu\\n", sizeof(%s));' % (cname, cname))
