@@ -66,7 +66,7 @@ def test_served_results_equal_alone(cuda, branch):
             p.set_chain_layout(srv.chain_layout)
             X = torch.from_numpy(np.asarray(r.X).copy()).cuda().reshape(1, -1)
             Ra = torch.tensor([r.Ra], dtype=torch.float64, device="cuda")
-            Xd, res = p.contin_step(X, Ra, RAS, r.sign, r.ds, tol=1e-10, restart=50, mixed_matvec=True,
+            Xd, res = p.contin_step(X, Ra, RAS, r.sign, r.ds, tol=1e-10, restart=50, mixed_matvec=srv.con_mixed,
                                     tangent_rtol=srv.tangent_rtol)
             assert res[0]["converged"] and r.result["converged"]
             assert np.array_equal(X.cpu().numpy().ravel(), r.result["X"]), r.id
