@@ -408,7 +408,11 @@ def _served_stats(srv, reqs, wall, rate, st0):
     ok_con = [r for r in con if r.error is None and r.result["converged"] and r.result["residual"] <= 1e-10]
     ok_int = [r for r in itg if r.error is None and np.isfinite(r.result["X"]).all()]
     lat = serve.latency_report(reqs)
-    return {"offered_rate_per_s": rate, "requests": len(reqs), "wall_s": wall,
+    # FP64 work done: the integrations' IMEX steps (mixed form: the linear part and the chains in FP64) and
+    # the continuation solves' Jacobian products (the FP64 chains, 8 M nr^2 per product and shell)
+    f64 = sum(r.n_steps * split_flops(r.N_theta, r.N_r - 1, "mixed")[0] for r in ok_int)
+    f64 += sum(r.result["matvecs"] * 8 * r.N_theta * (r.N_r - 1) ** 2 for r in ok_con)
+    return {"offered_rate_per_s": rate, "requests": len(reqs), "wall_s": wall, "fp64_flops": f64,
             "continuation_solves_per_s": len(ok_con) / wall,
             "integration_steps_per_s": sum(r.n_steps for r in ok_int) / wall,
             "integration_requests_per_s": len(ok_int) / wall,
@@ -429,7 +433,8 @@ P99_BOUND_MS = 1000.0
 
 
 def bench_served(device, n_requests=1000, rate=200.0, seed=2024, frac_continue=0.7, con_workers=4, branch=None,
-                 sweep=(100.0, 150.0, 200.0, 250.0, 275.0, 300.0, 400.0), sweep_requests=600, **server_kw):
+                 sweep=(100.0, 150.0, 200.0, 250.0, 275.0, 300.0, 400.0), sweep_requests=600, fp64_peak=None,
+                 **server_kw):
     """The served mix at `rate` arrivals/s (the headline block), then an arrival-rate sweep on the same
     server: capacity = the highest swept rate whose p99 latency stays under P99_BOUND_MS over a run of
     `sweep_requests` requests (past saturation the queue, and with it p99, grows with the run), and the
@@ -517,7 +522,14 @@ def bench_served(device, n_requests=1000, rate=200.0, seed=2024, frac_continue=0
     plain_mix = 1.0 / (frac_continue / plain_rate + (1.0 - frac_continue) * t_int)
     ok = [c for c in curve if c["p99_ms"] is not None and c["p99_ms"] <= P99_BOUND_MS]
     cap = max(ok, key=lambda c: c["offered_rate_per_s"]) if ok else None
+    def roof(run):
+        a = run["fp64_flops"] / run["wall_s"] / 1e12
+        return {"bound": "fp64", "achieved": a, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": a / fp64_peak if fp64_peak else None,
+                "note": "FP64 flops of the integrations' steps (linear part and chains of the mixed form) and of "
+                        "the continuation products' chains (8 M nr^2 per product), over the run's wall time"}
     main.update({
+        "roofline": roof(main), "capacity_roofline": roof(cap) if cap else None,
         "capacity_solves_per_s": cap["continuation_solves_per_s"] if cap else None,
         "capacity_offered_rate_per_s": cap["offered_rate_per_s"] if cap else None,
         "capacity_p50_ms": cap["p50_ms"] if cap else None, "capacity_p99_ms": cap["p99_ms"] if cap else None,
@@ -823,7 +835,7 @@ def bench_gb300(args):
 
     served = None
     if rank == 0 and not args.no_served:
-        served = bench_served(device, n_requests=args.served_requests)
+        served = bench_served(device, n_requests=args.served_requests, fp64_peak=fp64_peak_tf)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
