@@ -89,7 +89,10 @@ typedef struct sdd_plan_desc {
 
 typedef struct sdd_plan sdd_plan;
 
-/* Uploads the operators to the current device.  Replaces Main.py:179-225 (the returned tuple). */
+/* Uploads the operators to the current device.  Replaces Main.py:179-225 (the returned tuple).  Sizes:
+ * nr <= 64 (N_r <= 65); N_fm even, with P = 3 N_fm / 2 a product of the radices 2, 3, 4, 5, 7 and the fused
+ * FP64 row kernel's 34 P doubles beside its static shared memory within a CTA's limit (N_fm <= 540 on
+ * GB300); otherwise SDD_ERR_UNSUPPORTED before anything is allocated (odd N_fm: SDD_ERR_ODD_NFM). */
 int sdd_plan_create(const sdd_plan_desc* desc, sdd_plan** plan);
 int sdd_plan_destroy(sdd_plan* plan);
 /* Pre-allocates the plan's workspace for up to max_batch shells (otherwise grown on first use). */

@@ -573,11 +573,10 @@ int sdd_plan_create(const sdd_plan_desc* d, sdd_plan** out) {
   const int M = d->N_fm, nr = d->nr, P = (3 * M) / 2;
   int dev = 0;
   SDD_CUDA(cudaGetDevice(&dev));
-  int smem_optin = 0;
-  SDD_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  if (fx_smem_bytes(M, P, d->precision) > (size_t)smem_optin) return SDD_ERR_UNSUPPORTED;
-  // the FP64 nonlinear term is also needed by the mixed plan's Newton residual
-  if (fx_smem_bytes(M, P, SDD_PREC_FP64) > (size_t)smem_optin) return SDD_ERR_UNSUPPORTED;
+  // the fused row kernel's dynamic shared memory within what the device leaves beside its static part; the
+  // FP64 kernel is also needed by the mixed plan's Newton residual
+  if (fx_smem_bytes(M, P, d->precision) > fx_rows_max_dynamic_smem(d->precision)) return SDD_ERR_UNSUPPORTED;
+  if (fx_smem_bytes(M, P, SDD_PREC_FP64) > fx_rows_max_dynamic_smem(SDD_PREC_FP64)) return SDD_ERR_UNSUPPORTED;
   const FftPlan* fp = get_fft_plan(P);
   if (!fp) return SDD_ERR_UNSUPPORTED;
   sdd_plan* p = new sdd_plan();

@@ -1328,11 +1328,11 @@ cudaError_t launch_chunk_fix(const ChainArgs& a_in, int batch, int nfields, cuda
 
 int resolve_chain_layout(const ChainArgs& a, int batch, int nfields) {
   const int sms = sm_count();
-  static const int optin = [] {
+  static const int optin = [] {   // less a margin for the chain kernels' static shared memory (a few words)
     int dev = 0, n = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&n, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    return n;
+    return n - 256;
   }();
   int layout = a.layout;
   const ChunkSet& c2 = a.cset[0];

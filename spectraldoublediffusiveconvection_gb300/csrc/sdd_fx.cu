@@ -1264,6 +1264,33 @@ static cudaError_t launch_tc_for(const FxArgs& a, int batch, cudaStream_t s) {
   return launch_deriv_tc(t, s);
 }
 
+// The most dynamic shared memory a k_fx_rows launch of precision prec can take: the opt-in limit less the
+// kernel's static shared memory (the parity scans' chunk totals), over its three modes.
+size_t fx_rows_max_dynamic_smem(int prec) {
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  size_t stat = 0;
+  auto take = [&](const void* f) {
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, f) == cudaSuccess) stat = fa.sharedSizeBytes > stat ? fa.sharedSizeBytes : stat;
+    else cudaGetLastError();
+  };
+  if (prec == SDD_PREC_MIXED) {
+    take(reinterpret_cast<const void*>(k_fx_rows<float, 0>));
+    take(reinterpret_cast<const void*>(k_fx_rows<float, 1>));
+    take(reinterpret_cast<const void*>(k_fx_rows<float, 2>));
+  } else {
+    take(reinterpret_cast<const void*>(k_fx_rows<double, 0>));
+    take(reinterpret_cast<const void*>(k_fx_rows<double, 1>));
+    take(reinterpret_cast<const void*>(k_fx_rows<double, 2>));
+  }
+  return (size_t)optin > stat ? (size_t)optin - stat : 0;
+}
+
 template <typename T, int MODE>
 static cudaError_t launch_fx_t(const FxArgs& a, int batch, cudaStream_t s) {
   const size_t smem = fx_smem_bytes(a.M, a.P, sizeof(T) == 4 ? SDD_PREC_MIXED : SDD_PREC_FP64);

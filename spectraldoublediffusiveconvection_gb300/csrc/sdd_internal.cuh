@@ -348,6 +348,8 @@ size_t tc_smem_bytes(int KP, int NP);
 void build_tc_operator(const double* Dr, const double* D2r2, int nr, int KP, int NP, float* out);
 // whether launch_fx takes the split path for these arguments
 bool fx_uses_split(const FxArgs& a, int batch, int mode);
+// the largest dynamic shared memory a k_fx_rows launch of this precision can take on the current device
+size_t fx_rows_max_dynamic_smem(int prec);
 // the split-or-fused rule alone (split: 0 automatic, 1 fused, 2 split), for a plan whose scratch is not yet
 // reserved
 bool fx_split_rule(int split, int nr, int batch);

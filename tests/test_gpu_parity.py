@@ -277,3 +277,32 @@ def test_main_diagnostics_dropins_match_reference(cuda, tag):
     # a seeded (non-steady) temperature field has different fluxes at the two walls
     with pytest.raises(ValueError):
         Main.Nusselt(X[N:2 * N] * 1e3, d, R, D, N_fm, nr, check=True)
+
+
+def test_largest_supported_shape_and_the_limits(cuda):
+    """The largest shape a plan accepts on GB300 (N_r = 65: nr = 64 interior points; N_theta = 540: P = 810 =
+    2 3^4 5, the largest transform length of the FFT radices whose fused FP64 row kernel, 34 P doubles and its
+    static words, fits one CTA's shared memory): the nonlinear term and two steps of a batch of two against
+    the oracle, with the automatic kernel choices; one radial point more, or N_theta = 560 (P = 840 factors,
+    but its row kernel would pass the shared-memory limit by its static words), are refused with
+    SDD_ERR_UNSUPPORTED before anything is allocated."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    from spectraldoublediffusiveconvection_gb300 import _lib
+    torch = cuda
+    N_r, N_fm = 65, 540
+    d, dt, Pr, Tau, Ra, Ra_s = 2.0, 5e-4, 1.0, 0.01, 8000.0, 500.0
+    nr = N_r - 1
+    ops = O.Operators(N_fm, N_r, d, dt, Pr, Tau)
+    Xs = [O.seeded_state(N_fm, nr, 1234 + s) for s in range(2)]
+    p = Plan(N_fm, N_r, d, dt, Pr, Tau)
+    Xt = torch.from_numpy(np.stack(Xs)).cuda()
+    F = p.nlin_fx(Xt).cpu().numpy()
+    Y = p.step(Xt, Ra, Ra_s, nsteps=2).cpu().numpy()
+    for k, X in enumerate(Xs):
+        assert rel(F[k], O.NLIN_FX(X, ops.D, ops.R, N_fm, nr, False)) < 1e-12
+        r = O.step(ops, O.step(ops, X, Ra, Ra_s, False), Ra, Ra_s, False)
+        assert rel(Y[k], r) < 1e-12
+    for shape in [(N_fm, N_r + 1), (560, N_r)]:
+        with pytest.raises(_lib.SDDError) as e:
+            Plan(shape[0], shape[1], d, dt, Pr, Tau)
+        assert e.value.status == _lib.SDD_ERR_UNSUPPORTED
