@@ -14,7 +14,8 @@ from oracle import sdd_oracle as O
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(16, 16, False), (20, 64, False), (30, 256, False), (48, 512, False), (36, 384, True), (12, 10, True)]
+SHAPES = [(16, 16, False), (20, 64, False), (30, 256, False), (48, 512, False), (36, 384, True), (12, 10, True),
+          (3, 2, False), (2, 4, False)]
 
 
 @pytest.mark.parametrize("N_r,N_fm,sym", SHAPES)

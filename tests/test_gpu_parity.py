@@ -306,3 +306,34 @@ def test_largest_supported_shape_and_the_limits(cuda):
         with pytest.raises(_lib.SDDError) as e:
             Plan(shape[0], shape[1], d, dt, Pr, Tau)
         assert e.value.status == _lib.SDD_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("N_r,N_fm", [(3, 2), (2, 4), (5, 6)])
+def test_smallest_shapes_against_oracle(cuda, N_r, N_fm, precision):
+    """The smallest shapes (one or two interior radial points, two to six modes: one chain step per parity,
+    transforms of length 3 to 9, tensor-core tiles padded from K = 1): the nonlinear term and three steps of
+    a batch of two against the oracle (FP64 1e-12; mixed at FP32 level)."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    nr = N_r - 1
+    d, dt, Pr, Tau, Ra, Ra_s = 2.0, 1e-3, 1.0, 0.01, 8000.0, 500.0
+    ops = O.Operators(N_fm, N_r, d, dt, Pr, Tau)
+    Xs = [O.seeded_state(N_fm, nr, 70 + s) for s in range(2)]
+    p = Plan(N_fm, N_r, d, dt, Pr, Tau, precision=precision)
+    Xt = torch.from_numpy(np.stack(Xs)).cuda()
+    Y = p.step(Xt, Ra, Ra_s, nsteps=3).cpu().numpy()
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    for k, X in enumerate(Xs):
+        r = X
+        for _ in range(3):
+            r = O.step(ops, r, Ra, Ra_s, False)
+        assert rel(Y[k], r) < tol, (k, rel(Y[k], r))
+    if precision == "fp64":
+        F = p.nlin_fx(Xt).cpu().numpy()
+        for k, X in enumerate(Xs):
+            ref = O.NLIN_FX(X, ops.D, ops.R, N_fm, nr, False)
+            if np.linalg.norm(ref) > 0:
+                assert rel(F[k], ref) < 1e-12
+            else:
+                assert np.abs(F[k]).max() < 1e-18
