@@ -174,3 +174,22 @@ def test_fp32_basis_continuation_step(cuda):
         out.append((X.cpu().numpy().ravel(), float(Ra[0])))
     assert abs(out[1][1] - out[0][1]) <= 1e-8 * abs(out[0][1])
     assert rel(out[1][0], out[0][0]) <= 1e-7
+
+
+def test_mixed_plan_at_the_largest_shape(cuda):
+    """Mixed precision at the largest accepted shape (N_r = 65, N_theta = 540: tensor-core tiles with K = N =
+    64, the widest accumulator): two steps against the FP64 plan at FP32 level, and Newton with the FP32
+    basis (mixed_matvec=3) reaching the FP64 residual 1e-10."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    N_r, N_fm = 65, 540
+    X = torch.from_numpy(O.seeded_state(N_fm, N_r - 1, 4)).cuda().reshape(1, -1)
+    pm = Plan(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01, precision="mixed")
+    pd = Plan(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01)
+    e = rel(pm.step(X, 8000.0, 500.0, nsteps=2).cpu().numpy(), pd.step(X, 8000.0, 500.0, nsteps=2).cpu().numpy())
+    assert e < 1e-6, e
+    assert not pm.tensor_core_timed_out()
+    pn = Plan(N_fm, N_r, 2.0, 1.0, 1.0, 0.01, precision="mixed")
+    Xn = X.clone()
+    r = pn.newton(Xn, 8000.0, 500.0, tol=1e-10, mixed_matvec=3)[0]
+    assert r["converged"] and r["residual"] <= 1e-10, r
