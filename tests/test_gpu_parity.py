@@ -337,3 +337,33 @@ def test_smallest_shapes_against_oracle(cuda, N_r, N_fm, precision):
                 assert rel(F[k], ref) < 1e-12
             else:
                 assert np.abs(F[k]).max() < 1e-18
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_large_batch_equals_its_shells_alone(cuda, precision):
+    """700 shells of one plan in one call (the batched kernels' grids over 700 shells): a sample of shells
+    equals the same shells stepped alone bit for bit under one set of kernel choices (the automatic ones
+    differ between 700 shells and one, and different chain layouts round differently), and one of them
+    matches the oracle under the automatic choices."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    torch = cuda
+    N_fm, N_r, B = 64, 20, 700
+    nr = N_r - 1
+    p = Plan(N_fm, N_r, 2.0, 1e-3, 1.0, 0.01, precision=precision)
+    Xs = np.stack([O.seeded_state(N_fm, nr, 5000 + s) for s in range(B)])
+    Ra = torch.linspace(6000.0, 12000.0, B, dtype=torch.float64, device="cuda")
+    if precision == "fp64":
+        ops = O.Operators(N_fm, N_r, 2.0, 1e-3, 1.0, 0.01)
+        Ya = p.step(torch.from_numpy(Xs).cuda(), Ra, 500.0, nsteps=3)
+        for i in (0, 699):
+            r = Xs[i]
+            for _ in range(3):
+                r = O.step(ops, r, float(Ra[i]), 500.0, False)
+            assert rel(Ya[i].cpu().numpy(), r) < 1e-12
+    p.set_chain_layout(8)
+    p.set_fx_split(1)
+    Y = p.step(torch.from_numpy(Xs).cuda(), Ra, 500.0, nsteps=3)
+    assert p.chain_choice(B)[0] == 8 and p.chain_choice(1)[0] == 8
+    for i in (0, 1, 351, 699):
+        Yi = p.step(torch.from_numpy(Xs[i:i + 1]).cuda(), Ra[i:i + 1].clone(), 500.0, nsteps=3)
+        assert torch.equal(Y[i:i + 1], Yi), i
