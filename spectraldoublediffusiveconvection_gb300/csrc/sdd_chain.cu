@@ -66,16 +66,6 @@ __device__ __forceinline__ double group_sum(double v) {
   return v;
 }
 
-// y_i = sum_c AT[c*ld + i] x[c] over the columns c = q (mod TPR) of the lane, then summed over the group.
-// One accumulator: a dependent DFMA costs an SMSP the same 64 cycles as an independent one, so a second
-// accumulator would only add a DADD.
-template <int TPR>
-__device__ __forceinline__ double col_dot(const double* AT, int ld, const double* x, int nr, int i, int q) {
-  double s0 = 0.0;
-  for (int c = q; c < nr; c += TPR) s0 = fma(AT[c * ld + i], x[c], s0);
-  return group_sum<TPR>(s0);
-}
-
 __device__ __forceinline__ void chain_sync() {
   if (blockDim.x <= 32) __syncwarp();
   else __syncthreads();
