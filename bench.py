@@ -304,13 +304,13 @@ def bench_batched(device, precision, steps=1000, steps_per_launch=10, n_shells=6
             "fp32_tflops": f32 / sec / 1e12,
             "note": "algorithmic FP64 flops of all shells (the implicit solves, A2_SINE and the pointwise linear "
                     "terms; in plain FP64 also the nonlinear term) over the measured FP64 FMA peak"}
-    tune = {k: [v["chain_layout"], v["fx_split"]] for k, v in tuning.items() if isinstance(v, dict)
+    tune = {k: [v["chain_layout"], v["fx_split"], v.get("chunk_length")] for k, v in tuning.items() if isinstance(v, dict)
             and "chain_layout" in v}
     return {"shell_steps_per_s": shell_steps / sec, "seconds": sec, "shells": n_shells,
             "steps_per_shell": nsteps, "precision": precision, "roofline": roof,
             "graph": f"{launches} launches of one CUDA graph, {steps_per_launch} steps of all groups each",
             "groups": [f"N_r={a} N_theta={c} x{n}" for a, c, n in groups],
-            "tuning_chain_layout_fx_split": tune, "finite": finite}
+            "tuning_chain_layout_fx_split_chunk_lengths": tune, "finite": finite}
 
 
 def bench_batched_plain_alone(device, steps=100):

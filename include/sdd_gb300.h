@@ -119,6 +119,12 @@ int sdd_plan_reserve(sdd_plan* plan, int max_batch);
  * full FP64 right-hand side is there, and as 2 / 3 where it is fused (one shell: the pre-pass form is
  * faster there).  Set by the batch autotuner; no counterpart in the reference. */
 int sdd_plan_set_chain_layout(sdd_plan* plan, int layout);
+/* Chunk length (steps per chunk) of chunk set 0 (layouts 2 / 10, sequential carry) or 1 (layouts 3 / 11,
+ * parallel carry): the set's tables are rebuilt for kc and the carry workspace regrown; kc = 0 restores the
+ * plan's rule (round(sqrt(2 S)) / round(sqrt(S / 2)) steps, S = N_fm / 2).  2 <= kc <= S, at most 64 chunks
+ * (32 for set 1, whose products grow as the square); otherwise SDD_ERR_ARG.  Synchronises the device.  Set
+ * by the batch autotuner; no counterpart in the reference. */
+int sdd_plan_set_chunk_length(sdd_plan* plan, int set, int kc);
 /* The layout (1-11) a step of `batch` shells runs under the current setting, with its chunk length and
  * chunks per chain (0 and 1 when not chunked). */
 int sdd_plan_chain_choice(const sdd_plan* plan, int batch, int* layout, int* kc, int* nch);

@@ -104,6 +104,7 @@ SIGNATURES = [
     ("sdd_theta_op", _I, [_VP, _I, _I, _VP, _VP, _VP]),
     ("sdd_step", _I, [_VP, _I, _VP, _VP, _VP, _VP, _I, _I, _VP]),
     ("sdd_batch_step", _I, [ctypes.POINTER(BatchGroup), _I, _I, _I, _VP]),
+    ("sdd_plan_set_chunk_length", _I, [_VP, _I, _I]),
     ("sdd_step_cnab2", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _I, _VP]),
     ("sdd_pfx", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP]),
     ("sdd_pdfx", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),

@@ -109,6 +109,9 @@ class ShellBatch:
             if c:
                 g.plan.set_chain_layout(int(c["chain_layout"]))
                 g.plan.set_fx_split(int(c["fx_split"]))
+                for cset, kc in enumerate(c.get("chunk_length", (0, 0))):
+                    if g.plan.chunk_length[cset] != int(kc):
+                        g.plan.set_chunk_length(cset, int(kc))
                 self.tuning["N_r=%d,N_theta=%d" % g.shape] = dict(c)
         self.graph = None
 
@@ -170,15 +173,17 @@ class ShellBatch:
             best = min(best, e0.elapsed_time(e1) * 1e-3 / reps)
         return best
 
-    def autotune(self, steps_per_launch=5, reps=3, layouts=(1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11), fx_modes=(1, 2), min_gain=0.015):
+    def autotune(self, steps_per_launch=5, reps=3, layouts=(1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11), fx_modes=(1, 2),
+                 chunk_scales=(0.6, 1.6), min_gain=0.015):
         """Greedy per-group choice of the chain layout, then of the nonlinear-term kernel (fused or split),
+        then, for a group whose chains run chunked, of the chunk length (the rule's times chunk_scales),
         minimising the time of one graph launch; a change is kept only if it gains more than min_gain (the
         groups share the GPU, so single timings are noisy), and the starting choices are kept when the
         tuned ones do not beat them on a final re-measurement.  The shells' states are restored
         afterwards: tuning does not advance them."""
         saved = [g.X.clone() for g in self.groups]
         self.steps_per_launch = steps_per_launch
-        start = [(g.plan.chain_layout, g.plan.fx_split) for g in self.groups]
+        start = [(g.plan.chain_layout, g.plan.fx_split, list(g.plan.chunk_length)) for g in self.groups]
         t_start = best = self._time_graph(reps)
         for g in self.groups:
             choice = g.plan.chain_layout
@@ -199,14 +204,34 @@ class ShellBatch:
                 if t < best * (1.0 - min_gain):
                     best, fx_choice = t, fx
             g.plan.set_fx_split(fx_choice)
+            lay, kc0, _ = g.plan.chain_choice(len(g.idx))
+            if lay in (2, 3, 10, 11) and chunk_scales:
+                cset = 1 if lay in (3, 11) else 0
+                kc_choice = g.plan.chunk_length[cset]
+                for sc in chunk_scales:
+                    kc = max(2, int(round(kc0 * sc)))
+                    if kc == kc0:
+                        continue
+                    try:
+                        g.plan.set_chunk_length(cset, kc)
+                    except Exception:            # noqa: BLE001 - outside the allowed chunk counts
+                        continue
+                    t = self._time_graph(reps)
+                    if t < best * (1.0 - min_gain):
+                        best, kc_choice = t, kc
+                g.plan.set_chunk_length(cset, kc_choice)
         t_tuned = self._time_graph(reps)
         if t_tuned > t_start:
-            for g, (lay, fx) in zip(self.groups, start):
+            for g, (lay, fx, kcs) in zip(self.groups, start):
                 g.plan.set_chain_layout(lay)
                 g.plan.set_fx_split(fx)
+                for cset, kc in enumerate(kcs):
+                    if g.plan.chunk_length[cset] != kc:
+                        g.plan.set_chunk_length(cset, kc)
         for g in self.groups:
             self.tuning["N_r=%d,N_theta=%d" % g.shape] = {"chain_layout": g.plan.chain_layout,
-                                                          "fx_split": g.plan.fx_split}
+                                                          "fx_split": g.plan.fx_split,
+                                                          "chunk_length": list(g.plan.chunk_length)}
         for g, x in zip(self.groups, saved):
             g.X.copy_(x)
         self.capture(steps_per_launch)

@@ -132,6 +132,9 @@ struct sdd_plan {
   // carry); leading dimensions; workspaces sized for the larger chunk and product counts
   ChunkSet cs[2];
   int ldmA, ldmT, ldd, nch_alloc, np_alloc;
+  // host copies of what the chunk tables are built from, for sdd_plan_set_chunk_length: the psi step
+  // matrices [A B] (M x 2nr x ldl), Linv_T, Linv_S (M nr nr), the per-step scalars (4 M each)
+  double *h_AB, *h_LinvT, *h_LinvS, *h_cA, *h_cT, *h_cS;
   double *dbuf, *cbuf;              // [B][3][2][nch_alloc][ldd] chunk end states / carried states
   int* dcnt;                        // [B][6] chunk counters of the sequential carry
   double* pbuf;                     // [B][6][np_alloc][ldd] products of the parallel carry
@@ -327,8 +330,16 @@ static void clear_step_graphs(sdd_plan* p) {
   clear_mv_graphs(p);
 }
 
+static void free_chunk_set(ChunkSet& c) {
+  const double* t[] = {c.GA4, c.GT, c.GS, c.PhiA4, c.PhiT, c.PhiS, c.PA4, c.PT, c.PS};
+  for (const double* x : t) cudaFree(const_cast<double*>(x));
+  c = ChunkSet{};
+}
+
 static void free_plan(sdd_plan* p) {
   if (!p) return;
+  delete[] p->h_AB; delete[] p->h_LinvT; delete[] p->h_LinvS;
+  delete[] p->h_cA; delete[] p->h_cT; delete[] p->h_cS;
   clear_step_graphs(p);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   if (p->branch_stream) cudaStreamDestroy(p->branch_stream);
@@ -339,10 +350,7 @@ static void free_plan(sdd_plan* p) {
                  p->dbuf, p->cbuf, p->pbuf,
                  p->dg_ir, p->dg_tw, p->dg_wr, p->dg_nuw, p->dg_part, p->dg_out};
   for (double* x : d) cudaFree(x);
-  for (ChunkSet& c : p->cs) {
-    const double* t[] = {c.GA4, c.GT, c.GS, c.PhiA4, c.PhiT, c.PhiS, c.PA4, c.PT, c.PS};
-    for (const double* x : t) cudaFree(const_cast<double*>(x));
-  }
+  for (ChunkSet& c : p->cs) free_chunk_set(c);
   cudaFree(p->Dr32); cudaFree(p->D2r232); cudaFree(p->ir4r232); cudaFree(p->D2s32);
   cudaFree(p->tcB); cudaFree(p->tc_err);
   for (float* x : p->Linv32) cudaFree(x);
@@ -609,7 +617,6 @@ int sdd_plan_create(const sdd_plan_desc* d, sdd_plan** out) {
     free_plan(p);
     return st;
   }
-  (void)nm;
   if (p->prec == SDD_PREC_MIXED) {   // 3xTF32 operator tiles of the tensor-core contractions
     p->tcKP = p->tcNP = (nr + 7) / 8 * 8;
     std::vector<float> tb((size_t)2 * 2 * p->tcNP * p->tcKP);
@@ -678,6 +685,17 @@ int sdd_plan_create(const sdd_plan_desc* d, sdd_plan** out) {
       free_plan(p);
       return st;
     }
+    auto keep = [](const double* src, size_t n) {
+      double* h = new double[n];
+      std::memcpy(h, src, n * sizeof(double));
+      return h;
+    };
+    p->h_AB = keep(AB.data(), AB.size());
+    p->h_LinvT = keep(d->Linv_T, nm);
+    p->h_LinvS = keep(d->Linv_S, nm);
+    p->h_cA = keep(cA.data(), cA.size());
+    p->h_cT = keep(cT.data(), cT.size());
+    p->h_cS = keep(cS.data(), cS.size());
   }
   *out = p;
   return SDD_OK;
@@ -686,6 +704,38 @@ int sdd_plan_create(const sdd_plan_desc* d, sdd_plan** out) {
 int sdd_plan_destroy(sdd_plan* p) {
   if (!p) return SDD_ERR_ARG;
   free_plan(p);
+  return SDD_OK;
+}
+
+// Chunk length of chunk set `set` (0: the sequential-carry chunks of layouts 2 / 10, 1: the parallel-carry
+// chunks of layouts 3 / 11): the set's tables are rebuilt on the host from the plan's copies and uploaded; the
+// carry workspace follows on the next step (sdd_plan_reserve).  kc = 0 restores the plan's rule.
+int sdd_plan_set_chunk_length(sdd_plan* p, int set, int kc) {
+  if (!p || set < 0 || set > 1 || kc < 0 || !p->h_AB) return SDD_ERR_ARG;
+  const int S = p->M / 2;
+  if (kc == 0) kc = chunk_len(S, set == 1 ? 3 : 2);
+  const int nch = (S + kc - 1) / kc;
+  // at least two steps per chunk; the parallel carry's products grow as nch^2 / 2: at most 32 chunks
+  if (kc < 2 || kc > S || (set == 1 && nch > 32) || nch > 64) return SDD_ERR_ARG;
+  if (p->cs[set].kc == kc) return SDD_OK;
+  clear_step_graphs(p);                    // the graphs bake in the tables' pointers
+  SDD_CUDA(cudaDeviceSynchronize());      // no launch may still read the old tables
+  ChunkSet c{};
+  int st = build_chunk_set(p, kc, set == 1, p->h_AB, p->h_LinvT, p->h_LinvS, p->h_cA, p->h_cT, p->h_cS, &c);
+  if (st) {
+    free_chunk_set(c);
+    return st;
+  }
+  free_chunk_set(p->cs[set]);
+  p->cs[set] = c;
+  const int nch_alloc = std::max(p->cs[0].nch, p->cs[1].nch), np_alloc = std::max(p->cs[1].np, 1);
+  if (nch_alloc > p->nch_alloc || np_alloc > p->np_alloc) {
+    p->nch_alloc = std::max(p->nch_alloc, nch_alloc);
+    p->np_alloc = std::max(p->np_alloc, np_alloc);
+    const int b = p->ws_batch;
+    p->ws_batch = 0;                       // regrow the chunk workspace for the batch already reserved
+    if (b > 0 && (st = sdd_plan_reserve(p, b))) return st;
+  }
   return SDD_OK;
 }
 

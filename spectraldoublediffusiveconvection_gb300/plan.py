@@ -56,6 +56,7 @@ class Plan:
         self.symmetric = bool(symmetric)
         self.precision = precision
         self.chain_layout = 0          # automatic (sdd_plan_set_chain_layout)
+        self.chunk_length = [0, 0]     # steps per chunk of the two chunk sets, 0: the rule
         self.fx_split = 0              # automatic (sdd_plan_set_fx_split)
         self.tensor_cores = precision == "mixed"   # sdd_plan_set_tensor_cores
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
@@ -139,6 +140,12 @@ class Plan:
         or fused; otherwise 2 / 3) (sdd_plan_set_chain_layout); the results agree to rounding."""
         _lib.check(self._L.sdd_plan_set_chain_layout(self._h, int(layout)), "sdd_plan_set_chain_layout")
         self.chain_layout = int(layout)
+
+    def set_chunk_length(self, chunk_set, kc):
+        """Steps per chunk of chunk set 0 (layouts 2 / 10) or 1 (layouts 3 / 11); 0 restores the rule
+        (sdd_plan_set_chunk_length: the set's tables are rebuilt; synchronises the device)."""
+        _lib.check(self._L.sdd_plan_set_chunk_length(self._h, int(chunk_set), int(kc)), "sdd_plan_set_chunk_length")
+        self.chunk_length[int(chunk_set)] = int(kc)
 
     def set_fx_split(self, mode):
         """0 automatic, 1 fused row kernel, 2 split row work (sdd_plan_set_fx_split); identical results."""

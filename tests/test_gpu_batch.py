@@ -63,8 +63,10 @@ def test_autotune_records_choices(cuda):
     assert all(np.isfinite(x).all() for x in b.states())
     # a fresh batch built with the tuned choices runs the same kernels: the same states after a launch
     b2 = ShellBatch(SHELLS, precision="mixed", tuning=t)
-    assert all(b2.tuning[k] == {"chain_layout": v["chain_layout"], "fx_split": v["fx_split"]}
+    assert all(b2.tuning[k] == {"chain_layout": v["chain_layout"], "fx_split": v["fx_split"],
+                                "chunk_length": v["chunk_length"]}
                for k, v in t.items() if k.startswith("N_r"))
+    assert all(b2.groups[i].plan.chunk_length == b.groups[i].plan.chunk_length for i in range(len(b.groups)))
     b2.capture(2)
     b2.replay(1)
     for x, y in zip(b2.states(), b.states()):

@@ -320,3 +320,47 @@ def test_three_chain_layouts_symmetric(cuda, N_r, N_fm, layout):
     F = p1.pfx(Xt, 8000.0, 500.0).cpu().numpy()
     for k, x in enumerate(Xs):
         assert rel(F[k], O.PFX(ops1, x, 8000.0, 500.0, True)) < 1e-12
+
+
+@pytest.mark.parametrize("layout,cset,kc", [(2, 0, 6), (10, 0, 40), (3, 1, 4), (11, 1, 13)])
+def test_chunk_lengths_against_oracle(cuda, layout, cset, kc):
+    """sdd_plan_set_chunk_length: chunk sets rebuilt for a chunk length other than the rule (shorter: more
+    chunks, the carry workspace regrown; longer: fewer) give the oracle's steps and Newton operators, through
+    captured step graphs (dropped and recaptured with the new tables) and one by one; 0 restores the rule;
+    lengths outside 2..S or with too many chunks are refused."""
+    from spectraldoublediffusiveconvection_gb300.plan import Plan
+    from spectraldoublediffusiveconvection_gb300 import _lib
+    torch = cuda
+    N_fm, N_r = 256, 30
+    nr = N_r - 1
+    ops = O.Operators(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01)
+    X = O.seeded_state(N_fm, nr, 321)
+    Xt = torch.from_numpy(np.stack([X, 0.5 * X])).cuda()
+    p = Plan(N_fm, N_r, 2.0, 5e-4, 1.0, 0.01)
+    p.set_chain_layout(layout)
+    rule = p.chain_choice(2)
+    Y0 = p.step(Xt, 8000.0, 500.0, nsteps=10).cpu().numpy()     # graphs captured with the rule's tables
+    p.set_chunk_length(cset, kc)
+    lay, kc2, nch = p.chain_choice(2)
+    assert lay == layout and kc2 == kc and nch == (N_fm // 2 + kc - 1) // kc
+    Y = p.step(Xt, 8000.0, 500.0, nsteps=10).cpu().numpy()
+    Y1 = p.step(Xt, 8000.0, 500.0, nsteps=1).cpu().numpy()
+    for k, x in enumerate([X, 0.5 * X]):
+        r = x
+        r1 = O.step(ops, x, 8000.0, 500.0, False)
+        for _ in range(10):
+            r = O.step(ops, r, 8000.0, 500.0, False)
+        assert rel(Y[k], r) < 1e-12 and rel(Y0[k], r) < 1e-12
+        assert rel(Y1[k], r1) < 1e-12
+    p.set_chunk_length(cset, 0)
+    assert p.chain_choice(2) == rule
+    for bad in (1, N_fm, 3 if cset == 1 else 1):
+        with pytest.raises(_lib.SDDError):
+            p.set_chunk_length(cset, bad)
+    p1 = Plan(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
+    p1.set_chain_layout(layout)
+    p1.set_chunk_length(cset, kc)
+    dv = O.seeded_state(N_fm, nr, 77)
+    ops1 = O.Operators(N_fm, N_r, 2.0, 1.0, 1.0, 0.01)
+    J = p1.pdfx(torch.from_numpy(dv).cuda().reshape(1, -1), Xt[:1], 8000.0, 500.0).cpu().numpy().ravel()
+    assert rel(J, O.PDFX(ops1, dv, X, 8000.0, 500.0, False)) < 1e-12
