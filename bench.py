@@ -438,8 +438,8 @@ def bench_served(device, n_requests=1000, rate=200.0, seed=2024, frac_continue=0
     """The served mix at `rate` arrivals/s (the headline block), then an arrival-rate sweep on the same
     server: capacity = the highest swept rate whose p99 latency stays under P99_BOUND_MS over a run of
     `sweep_requests` requests (past saturation the queue, and with it p99, grows with the run), and the
-    continuation solves with an FP32 Krylov basis on top of FP32 right-hand sides (mixed_matvec 3) against
-    FP64 bases (2)."""
+    continuation solves with FP32 right-hand sides and an FP64 Krylov basis (mixed_matvec 2, the server's
+    default) against an FP32 basis (3)."""
     import torch
     from spectraldoublediffusiveconvection_gb300 import serve
     t0 = time.perf_counter()
@@ -447,7 +447,7 @@ def bench_served(device, n_requests=1000, rate=200.0, seed=2024, frac_continue=0
         branch = serve.branch_states(SERVED_SHAPES, Ra=9000.0, d=2.0, Pr=1.0, Tau=1.0, Ra_s=500.0, device=device)
     t_branch = time.perf_counter() - t0
     shapes = [s for s in SERVED_SHAPES if s in branch]
-    server_kw.setdefault("con_mixed", 3)
+    server_kw.setdefault("con_mixed", 2)
     srv = serve.Server(d=2.0, Pr=1.0, Tau=1.0, Ra_s=500.0, dt=1e-3, device=device, con_workers=con_workers,
                        **server_kw).start()
     try:

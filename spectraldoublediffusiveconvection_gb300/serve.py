@@ -132,15 +132,16 @@ class Server:
     """Request server over one GPU.  Integrations use plans with step dt and nonlinear-term precision
     ``int_precision``; continuation steps use plans with dt = 1 (Main.py:430, PFX over one unit of time),
     an FP64 residual <= tol, and inside the Jacobian products the FP32 nonlinear term when ``con_mixed`` is
-    1 (or True), FP32 right-hand sides and h = Linv g matvecs as well when it is 2, and an FP32 Krylov basis
-    too when it is 3 (the default: the lowest latency measured in the served mix).
+    1 (or True), FP32 right-hand sides and h = Linv g matvecs as well when it is 2 (the default), and an FP32
+    Krylov basis too when it is 3 (a few ms lower p50 in the served mix, but one corrector in about 20k
+    served steps ended on a non-finite state with it, none with 2).
     Integrations default to the mixed form (FP32 nonlinear term, FP64 implicit solves: 1.7x the served
     integration throughput of FP64 at these sizes; its trajectory error against FP64 is checked by the
     mixed-precision tests).  Every plan has the fixed chain layout ``chain_layout`` (default: chunked, the
     lowest latency at the served batch sizes); the tangent of each arclength step is solved to
     ``tangent_rtol`` (it only seeds the predictor: the corrector still converges to tol)."""
 
-    def __init__(self, d=2.0, Pr=1.0, Tau=1.0, Ra_s=500.0, dt=1e-3, int_precision="mixed", con_mixed=3,
+    def __init__(self, d=2.0, Pr=1.0, Tau=1.0, Ra_s=500.0, dt=1e-3, int_precision="mixed", con_mixed=2,
                  memory_budget=None, quantum=50, max_batch=16, device=None, chain_layout=2, tol=1e-10,
                  restart=50, con_workers=4, tangent_rtol=1e-4):
         torch = _torch()
