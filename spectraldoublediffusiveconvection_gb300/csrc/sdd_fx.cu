@@ -620,12 +620,15 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
   // which row quantities the pair's two fields need (fields: 0 JT_psi, 1 komega, 2 kDpsi, 3 DT, 4 DC,
   // 5 omega, 6 Dpsi, 7 kT, 8 kC)
   const bool need_psi = pr == 0 || pr == 2;            // pv (JT_psi, omega's A2 term) and D2 psi (omega)
-  // The linear parts of the fused right-hand sides: FP64 kernels split them between the two pairs that form
-  // psi's parity sums anyway (pair 0 the psi part, pair 2 the T and S parts: pair 0 carries the most work
-  // and sets the kernel's length); FP32 kernels form all three in pair 0 from FP64 copies of the row.
-  const bool lin = a.fuse_rhs && (pr == 0 || (sizeof(T) == 8 && pr == 2));
-  const bool lin_psi = lin && pr == 0;
+  // The linear parts of the fused right-hand sides.  FP64 kernels split them over three pairs: pair 2 the T
+  // and S parts, and psi's part by modes between pair 0 (k < M/2) and pair 4, whose one field leaves it the
+  // least work (it forms psi's parity sums for that alone): so no pair carries all of psi's part beside its
+  // own rows.  FP32 kernels form all three in pair 0 from FP64 copies of the row.
+  const bool lin = a.fuse_rhs && (pr == 0 || (sizeof(T) == 8 && (pr == 2 || pr == 4)));
+  const bool lin_psi = lin && (pr == 0 || pr == 4);
   const bool lin_ts = lin && (pr == 2 || sizeof(T) == 4);
+  const int kp0 = (sizeof(T) == 8 && pr == 4) ? M / 2 : 0;   // psi's part: modes [kp0, kp1) of this pair
+  const int kp1 = (sizeof(T) == 8 && pr == 0) ? M / 2 : M;
   double* pv64 = nullptr;
   if (sizeof(T) == 4 && lin)
     pv64 = reinterpret_cast<double*>(smem_raw + fx_grid_lin64_offset(M, P, SDD_PREC_MIXED));
@@ -635,7 +638,7 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
   // the psi part's FP64 D2 psi (k_fx_deriv's fifth block) for this thread's first mode, loaded with the row
   const double* D2p = reinterpret_cast<const double*>(Dv) + (size_t)4 * M * nr * sizeof(T) / 8;
   double d2s0 = 0.0;
-  if (lin_psi && tid < M && !(a.sym && (tid % 2 == 0))) d2s0 = D2p[(size_t)tid * nr + n];
+  if (lin_psi && tid >= kp0 && tid < kp1 && !(a.sym && (tid % 2 == 0))) d2s0 = D2p[(size_t)tid * nr + n];
   // the linear parts' per-row scalars, also loaded with the row (read after the parity sums)
   double lRa = 0.0, lRas = 0.0, lir2 = 0.0, lrsq = 0.0, ldT0 = 0.0, lgr = 0.0;
   if (lin) {
@@ -681,7 +684,7 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
   });
   cp_async_all_done();
   __syncthreads();
-  if (need_psi) {
+  if (need_psi || lin_psi) {
     parity_suffix<T>(pv, Sc, M);                       // (ends with a barrier)
     if (pv64) parity_suffix<double>(pv64, pv64 + M, M);
     // one loop: the linear parts of the right-hand sides at row n (k_rhs's expressions, Main.py:262-280, in
@@ -696,13 +699,11 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
     const double ir2 = lir2, rsq = lrsq, dT0 = ldT0, gr = lgr;
     double* R = lin ? r.rhs + (size_t)b * r.rhs_stride : nullptr;
     for (int k = tid; k < M; k += bd) {
-      jp_om<T>(k, M, kf, pv, Sc, ir4n, JP[k], OM[k]);
+      if (need_psi) jp_om<T>(k, M, kf, pv, Sc, ir4n, JP[k], OM[k]);
       if (lin) {
-        const double pk = pvd[k], pkm = k > 0 ? pvd[k - 1] : 0.0;
-        const double s1 = (k + 1 < M) ? Scd[k + 1] : 0.0;
-        const double JPk = (k == 0) ? 1.0 * s1 : (k + 1.0) * pkm + 2.0 * s1;
+        const double pk = pvd[k];
         const size_t o = (size_t)k * nr + n;
-        if (lin_psi) {
+        if (lin_psi && k >= kp0 && k < kp1) {
           const double s2 = (k + 2 < M) ? Scd[k + 2] : 0.0;
           const bool psi_on = !(a.sym && (k % 2 == 0));
           const double d2s = k == tid ? d2s0 : (psi_on ? D2p[(size_t)k * nr + n] : 0.0);
@@ -711,6 +712,9 @@ __global__ void __launch_bounds__(kFxSplitThreads) k_fx_grid(FxArgs a, T* grid, 
           R[o] = Om + dtPr * grv;
         }
         if (lin_ts) {
+          const double pkm = k > 0 ? pvd[k - 1] : 0.0;
+          const double s1 = (k + 1 < M) ? Scd[k + 1] : 0.0;
+          const double JPk = (k == 0) ? 1.0 * s1 : (k + 1.0) * pkm + 2.0 * s1;
           const double psiT0 = dT0 * JPk;
           R[N + o] = rsq * Tvd[k] - dt * psiT0;
           R[2 * N + o] = rsq * Svd[k] - dt * psiT0;
