@@ -1259,37 +1259,44 @@ static cudaError_t launch_chunked(const ChainArgs& a_in, int batch, int nfields,
     if (a.defer_fix) return cudaSuccess;   // the next step's nonlinear term applies the correction
     return launch_mode_mv<true>(a, batch, nfields, s, pw);
   }
-  // the carry ring of the psi chain (m = 2 nr) decides the ring depth for all fields of the launch
+  // The carry ring of the psi chain (m = 2 nr) sets the shared memory of every chunk CTA of the launch,
+  // though only the last-finishing CTA of each chain runs the carry: the ring is made as deep (4, 2 or 0
+  // slots: the carry then reads Phi through L2) as still lets all the launch's chunk CTAs be resident at
+  // once, so that a large batch's chunks do not run in waves for the carry's sake.  The carry's arithmetic
+  // is the same at every depth.
   const int mmax = a.field0 == 0 ? 2 * a.nr : a.nr;
   const int ldmax = a.field0 == 0 ? a.ldmA : a.ldmT;
   const size_t blkb = (size_t)mmax * ldmax * sizeof(double);
   const size_t st = 2 * (size_t)a.ldd * sizeof(double);
-  const int depth = (4 * blkb + st <= 200 * 1024) ? 4 : (2 * blkb + st <= 200 * 1024) ? 2 : 0;
-  const size_t smem = std::max(ref ? chunk_ref_smem_bytes(a.kc, a.nr, a.ldl, a.fuse_rhs)
-                                   : chunk_smem_bytes(a.kc, a.nr, a.ldl), depth * blkb + st);
+  const size_t base = ref ? chunk_ref_smem_bytes(a.kc, a.nr, a.ldl, a.fuse_rhs) : chunk_smem_bytes(a.kc, a.nr, a.ldl);
   const dim3 grid(2 * nfields, batch, a.nch);
-#define SDD_CHUNK(TPR_, R_)                                                                      \
-  do {                                                                                           \
-    if (ref) {                                                                                   \
-      static unsigned long long done = 0;                                                        \
-      if ((e = ensure_smem_attr(k_chain_cref<TPR_, R_>, &done)) != cudaSuccess) return e;        \
-      if ((e = launch_kernel(k_chain_cref<TPR_, R_>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e; \
-    } else {                                                                                     \
-      static unsigned long long done = 0;                                                        \
-      if ((e = ensure_smem_attr(k_chain<TPR_, true, R_>, &done)) != cudaSuccess) return e;       \
-      if ((e = launch_kernel(k_chain<TPR_, true, R_>, grid, dim3(128), smem, s, a)) != cudaSuccess) return e; \
-    }                                                                                            \
-  } while (0)
-  if (a.nr <= 32) {
-    if (depth == 4) SDD_CHUNK(4, 4);
-    else if (depth == 2) SDD_CHUNK(4, 2);
-    else SDD_CHUNK(4, 0);
-  } else {
-    if (depth == 4) SDD_CHUNK(2, 4);
-    else if (depth == 2) SDD_CHUNK(2, 2);
-    else SDD_CHUNK(2, 0);
+  const long ctas = (long)grid.x * grid.y * grid.z;
+  const int t = a.nr <= 32 ? 0 : 1;                    // rows over 4 lanes (nr <= 32) or 2
+  using Kern = void (*)(ChainArgs);
+  static const Kern kern[2][2][3] = {
+      {{k_chain<4, true, 0>, k_chain<4, true, 2>, k_chain<4, true, 4>},
+       {k_chain<2, true, 0>, k_chain<2, true, 2>, k_chain<2, true, 4>}},
+      {{k_chain_cref<4, 0>, k_chain_cref<4, 2>, k_chain_cref<4, 4>},
+       {k_chain_cref<2, 0>, k_chain_cref<2, 2>, k_chain_cref<2, 4>}}};
+  static unsigned long long done[2][2][3] = {};
+  const int r = ref ? 1 : 0;
+  int di = 0;
+  size_t smem = std::max(base, st);
+  for (int d = 2; d >= 1; --d) {                        // depth 4, then 2
+    const int depth = 2 * d;
+    const size_t sm = std::max(base, depth * blkb + st);
+    if (sm > 200 * 1024) continue;
+    if ((e = ensure_smem_attr(kern[r][t][d], &done[r][t][d])) != cudaSuccess) return e;
+    int per_sm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern[r][t][d], 128, sm)) != cudaSuccess) return e;
+    if ((long)per_sm * sm_count() >= ctas) {
+      di = d;
+      smem = sm;
+      break;
+    }
   }
-#undef SDD_CHUNK
+  if ((e = ensure_smem_attr(kern[r][t][di], &done[r][t][di])) != cudaSuccess) return e;
+  if ((e = launch_kernel(kern[r][t][di], grid, dim3(128), smem, s, a)) != cudaSuccess) return e;
   ktimer_mark(SDD_K_CHAIN, s);
   if (a.nch < 2) return cudaSuccess;
   return launch_mode_mv<true>(a, batch, nfields, s, pw);
